@@ -1,0 +1,176 @@
+"""Reader for a CATHY project directory (the files pyCATHY writes).
+
+Restates the input semantics of the reference's ``datin.f`` for the
+subsurface solver (parm :81-117, DEM/zone rasters via RAST_INPUT_DEM /
+RAST_INPUT_LZ :189-257, dem_parameters :195-266, ic :380-405, soil
+:421-517) plus the atmospheric (``atmone.f``) and non-atmospheric BC files
+(``bcone.f``; the first time block is used, held constant).  The result is a
+:class:`~pycathy_wrapper_gb300.inputs.Case`, so a pyCATHY project can be run
+on the GPU without changing how the project is written.
+"""
+from __future__ import annotations
+
+import os
+import re
+
+import numpy as np
+
+from .inputs import BC, Case, Dem, Parm, Soil
+
+_num = re.compile(r"^[+-]?(\d+\.?\d*|\.\d+)([eEdD][+-]?\d+)?$")
+
+
+def _nums(line):
+    out = []
+    for tok in line.replace(",", " ").split():
+        if _num.match(tok):
+            out.append(float(tok.replace("d", "e").replace("D", "e")))
+        else:
+            break
+    return out
+
+
+def _lines(path):
+    with open(path) as f:
+        return [ln for ln in f.read().splitlines()]
+
+
+def read_raster(path):
+    """GRASS-ASCII raster with a 6-line header (north/south/east/west/rows/cols)."""
+    ls = _lines(path)
+    hdr = {}
+    for ln in ls[:6]:
+        k, v = ln.split(":")
+        hdr[k.strip()] = float(v)
+    nrow, ncol = int(hdr["rows"]), int(hdr["cols"])
+    vals = np.array(" ".join(ls[6:]).replace("D", "E").split(), dtype=float)
+    return vals[: nrow * ncol].reshape(nrow, ncol), hdr
+
+
+def read_parm(path) -> Parm:
+    ls = [ln for ln in _lines(path) if ln.strip()]
+    v = [_nums(ln) for ln in ls]
+    p = Parm()
+    p.isimgr = int(v[1][0])
+    p.pondh_min = v[1][1]
+    p.kslope = int(v[2][0])
+    p.tetaf, p.lump, p.iopt = v[6][0], int(v[6][1]), int(v[6][2])
+    p.nlrelx, p.omega = int(v[7][0]), v[7][1]
+    p.l2norm, p.toluns, p.tolswi, p.ernlmx = int(v[8][0]), v[8][1], v[8][2], v[8][3]
+    p.ituns, p.ituns1, p.ituns2 = int(v[9][0]), int(v[9][1]), int(v[9][2])
+    p.isolv, p.itmxcg, p.tolcg = int(v[10][0]), int(v[10][1]), v[10][2]
+    p.deltat, p.dtmin, p.dtmax, p.tmax = v[11][:4]
+    p.dtmaga, p.dtmagm, p.dtreds, p.dtredm = v[12][:4]
+    p.tolksl = v[2][1]
+    return p
+
+
+def read_project(prj: str) -> Case:
+    """Read ``prj/input/*`` and ``prj/prepro/*`` into a Case."""
+    inp = lambda f: os.path.join(prj, "input", f)
+    pre = lambda f: os.path.join(prj, "prepro", f)
+    parm = read_parm(inp("parm"))
+    # dem_parameters: delta_x, delta_y, factor, dostep, nzone nstr n1,
+    # ivert isp base, zratio
+    dp = [_nums(ln) for ln in _lines(inp("dem_parameters")) if _nums(ln)]
+    delta_x, delta_y, factor = dp[0][0], dp[1][0], dp[2][0]
+    nzone, nstr = int(dp[4][0]), int(dp[4][1])
+    ivert, base = int(dp[5][0]), dp[5][2]
+    zr = np.array(dp[6][:nstr])
+    dem_map, hdr = read_raster(pre("dem"))
+    zone_map = None
+    if os.path.exists(pre("zone")):
+        z, _ = read_raster(pre("zone"))
+        zone_map = np.rint(z).astype(np.int32)
+    dem = Dem(dem=dem_map, delta_x=delta_x, delta_y=delta_y, zratio=zr,
+              base=base, ivert=ivert, zone=zone_map, factor=factor,
+              west=hdr.get("west", 0.0), south=hdr.get("south", 0.0))
+    # vegetation types: number of Feddes lines in the soil file
+    nveg = 1
+    if os.path.exists(inp("root_map")):
+        rm, _ = read_raster(inp("root_map"))
+        nveg = max(1, int(np.max(rm)))
+    sl = [ln for ln in _lines(inp("soil")) if _nums(ln)]
+    pmin = _nums(sl[0])[0]
+    scf = _nums(sl[1])[1]
+    ivghu = int(_nums(sl[3 + nveg])[0])
+    if ivghu != 0:
+        raise ValueError("only IVGHU=0 (van Genuchten) soils are supported")
+    rows = np.array([_nums(ln)[:8] for ln in sl[8 + nveg: 8 + nveg + nstr * nzone]])
+    rows = rows.reshape(nstr, nzone, 8).transpose(1, 0, 2)  # (zone, layer, 8)
+    soil = Soil(permx=rows[..., 0].copy(), permy=rows[..., 1].copy(),
+                permz=rows[..., 2].copy(), elstor=rows[..., 3].copy(),
+                poros=rows[..., 4].copy(), vgn=rows[..., 5].copy(),
+                vgrmc=rows[..., 6].copy(), vgpsat=rows[..., 7].copy(),
+                pmin=pmin, scf=scf, kslope=parm.kslope, tolksl=parm.tolksl)
+    # initial conditions
+    il = [ln for ln in _lines(inp("ic")) if ln.strip()]
+    indp = int(_nums(il[0])[0])
+    bc = BC(indp=indp)
+    if indp in (3, 4):
+        bc.wtposition = _nums(il[1])[0]
+    elif indp == 0:
+        bc.pinit = np.array([_nums(il[1])[0]])
+    elif indp == 1:
+        bc.pinit = np.array(" ".join(il[1:]).split(), dtype=float)
+    # atmospheric forcing
+    al = [ln for ln in _lines(inp("atmbc")) if ln.strip()]
+    h = _nums(al[0])
+    bc.hspatm, bc.ieto = int(h[0]), int(h[1])
+    toks = []
+    for ln in al[1:]:
+        toks.extend(_nums(ln))
+    times, vals = [], []
+    i = 0
+    per = 1 if bc.hspatm != 0 else None
+    while i < len(toks):
+        times.append(toks[i])
+        i += 1
+        if per is None:
+            # spatially variable: the rest of the block until the next time is
+            # NNOD values; NNOD is the number of active DEM cell corners
+            nnod = _count_nodes(dem_map)
+            per = nnod
+        vals.append(toks[i:i + per])
+        i += per
+    bc.atmtim = np.array(times)
+    bc.atminp = np.array(vals) if per != 1 else np.array([v[0] for v in vals])
+    parm_dir = _read_bc_list(inp("nansfdirbc"))
+    if parm_dir is not None:
+        bc.contp, bc.presc = parm_dir
+    neu = _read_bc_list(inp("nansfneubc"))
+    if neu is not None:
+        bc.contq, bc.q = neu
+    return Case(dem, soil, parm, bc, name=os.path.basename(os.path.normpath(prj)))
+
+
+def _count_nodes(dem_map):
+    nrow, ncol = dem_map.shape
+    act = np.zeros((nrow + 1, ncol + 1), bool)
+    on = dem_map != 0
+    act[:-1, :-1] |= on
+    act[1:, :-1] |= on
+    act[1:, 1:] |= on
+    act[:-1, 1:] |= on
+    return int(act.sum())
+
+
+def _read_bc_list(path):
+    """First time block of a nansfdirbc / nansfneubc file:
+    ``time`` / ``NDIR NDIRC`` (or ``ZERO NQ``) / node ids / values."""
+    if not os.path.exists(path):
+        return None
+    toks = []
+    for ln in _lines(path):
+        toks.extend(_nums(ln))
+    if len(toks) < 3:
+        return None
+    n1, n2 = int(toks[1]), int(toks[2])
+    cnt = n1 + n2
+    if cnt == 0:
+        return None
+    ids = np.array(toks[3:3 + cnt], dtype=np.int32)
+    vals = np.array(toks[3 + cnt:3 + 2 * cnt], dtype=float)
+    if len(vals) < cnt:
+        vals = np.zeros(cnt)
+    return ids, vals

@@ -1,0 +1,90 @@
+"""Generate the golden fixtures from the reference's stored CATHY runs.
+
+Run in a container where the reference checkout is mounted:
+
+    python tests/golden/make_golden.py /root/reference
+
+For each example project it stores (a) the project inputs as parsed by
+``pycathy_wrapper_gb300.project.read_project`` and (b) the values the
+reference CATHY binary printed for that project: the GEN3D mesh
+(``output/grid3d``), NTERM (``output/risul``), and the first nonlinear
+iteration record of the first time step (``output/iter`` and the linear
+solver line of ``output/risul``).  The first iteration is a clean known
+answer for initial conditions + assembly + boundary conditions + IC(0)-PCG:
+surface routing only starts once ponding occurs (cathy_main.f:2993).
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+from pycathy_wrapper_gb300.project import read_project  # noqa: E402
+
+EXAMPLES = {
+    "weill": "examples/SSHydro/weill_exemple",
+    "soil3d": "examples/SSHydro/soil3d_from_weill",
+}
+
+
+def first_iter(prj):
+    rec = None
+    for ln in open(os.path.join(prj, "output", "iter")):
+        t = ln.split()
+        if len(t) == 9 and t[0] == "1":
+            rec = dict(iter=int(t[0]), niter=int(t[1]), pl2=float(t[2]),
+                       pinf=float(t[3]), ikmax=int(t[4]), pnew_ik=float(t[5]),
+                       pold_ik=float(t[6]), fl2=float(t[7]), finf=float(t[8]))
+            break
+    nterm = None
+    lin = None
+    for ln in open(os.path.join(prj, "output", "risul")):
+        if "NTERM" in ln and nterm is None:
+            nterm = int(ln.split("=")[1])
+        if "<<SYMMETRIC SOLVER>>" in ln and lin is None:
+            t = ln.split()
+            lin = dict(niter=int(t[0]), err=float(t[1]), res=float(t[2]))
+    return rec, nterm, lin
+
+
+def case_to_npz(case, path):
+    d, s, p, b = case.dem, case.soil, case.parm, case.bc
+    arrs = dict(dem=d.dem, zratio=d.zratio,
+                zone=d.zone if d.zone is not None else np.ones_like(d.dem, np.int32))
+    for k in ("permx", "permy", "permz", "elstor", "poros", "vgn", "vgrmc", "vgpsat"):
+        arrs["soil_" + k] = getattr(s, k)
+    arrs["atmtim"] = b.atmtim
+    arrs["atminp"] = b.atminp
+    meta = dict(delta_x=d.delta_x, delta_y=d.delta_y, base=d.base, ivert=d.ivert,
+                west=d.west, south=d.south, factor=d.factor,
+                pmin=s.pmin, scf=s.scf, kslope=s.kslope, tolksl=s.tolksl,
+                parm={k: getattr(p, k) for k in p.__dataclass_fields__},
+                hspatm=b.hspatm, ieto=b.ieto, indp=b.indp, wtposition=b.wtposition)
+    np.savez_compressed(path, meta=json.dumps(meta), **arrs)
+
+
+def main(ref):
+    out = {}
+    for key, rel in EXAMPLES.items():
+        prj = os.path.join(ref, rel)
+        case = read_project(prj)
+        case_to_npz(case, os.path.join(HERE, f"{key}_case.npz"))
+        rec, nterm, lin = first_iter(prj)
+        out[key] = dict(source=rel, first_iter=rec, nterm=nterm, linear=lin)
+        if key == "weill":
+            g = open(os.path.join(prj, "output", "grid3d")).read().split("\n")
+            nnod, n, nt = (int(v) for v in g[0].split())
+            tet = np.array(" ".join(g[1:1 + nt]).split(), np.int32).reshape(nt, 5)
+            xyz = np.array(" ".join(g[1 + nt:1 + nt + n]).split(), float).reshape(n, 3)
+            np.savez_compressed(os.path.join(HERE, "weill_grid3d.npz"), tetra=tet,
+                                xyz=xyz, nnod=nnod)
+            out[key]["grid3d"] = dict(nnod=nnod, n=n, nt=nt)
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print(json.dumps(out, indent=1))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

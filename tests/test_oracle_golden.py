@@ -1,0 +1,61 @@
+"""Pin the CPU oracle on the reference's stored CATHY outputs.
+
+Known answers (tests/golden, generated by tests/golden/make_golden.py from
+examples/SSHydro/{weill_exemple,soil3d_from_weill}/output):
+GEN3D mesh (grid3d), NTERM (risul) and the first nonlinear iteration of the
+first time step (iter + the SYMMETRIC SOLVER line of risul).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_json, load_golden_case
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+@pytest.mark.parametrize("key", ["weill", "soil3d"])
+def test_first_iteration_matches_reference(key):
+    import oracle as O
+    g = golden_json()[key]
+    o = O.Oracle(load_golden_case(key))
+    assert o.nterm == g["nterm"]
+    r = o.first_iteration()
+    fi, lin = g["first_iter"], g["linear"]
+    assert r["niter"] == fi["niter"] == lin["niter"]
+    assert r["ikmax"] == fi["ikmax"]
+    # iter prints 4 significant digits (E10.3), risul 7 (E15.6)
+    for k in ("pl2", "pinf", "fl2", "finf"):
+        assert _rel(r[k], fi[k]) < 6e-4, (k, r[k], fi[k])
+    assert _rel(r["lin_err"], lin["err"]) < 2e-6
+    assert _rel(r["lin_res"], lin["res"]) < 2e-6
+    # PNEW/POLD at IKMAX are printed with 3 significant digits (E10.2)
+    assert _rel(r["pnew_ik"], fi["pnew_ik"]) < 5.1e-3
+    assert _rel(r["pold_ik"], fi["pold_ik"]) < 5.1e-3
+
+
+def test_gen3d_mesh_matches_grid3d():
+    import oracle as O
+    z = np.load(os.path.join(GOLDEN, "weill_grid3d.npz"))
+    o = O.Oracle(load_golden_case("weill"))
+    assert o.nnod == int(z["nnod"]) and o.n == z["xyz"].shape[0] and o.nt == z["tetra"].shape[0]
+    np.testing.assert_array_equal(o.tetra_gen3d(), z["tetra"])
+    m = o.mesh()
+    xyz = np.stack([m["x"], m["y"], m["z"]], 1)
+    # grid3d prints 7 significant digits (1PE15.6)
+    np.testing.assert_allclose(xyz, z["xyz"], rtol=1e-6, atol=1e-6)
+
+
+def test_strpic_pattern_properties():
+    """Symmetric upper CSR: diagonal first, strictly increasing columns."""
+    import oracle as O
+    o = O.Oracle(load_golden_case("weill"))
+    m = o.mesh()
+    topol, ja = m["topol"], m["ja"]
+    for k in range(o.n):
+        row = ja[topol[k] - 1:topol[k + 1] - 1]
+        assert row[0] == k + 1
+        assert np.all(np.diff(row) > 0)
