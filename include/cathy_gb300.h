@@ -1,0 +1,213 @@
+/*
+ * cathy_gb300.h -- C ABI of the GB300-native CATHY subsurface solver.
+ *
+ * The library replaces the CPU routines of CATHY's FLOW3D hot path with
+ * hand-written CUDA for sm_103a.  Two kinds of entry points are exported:
+ *
+ *  (1) Drop-ins for the reference's own Fortran subroutine boundaries, with
+ *      the same arguments (host arrays, Fortran 1-based index contents,
+ *      scalars by pointer so that an ISO_C_BINDING interface can pass them
+ *      by reference):
+ *        cathy_gb300_symslv   <- SYMSLV  (solscal-extended.f:4669)
+ *        cathy_gb300_nsyslv   <- NSYSLV  (solscal-extended.f:3063), ISOLV 0/-5
+ *        cathy_gb300_asspic   <- ASSPIC  (asspic.f:9)
+ *
+ *  (2) A handle API that owns the device state of one simulation or of a
+ *      whole ensemble and advances it time step by time step.  One call of
+ *      cathy_gb300_step replaces the body of the reference's time loop around
+ *      its FLOW3D call (cathy_main.f:2882-3843: BC update, FLOW3D
+ *      flow3d.f:8, back-stepping bkstep.f, mass balance masbal.f, TIMUPD
+ *      timupd.f) for every member of the handle at once.
+ *
+ * All functions return 0 on success or a negative CATHY_GB300_E* code.  The
+ * library never falls back to a CPU path: without a usable CUDA device every
+ * compute entry point returns CATHY_GB300_ENODEV.
+ */
+#ifndef CATHY_GB300_H
+#define CATHY_GB300_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CATHY_GB300_OK 0
+#define CATHY_GB300_ENODEV (-1)    /* no CUDA device / CUDA error          */
+#define CATHY_GB300_EINVAL (-2)    /* invalid argument                     */
+#define CATHY_GB300_EMESH (-3)     /* mesh construction failed             */
+#define CATHY_GB300_ENOMEM (-4)    /* device allocation failed             */
+#define CATHY_GB300_EUNSUP (-5)    /* option not supported                 */
+
+/* ---- inputs (contents of a CATHY project's input files) --------------- */
+
+/* prepro/dem + input/dem_parameters (read by datin.f:189-266) */
+typedef struct cathy_dem {
+  int32_t nrow, ncol;          /* DEM cells, row 1 = north                 */
+  double delta_x, delta_y;     /* cell sizes                               */
+  double west, south, factor;  /* origin, elevation multiplier             */
+  const double* dem;           /* nrow*ncol row-major; 0 = inactive cell   */
+  const int32_t* zone;         /* nrow*ncol zone ids (1-based) or NULL     */
+  int32_t nstr;                /* layers                                   */
+  const double* zratio;        /* nstr thickness fractions                 */
+  double base;                 /* depth scale                              */
+  int32_t ivert;               /* GEN3D vertical mode 0,1,2,4              */
+} cathy_dem_t;
+
+/* input/soil for IVGHU=0; tables indexed (zone-1)*nstr + (layer-1) */
+typedef struct cathy_soil {
+  int32_t nzone;
+  const double *permx, *permy, *permz, *elstor, *poros, *vgn, *vgrmc, *vgpsat;
+  double pmin, scf;
+  int32_t kslope;              /* 0 only                                   */
+  double tolksl;
+} cathy_soil_t;
+
+/* input/parm keys (datin.f:81-117) */
+typedef struct cathy_parm {
+  int32_t iopt, lump, isolv, itmxcg, ituns, ituns1, ituns2, l2norm, nlrelx;
+  int32_t isimgr;
+  double tetaf, toluns, tolswi, ernlmx, tolcg, omega;
+  double deltat, dtmin, dtmax, tmax, dtmaga, dtmagm, dtreds, dtredm;
+  double pondh_min;
+  int32_t precond;             /* Picard: 0 IC(0), 1 Jacobi, 2 column line */
+} cathy_parm_t;
+
+/* input/atmbc, nansfdirbc, nansfneubc, ic */
+typedef struct cathy_bc {
+  int32_t hspatm, ieto, natm;
+  const double* atmtim;        /* natm times                               */
+  const double* atminp;        /* natm * (hspatm ? 1 : nnod) rates         */
+  int32_t np; const int32_t* contp; const double* presc;
+  int32_t nq; const int32_t* contq; const double* q;
+  int32_t indp; double wtposition; const double* pinit;
+} cathy_bc_t;
+
+typedef struct cathy_member {
+  cathy_dem_t dem;
+  cathy_soil_t soil;
+  cathy_parm_t parm;
+  cathy_bc_t bc;
+} cathy_member_t;
+
+/* solver options of a handle */
+typedef struct cathy_opts {
+  int32_t precision;           /* 0: FP64 everywhere; 1: FP32 matrix and
+                                  Krylov inside FP64 residual/refinement   */
+  int32_t device;              /* CUDA device ordinal                      */
+  int32_t inner_maxit;         /* FP32 inner iterations per refinement     */
+  double inner_tol;            /* FP32 inner relative tolerance            */
+  int32_t verbose;
+} cathy_opts_t;
+
+/* per nonlinear iteration record (the reference's `iter` file) */
+typedef struct cathy_iter_rec {
+  int32_t nstep, iter, niter, ikmax;
+  double deltat, time, pl2, pinf, pnew_ik, pold_ik, fl2, finf, lin_err, lin_res;
+} cathy_iter_rec_t;
+
+/* per accepted time step record (the reference's `mbeconv` file) */
+typedef struct cathy_step_rec {
+  int32_t nstep, iter, nitert, nback;
+  double deltat, time, store1, store2, dstore, cdstor, vin, cvin, vout, cvout,
+         erras, errel, cerras, caeras;
+} cathy_step_rec_t;
+
+/* ---- library ----------------------------------------------------------- */
+int32_t cathy_gb300_version(void);
+/* number of usable CUDA devices (0 when none) */
+int32_t cathy_gb300_device_count(void);
+
+/* ---- host-only mesh construction (no device needed) --------------------- */
+/* Builds the mesh of a DEM exactly as the handle does (TRIANGOLI, GEN3D,
+ * RIORD for IOPT=1, full CSR pattern).  Call once with NULL arrays to get
+ * sizes (n, nt, nnod, ntri, nnz) in out5, then again with arrays of those
+ * sizes: x,y,z (n), tetra (5*nt, 1-based), rowptr (n+1), cols (nnz), both
+ * 0-based. */
+int32_t cathy_gb300_mesh(const cathy_dem_t* dem, int32_t iopt, int32_t* out5,
+                         double* x, double* y, double* z, int32_t* tetra,
+                         int32_t* rowptr, int32_t* cols);
+
+/* ---- handle API --------------------------------------------------------- */
+int32_t cathy_gb300_create(int32_t nmembers, const cathy_member_t* members,
+                           const cathy_opts_t* opts, void** handle);
+int32_t cathy_gb300_destroy(void* handle);
+/* sizes of member m: n, nt, nnod, ntri, nnz (full CSR) */
+int32_t cathy_gb300_sizes(void* handle, int32_t m, int32_t* out5);
+/* advance every unfinished member by one accepted time step (with its
+ * back-steps).  *nactive receives the number of members still running. */
+int32_t cathy_gb300_step(void* handle, int32_t* nactive);
+/* run every member to TMAX (or max_steps accepted steps) */
+int32_t cathy_gb300_run(void* handle, int32_t max_steps, int32_t* nsteps);
+/* state of member m: pressure heads (n), time, deltat, status
+ * (0 running, 1 finished, 2 failed) */
+int32_t cathy_gb300_get_state(void* handle, int32_t m, double* pnew,
+                              double* time, double* deltat, int32_t* status);
+int32_t cathy_gb300_set_state(void* handle, int32_t m, const double* ptimep,
+                              double time, double deltat);
+int32_t cathy_gb300_num_records(void* handle, int32_t m, int32_t* niter_recs,
+                                int32_t* nstep_recs);
+int32_t cathy_gb300_get_records(void* handle, int32_t m,
+                                cathy_iter_rec_t* iter_recs,
+                                cathy_step_rec_t* step_recs);
+/* mesh of member m as built on the device: x,y,z (n), tetra (5*nt, 1-based,
+ * node order as used for IOPT), rowptr (n+1, 0-based full CSR), cols (nnz,
+ * 0-based) */
+int32_t cathy_gb300_get_mesh(void* handle, int32_t m, double* x, double* y,
+                             double* z, int32_t* tetra, int32_t* rowptr,
+                             int32_t* cols);
+/* Picard system of member m at its current state (LHS full CSR values before
+ * Dirichlet masking, RHS after BCs, RHS before BCs, Dirichlet mask) */
+int32_t cathy_gb300_picard_system(void* handle, int32_t m, double* vals,
+                                  double* rhs, double* xt5, int32_t* dirmask);
+/* GPU time spent in the hot path (ms) since creation, and kernel launches */
+int32_t cathy_gb300_stats(void* handle, double* gpu_ms, int64_t* launches,
+                          int64_t* lin_iters, int64_t* nl_iters);
+
+/* ---- Fortran subroutine drop-ins ---------------------------------------- */
+/* SYMSLV(IOUT,N,NTERM,NUMDIR,NITER,ITMXCG,TOLCG,RMIN,NODDIR,JA,TOPOL,PNEW,
+ *        TNOTI,COEF1,COEF2,SCR): IC(0)-preconditioned CG on the symmetric
+ * upper-triangular CSR system (diagonal first in each row, 1-based TOPOL/JA,
+ * Dirichlet rows carrying the 1e-9*RMAX penalty).  PNEW receives the
+ * solution; COEF2 and SCR are scratch as in the reference (COEF2 receives
+ * the IC(0) factor).  ERR/RES (extra, may be NULL) receive the final
+ * preconditioned-recursion and true residual norms. */
+int32_t cathy_gb300_symslv(const int32_t* iout, const int32_t* n,
+                           const int32_t* nterm, const int32_t* numdir,
+                           int32_t* niter, const int32_t* itmxcg,
+                           const double* tolcg, const double* rmin,
+                           const int32_t* noddir, const int32_t* ja,
+                           const int32_t* topol, double* pnew,
+                           const double* tnoti, const double* coef1,
+                           double* coef2, double* scr, double* err,
+                           double* res);
+/* NSYSLV restricted to ISOLV=0 (ILU(0)-BiCGSTAB, split preconditioning) and
+ * ISOLV=-5 (Jacobi-BiCGSTAB) on the full nonsymmetric CSR (IA/JA/TOPOL). */
+int32_t cathy_gb300_nsyslv(const int32_t* isolv, const int32_t* iout,
+                           const int32_t* n, const int32_t* nterm,
+                           const int32_t* numdir, const int32_t* noddir,
+                           const int32_t* itmxcg, int32_t* niter,
+                           const int32_t* ia, const int32_t* ja,
+                           const int32_t* topol, const double* tolcg,
+                           const double* rmin, const double* coef1,
+                           double* coef2, double* pnew, const double* tnoti,
+                           double* err, double* res);
+/* ASSPIC(NT,NTRI,TETRA,TETJA,LMASS,COEF1,COEF2,COEF4,ET1E,PEL,PERMX,PERMY,
+ *        PERMZ,CKRWE,ETAE,VOLU,VOLUR,BI,CI,DI): element assembly of the
+ * Picard stiffness (COEF1) and mass (COEF2, COEF4) arrays, accumulated into
+ * the caller's arrays as the reference does.  MAXSTR is the leading
+ * dimension of PERMX/PERMY/PERMZ (CATHY.H), NTERM the length of COEF*. */
+int32_t cathy_gb300_asspic(const int32_t* nt, const int32_t* ntri,
+                           const int32_t* tetra, const int32_t* tetja,
+                           const double* lmass, double* coef1, double* coef2,
+                           double* coef4, const double* et1e,
+                           const double* pel, const double* permx,
+                           const double* permy, const double* permz,
+                           const double* ckrwe, const double* etae,
+                           const double* volu, const double* volur,
+                           const double* bi, const double* ci,
+                           const double* di, const int32_t* maxstr,
+                           const int32_t* nterm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,2874 @@
+// GB300-native CATHY FLOW3D engine: device kernels + batched orchestration.
+//
+// Reference correspondence (paths relative to the vendored CATHY src/):
+//   k_tpnodi            TPNODI (tpnodi.f:9-99) + CHPARM (chparm.f:24-45)
+//   k_geom              VOLBAS/VOLUMS/BASIS6 (volbas.f, volums.f, basis6.f)
+//   k_vg                CHPIC0 (chpic0.f:23-36) with FVGSE/FVGDSE/FVGKR,
+//                       CHNEW0 (chnew0.f) with FVGDKR/FVGDDS for Newton
+//   k_assemble_picard   ASSPIC+RHSPIC+CFMATP+RHSGRV+BCPIC (asspic.f,
+//                       rhspic.f, cfmatp.f, rhsgrv.f, bcpic.f), row-owned
+//   k_assemble_newton   ASSNEW+RHSNEW+CFMATN+RHSGRV+BCNEW (assnew.f, ...)
+//   PCG                 SYMSLV/GRADDP (solscal-extended.f:4669, :1260) with
+//                       the same recurrences and stopping rule; IC(0) as
+//                       INCLDP/PRODDP (:2142, :4169), level-scheduled
+//   BiCGSTAB            NSYSLV/GCSTAS/GCSTAD (:3063, :1010, :786), ILU(0)
+//                       as INCLU/PRODL/PRODU/PRU (:2194, :4205, :4228, :4251)
+//   k_update_shl        PNEW update + SHLPIC/SHLNEW (shlpic.f, shlnew.f)
+//   k_masbal_norms      MASBAL/BKPIC/BKNEW/STORMB/FLUXMB + RELAX + NORMS
+//   k_switch            SWITCH_OLD (switch_old.f:12-53)
+//   k_start_*           ATMNXT/ATMBAK interpolation, WEIGHT, BKSTEP restore
+// Time-step control (TIMUPD timupd.f:18-38, BKSTEP bkstep.f:54-80) and the
+// nonlinear convergence decision (flow3d.f:212-294) run per member on the
+// host from a few scalars copied back each nonlinear iteration.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "kernels.cuh"
+
+namespace cathy {
+
+// ============================================================================
+// device helpers
+// ============================================================================
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double group_sum16(double v) {
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float group_sum16f(float v) {
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-level sum of NV values, one atomicAdd per value into acc[0..NV).
+template <int NV>
+__device__ __forceinline__ void block_accumulate(double (&v)[NV], double* acc) {
+  __shared__ double sh[NV][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double s = warp_sum(v[i]);
+    if (lane == 0) sh[i][w] = s;
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double s = (lane < (int)(blockDim.x >> 5)) ? sh[i][lane] : 0.0;
+      s = warp_sum(s);
+      if (lane == 0 && s != 0.0) atomicAdd(acc + i, s);
+    }
+  }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double* a, double v) {
+  atomicMax((unsigned long long*)a, (unsigned long long)__double_as_longlong(v));
+}
+
+template <class T> __device__ __forceinline__ T dpow(T a, T b);
+template <> __device__ __forceinline__ double dpow<double>(double a, double b) { return pow(a, b); }
+template <> __device__ __forceinline__ float dpow<float>(float a, float b) { return powf(a, b); }
+
+// ---- van Genuchten (fvgse.f, fvgdse.f, fvgkr.f, fvgdkr.f, fvgdds.f) ----
+struct VGPar {
+  double vgn, vgm, vgpsat, vgn1, vgnr, vgpsn, vgmr, vgm52, vgmm1, vgpnot, vgrmc,
+      pnodi, snodi;
+};
+template <class T>
+__device__ __forceinline__ T vg_se(T psi, T psat, T n, T m) {
+  if (psi < T(-1.0e-14)) {
+    T beta = dpow<T>(fabs(psi / psat), n);
+    return dpow<T>(fabs(T(1) / (beta + T(1))), m);
+  }
+  return T(1);
+}
+template <class T>
+__device__ __forceinline__ T vg_dse(T psi, T psat, T n, T n1, T psn, T nr) {
+  if (psi < T(-1.0e-14)) {
+    T beta = dpow<T>(fabs(psi / psat), n);
+    T b1 = beta + T(1), b1r = T(1) / b1;
+    return n1 * (dpow<T>(fabs(psi), n1) / psn) * dpow<T>(fabs(b1), nr) * b1r * b1r;
+  }
+  return T(0);
+}
+template <class T>
+__device__ __forceinline__ T vg_kr(T psi, T se, T mr, T m) {
+  if (psi < T(-1.0e-14)) {
+    T om = dpow<T>(fabs(se), mr);
+    T v1 = T(1) - dpow<T>(fabs(T(1) - om), m);
+    return sqrt(se) * v1 * v1;
+  }
+  return T(1);
+}
+__device__ __forceinline__ double vg_dkr(double psi, double psat, double n,
+                                         double m, double n1, double m52,
+                                         double mm1) {
+  if (psi < -1.0e-14) {
+    double beta = pow(fabs(psi / psat), n);
+    double b1 = beta + 1.0;
+    double v1 = pow(fabs(b1), m) - pow(fabs(beta), m);
+    double v2 = psat / psi;
+    double v3 = n1 * beta * v2 * pow(fabs(1.0 / b1), m52) / psat;
+    double v4 = v2 * ((2.5 / b1) * beta - 2.0) - 0.5 * pow(fabs(b1), mm1);
+    return v3 * v1 * v4;
+  }
+  return 0.0;
+}
+__device__ __forceinline__ double vg_dds(double psi, double psat, double n,
+                                         double m, double n1) {
+  if (psi < -1.0e-14) {
+    double beta = pow(fabs(psi / psat), n);
+    double b1 = beta + 1.0, b1r = 1.0 / b1;
+    return n1 * (beta / psi) * (1.0 / psi) *
+           ((1.0 + n * (beta - 1.0)) / pow(fabs(b1), m)) * b1r * b1r;
+  }
+  return 0.0;
+}
+
+// ============================================================================
+// device state (raw pointers passed to kernels)
+// ============================================================================
+struct Nodal {  // per node
+  const int32_t* mem;        // member id
+  const int32_t* loc;        // local index inside the member
+  double *volnod, *pnodi, *snodi, *vgn, *vgm, *vgrmc, *vgpsat, *vgn1, *vgnr,
+      *vgpsn, *vgmr, *vgm52, *vgmm1, *vgpnot;
+  double *pnew, *pold, *ptnew, *ptold, *ptimep, *pdiff, *swnew, *swtimep;
+  double *rhs, *xt5, *qneu, *presc, *qpnew, *qpold;
+  double *sw, *et1, *et2, *ckrw, *etai, *dckrw, *detai;
+  uint8_t *sdir;             // static (non-atmospheric) Dirichlet node
+  uint8_t *dmask;            // current Dirichlet mask (static | atm 1,2)
+  // surface nodes (valid for loc < nnod)
+  int8_t *ifatm, *ifatmp;
+  double *arenod, *atmpot, *atmact, *atmold, *atm_a, *atm_b;
+};
+
+// ============================================================================
+// init kernels
+// ============================================================================
+// TPNODI + CHPARM: nodal soil parameters = mean over incident elements of the
+// per-(layer,zone) table values; element porosity for VPEL afterwards.
+__global__ void k_tpnodi(int n, const int32_t* inc_ptr, const int32_t* inc,
+                         const int32_t* tet_soil, const double* t_poros,
+                         const double* t_elstor, const double* t_vgn,
+                         const double* t_vgrmc, const double* t_vgpsat,
+                         Nodal nd) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double p = 0, s = 0, vn = 0, vr = 0, vp = 0;
+  int c = 0;
+  for (int q = inc_ptr[i]; q < inc_ptr[i + 1]; ++q) {
+    int e = inc[q] >> 2;
+    int id = tet_soil[e];
+    p += t_poros[id]; s += t_elstor[id]; vn += t_vgn[id]; vr += t_vgrmc[id];
+    vp += t_vgpsat[id];
+    c++;
+  }
+  p /= c; s /= c; vn /= c; vp /= c; vr /= c;
+  nd.pnodi[i] = p; nd.snodi[i] = s; nd.vgn[i] = vn; nd.vgrmc[i] = vr; nd.vgpsat[i] = vp;
+  double m = (vn - 1.0) / vn;
+  nd.vgm[i] = m;
+  nd.vgn1[i] = vn - 1.0;
+  nd.vgnr[i] = 1.0 / vn;
+  nd.vgmm1[i] = m - 1.0;
+  nd.vgpsn[i] = pow(fabs(vp), vn);
+  nd.vgmr[i] = 1.0 / m;
+  nd.vgm52[i] = 2.5 * m;
+  nd.vgpnot[i] = (p - vr) / p;
+}
+
+// VOLUMS/BASIS6 in the reference's summation order, then the element record.
+__device__ __forceinline__ void ip3_rows(int nn, int r[3][3]) {
+  // IP4(II,NN) = ((NN-1)+(II-1)) mod 4 (0-based), IP3 rows cyclic shifts
+  int c0[3];
+  for (int ii = 1; ii <= 3; ++ii) c0[ii - 1] = (nn + ii) % 4;
+  for (int lr = 0; lr < 3; ++lr) {
+    r[lr][0] = c0[lr];
+    r[lr][1] = c0[(lr + 1) % 3];
+    r[lr][2] = c0[(lr + 2) % 3];
+  }
+}
+
+template <class MT>
+__global__ void k_geom(int nt, const int4* tet, const double* x, const double* y,
+                       const double* z, const int32_t* tet_soil,
+                       const double* t_permx, const double* t_permy,
+                       const double* t_permz, const double* pnodi,
+                       TetRec<MT>* rec, double* volnod_acc, int8_t* ivol_out) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nt) return;
+  int4 t = tet[e];
+  int tl[4] = {t.x, t.y, t.z, t.w};
+  double X[4], Y[4], Z[4];
+  for (int q = 0; q < 4; ++q) { X[q] = x[tl[q]]; Y[q] = y[tl[q]]; Z[q] = z[tl[q]]; }
+  const double amen[5] = {-1.0, 1.0, -1.0, 1.0, -1.0};
+  double vol = 0.0, b[4], c[4], d[4];
+  for (int nn = 0; nn < 4; ++nn) {
+    int r[3][3];
+    ip3_rows(nn, r);
+    double a2 = 0.0, a3 = 0.0;
+    for (int ii = 0; ii < 3; ++ii) {
+      int I = r[ii][0], J = r[ii][1], M = r[ii][2];
+      a3 = __dadd_rn(__dmul_rn(Y[I], Z[J]), a3);
+      a2 = __dadd_rn(__dmul_rn(Y[I], Z[M]), a2);
+    }
+    vol = __dadd_rn(vol, __dmul_rn(__dmul_rn(X[nn], amen[nn]), __dsub_rn(a3, a2)) / 6.0);
+    b[nn] = amen[nn] * __dsub_rn(a3, a2) / 6.0;
+    a2 = 0.0; a3 = 0.0;
+    for (int ii = 0; ii < 3; ++ii) {
+      int I = r[ii][0], J = r[ii][1], M = r[ii][2];
+      a3 = __dadd_rn(__dmul_rn(X[I], Z[J]), a3);
+      a2 = __dadd_rn(__dmul_rn(X[I], Z[M]), a2);
+    }
+    c[nn] = amen[nn + 1] * __dsub_rn(a3, a2) / 6.0;
+    a2 = 0.0; a3 = 0.0;
+    for (int ii = 0; ii < 3; ++ii) {
+      int I = r[ii][0], J = r[ii][1], M = r[ii][2];
+      a3 = __dadd_rn(__dmul_rn(X[I], Y[J]), a3);
+      a2 = __dadd_rn(__dmul_rn(X[I], Y[M]), a2);
+    }
+    d[nn] = amen[nn] * __dsub_rn(a3, a2) / 6.0;
+  }
+  double ivol = vol < 0.0 ? -1.0 : 1.0;
+  double av = fabs(vol);
+  double volur = 1.0 / av;
+  int id = tet_soil[e];
+  double kx = t_permx[id] * volur, ky = t_permy[id] * volur, kz = t_permz[id] * volur;
+  TetRec<MT> R;
+  for (int k = 0; k < 4; ++k)
+    for (int l = k; l < 4; ++l)
+      R.S[sym_idx(k, l)] = (MT)(kx * b[k] * b[l] + ky * c[k] * c[l] + kz * d[k] * d[l]);
+  for (int k = 0; k < 4; ++k) R.g[k] = (MT)(t_permz[id] * d[k] * ivol);
+  double pel = 0.25 * (pnodi[tl[0]] + pnodi[tl[1]] + pnodi[tl[2]] + pnodi[tl[3]]);
+  R.vol = (MT)av;
+  R.vpel = (MT)(av * pel);
+  rec[e] = R;
+  if (ivol_out) ivol_out[e] = (int8_t)ivol;
+  if (volnod_acc) {
+    double v4 = av * 0.25;
+    for (int q = 0; q < 4; ++q) atomicAdd(volnod_acc + tl[q], v4);
+  }
+}
+
+// ============================================================================
+// step actions (per member masks)
+// ============================================================================
+// surface part: BKSTEP restore + COMMIT bookkeeping + ATM update + switching
+__global__ void k_start_surface(int nsurf_rows, const int32_t* srows,
+                                const uint8_t* act, const MemberScal* ms,
+                                Nodal nd) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nsurf_rows) return;
+  const int i = srows[q];
+  const int m = nd.mem[i];
+  const uint8_t a = act[m];
+  if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START))) return;
+  const MemberScal& S = ms[m];
+  int8_t f = nd.ifatm[i];
+  if (a & ACT_COMMIT) {
+    nd.ifatmp[i] = f;
+    nd.atmold[i] = nd.atmact[i];
+  }
+  if (a & ACT_BACKSTEP) {
+    f = nd.ifatmp[i];
+    nd.atmact[i] = nd.atmold[i];
+  }
+  if (a & ACT_START) {
+    double pot = nd.atmpot[i];
+    const double area = nd.arenod[i];
+    if (S.atm_mode == 1) {
+      double va = S.hspatm ? S.atm_va : nd.atm_a[i];
+      double vb = S.hspatm ? S.atm_vb : nd.atm_b[i];
+      double slope = (S.ieto != 0) ? 0.0 : (vb - va) / (S.atm_tb - S.atm_ta);
+      pot = (va + slope * (S.time - S.atm_ta)) * area;
+    } else if (S.atm_mode == 2) {
+      double vb = S.hspatm ? S.atm_vb : nd.atm_b[i];
+      pot = vb * area;
+    }
+    nd.atmpot[i] = pot;
+    double act_ = nd.atmact[i];
+    if (S.atm_mode != 0 && f == 0) act_ = (pot >= 0.0) ? pot : (1.0 - S.scf) * pot;
+    // SWITCH_OLD (switch_old.f)
+    double p = nd.pnew[i];
+    if (f != -1) {
+      if (f == 1 && p >= 0.0 && (pot < 0.0 || act_ > pot)) {
+        f = 0; act_ = pot;
+      } else if (f == 1 && p <= S.pmin && (pot > 0.0 || act_ < pot)) {
+        f = 0; act_ = pot;
+      } else if (f == 0 && p >= 0.0 && pot >= 0.0) {
+        f = 1; p = 0.0;
+      } else if (f == 0 && p <= S.pmin && pot < 0.0) {
+        f = 1; p = S.pmin;
+      }
+    }
+    nd.pnew[i] = p;
+    nd.atmact[i] = act_;
+  }
+  nd.ifatm[i] = f;
+}
+
+// all nodes.  phase 0: COMMIT (ptimep <- pnew) and BACKSTEP restore;
+// phase 1 (after the surface kernel): Dirichlet mask, START / NEXT updates.
+__global__ void k_start_nodes(const int32_t* bm_mem, const int32_t* bm_r0,
+                              const int32_t* bm_r1, const uint8_t* act,
+                              const MemberScal* ms, Nodal nd, int phase) {
+  const int m = bm_mem[blockIdx.x];
+  const uint8_t a = act[m];
+  if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START | ACT_NEXT))) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  if (phase == 0) {
+    if (a & ACT_COMMIT) {
+      nd.qpold[i] = nd.qpnew[i];
+      nd.ptimep[i] = nd.pnew[i];
+    }
+    if (a & ACT_BACKSTEP) {
+      nd.pnew[i] = nd.ptimep[i];
+      nd.qpnew[i] = nd.qpold[i];
+    }
+    return;
+  }
+  const double th = ms[m].tetaf;
+  const int loc = nd.loc[i];
+  const bool surf = loc < ms[m].nnod;
+  if (a & (ACT_START | ACT_BACKSTEP | ACT_COMMIT)) {
+    uint8_t dm = nd.sdir[i];
+    if (surf) dm |= (nd.ifatm[i] == 1 || nd.ifatm[i] == 2);
+    nd.dmask[i] = dm;
+  }
+  if (a & ACT_START) {
+    const double p = nd.pnew[i];
+    const double pt = th * p + (1.0 - th) * nd.ptimep[i];
+    nd.pold[i] = p;
+    nd.ptnew[i] = pt;
+    nd.ptold[i] = pt;
+    const double tp = nd.ptimep[i];
+    nd.swtimep[i] = nd.vgpnot[i] * vg_se<double>(tp, nd.vgpsat[i], nd.vgn[i], nd.vgm[i]) +
+                    nd.vgrmc[i] / nd.pnodi[i];
+  } else if (a & ACT_NEXT) {
+    const double p = nd.pnew[i];
+    nd.pold[i] = p;
+    nd.ptold[i] = nd.ptnew[i];
+    nd.ptnew[i] = th * p + (1.0 - th) * nd.ptimep[i];
+  }
+}
+
+// ============================================================================
+// nonlinear iteration kernels
+// ============================================================================
+// nodal soil characteristics; CT = compute type for the LHS-only quantities
+// (ckrw, et2); SWNEW is always evaluated in FP64 (it enters the residual).
+template <class CT>
+__global__ void k_vg(const int32_t* bm_mem, const int32_t* bm_r0,
+                     const int32_t* bm_r1, const uint8_t* act,
+                     const MemberScal* ms, Nodal nd, int newton) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const double psat = nd.vgpsat[i], n = nd.vgn[i], mm = nd.vgm[i];
+  const double pnot = nd.vgpnot[i], rmc = nd.vgrmc[i], por = nd.pnodi[i],
+               ss = nd.snodi[i];
+  const double pt = nd.ptnew[i];
+  if (!newton) {
+    const double p = nd.pnew[i];
+    const double se_new = vg_se<double>(p, psat, n, mm);
+    const double swn = pnot * se_new + rmc / por;
+    nd.swnew[i] = swn;
+    double sw;
+    CT se_c;
+    if (pt == p) {
+      sw = swn;
+      se_c = (CT)se_new;
+    } else {
+      const double se_t = vg_se<double>(pt, psat, n, mm);
+      sw = pnot * se_t + rmc / por;
+      se_c = (CT)se_t;
+    }
+    nd.et1[i] = sw * ss;
+    CT dse = vg_dse<CT>((CT)pt, (CT)psat, (CT)n, (CT)nd.vgn1[i], (CT)nd.vgpsn[i],
+                        (CT)nd.vgnr[i]);
+    nd.et2[i] = (double)((CT)pnot * dse);
+    nd.ckrw[i] = (double)vg_kr<CT>((CT)pt, se_c, (CT)nd.vgmr[i], (CT)mm);
+    nd.sw[i] = sw;
+  } else {
+    const double se = vg_se<double>(pt, psat, n, mm);
+    const double dsedp = vg_dse<double>(pt, psat, n, nd.vgn1[i], nd.vgpsn[i], nd.vgnr[i]);
+    const double dswdp = pnot * dsedp;
+    const double sw = pnot * se + rmc / por;
+    nd.sw[i] = sw;
+    nd.etai[i] = sw * ss + por * dswdp;
+    nd.detai[i] = dswdp * ss + por * pnot * vg_dds(pt, psat, n, mm, nd.vgn1[i]);
+    nd.ckrw[i] = vg_kr<double>(pt, se, nd.vgmr[i], mm);
+    nd.dckrw[i] = vg_dkr(pt, psat, n, mm, nd.vgn1[i], nd.vgm52[i], nd.vgmm1[i]);
+  }
+}
+
+// Row-owned Picard assembly: 16 lanes per row, lane l owns slot l of the row.
+// Computes LHS = theta*K + M/dt + diag(Ms*ET2)/dt (CFMATP), RHS (RHSPIC +
+// RHSGRV) in FP64, XT5 = RHS, then BCPIC (Dirichlet RHS zero, Neumann and
+// atmospheric fluxes).  lm_d / lm_o: local mass matrix diagonal/off-diagonal
+// weights (LOCMAS: 1/4,0 lumped; 1/10,1/20 consistent).
+template <class MT>
+__global__ void __launch_bounds__(kThreads)
+k_assemble_picard(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                  const uint8_t* act, const MemberScal* ms,
+                  const int32_t* rowptr, const int32_t* cols,
+                  const int32_t* inc_ptr, const int32_t* inc, const int4* tet,
+                  const TetRec<MT>* rec, Nodal nd, MT* vals, double lm_d,
+                  double lm_o) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  const MemberScal& S = ms[m];
+  const double rdt = 1.0 / S.deltat, th = S.tetaf;
+  int s0 = 0, s1 = 0, col = -1;
+  if (rowok) {
+    s0 = rowptr[i]; s1 = rowptr[i + 1];
+    if (s0 + lane < s1) col = cols[s0 + lane];
+  }
+  double lhs = 0.0, rpart = 0.0;
+  const double et2i = rowok ? nd.et2[i] : 0.0;
+  const int p0 = rowok ? inc_ptr[i] : 0, p1 = rowok ? inc_ptr[i + 1] : 0;
+  for (int p = p0; p < p1; ++p) {
+    const int ek = inc[p];
+    const int e = ek >> 2, k = ek & 3;
+    const int4 t = tet[e];
+    const int tn[4] = {t.x, t.y, t.z, t.w};
+    const TetRec<MT> R = rec[e];
+    const double kr = 0.25 * (nd.ckrw[t.x] + nd.ckrw[t.y] + nd.ckrw[t.z] + nd.ckrw[t.w]);
+    const double e1 = 0.25 * (nd.et1[t.x] + nd.et1[t.y] + nd.et1[t.z] + nd.et1[t.w]);
+    const double ve1 = (double)R.vol * e1, ve = (double)R.vpel;
+    int l = -1;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) if (tn[q] == col) l = q;
+    if (l >= 0) {
+      const double lm = (l == k) ? lm_d : lm_o;
+      lhs += th * (kr * (double)R.S[sym_idx(k, l)]) + ve1 * lm * rdt;
+      if (l == k) lhs += ve * lm_d * et2i * rdt;
+    }
+    if (lane < 4) {
+      const int nl = tn[lane];
+      const double lm = (lane == k) ? lm_d : lm_o;
+      const double kkl = kr * (double)R.S[sym_idx(k, lane)];
+      rpart -= kkl * nd.ptnew[nl] + ve1 * lm * rdt * (nd.pnew[nl] - nd.ptimep[nl]) +
+               ve * lm * rdt * (nd.swnew[nl] - nd.swtimep[nl]);
+    } else if (lane == 4) {
+      rpart -= kr * (double)R.g[k];
+    }
+  }
+  const double rhs = group_sum16(rpart);
+  if (!rowok) return;
+  if (col >= 0) vals[s0 + lane] = (MT)lhs;
+  if (lane == 0) {
+    nd.xt5[i] = rhs;
+    double b = rhs;
+    const int loc = nd.loc[i];
+    if (nd.dmask[i]) {
+      b = 0.0;
+    } else if (loc < S.nnod && nd.ifatm[i] == 0) {
+      b += th * nd.atmact[i] + (1.0 - th) * nd.atmold[i];
+    }
+    b += nd.qneu[i];
+    nd.rhs[i] = b;
+  }
+}
+
+// Row-owned Newton assembly (ASSNEW + RHSNEW + CFMATN + RHSGRV + BCNEW):
+// LHS = theta*K + M/dt + J where J holds the derivative terms.
+template <class MT>
+__global__ void __launch_bounds__(kThreads)
+k_assemble_newton(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                  const uint8_t* act, const MemberScal* ms,
+                  const int32_t* rowptr, const int32_t* cols,
+                  const int32_t* inc_ptr, const int32_t* inc, const int4* tet,
+                  const TetRec<MT>* rec, Nodal nd, MT* vals, double lm_d,
+                  double lm_o) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  const MemberScal& S = ms[m];
+  const double rdt = 1.0 / S.deltat, th = S.tetaf;
+  int s0 = 0, s1 = 0, col = -1;
+  if (rowok) {
+    s0 = rowptr[i]; s1 = rowptr[i + 1];
+    if (s0 + lane < s1) col = cols[s0 + lane];
+  }
+  double lhs = 0.0, rpart = 0.0;
+  const int p0 = rowok ? inc_ptr[i] : 0, p1 = rowok ? inc_ptr[i + 1] : 0;
+  for (int p = p0; p < p1; ++p) {
+    const int ek = inc[p];
+    const int e = ek >> 2, k = ek & 3;
+    const int4 t = tet[e];
+    const int tn[4] = {t.x, t.y, t.z, t.w};
+    const TetRec<MT> R = rec[e];
+    const double kr = 0.25 * (nd.ckrw[t.x] + nd.ckrw[t.y] + nd.ckrw[t.z] + nd.ckrw[t.w]);
+    const double ee = 0.25 * (nd.etai[t.x] + nd.etai[t.y] + nd.etai[t.z] + nd.etai[t.w]);
+    const double ve = (double)R.vol * ee;
+    // SUM = sum_m K0_km ptnew_m (K0 without kr), SUM1 = sum_m LM_km (pnew-ptimep)
+    double sum = 0.0, sum1 = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      sum += (double)R.S[sym_idx(k, q)] * nd.ptnew[tn[q]];
+      sum1 += ((q == k) ? lm_d : lm_o) * (nd.pnew[tn[q]] - nd.ptimep[tn[q]]);
+    }
+    const double tsumtd = th * sum + th * (double)R.g[k];
+    const double sum1tv = sum1 * th * (double)R.vol * rdt;
+    int l = -1;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) if (tn[q] == col) l = q;
+    if (l >= 0) {
+      const double lm = (l == k) ? lm_d : lm_o;
+      lhs += th * (kr * (double)R.S[sym_idx(k, l)]) + ve * lm * rdt +
+             nd.dckrw[tn[l]] * tsumtd + nd.detai[tn[l]] * sum1tv;
+    }
+    if (lane < 4) {
+      const int nl = tn[lane];
+      const double lm = (lane == k) ? lm_d : lm_o;
+      rpart -= kr * (double)R.S[sym_idx(k, lane)] * nd.ptnew[nl] +
+               ve * lm * rdt * (nd.pnew[nl] - nd.ptimep[nl]);
+    } else if (lane == 4) {
+      rpart -= kr * (double)R.g[k];
+    }
+  }
+  const double rhs = group_sum16(rpart);
+  if (!rowok) return;
+  if (col >= 0) vals[s0 + lane] = (MT)lhs;
+  if (lane == 0) {
+    nd.xt5[i] = rhs;
+    double b = rhs;
+    const int loc = nd.loc[i];
+    if (nd.dmask[i]) b = 0.0;
+    else if (loc < S.nnod && nd.ifatm[i] == 0)
+      b += th * nd.atmact[i] + (1.0 - th) * nd.atmold[i];
+    b += nd.qneu[i];
+    nd.rhs[i] = b;
+  }
+}
+
+// ============================================================================
+// sparse kernels
+// ============================================================================
+// y = A x with Dirichlet rows as identity; optionally accumulates per-member
+// dot products d0 += x.y and d1 += x.w (w optional).
+template <class MT, class VT>
+__global__ void __launch_bounds__(kThreads)
+k_spmv(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+       const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
+       const MT* vals, const uint8_t* dmask, const VT* x, VT* y, const VT* w,
+       double* acc, int acc_stride) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  double s = 0.0;
+  if (rowok) {
+    const int s0 = rowptr[i] + lane;
+    if (s0 < rowptr[i + 1]) s = (double)vals[s0] * (double)x[cols[s0]];
+  }
+  s = group_sum16(s);
+  double d[2] = {0.0, 0.0};
+  if (rowok && lane == 0) {
+    const double xi = (double)x[i];
+    const double yi = dmask[i] ? xi : s;
+    y[i] = (VT)yi;
+    d[0] = xi * yi;
+    if (w) d[1] = xi * (double)w[i];
+  }
+  if (acc) block_accumulate<2>(d, acc + (size_t)m * acc_stride);
+}
+
+// r = b - A x (masked), r zero at Dirichlet rows
+template <class MT, class VT>
+__global__ void __launch_bounds__(kThreads)
+k_resid(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+        const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
+        const MT* vals, const uint8_t* dmask, const VT* x, const VT* b, VT* r,
+        double* acc, int acc_stride) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  double s = 0.0;
+  if (rowok) {
+    const int s0 = rowptr[i] + lane;
+    if (s0 < rowptr[i + 1]) s = (double)vals[s0] * (double)x[cols[s0]];
+  }
+  s = group_sum16(s);
+  double d[1] = {0.0};
+  if (rowok && lane == 0) {
+    double ri = dmask[i] ? 0.0 : (double)b[i] - s;
+    r[i] = (VT)ri;
+    d[0] = ri * ri;
+  }
+  if (acc) block_accumulate<1>(d, acc + (size_t)m * acc_stride);
+}
+
+// ---- preconditioners ---------------------------------------------------
+// Jacobi: inv diag
+template <class MT, class VT>
+__global__ void k_jacobi_setup(const int32_t* bm_mem, const int32_t* bm_r0,
+                               const int32_t* bm_r1, const uint8_t* active,
+                               const int32_t* diag, const MT* vals,
+                               const uint8_t* dmask, VT* dinv) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  dinv[i] = dmask[i] ? (VT)1 : (VT)(1.0 / (double)vals[diag[i]]);
+}
+
+// Column-line preconditioner: exact tridiagonal solve along each vertical
+// column of the extruded mesh (the vertical edges carry >99% of the
+// off-diagonal weight on these thin-layered meshes).  Setup stores the
+// pivots' inverses and the masked vertical couplings.
+template <class MT, class VT>
+__global__ void k_line_setup(int ncol_rows, const int32_t* crows,
+                             const int32_t* mem, const uint8_t* active,
+                             const MemberScal* ms, const int32_t* diag,
+                             const int32_t* down, const MT* vals,
+                             const uint8_t* dmask, VT* pinv, VT* cdown) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ncol_rows) return;
+  const int top = crows[q];
+  const int m = mem[top];
+  if (!active[m]) return;
+  const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
+  double piv_prev = 1.0, c_prev = 0.0;
+  for (int k = 0; k < nl; ++k) {
+    const int i = top + k * nnod;
+    const bool di = dmask[i];
+    double a = di ? 1.0 : (double)vals[diag[i]];
+    double c = 0.0;
+    if (k + 1 < nl && !di && !dmask[i + nnod] && down[i] >= 0) c = (double)vals[down[i]];
+    double piv = a - c_prev * c_prev / piv_prev;
+    pinv[i] = (VT)(1.0 / piv);
+    cdown[i] = (VT)c;
+    piv_prev = piv;
+    c_prev = c;
+  }
+}
+
+// z = T^-1 r per column; accumulates w.z (w = q for the PCG beta) per member
+template <class VT>
+__global__ void k_line_apply(int ncol_rows, const int32_t* crows,
+                             const int32_t* mem, const uint8_t* active,
+                             const MemberScal* ms, const VT* pinv,
+                             const VT* cdown, const VT* r, VT* z, const VT* w,
+                             double* acc, int acc_stride, int acc_off) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = q < ncol_rows;
+  int top = 0, m = 0;
+  if (ok) {
+    top = crows[q];
+    m = mem[top];
+    ok = active[m];
+  }
+  if (ok) {
+    const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
+    VT y[kMaxLayers];
+    VT yprev = 0, cprev = 0;
+    for (int k = 0; k < nl; ++k) {
+      const int i = top + k * nnod;
+      VT yk = r[i] - cprev * yprev * (k > 0 ? pinv[i - nnod] : (VT)0);
+      y[k] = yk;
+      yprev = yk;
+      cprev = cdown[i];
+    }
+    VT znext = 0;
+    double dot = 0.0;
+    for (int k = nl - 1; k >= 0; --k) {
+      const int i = top + k * nnod;
+      VT zk = (y[k] - cdown[i] * znext) * pinv[i];
+      z[i] = zk;
+      if (w) dot += (double)w[i] * (double)zk;
+      znext = zk;
+    }
+    if (w) atomicAdd(acc + (size_t)m * acc_stride + acc_off, dot);
+  }
+}
+
+// IC(0) factor (left-looking row form of INCLDP), one thread per row of one
+// level.  F holds L in the lower+diagonal slots of each row.  Dirichlet rows
+// and columns are identity / zero (the reference's 1e-9*RMAX penalty makes
+// them decouple to within 1e-91).
+template <class MT, class FT>
+__global__ void k_ic0_level(int nrows, const int32_t* rows, const int32_t* rowptr,
+                            const int32_t* cols, const int32_t* diag,
+                            const MT* vals, const uint8_t* dmask,
+                            const uint8_t* active, const int32_t* mem, FT* F) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrows) return;
+  const int i = rows[q];
+  if (!active[mem[i]]) return;
+  const int s0 = rowptr[i], sd = diag[i];
+  if (dmask[i]) {
+    for (int s = s0; s < sd; ++s) F[s] = 0;
+    F[sd] = 1;
+    return;
+  }
+  double dsum = 0.0;
+  for (int s = s0; s < sd; ++s) {
+    const int j = cols[s];
+    double a = dmask[j] ? 0.0 : (double)vals[s];
+    // subtract sum_{k<j} L_ik L_jk over the common lower pattern
+    int pi = s0, pj = rowptr[j];
+    const int ej = diag[j];
+    double acc = 0.0;
+    while (pi < s && pj < ej) {
+      const int ci = cols[pi], cj = cols[pj];
+      if (ci == cj) { acc += (double)F[pi] * (double)F[pj]; ++pi; ++pj; }
+      else if (ci < cj) ++pi;
+      else ++pj;
+    }
+    const double lij = (a - acc) / (double)F[ej];
+    F[s] = (FT)lij;
+    dsum += lij * lij;
+  }
+  double a = (double)vals[sd] - dsum;
+  if (a <= 0.0) a = fabs((double)vals[sd]);  // breakdown guard
+  F[sd] = (FT)sqrt(a);
+}
+
+// forward L y = r (level of rows), 16 lanes per row
+template <class FT, class VT>
+__global__ void k_lsolve_level(int nrows, const int32_t* rows, const int32_t* rowptr,
+                               const int32_t* cols, const int32_t* diag,
+                               const FT* F, const uint8_t* active,
+                               const int32_t* mem, const VT* r, VT* y) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+  const int lane = threadIdx.x % kGroup;
+  const bool ok = grp < nrows;
+  int i = 0;
+  double s = 0.0;
+  bool act = false;
+  if (ok) {
+    i = rows[grp];
+    act = active[mem[i]];
+    if (act) {
+      const int sl = rowptr[i] + lane;
+      if (sl < diag[i]) s = (double)F[sl] * (double)y[cols[sl]];
+    }
+  }
+  s = group_sum16(s);
+  if (ok && act && lane == 0) y[i] = (VT)(((double)r[i] - s) / (double)F[diag[i]]);
+}
+
+// backward L^T x = y using the transposed slots (tslot[s] = slot of (j,i))
+template <class FT, class VT>
+__global__ void k_ltsolve_level(int nrows, const int32_t* rows, const int32_t* rowptr,
+                                const int32_t* cols, const int32_t* diag,
+                                const int32_t* tslot, const FT* F,
+                                const uint8_t* active, const int32_t* mem,
+                                const VT* y, VT* x) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+  const int lane = threadIdx.x % kGroup;
+  const bool ok = grp < nrows;
+  int i = 0;
+  double s = 0.0;
+  bool act = false;
+  if (ok) {
+    i = rows[grp];
+    act = active[mem[i]];
+    if (act) {
+      const int sl = diag[i] + 1 + lane;
+      if (sl < rowptr[i + 1]) s = (double)F[tslot[sl]] * (double)x[cols[sl]];
+    }
+  }
+  s = group_sum16(s);
+  if (ok && act && lane == 0) x[i] = (VT)(((double)y[i] - s) / (double)F[diag[i]]);
+}
+
+// ILU(0) (row IKJ / Doolittle), one thread per row of one level; then a
+// conversion pass to the reference's split (L with diagonal, unit U).
+template <class MT, class FT>
+__global__ void k_ilu0_level(int nrows, const int32_t* rows, const int32_t* rowptr,
+                             const int32_t* cols, const int32_t* diag,
+                             const MT* vals, const uint8_t* dmask,
+                             const uint8_t* active, const int32_t* mem, FT* F) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrows) return;
+  const int i = rows[q];
+  if (!active[mem[i]]) return;
+  const int s0 = rowptr[i], s1 = rowptr[i + 1], sd = diag[i];
+  if (dmask[i]) {
+    for (int s = s0; s < s1; ++s) F[s] = (s == sd) ? (FT)1 : (FT)0;
+    return;
+  }
+  for (int s = s0; s < s1; ++s) F[s] = dmask[cols[s]] ? (FT)0 : (FT)vals[s];
+  for (int s = s0; s < sd; ++s) {
+    const int k = cols[s];
+    if (dmask[k]) continue;
+    const double l = (double)F[s] / (double)F[diag[k]];
+    F[s] = (FT)l;
+    int pi = s + 1;
+    for (int t = diag[k] + 1; t < rowptr[k + 1]; ++t) {
+      const int j = cols[t];
+      while (pi < s1 && cols[pi] < j) ++pi;
+      if (pi < s1 && cols[pi] == j) F[pi] = (FT)((double)F[pi] - l * (double)F[t]);
+    }
+  }
+  if ((double)F[sd] == 0.0) F[sd] = (FT)1;
+}
+
+template <class FT>
+__global__ void k_ilu0_split(int n, const int32_t* rowptr, const int32_t* cols,
+                             const int32_t* diag, const uint8_t* active,
+                             const int32_t* mem, const FT* Fd, FT* G) {
+  // G = reference split of the Doolittle factor Fd
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !active[mem[i]]) return;
+  const double uii = (double)Fd[diag[i]];
+  for (int s = rowptr[i]; s < rowptr[i + 1]; ++s) {
+    const int j = cols[s];
+    if (j < i) G[s] = (FT)((double)Fd[s] * (double)Fd[diag[j]]);
+    else if (j == i) G[s] = (FT)uii;
+    else G[s] = (FT)((double)Fd[s] / uii);
+  }
+}
+
+// unit-upper solve x = U^-1 h (reference PRODU), backward levels
+template <class FT, class VT>
+__global__ void k_usolve_level(int nrows, const int32_t* rows, const int32_t* rowptr,
+                               const int32_t* cols, const int32_t* diag,
+                               const FT* G, const uint8_t* active,
+                               const int32_t* mem, const VT* h, VT* x) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+  const int lane = threadIdx.x % kGroup;
+  const bool ok = grp < nrows;
+  int i = 0;
+  double s = 0.0;
+  bool act = false;
+  if (ok) {
+    i = rows[grp];
+    act = active[mem[i]];
+    if (act) {
+      const int sl = diag[i] + 1 + lane;
+      if (sl < rowptr[i + 1]) s = (double)G[sl] * (double)x[cols[sl]];
+    }
+  }
+  s = group_sum16(s);
+  if (ok && act && lane == 0) x[i] = (VT)((double)h[i] - s);
+}
+
+// y = U x with unit-diagonal U (reference PRU)
+template <class FT, class VT>
+__global__ void k_umul(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                       const uint8_t* active, const int32_t* rowptr,
+                       const int32_t* cols, const int32_t* diag, const FT* G,
+                       const VT* x, VT* y) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  double s = 0.0;
+  if (rowok) {
+    const int sl = diag[i] + 1 + lane;
+    if (sl < rowptr[i + 1]) s = (double)G[sl] * (double)x[cols[sl]];
+  }
+  s = group_sum16(s);
+  if (rowok && lane == 0) y[i] = (VT)((double)x[i] + s);
+}
+
+// ---- Krylov vector kernels (per member scalars in sc[m*SC_N + ...]) ------
+// (k_spmv accumulates x.y, x.w into two consecutive slots: PQ, PR; the
+// r-update accumulates |r|^2 and q.z into RR, QZ.)
+enum {
+  SC_PQ = 0, SC_PR, SC_RR, SC_QZ, SC_XL, SC_ROJ, SC_SIG, SC_AA, SC_BB,
+  SC_ROJM1, SC_ALFJM1, SC_ETAJ, SC_ALF, SC_BETA, SC_ERR, SC_NB, SC_N
+};
+
+// x0 = M^-1 b path helpers: generic axpby-style kernels
+template <class VT>
+__global__ void k_pcg_update_rx(const int32_t* bm_mem, const int32_t* bm_r0,
+                                const int32_t* bm_r1, const uint8_t* active,
+                                const double* sc, VT* r, VT* x, const VT* p,
+                                const VT* q, const uint8_t* dmask,
+                                const VT* dinv, VT* z, double* acc) {
+  // alfa = (p.r)/(p.q); r -= alfa q; x += alfa p; rr += |r_masked|^2;
+  // Jacobi (dinv != NULL): z = dinv*r, qz += q.z
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  double d[2] = {0.0, 0.0};
+  if (i < bm_r1[blockIdx.x]) {
+    const double alfa = sc[m * SC_N + SC_PR] / sc[m * SC_N + SC_PQ];
+    const double ri = (double)r[i] - alfa * (double)q[i];
+    r[i] = (VT)ri;
+    x[i] = (VT)((double)x[i] + alfa * (double)p[i]);
+    if (!dmask[i]) d[0] = ri * ri;
+    if (dinv) {
+      const double zi = (double)dinv[i] * ri;
+      z[i] = (VT)zi;
+      d[1] = (double)q[i] * zi;
+    }
+  }
+  block_accumulate<2>(d, (double*)sc + (size_t)m * SC_N + SC_RR - 0);
+}
+
+template <class VT>
+__global__ void k_pcg_update_p(const int32_t* bm_mem, const int32_t* bm_r0,
+                               const int32_t* bm_r1, const uint8_t* active,
+                               const double* sc, VT* p, const VT* z) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const double beta = -sc[m * SC_N + SC_QZ] / sc[m * SC_N + SC_PQ];
+  p[i] = (VT)((double)z[i] + beta * (double)p[i]);
+}
+
+template <class VT>
+__global__ void k_dot(const int32_t* bm_mem, const int32_t* bm_r0,
+                      const int32_t* bm_r1, const uint8_t* active, const VT* a,
+                      const VT* b, const uint8_t* mask, double* acc,
+                      int acc_stride, int acc_off) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  double d[1] = {0.0};
+  if (i < bm_r1[blockIdx.x] && !(mask && mask[i])) d[0] = (double)a[i] * (double)b[i];
+  block_accumulate<1>(d, acc + (size_t)m * acc_stride + acc_off);
+}
+
+template <class VA, class VB>
+__global__ void k_copy_cast(const int32_t* bm_mem, const int32_t* bm_r0,
+                            const int32_t* bm_r1, const uint8_t* active,
+                            const VA* a, VB* b, const double* scale,
+                            int scale_stride) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  double s = scale ? scale[(size_t)m * scale_stride] : 1.0;
+  b[i] = (VB)((double)a[i] * s);
+}
+
+// x += s*e (refinement)
+template <class VE>
+__global__ void k_axpy_ref(const int32_t* bm_mem, const int32_t* bm_r0,
+                           const int32_t* bm_r1, const uint8_t* active,
+                           double* x, const VE* e, const double* scale,
+                           int scale_stride) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  x[i] += (double)e[i] * scale[(size_t)m * scale_stride];
+}
+
+// BiCGSTAB elementwise pieces
+template <class VT>
+__global__ void k_bicg_p(const int32_t* bm_mem, const int32_t* bm_r0,
+                         const int32_t* bm_r1, const uint8_t* active,
+                         const double* sc, VT* p, const VT* r, const VT* pjm,
+                         const VT* vjm) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const double* S = sc + (size_t)m * SC_N;
+  const double beta = (S[SC_ROJ] / S[SC_ROJM1]) * (S[SC_ALFJM1] / S[SC_ETAJ]);
+  p[i] = (VT)((double)r[i] + beta * ((double)pjm[i] - S[SC_ETAJ] * (double)vjm[i]));
+}
+template <class VT>
+__global__ void k_bicg_s(const int32_t* bm_mem, const int32_t* bm_r0,
+                         const int32_t* bm_r1, const uint8_t* active,
+                         const double* sc, VT* s, const VT* r, const VT* v) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const double alf = sc[m * SC_N + SC_ROJ] / sc[m * SC_N + SC_SIG];
+  s[i] = (VT)((double)r[i] - alf * (double)v[i]);
+}
+template <class VT>
+__global__ void k_bicg_st(const int32_t* bm_mem, const int32_t* bm_r0,
+                          const int32_t* bm_r1, const uint8_t* active,
+                          double* sc, const VT* s, const VT* t) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  double d[2] = {0.0, 0.0};
+  if (i < bm_r1[blockIdx.x]) {
+    d[0] = (double)s[i] * (double)t[i];
+    d[1] = (double)t[i] * (double)t[i];
+  }
+  block_accumulate<2>(d, sc + (size_t)m * SC_N + SC_AA);
+}
+template <class VT>
+__global__ void k_bicg_xr(const int32_t* bm_mem, const int32_t* bm_r0,
+                          const int32_t* bm_r1, const uint8_t* active,
+                          double* sc, VT* x, VT* r, const VT* p, const VT* s,
+                          const VT* t, const uint8_t* dmask) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  double d[1] = {0.0};
+  if (i < bm_r1[blockIdx.x]) {
+    const double* S = sc + (size_t)m * SC_N;
+    const double alf = S[SC_ROJ] / S[SC_SIG];
+    const double eta = S[SC_AA] / S[SC_BB];
+    x[i] = (VT)((double)x[i] + alf * (double)p[i] + eta * (double)s[i]);
+    double ri = dmask[i] ? 0.0 : (double)s[i] - eta * (double)t[i];
+    r[i] = (VT)ri;
+    d[0] = ri * ri;
+  }
+  block_accumulate<1>(d, sc + (size_t)m * SC_N + SC_RR);
+}
+template <class VT>
+__global__ void k_scale_vec(const int32_t* bm_mem, const int32_t* bm_r0,
+                            const int32_t* bm_r1, const uint8_t* active, VT* v,
+                            const VT* d) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  v[i] = (VT)((double)v[i] * (double)d[i]);
+}
+template <class VT>
+__global__ void k_sub_vec(const int32_t* bm_mem, const int32_t* bm_r0,
+                          const int32_t* bm_r1, const uint8_t* active, VT* out,
+                          const VT* a, const VT* b) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  out[i] = (VT)((double)a[i] - (double)b[i]);
+}
+template <class VT>
+__global__ void k_set_vec(const int32_t* bm_mem, const int32_t* bm_r0,
+                          const int32_t* bm_r1, const uint8_t* active, VT* out,
+                          const VT* a, VT c) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  out[i] = a ? a[i] : c;
+}
+
+// per-member Krylov decision: PCG (mode 0) or BiCGSTAB (mode 1)
+__global__ void k_krylov_decide(int nmem, uint8_t* active, double* sc,
+                                int32_t* niter, int itmax, double tol, int mode,
+                                int32_t* nact) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  int a = 0;
+  if (m < nmem && active[m]) {
+    double* S = sc + (size_t)m * SC_N;
+    const double xl = S[SC_XL];
+    const double err = (xl > 0.0) ? sqrt(S[SC_RR] / xl) : 0.0;
+    S[SC_ERR] = err;
+    bool cont = (mode == 0) ? (err > tol && niter[m] < itmax)
+                            : (niter[m] <= itmax && err > tol);
+    if (mode == 1 && cont) {
+      S[SC_ROJM1] = S[SC_ROJ];
+      S[SC_ALFJM1] = S[SC_ROJ] / S[SC_SIG];
+      S[SC_ETAJ] = S[SC_AA] / S[SC_BB];
+    }
+    if (cont) {
+      niter[m] += 1;
+      a = 1;
+    } else {
+      active[m] = 0;
+    }
+    S[SC_PR] = S[SC_PQ] = S[SC_QZ] = S[SC_RR] = 0.0;
+    S[SC_ROJ] = S[SC_SIG] = S[SC_AA] = S[SC_BB] = 0.0;
+  }
+  if (m < nmem) atomicAdd(nact, a);
+}
+
+// ============================================================================
+// post-solve kernels
+// ============================================================================
+// PNEW += PDIFF then SHLPIC/SHLNEW: Dirichlet nodes take PRESC (static) or
+// POLD (atmospheric Dirichlet).
+__global__ void k_update_shl(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* act,
+                             Nodal nd) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  double p = nd.pnew[i] + nd.pdiff[i];
+  if (nd.sdir[i]) p = nd.presc[i];
+  else if (nd.dmask[i]) p = nd.pold[i];
+  nd.pnew[i] = p;
+}
+
+// MASBAL (back-calculated Dirichlet fluxes, DSTORE, FLUXMB sums) + RELAX +
+// NORMS contributions.  One 16-lane group per row (row products for the
+// back-calculated flux).
+template <class MT>
+__global__ void __launch_bounds__(kThreads)
+k_masbal_norms(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+               const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
+               const int32_t* cols, const MT* vals, Nodal nd, double* red,
+               double* redmax, int newton_sw) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  const MemberScal& S = ms[m];
+  bool dir = rowok && nd.dmask[i];
+  double sp = 0.0;
+  if (dir) {
+    const int sl = rowptr[i] + lane;
+    if (sl < rowptr[i + 1]) sp = (double)vals[sl] * nd.pdiff[cols[sl]];
+  }
+  sp = group_sum16(sp);
+  double v[RD_STORE1] = {};
+  double pinf = 0.0, finf = 0.0;
+  if (rowok && lane == 0) {
+    const double th = S.tetaf, thr = 1.0 / th;
+    const int loc = nd.loc[i];
+    const bool surf = loc < S.nnod;
+    double swn = nd.swnew[i], swt = nd.swtimep[i];
+    const double p = nd.pnew[i], pt = nd.ptimep[i];
+    if (newton_sw) {  // Newton: evaluate SW at current and previous heads
+      swn = nd.vgpnot[i] * vg_se<double>(p, nd.vgpsat[i], nd.vgn[i], nd.vgm[i]) +
+            nd.vgrmc[i] / nd.pnodi[i];
+      swt = nd.vgpnot[i] * vg_se<double>(pt, nd.vgpsat[i], nd.vgn[i], nd.vgm[i]) +
+            nd.vgrmc[i] / nd.pnodi[i];
+    }
+    if (dir) {
+      const double scr = sp - nd.xt5[i];
+      if (nd.sdir[i]) {
+        const double qn = (scr - (1.0 - th) * nd.qpold[i]) * thr;
+        nd.qpnew[i] = qn;
+        if (qn > 0.0) v[RD_NDIN] += qn; else v[RD_NDOUT] += qn;
+      } else if (surf) {
+        const double aa = (scr - (1.0 - th) * nd.atmold[i]) * thr;
+        nd.atmact[i] = aa;
+      }
+    }
+    if (surf && nd.ifatm[i] != -1) {
+      const double aa = nd.atmact[i];
+      if (nd.ifatm[i] == 1 || nd.ifatm[i] == 2) {
+        if (aa > 0.0) v[RD_ADIN] += aa; else v[RD_ADOUT] += aa;
+      } else {
+        if (aa > 0.0) v[RD_ANIN] += aa; else v[RD_ANOUT] += aa;
+      }
+    }
+    if (S.deltat < 1.0e15)
+      v[RD_DSTORE] = nd.volnod[i] * (nd.snodi[i] * (swn + swt) * 0.5 * (p - pt) +
+                                     nd.pnodi[i] * (swn - swt));
+    double pn = p;
+    if (S.nlrelx == 1) {
+      pn = S.omega * p + (1.0 - S.omega) * nd.pold[i];
+      nd.pnew[i] = pn;
+    }
+    const double diff = pn - nd.pold[i];
+    v[RD_PL2] = diff * diff;
+    const double b = nd.rhs[i];
+    v[RD_FL2] = b * b;
+    pinf = fabs(diff);
+    finf = fabs(b);
+  }
+  block_accumulate<RD_STORE1>(v, red + (size_t)m * RD_NUM);
+  // block max of pinf/finf
+  __shared__ double shm[2][kThreads / 32];
+  const int wl = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double a = warp_max(pinf), b = warp_max(finf);
+  if (wl == 0) { shm[0][w] = a; shm[1][w] = b; }
+  __syncthreads();
+  if (w == 0) {
+    a = wl < (int)(blockDim.x >> 5) ? shm[0][wl] : 0.0;
+    b = wl < (int)(blockDim.x >> 5) ? shm[1][wl] : 0.0;
+    a = warp_max(a);
+    b = warp_max(b);
+    if (wl == 0) {
+      atomic_max_nonneg(redmax + (size_t)m * 2, a);
+      atomic_max_nonneg(redmax + (size_t)m * 2 + 1, b);
+    }
+  }
+}
+
+// IKMAX = largest node index attaining PINF (norms.f uses .GE.)
+__global__ void k_ikmax(const int32_t* bm_mem, const int32_t* bm_r0,
+                        const int32_t* bm_r1, const uint8_t* act, Nodal nd,
+                        const double* redmax, int32_t* ikmax) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  if (fabs(nd.pnew[i] - nd.pold[i]) == redmax[(size_t)m * 2]) atomicMax(ikmax + m, nd.loc[i]);
+}
+
+// per member: PNEW(IKMAX), POLD(IKMAX) gathered for the host
+__global__ void k_gather_ik(int nmem, const uint8_t* act, const int32_t* node_off,
+                            const int32_t* ikmax, Nodal nd, double* out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem || !(act[m] & ACT_ITER)) return;
+  const int i = node_off[m] + max(ikmax[m], 0);
+  out[2 * m] = nd.pnew[i];
+  out[2 * m + 1] = nd.pold[i];
+}
+
+// SWITCH_OLD after the norms when PINF (or PL2) <= TOLSWI
+__global__ void k_switch(int nsurf_rows, const int32_t* srows, const uint8_t* act,
+                         const uint8_t* do_switch, const MemberScal* ms,
+                         Nodal nd) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nsurf_rows) return;
+  const int i = srows[q];
+  const int m = nd.mem[i];
+  if (!(act[m] & ACT_ITER) || !do_switch[m]) return;
+  int8_t f = nd.ifatm[i];
+  if (f == -1) return;
+  const double pot = nd.atmpot[i], pmin = ms[m].pmin;
+  double a = nd.atmact[i], p = nd.pnew[i];
+  if (f == 1 && p >= 0.0 && (pot < 0.0 || a > pot)) { f = 0; a = pot; }
+  else if (f == 1 && p <= pmin && (pot > 0.0 || a < pot)) { f = 0; a = pot; }
+  else if (f == 0 && p >= 0.0 && pot >= 0.0) { f = 1; p = 0.0; }
+  else if (f == 0 && p <= pmin && pot < 0.0) { f = 1; p = pmin; }
+  nd.ifatm[i] = f;
+  nd.atmact[i] = a;
+  nd.pnew[i] = p;
+  nd.dmask[i] = nd.sdir[i] | (uint8_t)(f == 1 || f == 2);
+}
+
+// STORE1 = sum Sw(PNEW) * VOLNOD * PNODI (storcal.f) for members in mask
+__global__ void k_store1(const int32_t* bm_mem, const int32_t* bm_r0,
+                         const int32_t* bm_r1, const uint8_t* mask, Nodal nd,
+                         double* red) {
+  const int m = bm_mem[blockIdx.x];
+  if (!mask[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  double v[1] = {0.0};
+  if (i < bm_r1[blockIdx.x]) {
+    const double sw = nd.vgpnot[i] * vg_se<double>(nd.pnew[i], nd.vgpsat[i], nd.vgn[i], nd.vgm[i]) +
+                      nd.vgrmc[i] / nd.pnodi[i];
+    v[0] = sw * nd.volnod[i] * nd.pnodi[i];
+  }
+  block_accumulate<1>(v, red + (size_t)m * RD_NUM + RD_STORE1);
+}
+
+// generic per-member flag kernel: out[m] = (in[m] & bits) != 0
+__global__ void k_flags(int nmem, const uint8_t* act, uint8_t bits, uint8_t* out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < nmem) out[m] = (act[m] & bits) ? 1 : 0;
+}
+
+// ============================================================================
+// host side
+// ============================================================================
+static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+// Host view of one member: mesh, inputs and time-stepping state.
+struct MemberHost {
+  HostMesh mesh;
+  cathy_parm_t parm;
+  double pmin = -5, scf = 0, pondh_min = 1e10;
+  // atmospheric series (atmone.f/atmnxt.f/atmbak.f state)
+  int hspatm = 1, ieto = 0, natm = 0, atm_next = 0, htiatm = 0;
+  std::vector<double> atm_t, atm_v;
+  double atmtim[4] = {0, 0, 0, 0};
+  std::vector<double> atminp[4];
+  // time stepping
+  double time = 0, timep = 0, deltat = 0;
+  int nstep = 1, iter = 1, nitert = 0, itlin = 0, kbackt = 0, kback = 0;
+  bool dtgmin = true;
+  int status = 0;  // 0 running, 1 finished, 2 failed
+  // pending device actions for the next macro-iteration
+  uint8_t pend = 0;
+  bool iterating = false;
+  // mass balance
+  double adinp = 0, adoutp = 0, ndinp = 0, ndoutp = 0, aninp = 0, anoutp = 0,
+         nninp = 0, nnoutp = 0, nnin = 0, nnout = 0;
+  double store1 = 0, store2 = 0, cvin = 0, cvout = 0, cdstor = 0, cerras = 0,
+         caeras = 0, vtot = 0;
+  // last step
+  double dstore = 0, vin = 0, vout = 0, erras = 0, errel = 0;
+  double red_last[RD_NUM];
+  bool lsfail = false;
+  bool paused = false;
+  int steps_done = 0;
+  std::vector<cathy_iter_rec_t> iter_recs;
+  std::vector<cathy_step_rec_t> step_recs;
+  // atm interpolation to push to the device
+  int atm_mode = 0;
+  double atm_ta = 0, atm_tb = 0, atm_va = 0, atm_vb = 0;
+  bool atm_nodal_dirty = false;
+  std::vector<double> atm_a_nodal, atm_b_nodal;
+};
+
+struct Engine {
+  cathy_opts_t opts;
+  int nmem = 0;
+  std::vector<std::unique_ptr<MemberHost>> M;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int N = 0;
+  long NT = 0, NNZ = 0;
+  int iopt = 1, precond = 0, precision = 0;
+  double lm_d = 0.25, lm_o = 0.0;
+  std::vector<int32_t> node_off, tet_off, nnz_off;
+  // device buffers
+  DBuf<int32_t> d_mem, d_loc, d_node_off;
+  DBuf<double> d_nodal[48];
+  DBuf<uint8_t> d_sdir, d_dmask, d_act, d_active, d_switch, d_mask2, d_outer;
+  DBuf<int8_t> d_ifatm, d_ifatmp;
+  DBuf<int4> d_tet;
+  DBuf<TetRec<double>> d_rec64;
+  DBuf<TetRec<float>> d_rec32;
+  DBuf<int32_t> d_rowptr, d_cols, d_diag, d_down, d_tslot, d_inc_ptr, d_inc;
+  DBuf<int32_t> d_srows, d_lev_f, d_lev_b;
+  std::vector<int32_t> lev_f_ptr, lev_b_ptr;  // batched levels (host)
+  DBuf<double> d_vals64;
+  DBuf<float> d_vals32;
+  DBuf<MemberScal> d_ms;
+  DBuf<double> d_red, d_redmax, d_sc, d_ikval;
+  DBuf<int32_t> d_ikmax, d_niter, d_nact;
+  // Krylov workspace (FP64 and FP32 sets)
+  DBuf<double> w64[14];
+  DBuf<float> w32[14];
+  DBuf<double> d_F64, d_G64;
+  DBuf<float> d_F32, d_G32;
+  DBuf<float> d_linv32, d_lc32;
+  DBuf<double> d_linv64, d_lc64;
+  BlockMap bm1, bm16;
+  int nsurf = 0;
+  // stats
+  double gpu_ms = 0;
+  int64_t launches = 0, lin_iters = 0, nl_iters = 0;
+  Nodal nd;
+  std::vector<MemberScal> h_ms;
+  std::vector<uint8_t> h_act;
+
+  ~Engine() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+  }
+  void count(int k = 1) { launches += k; }
+  void check_launch() { CG_TRY(cudaPeekAtLastError()); }
+  void build(int nmembers, const cathy_member_t* mem);
+  void make_blockmap(BlockMap& bm, int rows_per_block);
+  void atm_setup_member(MemberHost& h, bool initial);
+  void atm_advance(MemberHost& h);  // ATMNXT series advance
+  void atm_back(MemberHost& h);     // ATMBAK
+  void push_scalars();
+  int macro_iteration();
+  void picard_or_newton_iteration(const std::vector<int>& itm);
+  template <class MT, class VT> void solve_pcg(int itmax, double tol, bool ref_mode);
+  template <class MT> void solve_mixed(int itmax, double tol);
+  void solve_bicgstab(int isolv, int itmax, double tol);
+  template <class MT> void assemble();
+  void bare_init(int n, const std::vector<int32_t>& rowptr,
+                 const std::vector<int32_t>& cols, const std::vector<uint8_t>& dm);
+};
+
+// ---- member input -> host mesh + device arrays ---------------------------
+enum {
+  ND_VOLNOD = 0, ND_PNODI, ND_SNODI, ND_VGN, ND_VGM, ND_VGRMC, ND_VGPSAT, ND_VGN1,
+  ND_VGNR, ND_VGPSN, ND_VGMR, ND_VGM52, ND_VGMM1, ND_VGPNOT, ND_PNEW, ND_POLD,
+  ND_PTNEW, ND_PTOLD, ND_PTIMEP, ND_PDIFF, ND_SWNEW, ND_SWTIMEP, ND_RHS, ND_XT5,
+  ND_QNEU, ND_PRESC, ND_QPNEW, ND_QPOLD, ND_SW, ND_ET1, ND_ET2, ND_CKRW, ND_ETAI,
+  ND_DCKRW, ND_DETAI, ND_ARENOD, ND_ATMPOT, ND_ATMACT, ND_ATMOLD, ND_ATMA, ND_ATMB,
+  ND_X, ND_Y, ND_Z, ND_NUM
+};
+
+void Engine::make_blockmap(BlockMap& bm, int rpb) {
+  std::vector<int32_t> mm, r0, r1;
+  for (int m = 0; m < nmem; ++m)
+    for (int a = node_off[m]; a < node_off[m + 1]; a += rpb) {
+      mm.push_back(m);
+      r0.push_back(a);
+      r1.push_back(std::min(a + rpb, node_off[m + 1]));
+    }
+  bm.nblk = (int)mm.size();
+  bm.mem.alloc(mm.size()); bm.mem.upload(mm.data(), mm.size(), st);
+  bm.r0.alloc(r0.size()); bm.r0.upload(r0.data(), r0.size(), st);
+  bm.r1.alloc(r1.size()); bm.r1.upload(r1.data(), r1.size(), st);
+}
+
+// read the next atmospheric record (atmone.f READ(IIN6,...))
+static bool atm_read(MemberHost& h, double& t, std::vector<double>& v) {
+  if (h.atm_next >= h.natm) return false;
+  const int nnod = h.mesh.nnod;
+  t = h.atm_t[h.atm_next];
+  v.assign(nnod, 0.0);
+  for (int i = 0; i < nnod; ++i)
+    v[i] = h.hspatm ? h.atm_v[h.atm_next] : h.atm_v[(size_t)h.atm_next * nnod + i];
+  h.atm_next++;
+  return true;
+}
+
+// advance the series while TIME > ATMTIM(3) and choose the interpolation
+void Engine::atm_advance(MemberHost& h) {
+  if (h.htiatm != 0) { h.atm_mode = 0; return; }
+  double t;
+  std::vector<double> v;
+  while (h.time > h.atmtim[3]) {
+    h.atmtim[1] = h.atmtim[2]; h.atmtim[2] = h.atmtim[3];
+    h.atminp[1] = h.atminp[2]; h.atminp[2] = h.atminp[3];
+    if (!atm_read(h, t, v)) { h.htiatm = 1; break; }
+    h.atmtim[3] = t;
+    h.atminp[3] = v;
+  }
+  if (h.atmtim[3] > h.atmtim[2]) {
+    h.atm_mode = 1;
+    h.atm_ta = h.atmtim[2]; h.atm_tb = h.atmtim[3];
+    h.atm_va = h.atminp[2].empty() ? 0.0 : h.atminp[2][0];
+    h.atm_vb = h.atminp[3].empty() ? 0.0 : h.atminp[3][0];
+    if (!h.hspatm) { h.atm_a_nodal = h.atminp[2]; h.atm_b_nodal = h.atminp[3]; h.atm_nodal_dirty = true; }
+  } else {
+    h.atm_mode = 2;
+    h.atm_vb = h.atminp[3].empty() ? 0.0 : h.atminp[3][0];
+    if (!h.hspatm) { h.atm_b_nodal = h.atminp[3]; h.atm_nodal_dirty = true; }
+  }
+}
+
+void Engine::atm_back(MemberHost& h) {
+  if (h.atmtim[1] >= h.atmtim[2]) { h.atm_mode = 0; return; }
+  h.atm_mode = 1;
+  h.atm_ta = h.atmtim[1]; h.atm_tb = h.atmtim[2];
+  h.atm_va = h.atminp[1].empty() ? 0.0 : h.atminp[1][0];
+  h.atm_vb = h.atminp[2].empty() ? 0.0 : h.atminp[2][0];
+  if (!h.hspatm) { h.atm_a_nodal = h.atminp[1]; h.atm_b_nodal = h.atminp[2]; h.atm_nodal_dirty = true; }
+}
+
+// ATMONE (atmone.f) on the host; returns ATMPOT/ATMACT/ATMOLD/IFATM and may
+// clamp PNEW/PTIMEP at PMIN.
+void Engine::atm_setup_member(MemberHost& h, bool) {
+  const int nnod = h.mesh.nnod;
+  for (int k = 1; k <= 3; ++k) h.atminp[k].assign(nnod, 0.0);
+  h.atmtim[1] = h.atmtim[2] = 0.0;
+  h.htiatm = 0;
+  double t;
+  std::vector<double> v;
+  if (!atm_read(h, t, v)) {
+    h.htiatm = 1;
+  } else {
+    h.atmtim[3] = t;
+    h.atminp[3] = v;
+  }
+}
+
+void Engine::build(int nmembers, const cathy_member_t* mem) {
+  nmem = nmembers;
+  CG_TRY(cudaSetDevice(opts.device));
+  CG_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CG_TRY(cudaEventCreate(&ev0));
+  CG_TRY(cudaEventCreate(&ev1));
+  precision = opts.precision;
+  iopt = mem[0].parm.iopt;
+  precond = mem[0].parm.precond;
+  const int lump = mem[0].parm.lump;
+  lm_d = lump ? 0.25 : 0.1;
+  lm_o = lump ? 0.0 : 0.05;
+  for (int m = 0; m < nmem; ++m) {
+    if (mem[m].parm.iopt != iopt || mem[m].parm.lump != lump ||
+        mem[m].parm.precond != precond)
+      throw std::string("members must share IOPT, LUMP and the preconditioner");
+    if (mem[m].soil.kslope != 0) throw std::string("KSLOPE != 0 not supported");
+  }
+  // meshes (topology cached per identical DEM activity/size)
+  M.resize(nmem);
+  node_off.assign(nmem + 1, 0);
+  tet_off.assign(nmem + 1, 0);
+  nnz_off.assign(nmem + 1, 0);
+  std::map<std::string, int> topo_cache;
+  for (int m = 0; m < nmem; ++m) {
+    M[m].reset(new MemberHost());
+    MemberHost& h = *M[m];
+    h.parm = mem[m].parm;
+    if (!build_mesh(mem[m].dem, iopt, h.mesh)) throw std::string("mesh construction failed");
+    node_off[m + 1] = node_off[m] + h.mesh.n;
+    tet_off[m + 1] = tet_off[m] + h.mesh.nt;
+    nnz_off[m + 1] = nnz_off[m] + (int32_t)h.mesh.nnz();
+  }
+  for (int m = 0; m < nmem; ++m) {
+    const HostMesh& g = M[m]->mesh;
+    for (int i = 0; i < g.n; ++i)
+      if (g.rowptr[i + 1] - g.rowptr[i] > kGroup)
+        throw std::string("matrix row longer than 16 entries");
+    if (precond == 2 && g.nstr + 1 > kMaxLayers)
+      throw std::string("too many layers for the column-line preconditioner");
+  }
+  N = node_off[nmem];
+  NT = tet_off[nmem];
+  NNZ = nnz_off[nmem];
+  if (NNZ > 2147483647L || (long)NT * 4 > 2147483647L)
+    throw std::string("problem too large for 32-bit indices");
+  // ---- concatenated host arrays ----
+  std::vector<int32_t> h_mem(N), h_loc(N), h_rowptr(N + 1), h_cols(NNZ), h_diag(N),
+      h_down(N), h_tslot(NNZ), h_incptr(N + 1), h_srows;
+  std::vector<int32_t> h_inc, h_tetsoil(NT);
+  std::vector<int4> h_tet(NT);
+  std::vector<double> h_x(N), h_y(N), h_z(N), h_arenod(N, 0.0);
+  std::vector<uint8_t> h_sdir(N, 0);
+  std::vector<double> h_presc(N, 0.0), h_qneu(N, 0.0), h_pinit(N, 0.0);
+  std::vector<double> tabs[8];
+  std::vector<int32_t> soil_off(nmem + 1, 0);
+  h_inc.reserve(4 * NT);
+  h_incptr[0] = 0;
+  h_rowptr[0] = 0;
+  for (int m = 0; m < nmem; ++m) {
+    MemberHost& h = *M[m];
+    const HostMesh& g = h.mesh;
+    const int no = node_off[m], to = tet_off[m], ao = nnz_off[m];
+    const cathy_soil_t& S = mem[m].soil;
+    const int nzone = S.nzone, nstr = g.nstr;
+    if (g.nzone > nzone) throw std::string("zone id exceeds NZONE");
+    soil_off[m + 1] = soil_off[m] + nzone * nstr;
+    const double* src[8] = {S.permx, S.permy, S.permz, S.elstor, S.poros, S.vgn, S.vgrmc, S.vgpsat};
+    for (int q = 0; q < 8; ++q) tabs[q].insert(tabs[q].end(), src[q], src[q] + (size_t)nzone * nstr);
+    for (int i = 0; i < g.n; ++i) {
+      h_mem[no + i] = m;
+      h_loc[no + i] = i;
+      h_x[no + i] = g.x[i]; h_y[no + i] = g.y[i]; h_z[no + i] = g.z[i];
+      h_diag[no + i] = ao + g.diag[i];
+      h_down[no + i] = g.down[i] >= 0 ? ao + g.down[i] : -1;
+      h_rowptr[no + i + 1] = ao + g.rowptr[i + 1];
+      h_incptr[no + i + 1] = (int32_t)(h_inc.size() + (g.inc_ptr[i + 1] - g.inc_ptr[i]));
+      for (int p = g.inc_ptr[i]; p < g.inc_ptr[i + 1]; ++p) {
+        const int e = g.inc[p] >> 2, k = g.inc[p] & 3;
+        h_inc.push_back((to + e) * 4 + k);
+      }
+    }
+    for (int s = 0; s < g.nnz(); ++s) h_cols[ao + s] = no + g.cols[s];
+    // transposed slots
+    for (int i = 0; i < g.n; ++i)
+      for (int s = g.rowptr[i]; s < g.rowptr[i + 1]; ++s) {
+        const int j = g.cols[s];
+        int t = (int)(std::lower_bound(g.cols.begin() + g.rowptr[j], g.cols.begin() + g.rowptr[j + 1], i) -
+                      g.cols.begin());
+        h_tslot[ao + s] = ao + t;
+      }
+    for (int e = 0; e < g.nt; ++e) {
+      const int32_t* t = &g.tetra[5 * e];
+      h_tet[to + e] = make_int4(no + t[0] - 1, no + t[1] - 1, no + t[2] - 1, no + t[3] - 1);
+      h_tetsoil[to + e] = soil_off[m] + (t[4] - 1) * nstr + (g.tet_layer[e] - 1);
+    }
+    for (int i = 0; i < g.nnod; ++i) {
+      h_arenod[no + i] = g.arenod[i];
+      h_srows.push_back(no + i);
+    }
+    // boundary conditions
+    const cathy_bc_t& B = mem[m].bc;
+    for (int k = 0; k < B.np; ++k) {
+      const int nd0 = B.contp[k] - 1;
+      if (nd0 < 0 || nd0 >= g.n) throw std::string("CONTP out of range");
+      h_sdir[no + nd0] = 1;
+      h_presc[no + nd0] = B.presc[k];
+    }
+    for (int k = 0; k < B.nq; ++k) {
+      const int nd0 = B.contq[k] - 1;
+      if (nd0 < 0 || nd0 >= g.n) throw std::string("CONTQ out of range");
+      h_qneu[no + nd0] += B.q[k];
+      if (B.q[k] > 0.0) h.nnin += B.q[k]; else h.nnout += B.q[k];
+    }
+    // initial conditions (inital.f:97-103)
+    for (int i = 0; i < g.nnod; ++i)
+      for (int k = 0; k <= nstr; ++k) {
+        const int kk = k * g.nnod + i;
+        double v;
+        if (B.indp == 0) v = B.pinit[0];
+        else if (B.indp == 1) v = B.pinit[kk];
+        else if (B.indp == 2) v = g.z[i] - g.z[kk];
+        else v = g.z[i] - g.z[kk] - B.wtposition;
+        h_pinit[no + kk] = v;
+      }
+    h.pmin = S.pmin;
+    h.scf = S.scf;
+    h.pondh_min = (h.parm.isimgr <= 1) ? 1.0e10 : h.parm.pondh_min;
+    h.hspatm = B.hspatm; h.ieto = B.ieto; h.natm = B.natm;
+    h.atm_t.assign(B.atmtim, B.atmtim + B.natm);
+    h.atm_v.assign(B.atminp, B.atminp + (size_t)B.natm * (B.hspatm ? 1 : g.nnod));
+    // INIT1
+    h.deltat = h.parm.deltat;
+    if (h.deltat > h.parm.dtmax) h.deltat = h.parm.dtmax;
+    if (h.deltat <= h.parm.dtmin) { h.deltat = h.parm.dtmin; h.dtgmin = false; }
+    else h.dtgmin = true;
+    h.timep = 0.0;
+    h.time = h.deltat;
+  }
+  nsurf = (int)h_srows.size();
+  // ---- ATMONE on the host (needs initial heads) ----
+  std::vector<int8_t> h_ifatm(N, 0), h_ifatmp(N, 0);
+  std::vector<double> h_atmpot(N, 0.0), h_atmact(N, 0.0), h_atmold(N, 0.0);
+  std::vector<double> h_pnew = h_pinit, h_ptimep = h_pinit;
+  for (int m = 0; m < nmem; ++m) {
+    MemberHost& h = *M[m];
+    const int no = node_off[m], nnod = h.mesh.nnod;
+    atm_setup_member(h, true);
+    if (h.htiatm == 0) {
+      if (h.atmtim[3] <= 0.0)
+        for (int i = 0; i < nnod; ++i) h_atmold[no + i] = h.atminp[3][i] * h.mesh.arenod[i];
+      double t;
+      std::vector<double> v;
+      while (h.time > h.atmtim[3]) {
+        h.atmtim[1] = h.atmtim[2]; h.atmtim[2] = h.atmtim[3];
+        h.atminp[1] = h.atminp[2]; h.atminp[2] = h.atminp[3];
+        if (!atm_read(h, t, v)) { h.htiatm = 1; break; }
+        h.atmtim[3] = t;
+        h.atminp[3] = v;
+      }
+      for (int i = 0; i < nnod; ++i) {
+        double pot;
+        if (h.atmtim[3] > h.atmtim[2]) {
+          double slope = (h.atminp[3][i] - h.atminp[2][i]) / (h.atmtim[3] - h.atmtim[2]);
+          if (h.ieto != 0) slope = 0.0;
+          pot = (h.atminp[2][i] + slope * (h.time - h.atmtim[2])) * h.mesh.arenod[i];
+        } else {
+          pot = h.atminp[3][i] * h.mesh.arenod[i];
+        }
+        h_atmpot[no + i] = pot;
+      }
+    }
+    for (int i = 0; i < nnod; ++i) {
+      const int g0 = no + i;
+      if (h_sdir[g0]) { h_ifatm[g0] = -1; h_ifatmp[g0] = -1; continue; }
+      if (h_qneu[g0] != 0.0) { h_ifatm[g0] = -1; h_ifatmp[g0] = -1; continue; }
+      if (h_pnew[g0] >= h.pondh_min) { h_ifatm[g0] = 2; h_ifatmp[g0] = 2; continue; }
+      if (h_pnew[g0] >= 0.0 && h_atmpot[g0] > 0.0) h_ifatm[g0] = 1;
+      if (h_ptimep[g0] >= 0.0 && h_atmold[g0] > 0.0) h_ifatmp[g0] = 1;
+      if (h_pnew[g0] <= h.pmin && h_atmpot[g0] < 0.0) { h_pnew[g0] = h.pmin; h_ifatm[g0] = 1; }
+      if (h_ptimep[g0] <= h.pmin && h_atmold[g0] < 0.0) { h_ptimep[g0] = h.pmin; h_ifatmp[g0] = 1; }
+    }
+    for (int i = 0; i < nnod; ++i) {
+      const int g0 = no + i;
+      if (h_ifatm[g0] == 0) h_atmact[g0] = h_atmpot[g0] >= 0.0 ? h_atmpot[g0] : (1.0 - h.scf) * h_atmpot[g0];
+      else h_atmact[g0] = 0.0;
+      if (h_ifatmp[g0] == 1 || h_ifatmp[g0] == 2) h_atmold[g0] = 0.0;
+      if (h_ifatmp[g0] == 0) {
+        if (h_atmold[g0] > 0.0) h.aninp += h_atmold[g0]; else h.anoutp += h_atmold[g0];
+      }
+    }
+    h.nninp = h.nnin; h.nnoutp = h.nnout;
+  }
+  // ---- device upload ----
+  d_mem.alloc(N); d_mem.upload(h_mem.data(), N, st);
+  d_loc.alloc(N); d_loc.upload(h_loc.data(), N, st);
+  d_node_off.alloc(nmem + 1); d_node_off.upload(node_off.data(), nmem + 1, st);
+  for (int k = 0; k < ND_NUM; ++k) { d_nodal[k].alloc(N); d_nodal[k].zero(st); }
+  d_nodal[ND_X].upload(h_x.data(), N, st);
+  d_nodal[ND_Y].upload(h_y.data(), N, st);
+  d_nodal[ND_Z].upload(h_z.data(), N, st);
+  d_nodal[ND_ARENOD].upload(h_arenod.data(), N, st);
+  d_nodal[ND_PRESC].upload(h_presc.data(), N, st);
+  d_nodal[ND_QNEU].upload(h_qneu.data(), N, st);
+  d_nodal[ND_PNEW].upload(h_pnew.data(), N, st);
+  d_nodal[ND_PTIMEP].upload(h_ptimep.data(), N, st);
+  d_nodal[ND_ATMPOT].upload(h_atmpot.data(), N, st);
+  d_nodal[ND_ATMACT].upload(h_atmact.data(), N, st);
+  d_nodal[ND_ATMOLD].upload(h_atmold.data(), N, st);
+  d_sdir.alloc(N); d_sdir.upload(h_sdir.data(), N, st);
+  d_dmask.alloc(N); d_dmask.zero(st);
+  d_ifatm.alloc(N); d_ifatm.upload(h_ifatm.data(), N, st);
+  d_ifatmp.alloc(N); d_ifatmp.upload(h_ifatmp.data(), N, st);
+  d_tet.alloc(NT); d_tet.upload(h_tet.data(), NT, st);
+  d_rowptr.alloc(N + 1); d_rowptr.upload(h_rowptr.data(), N + 1, st);
+  d_cols.alloc(NNZ); d_cols.upload(h_cols.data(), NNZ, st);
+  d_diag.alloc(N); d_diag.upload(h_diag.data(), N, st);
+  d_down.alloc(N); d_down.upload(h_down.data(), N, st);
+  d_tslot.alloc(NNZ); d_tslot.upload(h_tslot.data(), NNZ, st);
+  d_inc_ptr.alloc(N + 1); d_inc_ptr.upload(h_incptr.data(), N + 1, st);
+  d_inc.alloc(h_inc.size()); d_inc.upload(h_inc.data(), h_inc.size(), st);
+  d_srows.alloc(nsurf); d_srows.upload(h_srows.data(), nsurf, st);
+  // batched level schedules: level L of every member concatenated
+  {
+    auto batch_levels = [&](bool fwd, std::vector<int32_t>& ptr, DBuf<int32_t>& rows) {
+      int maxl = 0;
+      for (int m = 0; m < nmem; ++m) {
+        const auto& lp = fwd ? M[m]->mesh.lev_f_ptr : M[m]->mesh.lev_b_ptr;
+        maxl = std::max(maxl, (int)lp.size() - 1);
+      }
+      std::vector<int32_t> all;
+      all.reserve(N);
+      ptr.assign(maxl + 1, 0);
+      for (int l = 0; l < maxl; ++l) {
+        for (int m = 0; m < nmem; ++m) {
+          const auto& lp = fwd ? M[m]->mesh.lev_f_ptr : M[m]->mesh.lev_b_ptr;
+          const auto& lr = fwd ? M[m]->mesh.lev_f_rows : M[m]->mesh.lev_b_rows;
+          if (l + 1 < (int)lp.size())
+            for (int q = lp[l]; q < lp[l + 1]; ++q) all.push_back(node_off[m] + lr[q]);
+        }
+        ptr[l + 1] = (int32_t)all.size();
+      }
+      rows.alloc(all.size());
+      rows.upload(all.data(), all.size(), st);
+    };
+    batch_levels(true, lev_f_ptr, d_lev_f);
+    batch_levels(false, lev_b_ptr, d_lev_b);
+  }
+  // soil tables
+  DBuf<double> d_tab[8];
+  for (int q = 0; q < 8; ++q) { d_tab[q].alloc(tabs[q].size()); d_tab[q].upload(tabs[q].data(), tabs[q].size(), st); }
+  DBuf<int32_t> d_tetsoil;
+  d_tetsoil.alloc(NT); d_tetsoil.upload(h_tetsoil.data(), NT, st);
+  // nodal pointers
+  auto P = [&](int k) { return d_nodal[k].p; };
+  nd.mem = d_mem.p; nd.loc = d_loc.p;
+  nd.volnod = P(ND_VOLNOD); nd.pnodi = P(ND_PNODI); nd.snodi = P(ND_SNODI);
+  nd.vgn = P(ND_VGN); nd.vgm = P(ND_VGM); nd.vgrmc = P(ND_VGRMC); nd.vgpsat = P(ND_VGPSAT);
+  nd.vgn1 = P(ND_VGN1); nd.vgnr = P(ND_VGNR); nd.vgpsn = P(ND_VGPSN); nd.vgmr = P(ND_VGMR);
+  nd.vgm52 = P(ND_VGM52); nd.vgmm1 = P(ND_VGMM1); nd.vgpnot = P(ND_VGPNOT);
+  nd.pnew = P(ND_PNEW); nd.pold = P(ND_POLD); nd.ptnew = P(ND_PTNEW); nd.ptold = P(ND_PTOLD);
+  nd.ptimep = P(ND_PTIMEP); nd.pdiff = P(ND_PDIFF); nd.swnew = P(ND_SWNEW);
+  nd.swtimep = P(ND_SWTIMEP); nd.rhs = P(ND_RHS); nd.xt5 = P(ND_XT5); nd.qneu = P(ND_QNEU);
+  nd.presc = P(ND_PRESC); nd.qpnew = P(ND_QPNEW); nd.qpold = P(ND_QPOLD); nd.sw = P(ND_SW);
+  nd.et1 = P(ND_ET1); nd.et2 = P(ND_ET2); nd.ckrw = P(ND_CKRW); nd.etai = P(ND_ETAI);
+  nd.dckrw = P(ND_DCKRW); nd.detai = P(ND_DETAI); nd.arenod = P(ND_ARENOD);
+  nd.atmpot = P(ND_ATMPOT); nd.atmact = P(ND_ATMACT); nd.atmold = P(ND_ATMOLD);
+  nd.atm_a = P(ND_ATMA); nd.atm_b = P(ND_ATMB);
+  nd.sdir = d_sdir.p; nd.dmask = d_dmask.p; nd.ifatm = d_ifatm.p; nd.ifatmp = d_ifatmp.p;
+  // TPNODI/CHPARM then geometry
+  k_tpnodi<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, d_inc_ptr.p, d_inc.p, d_tetsoil.p,
+      d_tab[4].p, d_tab[3].p, d_tab[5].p, d_tab[6].p, d_tab[7].p, nd);
+  check_launch();
+  if (precision == 0) {
+    d_rec64.alloc(NT);
+    k_geom<double><<<cdiv(NT, 128), 128, 0, st>>>((int)NT, d_tet.p, P(ND_X), P(ND_Y), P(ND_Z),
+        d_tetsoil.p, d_tab[0].p, d_tab[1].p, d_tab[2].p, P(ND_PNODI), d_rec64.p, P(ND_VOLNOD), nullptr);
+  } else {
+    d_rec32.alloc(NT);
+    k_geom<float><<<cdiv(NT, 128), 128, 0, st>>>((int)NT, d_tet.p, P(ND_X), P(ND_Y), P(ND_Z),
+        d_tetsoil.p, d_tab[0].p, d_tab[1].p, d_tab[2].p, P(ND_PNODI), d_rec32.p, P(ND_VOLNOD), nullptr);
+  }
+  check_launch();
+  // matrix and solver workspace
+  if (precision == 0) { d_vals64.alloc(NNZ); d_vals64.zero(st); }
+  else { d_vals32.alloc(NNZ); d_vals32.zero(st); d_vals64.alloc(0); }
+  const int nw = 14;
+  if (precision == 0 || iopt == 2) for (int k = 0; k < nw; ++k) { w64[k].alloc(N); w64[k].zero(st); }
+  else for (int k = 0; k < 4; ++k) { w64[k].alloc(N); w64[k].zero(st); }
+  if (precision == 1) for (int k = 0; k < 8; ++k) { w32[k].alloc(N); w32[k].zero(st); }
+  if (precond == 0 || iopt == 2) {
+    if (precision == 0 || iopt == 2) { d_F64.alloc(NNZ); if (iopt == 2) d_G64.alloc(NNZ); }
+    else d_F32.alloc(NNZ);
+  }
+  if (precond == 2) {
+    if (precision == 0) { d_linv64.alloc(N); d_lc64.alloc(N); }
+    else { d_linv32.alloc(N); d_lc32.alloc(N); }
+  }
+  d_act.alloc(nmem); d_active.alloc(nmem); d_switch.alloc(nmem); d_mask2.alloc(nmem);
+  d_outer.alloc(nmem);
+  d_ms.alloc(nmem);
+  d_red.alloc((size_t)nmem * RD_NUM); d_redmax.alloc((size_t)nmem * 2);
+  d_sc.alloc((size_t)nmem * SC_N); d_sc.zero(st);
+  d_ikmax.alloc(nmem); d_ikval.alloc((size_t)nmem * 2); d_niter.alloc(nmem); d_nact.alloc(1);
+  make_blockmap(bm1, kThreads);
+  make_blockmap(bm16, kRowsPerBlock16);
+  h_ms.resize(nmem);
+  h_act.assign(nmem, 0);
+  // initial storage (STORCAL at PTIMEP = PNEW)
+  {
+    std::vector<uint8_t> ones(nmem, 1);
+    d_mask2.upload(ones.data(), nmem, st);
+    d_red.zero(st);
+    k_store1<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_mask2.p, nd, d_red.p);
+    check_launch();
+    std::vector<double> red((size_t)nmem * RD_NUM);
+    d_red.download(red.data(), red.size(), st);
+    CG_TRY(cudaStreamSynchronize(st));
+    for (int m = 0; m < nmem; ++m) {
+      M[m]->store1 = red[(size_t)m * RD_NUM + RD_STORE1];
+      M[m]->store2 = M[m]->store1;
+      M[m]->pend = ACT_START;
+    }
+  }
+  CG_TRY(cudaStreamSynchronize(st));
+}
+
+void Engine::push_scalars() {
+  bool nodal_dirty = false;
+  for (int m = 0; m < nmem; ++m) {
+    MemberHost& h = *M[m];
+    MemberScal& S = h_ms[m];
+    S.deltat = h.deltat; S.time = h.time; S.tetaf = h.parm.tetaf; S.scf = h.scf;
+    S.pmin = h.pmin; S.omega = h.parm.omega; S.tolswi = h.parm.tolswi;
+    S.atm_ta = h.atm_ta; S.atm_tb = h.atm_tb; S.atm_va = h.atm_va; S.atm_vb = h.atm_vb;
+    S.atm_mode = h.atm_mode; S.hspatm = h.hspatm; S.ieto = h.ieto; S.nlrelx = h.parm.nlrelx;
+    S.nnod = h.mesh.nnod; S.nstr = h.mesh.nstr; S.iopt = iopt; S.pad = 0;
+    if (h.atm_nodal_dirty) nodal_dirty = true;
+  }
+  d_ms.upload(h_ms.data(), nmem, st);
+  if (nodal_dirty) {
+    for (int m = 0; m < nmem; ++m) {
+      MemberHost& h = *M[m];
+      if (!h.atm_nodal_dirty) continue;
+      const int no = node_off[m], nnod = h.mesh.nnod;
+      if ((int)h.atm_a_nodal.size() == nnod)
+        CG_TRY(cudaMemcpyAsync(nd.atm_a + no, h.atm_a_nodal.data(), sizeof(double) * nnod, cudaMemcpyHostToDevice, st));
+      if ((int)h.atm_b_nodal.size() == nnod)
+        CG_TRY(cudaMemcpyAsync(nd.atm_b + no, h.atm_b_nodal.data(), sizeof(double) * nnod, cudaMemcpyHostToDevice, st));
+      h.atm_nodal_dirty = false;
+    }
+    CG_TRY(cudaStreamSynchronize(st));
+  }
+}
+
+// ---- assembly ----
+template <class MT>
+void Engine::assemble() {
+  const TetRec<MT>* rec;
+  MT* vals;
+  if constexpr (sizeof(MT) == 8) { rec = (const TetRec<MT>*)d_rec64.p; vals = (MT*)d_vals64.p; }
+  else { rec = (const TetRec<MT>*)d_rec32.p; vals = (MT*)d_vals32.p; }
+  if (iopt == 1)
+    k_assemble_picard<MT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+        d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, rec, nd, vals, lm_d, lm_o);
+  else
+    k_assemble_newton<MT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+        d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, rec, nd, vals, lm_d, lm_o);
+  check_launch();
+  count();
+}
+
+// Apply z = M^-1 r for the selected preconditioner (setup done already).
+// w/acc: optional dot w.z into sc[SC_QZ].
+template <class MT, class VT, class FT>
+static void precond_apply(Engine& E, int pc, const VT* r, VT* z, VT* tmp,
+                          const VT* w, const FT* F, const VT* dinv,
+                          const VT* linv, const VT* lc) {
+  cudaStream_t st = E.st;
+  if (pc == 1) {
+    k_copy_cast<VT, VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p,
+        E.d_active.p, r, z, nullptr, 0);
+    k_scale_vec<VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p,
+        E.d_active.p, z, dinv);
+    E.count(2);
+    if (w) {
+      k_dot<VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p, E.d_active.p,
+          w, z, nullptr, E.d_sc.p, SC_N, SC_QZ);
+      E.count();
+    }
+  } else if (pc == 2) {
+    k_line_apply<VT><<<cdiv(E.nsurf, 128), 128, 0, st>>>(E.nsurf, E.d_srows.p, E.d_mem.p,
+        E.d_active.p, E.d_ms.p, linv, lc, r, z, w, E.d_sc.p, SC_N, SC_QZ);
+    E.count();
+  } else {
+    for (size_t l = 0; l + 1 < E.lev_f_ptr.size(); ++l) {
+      const int nr = E.lev_f_ptr[l + 1] - E.lev_f_ptr[l];
+      if (!nr) continue;
+      k_lsolve_level<FT, VT><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
+          E.d_lev_f.p + E.lev_f_ptr[l], E.d_rowptr.p, E.d_cols.p, E.d_diag.p, F, E.d_active.p,
+          E.d_mem.p, r, tmp);
+      E.count();
+    }
+    for (size_t l = 0; l + 1 < E.lev_b_ptr.size(); ++l) {
+      const int nr = E.lev_b_ptr[l + 1] - E.lev_b_ptr[l];
+      if (!nr) continue;
+      k_ltsolve_level<FT, VT><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
+          E.d_lev_b.p + E.lev_b_ptr[l], E.d_rowptr.p, E.d_cols.p, E.d_diag.p, E.d_tslot.p, F,
+          E.d_active.p, E.d_mem.p, tmp, z);
+      E.count();
+    }
+    if (w) {
+      k_dot<VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p, E.d_active.p,
+          w, z, nullptr, E.d_sc.p, SC_N, SC_QZ);
+      E.count();
+    }
+  }
+}
+
+template <class MT, class VT, class FT>
+static void precond_setup(Engine& E, int pc, const MT* vals, FT* F, VT* dinv,
+                          VT* linv, VT* lc) {
+  cudaStream_t st = E.st;
+  if (pc == 1) {
+    k_jacobi_setup<MT, VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p,
+        E.d_active.p, E.d_diag.p, vals, E.d_dmask.p, dinv);
+    E.count();
+  } else if (pc == 2) {
+    k_line_setup<MT, VT><<<cdiv(E.nsurf, 128), 128, 0, st>>>(E.nsurf, E.d_srows.p, E.d_mem.p,
+        E.d_active.p, E.d_ms.p, E.d_diag.p, E.d_down.p, vals, E.d_dmask.p, linv, lc);
+    E.count();
+  } else {
+    for (size_t l = 0; l + 1 < E.lev_f_ptr.size(); ++l) {
+      const int nr = E.lev_f_ptr[l + 1] - E.lev_f_ptr[l];
+      if (!nr) continue;
+      k_ic0_level<MT, FT><<<cdiv(nr, 128), 128, 0, st>>>(nr, E.d_lev_f.p + E.lev_f_ptr[l],
+          E.d_rowptr.p, E.d_cols.p, E.d_diag.p, vals, E.d_dmask.p, E.d_active.p, E.d_mem.p, F);
+      E.count();
+    }
+  }
+  E.check_launch();
+}
+
+// Batched PCG with the reference's GRADDP recurrences (x0 = M^-1 b).
+// Solves A x = b for members with d_active set; b = w[0] (VT), x = w[1].
+// ref_mode: b is the FP64 RHS (nd.rhs) and x is nd.pdiff.
+template <class MT, class VT>
+void Engine::solve_pcg(int itmax, double tol, bool ref_mode) {
+  const MT* vals;
+  if constexpr (sizeof(MT) == 8) vals = (const MT*)d_vals64.p; else vals = (const MT*)d_vals32.p;
+  VT *b, *x, *r, *p, *q, *z, *tmp, *dinv, *linv = nullptr, *lc = nullptr;
+  using FT = VT;
+  FT* F;
+  if constexpr (sizeof(VT) == 8) {
+    b = ref_mode ? nd.rhs : w64[0].p; x = ref_mode ? nd.pdiff : w64[1].p;
+    r = w64[2].p; p = w64[3].p; q = w64[4].p; z = w64[5].p; tmp = w64[6].p; dinv = w64[7].p;
+    F = d_F64.p; linv = d_linv64.p; lc = d_lc64.p;
+  } else {
+    b = w32[0].p; x = w32[1].p; r = w32[2].p; p = w32[3].p; q = w32[4].p; z = w32[5].p;
+    tmp = w32[6].p; dinv = w32[7].p; F = d_F32.p; linv = d_linv32.p; lc = d_lc32.p;
+  }
+  const int pc = precond;
+  precond_setup<MT, VT, FT>(*this, pc, vals, F, dinv, linv, lc);
+  // x0 = M^-1 b, xlung = |b_masked|^2 (b is zero at Dirichlet rows)
+  CG_TRY(cudaMemsetAsync(d_sc.p, 0, sizeof(double) * nmem * SC_N, st));
+  k_dot<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, b, b,
+                                            d_dmask.p, d_sc.p, SC_N, SC_XL);
+  count();
+  precond_apply<MT, VT, FT>(*this, pc, b, x, tmp, nullptr, F, dinv, linv, lc);
+  // r = b - A x ; p = M^-1 r
+  k_resid<MT, VT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_active.p,
+      d_rowptr.p, d_cols.p, vals, d_dmask.p, x, b, r, nullptr, 0);
+  count();
+  precond_apply<MT, VT, FT>(*this, pc, r, p, tmp, nullptr, F, dinv, linv, lc);
+  std::vector<int32_t> ones(nmem, 1);
+  d_niter.upload(ones.data(), nmem, st);
+  check_launch();
+  for (int it = 0; it < itmax + 2; ++it) {
+    // q = A p, pq = p.q, pr = p.r
+    k_spmv<MT, VT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_active.p,
+        d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N);
+    count();
+    k_pcg_update_rx<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p,
+        d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
+    count();
+    precond_apply<MT, VT, FT>(*this, pc, r, z, tmp, q, F, dinv, linv, lc);
+    k_pcg_update_p<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p,
+        d_sc.p, p, z);
+    count();
+    CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
+    k_krylov_decide<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_active.p, d_sc.p, d_niter.p, itmax,
+        tol, 0, d_nact.p);
+    count();
+    check_launch();
+    int32_t nact = 0;
+    d_nact.download(&nact, 1, st);
+    CG_TRY(cudaStreamSynchronize(st));
+    if (nact == 0) break;
+  }
+}
+
+
+// ---- mixed precision: FP32 inner PCG inside FP64 iterative refinement ----
+// per member: rr = |r|^2 (into red2[m*2]), bb = |b|^2 (red2[m*2+1])
+__global__ void k_ref_decide(int nmem, uint8_t* outer, const double* red2,
+                             double* scale, double tol, int round, int maxround,
+                             int32_t* nact) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  int a = 0;
+  if (m < nmem && outer[m]) {
+    const double rr = red2[2 * m], bb = red2[2 * m + 1];
+    const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+    if (rel > tol && rr > 0.0 && round < maxround) {
+      scale[m] = 1.0 / sqrt(rr);
+      a = 1;
+    } else {
+      outer[m] = 0;
+    }
+  }
+  if (m < nmem) atomicAdd(nact, a);
+}
+__global__ void k_inv_scale(int nmem, const double* scale, double* inv) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < nmem) inv[m] = 1.0 / scale[m];
+}
+
+template <class MT>
+void Engine::solve_mixed(int itmax, double tol) {
+  const MT* vals = (const MT*)d_vals32.p;
+  double* x = nd.pdiff;
+  double* r = w64[0].p;
+  DBuf<double>& red2 = w64[1];  // per member (rr, bb) in the first 2*nmem entries
+  DBuf<double>& scale = w64[2];
+  DBuf<double>& inv = w64[3];
+  // outer mask = members iterating
+  DBuf<uint8_t>& outer = d_outer;
+  CG_TRY(cudaMemcpyAsync(outer.p, d_active.p, nmem, cudaMemcpyDeviceToDevice, st));
+  CG_TRY(cudaMemsetAsync(x, 0, sizeof(double) * N, st));
+  // r = b ; bb
+  CG_TRY(cudaMemsetAsync(red2.p, 0, sizeof(double) * 2 * nmem, st));
+  k_copy_cast<double, double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p,
+      outer.p, nd.rhs, r, nullptr, 0);
+  k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, nd.rhs,
+      nd.rhs, d_dmask.p, red2.p, 2, 1);
+  k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, r, r,
+      d_dmask.p, red2.p, 2, 0);
+  count(3);
+  std::vector<int32_t> tot(nmem, 0), its(nmem);
+  const int maxround = 4;
+  for (int round = 0; round <= maxround; ++round) {
+    CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
+    k_ref_decide<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, outer.p, red2.p, scale.p, tol, round,
+                                                  maxround, d_nact.p);
+    count();
+    int32_t nact = 0;
+    d_nact.download(&nact, 1, st);
+    CG_TRY(cudaStreamSynchronize(st));
+    if (!nact) break;
+    // b32 = r * scale ; inner solve
+    k_copy_cast<double, float><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p,
+        outer.p, r, w32[0].p, scale.p, 1);
+    CG_TRY(cudaMemcpyAsync(d_active.p, outer.p, nmem, cudaMemcpyDeviceToDevice, st));
+    count();
+    solve_pcg<MT, float>(opts.inner_maxit, opts.inner_tol, false);
+    d_niter.download(its.data(), nmem, st);
+    // x += e / scale ; r = b - A x
+    k_inv_scale<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, scale.p, inv.p);
+    k_axpy_ref<float><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, x,
+        w32[1].p, inv.p, 1);
+    CG_TRY(cudaMemsetAsync(red2.p, 0, sizeof(double) * 2 * nmem, st));
+    k_resid<MT, double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, outer.p,
+        d_rowptr.p, d_cols.p, vals, d_dmask.p, x, nd.rhs, r, red2.p, 2);
+    k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, nd.rhs,
+        nd.rhs, d_dmask.p, red2.p, 2, 1);
+    count(4);
+    check_launch();
+    CG_TRY(cudaStreamSynchronize(st));
+    std::vector<uint8_t> oa(nmem);
+    outer.download(oa.data(), nmem, st);
+    CG_TRY(cudaStreamSynchronize(st));
+    for (int m = 0; m < nmem; ++m) if (oa[m]) tot[m] += its[m];
+  }
+  d_niter.upload(tot.data(), nmem, st);
+  // error estimate for the records: relative FP64 residual
+  std::vector<double> rr(2 * nmem);
+  red2.download(rr.data(), 2 * nmem, st);
+  CG_TRY(cudaStreamSynchronize(st));
+  std::vector<double> scv((size_t)nmem * SC_N, 0.0);
+  for (int m = 0; m < nmem; ++m) scv[(size_t)m * SC_N + SC_ERR] = rr[2 * m + 1] > 0 ? std::sqrt(rr[2 * m] / rr[2 * m + 1]) : 0.0;
+  d_sc.upload(scv.data(), scv.size(), st);
+}
+
+// ---- BiCGSTAB (Newton), FP64, GCSTAS (isolv 0) / GCSTAD (isolv -5) ----
+void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
+  const double* vals = d_vals64.p;
+  double *x = nd.pdiff, *b = nd.rhs;
+  double *r = w64[2].p, *rt = w64[3].p, *p = w64[4].p, *v = w64[5].p, *s = w64[6].p,
+         *t = w64[7].p, *pjm = w64[8].p, *vjm = w64[9].p, *scr1 = w64[10].p,
+         *scr2 = w64[11].p, *dd = w64[12].p, *tmp = w64[13].p;
+  const bool jac = (isolv == -5);
+  auto E1 = [&](auto kern, auto... args) {
+    kern<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, args...);
+    count();
+  };
+  auto lsolve = [&](const double* in, double* out) {
+    for (size_t l = 0; l + 1 < lev_f_ptr.size(); ++l) {
+      const int nr = lev_f_ptr[l + 1] - lev_f_ptr[l];
+      if (!nr) continue;
+      k_lsolve_level<double, double><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
+          d_lev_f.p + lev_f_ptr[l], d_rowptr.p, d_cols.p, d_diag.p, d_G64.p, d_active.p, d_mem.p, in, out);
+      count();
+    }
+  };
+  auto usolve = [&](const double* in, double* out) {
+    for (size_t l = 0; l + 1 < lev_b_ptr.size(); ++l) {
+      const int nr = lev_b_ptr[l + 1] - lev_b_ptr[l];
+      if (!nr) continue;
+      k_usolve_level<double, double><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
+          d_lev_b.p + lev_b_ptr[l], d_rowptr.p, d_cols.p, d_diag.p, d_G64.p, d_active.p, d_mem.p, in, out);
+      count();
+    }
+  };
+  auto spmv = [&](const double* in, double* out) {
+    k_spmv<double, double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
+        d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out, nullptr, nullptr, 0);
+    count();
+  };
+  auto applyB = [&](const double* in, double* out) {
+    if (jac) {
+      spmv(in, out);
+      E1(k_scale_vec<double>, out, (const double*)dd);
+    } else {
+      usolve(in, scr1);
+      spmv(scr1, scr2);
+      lsolve(scr2, out);
+    }
+  };
+  // scalars init: rojm1 = alfjm1 = etaj = 1
+  std::vector<double> scv((size_t)nmem * SC_N, 0.0);
+  for (int m = 0; m < nmem; ++m) {
+    scv[(size_t)m * SC_N + SC_ROJM1] = 1.0;
+    scv[(size_t)m * SC_N + SC_ALFJM1] = 1.0;
+    scv[(size_t)m * SC_N + SC_ETAJ] = 1.0;
+  }
+  d_sc.upload(scv.data(), scv.size(), st);
+  k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, b, b,
+      d_dmask.p, d_sc.p, SC_N, SC_XL);
+  count();
+  if (jac) {
+    k_jacobi_setup<double, double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p,
+        d_active.p, d_diag.p, vals, d_dmask.p, dd);
+    count();
+    E1(k_copy_cast<double, double>, (const double*)b, x, (const double*)nullptr, 0);
+    E1(k_scale_vec<double>, x, (const double*)dd);
+    spmv(x, scr1);
+    E1(k_sub_vec<double>, scr1, (const double*)b, (const double*)scr1);
+    E1(k_copy_cast<double, double>, (const double*)scr1, r, (const double*)nullptr, 0);
+    E1(k_scale_vec<double>, r, (const double*)dd);
+  } else {
+    for (size_t l = 0; l + 1 < lev_f_ptr.size(); ++l) {
+      const int nr = lev_f_ptr[l + 1] - lev_f_ptr[l];
+      if (!nr) continue;
+      k_ilu0_level<double, double><<<cdiv(nr, 128), 128, 0, st>>>(nr, d_lev_f.p + lev_f_ptr[l],
+          d_rowptr.p, d_cols.p, d_diag.p, vals, d_dmask.p, d_active.p, d_mem.p, d_F64.p);
+      count();
+    }
+    k_ilu0_split<double><<<cdiv(N, 256), 256, 0, st>>>(N, d_rowptr.p, d_cols.p, d_diag.p,
+        d_active.p, d_mem.p, d_F64.p, d_G64.p);
+    count();
+    lsolve(b, tmp);
+    usolve(tmp, x);              // x0 = (LU)^-1 b   (PROD1)
+    spmv(x, scr1);
+    E1(k_sub_vec<double>, scr1, (const double*)b, (const double*)scr1);
+    lsolve(scr1, r);             // r0 = L^-1 (b - A x0)
+    k_umul<double, double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
+        d_active.p, d_rowptr.p, d_cols.p, d_diag.p, d_G64.p, x, scr1);
+    count();
+    E1(k_copy_cast<double, double>, (const double*)scr1, x, (const double*)nullptr, 0);  // y0 = U x0
+  }
+  E1(k_copy_cast<double, double>, (const double*)r, rt, (const double*)nullptr, 0);
+  E1(k_set_vec<double>, pjm, (const double*)nullptr, 0.0);
+  E1(k_set_vec<double>, vjm, (const double*)nullptr, 0.0);
+  std::vector<int32_t> ones(nmem, 1);
+  d_niter.upload(ones.data(), nmem, st);
+  check_launch();
+  for (int it = 0; it < itmax + 3; ++it) {
+    k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, rt, r,
+        nullptr, d_sc.p, SC_N, SC_ROJ);
+    count();
+    E1(k_bicg_p<double>, (const double*)d_sc.p, p, (const double*)r, (const double*)pjm, (const double*)vjm);
+    applyB(p, v);
+    k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, rt, v,
+        nullptr, d_sc.p, SC_N, SC_SIG);
+    count();
+    E1(k_bicg_s<double>, (const double*)d_sc.p, s, (const double*)r, (const double*)v);
+    applyB(s, t);
+    E1(k_bicg_st<double>, d_sc.p, (const double*)s, (const double*)t);
+    E1(k_bicg_xr<double>, d_sc.p, x, r, (const double*)p, (const double*)s, (const double*)t,
+       (const uint8_t*)d_dmask.p);
+    CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
+    k_krylov_decide<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_active.p, d_sc.p, d_niter.p, itmax,
+        tol, 1, d_nact.p);
+    count();
+    E1(k_copy_cast<double, double>, (const double*)p, pjm, (const double*)nullptr, 0);
+    E1(k_copy_cast<double, double>, (const double*)v, vjm, (const double*)nullptr, 0);
+    check_launch();
+    int32_t nact = 0;
+    d_nact.download(&nact, 1, st);
+    CG_TRY(cudaStreamSynchronize(st));
+    if (nact == 0) break;
+  }
+  if (!jac) {
+    // x = U^-1 y for every member that iterated
+    k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
+    E1(k_copy_cast<double, double>, (const double*)x, tmp, (const double*)nullptr, 0);
+    usolve(tmp, x);
+  }
+}
+
+__global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
+                               const double* redmax, const MemberScal* ms,
+                               int l2norm, uint8_t* out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  const double pinf = redmax[2 * m], pl2 = sqrt(red[(size_t)m * RD_NUM + RD_PL2]);
+  out[m] = (act[m] & ACT_ITER) && ((l2norm == 0 && pinf <= ms[m].tolswi) ||
+                                   (l2norm != 0 && pl2 <= ms[m].tolswi));
+}
+
+// One nonlinear iteration for every member flagged ACT_ITER.
+void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
+  (void)itm;
+  const bool mixed = (precision == 1 && iopt == 1);
+  if (mixed)
+    k_vg<float><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 0);
+  else
+    k_vg<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd,
+                                                iopt == 2);
+  count();
+  check_launch();
+  if (mixed) assemble<float>(); else assemble<double>();
+  k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
+  count();
+  const cathy_parm_t& P0 = M[0]->parm;
+  if (iopt == 1) {
+    if (!mixed) solve_pcg<double, double>(P0.itmxcg, P0.tolcg, true);
+    else solve_mixed<float>(P0.itmxcg, P0.tolcg);
+  } else {
+    solve_bicgstab(P0.isolv, P0.itmxcg, P0.tolcg);
+  }
+  k_update_shl<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd);
+  count();
+  CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
+  CG_TRY(cudaMemsetAsync(d_redmax.p, 0, sizeof(double) * nmem * 2, st));
+  CG_TRY(cudaMemsetAsync(d_ikmax.p, 0, sizeof(int32_t) * nmem, st));
+  if (mixed)
+    k_masbal_norms<float><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+        d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, d_red.p, d_redmax.p, 0);
+  else
+    k_masbal_norms<double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+        d_ms.p, d_rowptr.p, d_cols.p, d_vals64.p, nd, d_red.p, d_redmax.p, iopt == 2);
+  k_ikmax<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd, d_redmax.p,
+                                         d_ikmax.p);
+  k_gather_ik<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_node_off.p, d_ikmax.p, nd, d_ikval.p);
+  k_switch_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_red.p, d_redmax.p, d_ms.p,
+                                                  P0.l2norm, d_switch.p);
+  k_switch<<<cdiv(nsurf, kThreads), kThreads, 0, st>>>(nsurf, d_srows.p, d_act.p, d_switch.p, d_ms.p, nd);
+  count(5);
+  check_launch();
+}
+
+// ---- macro-iteration: device step actions, one nonlinear iteration, host
+// decisions (flow3d.f:212-294, TIMUPD, BKSTEP) ----
+int Engine::macro_iteration() {
+  int niter_members = 0;
+  std::vector<int> itm;
+  for (int m = 0; m < nmem; ++m) {
+    MemberHost& h = *M[m];
+    uint8_t a = h.pend;
+    if (h.status == 0 && !h.paused) {
+      if (a & ACT_START) { h.iterating = true; h.iter = 1; h.nitert = 0; }
+      if (h.iterating) { a |= ACT_ITER; niter_members++; itm.push_back(m); }
+    } else {
+      a &= (ACT_COMMIT);  // finished members still commit their last step
+    }
+    h_act[m] = a;
+    h.pend = 0;
+  }
+  push_scalars();
+  d_act.upload(h_act.data(), nmem, st);
+  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 0);
+  k_start_surface<<<cdiv(nsurf, kThreads), kThreads, 0, st>>>(nsurf, d_srows.p, d_act.p, d_ms.p, nd);
+  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 1);
+  count(3);
+  check_launch();
+  if (niter_members == 0) {
+    CG_TRY(cudaStreamSynchronize(st));
+    return 0;
+  }
+  picard_or_newton_iteration(itm);
+  // results
+  std::vector<double> red((size_t)nmem * RD_NUM), redmax(2 * nmem), ikv(2 * nmem), scv((size_t)nmem * SC_N);
+  std::vector<int32_t> ikmax(nmem), nit(nmem);
+  d_red.download(red.data(), red.size(), st);
+  d_redmax.download(redmax.data(), redmax.size(), st);
+  d_ikval.download(ikv.data(), ikv.size(), st);
+  d_ikmax.download(ikmax.data(), nmem, st);
+  d_niter.download(nit.data(), nmem, st);
+  d_sc.download(scv.data(), scv.size(), st);
+  CG_TRY(cudaStreamSynchronize(st));
+  nl_iters += niter_members;
+  std::vector<uint8_t> conv_mask(nmem, 0);
+  bool any_conv = false;
+  for (int m : itm) {
+    MemberHost& h = *M[m];
+    const cathy_parm_t& P = h.parm;
+    const double* R = &red[(size_t)m * RD_NUM];
+    const int niter = nit[m];
+    h.itlin += niter; h.nitert += niter;
+    lin_iters += niter;
+    const bool lsfail = niter >= P.itmxcg;
+    const double pl2 = std::sqrt(R[RD_PL2]), fl2 = std::sqrt(R[RD_FL2]);
+    const double pinf = redmax[2 * m], finf = redmax[2 * m + 1];
+    cathy_iter_rec_t rec;
+    rec.nstep = h.nstep; rec.iter = h.iter; rec.niter = niter; rec.ikmax = ikmax[m] + 1;
+    rec.deltat = h.deltat; rec.time = h.time; rec.pl2 = pl2; rec.pinf = pinf;
+    rec.pnew_ik = ikv[2 * m]; rec.pold_ik = ikv[2 * m + 1]; rec.fl2 = fl2; rec.finf = finf;
+    rec.lin_err = scv[(size_t)m * SC_N + SC_ERR]; rec.lin_res = -1.0;
+    h.iter_recs.push_back(rec);
+    // mass balance of this iteration (kept for the accepted one)
+    std::memcpy(h.red_last, R, sizeof(double) * RD_NUM);
+    const bool itagen = h.iter < P.ituns;
+    const bool errgmx = (pl2 >= P.ernlmx || pinf >= P.ernlmx || fl2 >= P.ernlmx || finf >= P.ernlmx);
+    const bool normcv = (P.l2norm == 0) ? (pinf <= P.toluns) : (pl2 <= P.toluns);
+    if (!lsfail && !errgmx && !normcv && itagen) {
+      h.pend |= ACT_NEXT;
+      h.iter++;
+      continue;
+    }
+    h.iterating = false;
+    if (!lsfail && !errgmx && normcv) {
+      conv_mask[m] = 1;
+      any_conv = true;
+    } else if (h.dtgmin) {
+      // BKSTEP (bkstep.f:54-80)
+      h.time = h.timep;
+      h.deltat = h.deltat * P.dtredm - P.dtreds;
+      if (h.deltat <= P.dtmin) { h.deltat = P.dtmin; h.dtgmin = false; }
+      else h.dtgmin = true;
+      h.time = h.time + h.deltat;
+      h.kbackt++; h.kback++;
+      h.iter = 1; h.nitert = 0;
+      if (h.time > h.atmtim[2]) atm_advance(h);
+      else atm_back(h);
+      h.pend |= ACT_BACKSTEP | ACT_START;
+    } else {
+      h.status = 2;  // no back-stepping possible
+    }
+  }
+  if (any_conv) {
+    d_mask2.upload(conv_mask.data(), nmem, st);
+    CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
+    k_store1<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_mask2.p, nd, d_red.p);
+    count();
+    check_launch();
+    d_red.download(red.data(), red.size(), st);
+    CG_TRY(cudaStreamSynchronize(st));
+    for (int m = 0; m < nmem; ++m) {
+      if (!conv_mask[m]) continue;
+      MemberHost& h = *M[m];
+      const cathy_parm_t& P = h.parm;
+      const double* R = h.red_last;
+      const double deltam = (h.deltat < 1.0e15) ? 0.5 * h.deltat : 1.0;
+      const double dstore = R[RD_DSTORE];
+      const double vadin = (R[RD_ADIN] + h.adinp) * deltam, vadout = (R[RD_ADOUT] + h.adoutp) * deltam;
+      const double vndin = (R[RD_NDIN] + h.ndinp) * deltam, vndout = (R[RD_NDOUT] + h.ndoutp) * deltam;
+      const double vanin = (R[RD_ANIN] + h.aninp) * deltam, vanout = (R[RD_ANOUT] + h.anoutp) * deltam;
+      const double vnnin = (h.nnin + h.nninp) * deltam, vnnout = (h.nnout + h.nnoutp) * deltam;
+      const double vin = vadin + vndin + vanin + vnnin;
+      const double vout = vadout + vndout + vanout + vnnout;
+      const double erras = vin + vout - dstore;
+      double errel;
+      if (h.deltat >= 1.0e15) errel = vin != 0.0 ? 100.0 * erras / vin : 0.0;
+      else errel = (vin + vout) != 0.0 ? 100.0 * erras / (vin + vout) : 0.0;
+      h.store1 = red[(size_t)m * RD_NUM + RD_STORE1];
+      h.store2 += dstore;
+      h.vtot += vin + vout;
+      h.cvin += vin; h.cvout += vout; h.cdstor += dstore; h.cerras += erras;
+      h.caeras += std::fabs(erras);
+      h.dstore = dstore; h.vin = vin; h.vout = vout; h.erras = erras; h.errel = errel;
+      cathy_step_rec_t sr;
+      sr.nstep = h.nstep; sr.iter = h.iter; sr.nitert = h.nitert; sr.nback = h.kbackt;
+      sr.deltat = h.deltat; sr.time = h.time; sr.store1 = h.store1; sr.store2 = h.store2;
+      sr.dstore = dstore; sr.cdstor = h.cdstor; sr.vin = vin; sr.cvin = h.cvin; sr.vout = vout;
+      sr.cvout = h.cvout; sr.erras = erras; sr.errel = errel; sr.cerras = h.cerras;
+      sr.caeras = h.caeras;
+      h.step_recs.push_back(sr);
+      h.adinp = R[RD_ADIN]; h.adoutp = R[RD_ADOUT]; h.ndinp = R[RD_NDIN]; h.ndoutp = R[RD_NDOUT];
+      h.aninp = R[RD_ANIN]; h.anoutp = R[RD_ANOUT]; h.nninp = h.nnin; h.nnoutp = h.nnout;
+      h.steps_done++;
+      h.pend |= ACT_COMMIT;
+      if (h.deltat >= 1.0e15 || std::fabs(h.time - P.tmax) <= 0.001 * h.deltat) {
+        h.status = 1;
+        continue;
+      }
+      // TIMUPD
+      h.timep = h.time;
+      if (h.iter < P.ituns1) {
+        h.deltat = h.deltat * P.dtmagm + P.dtmaga;
+        if (h.deltat > P.dtmax) h.deltat = P.dtmax;
+      }
+      if (h.iter >= P.ituns2) {
+        h.deltat = h.deltat * P.dtredm - P.dtreds;
+        if (h.deltat < P.dtmin) h.deltat = P.dtmin;
+      }
+      if (h.time + h.deltat >= P.tmax) {
+        h.deltat = P.tmax - h.time;
+        h.time = P.tmax;
+      } else {
+        if (h.time + 2 * h.deltat > P.tmax) h.deltat = (P.tmax - h.time) / 2;
+        h.time = h.time + h.deltat;
+      }
+      h.dtgmin = !(h.deltat <= P.dtmin);
+      h.nstep++;
+      h.iter = 1; h.nitert = 0; h.kbackt = 0;
+      atm_advance(h);
+      h.pend |= ACT_START;
+    }
+  }
+  return niter_members;
+}
+
+// ============================================================================
+// public engine functions
+// ============================================================================
+Engine* engine_create(int nmembers, const cathy_member_t* members,
+                      const cathy_opts_t& opts) {
+  Engine* e = new Engine();
+  e->opts = opts;
+  if (e->opts.inner_maxit <= 0) e->opts.inner_maxit = 200;
+  if (e->opts.inner_tol <= 0) e->opts.inner_tol = 1e-5;
+  try {
+    e->build(nmembers, members);
+    // the first time level: ATMNXT at TIME (cathy_main.f:2938) for every member
+    for (int m = 0; m < e->nmem; ++m) e->atm_advance(*e->M[m]);
+  } catch (...) {
+    delete e;
+    throw;
+  }
+  return e;
+}
+
+void engine_destroy(Engine* e) { delete e; }
+
+static int run_until(Engine* e, int target_mode, int max_macro) {
+  // target_mode 1: every running member accepts exactly one more step
+  std::vector<int> target(e->nmem);
+  for (int m = 0; m < e->nmem; ++m) {
+    target[m] = e->M[m]->steps_done + 1;
+    e->M[m]->paused = false;
+  }
+  CG_TRY(cudaEventRecord(e->ev0, e->st));
+  for (int it = 0; it < max_macro; ++it) {
+    bool any = false;
+    for (int m = 0; m < e->nmem; ++m) {
+      MemberHost& h = *e->M[m];
+      if (target_mode == 1) h.paused = (h.steps_done >= target[m]);
+      if (h.status == 0 && !h.paused) any = true;
+    }
+    if (!any) break;
+    e->macro_iteration();
+  }
+  // flush pending commits of paused/finished members
+  bool pending = false;
+  for (int m = 0; m < e->nmem; ++m)
+    if (e->M[m]->pend & ACT_COMMIT) pending = true;
+  if (pending) {
+    for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = true;
+    e->macro_iteration();
+    for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = false;
+  }
+  CG_TRY(cudaEventRecord(e->ev1, e->st));
+  CG_TRY(cudaEventSynchronize(e->ev1));
+  float ms = 0;
+  CG_TRY(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  e->gpu_ms += ms;
+  return 0;
+}
+
+int engine_step(Engine* e, int* nactive) {
+  run_until(e, 1, 1 << 30);
+  int a = 0;
+  for (int m = 0; m < e->nmem; ++m) a += (e->M[m]->status == 0);
+  if (nactive) *nactive = a;
+  return 0;
+}
+
+int engine_run(Engine* e, int max_steps, int* nsteps) {
+  int done = 0;
+  if (max_steps <= 0) max_steps = 1 << 30;
+  // free-running: members advance independently until finished
+  std::vector<int> start(e->nmem);
+  for (int m = 0; m < e->nmem; ++m) start[m] = e->M[m]->steps_done;
+  CG_TRY(cudaEventRecord(e->ev0, e->st));
+  for (;;) {
+    bool any = false;
+    for (int m = 0; m < e->nmem; ++m) {
+      MemberHost& h = *e->M[m];
+      h.paused = (h.steps_done - start[m] >= max_steps);
+      if (h.status == 0 && !h.paused) any = true;
+    }
+    if (!any) break;
+    e->macro_iteration();
+  }
+  bool pending = false;
+  for (int m = 0; m < e->nmem; ++m)
+    if (e->M[m]->pend & ACT_COMMIT) pending = true;
+  if (pending) {
+    for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = true;
+    e->macro_iteration();
+  }
+  for (int m = 0; m < e->nmem; ++m) {
+    e->M[m]->paused = false;
+    done = std::max(done, e->M[m]->steps_done - start[m]);
+  }
+  CG_TRY(cudaEventRecord(e->ev1, e->st));
+  CG_TRY(cudaEventSynchronize(e->ev1));
+  float ms = 0;
+  CG_TRY(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  e->gpu_ms += ms;
+  if (nsteps) *nsteps = done;
+  return 0;
+}
+
+int engine_sizes(Engine* e, int m, int32_t* out5) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  const HostMesh& g = e->M[m]->mesh;
+  out5[0] = g.n; out5[1] = g.nt; out5[2] = g.nnod; out5[3] = g.ntri; out5[4] = (int32_t)g.nnz();
+  return 0;
+}
+
+int engine_get_state(Engine* e, int m, double* pnew, double* time,
+                     double* deltat, int32_t* status) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  MemberHost& h = *e->M[m];
+  if (pnew)
+    CG_TRY(cudaMemcpyAsync(pnew, e->nd.pnew + e->node_off[m], sizeof(double) * h.mesh.n,
+                           cudaMemcpyDeviceToHost, e->st));
+  CG_TRY(cudaStreamSynchronize(e->st));
+  // the reported time is that of the last accepted step
+  if (time) *time = h.step_recs.empty() ? 0.0 : h.step_recs.back().time;
+  if (deltat) *deltat = h.step_recs.empty() ? h.deltat : h.step_recs.back().deltat;
+  if (status) *status = h.status;
+  return 0;
+}
+
+int engine_set_state(Engine* e, int m, const double* ptimep, double time,
+                     double deltat) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  MemberHost& h = *e->M[m];
+  const size_t n = h.mesh.n;
+  CG_TRY(cudaMemcpyAsync(e->nd.pnew + e->node_off[m], ptimep, sizeof(double) * n,
+                         cudaMemcpyHostToDevice, e->st));
+  CG_TRY(cudaMemcpyAsync(e->nd.ptimep + e->node_off[m], ptimep, sizeof(double) * n,
+                         cudaMemcpyHostToDevice, e->st));
+  CG_TRY(cudaStreamSynchronize(e->st));
+  h.time = time;
+  h.deltat = deltat;
+  h.timep = time - deltat;
+  h.status = 0;
+  h.pend = ACT_START;
+  h.iterating = false;
+  return 0;
+}
+
+int engine_num_records(Engine* e, int m, int32_t* ni, int32_t* ns) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  *ni = (int32_t)e->M[m]->iter_recs.size();
+  *ns = (int32_t)e->M[m]->step_recs.size();
+  return 0;
+}
+
+int engine_get_records(Engine* e, int m, cathy_iter_rec_t* ir, cathy_step_rec_t* sr) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  MemberHost& h = *e->M[m];
+  if (ir && !h.iter_recs.empty())
+    std::memcpy(ir, h.iter_recs.data(), sizeof(cathy_iter_rec_t) * h.iter_recs.size());
+  if (sr && !h.step_recs.empty())
+    std::memcpy(sr, h.step_recs.data(), sizeof(cathy_step_rec_t) * h.step_recs.size());
+  return 0;
+}
+
+int engine_get_mesh(Engine* e, int m, double* x, double* y, double* z,
+                    int32_t* tetra, int32_t* rowptr, int32_t* cols) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  const HostMesh& g = e->M[m]->mesh;
+  if (x) std::memcpy(x, g.x.data(), sizeof(double) * g.n);
+  if (y) std::memcpy(y, g.y.data(), sizeof(double) * g.n);
+  if (z) std::memcpy(z, g.z.data(), sizeof(double) * g.n);
+  if (tetra) std::memcpy(tetra, g.tetra.data(), sizeof(int32_t) * 5 * g.nt);
+  if (rowptr) std::memcpy(rowptr, g.rowptr.data(), sizeof(int32_t) * (g.n + 1));
+  if (cols) std::memcpy(cols, g.cols.data(), sizeof(int32_t) * g.nnz());
+  return 0;
+}
+
+// Assemble member m's system at its current state without solving: the next
+// nonlinear iteration's LHS (before Dirichlet masking), RHS and XT5.
+int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt5,
+                         int32_t* dirmask) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  MemberHost& h = *e->M[m];
+  // apply pending START so that pold/ptnew/swtimep are current
+  std::vector<uint8_t> act(e->nmem, 0);
+  uint8_t a = h.pend & (ACT_COMMIT | ACT_BACKSTEP | ACT_START | ACT_NEXT);
+  act[m] = a;
+  h.pend &= ~a;
+  if (a & ACT_START) { h.iterating = true; h.iter = 1; h.nitert = 0; }
+  e->push_scalars();
+  e->d_act.upload(act.data(), e->nmem, e->st);
+  k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0);
+  k_start_surface<<<cdiv(e->nsurf, kThreads), kThreads, 0, e->st>>>(e->nsurf, e->d_srows.p, e->d_act.p, e->d_ms.p, e->nd);
+  k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 1);
+  act[m] = ACT_ITER;
+  e->d_act.upload(act.data(), e->nmem, e->st);
+  const bool mixed = (e->precision == 1 && e->iopt == 1);
+  if (mixed) {
+    k_vg<float><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0);
+    e->assemble<float>();
+  } else {
+    k_vg<double><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->iopt == 2);
+    e->assemble<double>();
+  }
+  e->check_launch();
+  const int no = e->node_off[m];
+  const long ao = e->nnz_off[m];
+  const int n = h.mesh.n;
+  const long nnz = h.mesh.nnz();
+  if (mixed) {
+    std::vector<float> v(nnz);
+    CG_TRY(cudaMemcpyAsync(v.data(), e->d_vals32.p + ao, sizeof(float) * nnz, cudaMemcpyDeviceToHost, e->st));
+    CG_TRY(cudaStreamSynchronize(e->st));
+    for (long s = 0; s < nnz; ++s) vals[s] = v[s];
+  } else {
+    CG_TRY(cudaMemcpyAsync(vals, e->d_vals64.p + ao, sizeof(double) * nnz, cudaMemcpyDeviceToHost, e->st));
+  }
+  CG_TRY(cudaMemcpyAsync(rhs, e->nd.rhs + no, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+  CG_TRY(cudaMemcpyAsync(xt5, e->nd.xt5 + no, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+  std::vector<uint8_t> dm(n);
+  CG_TRY(cudaMemcpyAsync(dm.data(), e->nd.dmask + no, n, cudaMemcpyDeviceToHost, e->st));
+  CG_TRY(cudaStreamSynchronize(e->st));
+  for (int i = 0; i < n; ++i) dirmask[i] = dm[i];
+  return 0;
+}
+
+int engine_stats(Engine* e, double* gpu_ms, int64_t* launches, int64_t* lin_iters,
+                 int64_t* nl_iters) {
+  if (gpu_ms) *gpu_ms = e->gpu_ms;
+  if (launches) *launches = e->launches;
+  if (lin_iters) *lin_iters = e->lin_iters;
+  if (nl_iters) *nl_iters = e->nl_iters;
+  return 0;
+}
+
+
+// ============================================================================
+// Fortran drop-ins: a one-member engine around a caller-provided matrix
+// ============================================================================
+void Engine::bare_init(int n, const std::vector<int32_t>& rowptr,
+                       const std::vector<int32_t>& cols, const std::vector<uint8_t>& dm) {
+  nmem = 1;
+  CG_TRY(cudaSetDevice(opts.device));
+  CG_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CG_TRY(cudaEventCreate(&ev0));
+  CG_TRY(cudaEventCreate(&ev1));
+  N = n;
+  NNZ = (long)cols.size();
+  node_off = {0, n};
+  std::vector<int32_t> diag(n, -1), tslot(NNZ), lfp, lfr, lbp, lbr;
+  for (int i = 0; i < n; ++i)
+    for (int s = rowptr[i]; s < rowptr[i + 1]; ++s) {
+      const int j = cols[s];
+      if (j == i) diag[i] = s;
+      tslot[s] = (int)(std::lower_bound(cols.begin() + rowptr[j], cols.begin() + rowptr[j + 1], i) - cols.begin());
+    }
+  for (int i = 0; i < n; ++i) {
+    if (diag[i] < 0) throw std::string("matrix row without diagonal");
+    if (rowptr[i + 1] - rowptr[i] > kGroup)
+      throw std::string("matrix row longer than 16 entries (unsupported)");
+  }
+  level_schedule(n, rowptr, cols, true, lfp, lfr);
+  level_schedule(n, rowptr, cols, false, lbp, lbr);
+  lev_f_ptr = lfp;
+  lev_b_ptr = lbp;
+  d_lev_f.alloc(n); d_lev_f.upload(lfr.data(), n, st);
+  d_lev_b.alloc(n); d_lev_b.upload(lbr.data(), n, st);
+  std::vector<int32_t> zeros(n, 0), loc(n);
+  for (int i = 0; i < n; ++i) loc[i] = i;
+  d_mem.alloc(n); d_mem.upload(zeros.data(), n, st);
+  d_loc.alloc(n); d_loc.upload(loc.data(), n, st);
+  d_rowptr.alloc(n + 1); d_rowptr.upload(rowptr.data(), n + 1, st);
+  d_cols.alloc(NNZ); d_cols.upload(cols.data(), NNZ, st);
+  d_diag.alloc(n); d_diag.upload(diag.data(), n, st);
+  d_tslot.alloc(NNZ); d_tslot.upload(tslot.data(), NNZ, st);
+  d_dmask.alloc(n); d_dmask.upload(dm.data(), n, st);
+  d_vals64.alloc(NNZ);
+  d_F64.alloc(NNZ);
+  d_G64.alloc(NNZ);
+  for (int k = 0; k < 14; ++k) { w64[k].alloc(n); w64[k].zero(st); }
+  d_nodal[ND_RHS].alloc(n);
+  d_nodal[ND_PDIFF].alloc(n);
+  nd.rhs = d_nodal[ND_RHS].p;
+  nd.pdiff = d_nodal[ND_PDIFF].p;
+  nd.mem = d_mem.p;
+  nd.loc = d_loc.p;
+  nd.dmask = d_dmask.p;
+  d_act.alloc(1); d_active.alloc(1); d_ms.alloc(1);
+  d_sc.alloc(SC_N); d_sc.zero(st);
+  d_niter.alloc(1); d_nact.alloc(1);
+  make_blockmap(bm1, kThreads);
+  make_blockmap(bm16, kRowsPerBlock16);
+  uint8_t one = 1, it = ACT_ITER;
+  d_active.upload(&one, 1, st);
+  d_act.upload(&it, 1, st);
+  precond = 0;
+}
+
+static double host_masked_resid(int n, const std::vector<int32_t>& rowptr,
+                                const std::vector<int32_t>& cols,
+                                const std::vector<double>& vals,
+                                const std::vector<uint8_t>& dm, const double* b,
+                                const double* x) {
+  double rr = 0.0, bb = 0.0;
+  for (int i = 0; i < n; ++i) {
+    if (dm[i]) continue;
+    double s = b[i];
+    for (int q = rowptr[i]; q < rowptr[i + 1]; ++q)
+      if (!dm[cols[q]]) s -= vals[q] * x[cols[q]];
+    rr += s * s;
+    bb += b[i] * b[i];
+  }
+  return bb > 1.7e-100 ? std::sqrt(rr / bb) : std::sqrt(rr / n);
+}
+
+int dropin_symslv(int n, int nterm, int numdir, const int32_t* noddir,
+                  const int32_t* ja, const int32_t* topol, double* pnew,
+                  const double* tnoti, const double* coef1, double* coef2,
+                  int itmxcg, double tolcg, double rmin, int32_t* niter,
+                  double* err, double* res) {
+  (void)rmin; (void)nterm;
+  std::vector<int32_t> rowptr, cols, up;
+  upper_to_full(n, topol, ja, rowptr, cols, up);
+  std::vector<double> vals(cols.size());
+  for (size_t s = 0; s < cols.size(); ++s) vals[s] = coef1[up[s]];
+  std::vector<uint8_t> dm(n, 0);
+  for (int k = 0; k < numdir; ++k) dm[noddir[k] - 1] = 1;
+  std::vector<double> b(tnoti, tnoti + n);
+  for (int i = 0; i < n; ++i) if (dm[i]) b[i] = 0.0;
+  Engine E;
+  E.opts = cathy_opts_t{0, 0, 0, 0.0, 0};
+  E.bare_init(n, rowptr, cols, dm);
+  E.d_vals64.upload(vals.data(), vals.size(), E.st);
+  E.d_nodal[ND_RHS].upload(b.data(), n, E.st);
+  E.solve_pcg<double, double>(itmxcg, tolcg, true);
+  int32_t it = 0;
+  double sc[SC_N];
+  E.d_niter.download(&it, 1, E.st);
+  E.d_sc.download(sc, SC_N, E.st);
+  E.d_nodal[ND_PDIFF].download(pnew, n, E.st);
+  std::vector<double> F(cols.size());
+  if (coef2) E.d_F64.download(F.data(), F.size(), E.st);
+  CG_TRY(cudaStreamSynchronize(E.st));
+  if (coef2) {
+    // factor back in the reference's upper storage: U_ij = L_ji
+    for (int i = 0; i < n; ++i)
+      for (int s = rowptr[i]; s < rowptr[i + 1]; ++s)
+        if (cols[s] <= i) coef2[up[s]] = F[s];
+  }
+  *niter = it;
+  if (err) *err = sc[SC_ERR];
+  if (res) *res = host_masked_resid(n, rowptr, cols, vals, dm, b.data(), pnew);
+  return 0;
+}
+
+int dropin_nsyslv(int isolv, int n, int nterm, int numdir, const int32_t* noddir,
+                  const int32_t* ja, const int32_t* topol, double* pnew,
+                  const double* tnoti, const double* coef1, double* coef2,
+                  int itmxcg, double tolcg, double rmin, int32_t* niter,
+                  double* err, double* res) {
+  (void)rmin; (void)coef2;
+  if (isolv != 0 && isolv != -5) return CATHY_GB300_EUNSUP;
+  std::vector<int32_t> rowptr(n + 1), cols(nterm);
+  for (int i = 0; i <= n; ++i) rowptr[i] = topol[i] - 1;
+  for (int s = 0; s < nterm; ++s) cols[s] = ja[s] - 1;
+  std::vector<double> vals(coef1, coef1 + nterm);
+  std::vector<uint8_t> dm(n, 0);
+  for (int k = 0; k < numdir; ++k) dm[noddir[k] - 1] = 1;
+  std::vector<double> b(tnoti, tnoti + n);
+  double bn = 0.0;
+  for (int i = 0; i < n; ++i) { if (dm[i]) b[i] = 0.0; bn += tnoti[i] * tnoti[i]; }
+  if (bn == 0.0) {  // NSYSLV returns PNEW = 0 for a zero RHS
+    for (int i = 0; i < n; ++i) pnew[i] = 0.0;
+    *niter = 0;
+    if (err) *err = 0.0;
+    if (res) *res = 0.0;
+    return 0;
+  }
+  Engine E;
+  E.opts = cathy_opts_t{0, 0, 0, 0.0, 0};
+  E.bare_init(n, rowptr, cols, dm);
+  E.d_vals64.upload(vals.data(), vals.size(), E.st);
+  E.d_nodal[ND_RHS].upload(b.data(), n, E.st);
+  E.solve_bicgstab(isolv, itmxcg, tolcg);
+  int32_t it = 0;
+  double sc[SC_N];
+  E.d_niter.download(&it, 1, E.st);
+  E.d_sc.download(sc, SC_N, E.st);
+  E.d_nodal[ND_PDIFF].download(pnew, n, E.st);
+  CG_TRY(cudaStreamSynchronize(E.st));
+  *niter = it;
+  if (err) *err = sc[SC_ERR];
+  if (res) *res = host_masked_resid(n, rowptr, cols, vals, dm, b.data(), pnew);
+  return 0;
+}
+
+// ASSPIC drop-in: element-parallel assembly into the caller's upper CSR
+// arrays through TETJA (atomic accumulation).
+__global__ void k_asspic(int nt, int ntri, int maxstr, const int32_t* tetra,
+                         const int32_t* tetja, const double* lmass,
+                         double* coef1, double* coef2, double* coef4,
+                         const double* et1e, const double* pel,
+                         const double* permx, const double* permy,
+                         const double* permz, const double* ckrwe,
+                         const double* volur, const double* volu,
+                         const double* bi, const double* ci, const double* di) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nt) return;
+  const int iel = e + 1;
+  int istr = 1 + iel / (ntri * 3);
+  if (iel % (ntri * 3) == 0) istr -= 1;
+  const int mtype = tetra[5 * e + 4];
+  const int id = (mtype - 1) * maxstr + (istr - 1);
+  const double vk = volur[e] * ckrwe[e];
+  const double ve1 = volu[e] * et1e[e], ve = volu[e] * pel[e];
+  const double pvk1 = permx[id] * vk, pvk2 = permy[id] * vk, pvk3 = permz[id] * vk;
+  for (int k = 0; k < 4; ++k) {
+    const double pvkb = pvk1 * bi[4 * e + k], pvkc = pvk2 * ci[4 * e + k], pvkd = pvk3 * di[4 * e + k];
+    for (int l = k; l < 4; ++l) {
+      const int ind = tetja[16 * e + 4 * l + k] - 1;
+      atomicAdd(coef1 + ind, pvkb * bi[4 * e + l] + pvkc * ci[4 * e + l] + pvkd * di[4 * e + l]);
+      atomicAdd(coef2 + ind, ve1 * lmass[4 * l + k]);
+      atomicAdd(coef4 + ind, ve * lmass[4 * l + k]);
+    }
+  }
+}
+
+int dropin_asspic(int nt, int ntri, const int32_t* tetra, const int32_t* tetja,
+                  const double* lmass, double* coef1, double* coef2,
+                  double* coef4, const double* et1e, const double* pel,
+                  const double* permx, const double* permy,
+                  const double* permz, const double* ckrwe,
+                  const double* volur, const double* volu, const double* bi,
+                  const double* ci, const double* di, int maxstr, int nterm) {
+  cudaStream_t st;
+  CG_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int nzone = 0;
+  for (int e = 0; e < nt; ++e) nzone = std::max(nzone, (int)tetra[5 * e + 4]);
+  const size_t tsz = (size_t)maxstr * nzone;
+  DBuf<int32_t> t, tj;
+  DBuf<double> lm, c1, c2, c4, a1, a2, px, py, pz, kr, vr, vo, b, c, d;
+  t.alloc(5 * (size_t)nt); t.upload(tetra, 5 * (size_t)nt, st);
+  tj.alloc(16 * (size_t)nt); tj.upload(tetja, 16 * (size_t)nt, st);
+  lm.alloc(16); lm.upload(lmass, 16, st);
+  c1.alloc(nterm); c1.upload(coef1, nterm, st);
+  c2.alloc(nterm); c2.upload(coef2, nterm, st);
+  c4.alloc(nterm); c4.upload(coef4, nterm, st);
+  a1.alloc(nt); a1.upload(et1e, nt, st);
+  a2.alloc(nt); a2.upload(pel, nt, st);
+  px.alloc(tsz); px.upload(permx, tsz, st);
+  py.alloc(tsz); py.upload(permy, tsz, st);
+  pz.alloc(tsz); pz.upload(permz, tsz, st);
+  kr.alloc(nt); kr.upload(ckrwe, nt, st);
+  vr.alloc(nt); vr.upload(volur, nt, st);
+  vo.alloc(nt); vo.upload(volu, nt, st);
+  b.alloc(4 * (size_t)nt); b.upload(bi, 4 * (size_t)nt, st);
+  c.alloc(4 * (size_t)nt); c.upload(ci, 4 * (size_t)nt, st);
+  d.alloc(4 * (size_t)nt); d.upload(di, 4 * (size_t)nt, st);
+  k_asspic<<<cdiv(nt, 128), 128, 0, st>>>(nt, ntri, maxstr, t.p, tj.p, lm.p, c1.p, c2.p, c4.p,
+                                          a1.p, a2.p, px.p, py.p, pz.p, kr.p, vr.p, vo.p, b.p, c.p, d.p);
+  CG_TRY(cudaPeekAtLastError());
+  c1.download(coef1, nterm, st);
+  c2.download(coef2, nterm, st);
+  c4.download(coef4, nterm, st);
+  CG_TRY(cudaStreamSynchronize(st));
+  cudaStreamDestroy(st);
+  return 0;
+}
+
+}  // namespace cathy

@@ -1,0 +1,97 @@
+"""C-ABI library: builds, loads, exports every declared symbol; host-side
+mesh construction matches the oracle (and so the reference's grid3d); no
+CPU fallback when no GPU is present."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, GOLDEN, has_gpu, load_golden_case
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "cathy_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(cathy_gb300_\w+)\s*\(", src)))
+
+
+def test_exports_every_declared_symbol():
+    from pycathy_wrapper_gb300 import _lib
+    L = _lib.load()
+    names = _declared()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in _lib.EXPORTS, n
+    assert L.cathy_gb300_version() >= 100
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-device path")
+def test_no_cpu_fallback_without_device():
+    from pycathy_wrapper_gb300 import _lib
+    from pycathy_wrapper_gb300.api import Simulation
+    from pycathy_wrapper_gb300.inputs import config0
+    assert _lib.load().cathy_gb300_device_count() == 0
+    with pytest.raises(_lib.CathyError) as ei:
+        Simulation(config0(tmax=10.0))
+    assert ei.value.code == _lib.ENODEV
+
+
+@pytest.mark.parametrize("key", ["weill", "soil3d"])
+def test_host_mesh_matches_oracle(key):
+    import oracle as O
+    from pycathy_wrapper_gb300.api import build_mesh
+    case = load_golden_case(key)
+    m = build_mesh(case, iopt=1)
+    o = O.Oracle(case)
+    om = o.mesh()
+    assert (m["n"], m["nt"], m["nnod"], m["ntri"]) == (o.n, o.nt, o.nnod, o.ntri)
+    np.testing.assert_array_equal(m["tetra"], om["tetra"])
+    np.testing.assert_array_equal(m["x"], om["x"])
+    np.testing.assert_array_equal(m["y"], om["y"])
+    np.testing.assert_array_equal(m["z"], om["z"])
+    # full CSR pattern == symmetric expansion of STRPIC's upper storage
+    topol, ja = om["topol"], om["ja"]
+    rows = np.repeat(np.arange(o.n), np.diff(topol))
+    up = set(zip(rows.tolist(), (ja - 1).tolist()))
+    full = up | {(j, i) for i, j in up}
+    mrows = np.repeat(np.arange(m["n"]), np.diff(m["rowptr"]))
+    got = set(zip(mrows.tolist(), m["cols"].tolist()))
+    assert got == full
+    assert len(m["cols"]) == 2 * o.nterm - o.n
+
+
+def test_host_mesh_newton_pattern_matches_strnew():
+    import oracle as O
+    from pycathy_wrapper_gb300.api import build_mesh
+    from pycathy_wrapper_gb300.inputs import config0
+    case = config0()
+    case.parm.iopt = 2
+    m = build_mesh(case, iopt=2)
+    o = O.Oracle(case)
+    om = o.mesh()
+    np.testing.assert_array_equal(m["rowptr"], om["topol"] - 1)
+    np.testing.assert_array_equal(m["cols"], om["ja"] - 1)
+    np.testing.assert_array_equal(m["tetra"], o.tetra_gen3d())
+
+
+def test_mesh_with_inactive_cells_and_zones():
+    import oracle as O
+    from pycathy_wrapper_gb300.api import build_mesh
+    from pycathy_wrapper_gb300.inputs import config0
+    case = config0()
+    dem = case.dem.dem.copy()
+    dem[0, 0] = 0.0
+    dem[5, 7] = 0.0
+    case.dem.dem = dem
+    zone = np.ones(dem.shape, np.int32)
+    zone[:, 10:] = 2
+    case.dem.zone = zone
+    from pycathy_wrapper_gb300.inputs import Soil
+    case.soil = Soil.homogeneous(case.dem.nstr, nzone=2)
+    m = build_mesh(case, iopt=1)
+    o = O.Oracle(case)
+    om = o.mesh()
+    np.testing.assert_array_equal(m["tetra"], om["tetra"])
+    np.testing.assert_array_equal(m["z"], om["z"])

@@ -1,0 +1,201 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle and the
+reference's golden first iteration.
+
+Tolerances: heads within 1e-6 m (the spec bar, TOLUNS = 1e-6 for the
+synthetic configurations), relative mass-balance errors within 1e-8 of the
+oracle's, linear-solver iteration counts equal for the FP64 path (same
+recurrences and preconditioner), within +-1 where round-off decides a stop.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_json, load_golden_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(case, **kw):
+    from pycathy_wrapper_gb300.api import Simulation
+    return Simulation(case, **kw)
+
+
+@pytest.mark.parametrize("key", ["weill", "soil3d"])
+def test_first_iteration_matches_reference_golden(key):
+    g = golden_json()[key]
+    case = load_golden_case(key)
+    with _sim(case) as s:
+        s.step()
+        its, _ = s.records(0)
+    r = its[0]
+    fi, lin = g["first_iter"], g["linear"]
+    assert r["niter"] == fi["niter"]
+    assert r["ikmax"] == fi["ikmax"]
+    for k in ("pl2", "pinf", "fl2", "finf"):
+        assert abs(r[k] - fi[k]) / abs(fi[k]) < 6e-4, (k, r[k], fi[k])
+    assert abs(r["lin_err"] - lin["err"]) / lin["err"] < 1e-4
+
+
+@pytest.mark.parametrize("key", ["weill", "soil3d"])
+def test_picard_system_matches_oracle(key):
+    import oracle as O
+    case = load_golden_case(key)
+    o = O.Oracle(case)
+    c1, tn, xt5, dm = o.picard_system()
+    with _sim(case) as s:
+        vals, rhs, xt5g, dmg = s.picard_system(0)
+        m = s.mesh(0)
+    n = o.n
+    om = o.mesh()
+    topol, ja = om["topol"], om["ja"]
+    rows = np.repeat(np.arange(n), np.diff(topol))
+    up = {(i, j - 1): c1[k] for k, (i, j) in enumerate(zip(rows, ja))}
+    grow = np.repeat(np.arange(n), np.diff(m["rowptr"]))
+    ref = np.array([up[(i, j)] if (i, j) in up else up[(j, i)] for i, j in zip(grow, m["cols"])])
+    scale = np.abs(ref).max()
+    assert np.max(np.abs(vals - ref)) <= 1e-12 * scale
+    np.testing.assert_array_equal(dmg, dm)
+    assert np.max(np.abs(rhs - tn)) <= 1e-12 * max(np.abs(tn).max(), 1e-30)
+    assert np.max(np.abs(xt5g - xt5)) <= 1e-12 * max(np.abs(xt5).max(), 1e-30)
+
+
+def _run_both(case, nsteps, **kw):
+    import oracle as O
+    o = O.Oracle(case)
+    for _ in range(nsteps):
+        if o.step() != 0:
+            break
+    with _sim(case, **kw) as s:
+        for _ in range(nsteps):
+            s.step()
+        p, t, dt, st = s.state(0)
+        its, sts = s.records(0)
+    po, to, dto = o.state()
+    return o, (p, t, sts, its), (po, o.step_records(), o.iter_records())
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+def test_hillslope_steps_match_oracle(precond):
+    from pycathy_wrapper_gb300.inputs import config0
+    case = config0(tmax=3600.0, precond=precond)
+    o, (p, t, sts, its), (po, osr, oir) = _run_both(case, 25)
+    assert len(sts) == len(osr)
+    assert [r["iter"] for r in sts] == [r["iter"] for r in osr]
+    np.testing.assert_allclose([r["time"] for r in sts], [r["time"] for r in osr], rtol=0, atol=1e-9)
+    assert np.max(np.abs(p - po)) <= 1e-6
+    for a, b in zip(sts, osr):
+        assert abs(a["errel"] - b["errel"]) <= 1e-8 * max(1.0, abs(b["errel"])) + 1e-8
+        assert abs(a["dstore"] - b["dstore"]) <= 1e-8 * max(abs(b["dstore"]), 1e-12)
+    dn = [abs(a["niter"] - b["niter"]) for a, b in zip(its, oir)]
+    assert max(dn) <= 1
+
+
+def test_hillslope_column_line_preconditioner_matches_oracle_heads():
+    from pycathy_wrapper_gb300.inputs import config0
+    import oracle as O
+    case = config0(tmax=3600.0, precond=0)
+    o = O.Oracle(case)
+    for _ in range(25):
+        o.step()
+    case2 = config0(tmax=3600.0, precond=2)
+    with _sim(case2) as s:
+        for _ in range(25):
+            s.step()
+        p, t, dt, st = s.state(0)
+        _, sts = s.records(0)
+    po, to, _ = o.state()
+    assert abs(sts[-1]["time"] - o.step_records()[-1]["time"]) < 1e-9
+    assert np.max(np.abs(p - po)) <= 1e-6
+
+
+def test_mixed_precision_heads_within_tolerance():
+    from pycathy_wrapper_gb300.inputs import config0
+    import oracle as O
+    case = config0(tmax=3600.0, precond=0)
+    o = O.Oracle(case)
+    for _ in range(25):
+        o.step()
+    case2 = config0(tmax=3600.0, precond=2)
+    with _sim(case2, precision=1) as s:
+        for _ in range(25):
+            s.step()
+        p, t, dt, st = s.state(0)
+        _, sts = s.records(0)
+    po, to, _ = o.state()
+    assert abs(sts[-1]["time"] - o.step_records()[-1]["time"]) < 1e-9
+    assert np.max(np.abs(p - po)) <= 1e-6
+    osr = o.step_records()
+    assert abs(sts[-1]["cerras"] - osr[-1]["cerras"]) <= 1e-8 * max(1.0, abs(osr[-1]["cvin"]))
+
+
+def test_symslv_dropin_matches_oracle():
+    import oracle as O
+    from pycathy_wrapper_gb300.api import symslv
+    case = load_golden_case("weill")
+    o = O.Oracle(case)
+    c1, tn, xt5, dm = o.picard_system()
+    om = o.mesh()
+    noddir = np.nonzero(dm)[0] + 1
+    c1p = c1.copy()
+    c1p[om["topol"][noddir - 1] - 1] = 1.7e91  # BCPIC penalty as the Fortran caller passes it
+    xo, no, eo, ro = O.symslv(om["topol"], om["ja"], c1p, tn, noddir)
+    xg, ng, eg, rg, coef2 = symslv(om["topol"], om["ja"], c1p, tn, noddir)
+    assert abs(ng - no) <= 1
+    assert np.max(np.abs(xg - xo)) <= 1e-8 * np.max(np.abs(xo))
+    assert rg < 1e-9
+
+
+@pytest.mark.parametrize("isolv", [0, -5])
+def test_nsyslv_dropin_matches_oracle(isolv):
+    import oracle as O
+    from pycathy_wrapper_gb300.api import nsyslv
+    case = load_golden_case("soil3d")
+    o = O.Oracle(case)
+    c1, tn, xt5, dm = o.picard_system()
+    om = o.mesh()
+    n = o.n
+    rows = np.repeat(np.arange(n), np.diff(om["topol"]))
+    cols = om["ja"] - 1
+    import scipy.sparse as sp
+    U = sp.csr_matrix((c1, (rows, cols)), shape=(n, n))
+    A = (U + U.T - sp.diags(U.diagonal())).tocsr()
+    A.sort_indices()
+    noddir = np.nonzero(dm)[0] + 1
+    A = A.tolil()
+    for d in noddir - 1:
+        A[d, d] = 1.7e91
+    A = A.tocsr()
+    A.sort_indices()
+    topol = (A.indptr + 1).astype(np.int32)
+    ja = (A.indices + 1).astype(np.int32)
+    xo, no, eo, ro = O.nsyslv(topol, ja, A.data, tn, noddir, isolv=isolv)
+    xg, ng, eg, rg = nsyslv(topol, ja, A.data, tn, noddir, isolv=isolv)
+    assert abs(ng - no) <= 1
+    assert np.max(np.abs(xg - xo)) <= 1e-7 * np.max(np.abs(xo))
+
+
+def test_newton_ponded_steps_match_oracle():
+    from pycathy_wrapper_gb300.inputs import config4_member
+    case = config4_member(ncell=12, nstr=8, tmax=600.0)
+    o, (p, t, sts, its), (po, osr, oir) = _run_both(case, 8)
+    assert [r["iter"] for r in sts] == [r["iter"] for r in osr]
+    assert np.max(np.abs(p - po)) <= 1e-6
+
+
+def test_ensemble_batch_matches_single_runs():
+    from pycathy_wrapper_gb300.inputs import config2_members
+    import oracle as O
+    cases = config2_members(3, tmax=1200.0, min_cells=8, max_cells=14)
+    for c in cases:
+        c.parm.precond = 0
+    with _sim(cases) as s:
+        s.run()
+        got = [s.state(m) for m in range(3)]
+        recs = [s.records(m)[1] for m in range(3)]
+    for m, c in enumerate(cases):
+        o = O.Oracle(c)
+        o.run()
+        po, to, _ = o.state()
+        osr = o.step_records()
+        assert len(recs[m]) == len(osr)
+        assert abs(recs[m][-1]["time"] - osr[-1]["time"]) < 1e-9
+        assert np.max(np.abs(got[m][0] - po)) <= 1e-6
