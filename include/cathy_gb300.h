@@ -158,6 +158,14 @@ int32_t cathy_gb300_get_mesh(void* handle, int32_t m, double* x, double* y,
  * Dirichlet masking, RHS after BCs, RHS before BCs, Dirichlet mask) */
 int32_t cathy_gb300_picard_system(void* handle, int32_t m, double* vals,
                                   double* rhs, double* xt5, int32_t* dirmask);
+/* restore every member to its initial condition (device-side copies) */
+int32_t cathy_gb300_reset(void* handle);
+/* live timing of the SpMV kernel: enable (1) / disable (0) resets the
+ * counters; -1 only reads them.  Outputs: total device time of the timed
+ * launches (ms, CUDA events on the solver stream), launches, and their
+ * algorithmic bytes (values+columns+row pointers+vectors). */
+int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
+                            int64_t* spmv_launches, double* spmv_bytes);
 /* GPU time spent in the hot path (ms) since creation, and kernel launches */
 int32_t cathy_gb300_stats(void* handle, double* gpu_ms, int64_t* launches,
                           int64_t* lin_iters, int64_t* nl_iters);

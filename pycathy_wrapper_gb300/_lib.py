@@ -105,6 +105,9 @@ EXPORTS = {
                                          i32p, i32p]),
     "cathy_gb300_picard_system": (C.c_int32, [C.c_void_p, C.c_int32, f64p, f64p, f64p,
                                               i32p]),
+    "cathy_gb300_reset": (C.c_int32, [C.c_void_p]),
+    "cathy_gb300_profile": (C.c_int32, [C.c_void_p, C.c_int32, f64p, C.POINTER(C.c_int64),
+                                        f64p]),
     "cathy_gb300_stats": (C.c_int32, [C.c_void_p, f64p, C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "cathy_gb300_symslv": (C.c_int32, [i32p, i32p, i32p, i32p, i32p, i32p, f64p, f64p,

@@ -180,6 +180,19 @@ class Simulation:
                                                _ptr(xt5, f64p), _ptr(dm, i32p)), "picard_system")
         return vals, rhs, xt5, dm
 
+    def reset(self):
+        """Restore every member to its initial condition (device-side)."""
+        check(self.L.cathy_gb300_reset(self.h), "cathy_gb300_reset")
+
+    def profile(self, enable: int = -1):
+        """Live SpMV timing: enable=1 starts (and zeroes) it, 0 stops, -1 reads.
+        Returns (device ms, launches, algorithmic bytes) accumulated so far."""
+        ms, bts = C.c_double(), C.c_double()
+        n = C.c_int64()
+        check(self.L.cathy_gb300_profile(self.h, enable, C.byref(ms), C.byref(n), C.byref(bts)),
+              "cathy_gb300_profile")
+        return ms.value, n.value, bts.value
+
     def stats(self):
         ms = C.c_double()
         la, li, nl = C.c_int64(), C.c_int64(), C.c_int64()

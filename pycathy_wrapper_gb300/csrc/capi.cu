@@ -124,6 +124,17 @@ int32_t cathy_gb300_picard_system(void* h, int32_t m, double* vals, double* rhs,
   return guarded([&]() { return engine_picard_system((Engine*)h, m, vals, rhs, xt5, dirmask); });
 }
 
+int32_t cathy_gb300_reset(void* h) {
+  if (!h) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_reset((Engine*)h); });
+}
+
+int32_t cathy_gb300_profile(void* h, int32_t enable, double* spmv_ms,
+                            int64_t* spmv_launches, double* spmv_bytes) {
+  if (!h) return CATHY_GB300_EINVAL;
+  return engine_profile((Engine*)h, enable, spmv_ms, spmv_launches, spmv_bytes);
+}
+
 int32_t cathy_gb300_stats(void* h, double* gpu_ms, int64_t* launches,
                           int64_t* lin_iters, int64_t* nl_iters) {
   if (!h) return CATHY_GB300_EINVAL;

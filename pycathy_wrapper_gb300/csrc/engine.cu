@@ -410,7 +410,22 @@ __global__ void k_vg(const int32_t* bm_mem, const int32_t* bm_r0,
     CT dse = vg_dse<CT>((CT)pt, (CT)psat, (CT)n, (CT)nd.vgn1[i], (CT)nd.vgpsn[i],
                         (CT)nd.vgnr[i]);
     nd.et2[i] = (double)((CT)pnot * dse);
-    nd.ckrw[i] = (double)vg_kr<CT>((CT)pt, se_c, (CT)nd.vgmr[i], (CT)mm);
+    if constexpr (sizeof(CT) == 8) {
+      nd.ckrw[i] = vg_kr<double>(pt, se_c, nd.vgmr[i], mm);
+    } else {
+      // FP32 relative conductivity in a cancellation-free form of FVGKR:
+      // Se^(1/m) = 1/(1+beta), so 1 - Se^(1/m) = beta/(1+beta) and
+      // 1 - (beta/(1+beta))^m = -expm1(-m*log1p(1/beta)).
+      float kr = 1.0f;
+      if (pt < -1.0e-14) {
+        const float beta = powf(fabsf((float)pt / (float)psat), (float)n);
+        const float sef = expf(-(float)mm * log1pf(beta));
+        const float q = -expm1f(-(float)mm * log1pf(1.0f / beta));
+        kr = sqrtf(sef) * q * q;
+      }
+      nd.ckrw[i] = (double)kr;
+    }
+    (void)se_c;
     nd.sw[i] = sw;
   } else {
     const double se = vg_se<double>(pt, psat, n, mm);
@@ -1285,7 +1300,7 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 // Host view of one member: mesh, inputs and time-stepping state.
 struct MemberHost {
-  HostMesh mesh;
+  std::shared_ptr<HostMesh> meshp = std::make_shared<HostMesh>();
   cathy_parm_t parm;
   double pmin = -5, scf = 0, pondh_min = 1e10;
   // atmospheric series (atmone.f/atmnxt.f/atmbak.f state)
@@ -1365,6 +1380,8 @@ struct Engine {
   std::vector<uint8_t> h_act;
 
   ~Engine() {
+    if (pe0) cudaEventDestroy(pe0);
+    if (pe1) cudaEventDestroy(pe1);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -1383,6 +1400,21 @@ struct Engine {
   template <class MT> void solve_mixed(int itmax, double tol);
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
+  // initial state for reset()
+  std::vector<MemberHost> snap;
+  DBuf<double> s_pnew, s_ptimep, s_atmpot, s_atmact, s_atmold, s_qpnew;
+  DBuf<int8_t> s_ifatm, s_ifatmp;
+  void save_initial();
+  void reset();
+  // live timing of the SpMV launches (CUDA events on the engine stream)
+  bool prof = false;
+  cudaEvent_t pe0 = nullptr, pe1 = nullptr;
+  double prof_ms = 0, prof_bytes = 0;
+  int64_t prof_n = 0;
+  // algorithmic bytes of one SpMV per member: nnz*(s_v+s_i) + (n+1)*s_i is
+  // spmv_bytes (for s_v+s_i = 8) scaled by the value size; 2*n*s_v vectors
+  // (x read, y written) + the fused dot's w read = spmv_bytes_vec * s_v
+  std::vector<double> spmv_bytes, spmv_bytes_vec;
   void bare_init(int n, const std::vector<int32_t>& rowptr,
                  const std::vector<int32_t>& cols, const std::vector<uint8_t>& dm);
 };
@@ -1414,7 +1446,7 @@ void Engine::make_blockmap(BlockMap& bm, int rpb) {
 // read the next atmospheric record (atmone.f READ(IIN6,...))
 static bool atm_read(MemberHost& h, double& t, std::vector<double>& v) {
   if (h.atm_next >= h.natm) return false;
-  const int nnod = h.mesh.nnod;
+  const int nnod = h.meshp->nnod;
   t = h.atm_t[h.atm_next];
   v.assign(nnod, 0.0);
   for (int i = 0; i < nnod; ++i)
@@ -1460,7 +1492,7 @@ void Engine::atm_back(MemberHost& h) {
 // ATMONE (atmone.f) on the host; returns ATMPOT/ATMACT/ATMOLD/IFATM and may
 // clamp PNEW/PTIMEP at PMIN.
 void Engine::atm_setup_member(MemberHost& h, bool) {
-  const int nnod = h.mesh.nnod;
+  const int nnod = h.meshp->nnod;
   for (int k = 1; k <= 3; ++k) h.atminp[k].assign(nnod, 0.0);
   h.atmtim[1] = h.atmtim[2] = 0.0;
   h.htiatm = 0;
@@ -1502,13 +1534,13 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     M[m].reset(new MemberHost());
     MemberHost& h = *M[m];
     h.parm = mem[m].parm;
-    if (!build_mesh(mem[m].dem, iopt, h.mesh)) throw std::string("mesh construction failed");
-    node_off[m + 1] = node_off[m] + h.mesh.n;
-    tet_off[m + 1] = tet_off[m] + h.mesh.nt;
-    nnz_off[m + 1] = nnz_off[m] + (int32_t)h.mesh.nnz();
+    if (!build_mesh(mem[m].dem, iopt, *h.meshp)) throw std::string("mesh construction failed");
+    node_off[m + 1] = node_off[m] + h.meshp->n;
+    tet_off[m + 1] = tet_off[m] + h.meshp->nt;
+    nnz_off[m + 1] = nnz_off[m] + (int32_t)h.meshp->nnz();
   }
   for (int m = 0; m < nmem; ++m) {
-    const HostMesh& g = M[m]->mesh;
+    const HostMesh& g = *M[m]->meshp;
     for (int i = 0; i < g.n; ++i)
       if (g.rowptr[i + 1] - g.rowptr[i] > kGroup)
         throw std::string("matrix row longer than 16 entries");
@@ -1535,7 +1567,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   h_rowptr[0] = 0;
   for (int m = 0; m < nmem; ++m) {
     MemberHost& h = *M[m];
-    const HostMesh& g = h.mesh;
+    const HostMesh& g = *h.meshp;
     const int no = node_off[m], to = tet_off[m], ao = nnz_off[m];
     const cathy_soil_t& S = mem[m].soil;
     const int nzone = S.nzone, nstr = g.nstr;
@@ -1620,11 +1652,11 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   std::vector<double> h_pnew = h_pinit, h_ptimep = h_pinit;
   for (int m = 0; m < nmem; ++m) {
     MemberHost& h = *M[m];
-    const int no = node_off[m], nnod = h.mesh.nnod;
+    const int no = node_off[m], nnod = h.meshp->nnod;
     atm_setup_member(h, true);
     if (h.htiatm == 0) {
       if (h.atmtim[3] <= 0.0)
-        for (int i = 0; i < nnod; ++i) h_atmold[no + i] = h.atminp[3][i] * h.mesh.arenod[i];
+        for (int i = 0; i < nnod; ++i) h_atmold[no + i] = h.atminp[3][i] * h.meshp->arenod[i];
       double t;
       std::vector<double> v;
       while (h.time > h.atmtim[3]) {
@@ -1639,9 +1671,9 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         if (h.atmtim[3] > h.atmtim[2]) {
           double slope = (h.atminp[3][i] - h.atminp[2][i]) / (h.atmtim[3] - h.atmtim[2]);
           if (h.ieto != 0) slope = 0.0;
-          pot = (h.atminp[2][i] + slope * (h.time - h.atmtim[2])) * h.mesh.arenod[i];
+          pot = (h.atminp[2][i] + slope * (h.time - h.atmtim[2])) * h.meshp->arenod[i];
         } else {
-          pot = h.atminp[3][i] * h.mesh.arenod[i];
+          pot = h.atminp[3][i] * h.meshp->arenod[i];
         }
         h_atmpot[no + i] = pot;
       }
@@ -1701,7 +1733,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     auto batch_levels = [&](bool fwd, std::vector<int32_t>& ptr, DBuf<int32_t>& rows) {
       int maxl = 0;
       for (int m = 0; m < nmem; ++m) {
-        const auto& lp = fwd ? M[m]->mesh.lev_f_ptr : M[m]->mesh.lev_b_ptr;
+        const auto& lp = fwd ? M[m]->meshp->lev_f_ptr : M[m]->meshp->lev_b_ptr;
         maxl = std::max(maxl, (int)lp.size() - 1);
       }
       std::vector<int32_t> all;
@@ -1709,8 +1741,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       ptr.assign(maxl + 1, 0);
       for (int l = 0; l < maxl; ++l) {
         for (int m = 0; m < nmem; ++m) {
-          const auto& lp = fwd ? M[m]->mesh.lev_f_ptr : M[m]->mesh.lev_b_ptr;
-          const auto& lr = fwd ? M[m]->mesh.lev_f_rows : M[m]->mesh.lev_b_rows;
+          const auto& lp = fwd ? M[m]->meshp->lev_f_ptr : M[m]->meshp->lev_b_ptr;
+          const auto& lr = fwd ? M[m]->meshp->lev_f_rows : M[m]->meshp->lev_b_rows;
           if (l + 1 < (int)lp.size())
             for (int q = lp[l]; q < lp[l + 1]; ++q) all.push_back(node_off[m] + lr[q]);
         }
@@ -1798,7 +1830,44 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       M[m]->pend = ACT_START;
     }
   }
+  spmv_bytes.assign(nmem, 0.0);
+  spmv_bytes_vec.assign(nmem, 0.0);
+  for (int m = 0; m < nmem; ++m) {
+    const HostMesh& g = *M[m]->meshp;
+    spmv_bytes[m] = 8.0 * (double)g.nnz() + 4.0 * (g.n + 1);
+    spmv_bytes_vec[m] = 3.0 * g.n;
+  }
+  CG_TRY(cudaEventCreate(&pe0));
+  CG_TRY(cudaEventCreate(&pe1));
   CG_TRY(cudaStreamSynchronize(st));
+}
+
+void Engine::save_initial() {
+  snap.clear();
+  for (int m = 0; m < nmem; ++m) snap.push_back(*M[m]);
+  auto cp = [&](DBuf<double>& dst, const double* src) {
+    dst.alloc(N);
+    CG_TRY(cudaMemcpyAsync(dst.p, src, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+  };
+  cp(s_pnew, nd.pnew); cp(s_ptimep, nd.ptimep); cp(s_atmpot, nd.atmpot);
+  cp(s_atmact, nd.atmact); cp(s_atmold, nd.atmold); cp(s_qpnew, nd.qpnew);
+  s_ifatm.alloc(N); s_ifatmp.alloc(N);
+  CG_TRY(cudaMemcpyAsync(s_ifatm.p, nd.ifatm, N, cudaMemcpyDeviceToDevice, st));
+  CG_TRY(cudaMemcpyAsync(s_ifatmp.p, nd.ifatmp, N, cudaMemcpyDeviceToDevice, st));
+  CG_TRY(cudaStreamSynchronize(st));
+}
+
+// Restore every member to its initial condition (device-side copies).
+void Engine::reset() {
+  for (int m = 0; m < nmem; ++m) *M[m] = snap[m];
+  auto cp = [&](double* dst, const DBuf<double>& src) {
+    CG_TRY(cudaMemcpyAsync(dst, src.p, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+  };
+  cp(nd.pnew, s_pnew); cp(nd.ptimep, s_ptimep); cp(nd.atmpot, s_atmpot);
+  cp(nd.atmact, s_atmact); cp(nd.atmold, s_atmold); cp(nd.qpnew, s_qpnew);
+  cp(nd.qpold, s_qpnew);
+  CG_TRY(cudaMemcpyAsync(nd.ifatm, s_ifatm.p, N, cudaMemcpyDeviceToDevice, st));
+  CG_TRY(cudaMemcpyAsync(nd.ifatmp, s_ifatmp.p, N, cudaMemcpyDeviceToDevice, st));
 }
 
 void Engine::push_scalars() {
@@ -1810,7 +1879,7 @@ void Engine::push_scalars() {
     S.pmin = h.pmin; S.omega = h.parm.omega; S.tolswi = h.parm.tolswi;
     S.atm_ta = h.atm_ta; S.atm_tb = h.atm_tb; S.atm_va = h.atm_va; S.atm_vb = h.atm_vb;
     S.atm_mode = h.atm_mode; S.hspatm = h.hspatm; S.ieto = h.ieto; S.nlrelx = h.parm.nlrelx;
-    S.nnod = h.mesh.nnod; S.nstr = h.mesh.nstr; S.iopt = iopt; S.pad = 0;
+    S.nnod = h.meshp->nnod; S.nstr = h.meshp->nstr; S.iopt = iopt; S.pad = 0;
     if (h.atm_nodal_dirty) nodal_dirty = true;
   }
   d_ms.upload(h_ms.data(), nmem, st);
@@ -1818,7 +1887,7 @@ void Engine::push_scalars() {
     for (int m = 0; m < nmem; ++m) {
       MemberHost& h = *M[m];
       if (!h.atm_nodal_dirty) continue;
-      const int no = node_off[m], nnod = h.mesh.nnod;
+      const int no = node_off[m], nnod = h.meshp->nnod;
       if ((int)h.atm_a_nodal.size() == nnod)
         CG_TRY(cudaMemcpyAsync(nd.atm_a + no, h.atm_a_nodal.data(), sizeof(double) * nnod, cudaMemcpyHostToDevice, st));
       if ((int)h.atm_b_nodal.size() == nnod)
@@ -1953,9 +2022,16 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode) {
   check_launch();
   for (int it = 0; it < itmax + 2; ++it) {
     // q = A p, pq = p.q, pr = p.r
+    std::vector<uint8_t> actv;
+    if (prof) {
+      actv.resize(nmem);
+      d_active.download(actv.data(), nmem, st);
+      CG_TRY(cudaEventRecord(pe0, st));
+    }
     k_spmv<MT, VT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_active.p,
         d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N);
     count();
+    if (prof) CG_TRY(cudaEventRecord(pe1, st));
     k_pcg_update_rx<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p,
         d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
     count();
@@ -1971,6 +2047,15 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode) {
     int32_t nact = 0;
     d_nact.download(&nact, 1, st);
     CG_TRY(cudaStreamSynchronize(st));
+    if (prof) {
+      float ms = 0;
+      CG_TRY(cudaEventElapsedTime(&ms, pe0, pe1));
+      prof_ms += ms;
+      prof_n += 1;
+      for (int m = 0; m < nmem; ++m)
+        if (actv[m]) prof_bytes += spmv_bytes[m] * (sizeof(MT) + 4.0) / 8.0 +
+                                   spmv_bytes_vec[m] * (double)sizeof(VT);
+    }
     if (nact == 0) break;
   }
 }
@@ -2257,10 +2342,10 @@ int Engine::macro_iteration() {
       if (a & ACT_START) { h.iterating = true; h.iter = 1; h.nitert = 0; }
       if (h.iterating) { a |= ACT_ITER; niter_members++; itm.push_back(m); }
     } else {
-      a &= (ACT_COMMIT);  // finished members still commit their last step
+      a &= (ACT_COMMIT);  // finished or paused members only commit
     }
     h_act[m] = a;
-    h.pend = 0;
+    h.pend &= (uint8_t)~a;  // bits not executed now stay pending
   }
   push_scalars();
   d_act.upload(h_act.data(), nmem, st);
@@ -2419,6 +2504,7 @@ Engine* engine_create(int nmembers, const cathy_member_t* members,
     e->build(nmembers, members);
     // the first time level: ATMNXT at TIME (cathy_main.f:2938) for every member
     for (int m = 0; m < e->nmem; ++m) e->atm_advance(*e->M[m]);
+    e->save_initial();
   } catch (...) {
     delete e;
     throw;
@@ -2436,6 +2522,7 @@ static int run_until(Engine* e, int target_mode, int max_macro) {
     e->M[m]->paused = false;
   }
   CG_TRY(cudaEventRecord(e->ev0, e->st));
+  int idle = 0;
   for (int it = 0; it < max_macro; ++it) {
     bool any = false;
     for (int m = 0; m < e->nmem; ++m) {
@@ -2444,17 +2531,10 @@ static int run_until(Engine* e, int target_mode, int max_macro) {
       if (h.status == 0 && !h.paused) any = true;
     }
     if (!any) break;
-    e->macro_iteration();
+    if (e->macro_iteration() == 0 && ++idle > 2)
+      throw std::string("no member made progress (internal state error)");
   }
-  // flush pending commits of paused/finished members
-  bool pending = false;
-  for (int m = 0; m < e->nmem; ++m)
-    if (e->M[m]->pend & ACT_COMMIT) pending = true;
-  if (pending) {
-    for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = true;
-    e->macro_iteration();
-    for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = false;
-  }
+  for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = false;
   CG_TRY(cudaEventRecord(e->ev1, e->st));
   CG_TRY(cudaEventSynchronize(e->ev1));
   float ms = 0;
@@ -2478,6 +2558,7 @@ int engine_run(Engine* e, int max_steps, int* nsteps) {
   std::vector<int> start(e->nmem);
   for (int m = 0; m < e->nmem; ++m) start[m] = e->M[m]->steps_done;
   CG_TRY(cudaEventRecord(e->ev0, e->st));
+  int idle = 0;
   for (;;) {
     bool any = false;
     for (int m = 0; m < e->nmem; ++m) {
@@ -2486,14 +2567,8 @@ int engine_run(Engine* e, int max_steps, int* nsteps) {
       if (h.status == 0 && !h.paused) any = true;
     }
     if (!any) break;
-    e->macro_iteration();
-  }
-  bool pending = false;
-  for (int m = 0; m < e->nmem; ++m)
-    if (e->M[m]->pend & ACT_COMMIT) pending = true;
-  if (pending) {
-    for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = true;
-    e->macro_iteration();
+    if (e->macro_iteration() == 0 && ++idle > 2)
+      throw std::string("no member made progress (internal state error)");
   }
   for (int m = 0; m < e->nmem; ++m) {
     e->M[m]->paused = false;
@@ -2510,7 +2585,7 @@ int engine_run(Engine* e, int max_steps, int* nsteps) {
 
 int engine_sizes(Engine* e, int m, int32_t* out5) {
   if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
-  const HostMesh& g = e->M[m]->mesh;
+  const HostMesh& g = *e->M[m]->meshp;
   out5[0] = g.n; out5[1] = g.nt; out5[2] = g.nnod; out5[3] = g.ntri; out5[4] = (int32_t)g.nnz();
   return 0;
 }
@@ -2520,7 +2595,7 @@ int engine_get_state(Engine* e, int m, double* pnew, double* time,
   if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
   MemberHost& h = *e->M[m];
   if (pnew)
-    CG_TRY(cudaMemcpyAsync(pnew, e->nd.pnew + e->node_off[m], sizeof(double) * h.mesh.n,
+    CG_TRY(cudaMemcpyAsync(pnew, e->nd.pnew + e->node_off[m], sizeof(double) * h.meshp->n,
                            cudaMemcpyDeviceToHost, e->st));
   CG_TRY(cudaStreamSynchronize(e->st));
   // the reported time is that of the last accepted step
@@ -2534,7 +2609,7 @@ int engine_set_state(Engine* e, int m, const double* ptimep, double time,
                      double deltat) {
   if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
   MemberHost& h = *e->M[m];
-  const size_t n = h.mesh.n;
+  const size_t n = h.meshp->n;
   CG_TRY(cudaMemcpyAsync(e->nd.pnew + e->node_off[m], ptimep, sizeof(double) * n,
                          cudaMemcpyHostToDevice, e->st));
   CG_TRY(cudaMemcpyAsync(e->nd.ptimep + e->node_off[m], ptimep, sizeof(double) * n,
@@ -2569,7 +2644,7 @@ int engine_get_records(Engine* e, int m, cathy_iter_rec_t* ir, cathy_step_rec_t*
 int engine_get_mesh(Engine* e, int m, double* x, double* y, double* z,
                     int32_t* tetra, int32_t* rowptr, int32_t* cols) {
   if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
-  const HostMesh& g = e->M[m]->mesh;
+  const HostMesh& g = *e->M[m]->meshp;
   if (x) std::memcpy(x, g.x.data(), sizeof(double) * g.n);
   if (y) std::memcpy(y, g.y.data(), sizeof(double) * g.n);
   if (z) std::memcpy(z, g.z.data(), sizeof(double) * g.n);
@@ -2609,8 +2684,8 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   e->check_launch();
   const int no = e->node_off[m];
   const long ao = e->nnz_off[m];
-  const int n = h.mesh.n;
-  const long nnz = h.mesh.nnz();
+  const int n = h.meshp->n;
+  const long nnz = h.meshp->nnz();
   if (mixed) {
     std::vector<float> v(nnz);
     CG_TRY(cudaMemcpyAsync(v.data(), e->d_vals32.p + ao, sizeof(float) * nnz, cudaMemcpyDeviceToHost, e->st));
@@ -2625,6 +2700,23 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   CG_TRY(cudaMemcpyAsync(dm.data(), e->nd.dmask + no, n, cudaMemcpyDeviceToHost, e->st));
   CG_TRY(cudaStreamSynchronize(e->st));
   for (int i = 0; i < n; ++i) dirmask[i] = dm[i];
+  return 0;
+}
+
+int engine_reset(Engine* e) {
+  e->reset();
+  return 0;
+}
+
+int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launches,
+                   double* spmv_bytes) {
+  if (spmv_ms) *spmv_ms = e->prof_ms;
+  if (spmv_launches) *spmv_launches = e->prof_n;
+  if (spmv_bytes) *spmv_bytes = e->prof_bytes;
+  if (enable >= 0) {
+    e->prof = enable != 0;
+    e->prof_ms = 0; e->prof_n = 0; e->prof_bytes = 0;
+  }
   return 0;
 }
 

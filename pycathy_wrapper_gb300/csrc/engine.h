@@ -77,6 +77,9 @@ int engine_get_mesh(Engine* e, int m, double* x, double* y, double* z,
                     int32_t* tetra, int32_t* rowptr, int32_t* cols);
 int engine_picard_system(Engine* e, int m, double* vals, double* rhs,
                          double* xt5, int32_t* dirmask);
+int engine_reset(Engine* e);
+int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launches,
+                   double* spmv_bytes);
 int engine_stats(Engine* e, double* gpu_ms, int64_t* launches,
                  int64_t* lin_iters, int64_t* nl_iters);
 
