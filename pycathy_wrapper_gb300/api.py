@@ -87,7 +87,7 @@ class Simulation:
     """
 
     def __init__(self, cases: Union[Case, Sequence[Case]], precision: int = 0,
-                 device: int = 0, inner_maxit: int = 200, inner_tol: float = 1e-5):
+                 device: int = 0, inner_maxit: int = 200, inner_tol: float = 1e-6):
         self.L = _lib.load()
         self.cases: List[Case] = [cases] if isinstance(cases, Case) else list(cases)
         keep = _Keep()

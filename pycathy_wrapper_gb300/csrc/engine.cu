@@ -55,6 +55,18 @@ __device__ __forceinline__ float group_sum16f(float v) {
   for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+template <class T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -70,6 +82,28 @@ __device__ __forceinline__ void block_accumulate(double (&v)[NV], double* acc) {
   for (int i = 0; i < NV; ++i) {
     double s = warp_sum(v[i]);
     if (lane == 0) sh[i][w] = s;
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double s = (lane < (int)(blockDim.x >> 5)) ? sh[i][lane] : 0.0;
+      s = warp_sum(s);
+      if (lane == 0 && s != 0.0) atomicAdd(acc + i, s);
+    }
+  }
+}
+
+// Block sum of NV values of type T: warp sums in T, cross-warp sum in FP64,
+// one FP64 atomicAdd per value.
+template <class T, int NV>
+__device__ __forceinline__ void block_accumulate_t(T (&v)[NV], double* acc) {
+  __shared__ double sh[NV][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    T s = warp_sum_t<T>(v[i]);
+    if (lane == 0) sh[i][w] = (double)s;
   }
   __syncthreads();
   if (w == 0) {
@@ -590,33 +624,40 @@ k_assemble_newton(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm
 // sparse kernels
 // ============================================================================
 // y = A x with Dirichlet rows as identity; optionally accumulates per-member
-// dot products d0 += x.y and d1 += x.w (w optional).
+// dot products d0 += x.y and d1 += x.w (w optional).  Arithmetic in the
+// vector type VT; per-block sums are promoted to FP64 before the atomics.
 template <class MT, class VT>
 __global__ void __launch_bounds__(kThreads)
 k_spmv(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
        const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
        const MT* vals, const uint8_t* dmask, const VT* x, VT* y, const VT* w,
-       double* acc, int acc_stride) {
+       double* acc, int acc_stride, double* alg_bytes) {
   const int m = bm_mem[blockIdx.x];
   if (!active[m]) return;
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
   const int i = bm_r0[blockIdx.x] + grp;
   const bool rowok = i < bm_r1[blockIdx.x];
-  double s = 0.0;
+  if (alg_bytes && threadIdx.x == 0) {
+    // values + column indices + row pointers + x read + y written (+ w read)
+    const int r0 = bm_r0[blockIdx.x], r1 = bm_r1[blockIdx.x];
+    const double nz = (double)(rowptr[r1] - rowptr[r0]);
+    atomicAdd(alg_bytes, nz * (sizeof(MT) + 4) + (r1 - r0) * (4.0 + (w ? 3.0 : 2.0) * sizeof(VT)));
+  }
+  VT s = 0;
   if (rowok) {
     const int s0 = rowptr[i] + lane;
-    if (s0 < rowptr[i + 1]) s = (double)vals[s0] * (double)x[cols[s0]];
+    if (s0 < rowptr[i + 1]) s = (VT)vals[s0] * x[cols[s0]];
   }
-  s = group_sum16(s);
-  double d[2] = {0.0, 0.0};
+  s = group_sum<VT>(s);
+  VT d[2] = {0, 0};
   if (rowok && lane == 0) {
-    const double xi = (double)x[i];
-    const double yi = dmask[i] ? xi : s;
-    y[i] = (VT)yi;
+    const VT xi = x[i];
+    const VT yi = dmask[i] ? xi : s;
+    y[i] = yi;
     d[0] = xi * yi;
-    if (w) d[1] = xi * (double)w[i];
+    if (w) d[1] = xi * w[i];
   }
-  if (acc) block_accumulate<2>(d, acc + (size_t)m * acc_stride);
+  if (acc) block_accumulate_t<VT, 2>(d, acc + (size_t)m * acc_stride);
 }
 
 // r = b - A x (masked), r zero at Dirichlet rows
@@ -701,6 +742,7 @@ __global__ void k_line_apply(int ncol_rows, const int32_t* crows,
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   bool ok = q < ncol_rows;
   int top = 0, m = 0;
+  VT red_dot = 0;
   if (ok) {
     top = crows[q];
     m = mem[top];
@@ -718,15 +760,27 @@ __global__ void k_line_apply(int ncol_rows, const int32_t* crows,
       cprev = cdown[i];
     }
     VT znext = 0;
-    double dot = 0.0;
+    VT dot = 0;
     for (int k = nl - 1; k >= 0; --k) {
       const int i = top + k * nnod;
       VT zk = (y[k] - cdown[i] * znext) * pinv[i];
       z[i] = zk;
-      if (w) dot += (double)w[i] * (double)zk;
+      if (w) dot += w[i] * zk;
       znext = zk;
     }
-    if (w) atomicAdd(acc + (size_t)m * acc_stride + acc_off, dot);
+    if (w) red_dot = dot;
+  }
+  // warp-level pre-reduction when the whole warp belongs to one member
+  if (w) {
+    const int lane = threadIdx.x & 31;
+    const int m0 = __shfl_sync(0xffffffffu, ok ? m : -1, 0);
+    const bool uni = __all_sync(0xffffffffu, ok && m == m0);
+    if (uni) {
+      const VT sum = warp_sum_t<VT>(red_dot);
+      if (lane == 0) atomicAdd(acc + (size_t)m0 * acc_stride + acc_off, (double)sum);
+    } else if (ok) {
+      atomicAdd(acc + (size_t)m * acc_stride + acc_off, (double)red_dot);
+    }
   }
 }
 
@@ -933,20 +987,20 @@ __global__ void k_pcg_update_rx(const int32_t* bm_mem, const int32_t* bm_r0,
   const int m = bm_mem[blockIdx.x];
   if (!active[m]) return;
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  double d[2] = {0.0, 0.0};
+  VT d[2] = {0, 0};
   if (i < bm_r1[blockIdx.x]) {
-    const double alfa = sc[m * SC_N + SC_PR] / sc[m * SC_N + SC_PQ];
-    const double ri = (double)r[i] - alfa * (double)q[i];
-    r[i] = (VT)ri;
-    x[i] = (VT)((double)x[i] + alfa * (double)p[i]);
+    const VT alfa = (VT)(sc[m * SC_N + SC_PR] / sc[m * SC_N + SC_PQ]);
+    const VT ri = r[i] - alfa * q[i];
+    r[i] = ri;
+    x[i] = x[i] + alfa * p[i];
     if (!dmask[i]) d[0] = ri * ri;
     if (dinv) {
-      const double zi = (double)dinv[i] * ri;
-      z[i] = (VT)zi;
-      d[1] = (double)q[i] * zi;
+      const VT zi = dinv[i] * ri;
+      z[i] = zi;
+      d[1] = q[i] * zi;
     }
   }
-  block_accumulate<2>(d, (double*)sc + (size_t)m * SC_N + SC_RR - 0);
+  block_accumulate_t<VT, 2>(d, (double*)sc + (size_t)m * SC_N + SC_RR);
 }
 
 template <class VT>
@@ -957,8 +1011,8 @@ __global__ void k_pcg_update_p(const int32_t* bm_mem, const int32_t* bm_r0,
   if (!active[m]) return;
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
   if (i >= bm_r1[blockIdx.x]) return;
-  const double beta = -sc[m * SC_N + SC_QZ] / sc[m * SC_N + SC_PQ];
-  p[i] = (VT)((double)z[i] + beta * (double)p[i]);
+  const VT beta = (VT)(-sc[m * SC_N + SC_QZ] / sc[m * SC_N + SC_PQ]);
+  p[i] = z[i] + beta * p[i];
 }
 
 template <class VT>
@@ -969,9 +1023,9 @@ __global__ void k_dot(const int32_t* bm_mem, const int32_t* bm_r0,
   const int m = bm_mem[blockIdx.x];
   if (!active[m]) return;
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  double d[1] = {0.0};
-  if (i < bm_r1[blockIdx.x] && !(mask && mask[i])) d[0] = (double)a[i] * (double)b[i];
-  block_accumulate<1>(d, acc + (size_t)m * acc_stride + acc_off);
+  VT d[1] = {0};
+  if (i < bm_r1[blockIdx.x] && !(mask && mask[i])) d[0] = a[i] * b[i];
+  block_accumulate_t<VT, 1>(d, acc + (size_t)m * acc_stride + acc_off);
 }
 
 template <class VA, class VB>
@@ -1293,6 +1347,250 @@ __global__ void k_flags(int nmem, const uint8_t* act, uint8_t bits, uint8_t* out
   if (m < nmem) out[m] = (act[m] & bits) ? 1 : 0;
 }
 
+
+// ============================================================================
+// FP32 nonlinear-iteration kernels (mixed precision path)
+//
+// FP32 arithmetic with FP64-grade accuracy of the nonlinear residual:
+//  * the stiffness/gravity part of RHSPIC+RHSGRV is evaluated as
+//    -sum_l K_kl (h_l - h_k) with total head h = PTNEW + z held as a float
+//    (hi, lo) pair: P1 stiffness rows sum to zero and K.z equals the gravity
+//    term Kz d_k ivol, so this is the reference's residual, with the
+//    cancelling large terms removed before rounding;
+//  * SWNEW - SWTIMEP is evaluated directly (expm1/log1p form of FVGSE), so
+//    it is accurate relative to its own size;
+//  * head differences (PNEW - PTIMEP, PNEW - POLD) are formed in FP64.
+// ============================================================================
+struct NodalF {
+  float *ckrw, *et1, *et2, *sw, *dsw, *dpsi, *hhi, *hlo, *rhs, *xt5, *pdiff;
+  float *vgn, *vgm, *vgpsat, *vgn1, *vgnr, *vgpsn, *vgpnot, *ss;
+};
+
+// Se(psi) and Se(psi1) - Se(psi0) in FP32 (fvgse.f semantics for the sign
+// test at -1e-14).
+__device__ __forceinline__ float vgf_beta(float psi, float psat, float n) {
+  return powf(fabsf(psi / psat), n);
+}
+__device__ __forceinline__ float vgf_dse(double psi1, double psi0, float psat,
+                                         float n, float m) {
+  const bool u1 = psi1 < -1.0e-14, u0 = psi0 < -1.0e-14;
+  if (!u1 && !u0) return 0.0f;
+  if (u1 && !u0) return expm1f(-m * log1pf(vgf_beta((float)psi1, psat, n)));
+  if (!u1 && u0) return -expm1f(-m * log1pf(vgf_beta((float)psi0, psat, n)));
+  const float b0 = vgf_beta((float)psi0, psat, n);
+  const float r = (float)(psi1 - psi0) / (float)psi0;   // psi1/psi0 - 1 > -1
+  const float db = b0 * expm1f(n * log1pf(r));
+  const float se0 = expf(-m * log1pf(b0));
+  return se0 * expm1f(-m * log1pf(db / (1.0f + b0)));
+}
+
+__global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                         const int32_t* bm_r1, const uint8_t* act, Nodal nd,
+                         NodalF nf, const double* z) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const float psat = nf.vgpsat[i], n = nf.vgn[i], mm = nf.vgm[i], pnot = nf.vgpnot[i];
+  const float rmcp = (float)(nd.vgrmc[i] / nd.pnodi[i]);
+  const double p = nd.pnew[i], pt = nd.ptnew[i], pn = nd.ptimep[i];
+  // Sw at PTNEW (coefficients), dSw = Sw(PNEW) - Sw(PTIMEP) (residual)
+  const float ptf = (float)pt;
+  float se = 1.0f, kr = 1.0f, dse = 0.0f;
+  if (pt < -1.0e-14) {
+    const float beta = vgf_beta(ptf, psat, n);
+    se = expf(-mm * log1pf(beta));
+    const float q = -expm1f(-mm * log1pf(1.0f / beta));
+    kr = sqrtf(se) * q * q;
+    const float b1 = beta + 1.0f, b1r = 1.0f / b1;
+    dse = nf.vgn1[i] * (__powf(fabsf(ptf), nf.vgn1[i]) / nf.vgpsn[i]) *
+          __powf(fabsf(b1), nf.vgnr[i]) * b1r * b1r;
+  }
+  const float sw = pnot * se + rmcp;
+  nf.ckrw[i] = kr;
+  nf.et1[i] = sw * nf.ss[i];
+  nf.et2[i] = pnot * dse;
+  nf.sw[i] = sw;
+  nf.dsw[i] = pnot * vgf_dse(p, pn, psat, n, mm);
+  nf.dpsi[i] = (float)(p - pn);
+  const double h = pt + z[i];
+  const float hh = (float)h;
+  nf.hhi[i] = hh;
+  nf.hlo[i] = (float)(h - (double)hh);
+}
+
+// Row-owned Picard assembly in FP32 (see the block comment above); writes
+// the FP32 LHS, the FP32 residual with BCs (the inner solve's RHS) and XT5.
+__global__ void __launch_bounds__(kThreads)
+k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                      const uint8_t* act, const MemberScal* ms,
+                      const int32_t* rowptr, const int32_t* cols,
+                      const int32_t* inc_ptr, const int32_t* inc, const int4* tet,
+                      const TetRec<float>* rec, Nodal nd, NodalF nf, float* vals,
+                      float lm_d, float lm_o) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  const MemberScal& S = ms[m];
+  const float rdt = (float)(1.0 / S.deltat), th = (float)S.tetaf;
+  int s0 = 0, s1 = 0, col = -1;
+  if (rowok) {
+    s0 = rowptr[i]; s1 = rowptr[i + 1];
+    if (s0 + lane < s1) col = cols[s0 + lane];
+  }
+  float lhs = 0.0f, rpart = 0.0f;
+  float et2i = 0.0f, hhi_i = 0.0f, hlo_i = 0.0f;
+  int p0 = 0, p1 = 0;
+  if (rowok) {
+    et2i = nf.et2[i]; hhi_i = nf.hhi[i]; hlo_i = nf.hlo[i];
+    p0 = inc_ptr[i]; p1 = inc_ptr[i + 1];
+  }
+  for (int p = p0; p < p1; ++p) {
+    const int ek = inc[p];
+    const int e = ek >> 2, k = ek & 3;
+    const int4 t = tet[e];
+    const int tn[4] = {t.x, t.y, t.z, t.w};
+    const TetRec<float> R = rec[e];
+    const float kr = 0.25f * (nf.ckrw[t.x] + nf.ckrw[t.y] + nf.ckrw[t.z] + nf.ckrw[t.w]);
+    const float e1 = 0.25f * (nf.et1[t.x] + nf.et1[t.y] + nf.et1[t.z] + nf.et1[t.w]);
+    const float ve1 = R.vol * e1, ve = R.vpel;
+    int l = -1;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) if (tn[q] == col) l = q;
+    if (l >= 0) {
+      const float lm = (l == k) ? lm_d : lm_o;
+      lhs += th * (kr * R.S[sym_idx(k, l)]) + ve1 * lm * rdt;
+      if (l == k) lhs += ve * lm_d * et2i * rdt;
+    }
+    if (lane < 4) {
+      const int nl = tn[lane];
+      const float lm = (lane == k) ? lm_d : lm_o;
+      const float dh = (nf.hhi[nl] - hhi_i) + (nf.hlo[nl] - hlo_i);
+      rpart -= kr * R.S[sym_idx(k, lane)] * dh +
+               (ve1 * lm * nf.dpsi[nl] + ve * lm * nf.dsw[nl]) * rdt;
+    }
+  }
+  const float rhs = group_sum<float>(rpart);
+  if (!rowok) return;
+  if (col >= 0) vals[s0 + lane] = lhs;
+  if (lane == 0) {
+    nf.xt5[i] = rhs;
+    float b = rhs;
+    if (nd.dmask[i]) {
+      b = 0.0f;
+    } else if (nd.loc[i] < S.nnod && nd.ifatm[i] == 0) {
+      b += (float)(S.tetaf * nd.atmact[i] + (1.0 - S.tetaf) * nd.atmold[i]);
+    }
+    b += (float)nd.qneu[i];
+    nf.rhs[i] = b;
+  }
+}
+
+// PNEW += PDIFF (FP32 correction into FP64 heads) + SHLPIC
+__global__ void k_update_shl_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                                 const int32_t* bm_r1, const uint8_t* act,
+                                 Nodal nd, const float* pdiff) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  double p = nd.pnew[i] + (double)pdiff[i];
+  if (nd.sdir[i]) p = nd.presc[i];
+  else if (nd.dmask[i]) p = nd.pold[i];
+  nd.pnew[i] = p;
+}
+
+// MASBAL + RELAX + NORMS for the FP32 path.  SWNEW/SWTIMEP enter only
+// through dSw = SWNEW - SWTIMEP and their sum (STORMB).
+__global__ void __launch_bounds__(kThreads)
+k_masbal_norms_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                   const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
+                   const int32_t* cols, const float* vals, Nodal nd, NodalF nf,
+                   double* red, double* redmax) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  const MemberScal& S = ms[m];
+  const bool dir = rowok && nd.dmask[i];
+  float sp = 0.0f;
+  if (dir) {
+    const int sl = rowptr[i] + lane;
+    if (sl < rowptr[i + 1]) sp = vals[sl] * nf.pdiff[cols[sl]];
+  }
+  sp = group_sum<float>(sp);
+  double v[RD_STORE1] = {};
+  double pinf = 0.0, finf = 0.0;
+  if (rowok && lane == 0) {
+    const double th = S.tetaf, thr = 1.0 / th;
+    const bool surf = nd.loc[i] < S.nnod;
+    if (dir) {
+      const double scr = (double)sp - (double)nf.xt5[i];
+      if (nd.sdir[i]) {
+        const double qn = (scr - (1.0 - th) * nd.qpold[i]) * thr;
+        nd.qpnew[i] = qn;
+        if (qn > 0.0) v[RD_NDIN] += qn; else v[RD_NDOUT] += qn;
+      } else if (surf) {
+        nd.atmact[i] = (scr - (1.0 - th) * nd.atmold[i]) * thr;
+      }
+    }
+    if (surf && nd.ifatm[i] != -1) {
+      const double aa = nd.atmact[i];
+      if (nd.ifatm[i] == 1 || nd.ifatm[i] == 2) {
+        if (aa > 0.0) v[RD_ADIN] += aa; else v[RD_ADOUT] += aa;
+      } else {
+        if (aa > 0.0) v[RD_ANIN] += aa; else v[RD_ANOUT] += aa;
+      }
+    }
+    const double p = nd.pnew[i];
+    if (S.deltat < 1.0e15) {
+      const float sw = nf.sw[i], dsw = nf.dsw[i];
+      const float dp = (float)(p - nd.ptimep[i]);
+      v[RD_DSTORE] = nd.volnod[i] * (double)(nf.ss[i] * (2.0f * sw - dsw) * 0.5f * dp +
+                                             (float)nd.pnodi[i] * dsw);
+    }
+    double pn = p;
+    if (S.nlrelx == 1) {
+      pn = S.omega * p + (1.0 - S.omega) * nd.pold[i];
+      nd.pnew[i] = pn;
+    }
+    const double diff = pn - nd.pold[i];
+    v[RD_PL2] = diff * diff;
+    const double b = nf.rhs[i];
+    v[RD_FL2] = b * b;
+    pinf = fabs(diff);
+    finf = fabs(b);
+  }
+  block_accumulate<RD_STORE1>(v, red + (size_t)m * RD_NUM);
+  __shared__ double shm[2][kThreads / 32];
+  const int wl = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double a = warp_max(pinf), b = warp_max(finf);
+  if (wl == 0) { shm[0][w] = a; shm[1][w] = b; }
+  __syncthreads();
+  if (w == 0) {
+    a = wl < (int)(blockDim.x >> 5) ? shm[0][wl] : 0.0;
+    b = wl < (int)(blockDim.x >> 5) ? shm[1][wl] : 0.0;
+    a = warp_max(a);
+    b = warp_max(b);
+    if (wl == 0) {
+      atomic_max_nonneg(redmax + (size_t)m * 2, a);
+      atomic_max_nonneg(redmax + (size_t)m * 2 + 1, b);
+    }
+  }
+}
+
+// FP32 copies of the nodal van Genuchten parameters (after CHPARM)
+__global__ void k_params_f32(int n, Nodal nd, NodalF nf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  nf.vgn[i] = (float)nd.vgn[i]; nf.vgm[i] = (float)nd.vgm[i]; nf.vgpsat[i] = (float)nd.vgpsat[i];
+  nf.vgn1[i] = (float)nd.vgn1[i]; nf.vgnr[i] = (float)nd.vgnr[i]; nf.vgpsn[i] = (float)nd.vgpsn[i];
+  nf.vgpnot[i] = (float)nd.vgpnot[i]; nf.ss[i] = (float)nd.snodi[i];
+}
+
 // ============================================================================
 // host side
 // ============================================================================
@@ -1350,6 +1648,8 @@ struct Engine {
   // device buffers
   DBuf<int32_t> d_mem, d_loc, d_node_off;
   DBuf<double> d_nodal[48];
+  DBuf<float> d_nodf[20];
+  NodalF nf{};
   DBuf<uint8_t> d_sdir, d_dmask, d_act, d_active, d_switch, d_mask2, d_outer;
   DBuf<int8_t> d_ifatm, d_ifatmp;
   DBuf<int4> d_tet;
@@ -1380,6 +1680,7 @@ struct Engine {
   std::vector<uint8_t> h_act;
 
   ~Engine() {
+    for (auto& ev : pev) cudaEventDestroy(ev);
     if (pe0) cudaEventDestroy(pe0);
     if (pe1) cudaEventDestroy(pe1);
     if (ev0) cudaEventDestroy(ev0);
@@ -1396,8 +1697,30 @@ struct Engine {
   void push_scalars();
   int macro_iteration();
   void picard_or_newton_iteration(const std::vector<int>& itm);
-  template <class MT, class VT> void solve_pcg(int itmax, double tol, bool ref_mode);
-  template <class MT> void solve_mixed(int itmax, double tol);
+  template <class MT, class VT> void solve_pcg(int itmax, double tol, bool ref_mode, int chk = 1);
+  DBuf<int32_t> d_nact_dummy;
+  DBuf<double> d_prof_bytes;
+  std::vector<cudaEvent_t> pev;
+  int pev_used = 0;
+  void prof_begin() {
+    if (pev_used * 2 + 2 > (int)pev.size()) prof_flush();
+    CG_TRY(cudaEventRecord(pev[2 * pev_used], st));
+  }
+  void prof_end() {
+    CG_TRY(cudaEventRecord(pev[2 * pev_used + 1], st));
+    pev_used++;
+  }
+  void prof_flush() {
+    if (!pev_used) return;
+    CG_TRY(cudaEventSynchronize(pev[2 * pev_used - 1]));
+    for (int u = 0; u < pev_used; ++u) {
+      float ms = 0;
+      CG_TRY(cudaEventElapsedTime(&ms, pev[2 * u], pev[2 * u + 1]));
+      prof_ms += ms;
+      prof_n += 1;
+    }
+    pev_used = 0;
+  }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
   // initial state for reset()
@@ -1789,6 +2112,15 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         d_tetsoil.p, d_tab[0].p, d_tab[1].p, d_tab[2].p, P(ND_PNODI), d_rec32.p, P(ND_VOLNOD), nullptr);
   }
   check_launch();
+  if (precision == 1 && iopt == 1) {
+    for (int k = 0; k < 19; ++k) { d_nodf[k].alloc(N); d_nodf[k].zero(st); }
+    float** fp[19] = {&nf.ckrw, &nf.et1, &nf.et2, &nf.sw, &nf.dsw, &nf.dpsi, &nf.hhi, &nf.hlo,
+                      &nf.rhs, &nf.xt5, &nf.pdiff, &nf.vgn, &nf.vgm, &nf.vgpsat, &nf.vgn1,
+                      &nf.vgnr, &nf.vgpsn, &nf.vgpnot, &nf.ss};
+    for (int k = 0; k < 19; ++k) *fp[k] = d_nodf[k].p;
+    k_params_f32<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, nd, nf);
+    check_launch();
+  }
   // matrix and solver workspace
   if (precision == 0) { d_vals64.alloc(NNZ); d_vals64.zero(st); }
   else { d_vals32.alloc(NNZ); d_vals32.zero(st); d_vals64.alloc(0); }
@@ -1839,6 +2171,11 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   }
   CG_TRY(cudaEventCreate(&pe0));
   CG_TRY(cudaEventCreate(&pe1));
+  pev.resize(256);
+  for (auto& ev : pev) CG_TRY(cudaEventCreate(&ev));
+  d_nact_dummy.alloc(1);
+  d_prof_bytes.alloc(1);
+  d_prof_bytes.zero(st);
   CG_TRY(cudaStreamSynchronize(st));
 }
 
@@ -1987,10 +2324,12 @@ static void precond_setup(Engine& E, int pc, const MT* vals, FT* F, VT* dinv,
 }
 
 // Batched PCG with the reference's GRADDP recurrences (x0 = M^-1 b).
-// Solves A x = b for members with d_active set; b = w[0] (VT), x = w[1].
-// ref_mode: b is the FP64 RHS (nd.rhs) and x is nd.pdiff.
+// ref_mode: b is the system RHS (nd.rhs / nf.rhs), x the head correction
+// (nd.pdiff / nf.pdiff); otherwise b = w[0], x = w[1].  Converged members are
+// masked on the device after every iteration; the host reads the number of
+// active members every `chk` iterations.
 template <class MT, class VT>
-void Engine::solve_pcg(int itmax, double tol, bool ref_mode) {
+void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk) {
   const MT* vals;
   if constexpr (sizeof(MT) == 8) vals = (const MT*)d_vals64.p; else vals = (const MT*)d_vals32.p;
   VT *b, *x, *r, *p, *q, *z, *tmp, *dinv, *linv = nullptr, *lc = nullptr;
@@ -2001,7 +2340,8 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode) {
     r = w64[2].p; p = w64[3].p; q = w64[4].p; z = w64[5].p; tmp = w64[6].p; dinv = w64[7].p;
     F = d_F64.p; linv = d_linv64.p; lc = d_lc64.p;
   } else {
-    b = w32[0].p; x = w32[1].p; r = w32[2].p; p = w32[3].p; q = w32[4].p; z = w32[5].p;
+    b = ref_mode ? nf.rhs : w32[0].p; x = ref_mode ? nf.pdiff : w32[1].p;
+    r = w32[2].p; p = w32[3].p; q = w32[4].p; z = w32[5].p;
     tmp = w32[6].p; dinv = w32[7].p; F = d_F32.p; linv = d_linv32.p; lc = d_lc32.p;
   }
   const int pc = precond;
@@ -2020,18 +2360,15 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode) {
   std::vector<int32_t> ones(nmem, 1);
   d_niter.upload(ones.data(), nmem, st);
   check_launch();
+  if (chk < 1) chk = 1;
   for (int it = 0; it < itmax + 2; ++it) {
     // q = A p, pq = p.q, pr = p.r
-    std::vector<uint8_t> actv;
-    if (prof) {
-      actv.resize(nmem);
-      d_active.download(actv.data(), nmem, st);
-      CG_TRY(cudaEventRecord(pe0, st));
-    }
+    if (prof) prof_begin();
     k_spmv<MT, VT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_active.p,
-        d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N);
+        d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N,
+        prof ? d_prof_bytes.p : nullptr);
     count();
-    if (prof) CG_TRY(cudaEventRecord(pe1, st));
+    if (prof) prof_end();
     k_pcg_update_rx<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p,
         d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
     count();
@@ -2039,116 +2376,19 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode) {
     k_pcg_update_p<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p,
         d_sc.p, p, z);
     count();
-    CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
+    if (it % chk == 0) CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
     k_krylov_decide<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_active.p, d_sc.p, d_niter.p, itmax,
-        tol, 0, d_nact.p);
+        tol, 0, (it % chk == chk - 1 || it == itmax + 1) ? d_nact.p : d_nact_dummy.p);
     count();
     check_launch();
-    int32_t nact = 0;
-    d_nact.download(&nact, 1, st);
-    CG_TRY(cudaStreamSynchronize(st));
-    if (prof) {
-      float ms = 0;
-      CG_TRY(cudaEventElapsedTime(&ms, pe0, pe1));
-      prof_ms += ms;
-      prof_n += 1;
-      for (int m = 0; m < nmem; ++m)
-        if (actv[m]) prof_bytes += spmv_bytes[m] * (sizeof(MT) + 4.0) / 8.0 +
-                                   spmv_bytes_vec[m] * (double)sizeof(VT);
-    }
-    if (nact == 0) break;
-  }
-}
-
-
-// ---- mixed precision: FP32 inner PCG inside FP64 iterative refinement ----
-// per member: rr = |r|^2 (into red2[m*2]), bb = |b|^2 (red2[m*2+1])
-__global__ void k_ref_decide(int nmem, uint8_t* outer, const double* red2,
-                             double* scale, double tol, int round, int maxround,
-                             int32_t* nact) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  int a = 0;
-  if (m < nmem && outer[m]) {
-    const double rr = red2[2 * m], bb = red2[2 * m + 1];
-    const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
-    if (rel > tol && rr > 0.0 && round < maxround) {
-      scale[m] = 1.0 / sqrt(rr);
-      a = 1;
-    } else {
-      outer[m] = 0;
+    if (it % chk == chk - 1 || it == itmax + 1) {
+      int32_t nact = 0;
+      d_nact.download(&nact, 1, st);
+      CG_TRY(cudaStreamSynchronize(st));
+      if (prof) prof_flush();
+      if (nact == 0) break;
     }
   }
-  if (m < nmem) atomicAdd(nact, a);
-}
-__global__ void k_inv_scale(int nmem, const double* scale, double* inv) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m < nmem) inv[m] = 1.0 / scale[m];
-}
-
-template <class MT>
-void Engine::solve_mixed(int itmax, double tol) {
-  const MT* vals = (const MT*)d_vals32.p;
-  double* x = nd.pdiff;
-  double* r = w64[0].p;
-  DBuf<double>& red2 = w64[1];  // per member (rr, bb) in the first 2*nmem entries
-  DBuf<double>& scale = w64[2];
-  DBuf<double>& inv = w64[3];
-  // outer mask = members iterating
-  DBuf<uint8_t>& outer = d_outer;
-  CG_TRY(cudaMemcpyAsync(outer.p, d_active.p, nmem, cudaMemcpyDeviceToDevice, st));
-  CG_TRY(cudaMemsetAsync(x, 0, sizeof(double) * N, st));
-  // r = b ; bb
-  CG_TRY(cudaMemsetAsync(red2.p, 0, sizeof(double) * 2 * nmem, st));
-  k_copy_cast<double, double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p,
-      outer.p, nd.rhs, r, nullptr, 0);
-  k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, nd.rhs,
-      nd.rhs, d_dmask.p, red2.p, 2, 1);
-  k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, r, r,
-      d_dmask.p, red2.p, 2, 0);
-  count(3);
-  std::vector<int32_t> tot(nmem, 0), its(nmem);
-  const int maxround = 4;
-  for (int round = 0; round <= maxround; ++round) {
-    CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
-    k_ref_decide<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, outer.p, red2.p, scale.p, tol, round,
-                                                  maxround, d_nact.p);
-    count();
-    int32_t nact = 0;
-    d_nact.download(&nact, 1, st);
-    CG_TRY(cudaStreamSynchronize(st));
-    if (!nact) break;
-    // b32 = r * scale ; inner solve
-    k_copy_cast<double, float><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p,
-        outer.p, r, w32[0].p, scale.p, 1);
-    CG_TRY(cudaMemcpyAsync(d_active.p, outer.p, nmem, cudaMemcpyDeviceToDevice, st));
-    count();
-    solve_pcg<MT, float>(opts.inner_maxit, opts.inner_tol, false);
-    d_niter.download(its.data(), nmem, st);
-    // x += e / scale ; r = b - A x
-    k_inv_scale<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, scale.p, inv.p);
-    k_axpy_ref<float><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, x,
-        w32[1].p, inv.p, 1);
-    CG_TRY(cudaMemsetAsync(red2.p, 0, sizeof(double) * 2 * nmem, st));
-    k_resid<MT, double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, outer.p,
-        d_rowptr.p, d_cols.p, vals, d_dmask.p, x, nd.rhs, r, red2.p, 2);
-    k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, outer.p, nd.rhs,
-        nd.rhs, d_dmask.p, red2.p, 2, 1);
-    count(4);
-    check_launch();
-    CG_TRY(cudaStreamSynchronize(st));
-    std::vector<uint8_t> oa(nmem);
-    outer.download(oa.data(), nmem, st);
-    CG_TRY(cudaStreamSynchronize(st));
-    for (int m = 0; m < nmem; ++m) if (oa[m]) tot[m] += its[m];
-  }
-  d_niter.upload(tot.data(), nmem, st);
-  // error estimate for the records: relative FP64 residual
-  std::vector<double> rr(2 * nmem);
-  red2.download(rr.data(), 2 * nmem, st);
-  CG_TRY(cudaStreamSynchronize(st));
-  std::vector<double> scv((size_t)nmem * SC_N, 0.0);
-  for (int m = 0; m < nmem; ++m) scv[(size_t)m * SC_N + SC_ERR] = rr[2 * m + 1] > 0 ? std::sqrt(rr[2 * m] / rr[2 * m + 1]) : 0.0;
-  d_sc.upload(scv.data(), scv.size(), st);
 }
 
 // ---- BiCGSTAB (Newton), FP64, GCSTAS (isolv 0) / GCSTAD (isolv -5) ----
@@ -2183,7 +2423,7 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
   };
   auto spmv = [&](const double* in, double* out) {
     k_spmv<double, double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
-        d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out, nullptr, nullptr, 0);
+        d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out, nullptr, nullptr, 0, nullptr);
     count();
   };
   auto applyB = [&](const double* in, double* out) {
@@ -2292,31 +2532,43 @@ __global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
 void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
   (void)itm;
   const bool mixed = (precision == 1 && iopt == 1);
-  if (mixed)
-    k_vg<float><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 0);
-  else
+  const cathy_parm_t& P0 = M[0]->parm;
+  if (mixed) {
+    // FP32 path: the Picard loop is the FP64 refinement loop (its residual is
+    // FP64-grade, see the FP32 kernels); the inner FP32 PCG solves each
+    // correction to opts.inner_tol.
+    k_vg_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd, nf,
+                                            d_nodal[ND_Z].p);
+    k_assemble_picard_f32<<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
+        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, d_rec32.p, nd, nf,
+        d_vals32.p, (float)lm_d, (float)lm_o);
+    k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
+    count(3);
+    check_launch();
+    solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
+                            std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1);
+    k_update_shl_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd,
+                                                    nf.pdiff);
+    count();
+  } else {
     k_vg<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd,
                                                 iopt == 2);
-  count();
-  check_launch();
-  if (mixed) assemble<float>(); else assemble<double>();
-  k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
-  count();
-  const cathy_parm_t& P0 = M[0]->parm;
-  if (iopt == 1) {
-    if (!mixed) solve_pcg<double, double>(P0.itmxcg, P0.tolcg, true);
-    else solve_mixed<float>(P0.itmxcg, P0.tolcg);
-  } else {
-    solve_bicgstab(P0.isolv, P0.itmxcg, P0.tolcg);
+    count();
+    check_launch();
+    assemble<double>();
+    k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
+    count();
+    if (iopt == 1) solve_pcg<double, double>(P0.itmxcg, P0.tolcg, true, 1);
+    else solve_bicgstab(P0.isolv, P0.itmxcg, P0.tolcg);
+    k_update_shl<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd);
+    count();
   }
-  k_update_shl<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd);
-  count();
   CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
   CG_TRY(cudaMemsetAsync(d_redmax.p, 0, sizeof(double) * nmem * 2, st));
   CG_TRY(cudaMemsetAsync(d_ikmax.p, 0, sizeof(int32_t) * nmem, st));
   if (mixed)
-    k_masbal_norms<float><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
-        d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, d_red.p, d_redmax.p, 0);
+    k_masbal_norms_f32<<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+        d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf, d_red.p, d_redmax.p);
   else
     k_masbal_norms<double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
         d_ms.p, d_rowptr.p, d_cols.p, d_vals64.p, nd, d_red.p, d_redmax.p, iopt == 2);
@@ -2379,7 +2631,11 @@ int Engine::macro_iteration() {
     const int niter = nit[m];
     h.itlin += niter; h.nitert += niter;
     lin_iters += niter;
-    const bool lsfail = niter >= P.itmxcg;
+    // FP32 inner solves stop at their own iteration cap; they count as a
+    // linear-solver failure only if the residual did not fall below 1e-3
+    const bool lsfail = (precision == 1 && iopt == 1)
+        ? (niter >= std::min(P.itmxcg, opts.inner_maxit) && scv[(size_t)m * SC_N + SC_ERR] > 1e-3)
+        : (niter >= P.itmxcg);
     const double pl2 = std::sqrt(R[RD_PL2]), fl2 = std::sqrt(R[RD_FL2]);
     const double pinf = redmax[2 * m], finf = redmax[2 * m + 1];
     cathy_iter_rec_t rec;
@@ -2675,8 +2931,11 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   e->d_act.upload(act.data(), e->nmem, e->st);
   const bool mixed = (e->precision == 1 && e->iopt == 1);
   if (mixed) {
-    k_vg<float><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0);
-    e->assemble<float>();
+    k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->nd, e->nf,
+                                                  e->d_nodal[ND_Z].p);
+    k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
+        e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_tet.p,
+        e->d_rec32.p, e->nd, e->nf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o);
   } else {
     k_vg<double><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->iopt == 2);
     e->assemble<double>();
@@ -2694,8 +2953,16 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   } else {
     CG_TRY(cudaMemcpyAsync(vals, e->d_vals64.p + ao, sizeof(double) * nnz, cudaMemcpyDeviceToHost, e->st));
   }
-  CG_TRY(cudaMemcpyAsync(rhs, e->nd.rhs + no, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
-  CG_TRY(cudaMemcpyAsync(xt5, e->nd.xt5 + no, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+  if (mixed) {
+    std::vector<float> r(n), x(n);
+    CG_TRY(cudaMemcpyAsync(r.data(), e->nf.rhs + no, sizeof(float) * n, cudaMemcpyDeviceToHost, e->st));
+    CG_TRY(cudaMemcpyAsync(x.data(), e->nf.xt5 + no, sizeof(float) * n, cudaMemcpyDeviceToHost, e->st));
+    CG_TRY(cudaStreamSynchronize(e->st));
+    for (int i = 0; i < n; ++i) { rhs[i] = r[i]; xt5[i] = x[i]; }
+  } else {
+    CG_TRY(cudaMemcpyAsync(rhs, e->nd.rhs + no, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+    CG_TRY(cudaMemcpyAsync(xt5, e->nd.xt5 + no, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+  }
   std::vector<uint8_t> dm(n);
   CG_TRY(cudaMemcpyAsync(dm.data(), e->nd.dmask + no, n, cudaMemcpyDeviceToHost, e->st));
   CG_TRY(cudaStreamSynchronize(e->st));
@@ -2710,12 +2977,21 @@ int engine_reset(Engine* e) {
 
 int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launches,
                    double* spmv_bytes) {
+  e->prof_flush();
+  if (e->d_prof_bytes.p) {
+    e->d_prof_bytes.download(&e->prof_bytes, 1, e->st);
+    CG_TRY(cudaStreamSynchronize(e->st));
+  }
   if (spmv_ms) *spmv_ms = e->prof_ms;
   if (spmv_launches) *spmv_launches = e->prof_n;
   if (spmv_bytes) *spmv_bytes = e->prof_bytes;
   if (enable >= 0) {
     e->prof = enable != 0;
     e->prof_ms = 0; e->prof_n = 0; e->prof_bytes = 0;
+    if (e->d_prof_bytes.p) {
+      e->d_prof_bytes.zero(e->st);
+      CG_TRY(cudaStreamSynchronize(e->st));
+    }
   }
   return 0;
 }
@@ -2783,7 +3059,7 @@ void Engine::bare_init(int n, const std::vector<int32_t>& rowptr,
   nd.dmask = d_dmask.p;
   d_act.alloc(1); d_active.alloc(1); d_ms.alloc(1);
   d_sc.alloc(SC_N); d_sc.zero(st);
-  d_niter.alloc(1); d_nact.alloc(1);
+  d_niter.alloc(1); d_nact.alloc(1); d_nact_dummy.alloc(1);
   make_blockmap(bm1, kThreads);
   make_blockmap(bm16, kRowsPerBlock16);
   uint8_t one = 1, it = ACT_ITER;
