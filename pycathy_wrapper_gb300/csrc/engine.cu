@@ -366,7 +366,7 @@ __global__ void k_start_surface(int nsurf_rows, const int32_t* srows,
 // phase 1 (after the surface kernel): Dirichlet mask, START / NEXT updates.
 __global__ void k_start_nodes(const int32_t* bm_mem, const int32_t* bm_r0,
                               const int32_t* bm_r1, const uint8_t* act,
-                              const MemberScal* ms, Nodal nd, int phase) {
+                              const MemberScal* ms, Nodal nd, int phase, int need_sw) {
   const int m = bm_mem[blockIdx.x];
   const uint8_t a = act[m];
   if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START | ACT_NEXT))) return;
@@ -393,18 +393,20 @@ __global__ void k_start_nodes(const int32_t* bm_mem, const int32_t* bm_r0,
   }
   if (a & ACT_START) {
     const double p = nd.pnew[i];
-    const double pt = th * p + (1.0 - th) * nd.ptimep[i];
+    const double pt = (th == 1.0) ? p : th * p + (1.0 - th) * nd.ptimep[i];
     nd.pold[i] = p;
     nd.ptnew[i] = pt;
     nd.ptold[i] = pt;
-    const double tp = nd.ptimep[i];
-    nd.swtimep[i] = nd.vgpnot[i] * vg_se<double>(tp, nd.vgpsat[i], nd.vgn[i], nd.vgm[i]) +
-                    nd.vgrmc[i] / nd.pnodi[i];
+    if (need_sw) {
+      const double tp = nd.ptimep[i];
+      nd.swtimep[i] = nd.vgpnot[i] * vg_se<double>(tp, nd.vgpsat[i], nd.vgn[i], nd.vgm[i]) +
+                      nd.vgrmc[i] / nd.pnodi[i];
+    }
   } else if (a & ACT_NEXT) {
     const double p = nd.pnew[i];
     nd.pold[i] = p;
     nd.ptold[i] = nd.ptnew[i];
-    nd.ptnew[i] = th * p + (1.0 - th) * nd.ptimep[i];
+    nd.ptnew[i] = (th == 1.0) ? p : th * p + (1.0 - th) * nd.ptimep[i];
   }
 }
 
@@ -672,19 +674,19 @@ k_resid(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
   const int i = bm_r0[blockIdx.x] + grp;
   const bool rowok = i < bm_r1[blockIdx.x];
-  double s = 0.0;
+  VT s = 0;
   if (rowok) {
     const int s0 = rowptr[i] + lane;
-    if (s0 < rowptr[i + 1]) s = (double)vals[s0] * (double)x[cols[s0]];
+    if (s0 < rowptr[i + 1]) s = (VT)vals[s0] * x[cols[s0]];
   }
-  s = group_sum16(s);
-  double d[1] = {0.0};
+  s = group_sum<VT>(s);
+  VT d[1] = {0};
   if (rowok && lane == 0) {
-    double ri = dmask[i] ? 0.0 : (double)b[i] - s;
-    r[i] = (VT)ri;
+    const VT ri = dmask[i] ? (VT)0 : b[i] - s;
+    r[i] = ri;
     d[0] = ri * ri;
   }
-  if (acc) block_accumulate<1>(d, acc + (size_t)m * acc_stride);
+  if (acc) block_accumulate_t<VT, 1>(d, acc + (size_t)m * acc_stride);
 }
 
 // ---- preconditioners ---------------------------------------------------
@@ -1284,12 +1286,14 @@ k_masbal_norms(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1
 // IKMAX = largest node index attaining PINF (norms.f uses .GE.)
 __global__ void k_ikmax(const int32_t* bm_mem, const int32_t* bm_r0,
                         const int32_t* bm_r1, const uint8_t* act, Nodal nd,
-                        const double* redmax, int32_t* ikmax) {
+                        const double* redmax, int32_t* ikmax, int f32) {
   const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
   if (i >= bm_r1[blockIdx.x]) return;
-  if (fabs(nd.pnew[i] - nd.pold[i]) == redmax[(size_t)m * 2]) atomicMax(ikmax + m, nd.loc[i]);
+  const bool hit = f32 ? (fabsf((float)(nd.pnew[i] - nd.pold[i])) == (float)redmax[(size_t)m * 2])
+                       : (fabs(nd.pnew[i] - nd.pold[i]) == redmax[(size_t)m * 2]);
+  if (hit) atomicMax(ikmax + m, nd.loc[i]);
 }
 
 // per member: PNEW(IKMAX), POLD(IKMAX) gathered for the host
@@ -1364,6 +1368,7 @@ __global__ void k_flags(int nmem, const uint8_t* act, uint8_t bits, uint8_t* out
 struct NodalF {
   float *ckrw, *et1, *et2, *sw, *dsw, *dpsi, *hhi, *hlo, *rhs, *xt5, *pdiff;
   float *vgn, *vgm, *vgpsat, *vgn1, *vgnr, *vgpsn, *vgpnot, *ss;
+  float *rmcp, *bcf, *qneu, *volnod, *pnodi;
 };
 
 // Se(psi) and Se(psi1) - Se(psi0) in FP32 (fvgse.f semantics for the sign
@@ -1392,7 +1397,7 @@ __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
   if (i >= bm_r1[blockIdx.x]) return;
   const float psat = nf.vgpsat[i], n = nf.vgn[i], mm = nf.vgm[i], pnot = nf.vgpnot[i];
-  const float rmcp = (float)(nd.vgrmc[i] / nd.pnodi[i]);
+  const float rmcp = nf.rmcp[i];
   const double p = nd.pnew[i], pt = nd.ptnew[i], pn = nd.ptimep[i];
   // Sw at PTNEW (coefficients), dSw = Sw(PNEW) - Sw(PTIMEP) (residual)
   const float ptf = (float)pt;
@@ -1419,72 +1424,257 @@ __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
   nf.hlo[i] = (float)(h - (double)hh);
 }
 
-// Row-owned Picard assembly in FP32 (see the block comment above); writes
-// the FP32 LHS, the FP32 residual with BCs (the inner solve's RHS) and XT5.
+// ---- compensated FP32 sums (TwoSum) for the mass-balance reductions ----
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b.hi - bb);
+  return FF{s, err + a.lo + b.lo};
+}
+// Block sum of NV compensated values, one FP64 atomic per value.
+template <int NV>
+__device__ __forceinline__ void block_accumulate_ff(FF (&v)[NV], double* acc) {
+  __shared__ float shh[NV][kThreads / 32], shl[NV][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    FF s = v[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      FF t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
+      s = ff_add(s, t);
+    }
+    if (lane == 0) { shh[i][w] = s.hi; shl[i][w] = s.lo; }
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      FF s{lane < nw ? shh[i][lane] : 0.0f, lane < nw ? shl[i][lane] : 0.0f};
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        FF t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
+        s = ff_add(s, t);
+      }
+      if (lane == 0 && (s.hi != 0.0f || s.lo != 0.0f))
+        atomicAdd(acc + i, (double)s.hi + (double)s.lo);
+    }
+  }
+}
+
+// Row-owned Picard assembly in FP32.  One 16-lane group per row; the lanes
+// take the row's incident elements in parallel (lane j: incidences j, j+16,
+// ...), compute each element's four local LHS entries and RHS terms, and the
+// slot owners then add the contributions in a fixed order (deterministic,
+// no atomics).  RHS = -sum K (h_l - h_k) - mass terms, see the FP32 block
+// comment; BC fluxes come precomputed in FP32 (bcf).
 __global__ void __launch_bounds__(kThreads)
 k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
                       const uint8_t* act, const MemberScal* ms,
                       const int32_t* rowptr, const int32_t* cols,
                       const int32_t* inc_ptr, const int32_t* inc, const int4* tet,
-                      const TetRec<float>* rec, Nodal nd, NodalF nf, float* vals,
-                      float lm_d, float lm_o) {
+                      const TetRec<float>* rec, const uint8_t* dmask, NodalF nf,
+                      const float* bcf, float* vals, float lm_d, float lm_o) {
   const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
+  __shared__ int scol[kRowsPerBlock16][kGroup];
+  __shared__ float sval[kRowsPerBlock16][kGroup * 4];
+  __shared__ int8_t sidx[kRowsPerBlock16][kGroup * 4];
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
   const int i = bm_r0[blockIdx.x] + grp;
   const bool rowok = i < bm_r1[blockIdx.x];
   const MemberScal& S = ms[m];
-  const float rdt = (float)(1.0 / S.deltat), th = (float)S.tetaf;
-  int s0 = 0, s1 = 0, col = -1;
+  const float rdt = (float)S.deltat_r, th = (float)S.tetaf;
+  int s0 = 0, rlen = 0, p0 = 0, p1 = 0;
+  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f;
   if (rowok) {
-    s0 = rowptr[i]; s1 = rowptr[i + 1];
-    if (s0 + lane < s1) col = cols[s0 + lane];
+    s0 = rowptr[i];
+    rlen = rowptr[i + 1] - s0;
+    p0 = inc_ptr[i];
+    p1 = inc_ptr[i + 1];
+    et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
   }
-  float lhs = 0.0f, rpart = 0.0f;
-  float et2i = 0.0f, hhi_i = 0.0f, hlo_i = 0.0f;
-  int p0 = 0, p1 = 0;
-  if (rowok) {
-    et2i = nf.et2[i]; hhi_i = nf.hhi[i]; hlo_i = nf.hlo[i];
-    p0 = inc_ptr[i]; p1 = inc_ptr[i + 1];
-  }
-  for (int p = p0; p < p1; ++p) {
-    const int ek = inc[p];
-    const int e = ek >> 2, k = ek & 3;
-    const int4 t = tet[e];
-    const int tn[4] = {t.x, t.y, t.z, t.w};
-    const TetRec<float> R = rec[e];
-    const float kr = 0.25f * (nf.ckrw[t.x] + nf.ckrw[t.y] + nf.ckrw[t.z] + nf.ckrw[t.w]);
-    const float e1 = 0.25f * (nf.et1[t.x] + nf.et1[t.y] + nf.et1[t.z] + nf.et1[t.w]);
-    const float ve1 = R.vol * e1, ve = R.vpel;
-    int l = -1;
+  scol[grp][lane] = (lane < rlen) ? cols[s0 + lane] : 0x7fffffff;
+  int ntrip = (p1 - p0 + kGroup - 1) / kGroup;
+  ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
+  __syncwarp();
+  float lhs = 0.0f, rp = 0.0f;
+  for (int trip = 0; trip < ntrip; ++trip) {
+    const int p = p0 + trip * kGroup + lane;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) if (tn[q] == col) l = q;
-    if (l >= 0) {
-      const float lm = (l == k) ? lm_d : lm_o;
-      lhs += th * (kr * R.S[sym_idx(k, l)]) + ve1 * lm * rdt;
-      if (l == k) lhs += ve * lm_d * et2i * rdt;
+    for (int l = 0; l < 4; ++l) sidx[grp][lane * 4 + l] = -1;
+    if (rowok && p < p1) {
+      const int ek = inc[p];
+      const int e = ek >> 2, k = ek & 3;
+      const int4 t = tet[e];
+      const int tn[4] = {t.x, t.y, t.z, t.w};
+      const float4* rv = reinterpret_cast<const float4*>(rec + e);
+      const float4 r0 = rv[0], r1 = rv[1], r2 = rv[2], r3 = rv[3];
+      const float Sv[10] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y};
+      const float vol = r3.z, vpel = r3.w;
+      const float kr = 0.25f * (nf.ckrw[t.x] + nf.ckrw[t.y] + nf.ckrw[t.z] + nf.ckrw[t.w]);
+      const float e1 = 0.25f * (nf.et1[t.x] + nf.et1[t.y] + nf.et1[t.z] + nf.et1[t.w]);
+      const float ve1 = vol * e1;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const float lm = (l == k) ? lm_d : lm_o;
+        const float skl = Sv[sym_idx(k, l)];
+        float c = th * (kr * skl) + ve1 * lm * rdt;
+        if (l == k) c += vpel * lm_d * et2i * rdt;
+        // binary search of node tn[l] among the row's sorted columns
+        int lo = 0, hi = rlen - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (scol[grp][mid] < tn[l]) lo = mid + 1; else hi = mid;
+        }
+        sval[grp][lane * 4 + l] = c;
+        sidx[grp][lane * 4 + l] = (int8_t)lo;
+        const int nl = tn[l];
+        const float dh = (nf.hhi[nl] - hh_i) + (nf.hlo[nl] - hl_i);
+        rp -= kr * skl * dh + (ve1 * lm * nf.dpsi[nl] + vpel * lm * nf.dsw[nl]) * rdt;
+      }
     }
-    if (lane < 4) {
-      const int nl = tn[lane];
-      const float lm = (lane == k) ? lm_d : lm_o;
-      const float dh = (nf.hhi[nl] - hhi_i) + (nf.hlo[nl] - hlo_i);
-      rpart -= kr * R.S[sym_idx(k, lane)] * dh +
-               (ve1 * lm * nf.dpsi[nl] + ve * lm * nf.dsw[nl]) * rdt;
+    __syncwarp();
+    if (lane < rlen) {
+#pragma unroll 8
+      for (int q = 0; q < kGroup * 4; ++q)
+        if (sidx[grp][q] == lane) lhs += sval[grp][q];
     }
+    __syncwarp();
   }
-  const float rhs = group_sum<float>(rpart);
+  const float rhs = group_sum<float>(rp);
   if (!rowok) return;
-  if (col >= 0) vals[s0 + lane] = lhs;
+  if (lane < rlen) vals[s0 + lane] = lhs;
   if (lane == 0) {
     nf.xt5[i] = rhs;
-    float b = rhs;
-    if (nd.dmask[i]) {
-      b = 0.0f;
-    } else if (nd.loc[i] < S.nnod && nd.ifatm[i] == 0) {
-      b += (float)(S.tetaf * nd.atmact[i] + (1.0 - S.tetaf) * nd.atmold[i]);
+    nf.rhs[i] = dmask[i] ? 0.0f : rhs + bcf[i];
+  }
+}
+
+// FP32 boundary fluxes of the surface nodes for this iteration (BCPIC):
+// theta*ATMACT + (1-theta)*ATMOLD for Neumann atmospheric nodes, plus the
+// static non-atmospheric Neumann flux.
+__global__ void k_bcflux_f32(int nsurf_rows, const int32_t* srows, const uint8_t* act,
+                             const MemberScal* ms, Nodal nd, const float* qneu_f,
+                             float* bcf) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nsurf_rows) return;
+  const int i = srows[q];
+  const int m = nd.mem[i];
+  if (!(act[m] & ACT_ITER)) return;
+  float f = qneu_f[i];
+  if (nd.ifatm[i] == 0) {
+    const double th = ms[m].tetaf;
+    f += (th == 1.0) ? (float)nd.atmact[i]
+                     : (float)(th * nd.atmact[i] + (1.0 - th) * nd.atmold[i]);
+  }
+  bcf[i] = f;
+}
+
+// Back-calculated flux at Dirichlet rows (BKPIC): SCR = A*PDIFF - XT5, then
+// QPNEW (static Dirichlet) or ATMACT (atmospheric Dirichlet).  16 lanes per
+// candidate row (surface rows and static Dirichlet rows).
+__global__ void k_bkflux_f32(int nrows, const int32_t* rows, const uint8_t* act,
+                             const MemberScal* ms, const int32_t* rowptr,
+                             const int32_t* cols, const float* vals, Nodal nd,
+                             NodalF nf) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+  const int lane = threadIdx.x % kGroup;
+  const bool ok = grp < nrows;
+  int i = 0;
+  bool dir = false;
+  if (ok) {
+    i = rows[grp];
+    dir = (act[nd.mem[i]] & ACT_ITER) && nd.dmask[i];
+  }
+  float sp = 0.0f;
+  if (dir) {
+    const int sl = rowptr[i] + lane;
+    if (sl < rowptr[i + 1]) sp = vals[sl] * nf.pdiff[cols[sl]];
+  }
+  sp = group_sum<float>(sp);
+  if (dir && lane == 0) {
+    const int m = nd.mem[i];
+    const double th = ms[m].tetaf;
+    const double scr = (double)sp - (double)nf.xt5[i];
+    if (nd.sdir[i]) nd.qpnew[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.qpold[i]) / th;
+    else if (nd.loc[i] < ms[m].nnod)
+      nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
+  }
+}
+
+// MASBAL sums (STORMB, FLUXMB), RELAX and NORMS for the FP32 path, one thread
+// per row; compensated FP32 block sums.
+__global__ void __launch_bounds__(kThreads)
+k_masbal_norms_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                   const uint8_t* act, const MemberScal* ms, Nodal nd, NodalF nf,
+                   const float* volnod_f, const float* pnodi_f, double* red,
+                   double* redmax) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  const MemberScal& S = ms[m];
+  FF v[RD_PL2];
+  for (int q = 0; q < RD_PL2; ++q) v[q] = FF{0.0f, 0.0f};
+  float pl2 = 0.0f, fl2 = 0.0f, pinf = 0.0f, finf = 0.0f;
+  if (i < bm_r1[blockIdx.x]) {
+    const bool surf = nd.loc[i] < S.nnod;
+    const int8_t f = surf ? nd.ifatm[i] : (int8_t)-1;
+    if (nd.sdir[i]) {
+      const float qn = (float)nd.qpnew[i];
+      if (qn > 0.0f) v[RD_NDIN].hi = qn; else v[RD_NDOUT].hi = qn;
     }
-    b += (float)nd.qneu[i];
-    nf.rhs[i] = b;
+    if (f != -1) {
+      const float aa = (float)nd.atmact[i];
+      if (f == 1 || f == 2) {
+        if (aa > 0.0f) v[RD_ADIN].hi = aa; else v[RD_ADOUT].hi = aa;
+      } else {
+        if (aa > 0.0f) v[RD_ANIN].hi = aa; else v[RD_ANOUT].hi = aa;
+      }
+    }
+    double p = nd.pnew[i];
+    if (S.nlrelx == 1) {
+      p = S.omega * p + (1.0 - S.omega) * nd.pold[i];
+      nd.pnew[i] = p;
+    }
+    const float dp = (float)(p - nd.ptimep[i]);
+    const float sw = nf.sw[i], dsw = nf.dsw[i];
+    v[RD_DSTORE].hi = volnod_f[i] * (nf.ss[i] * (2.0f * sw - dsw) * 0.5f * dp + pnodi_f[i] * dsw);
+    const float diff = (float)(p - nd.pold[i]);
+    pl2 = diff * diff;
+    pinf = fabsf(diff);
+    const float b = nf.rhs[i];
+    fl2 = b * b;
+    finf = fabsf(b);
+  }
+  block_accumulate_ff<RD_PL2>(v, red + (size_t)m * RD_NUM);
+  float sums[2] = {pl2, fl2};
+  block_accumulate_t<float, 2>(sums, red + (size_t)m * RD_NUM + RD_PL2);
+  __shared__ float shm[2][kThreads / 32];
+  const int wl = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    pinf = fmaxf(pinf, __shfl_xor_sync(0xffffffffu, pinf, o));
+    finf = fmaxf(finf, __shfl_xor_sync(0xffffffffu, finf, o));
+  }
+  if (wl == 0) { shm[0][w] = pinf; shm[1][w] = finf; }
+  __syncthreads();
+  if (w == 0) {
+    float a = wl < (int)(blockDim.x >> 5) ? shm[0][wl] : 0.0f;
+    float b = wl < (int)(blockDim.x >> 5) ? shm[1][wl] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+      b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    if (wl == 0) {
+      atomic_max_nonneg(redmax + (size_t)m * 2, (double)a);
+      atomic_max_nonneg(redmax + (size_t)m * 2 + 1, (double)b);
+    }
   }
 }
 
@@ -1502,90 +1692,34 @@ __global__ void k_update_shl_f32(const int32_t* bm_mem, const int32_t* bm_r0,
   nd.pnew[i] = p;
 }
 
-// MASBAL + RELAX + NORMS for the FP32 path.  SWNEW/SWTIMEP enter only
-// through dSw = SWNEW - SWTIMEP and their sum (STORMB).
-__global__ void __launch_bounds__(kThreads)
-k_masbal_norms_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                   const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
-                   const int32_t* cols, const float* vals, Nodal nd, NodalF nf,
-                   double* red, double* redmax) {
+
+// STORE1 for the FP32 path: Sw(PNEW) in FP32, compensated sums.
+__global__ void k_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* mask, Nodal nd,
+                             NodalF nf, double* red) {
   const int m = bm_mem[blockIdx.x];
-  if (!(act[m] & ACT_ITER)) return;
-  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
-  const int i = bm_r0[blockIdx.x] + grp;
-  const bool rowok = i < bm_r1[blockIdx.x];
-  const MemberScal& S = ms[m];
-  const bool dir = rowok && nd.dmask[i];
-  float sp = 0.0f;
-  if (dir) {
-    const int sl = rowptr[i] + lane;
-    if (sl < rowptr[i + 1]) sp = vals[sl] * nf.pdiff[cols[sl]];
-  }
-  sp = group_sum<float>(sp);
-  double v[RD_STORE1] = {};
-  double pinf = 0.0, finf = 0.0;
-  if (rowok && lane == 0) {
-    const double th = S.tetaf, thr = 1.0 / th;
-    const bool surf = nd.loc[i] < S.nnod;
-    if (dir) {
-      const double scr = (double)sp - (double)nf.xt5[i];
-      if (nd.sdir[i]) {
-        const double qn = (scr - (1.0 - th) * nd.qpold[i]) * thr;
-        nd.qpnew[i] = qn;
-        if (qn > 0.0) v[RD_NDIN] += qn; else v[RD_NDOUT] += qn;
-      } else if (surf) {
-        nd.atmact[i] = (scr - (1.0 - th) * nd.atmold[i]) * thr;
-      }
-    }
-    if (surf && nd.ifatm[i] != -1) {
-      const double aa = nd.atmact[i];
-      if (nd.ifatm[i] == 1 || nd.ifatm[i] == 2) {
-        if (aa > 0.0) v[RD_ADIN] += aa; else v[RD_ADOUT] += aa;
-      } else {
-        if (aa > 0.0) v[RD_ANIN] += aa; else v[RD_ANOUT] += aa;
-      }
-    }
+  if (!mask[m]) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  FF v[1] = {FF{0.0f, 0.0f}};
+  if (i < bm_r1[blockIdx.x]) {
     const double p = nd.pnew[i];
-    if (S.deltat < 1.0e15) {
-      const float sw = nf.sw[i], dsw = nf.dsw[i];
-      const float dp = (float)(p - nd.ptimep[i]);
-      v[RD_DSTORE] = nd.volnod[i] * (double)(nf.ss[i] * (2.0f * sw - dsw) * 0.5f * dp +
-                                             (float)nd.pnodi[i] * dsw);
-    }
-    double pn = p;
-    if (S.nlrelx == 1) {
-      pn = S.omega * p + (1.0 - S.omega) * nd.pold[i];
-      nd.pnew[i] = pn;
-    }
-    const double diff = pn - nd.pold[i];
-    v[RD_PL2] = diff * diff;
-    const double b = nf.rhs[i];
-    v[RD_FL2] = b * b;
-    pinf = fabs(diff);
-    finf = fabs(b);
+    float se = 1.0f;
+    if (p < -1.0e-14) se = expf(-nf.vgm[i] * log1pf(vgf_beta((float)p, nf.vgpsat[i], nf.vgn[i])));
+    const float sw = nf.vgpnot[i] * se + nf.rmcp[i];
+    v[0].hi = sw * nf.volnod[i] * nf.pnodi[i];
   }
-  block_accumulate<RD_STORE1>(v, red + (size_t)m * RD_NUM);
-  __shared__ double shm[2][kThreads / 32];
-  const int wl = threadIdx.x & 31, w = threadIdx.x >> 5;
-  double a = warp_max(pinf), b = warp_max(finf);
-  if (wl == 0) { shm[0][w] = a; shm[1][w] = b; }
-  __syncthreads();
-  if (w == 0) {
-    a = wl < (int)(blockDim.x >> 5) ? shm[0][wl] : 0.0;
-    b = wl < (int)(blockDim.x >> 5) ? shm[1][wl] : 0.0;
-    a = warp_max(a);
-    b = warp_max(b);
-    if (wl == 0) {
-      atomic_max_nonneg(redmax + (size_t)m * 2, a);
-      atomic_max_nonneg(redmax + (size_t)m * 2 + 1, b);
-    }
-  }
+  block_accumulate_ff<1>(v, red + (size_t)m * RD_NUM + RD_STORE1);
 }
 
 // FP32 copies of the nodal van Genuchten parameters (after CHPARM)
 __global__ void k_params_f32(int n, Nodal nd, NodalF nf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  nf.rmcp[i] = (float)(nd.vgrmc[i] / nd.pnodi[i]);
+  nf.qneu[i] = (float)nd.qneu[i];
+  nf.volnod[i] = (float)nd.volnod[i];
+  nf.pnodi[i] = (float)nd.pnodi[i];
+  nf.bcf[i] = (float)nd.qneu[i];
   nf.vgn[i] = (float)nd.vgn[i]; nf.vgm[i] = (float)nd.vgm[i]; nf.vgpsat[i] = (float)nd.vgpsat[i];
   nf.vgn1[i] = (float)nd.vgn1[i]; nf.vgnr[i] = (float)nd.vgnr[i]; nf.vgpsn[i] = (float)nd.vgpsn[i];
   nf.vgpnot[i] = (float)nd.vgpnot[i]; nf.ss[i] = (float)nd.snodi[i];
@@ -1648,7 +1782,9 @@ struct Engine {
   // device buffers
   DBuf<int32_t> d_mem, d_loc, d_node_off;
   DBuf<double> d_nodal[48];
-  DBuf<float> d_nodf[20];
+  DBuf<float> d_nodf[24];
+  DBuf<int32_t> d_drows;  // Dirichlet candidate rows (surface + static)
+  int ndrows = 0;
   NodalF nf{};
   DBuf<uint8_t> d_sdir, d_dmask, d_act, d_active, d_switch, d_mask2, d_outer;
   DBuf<int8_t> d_ifatm, d_ifatmp;
@@ -1738,6 +1874,7 @@ struct Engine {
   // spmv_bytes (for s_v+s_i = 8) scaled by the value size; 2*n*s_v vectors
   // (x read, y written) + the fused dot's w read = spmv_bytes_vec * s_v
   std::vector<double> spmv_bytes, spmv_bytes_vec;
+  int need_sw_flag() const { return (precision == 1 && iopt == 1) ? 0 : 1; }
   void bare_init(int n, const std::vector<int32_t>& rowptr,
                  const std::vector<int32_t>& cols, const std::vector<uint8_t>& dm);
 };
@@ -2051,6 +2188,14 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_inc_ptr.alloc(N + 1); d_inc_ptr.upload(h_incptr.data(), N + 1, st);
   d_inc.alloc(h_inc.size()); d_inc.upload(h_inc.data(), h_inc.size(), st);
   d_srows.alloc(nsurf); d_srows.upload(h_srows.data(), nsurf, st);
+  {
+    std::vector<int32_t> dr = h_srows;
+    for (int i = 0; i < N; ++i)
+      if (h_sdir[i] && h_loc[i] >= M[h_mem[i]]->meshp->nnod) dr.push_back(i);
+    ndrows = (int)dr.size();
+    d_drows.alloc(dr.size());
+    d_drows.upload(dr.data(), dr.size(), st);
+  }
   // batched level schedules: level L of every member concatenated
   {
     auto batch_levels = [&](bool fwd, std::vector<int32_t>& ptr, DBuf<int32_t>& rows) {
@@ -2113,11 +2258,12 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   }
   check_launch();
   if (precision == 1 && iopt == 1) {
-    for (int k = 0; k < 19; ++k) { d_nodf[k].alloc(N); d_nodf[k].zero(st); }
-    float** fp[19] = {&nf.ckrw, &nf.et1, &nf.et2, &nf.sw, &nf.dsw, &nf.dpsi, &nf.hhi, &nf.hlo,
+    for (int k = 0; k < 24; ++k) { d_nodf[k].alloc(N); d_nodf[k].zero(st); }
+    float** fp[24] = {&nf.ckrw, &nf.et1, &nf.et2, &nf.sw, &nf.dsw, &nf.dpsi, &nf.hhi, &nf.hlo,
                       &nf.rhs, &nf.xt5, &nf.pdiff, &nf.vgn, &nf.vgm, &nf.vgpsat, &nf.vgn1,
-                      &nf.vgnr, &nf.vgpsn, &nf.vgpnot, &nf.ss};
-    for (int k = 0; k < 19; ++k) *fp[k] = d_nodf[k].p;
+                      &nf.vgnr, &nf.vgpsn, &nf.vgpnot, &nf.ss, &nf.rmcp, &nf.bcf, &nf.qneu,
+                      &nf.volnod, &nf.pnodi};
+    for (int k = 0; k < 24; ++k) *fp[k] = d_nodf[k].p;
     k_params_f32<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, nd, nf);
     check_launch();
   }
@@ -2212,7 +2358,7 @@ void Engine::push_scalars() {
   for (int m = 0; m < nmem; ++m) {
     MemberHost& h = *M[m];
     MemberScal& S = h_ms[m];
-    S.deltat = h.deltat; S.time = h.time; S.tetaf = h.parm.tetaf; S.scf = h.scf;
+    S.deltat = h.deltat; S.deltat_r = 1.0 / h.deltat; S.time = h.time; S.tetaf = h.parm.tetaf; S.scf = h.scf;
     S.pmin = h.pmin; S.omega = h.parm.omega; S.tolswi = h.parm.tolswi;
     S.atm_ta = h.atm_ta; S.atm_tb = h.atm_tb; S.atm_va = h.atm_va; S.atm_vb = h.atm_vb;
     S.atm_mode = h.atm_mode; S.hspatm = h.hspatm; S.ieto = h.ieto; S.nlrelx = h.parm.nlrelx;
@@ -2539,11 +2685,13 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
     // correction to opts.inner_tol.
     k_vg_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd, nf,
                                             d_nodal[ND_Z].p);
+    k_bcflux_f32<<<cdiv(nsurf, kThreads), kThreads, 0, st>>>(nsurf, d_srows.p, d_act.p, d_ms.p, nd,
+                                                             nf.qneu, nf.bcf);
     k_assemble_picard_f32<<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
-        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, d_rec32.p, nd, nf,
-        d_vals32.p, (float)lm_d, (float)lm_o);
+        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, d_rec32.p, d_dmask.p,
+        nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o);
     k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
-    count(3);
+    count(4);
     check_launch();
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
                             std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1);
@@ -2566,14 +2714,17 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
   CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
   CG_TRY(cudaMemsetAsync(d_redmax.p, 0, sizeof(double) * nmem * 2, st));
   CG_TRY(cudaMemsetAsync(d_ikmax.p, 0, sizeof(int32_t) * nmem, st));
-  if (mixed)
-    k_masbal_norms_f32<<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
-        d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf, d_red.p, d_redmax.p);
-  else
+  if (mixed) {
+    k_bkflux_f32<<<cdiv((long)ndrows * kGroup, kThreads), kThreads, 0, st>>>(ndrows, d_drows.p,
+        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
+    k_masbal_norms_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p,
+        d_ms.p, nd, nf, nf.volnod, nf.pnodi, d_red.p, d_redmax.p);
+    count();
+  } else
     k_masbal_norms<double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
         d_ms.p, d_rowptr.p, d_cols.p, d_vals64.p, nd, d_red.p, d_redmax.p, iopt == 2);
   k_ikmax<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd, d_redmax.p,
-                                         d_ikmax.p);
+                                         d_ikmax.p, mixed ? 1 : 0);
   k_gather_ik<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_node_off.p, d_ikmax.p, nd, d_ikval.p);
   k_switch_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_red.p, d_redmax.p, d_ms.p,
                                                   P0.l2norm, d_switch.p);
@@ -2601,9 +2752,9 @@ int Engine::macro_iteration() {
   }
   push_scalars();
   d_act.upload(h_act.data(), nmem, st);
-  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 0);
+  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 0, need_sw_flag());
   k_start_surface<<<cdiv(nsurf, kThreads), kThreads, 0, st>>>(nsurf, d_srows.p, d_act.p, d_ms.p, nd);
-  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 1);
+  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 1, need_sw_flag());
   count(3);
   check_launch();
   if (niter_members == 0) {
@@ -2677,7 +2828,10 @@ int Engine::macro_iteration() {
   if (any_conv) {
     d_mask2.upload(conv_mask.data(), nmem, st);
     CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
-    k_store1<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_mask2.p, nd, d_red.p);
+    if (precision == 1 && iopt == 1)
+      k_store1_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_mask2.p, nd, nf, d_red.p);
+    else
+      k_store1<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_mask2.p, nd, d_red.p);
     count();
     check_launch();
     d_red.download(red.data(), red.size(), st);
@@ -2924,18 +3078,20 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   if (a & ACT_START) { h.iterating = true; h.iter = 1; h.nitert = 0; }
   e->push_scalars();
   e->d_act.upload(act.data(), e->nmem, e->st);
-  k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0);
+  k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0, e->need_sw_flag());
   k_start_surface<<<cdiv(e->nsurf, kThreads), kThreads, 0, e->st>>>(e->nsurf, e->d_srows.p, e->d_act.p, e->d_ms.p, e->nd);
-  k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 1);
+  k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 1, e->need_sw_flag());
   act[m] = ACT_ITER;
   e->d_act.upload(act.data(), e->nmem, e->st);
   const bool mixed = (e->precision == 1 && e->iopt == 1);
   if (mixed) {
     k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->nd, e->nf,
                                                   e->d_nodal[ND_Z].p);
+    k_bcflux_f32<<<cdiv(e->nsurf, kThreads), kThreads, 0, e->st>>>(e->nsurf, e->d_srows.p, e->d_act.p,
+        e->d_ms.p, e->nd, e->nf.qneu, e->nf.bcf);
     k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
         e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_tet.p,
-        e->d_rec32.p, e->nd, e->nf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o);
+        e->d_rec32.p, e->d_dmask.p, e->nf, e->nf.bcf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o);
   } else {
     k_vg<double><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->iopt == 2);
     e->assemble<double>();

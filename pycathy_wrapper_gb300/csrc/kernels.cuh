@@ -34,7 +34,7 @@ enum : uint8_t {
 
 // per-member scalars on the device (read by kernels)
 struct MemberScal {
-  double deltat, time, tetaf, scf, pmin, omega, tolswi;
+  double deltat, time, tetaf, scf, pmin, omega, tolswi, deltat_r;
   double atm_ta, atm_tb;   // interpolation times for ATMPOT
   double atm_va, atm_vb;   // homogeneous rates (hspatm != 0)
   int32_t atm_mode;        // 0 keep, 1 interpolate, 2 constant vb

@@ -294,7 +294,8 @@ def config2_members(nmembers=256, tmax=86400.0, base_seed=1000,
                   zratio=np.full(nstr, 1.0 / nstr), base=3.0, ivert=0)
         soil = Soil.homogeneous(nstr, ks=ks, alpha=alpha, n=nvg, theta_s=ths,
                                 theta_r=0.05)
-        parm = Parm(toluns=1e-6, deltat=1.0, dtmin=0.1, dtmax=600.0, tmax=tmax)
+        # DTMIN is the CATHY template's default (0.01 s)
+        parm = Parm(toluns=1e-6, deltat=1.0, dtmin=0.01, dtmax=600.0, tmax=tmax)
         bc = BC(atmtim=np.array([0.0, 1e9]), atminp=np.array([1e-7, 1e-7]),
                 indp=4, wtposition=wt)
         cases.append(Case(dem, soil, parm, bc, name=f"member{m}"))
