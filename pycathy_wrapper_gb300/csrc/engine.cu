@@ -98,20 +98,20 @@ __device__ __forceinline__ void block_accumulate(double (&v)[NV], double* acc) {
 // one FP64 atomicAdd per value.
 template <class T, int NV>
 __device__ __forceinline__ void block_accumulate_t(T (&v)[NV], double* acc) {
-  __shared__ double sh[NV][kThreads / 32];
+  __shared__ T sht[NV][kThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
     T s = warp_sum_t<T>(v[i]);
-    if (lane == 0) sh[i][w] = (double)s;
+    if (lane == 0) sht[i][w] = s;
   }
   __syncthreads();
   if (w == 0) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-      double s = (lane < (int)(blockDim.x >> 5)) ? sh[i][lane] : 0.0;
-      s = warp_sum(s);
-      if (lane == 0 && s != 0.0) atomicAdd(acc + i, s);
+      T s = (lane < (int)(blockDim.x >> 5)) ? sht[i][lane] : (T)0;
+      s = warp_sum_t<T>(s);
+      if (lane == 0 && s != (T)0) atomicAdd(acc + i, (double)s);
     }
   }
 }
@@ -309,12 +309,11 @@ __global__ void k_geom(int nt, const int4* tet, const double* x, const double* y
 // step actions (per member masks)
 // ============================================================================
 // surface part: BKSTEP restore + COMMIT bookkeeping + ATM update + switching
-__global__ void k_start_surface(int nsurf_rows, const int32_t* srows,
-                                const uint8_t* act, const MemberScal* ms,
-                                Nodal nd) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nsurf_rows) return;
-  const int i = srows[q];
+__global__ void k_start_surface(const int32_t* bm_mem, const int32_t* bm_r0,
+                                const int32_t* bm_r1, const uint8_t* act,
+                                const MemberScal* ms, Nodal nd) {
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
   const int m = nd.mem[i];
   const uint8_t a = act[m];
   if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START))) return;
@@ -708,16 +707,15 @@ __global__ void k_jacobi_setup(const int32_t* bm_mem, const int32_t* bm_r0,
 // off-diagonal weight on these thin-layered meshes).  Setup stores the
 // pivots' inverses and the masked vertical couplings.
 template <class MT, class VT>
-__global__ void k_line_setup(int ncol_rows, const int32_t* crows,
-                             const int32_t* mem, const uint8_t* active,
+__global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* active,
                              const MemberScal* ms, const int32_t* diag,
                              const int32_t* down, const MT* vals,
                              const uint8_t* dmask, VT* pinv, VT* cdown) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= ncol_rows) return;
-  const int top = crows[q];
-  const int m = mem[top];
+  const int m = bm_mem[blockIdx.x];
   if (!active[m]) return;
+  const int top = bm_r0[blockIdx.x] + threadIdx.x;
+  if (top >= bm_r1[blockIdx.x]) return;
   const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
   double piv_prev = 1.0, c_prev = 0.0;
   for (int k = 0; k < nl; ++k) {
@@ -736,21 +734,16 @@ __global__ void k_line_setup(int ncol_rows, const int32_t* crows,
 
 // z = T^-1 r per column; accumulates w.z (w = q for the PCG beta) per member
 template <class VT>
-__global__ void k_line_apply(int ncol_rows, const int32_t* crows,
-                             const int32_t* mem, const uint8_t* active,
+__global__ void k_line_apply(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* active,
                              const MemberScal* ms, const VT* pinv,
                              const VT* cdown, const VT* r, VT* z, const VT* w,
                              double* acc, int acc_stride, int acc_off) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  bool ok = q < ncol_rows;
-  int top = 0, m = 0;
-  VT red_dot = 0;
-  if (ok) {
-    top = crows[q];
-    m = mem[top];
-    ok = active[m];
-  }
-  if (ok) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int top = bm_r0[blockIdx.x] + threadIdx.x;
+  VT dot[1] = {0};
+  if (top < bm_r1[blockIdx.x]) {
     const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
     VT y[kMaxLayers];
     VT yprev = 0, cprev = 0;
@@ -762,28 +755,15 @@ __global__ void k_line_apply(int ncol_rows, const int32_t* crows,
       cprev = cdown[i];
     }
     VT znext = 0;
-    VT dot = 0;
     for (int k = nl - 1; k >= 0; --k) {
       const int i = top + k * nnod;
       VT zk = (y[k] - cdown[i] * znext) * pinv[i];
       z[i] = zk;
-      if (w) dot += w[i] * zk;
+      if (w) dot[0] += w[i] * zk;
       znext = zk;
     }
-    if (w) red_dot = dot;
   }
-  // warp-level pre-reduction when the whole warp belongs to one member
-  if (w) {
-    const int lane = threadIdx.x & 31;
-    const int m0 = __shfl_sync(0xffffffffu, ok ? m : -1, 0);
-    const bool uni = __all_sync(0xffffffffu, ok && m == m0);
-    if (uni) {
-      const VT sum = warp_sum_t<VT>(red_dot);
-      if (lane == 0) atomicAdd(acc + (size_t)m0 * acc_stride + acc_off, (double)sum);
-    } else if (ok) {
-      atomicAdd(acc + (size_t)m * acc_stride + acc_off, (double)red_dot);
-    }
-  }
+  if (w) block_accumulate_t<VT, 1>(dot, acc + (size_t)m * acc_stride + acc_off);
 }
 
 // IC(0) factor (left-looking row form of INCLDP), one thread per row of one
@@ -1307,13 +1287,12 @@ __global__ void k_gather_ik(int nmem, const uint8_t* act, const int32_t* node_of
 }
 
 // SWITCH_OLD after the norms when PINF (or PL2) <= TOLSWI
-__global__ void k_switch(int nsurf_rows, const int32_t* srows, const uint8_t* act,
-                         const uint8_t* do_switch, const MemberScal* ms,
+__global__ void k_switch(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                         const uint8_t* act, const uint8_t* do_switch, const MemberScal* ms,
                          Nodal nd) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nsurf_rows) return;
-  const int i = srows[q];
-  const int m = nd.mem[i];
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER) || !do_switch[m]) return;
   int8_t f = nd.ifatm[i];
   if (f == -1) return;
@@ -1367,6 +1346,9 @@ __global__ void k_flags(int nmem, const uint8_t* act, uint8_t bits, uint8_t* out
 // ============================================================================
 struct NodalF {
   float *ckrw, *et1, *et2, *sw, *dsw, *dpsi, *hhi, *hlo, *rhs, *xt5, *pdiff;
+  float2 *krE;   // per element: (mean kr, mean Sw*Ss)
+  float2 *ckr2;  // per node: (kr, Sw*Ss)
+  float2 *h2;    // per node: total head (hi, lo)
   float *vgn, *vgm, *vgpsat, *vgn1, *vgnr, *vgpsn, *vgpnot, *ss;
   float *rmcp, *bcf, *qneu, *volnod, *pnodi;
 };
@@ -1414,14 +1396,30 @@ __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
   const float sw = pnot * se + rmcp;
   nf.ckrw[i] = kr;
   nf.et1[i] = sw * nf.ss[i];
+  nf.ckr2[i] = make_float2(kr, sw * nf.ss[i]);
   nf.et2[i] = pnot * dse;
   nf.sw[i] = sw;
   nf.dsw[i] = pnot * vgf_dse(p, pn, psat, n, mm);
   nf.dpsi[i] = (float)(p - pn);
   const double h = pt + z[i];
   const float hh = (float)h;
+  const float hl = (float)(h - (double)hh);
   nf.hhi[i] = hh;
-  nf.hlo[i] = (float)(h - (double)hh);
+  nf.hlo[i] = hl;
+  nf.h2[i] = make_float2(hh, hl);
+}
+
+// Element means of kr and Sw*Ss (NODELT) for the FP32 assembly.
+__global__ void k_elem_f32(const int32_t* ebm_mem, const int32_t* ebm_e0,
+                           const int32_t* ebm_e1, const uint8_t* act, const int4* tet,
+                           NodalF nf) {
+  const int m = ebm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int e = ebm_e0[blockIdx.x] + threadIdx.x;
+  if (e >= ebm_e1[blockIdx.x]) return;
+  const int4 t = tet[e];
+  const float2 a = nf.ckr2[t.x], b = nf.ckr2[t.y], c = nf.ckr2[t.z], d = nf.ckr2[t.w];
+  nf.krE[e] = make_float2(0.25f * (a.x + b.x + c.x + d.x), 0.25f * (a.y + b.y + c.y + d.y));
 }
 
 // ---- compensated FP32 sums (TwoSum) for the mass-balance reductions ----
@@ -1502,7 +1500,7 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   int ntrip = (p1 - p0 + kGroup - 1) / kGroup;
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
   __syncwarp();
-  float lhs = 0.0f, rp = 0.0f;
+  float lhs = 0.0f, rp = 0.0f, msum = 0.0f, mssum = 0.0f;
   for (int trip = 0; trip < ntrip; ++trip) {
     const int p = p0 + trip * kGroup + lane;
 #pragma unroll
@@ -1516,8 +1514,8 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
       const float4 r0 = rv[0], r1 = rv[1], r2 = rv[2], r3 = rv[3];
       const float Sv[10] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y};
       const float vol = r3.z, vpel = r3.w;
-      const float kr = 0.25f * (nf.ckrw[t.x] + nf.ckrw[t.y] + nf.ckrw[t.z] + nf.ckrw[t.w]);
-      const float e1 = 0.25f * (nf.et1[t.x] + nf.et1[t.y] + nf.et1[t.z] + nf.et1[t.w]);
+      const float2 ke = nf.krE[e];
+      const float kr = ke.x, e1 = ke.y;
       const float ve1 = vol * e1;
 #pragma unroll
       for (int l = 0; l < 4; ++l) {
@@ -1534,8 +1532,15 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
         sval[grp][lane * 4 + l] = c;
         sidx[grp][lane * 4 + l] = (int8_t)lo;
         const int nl = tn[l];
-        const float dh = (nf.hhi[nl] - hh_i) + (nf.hlo[nl] - hl_i);
-        rp -= kr * skl * dh + (ve1 * lm * nf.dpsi[nl] + vpel * lm * nf.dsw[nl]) * rdt;
+        const float2 hn = nf.h2[nl];
+        const float dh = (hn.x - hh_i) + (hn.y - hl_i);
+        rp -= kr * skl * dh;
+        if (l == k) {
+          msum += ve1 * lm_d;
+          mssum += vpel * lm_d;
+        } else if (lm_o != 0.0f) {
+          rp -= (ve1 * lm_o * nf.dpsi[nl] + vpel * lm_o * nf.dsw[nl]) * rdt;
+        }
       }
     }
     __syncwarp();
@@ -1546,10 +1551,14 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     }
     __syncwarp();
   }
-  const float rhs = group_sum<float>(rp);
+  float rhs = group_sum<float>(rp);
+  // diagonal (lumped) mass terms of the row node itself
+  msum = group_sum<float>(msum);
+  mssum = group_sum<float>(mssum);
   if (!rowok) return;
   if (lane < rlen) vals[s0 + lane] = lhs;
   if (lane == 0) {
+    rhs -= (msum * nf.dpsi[i] + mssum * nf.dsw[i]) * rdt;
     nf.xt5[i] = rhs;
     nf.rhs[i] = dmask[i] ? 0.0f : rhs + bcf[i];
   }
@@ -1558,13 +1567,12 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
 // FP32 boundary fluxes of the surface nodes for this iteration (BCPIC):
 // theta*ATMACT + (1-theta)*ATMOLD for Neumann atmospheric nodes, plus the
 // static non-atmospheric Neumann flux.
-__global__ void k_bcflux_f32(int nsurf_rows, const int32_t* srows, const uint8_t* act,
-                             const MemberScal* ms, Nodal nd, const float* qneu_f,
-                             float* bcf) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nsurf_rows) return;
-  const int i = srows[q];
-  const int m = nd.mem[i];
+__global__ void k_bcflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                             const uint8_t* act, const MemberScal* ms, Nodal nd,
+                             const float* qneu_f, float* bcf) {
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
   float f = qneu_f[i];
   if (nd.ifatm[i] == 0) {
@@ -1577,20 +1585,14 @@ __global__ void k_bcflux_f32(int nsurf_rows, const int32_t* srows, const uint8_t
 
 // Back-calculated flux at Dirichlet rows (BKPIC): SCR = A*PDIFF - XT5, then
 // QPNEW (static Dirichlet) or ATMACT (atmospheric Dirichlet).  16 lanes per
-// candidate row (surface rows and static Dirichlet rows).
-__global__ void k_bkflux_f32(int nrows, const int32_t* rows, const uint8_t* act,
-                             const MemberScal* ms, const int32_t* rowptr,
-                             const int32_t* cols, const float* vals, Nodal nd,
-                             NodalF nf) {
-  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
-  const int lane = threadIdx.x % kGroup;
-  const bool ok = grp < nrows;
-  int i = 0;
+// candidate row: surface rows through a member block map (rows == nullptr)
+// or an explicit list of deep static Dirichlet rows.
+__device__ __forceinline__ void bkflux_row(int i, bool valid, int lane, const uint8_t* act,
+                                           const MemberScal* ms, const int32_t* rowptr,
+                                           const int32_t* cols, const float* vals,
+                                           Nodal& nd, NodalF& nf) {
   bool dir = false;
-  if (ok) {
-    i = rows[grp];
-    dir = (act[nd.mem[i]] & ACT_ITER) && nd.dmask[i];
-  }
+  if (valid) dir = (act[nd.mem[i]] & ACT_ITER) && nd.dmask[i];
   float sp = 0.0f;
   if (dir) {
     const int sl = rowptr[i] + lane;
@@ -1605,6 +1607,21 @@ __global__ void k_bkflux_f32(int nrows, const int32_t* rows, const uint8_t* act,
     else if (nd.loc[i] < ms[m].nnod)
       nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
   }
+}
+__global__ void k_bkflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                             const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
+                             const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  bkflux_row(i, i < bm_r1[blockIdx.x], lane, act, ms, rowptr, cols, vals, nd, nf);
+}
+__global__ void k_bkflux_list_f32(int nrows, const int32_t* rows, const uint8_t* act,
+                                  const MemberScal* ms, const int32_t* rowptr,
+                                  const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+  const int lane = threadIdx.x % kGroup;
+  const bool ok = grp < nrows;
+  bkflux_row(ok ? rows[grp] : 0, ok, lane, act, ms, rowptr, cols, vals, nd, nf);
 }
 
 // MASBAL sums (STORMB, FLUXMB), RELAX and NORMS for the FP32 path, one thread
@@ -1725,6 +1742,25 @@ __global__ void k_params_f32(int n, Nodal nd, NodalF nf) {
   nf.vgpnot[i] = (float)nd.vgpnot[i]; nf.ss[i] = (float)nd.snodi[i];
 }
 
+
+// Compacted block map: out[b] = full[first[amem[j]] + b - cum[j]] where j is
+// the active member slot holding block b (binary search over cum).
+__global__ void k_compact_map(int ntot, int nact, const int32_t* amem, const int32_t* cum,
+                              const int32_t* first, const int32_t* fmem, const int32_t* fr0,
+                              const int32_t* fr1, int32_t* omem, int32_t* or0, int32_t* or1) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= ntot) return;
+  int lo = 0, hi = nact - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (cum[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  const int src = first[amem[lo]] + (b - cum[lo]);
+  omem[b] = fmem[src];
+  or0[b] = fr0[src];
+  or1[b] = fr1[src];
+}
+
 // ============================================================================
 // host side
 // ============================================================================
@@ -1783,6 +1819,8 @@ struct Engine {
   DBuf<int32_t> d_mem, d_loc, d_node_off;
   DBuf<double> d_nodal[48];
   DBuf<float> d_nodf[24];
+  DBuf<float2> d_krE, d_ckr2, d_h2;
+  BlockMap bme;  // element blocks per member
   DBuf<int32_t> d_drows;  // Dirichlet candidate rows (surface + static)
   int ndrows = 0;
   NodalF nf{};
@@ -1807,6 +1845,17 @@ struct Engine {
   DBuf<float> d_linv32, d_lc32;
   DBuf<double> d_linv64, d_lc64;
   BlockMap bm1, bm16;
+  // surface-row maps (1 thread / 16 lanes per surface node)
+  BlockMap bms, bms16;
+  // compacted maps over the members that have work in this macro-iteration
+  BlockMap cbm1, cbm16, cbme, cbms, cbms16;
+  std::vector<int32_t> nblk1, nblk16, nblke, nblks, nblks16;  // blocks per member
+  std::vector<int32_t> first1, first16, firste, firsts, firsts16;
+  DBuf<int32_t> d_first, d_amem_cum;
+  std::vector<uint8_t> last_active;
+  DBuf<int32_t> d_deep;  // static Dirichlet rows below the surface
+  int ndeep = 0;
+  void compact_maps(const std::vector<uint8_t>& memact);
   int nsurf = 0;
   // stats
   double gpu_ms = 0;
@@ -1827,6 +1876,9 @@ struct Engine {
   void check_launch() { CG_TRY(cudaPeekAtLastError()); }
   void build(int nmembers, const cathy_member_t* mem);
   void make_blockmap(BlockMap& bm, int rows_per_block);
+  void make_elem_blockmap(BlockMap& bm, int elems_per_block);
+  void make_surface_blockmap(BlockMap& bm, int rows_per_block);
+  void init_compaction();
   void atm_setup_member(MemberHost& h, bool initial);
   void atm_advance(MemberHost& h);  // ATMNXT series advance
   void atm_back(MemberHost& h);     // ATMBAK
@@ -1888,6 +1940,45 @@ enum {
   ND_DCKRW, ND_DETAI, ND_ARENOD, ND_ATMPOT, ND_ATMACT, ND_ATMOLD, ND_ATMA, ND_ATMB,
   ND_X, ND_Y, ND_Z, ND_NUM
 };
+
+void Engine::make_elem_blockmap(BlockMap& bm, int epb) {
+  std::vector<int32_t> mm, r0, r1;
+  for (int m = 0; m < nmem; ++m)
+    for (long a = tet_off[m]; a < tet_off[m + 1]; a += epb) {
+      mm.push_back(m);
+      r0.push_back((int32_t)a);
+      r1.push_back((int32_t)std::min<long>(a + epb, tet_off[m + 1]));
+    }
+  bm.nblk = (int)mm.size();
+  bm.mem.alloc(mm.size()); bm.mem.upload(mm.data(), mm.size(), st);
+  bm.r0.alloc(r0.size()); bm.r0.upload(r0.data(), r0.size(), st);
+  bm.r1.alloc(r1.size()); bm.r1.upload(r1.data(), r1.size(), st);
+}
+
+void Engine::make_surface_blockmap(BlockMap& bm, int rpb) {
+  std::vector<int32_t> mm, r0, r1;
+  for (int m = 0; m < nmem; ++m) {
+    const int lo = node_off[m], hi = node_off[m] + M[m]->meshp->nnod;
+    for (int a = lo; a < hi; a += rpb) {
+      mm.push_back(m);
+      r0.push_back(a);
+      r1.push_back(std::min(a + rpb, hi));
+    }
+  }
+  bm.nblk = (int)mm.size();
+  bm.mem.alloc(mm.size()); bm.mem.upload(mm.data(), mm.size(), st);
+  bm.r0.alloc(r0.size()); bm.r0.upload(r0.data(), r0.size(), st);
+  bm.r1.alloc(r1.size()); bm.r1.upload(r1.data(), r1.size(), st);
+}
+
+static void per_member_counts(const std::vector<int32_t>& mm, int nmem, std::vector<int32_t>& cnt,
+                              std::vector<int32_t>& first) {
+  cnt.assign(nmem, 0);
+  first.assign(nmem, 0);
+  for (size_t b = 0; b < mm.size(); ++b) cnt[mm[b]]++;
+  int acc = 0;
+  for (int m = 0; m < nmem; ++m) { first[m] = acc; acc += cnt[m]; }
+}
 
 void Engine::make_blockmap(BlockMap& bm, int rpb) {
   std::vector<int32_t> mm, r0, r1;
@@ -2189,12 +2280,12 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_inc.alloc(h_inc.size()); d_inc.upload(h_inc.data(), h_inc.size(), st);
   d_srows.alloc(nsurf); d_srows.upload(h_srows.data(), nsurf, st);
   {
-    std::vector<int32_t> dr = h_srows;
+    std::vector<int32_t> dr;
     for (int i = 0; i < N; ++i)
       if (h_sdir[i] && h_loc[i] >= M[h_mem[i]]->meshp->nnod) dr.push_back(i);
-    ndrows = (int)dr.size();
-    d_drows.alloc(dr.size());
-    d_drows.upload(dr.data(), dr.size(), st);
+    ndeep = (int)dr.size();
+    d_deep.alloc(std::max<size_t>(dr.size(), 1));
+    if (ndeep) d_deep.upload(dr.data(), dr.size(), st);
   }
   // batched level schedules: level L of every member concatenated
   {
@@ -2264,6 +2355,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
                       &nf.vgnr, &nf.vgpsn, &nf.vgpnot, &nf.ss, &nf.rmcp, &nf.bcf, &nf.qneu,
                       &nf.volnod, &nf.pnodi};
     for (int k = 0; k < 24; ++k) *fp[k] = d_nodf[k].p;
+    d_krE.alloc(NT); d_ckr2.alloc(N); d_h2.alloc(N);
+    nf.krE = d_krE.p; nf.ckr2 = d_ckr2.p; nf.h2 = d_h2.p;
     k_params_f32<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, nd, nf);
     check_launch();
   }
@@ -2290,6 +2383,10 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_ikmax.alloc(nmem); d_ikval.alloc((size_t)nmem * 2); d_niter.alloc(nmem); d_nact.alloc(1);
   make_blockmap(bm1, kThreads);
   make_blockmap(bm16, kRowsPerBlock16);
+  make_elem_blockmap(bme, kThreads);
+  make_surface_blockmap(bms, kThreads);
+  make_surface_blockmap(bms16, kRowsPerBlock16);
+  init_compaction();
   h_ms.resize(nmem);
   h_act.assign(nmem, 0);
   // initial storage (STORCAL at PTIMEP = PNEW)
@@ -2323,6 +2420,75 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_prof_bytes.alloc(1);
   d_prof_bytes.zero(st);
   CG_TRY(cudaStreamSynchronize(st));
+}
+
+
+// Device copies of the block maps that macro-iterations launch over; they
+// start as the full maps and are compacted to the members with work.
+void Engine::init_compaction() {
+  auto host_mem = [&](const BlockMap& bm) {
+    std::vector<int32_t> mm(bm.nblk);
+    if (bm.nblk) bm.mem.download(mm.data(), bm.nblk, st);
+    CG_TRY(cudaStreamSynchronize(st));
+    return mm;
+  };
+  auto clone = [&](const BlockMap& src, BlockMap& dst) {
+    dst.nblk = src.nblk;
+    dst.mem.alloc(std::max(src.nblk, 1)); dst.r0.alloc(std::max(src.nblk, 1)); dst.r1.alloc(std::max(src.nblk, 1));
+    if (src.nblk) {
+      CG_TRY(cudaMemcpyAsync(dst.mem.p, src.mem.p, 4 * src.nblk, cudaMemcpyDeviceToDevice, st));
+      CG_TRY(cudaMemcpyAsync(dst.r0.p, src.r0.p, 4 * src.nblk, cudaMemcpyDeviceToDevice, st));
+      CG_TRY(cudaMemcpyAsync(dst.r1.p, src.r1.p, 4 * src.nblk, cudaMemcpyDeviceToDevice, st));
+    }
+  };
+  per_member_counts(host_mem(bm1), nmem, nblk1, first1);
+  per_member_counts(host_mem(bm16), nmem, nblk16, first16);
+  per_member_counts(host_mem(bme), nmem, nblke, firste);
+  per_member_counts(host_mem(bms), nmem, nblks, firsts);
+  per_member_counts(host_mem(bms16), nmem, nblks16, firsts16);
+  clone(bm1, cbm1); clone(bm16, cbm16); clone(bme, cbme); clone(bms, cbms); clone(bms16, cbms16);
+  std::vector<int32_t> fst;
+  for (auto* f : {&first1, &first16, &firste, &firsts, &firsts16}) fst.insert(fst.end(), f->begin(), f->end());
+  d_first.alloc(fst.size());
+  d_first.upload(fst.data(), fst.size(), st);
+  d_amem_cum.alloc((size_t)6 * (nmem + 1));
+  last_active.assign(nmem, 1);
+}
+
+void Engine::compact_maps(const std::vector<uint8_t>& memact) {
+  if (memact == last_active) return;
+  last_active = memact;
+  std::vector<int32_t> amem;
+  for (int m = 0; m < nmem; ++m) if (memact[m]) amem.push_back(m);
+  const int na = (int)amem.size();
+  if (na == 0) {
+    cbm1.nblk = cbm16.nblk = cbme.nblk = cbms.nblk = cbms16.nblk = 0;
+    return;
+  }
+  std::vector<int32_t> hostbuf((size_t)6 * (nmem + 1), 0);
+  std::copy(amem.begin(), amem.end(), hostbuf.begin());
+  const std::vector<int32_t>* counts[5] = {&nblk1, &nblk16, &nblke, &nblks, &nblks16};
+  int tot[5];
+  for (int q = 0; q < 5; ++q) {
+    int acc = 0;
+    for (int j = 0; j < na; ++j) {
+      hostbuf[(size_t)(q + 1) * (nmem + 1) + j] = acc;
+      acc += (*counts[q])[amem[j]];
+    }
+    tot[q] = acc;
+  }
+  d_amem_cum.upload(hostbuf.data(), hostbuf.size(), st);
+  const BlockMap* full[5] = {&bm1, &bm16, &bme, &bms, &bms16};
+  BlockMap* comp[5] = {&cbm1, &cbm16, &cbme, &cbms, &cbms16};
+  for (int q = 0; q < 5; ++q) {
+    comp[q]->nblk = tot[q];
+    if (!tot[q]) continue;
+    k_compact_map<<<cdiv(tot[q], 256), 256, 0, st>>>(tot[q], na, d_amem_cum.p,
+        d_amem_cum.p + (size_t)(q + 1) * (nmem + 1), d_first.p + (size_t)q * nmem, full[q]->mem.p,
+        full[q]->r0.p, full[q]->r1.p, comp[q]->mem.p, comp[q]->r0.p, comp[q]->r1.p);
+    count();
+  }
+  check_launch();
 }
 
 void Engine::save_initial() {
@@ -2389,10 +2555,10 @@ void Engine::assemble() {
   if constexpr (sizeof(MT) == 8) { rec = (const TetRec<MT>*)d_rec64.p; vals = (MT*)d_vals64.p; }
   else { rec = (const TetRec<MT>*)d_rec32.p; vals = (MT*)d_vals32.p; }
   if (iopt == 1)
-    k_assemble_picard<MT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+    k_assemble_picard<MT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_act.p,
         d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, rec, nd, vals, lm_d, lm_o);
   else
-    k_assemble_newton<MT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+    k_assemble_newton<MT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_act.p,
         d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, rec, nd, vals, lm_d, lm_o);
   check_launch();
   count();
@@ -2406,19 +2572,20 @@ static void precond_apply(Engine& E, int pc, const VT* r, VT* z, VT* tmp,
                           const VT* linv, const VT* lc) {
   cudaStream_t st = E.st;
   if (pc == 1) {
-    k_copy_cast<VT, VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p,
+    k_copy_cast<VT, VT><<<E.cbm1.nblk, kThreads, 0, st>>>(E.cbm1.mem.p, E.cbm1.r0.p, E.cbm1.r1.p,
         E.d_active.p, r, z, nullptr, 0);
-    k_scale_vec<VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p,
+    k_scale_vec<VT><<<E.cbm1.nblk, kThreads, 0, st>>>(E.cbm1.mem.p, E.cbm1.r0.p, E.cbm1.r1.p,
         E.d_active.p, z, dinv);
     E.count(2);
     if (w) {
-      k_dot<VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p, E.d_active.p,
+      k_dot<VT><<<E.cbm1.nblk, kThreads, 0, st>>>(E.cbm1.mem.p, E.cbm1.r0.p, E.cbm1.r1.p, E.d_active.p,
           w, z, nullptr, E.d_sc.p, SC_N, SC_QZ);
       E.count();
     }
   } else if (pc == 2) {
-    k_line_apply<VT><<<cdiv(E.nsurf, 128), 128, 0, st>>>(E.nsurf, E.d_srows.p, E.d_mem.p,
-        E.d_active.p, E.d_ms.p, linv, lc, r, z, w, E.d_sc.p, SC_N, SC_QZ);
+    if (E.cbms.nblk)
+      k_line_apply<VT><<<E.cbms.nblk, kThreads, 0, st>>>(E.cbms.mem.p, E.cbms.r0.p, E.cbms.r1.p,
+          E.d_active.p, E.d_ms.p, linv, lc, r, z, w, E.d_sc.p, SC_N, SC_QZ);
     E.count();
   } else {
     for (size_t l = 0; l + 1 < E.lev_f_ptr.size(); ++l) {
@@ -2438,7 +2605,7 @@ static void precond_apply(Engine& E, int pc, const VT* r, VT* z, VT* tmp,
       E.count();
     }
     if (w) {
-      k_dot<VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p, E.d_active.p,
+      k_dot<VT><<<E.cbm1.nblk, kThreads, 0, st>>>(E.cbm1.mem.p, E.cbm1.r0.p, E.cbm1.r1.p, E.d_active.p,
           w, z, nullptr, E.d_sc.p, SC_N, SC_QZ);
       E.count();
     }
@@ -2450,12 +2617,13 @@ static void precond_setup(Engine& E, int pc, const MT* vals, FT* F, VT* dinv,
                           VT* linv, VT* lc) {
   cudaStream_t st = E.st;
   if (pc == 1) {
-    k_jacobi_setup<MT, VT><<<E.bm1.nblk, kThreads, 0, st>>>(E.bm1.mem.p, E.bm1.r0.p, E.bm1.r1.p,
+    k_jacobi_setup<MT, VT><<<E.cbm1.nblk, kThreads, 0, st>>>(E.cbm1.mem.p, E.cbm1.r0.p, E.cbm1.r1.p,
         E.d_active.p, E.d_diag.p, vals, E.d_dmask.p, dinv);
     E.count();
   } else if (pc == 2) {
-    k_line_setup<MT, VT><<<cdiv(E.nsurf, 128), 128, 0, st>>>(E.nsurf, E.d_srows.p, E.d_mem.p,
-        E.d_active.p, E.d_ms.p, E.d_diag.p, E.d_down.p, vals, E.d_dmask.p, linv, lc);
+    if (E.cbms.nblk)
+      k_line_setup<MT, VT><<<E.cbms.nblk, kThreads, 0, st>>>(E.cbms.mem.p, E.cbms.r0.p, E.cbms.r1.p,
+          E.d_active.p, E.d_ms.p, E.d_diag.p, E.d_down.p, vals, E.d_dmask.p, linv, lc);
     E.count();
   } else {
     for (size_t l = 0; l + 1 < E.lev_f_ptr.size(); ++l) {
@@ -2494,12 +2662,12 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk) {
   precond_setup<MT, VT, FT>(*this, pc, vals, F, dinv, linv, lc);
   // x0 = M^-1 b, xlung = |b_masked|^2 (b is zero at Dirichlet rows)
   CG_TRY(cudaMemsetAsync(d_sc.p, 0, sizeof(double) * nmem * SC_N, st));
-  k_dot<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, b, b,
+  k_dot<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, b, b,
                                             d_dmask.p, d_sc.p, SC_N, SC_XL);
   count();
   precond_apply<MT, VT, FT>(*this, pc, b, x, tmp, nullptr, F, dinv, linv, lc);
   // r = b - A x ; p = M^-1 r
-  k_resid<MT, VT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_active.p,
+  k_resid<MT, VT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_active.p,
       d_rowptr.p, d_cols.p, vals, d_dmask.p, x, b, r, nullptr, 0);
   count();
   precond_apply<MT, VT, FT>(*this, pc, r, p, tmp, nullptr, F, dinv, linv, lc);
@@ -2510,16 +2678,16 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk) {
   for (int it = 0; it < itmax + 2; ++it) {
     // q = A p, pq = p.q, pr = p.r
     if (prof) prof_begin();
-    k_spmv<MT, VT><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_active.p,
+    k_spmv<MT, VT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_active.p,
         d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N,
         prof ? d_prof_bytes.p : nullptr);
     count();
     if (prof) prof_end();
-    k_pcg_update_rx<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p,
+    k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
         d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
     count();
     precond_apply<MT, VT, FT>(*this, pc, r, z, tmp, q, F, dinv, linv, lc);
-    k_pcg_update_p<VT><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p,
+    k_pcg_update_p<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
         d_sc.p, p, z);
     count();
     if (it % chk == 0) CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
@@ -2546,7 +2714,7 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
          *scr2 = w64[11].p, *dd = w64[12].p, *tmp = w64[13].p;
   const bool jac = (isolv == -5);
   auto E1 = [&](auto kern, auto... args) {
-    kern<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, args...);
+    kern<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, args...);
     count();
   };
   auto lsolve = [&](const double* in, double* out) {
@@ -2568,7 +2736,7 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
     }
   };
   auto spmv = [&](const double* in, double* out) {
-    k_spmv<double, double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
+    k_spmv<double, double><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
         d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out, nullptr, nullptr, 0, nullptr);
     count();
   };
@@ -2590,11 +2758,11 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
     scv[(size_t)m * SC_N + SC_ETAJ] = 1.0;
   }
   d_sc.upload(scv.data(), scv.size(), st);
-  k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, b, b,
+  k_dot<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, b, b,
       d_dmask.p, d_sc.p, SC_N, SC_XL);
   count();
   if (jac) {
-    k_jacobi_setup<double, double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p,
+    k_jacobi_setup<double, double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
         d_active.p, d_diag.p, vals, d_dmask.p, dd);
     count();
     E1(k_copy_cast<double, double>, (const double*)b, x, (const double*)nullptr, 0);
@@ -2619,7 +2787,7 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
     spmv(x, scr1);
     E1(k_sub_vec<double>, scr1, (const double*)b, (const double*)scr1);
     lsolve(scr1, r);             // r0 = L^-1 (b - A x0)
-    k_umul<double, double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
+    k_umul<double, double><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
         d_active.p, d_rowptr.p, d_cols.p, d_diag.p, d_G64.p, x, scr1);
     count();
     E1(k_copy_cast<double, double>, (const double*)scr1, x, (const double*)nullptr, 0);  // y0 = U x0
@@ -2631,12 +2799,12 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
   d_niter.upload(ones.data(), nmem, st);
   check_launch();
   for (int it = 0; it < itmax + 3; ++it) {
-    k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, rt, r,
+    k_dot<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, rt, r,
         nullptr, d_sc.p, SC_N, SC_ROJ);
     count();
     E1(k_bicg_p<double>, (const double*)d_sc.p, p, (const double*)r, (const double*)pjm, (const double*)vjm);
     applyB(p, v);
-    k_dot<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_active.p, rt, v,
+    k_dot<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, rt, v,
         nullptr, d_sc.p, SC_N, SC_SIG);
     count();
     E1(k_bicg_s<double>, (const double*)d_sc.p, s, (const double*)r, (const double*)v);
@@ -2683,11 +2851,14 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
     // FP32 path: the Picard loop is the FP64 refinement loop (its residual is
     // FP64-grade, see the FP32 kernels); the inner FP32 PCG solves each
     // correction to opts.inner_tol.
-    k_vg_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd, nf,
+    k_vg_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd, nf,
                                             d_nodal[ND_Z].p);
-    k_bcflux_f32<<<cdiv(nsurf, kThreads), kThreads, 0, st>>>(nsurf, d_srows.p, d_act.p, d_ms.p, nd,
-                                                             nf.qneu, nf.bcf);
-    k_assemble_picard_f32<<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p,
+    k_elem_f32<<<cbme.nblk, kThreads, 0, st>>>(cbme.mem.p, cbme.r0.p, cbme.r1.p, d_act.p, d_tet.p, nf);
+    count();
+    if (cbms.nblk)
+      k_bcflux_f32<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p,
+                                                   nd, nf.qneu, nf.bcf);
+    k_assemble_picard_f32<<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
         d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, d_rec32.p, d_dmask.p,
         nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o);
     k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
@@ -2695,11 +2866,11 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
     check_launch();
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
                             std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1);
-    k_update_shl_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd,
+    k_update_shl_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
                                                     nf.pdiff);
     count();
   } else {
-    k_vg<double><<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd,
+    k_vg<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd,
                                                 iopt == 2);
     count();
     check_launch();
@@ -2708,27 +2879,32 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
     count();
     if (iopt == 1) solve_pcg<double, double>(P0.itmxcg, P0.tolcg, true, 1);
     else solve_bicgstab(P0.isolv, P0.itmxcg, P0.tolcg);
-    k_update_shl<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd);
+    k_update_shl<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd);
     count();
   }
   CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
   CG_TRY(cudaMemsetAsync(d_redmax.p, 0, sizeof(double) * nmem * 2, st));
   CG_TRY(cudaMemsetAsync(d_ikmax.p, 0, sizeof(int32_t) * nmem, st));
   if (mixed) {
-    k_bkflux_f32<<<cdiv((long)ndrows * kGroup, kThreads), kThreads, 0, st>>>(ndrows, d_drows.p,
-        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
-    k_masbal_norms_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p,
+    if (cbms16.nblk)
+      k_bkflux_f32<<<cbms16.nblk, kThreads, 0, st>>>(cbms16.mem.p, cbms16.r0.p, cbms16.r1.p,
+          d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
+    if (ndeep)
+      k_bkflux_list_f32<<<cdiv((long)ndeep * kGroup, kThreads), kThreads, 0, st>>>(ndeep, d_deep.p,
+          d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
+    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
         d_ms.p, nd, nf, nf.volnod, nf.pnodi, d_red.p, d_redmax.p);
     count();
   } else
-    k_masbal_norms<double><<<bm16.nblk, kThreads, 0, st>>>(bm16.mem.p, bm16.r0.p, bm16.r1.p, d_act.p,
+    k_masbal_norms<double><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_act.p,
         d_ms.p, d_rowptr.p, d_cols.p, d_vals64.p, nd, d_red.p, d_redmax.p, iopt == 2);
-  k_ikmax<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, nd, d_redmax.p,
+  k_ikmax<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd, d_redmax.p,
                                          d_ikmax.p, mixed ? 1 : 0);
   k_gather_ik<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_node_off.p, d_ikmax.p, nd, d_ikval.p);
   k_switch_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_red.p, d_redmax.p, d_ms.p,
                                                   P0.l2norm, d_switch.p);
-  k_switch<<<cdiv(nsurf, kThreads), kThreads, 0, st>>>(nsurf, d_srows.p, d_act.p, d_switch.p, d_ms.p, nd);
+  if (cbms.nblk)
+    k_switch<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_switch.p, d_ms.p, nd);
   count(5);
   check_launch();
 }
@@ -2752,9 +2928,17 @@ int Engine::macro_iteration() {
   }
   push_scalars();
   d_act.upload(h_act.data(), nmem, st);
-  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 0, need_sw_flag());
-  k_start_surface<<<cdiv(nsurf, kThreads), kThreads, 0, st>>>(nsurf, d_srows.p, d_act.p, d_ms.p, nd);
-  k_start_nodes<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_act.p, d_ms.p, nd, 1, need_sw_flag());
+  {
+    std::vector<uint8_t> memact(nmem);
+    for (int m = 0; m < nmem; ++m) memact[m] = h_act[m] != 0;
+    compact_maps(memact);
+  }
+  if (cbm1.nblk)
+    k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 0, need_sw_flag());
+  if (cbms.nblk)
+    k_start_surface<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p, nd);
+  if (cbm1.nblk)
+    k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 1, need_sw_flag());
   count(3);
   check_launch();
   if (niter_members == 0) {
@@ -2829,9 +3013,9 @@ int Engine::macro_iteration() {
     d_mask2.upload(conv_mask.data(), nmem, st);
     CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
     if (precision == 1 && iopt == 1)
-      k_store1_f32<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_mask2.p, nd, nf, d_red.p);
+      k_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, nf, d_red.p);
     else
-      k_store1<<<bm1.nblk, kThreads, 0, st>>>(bm1.mem.p, bm1.r0.p, bm1.r1.p, d_mask2.p, nd, d_red.p);
+      k_store1<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, d_red.p);
     count();
     check_launch();
     d_red.download(red.data(), red.size(), st);
@@ -3078,8 +3262,9 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   if (a & ACT_START) { h.iterating = true; h.iter = 1; h.nitert = 0; }
   e->push_scalars();
   e->d_act.upload(act.data(), e->nmem, e->st);
+  e->compact_maps(std::vector<uint8_t>(e->nmem, 1));
   k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0, e->need_sw_flag());
-  k_start_surface<<<cdiv(e->nsurf, kThreads), kThreads, 0, e->st>>>(e->nsurf, e->d_srows.p, e->d_act.p, e->d_ms.p, e->nd);
+  k_start_surface<<<e->bms.nblk, kThreads, 0, e->st>>>(e->bms.mem.p, e->bms.r0.p, e->bms.r1.p, e->d_act.p, e->d_ms.p, e->nd);
   k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 1, e->need_sw_flag());
   act[m] = ACT_ITER;
   e->d_act.upload(act.data(), e->nmem, e->st);
@@ -3087,7 +3272,9 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   if (mixed) {
     k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->nd, e->nf,
                                                   e->d_nodal[ND_Z].p);
-    k_bcflux_f32<<<cdiv(e->nsurf, kThreads), kThreads, 0, e->st>>>(e->nsurf, e->d_srows.p, e->d_act.p,
+    k_elem_f32<<<e->bme.nblk, kThreads, 0, e->st>>>(e->bme.mem.p, e->bme.r0.p, e->bme.r1.p, e->d_act.p,
+                                                    e->d_tet.p, e->nf);
+    k_bcflux_f32<<<e->bms.nblk, kThreads, 0, e->st>>>(e->bms.mem.p, e->bms.r0.p, e->bms.r1.p, e->d_act.p,
         e->d_ms.p, e->nd, e->nf.qneu, e->nf.bcf);
     k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
         e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_tet.p,
@@ -3218,6 +3405,11 @@ void Engine::bare_init(int n, const std::vector<int32_t>& rowptr,
   d_niter.alloc(1); d_nact.alloc(1); d_nact_dummy.alloc(1);
   make_blockmap(bm1, kThreads);
   make_blockmap(bm16, kRowsPerBlock16);
+  {
+    std::vector<int32_t> mm(1, 0);
+    (void)mm;
+  }
+  init_compaction();
   uint8_t one = 1, it = ACT_ITER;
   d_active.upload(&one, 1, st);
   d_act.upload(&it, 1, st);
