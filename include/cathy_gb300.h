@@ -215,6 +215,40 @@ int32_t cathy_gb300_asspic(const int32_t* nt, const int32_t* ntri,
                            const double* di, const int32_t* maxstr,
                            const int32_t* nterm);
 
+/* ---- learned column-line preconditioner -------------------------------- */
+/* No reference counterpart (the reference has no learned component); it is
+ * the learned preconditioner wrapped inside the Picard PCG of the handle API
+ * (SYMSLV's role, solscal-extended.f:4669).  A model is a small edge-wise
+ * message-passing network (hidden width 64, BF16 weights, FP32
+ * accumulation) that predicts per-edge weights omega_ij for the row-sum
+ * compensation of the column-line (vertical tridiagonal block Jacobi)
+ * factor: d'_i = a_ii + sum_{j horizontal} omega_ij a_ij.  Parameters are a
+ * packed float vector of CATHY_GB300_LP_NPARAMS values:
+ * W1 (64x16) | b1 (64) | W2 (64x64) | b2 (64) | w3 (64) | b3 (1). */
+#define CATHY_GB300_LP_NPARAMS 5313
+#define CATHY_GB300_LP_NPAIRS 4
+/* params may be NULL (all zero) */
+int32_t cathy_gb300_lp_create(const float* params, int32_t device, void** model);
+int32_t cathy_gb300_lp_destroy(void* model);
+/* get (may be NULL) / set (may be NULL) parameters; lr > 0 sets the Adam
+ * learning rate; steps (may be NULL) receives the Adam steps taken */
+int32_t cathy_gb300_lp_params(void* model, float* get, const float* set,
+                              double lr, int64_t* steps);
+/* One graph given on the host: full 0-based CSR of the Picard matrix (n
+ * rows, nodes numbered layer by layer with nnod nodes per layer), Dirichlet
+ * mask, nodal Ks, porosity and dSw/dpsi, the time step, and npairs Krylov
+ * pairs (P, Q = A P; npairs x n).  train_steps = 0 evaluates the loss, the
+ * network outputs (dprime: n, omega: nnz) and the parameter gradients
+ * (grads: NPARAMS); train_steps > 0 first takes that many Adam steps. */
+int32_t cathy_gb300_lp_eval(void* model, int32_t n, int32_t nnod,
+                            const int32_t* rowptr, const int32_t* cols,
+                            const float* vals, const uint8_t* dmask,
+                            const float* ks, const float* pnodi,
+                            const float* et2, float dt, int32_t npairs,
+                            const float* P, const float* Q,
+                            int32_t train_steps, double* loss, float* dprime,
+                            float* omega, float* grads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,6 +14,8 @@ from . import build as _build
 
 i32p = C.POINTER(C.c_int32)
 f64p = C.POINTER(C.c_double)
+f32p = C.POINTER(C.c_float)
+u8p = C.POINTER(C.c_uint8)
 
 OK, ENODEV, EINVAL, EMESH, ENOMEM, EUNSUP = 0, -1, -2, -3, -4, -5
 _ERRS = {ENODEV: "no usable CUDA device / CUDA error", EINVAL: "invalid argument",
@@ -119,6 +121,13 @@ EXPORTS = {
     "cathy_gb300_asspic": (C.c_int32, [i32p, i32p, i32p, i32p, f64p, f64p, f64p, f64p,
                                        f64p, f64p, f64p, f64p, f64p, f64p, f64p, f64p,
                                        f64p, f64p, f64p, f64p, i32p, i32p]),
+    "cathy_gb300_lp_create": (C.c_int32, [f32p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "cathy_gb300_lp_destroy": (C.c_int32, [C.c_void_p]),
+    "cathy_gb300_lp_params": (C.c_int32, [C.c_void_p, f32p, f32p, C.c_double,
+                                          C.POINTER(C.c_int64)]),
+    "cathy_gb300_lp_eval": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, i32p, i32p, f32p,
+                                        u8p, f32p, f32p, f32p, C.c_float, C.c_int32, f32p,
+                                        f32p, C.c_int32, f64p, f32p, f32p, f32p]),
 }
 
 _lib = None
