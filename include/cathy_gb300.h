@@ -249,6 +249,36 @@ int32_t cathy_gb300_lp_eval(void* model, int32_t n, int32_t nnod,
                             int32_t train_steps, double* loss, float* dprime,
                             float* omega, float* grads);
 
+/* ---- allocation-free solve ----------------------------------------------- */
+/* No counterpart in the reference: an extra entry point of this library for
+ * callers that may not allocate device memory while they run (a driver whose
+ * device memory belongs to a host framework's pool, or code that must not
+ * allocate between time steps).  It runs the NSYSLV ISOLV=-5 solve of
+ * cathy_gb300_nsyslv (Jacobi-preconditioned BiCGSTAB, same recurrences and
+ * stopping rule) on arrays the caller already holds in DEVICE memory:
+ * NODDIR (numdir, 1-based), JA/TOPOL (1-based full CSR), COEF1, TNOTI and
+ * the output PNEW.  Scalars and the outputs NITER/ERR/RES are host pointers;
+ * `stream` is a cudaStream_t (NULL = default stream).
+ *
+ * All workspace lives in one fixed device array compiled into the library,
+ * so nothing is allocated: no cudaMalloc, cudaFree or allocating library
+ * call.  That array is held on every GPU that loads the library until the
+ * process exits, and it bounds n at CATHY_GB300_NOALLOC_MAXN rows; larger
+ * systems are rejected with CATHY_GB300_EINVAL.  The first call on a device
+ * looks up the array's device address (make that first call before any
+ * stream capture).  Every call reuses the same array, so calls that overlap
+ * on the GPU (from two streams or two host threads) race on it. */
+#define CATHY_GB300_NOALLOC_MAXN 131072
+int32_t cathy_gb300_nsyslv_noalloc(const int32_t* n, const int32_t* numdir,
+                                   const int32_t* noddir_dev,
+                                   const int32_t* itmxcg, int32_t* niter,
+                                   const int32_t* ja_dev,
+                                   const int32_t* topol_dev,
+                                   const double* tolcg,
+                                   const double* coef1_dev, double* pnew_dev,
+                                   const double* tnoti_dev, double* err,
+                                   double* res, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcathy_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "capi.cu", "mesh.cpp", "learned.cu"]
+SOURCES = ["engine.cu", "capi.cu", "mesh.cpp", "noalloc.cu", "learned.cu"]
 HEADERS = ["engine.h", "kernels.cuh", "mesh.h", "learned.h"]
 
 
