@@ -96,6 +96,10 @@ typedef struct cathy_opts {
   int32_t inner_maxit;         /* FP32 inner iterations per refinement     */
   double inner_tol;            /* FP32 inner relative tolerance            */
   int32_t verbose;
+  int32_t graphs;              /* 1: run each Picard iteration of the FP32
+                                  path as one CUDA graph launch (the PCG
+                                  loop as a device-driven conditional node);
+                                  0: launch kernel by kernel               */
 } cathy_opts_t;
 
 /* per nonlinear iteration record (the reference's `iter` file) */
@@ -169,6 +173,12 @@ int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
 /* GPU time spent in the hot path (ms) since creation, and kernel launches */
 int32_t cathy_gb300_stats(void* handle, double* gpu_ms, int64_t* launches,
                           int64_t* lin_iters, int64_t* nl_iters);
+
+/* Host-side timers of the time stepping (out[0..n), n <= 7): macro-iterations
+ * (one nonlinear iteration of every member with work), CUDA graph launches,
+ * graph builds, host preparation ms, device wait ms (launch + synchronise),
+ * host decision ms, GPU ms of the hot path. */
+int32_t cathy_gb300_timers(void* handle, double* out, int32_t n);
 
 /* ---- Fortran subroutine drop-ins ---------------------------------------- */
 /* SYMSLV(IOUT,N,NTERM,NUMDIR,NITER,ITMXCG,TOLCG,RMIN,NODDIR,JA,TOPOL,PNEW,

@@ -70,7 +70,7 @@ class Member(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
                 ("inner_maxit", C.c_int32), ("inner_tol", C.c_double),
-                ("verbose", C.c_int32)]
+                ("verbose", C.c_int32), ("graphs", C.c_int32)]
 
 
 class IterRec(C.Structure):
@@ -112,6 +112,7 @@ EXPORTS = {
                                         f64p]),
     "cathy_gb300_stats": (C.c_int32, [C.c_void_p, f64p, C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "cathy_gb300_timers": (C.c_int32, [C.c_void_p, f64p, C.c_int32]),
     "cathy_gb300_symslv": (C.c_int32, [i32p, i32p, i32p, i32p, i32p, i32p, f64p, f64p,
                                        i32p, i32p, i32p, f64p, f64p, f64p, f64p, f64p,
                                        f64p, f64p]),

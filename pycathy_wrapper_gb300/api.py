@@ -87,7 +87,8 @@ class Simulation:
     """
 
     def __init__(self, cases: Union[Case, Sequence[Case]], precision: int = 0,
-                 device: int = 0, inner_maxit: int = 200, inner_tol: float = 1e-6):
+                 device: int = 0, inner_maxit: int = 200, inner_tol: float = 1e-6,
+                 graphs: bool = True):
         self.L = _lib.load()
         self.cases: List[Case] = [cases] if isinstance(cases, Case) else list(cases)
         keep = _Keep()
@@ -95,7 +96,7 @@ class Simulation:
         for m, c in enumerate(self.cases):
             arr[m] = _member(c, keep)
         opts = _lib.Opts(precision=precision, device=device, inner_maxit=inner_maxit,
-                         inner_tol=inner_tol, verbose=0)
+                         inner_tol=inner_tol, verbose=0, graphs=1 if graphs else 0)
         h = C.c_void_p()
         check(self.L.cathy_gb300_create(len(self.cases), arr, C.byref(opts), C.byref(h)),
               "cathy_gb300_create")
@@ -192,6 +193,14 @@ class Simulation:
         check(self.L.cathy_gb300_profile(self.h, enable, C.byref(ms), C.byref(n), C.byref(bts)),
               "cathy_gb300_profile")
         return ms.value, n.value, bts.value
+
+    def timers(self):
+        """Host-side phase timers of the time stepping."""
+        out = (C.c_double * 7)()
+        check(self.L.cathy_gb300_timers(self.h, out, 7), "cathy_gb300_timers")
+        k = ("macro_iterations", "graph_launches", "graph_builds", "host_prep_ms",
+             "device_wait_ms", "host_decision_ms", "gpu_ms")
+        return {a: out[i] for i, a in enumerate(k)}
 
     def stats(self):
         ms = C.c_double()

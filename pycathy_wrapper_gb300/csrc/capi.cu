@@ -60,7 +60,7 @@ int32_t cathy_gb300_create(int32_t nmembers, const cathy_member_t* members,
                            const cathy_opts_t* opts, void** handle) {
   if (!handle || nmembers <= 0 || !members) return CATHY_GB300_EINVAL;
   if (!have_device()) return CATHY_GB300_ENODEV;
-  cathy_opts_t o = opts ? *opts : cathy_opts_t{0, 0, 0, 0.0, 0};
+  cathy_opts_t o = opts ? *opts : cathy_opts_t{0, 0, 0, 0.0, 0, 1};
   g_last_verbose = o.verbose;
   return guarded([&]() {
     *handle = engine_create(nmembers, members, o);
@@ -139,6 +139,11 @@ int32_t cathy_gb300_stats(void* h, double* gpu_ms, int64_t* launches,
                           int64_t* lin_iters, int64_t* nl_iters) {
   if (!h) return CATHY_GB300_EINVAL;
   return engine_stats((Engine*)h, gpu_ms, launches, lin_iters, nl_iters);
+}
+
+int32_t cathy_gb300_timers(void* h, double* out, int32_t n) {
+  if (!h || !out || n < 0) return CATHY_GB300_EINVAL;
+  return engine_timers((Engine*)h, out, n);
 }
 
 int32_t cathy_gb300_symslv(const int32_t* iout, const int32_t* n,

@@ -627,38 +627,95 @@ k_assemble_newton(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm
 // y = A x with Dirichlet rows as identity; optionally accumulates per-member
 // dot products d0 += x.y and d1 += x.w (w optional).  Arithmetic in the
 // vector type VT; per-block sums are promoted to FP64 before the atomics.
+// Device-clock timing of one kernel launch: the first block to start records
+// the start time, the last block to finish the end time, into a per-launch
+// slot; slot = LT_SEQ advances when a launch completes.  Works inside CUDA
+// graphs (where event records are not allowed in conditional bodies).
+enum { LT_SEQ = 0, LT_DONE = 1, LT_HDR = 2 };
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// y = A x with Dirichlet rows as identity; optionally accumulates per-member
+// dot products d0 += x.y and d1 += x.w (w optional).  Persistent grid: each
+// block walks a contiguous run of block-map entries (16 rows per entry, 16
+// lanes per row); per-member sums stay in registers while the entries belong
+// to the same member and are flushed (one block reduction, one FP64 atomic
+// per quantity) when the member changes.  Arithmetic in the vector type VT.
 template <class MT, class VT>
 __global__ void __launch_bounds__(kThreads)
-k_spmv(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
        const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
        const MT* vals, const uint8_t* dmask, const VT* x, VT* y, const VT* w,
-       double* acc, int acc_stride, double* alg_bytes) {
-  const int m = bm_mem[blockIdx.x];
-  if (!active[m]) return;
+       double* acc, int acc_stride, double* alg_bytes, unsigned long long* lt,
+       int lt_cap) {
+  __shared__ int s_slot;
+  if (lt) {
+    if (threadIdx.x == 0) {
+      const unsigned long long q = lt[LT_SEQ];
+      s_slot = q < (unsigned long long)lt_cap ? (int)q : -1;  // full: stop timing
+      if (s_slot >= 0) atomicMin(&lt[LT_HDR + 2 * s_slot], (unsigned long long)gtimer());
+    }
+    __syncthreads();
+    if (s_slot < 0) lt = nullptr;
+  }
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
-  const int i = bm_r0[blockIdx.x] + grp;
-  const bool rowok = i < bm_r1[blockIdx.x];
-  if (alg_bytes && threadIdx.x == 0) {
-    // values + column indices + row pointers + x read + y written (+ w read)
-    const int r0 = bm_r0[blockIdx.x], r1 = bm_r1[blockIdx.x];
-    const double nz = (double)(rowptr[r1] - rowptr[r0]);
-    atomicAdd(alg_bytes, nz * (sizeof(MT) + 4) + (r1 - r0) * (4.0 + (w ? 3.0 : 2.0) * sizeof(VT)));
-  }
-  VT s = 0;
-  if (rowok) {
-    const int s0 = rowptr[i] + lane;
-    if (s0 < rowptr[i + 1]) s = (VT)vals[s0] * x[cols[s0]];
-  }
-  s = group_sum<VT>(s);
   VT d[2] = {0, 0};
-  if (rowok && lane == 0) {
-    const VT xi = x[i];
-    const VT yi = dmask[i] ? xi : s;
-    y[i] = yi;
-    d[0] = xi * yi;
-    if (w) d[1] = xi * w[i];
+  int cur = -1;
+  double bytes = 0.0;
+  // each block takes a contiguous run of map entries (one or two members)
+  const int chunk = (nblk + gridDim.x - 1) / gridDim.x;
+  const int b0 = blockIdx.x * chunk, b1 = min(nblk, b0 + chunk);
+  for (int b = b0; b < b1; ++b) {
+    const int m = bm_mem[b];
+    if (!active[m]) continue;  // block-uniform
+    if (acc && m != cur) {
+      if (cur >= 0) {
+        block_accumulate_t<VT, 2>(d, acc + (size_t)cur * acc_stride);
+        __syncthreads();
+      }
+      d[0] = d[1] = 0;
+      cur = m;
+    }
+    const int r0 = bm_r0[b], r1 = bm_r1[b];
+    const int i = r0 + grp;
+    const bool rowok = i < r1;
+    if (alg_bytes && threadIdx.x == 0) {
+      // values + column indices + row pointers + x read + y written (+ w read)
+      const double nz = (double)(rowptr[r1] - rowptr[r0]);
+      bytes += nz * (sizeof(MT) + 4) + (r1 - r0) * (4.0 + (w ? 3.0 : 2.0) * sizeof(VT));
+    }
+    VT s = 0;
+    if (rowok) {
+      const int s0 = rowptr[i] + lane;
+      if (s0 < rowptr[i + 1]) s = (VT)vals[s0] * x[cols[s0]];
+    }
+    s = group_sum<VT>(s);
+    if (rowok && lane == 0) {
+      const VT xi = x[i];
+      const VT yi = dmask[i] ? xi : s;
+      y[i] = yi;
+      d[0] += xi * yi;
+      if (w) d[1] += xi * w[i];
+    }
   }
-  if (acc) block_accumulate_t<VT, 2>(d, acc + (size_t)m * acc_stride);
+  if (acc && cur >= 0) block_accumulate_t<VT, 2>(d, acc + (size_t)cur * acc_stride);
+  if (alg_bytes && threadIdx.x == 0 && bytes != 0.0) atomicAdd(alg_bytes, bytes);
+  if (lt) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicMax(&lt[LT_HDR + 2 * s_slot + 1], (unsigned long long)gtimer());
+      const unsigned long long done = atomicAdd(&lt[LT_DONE], 1ull);
+      if (done == gridDim.x - 1) {
+        lt[LT_DONE] = 0;
+        __threadfence();
+        lt[LT_SEQ] = (unsigned long long)(s_slot + 1);
+      }
+    }
+  }
 }
 
 // r = b - A x (masked), r zero at Dirichlet rows
@@ -1154,6 +1211,45 @@ __global__ void k_krylov_decide(int nmem, uint8_t* active, double* sc,
     S[SC_ROJ] = S[SC_SIG] = S[SC_AA] = S[SC_BB] = 0.0;
   }
   if (m < nmem) atomicAdd(nact, a);
+}
+
+// PCG decision inside a CUDA graph: the same per-member test as
+// k_krylov_decide (mode 0) by one block, then the condition of the graph's
+// WHILE node = (any member still iterating) and (loop count below cap).
+__global__ void __launch_bounds__(256)
+k_krylov_decide_g(int nmem, uint8_t* active, double* sc, int32_t* niter, int itmax,
+                  double tol, int32_t* loops, int maxloops, cudaGraphConditionalHandle h) {
+  __shared__ int s_cnt;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int m = threadIdx.x; m < nmem; m += blockDim.x) {
+    if (!active[m]) continue;
+    double* S = sc + (size_t)m * SC_N;
+    const double xl = S[SC_XL];
+    const double err = (xl > 0.0) ? sqrt(S[SC_RR] / xl) : 0.0;
+    S[SC_ERR] = err;
+    if (err > tol && niter[m] < itmax) {
+      niter[m] += 1;
+      mine++;
+    } else {
+      active[m] = 0;
+    }
+    S[SC_PR] = S[SC_PQ] = S[SC_QZ] = S[SC_RR] = 0.0;
+  }
+  if (mine) atomicAdd(&s_cnt, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int l = *loops + 1;
+    *loops = l;
+    cudaGraphSetConditional(h, (s_cnt > 0 && l < maxloops) ? 1u : 0u);
+  }
+}
+
+// niter[m] = 1 for the members in the Krylov solve
+__global__ void k_niter_init(int nmem, const uint8_t* active, int32_t* niter) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < nmem && active[m]) niter[m] = 1;
 }
 
 // ============================================================================
@@ -1865,9 +1961,8 @@ struct Engine {
   std::vector<uint8_t> h_act;
 
   ~Engine() {
-    for (auto& ev : pev) cudaEventDestroy(ev);
-    if (pe0) cudaEventDestroy(pe0);
-    if (pe1) cudaEventDestroy(pe1);
+    graph_free();
+    pinned_free();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -1885,32 +1980,76 @@ struct Engine {
   void push_scalars();
   int macro_iteration();
   void picard_or_newton_iteration(const std::vector<int>& itm);
-  template <class MT, class VT> void solve_pcg(int itmax, double tol, bool ref_mode, int chk = 1);
+  // phase 0: whole solve with host checks every chk iterations; 1: set-up
+  // only; 2: one iteration + graph decision (the body of a WHILE node)
+  template <class MT, class VT> void solve_pcg(int itmax, double tol, bool ref_mode, int chk = 1,
+                                               int phase = 0,
+                                               cudaGraphConditionalHandle gh = 0);
   DBuf<int32_t> d_nact_dummy;
   DBuf<double> d_prof_bytes;
-  std::vector<cudaEvent_t> pev;
-  int pev_used = 0;
-  void prof_begin() {
-    if (pev_used * 2 + 2 > (int)pev.size()) prof_flush();
-    CG_TRY(cudaEventRecord(pev[2 * pev_used], st));
-  }
-  void prof_end() {
-    CG_TRY(cudaEventRecord(pev[2 * pev_used + 1], st));
-    pev_used++;
+  // live SpMV timing on the device clock (see k_spmv): slots of
+  // (start, end) per launch; flushed into prof_ms by the host
+  DBuf<unsigned long long> d_lt;
+  int lt_cap = 1 << 16;
+  int64_t lt_pending = 0;     // launches written since the last flush
+  int persist_blocks = 1216;  // grid of the persistent kernels (8 per SM)
+  void lt_reset() {
+    std::vector<unsigned long long> h((size_t)LT_HDR + 2 * (size_t)lt_cap);
+    h[LT_SEQ] = 0;
+    h[LT_DONE] = 0;
+    for (int q = 0; q < lt_cap; ++q) {
+      h[LT_HDR + 2 * q] = ~0ull;
+      h[LT_HDR + 2 * q + 1] = 0ull;
+    }
+    if (!d_lt.p) d_lt.alloc(h.size());
+    d_lt.upload(h.data(), h.size(), st);
+    CG_TRY(cudaStreamSynchronize(st));
+    lt_pending = 0;
   }
   void prof_flush() {
-    if (!pev_used) return;
-    CG_TRY(cudaEventSynchronize(pev[2 * pev_used - 1]));
-    for (int u = 0; u < pev_used; ++u) {
-      float ms = 0;
-      CG_TRY(cudaEventElapsedTime(&ms, pev[2 * u], pev[2 * u + 1]));
-      prof_ms += ms;
-      prof_n += 1;
-    }
-    pev_used = 0;
+    if (!d_lt.p) return;
+    unsigned long long seq = 0;
+    CG_TRY(cudaStreamSynchronize(st));
+    d_lt.download(&seq, 1, st);
+    CG_TRY(cudaStreamSynchronize(st));
+    if (seq == 0) return;
+    const size_t k = std::min<size_t>(seq, (size_t)lt_cap);
+    std::vector<unsigned long long> h(2 * k);
+    CG_TRY(cudaMemcpyAsync(h.data(), d_lt.p + LT_HDR, sizeof(unsigned long long) * 2 * k,
+                           cudaMemcpyDeviceToHost, st));
+    CG_TRY(cudaStreamSynchronize(st));
+    for (size_t q = 0; q < k; ++q)
+      if (h[2 * q + 1] > h[2 * q]) {
+        prof_ms += (double)(h[2 * q + 1] - h[2 * q]) * 1e-6;
+        prof_n += 1;
+      }
+    lt_reset();
   }
+  int grid_persist(int nblk) const { return std::max(1, std::min(nblk, persist_blocks)); }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
+  void iteration_pre(int solve_phase);
+  void iteration_post();
+  void start_kernels();
+  // CUDA graph of one macro-iteration (FP32 Picard path)
+  cudaGraph_t g_graph = nullptr;
+  cudaGraphExec_t g_exec = nullptr;
+  int g_key[6] = {-1, -1, -1, -1, -1, -1};
+  int64_t g_nA = 0, g_nB = 0, g_nC = 0, g_builds = 0, g_launches = 0;
+  // host-side phase timers of macro-iterations (ms): preparation, waiting for
+  // the device (launch + synchronise), decisions; macro-iteration count
+  double tm_prep = 0, tm_dev = 0, tm_host = 0;
+  int64_t n_macro = 0;
+  DBuf<int32_t> d_loops;
+  uint8_t* hp_act = nullptr;
+  MemberScal* hp_ms = nullptr;
+  double *hp_red = nullptr, *hp_redmax = nullptr, *hp_ikv = nullptr, *hp_sc = nullptr;
+  int32_t *hp_ikmax = nullptr, *hp_nit = nullptr, *hp_loops = nullptr;
+  bool graphs_on() const { return opts.graphs != 0 && precision == 1 && iopt == 1; }
+  void graph_free();
+  void graph_build();
+  void pinned_alloc();
+  void pinned_free();
   // initial state for reset()
   std::vector<MemberHost> snap;
   DBuf<double> s_pnew, s_ptimep, s_atmpot, s_atmact, s_atmold, s_qpnew;
@@ -1919,7 +2058,6 @@ struct Engine {
   void reset();
   // live timing of the SpMV launches (CUDA events on the engine stream)
   bool prof = false;
-  cudaEvent_t pe0 = nullptr, pe1 = nullptr;
   double prof_ms = 0, prof_bytes = 0;
   int64_t prof_n = 0;
   // algorithmic bytes of one SpMV per member: nnz*(s_v+s_i) + (n+1)*s_i is
@@ -2412,13 +2550,16 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     spmv_bytes[m] = 8.0 * (double)g.nnz() + 4.0 * (g.n + 1);
     spmv_bytes_vec[m] = 3.0 * g.n;
   }
-  CG_TRY(cudaEventCreate(&pe0));
-  CG_TRY(cudaEventCreate(&pe1));
-  pev.resize(256);
-  for (auto& ev : pev) CG_TRY(cudaEventCreate(&ev));
+  {
+    int dev = 0, nsm = 0;
+    CG_TRY(cudaGetDevice(&dev));
+    CG_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    persist_blocks = std::max(1, nsm) * 8;
+  }
   d_nact_dummy.alloc(1);
   d_prof_bytes.alloc(1);
   d_prof_bytes.zero(st);
+  if (graphs_on()) pinned_alloc();
   CG_TRY(cudaStreamSynchronize(st));
 }
 
@@ -2531,7 +2672,8 @@ void Engine::push_scalars() {
     S.nnod = h.meshp->nnod; S.nstr = h.meshp->nstr; S.iopt = iopt; S.pad = 0;
     if (h.atm_nodal_dirty) nodal_dirty = true;
   }
-  d_ms.upload(h_ms.data(), nmem, st);
+  if (graphs_on()) std::memcpy(hp_ms, h_ms.data(), sizeof(MemberScal) * nmem);
+  else d_ms.upload(h_ms.data(), nmem, st);
   if (nodal_dirty) {
     for (int m = 0; m < nmem; ++m) {
       MemberHost& h = *M[m];
@@ -2643,7 +2785,8 @@ static void precond_setup(Engine& E, int pc, const MT* vals, FT* F, VT* dinv,
 // masked on the device after every iteration; the host reads the number of
 // active members every `chk` iterations.
 template <class MT, class VT>
-void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk) {
+void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
+                       cudaGraphConditionalHandle gh) {
   const MT* vals;
   if constexpr (sizeof(MT) == 8) vals = (const MT*)d_vals64.p; else vals = (const MT*)d_vals32.p;
   VT *b, *x, *r, *p, *q, *z, *tmp, *dinv, *linv = nullptr, *lc = nullptr;
@@ -2659,6 +2802,23 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk) {
     tmp = w32[6].p; dinv = w32[7].p; F = d_F32.p; linv = d_linv32.p; lc = d_lc32.p;
   }
   const int pc = precond;
+  if (phase == 2) {
+    // one PCG iteration of the graph's WHILE body (see below for the steps)
+    k_spmv<MT, VT><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+        cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
+        d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+    k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
+        d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
+    count(2);
+    precond_apply<MT, VT, FT>(*this, pc, r, z, tmp, q, F, dinv, linv, lc);
+    k_pcg_update_p<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
+        d_sc.p, p, z);
+    k_krylov_decide_g<<<1, 256, 0, st>>>(nmem, d_active.p, d_sc.p, d_niter.p, itmax, tol,
+        d_loops.p, itmax + 2, gh);
+    count(2);
+    check_launch();
+    return;
+  }
   precond_setup<MT, VT, FT>(*this, pc, vals, F, dinv, linv, lc);
   // x0 = M^-1 b, xlung = |b_masked|^2 (b is zero at Dirichlet rows)
   CG_TRY(cudaMemsetAsync(d_sc.p, 0, sizeof(double) * nmem * SC_N, st));
@@ -2671,18 +2831,25 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk) {
       d_rowptr.p, d_cols.p, vals, d_dmask.p, x, b, r, nullptr, 0);
   count();
   precond_apply<MT, VT, FT>(*this, pc, r, p, tmp, nullptr, F, dinv, linv, lc);
+  if (phase == 1) {
+    // graph set-up part: iteration counts and the WHILE node's loop counter
+    k_niter_init<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_active.p, d_niter.p);
+    CG_TRY(cudaMemsetAsync(d_loops.p, 0, sizeof(int32_t), st));
+    count();
+    check_launch();
+    return;
+  }
   std::vector<int32_t> ones(nmem, 1);
   d_niter.upload(ones.data(), nmem, st);
   check_launch();
   if (chk < 1) chk = 1;
   for (int it = 0; it < itmax + 2; ++it) {
     // q = A p, pq = p.q, pr = p.r
-    if (prof) prof_begin();
-    k_spmv<MT, VT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_active.p,
-        d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N,
-        prof ? d_prof_bytes.p : nullptr);
+    k_spmv<MT, VT><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+        cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
+        d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
     count();
-    if (prof) prof_end();
+    if (prof) lt_pending++;
     k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
         d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
     count();
@@ -2699,7 +2866,7 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk) {
       int32_t nact = 0;
       d_nact.download(&nact, 1, st);
       CG_TRY(cudaStreamSynchronize(st));
-      if (prof) prof_flush();
+      if (prof && lt_pending > lt_cap - 2 * (itmax + 4)) prof_flush();
       if (nact == 0) break;
     }
   }
@@ -2736,8 +2903,9 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
     }
   };
   auto spmv = [&](const double* in, double* out) {
-    k_spmv<double, double><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-        d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out, nullptr, nullptr, 0, nullptr);
+    k_spmv<double, double><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+        cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out,
+        nullptr, nullptr, 0, nullptr, nullptr, 0);
     count();
   };
   auto applyB = [&](const double* in, double* out) {
@@ -2842,9 +3010,11 @@ __global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
                                    (l2norm != 0 && pl2 <= ms[m].tolswi));
 }
 
-// One nonlinear iteration for every member flagged ACT_ITER.
-void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
-  (void)itm;
+// One nonlinear iteration for every member flagged ACT_ITER, in three
+// phases: pre-solve (soil characteristics, assembly, BCs), the linear solve,
+// post-solve (head update, mass balance, norms, switching).  The FP32
+// Picard path can also run as one CUDA graph (graph_build).
+void Engine::iteration_pre(int solve_phase) {
   const bool mixed = (precision == 1 && iopt == 1);
   const cathy_parm_t& P0 = M[0]->parm;
   if (mixed) {
@@ -2865,10 +3035,8 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
     count(4);
     check_launch();
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
-                            std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1);
-    k_update_shl_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
-                                                    nf.pdiff);
-    count();
+                            std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1,
+                            solve_phase);
   } else {
     k_vg<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd,
                                                 iopt == 2);
@@ -2879,9 +3047,18 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
     count();
     if (iopt == 1) solve_pcg<double, double>(P0.itmxcg, P0.tolcg, true, 1);
     else solve_bicgstab(P0.isolv, P0.itmxcg, P0.tolcg);
-    k_update_shl<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd);
-    count();
   }
+}
+
+void Engine::iteration_post() {
+  const bool mixed = (precision == 1 && iopt == 1);
+  const cathy_parm_t& P0 = M[0]->parm;
+  if (mixed)
+    k_update_shl_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
+                                                    nf.pdiff);
+  else
+    k_update_shl<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd);
+  count();
   CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
   CG_TRY(cudaMemsetAsync(d_redmax.p, 0, sizeof(double) * nmem * 2, st));
   CG_TRY(cudaMemsetAsync(d_ikmax.p, 0, sizeof(int32_t) * nmem, st));
@@ -2909,9 +3086,134 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
   check_launch();
 }
 
+void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
+  (void)itm;
+  iteration_pre(0);
+  iteration_post();
+}
+
+// The step actions at the start of a macro-iteration (COMMIT, BACKSTEP,
+// START/NEXT for every member with work).
+void Engine::start_kernels() {
+  if (cbm1.nblk)
+    k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 0, need_sw_flag());
+  if (cbms.nblk)
+    k_start_surface<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p, nd);
+  if (cbm1.nblk)
+    k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 1, need_sw_flag());
+  count(3);
+  check_launch();
+}
+
+// ---- one macro-iteration of the FP32 Picard path as a CUDA graph ---------
+// A: copy the action bits and member scalars from pinned host memory, step
+//    actions, pre-solve kernels, PCG set-up;
+// B: WHILE node: one PCG iteration per body execution, the decision kernel
+//    sets the condition (any member still iterating, loop cap);
+// C: post-solve kernels, STORE1 of every iterating member, copies of the
+//    per-member results into pinned host memory.
+// The graph depends only on the sizes of the compacted block maps (kernel
+// grids); everything that changes between macro-iterations is read from
+// device memory.  It is rebuilt when the set of members with work changes.
+void Engine::graph_free() {
+  if (g_exec) cudaGraphExecDestroy(g_exec);
+  if (g_graph) cudaGraphDestroy(g_graph);
+  g_exec = nullptr;
+  g_graph = nullptr;
+}
+
+void Engine::pinned_alloc() {
+  pinned_free();
+  CG_TRY(cudaMallocHost((void**)&hp_act, std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_ms, sizeof(MemberScal) * std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_red, sizeof(double) * RD_NUM * std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_redmax, sizeof(double) * 2 * std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_ikv, sizeof(double) * 2 * std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_sc, sizeof(double) * SC_N * std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_ikmax, sizeof(int32_t) * std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_nit, sizeof(int32_t) * std::max(nmem, 1)));
+  CG_TRY(cudaMallocHost((void**)&hp_loops, sizeof(int32_t)));
+  d_loops.alloc(1);
+}
+
+void Engine::pinned_free() {
+  void* ps[] = {hp_act, hp_ms, hp_red, hp_redmax, hp_ikv, hp_sc, hp_ikmax, hp_nit, hp_loops};
+  for (void* q : ps)
+    if (q) cudaFreeHost(q);
+  hp_act = nullptr; hp_ms = nullptr; hp_red = hp_redmax = hp_ikv = hp_sc = nullptr;
+  hp_ikmax = hp_nit = hp_loops = nullptr;
+}
+
+void Engine::graph_build() {
+  graph_free();
+  const int64_t l0 = launches;
+  cudaGraph_t G = nullptr;
+  CG_TRY(cudaGraphCreate(&G, 0));
+  cudaGraphConditionalHandle h;
+  CG_TRY(cudaGraphConditionalHandleCreate(&h, G, 1, cudaGraphCondAssignDefault));
+  // A
+  int64_t c0 = launches;
+  CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  CG_TRY(cudaMemcpyAsync(d_act.p, hp_act, nmem, cudaMemcpyHostToDevice, st));
+  CG_TRY(cudaMemcpyAsync(d_ms.p, hp_ms, sizeof(MemberScal) * nmem, cudaMemcpyHostToDevice, st));
+  start_kernels();
+  iteration_pre(1);
+  cudaGraph_t gA = nullptr;
+  CG_TRY(cudaStreamEndCapture(st, &gA));
+  g_nA = launches - c0;
+  cudaGraphNode_t nA, nB, nC;
+  CG_TRY(cudaGraphAddChildGraphNode(&nA, G, nullptr, 0, gA));
+  cudaGraphDestroy(gA);
+  // B
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  CG_TRY(cudaGraphAddNode(&nB, G, &nA, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  c0 = launches;
+  CG_TRY(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  {
+    const cathy_parm_t& P0 = M[0]->parm;
+    solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
+                            std::max(P0.tolcg, opts.inner_tol), true, 1, 2, h);
+  }
+  CG_TRY(cudaStreamEndCapture(st, &body));
+  g_nB = launches - c0;
+  // C
+  c0 = launches;
+  CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  iteration_post();
+  k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_mask2.p);
+  k_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, nf, d_red.p);
+  count(2);
+  CG_TRY(cudaMemcpyAsync(hp_red, d_red.p, sizeof(double) * nmem * RD_NUM, cudaMemcpyDeviceToHost, st));
+  CG_TRY(cudaMemcpyAsync(hp_redmax, d_redmax.p, sizeof(double) * nmem * 2, cudaMemcpyDeviceToHost, st));
+  CG_TRY(cudaMemcpyAsync(hp_ikv, d_ikval.p, sizeof(double) * nmem * 2, cudaMemcpyDeviceToHost, st));
+  CG_TRY(cudaMemcpyAsync(hp_ikmax, d_ikmax.p, sizeof(int32_t) * nmem, cudaMemcpyDeviceToHost, st));
+  CG_TRY(cudaMemcpyAsync(hp_nit, d_niter.p, sizeof(int32_t) * nmem, cudaMemcpyDeviceToHost, st));
+  CG_TRY(cudaMemcpyAsync(hp_sc, d_sc.p, sizeof(double) * nmem * SC_N, cudaMemcpyDeviceToHost, st));
+  CG_TRY(cudaMemcpyAsync(hp_loops, d_loops.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  cudaGraph_t gC = nullptr;
+  CG_TRY(cudaStreamEndCapture(st, &gC));
+  g_nC = launches - c0;
+  CG_TRY(cudaGraphAddChildGraphNode(&nC, G, &nB, 1, gC));
+  cudaGraphDestroy(gC);
+  CG_TRY(cudaGraphInstantiate(&g_exec, G, 0));
+  g_graph = G;
+  launches = l0;  // capturing launches nothing
+  g_key[0] = cbm1.nblk; g_key[1] = cbm16.nblk; g_key[2] = cbme.nblk;
+  g_key[3] = cbms.nblk; g_key[4] = cbms16.nblk; g_key[5] = prof ? 1 : 0;
+  g_builds++;
+}
+
 // ---- macro-iteration: device step actions, one nonlinear iteration, host
 // decisions (flow3d.f:212-294, TIMUPD, BKSTEP) ----
 int Engine::macro_iteration() {
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
+  n_macro++;
   int niter_members = 0;
   std::vector<int> itm;
   for (int m = 0; m < nmem; ++m) {
@@ -2927,35 +3229,59 @@ int Engine::macro_iteration() {
     h.pend &= (uint8_t)~a;  // bits not executed now stay pending
   }
   push_scalars();
-  d_act.upload(h_act.data(), nmem, st);
+  const bool graph = graphs_on() && niter_members > 0;
+  if (!graph) d_act.upload(h_act.data(), nmem, st);
+  else std::memcpy(hp_act, h_act.data(), nmem);
   {
     std::vector<uint8_t> memact(nmem);
     for (int m = 0; m < nmem; ++m) memact[m] = h_act[m] != 0;
     compact_maps(memact);
   }
-  if (cbm1.nblk)
-    k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 0, need_sw_flag());
-  if (cbms.nblk)
-    k_start_surface<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p, nd);
-  if (cbm1.nblk)
-    k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 1, need_sw_flag());
-  count(3);
-  check_launch();
-  if (niter_members == 0) {
+  const double *red, *redmax, *ikv, *scv;
+  const int32_t *ikmax, *nit;
+  std::vector<double> v_red, v_redmax, v_ikv, v_scv;
+  std::vector<int32_t> v_ikmax, v_nit;
+  auto t1 = clk::now();
+  if (graph) {
+    const int key[6] = {cbm1.nblk, cbm16.nblk, cbme.nblk, cbms.nblk, cbms16.nblk, prof ? 1 : 0};
+    if (!g_exec || std::memcmp(key, g_key, sizeof(key)) != 0) graph_build();
+    t1 = clk::now();
+    CG_TRY(cudaGraphLaunch(g_exec, st));
     CG_TRY(cudaStreamSynchronize(st));
-    return 0;
+    g_launches++;
+    launches += g_nA + g_nC + g_nB * (int64_t)(*hp_loops);
+    if (prof) {
+      lt_pending += *hp_loops;
+      if (lt_pending > lt_cap - 2 * (opts.inner_maxit + 8)) prof_flush();
+    }
+    red = hp_red; redmax = hp_redmax; ikv = hp_ikv; scv = hp_sc; ikmax = hp_ikmax; nit = hp_nit;
+  } else {
+    start_kernels();
+    if (niter_members == 0) {
+      CG_TRY(cudaStreamSynchronize(st));
+      return 0;
+    }
+    picard_or_newton_iteration(itm);
+    v_red.resize((size_t)nmem * RD_NUM); v_redmax.resize(2 * nmem); v_ikv.resize(2 * nmem);
+    v_scv.resize((size_t)nmem * SC_N); v_ikmax.resize(nmem); v_nit.resize(nmem);
+    d_red.download(v_red.data(), v_red.size(), st);
+    d_redmax.download(v_redmax.data(), v_redmax.size(), st);
+    d_ikval.download(v_ikv.data(), v_ikv.size(), st);
+    d_ikmax.download(v_ikmax.data(), nmem, st);
+    d_niter.download(v_nit.data(), nmem, st);
+    d_sc.download(v_scv.data(), v_scv.size(), st);
+    CG_TRY(cudaStreamSynchronize(st));
+    red = v_red.data(); redmax = v_redmax.data(); ikv = v_ikv.data(); scv = v_scv.data();
+    ikmax = v_ikmax.data(); nit = v_nit.data();
   }
-  picard_or_newton_iteration(itm);
-  // results
-  std::vector<double> red((size_t)nmem * RD_NUM), redmax(2 * nmem), ikv(2 * nmem), scv((size_t)nmem * SC_N);
-  std::vector<int32_t> ikmax(nmem), nit(nmem);
-  d_red.download(red.data(), red.size(), st);
-  d_redmax.download(redmax.data(), redmax.size(), st);
-  d_ikval.download(ikv.data(), ikv.size(), st);
-  d_ikmax.download(ikmax.data(), nmem, st);
-  d_niter.download(nit.data(), nmem, st);
-  d_sc.download(scv.data(), scv.size(), st);
-  CG_TRY(cudaStreamSynchronize(st));
+  const auto t2 = clk::now();
+  tm_prep += std::chrono::duration<double, std::milli>(t1 - t0).count();
+  tm_dev += std::chrono::duration<double, std::milli>(t2 - t1).count();
+  struct HostTimer {
+    Engine* e;
+    clk::time_point t;
+    ~HostTimer() { e->tm_host += std::chrono::duration<double, std::milli>(clk::now() - t).count(); }
+  } host_timer{this, t2};
   nl_iters += niter_members;
   std::vector<uint8_t> conv_mask(nmem, 0);
   bool any_conv = false;
@@ -3010,16 +3336,22 @@ int Engine::macro_iteration() {
     }
   }
   if (any_conv) {
-    d_mask2.upload(conv_mask.data(), nmem, st);
-    CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
-    if (precision == 1 && iopt == 1)
-      k_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, nf, d_red.p);
-    else
-      k_store1<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, d_red.p);
-    count();
-    check_launch();
-    d_red.download(red.data(), red.size(), st);
-    CG_TRY(cudaStreamSynchronize(st));
+    // STORE1 (storcal.f) at the converged heads: the graph computed it for
+    // every iterating member; the kernel-by-kernel path computes it now
+    const double* st1 = red;
+    if (!graph) {
+      d_mask2.upload(conv_mask.data(), nmem, st);
+      CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
+      if (precision == 1 && iopt == 1)
+        k_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, nf, d_red.p);
+      else
+        k_store1<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, d_red.p);
+      count();
+      check_launch();
+      d_red.download(v_red.data(), v_red.size(), st);
+      CG_TRY(cudaStreamSynchronize(st));
+      st1 = v_red.data();
+    }
     for (int m = 0; m < nmem; ++m) {
       if (!conv_mask[m]) continue;
       MemberHost& h = *M[m];
@@ -3037,7 +3369,7 @@ int Engine::macro_iteration() {
       double errel;
       if (h.deltat >= 1.0e15) errel = vin != 0.0 ? 100.0 * erras / vin : 0.0;
       else errel = (vin + vout) != 0.0 ? 100.0 * erras / (vin + vout) : 0.0;
-      h.store1 = red[(size_t)m * RD_NUM + RD_STORE1];
+      h.store1 = st1[(size_t)m * RD_NUM + RD_STORE1];
       h.store2 += dstore;
       h.vtot += vin + vout;
       h.cvin += vin; h.cvout += vout; h.cdstor += dstore; h.cerras += erras;
@@ -3331,11 +3663,19 @@ int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launche
   if (enable >= 0) {
     e->prof = enable != 0;
     e->prof_ms = 0; e->prof_n = 0; e->prof_bytes = 0;
+    if (e->prof) e->lt_reset();
     if (e->d_prof_bytes.p) {
       e->d_prof_bytes.zero(e->st);
       CG_TRY(cudaStreamSynchronize(e->st));
     }
   }
+  return 0;
+}
+
+int engine_timers(Engine* e, double* out, int n) {
+  const double v[7] = {(double)e->n_macro, (double)e->g_launches, (double)e->g_builds,
+                       e->tm_prep, e->tm_dev, e->tm_host, e->gpu_ms};
+  for (int q = 0; q < n && q < 7; ++q) out[q] = v[q];
   return 0;
 }
 
@@ -3448,7 +3788,7 @@ int dropin_symslv(int n, int nterm, int numdir, const int32_t* noddir,
   std::vector<double> b(tnoti, tnoti + n);
   for (int i = 0; i < n; ++i) if (dm[i]) b[i] = 0.0;
   Engine E;
-  E.opts = cathy_opts_t{0, 0, 0, 0.0, 0};
+  E.opts = cathy_opts_t{0, 0, 0, 0.0, 0, 0};
   E.bare_init(n, rowptr, cols, dm);
   E.d_vals64.upload(vals.data(), vals.size(), E.st);
   E.d_nodal[ND_RHS].upload(b.data(), n, E.st);
@@ -3497,7 +3837,7 @@ int dropin_nsyslv(int isolv, int n, int nterm, int numdir, const int32_t* noddir
     return 0;
   }
   Engine E;
-  E.opts = cathy_opts_t{0, 0, 0, 0.0, 0};
+  E.opts = cathy_opts_t{0, 0, 0, 0.0, 0, 0};
   E.bare_init(n, rowptr, cols, dm);
   E.d_vals64.upload(vals.data(), vals.size(), E.st);
   E.d_nodal[ND_RHS].upload(b.data(), n, E.st);

@@ -80,6 +80,7 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs,
 int engine_reset(Engine* e);
 int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launches,
                    double* spmv_bytes);
+int engine_timers(Engine* e, double* out, int n);
 int engine_stats(Engine* e, double* gpu_ms, int64_t* launches,
                  int64_t* lin_iters, int64_t* nl_iters);
 

@@ -205,3 +205,26 @@ def test_ensemble_batch_matches_single_runs():
         assert len(recs[m]) == len(osr)
         assert abs(recs[m][-1]["time"] - osr[-1]["time"]) < 1e-9
         assert np.max(np.abs(got[m][0] - po)) <= 1e-6
+
+
+def test_graph_path_matches_kernel_by_kernel_path():
+    """The FP32 path run as one CUDA graph per Picard iteration (PCG loop as
+    a device-driven conditional node) takes the same steps and iterations
+    and reaches the same heads as the kernel-by-kernel path."""
+    from pycathy_wrapper_gb300.inputs import config2_members
+    cases = config2_members(4, tmax=3600.0, min_cells=8, max_cells=16)
+    for c in cases:
+        c.parm.precond = 2
+    out = {}
+    for graphs in (False, True):
+        with _sim(cases, precision=1, graphs=graphs) as s:
+            s.run()
+            out[graphs] = [(s.state(m), s.records(m)) for m in range(len(cases))]
+    for m in range(len(cases)):
+        (pa, ta, _, sa), (ia, ra) = out[False][m]
+        (pb, tb, _, sb), (ib, rb) = out[True][m]
+        assert sa == sb == 1 and ta == tb
+        assert [r["iter"] for r in ra] == [r["iter"] for r in rb]
+        assert [r["niter"] for r in ia] == [r["niter"] for r in ib]
+        assert np.max(np.abs(pa - pb)) <= 1e-9
+        assert abs(ra[-1]["cerras"] - rb[-1]["cerras"]) <= 1e-9 * max(abs(ra[-1]["cvin"]), 1e-30)
