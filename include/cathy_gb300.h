@@ -174,10 +174,11 @@ int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
 int32_t cathy_gb300_stats(void* handle, double* gpu_ms, int64_t* launches,
                           int64_t* lin_iters, int64_t* nl_iters);
 
-/* Host-side timers of the time stepping (out[0..n), n <= 7): macro-iterations
- * (one nonlinear iteration of every member with work), CUDA graph launches,
- * graph builds, host preparation ms, device wait ms (launch + synchronise),
- * host decision ms, GPU ms of the hot path. */
+/* Timers of the time stepping (out[0..n), n <= 8): macro-iterations (one
+ * nonlinear iteration of every member with work), CUDA graph launches, graph
+ * builds, host preparation ms, device wait ms (launch + synchronise), host
+ * decision ms, GPU ms of the hot path, GPU ms inside graph launches (CUDA
+ * events around each launch). */
 int32_t cathy_gb300_timers(void* handle, double* out, int32_t n);
 
 /* ---- Fortran subroutine drop-ins ---------------------------------------- */

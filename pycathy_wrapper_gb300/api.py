@@ -196,10 +196,10 @@ class Simulation:
 
     def timers(self):
         """Host-side phase timers of the time stepping."""
-        out = (C.c_double * 7)()
-        check(self.L.cathy_gb300_timers(self.h, out, 7), "cathy_gb300_timers")
+        out = (C.c_double * 8)()
+        check(self.L.cathy_gb300_timers(self.h, out, 8), "cathy_gb300_timers")
         k = ("macro_iterations", "graph_launches", "graph_builds", "host_prep_ms",
-             "device_wait_ms", "host_decision_ms", "gpu_ms")
+             "device_wait_ms", "host_decision_ms", "gpu_ms", "graph_gpu_ms")
         return {a: out[i] for i, a in enumerate(k)}
 
     def stats(self):

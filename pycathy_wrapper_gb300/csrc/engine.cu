@@ -762,39 +762,72 @@ __global__ void k_jacobi_setup(const int32_t* bm_mem, const int32_t* bm_r0,
 // Column-line preconditioner: exact tridiagonal solve along each vertical
 // column of the extruded mesh (the vertical edges carry >99% of the
 // off-diagonal weight on these thin-layered meshes).  Setup stores the
-// pivots' inverses and the masked vertical couplings.
+// pivots' inverses and the masked vertical couplings.  One thread per
+// column; the sweeps are sequential along the column, so every kernel loads
+// a chunk of kLineChunk layers first (independent loads in flight together)
+// and then runs the recurrence on registers.
+constexpr int kLineChunk = 8;
+
 template <class MT, class VT>
 __global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* active,
-                             const MemberScal* ms, const int32_t* diag,
-                             const int32_t* down, const MT* vals,
-                             const uint8_t* dmask, VT* pinv, VT* cdown) {
+                             const MemberScal* ms, const int32_t* __restrict__ diag,
+                             const int32_t* __restrict__ down, const MT* __restrict__ vals,
+                             const uint8_t* __restrict__ dmask, VT* __restrict__ pinv,
+                             VT* __restrict__ cdown) {
   const int m = bm_mem[blockIdx.x];
   if (!active[m]) return;
   const int top = bm_r0[blockIdx.x] + threadIdx.x;
   if (top >= bm_r1[blockIdx.x]) return;
   const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
   double piv_prev = 1.0, c_prev = 0.0;
-  for (int k = 0; k < nl; ++k) {
-    const int i = top + k * nnod;
-    const bool di = dmask[i];
-    double a = di ? 1.0 : (double)vals[diag[i]];
-    double c = 0.0;
-    if (k + 1 < nl && !di && !dmask[i + nnod] && down[i] >= 0) c = (double)vals[down[i]];
-    double piv = a - c_prev * c_prev / piv_prev;
-    pinv[i] = (VT)(1.0 / piv);
-    cdown[i] = (VT)c;
-    piv_prev = piv;
-    c_prev = c;
+  for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
+    int id[kLineChunk], iw[kLineChunk];
+    bool dm[kLineChunk], dmb[kLineChunk];
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      const int k = k0 + j;
+      id[j] = -1; iw[j] = -1; dm[j] = true; dmb[j] = true;
+      if (k < nl) {
+        const int i = top + k * nnod;
+        dm[j] = dmask[i] != 0;
+        id[j] = diag[i];
+        if (k + 1 < nl) { iw[j] = down[i]; dmb[j] = dmask[i + nnod] != 0; }
+      }
+    }
+    double a[kLineChunk], c[kLineChunk];
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      a[j] = 1.0;
+      c[j] = 0.0;
+      if (k0 + j < nl) {
+        if (!dm[j]) a[j] = (double)vals[id[j]];
+        if (!dm[j] && !dmb[j] && iw[j] >= 0) c[j] = (double)vals[iw[j]];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      const int k = k0 + j;
+      if (k < nl) {
+        const int i = top + k * nnod;
+        const double piv = a[j] - c_prev * c_prev / piv_prev;
+        pinv[i] = (VT)(1.0 / piv);
+        cdown[i] = (VT)c[j];
+        piv_prev = piv;
+        c_prev = c[j];
+      }
+    }
   }
 }
 
-// z = T^-1 r per column; accumulates w.z (w = q for the PCG beta) per member
+// z = T^-1 r per column; accumulates w.z (w = q for the PCG beta) per
+// member.  The forward sweep keeps y in z, the backward sweep overwrites it.
 template <class VT>
 __global__ void k_line_apply(const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* active,
-                             const MemberScal* ms, const VT* pinv,
-                             const VT* cdown, const VT* r, VT* z, const VT* w,
+                             const MemberScal* ms, const VT* __restrict__ pinv,
+                             const VT* __restrict__ cdown, const VT* __restrict__ r,
+                             VT* __restrict__ z, const VT* __restrict__ w,
                              double* acc, int acc_stride, int acc_off) {
   const int m = bm_mem[blockIdx.x];
   if (!active[m]) return;
@@ -802,22 +835,53 @@ __global__ void k_line_apply(const int32_t* bm_mem, const int32_t* bm_r0,
   VT dot[1] = {0};
   if (top < bm_r1[blockIdx.x]) {
     const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
-    VT y[kMaxLayers];
-    VT yprev = 0, cprev = 0;
-    for (int k = 0; k < nl; ++k) {
-      const int i = top + k * nnod;
-      VT yk = r[i] - cprev * yprev * (k > 0 ? pinv[i - nnod] : (VT)0);
-      y[k] = yk;
-      yprev = yk;
-      cprev = cdown[i];
+    VT yprev = 0, cprev = 0, pprev = 0;
+    for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
+      VT rr[kLineChunk], pv[kLineChunk], cd[kLineChunk];
+#pragma unroll
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k0 + j;
+        rr[j] = pv[j] = cd[j] = (VT)0;
+        if (k < nl) {
+          const int i = top + k * nnod;
+          rr[j] = r[i]; pv[j] = pinv[i]; cd[j] = cdown[i];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k0 + j;
+        if (k < nl) {
+          const VT yk = rr[j] - cprev * yprev * pprev;
+          z[top + k * nnod] = yk;
+          yprev = yk;
+          cprev = cd[j];
+          pprev = pv[j];
+        }
+      }
     }
     VT znext = 0;
-    for (int k = nl - 1; k >= 0; --k) {
-      const int i = top + k * nnod;
-      VT zk = (y[k] - cdown[i] * znext) * pinv[i];
-      z[i] = zk;
-      if (w) dot[0] += w[i] * zk;
-      znext = zk;
+    for (int k1 = nl - 1; k1 >= 0; k1 -= kLineChunk) {
+      VT yy[kLineChunk], pv[kLineChunk], cd[kLineChunk], ww[kLineChunk];
+#pragma unroll
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k1 - j;
+        yy[j] = pv[j] = cd[j] = ww[j] = (VT)0;
+        if (k >= 0) {
+          const int i = top + k * nnod;
+          yy[j] = z[i]; pv[j] = pinv[i]; cd[j] = cdown[i];
+          if (w) ww[j] = w[i];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k1 - j;
+        if (k >= 0) {
+          const VT zk = (yy[j] - cd[j] * znext) * pv[j];
+          z[top + k * nnod] = zk;
+          if (w) dot[0] += ww[j] * zk;
+          znext = zk;
+        }
+      }
     }
   }
   if (w) block_accumulate_t<VT, 1>(dot, acc + (size_t)m * acc_stride + acc_off);
@@ -1562,9 +1626,13 @@ __device__ __forceinline__ void block_accumulate_ff(FF (&v)[NV], double* acc) {
 
 // Row-owned Picard assembly in FP32.  One 16-lane group per row; the lanes
 // take the row's incident elements in parallel (lane j: incidences j, j+16,
-// ...), compute each element's four local LHS entries and RHS terms, and the
-// slot owners then add the contributions in a fixed order (deterministic,
-// no atomics).  RHS = -sum K (h_l - h_k) - mass terms, see the FP32 block
+// ...) and compute each element's four local LHS entries and RHS terms.  The
+// diagonal entries are summed by a shuffle reduction; the off-diagonal ones
+// are written to shared memory at position q*4 + l (incidence q, local node
+// l) and each slot's owner lane adds its contributions through a gather list
+// precomputed from the mesh (the slot of (i, j) collects the incidences
+// whose element contains j, in incidence order): deterministic, no atomics,
+// no search.  RHS = -sum K (h_l - h_k) - mass terms, see the FP32 block
 // comment; BC fluxes come precomputed in FP32 (bcf).
 __global__ void __launch_bounds__(kThreads)
 k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
@@ -1572,12 +1640,12 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
                       const int32_t* rowptr, const int32_t* cols,
                       const int32_t* inc_ptr, const int32_t* inc, const int4* tet,
                       const TetRec<float>* rec, const uint8_t* dmask, NodalF nf,
-                      const float* bcf, float* vals, float lm_d, float lm_o) {
+                      const float* bcf, float* vals, float lm_d, float lm_o,
+                      const int64_t* __restrict__ glrow, const uint8_t* __restrict__ gloff,
+                      const uint8_t* __restrict__ gl) {
   const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
-  __shared__ int scol[kRowsPerBlock16][kGroup];
-  __shared__ float sval[kRowsPerBlock16][kGroup * 4];
-  __shared__ int8_t sidx[kRowsPerBlock16][kGroup * 4];
+  __shared__ float sval[kRowsPerBlock16][64 * 4];
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
   const int i = bm_r0[blockIdx.x] + grp;
   const bool rowok = i < bm_r1[blockIdx.x];
@@ -1592,15 +1660,12 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     p1 = inc_ptr[i + 1];
     et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
   }
-  scol[grp][lane] = (lane < rlen) ? cols[s0 + lane] : 0x7fffffff;
   int ntrip = (p1 - p0 + kGroup - 1) / kGroup;
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
-  __syncwarp();
-  float lhs = 0.0f, rp = 0.0f, msum = 0.0f, mssum = 0.0f;
+  float dacc = 0.0f, rp = 0.0f, msum = 0.0f, mssum = 0.0f;
   for (int trip = 0; trip < ntrip; ++trip) {
-    const int p = p0 + trip * kGroup + lane;
-#pragma unroll
-    for (int l = 0; l < 4; ++l) sidx[grp][lane * 4 + l] = -1;
+    const int q = trip * kGroup + lane;
+    const int p = p0 + q;
     if (rowok && p < p1) {
       const int ek = inc[p];
       const int e = ek >> 2, k = ek & 3;
@@ -1618,15 +1683,12 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
         const float lm = (l == k) ? lm_d : lm_o;
         const float skl = Sv[sym_idx(k, l)];
         float c = th * (kr * skl) + ve1 * lm * rdt;
-        if (l == k) c += vpel * lm_d * et2i * rdt;
-        // binary search of node tn[l] among the row's sorted columns
-        int lo = 0, hi = rlen - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (scol[grp][mid] < tn[l]) lo = mid + 1; else hi = mid;
+        if (l == k) {
+          c += vpel * lm_d * et2i * rdt;
+          dacc += c;
+        } else {
+          sval[grp][q * 4 + l] = c;
         }
-        sval[grp][lane * 4 + l] = c;
-        sidx[grp][lane * 4 + l] = (int8_t)lo;
         const int nl = tn[l];
         const float2 hn = nf.h2[nl];
         const float dh = (hn.x - hh_i) + (hn.y - hl_i);
@@ -1639,20 +1701,27 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
         }
       }
     }
-    __syncwarp();
-    if (lane < rlen) {
-#pragma unroll 8
-      for (int q = 0; q < kGroup * 4; ++q)
-        if (sidx[grp][q] == lane) lhs += sval[grp][q];
-    }
-    __syncwarp();
   }
+  __syncwarp();
+  const float dsum = group_sum<float>(dacc);
   float rhs = group_sum<float>(rp);
-  // diagonal (lumped) mass terms of the row node itself
   msum = group_sum<float>(msum);
   mssum = group_sum<float>(mssum);
   if (!rowok) return;
-  if (lane < rlen) vals[s0 + lane] = lhs;
+  if (lane < rlen) {
+    const int sl = s0 + lane;
+    float lhs;
+    if (cols[sl] == i) {
+      lhs = dsum;
+    } else {
+      const int64_t base = glrow[i];
+      const int a = gloff[sl];
+      const int b = (lane + 1 < rlen) ? (int)gloff[sl + 1] : (int)(glrow[i + 1] - base);
+      lhs = 0.0f;
+      for (int u = a; u < b; ++u) lhs += sval[grp][gl[base + u]];
+    }
+    vals[sl] = lhs;
+  }
   if (lane == 0) {
     rhs -= (msum * nf.dpsi[i] + mssum * nf.dsw[i]) * rdt;
     nf.xt5[i] = rhs;
@@ -1926,6 +1995,10 @@ struct Engine {
   DBuf<TetRec<double>> d_rec64;
   DBuf<TetRec<float>> d_rec32;
   DBuf<int32_t> d_rowptr, d_cols, d_diag, d_down, d_tslot, d_inc_ptr, d_inc;
+  // FP32 assembly gather lists: row base offsets, per-slot relative starts,
+  // contribution positions q*4 + l
+  DBuf<int64_t> d_glrow;
+  DBuf<uint8_t> d_gloff, d_gl;
   DBuf<int32_t> d_srows, d_lev_f, d_lev_b;
   std::vector<int32_t> lev_f_ptr, lev_b_ptr;  // batched levels (host)
   DBuf<double> d_vals64;
@@ -1962,6 +2035,8 @@ struct Engine {
 
   ~Engine() {
     graph_free();
+    if (gev0) cudaEventDestroy(gev0);
+    if (gev1) cudaEventDestroy(gev1);
     pinned_free();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -2038,8 +2113,9 @@ struct Engine {
   int64_t g_nA = 0, g_nB = 0, g_nC = 0, g_builds = 0, g_launches = 0;
   // host-side phase timers of macro-iterations (ms): preparation, waiting for
   // the device (launch + synchronise), decisions; macro-iteration count
-  double tm_prep = 0, tm_dev = 0, tm_host = 0;
+  double tm_prep = 0, tm_dev = 0, tm_host = 0, tm_graph = 0;
   int64_t n_macro = 0;
+  cudaEvent_t gev0 = nullptr, gev1 = nullptr;  // around graph launches
   DBuf<int32_t> d_loops;
   uint8_t* hp_act = nullptr;
   MemberScal* hp_ms = nullptr;
@@ -2245,6 +2321,10 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   std::vector<int32_t> h_mem(N), h_loc(N), h_rowptr(N + 1), h_cols(NNZ), h_diag(N),
       h_down(N), h_tslot(NNZ), h_incptr(N + 1), h_srows;
   std::vector<int32_t> h_inc, h_tetsoil(NT);
+  const bool glists = (precision == 1 && iopt == 1);
+  std::vector<int64_t> h_glrow(glists ? N + 1 : 0, 0);
+  std::vector<uint8_t> h_gloff(glists ? NNZ : 0, 0), h_gl;
+  if (glists) h_gl.reserve((size_t)12 * NT);
   std::vector<int4> h_tet(NT);
   std::vector<double> h_x(N), h_y(N), h_z(N), h_arenod(N, 0.0);
   std::vector<uint8_t> h_sdir(N, 0);
@@ -2290,6 +2370,38 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       const int32_t* t = &g.tetra[5 * e];
       h_tet[to + e] = make_int4(no + t[0] - 1, no + t[1] - 1, no + t[2] - 1, no + t[3] - 1);
       h_tetsoil[to + e] = soil_off[m] + (t[4] - 1) * nstr + (g.tet_layer[e] - 1);
+    }
+    // FP32 assembly gather lists: for every off-diagonal slot (i, j), the
+    // positions q*4 + l of the contributions of row i's incidences q (local
+    // node l of the element is j), in incidence order.  Per row: base offset
+    // (int32); per slot: start relative to the row base (uint8).
+    if (precision == 1 && iopt == 1) {
+      uint8_t lst[kGroup][3 * 64];
+      int cnt[kGroup];
+      for (int i = 0; i < g.n; ++i) {
+        const int p0 = g.inc_ptr[i], ninc = g.inc_ptr[i + 1] - p0;
+        if (ninc > 64) throw std::string("node with more than 64 incident elements");
+        const int s0 = g.rowptr[i], rl = g.rowptr[i + 1] - s0;
+        for (int sj = 0; sj < rl; ++sj) cnt[sj] = 0;
+        for (int q = 0; q < ninc; ++q) {
+          const int e = g.inc[p0 + q] >> 2, k = g.inc[p0 + q] & 3;
+          for (int l = 0; l < 4; ++l) {
+            if (l == k) continue;
+            const int j = g.tetra[5 * e + l] - 1;
+            const int sj = (int)(std::lower_bound(g.cols.begin() + s0, g.cols.begin() + s0 + rl, j) -
+                                 (g.cols.begin() + s0));
+            lst[sj][cnt[sj]++] = (uint8_t)(q * 4 + l);
+          }
+        }
+        h_glrow[no + i] = (int64_t)h_gl.size();
+        int off = 0;
+        for (int sj = 0; sj < rl; ++sj) {
+          h_gloff[ao + s0 + sj] = (uint8_t)off;
+          h_gl.insert(h_gl.end(), lst[sj], lst[sj] + cnt[sj]);
+          off += cnt[sj];
+        }
+        h_glrow[no + i + 1] = (int64_t)h_gl.size();
+      }
     }
     for (int i = 0; i < g.nnod; ++i) {
       h_arenod[no + i] = g.arenod[i];
@@ -2416,6 +2528,11 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_tslot.alloc(NNZ); d_tslot.upload(h_tslot.data(), NNZ, st);
   d_inc_ptr.alloc(N + 1); d_inc_ptr.upload(h_incptr.data(), N + 1, st);
   d_inc.alloc(h_inc.size()); d_inc.upload(h_inc.data(), h_inc.size(), st);
+  if (glists) {
+    d_glrow.alloc(N + 1); d_glrow.upload(h_glrow.data(), N + 1, st);
+    d_gloff.alloc(NNZ); d_gloff.upload(h_gloff.data(), NNZ, st);
+    d_gl.alloc(std::max<size_t>(h_gl.size(), 1)); d_gl.upload(h_gl.data(), h_gl.size(), st);
+  }
   d_srows.alloc(nsurf); d_srows.upload(h_srows.data(), nsurf, st);
   {
     std::vector<int32_t> dr;
@@ -3030,7 +3147,7 @@ void Engine::iteration_pre(int solve_phase) {
                                                    nd, nf.qneu, nf.bcf);
     k_assemble_picard_f32<<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
         d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, d_rec32.p, d_dmask.p,
-        nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o);
+        nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
     k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
     count(4);
     check_launch();
@@ -3246,8 +3363,19 @@ int Engine::macro_iteration() {
     const int key[6] = {cbm1.nblk, cbm16.nblk, cbme.nblk, cbms.nblk, cbms16.nblk, prof ? 1 : 0};
     if (!g_exec || std::memcmp(key, g_key, sizeof(key)) != 0) graph_build();
     t1 = clk::now();
+    if (!gev0) {
+      CG_TRY(cudaEventCreate(&gev0));
+      CG_TRY(cudaEventCreate(&gev1));
+    }
+    CG_TRY(cudaEventRecord(gev0, st));
     CG_TRY(cudaGraphLaunch(g_exec, st));
+    CG_TRY(cudaEventRecord(gev1, st));
     CG_TRY(cudaStreamSynchronize(st));
+    {
+      float gms = 0.0f;
+      CG_TRY(cudaEventElapsedTime(&gms, gev0, gev1));
+      tm_graph += gms;
+    }
     g_launches++;
     launches += g_nA + g_nC + g_nB * (int64_t)(*hp_loops);
     if (prof) {
@@ -3610,7 +3738,8 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
         e->d_ms.p, e->nd, e->nf.qneu, e->nf.bcf);
     k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
         e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_tet.p,
-        e->d_rec32.p, e->d_dmask.p, e->nf, e->nf.bcf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o);
+        e->d_rec32.p, e->d_dmask.p, e->nf, e->nf.bcf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o,
+        e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
   } else {
     k_vg<double><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->iopt == 2);
     e->assemble<double>();
@@ -3673,9 +3802,9 @@ int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launche
 }
 
 int engine_timers(Engine* e, double* out, int n) {
-  const double v[7] = {(double)e->n_macro, (double)e->g_launches, (double)e->g_builds,
-                       e->tm_prep, e->tm_dev, e->tm_host, e->gpu_ms};
-  for (int q = 0; q < n && q < 7; ++q) out[q] = v[q];
+  const double v[8] = {(double)e->n_macro, (double)e->g_launches, (double)e->g_builds,
+                       e->tm_prep, e->tm_dev, e->tm_host, e->gpu_ms, e->tm_graph};
+  for (int q = 0; q < n && q < 8; ++q) out[q] = v[q];
   return 0;
 }
 
