@@ -178,7 +178,8 @@ int32_t cathy_gb300_stats(void* handle, double* gpu_ms, int64_t* launches,
  * nonlinear iteration of every member with work), CUDA graph launches, graph
  * builds, host preparation ms, device wait ms (launch + synchronise), host
  * decision ms, GPU ms of the hot path, GPU ms inside graph launches (CUDA
- * events around each launch). */
+ * events around each launch); then, for n up to 72, 32 pairs (graph
+ * launches, their GPU ms) binned by floor(log2(rows with work)). */
 int32_t cathy_gb300_timers(void* handle, double* out, int32_t n);
 
 /* ---- Fortran subroutine drop-ins ---------------------------------------- */

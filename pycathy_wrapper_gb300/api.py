@@ -196,11 +196,14 @@ class Simulation:
 
     def timers(self):
         """Host-side phase timers of the time stepping."""
-        out = (C.c_double * 8)()
-        check(self.L.cathy_gb300_timers(self.h, out, 8), "cathy_gb300_timers")
+        out = (C.c_double * 72)()
+        check(self.L.cathy_gb300_timers(self.h, out, 72), "cathy_gb300_timers")
         k = ("macro_iterations", "graph_launches", "graph_builds", "host_prep_ms",
              "device_wait_ms", "host_decision_ms", "gpu_ms", "graph_gpu_ms")
-        return {a: out[i] for i, a in enumerate(k)}
+        d = {a: out[i] for i, a in enumerate(k)}
+        d["by_log2_rows"] = {b: (out[8 + 2 * b], out[9 + 2 * b]) for b in range(32)
+                             if out[8 + 2 * b] > 0}
+        return d
 
     def stats(self):
         ms = C.c_double()

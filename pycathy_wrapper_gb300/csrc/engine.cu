@@ -769,16 +769,16 @@ __global__ void k_jacobi_setup(const int32_t* bm_mem, const int32_t* bm_r0,
 constexpr int kLineChunk = 8;
 
 template <class MT, class VT>
-__global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
+__device__ __forceinline__ void k_line_setup_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* active,
                              const MemberScal* ms, const int32_t* __restrict__ diag,
                              const int32_t* __restrict__ down, const MT* __restrict__ vals,
                              const uint8_t* __restrict__ dmask, VT* __restrict__ pinv,
                              VT* __restrict__ cdown) {
-  const int m = bm_mem[blockIdx.x];
+  const int m = bm_mem[bid_];
   if (!active[m]) return;
-  const int top = bm_r0[blockIdx.x] + threadIdx.x;
-  if (top >= bm_r1[blockIdx.x]) return;
+  const int top = bm_r0[bid_] + threadIdx.x;
+  if (top >= bm_r1[bid_]) return;
   const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
   double piv_prev = 1.0, c_prev = 0.0;
   for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
@@ -819,21 +819,30 @@ __global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
     }
   }
 }
+template <class MT, class VT>
+__global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* active,
+                             const MemberScal* ms, const int32_t* __restrict__ diag,
+                             const int32_t* __restrict__ down, const MT* __restrict__ vals,
+                             const uint8_t* __restrict__ dmask, VT* __restrict__ pinv,
+                             VT* __restrict__ cdown) {
+  k_line_setup_b<MT, VT>(blockIdx.x, bm_mem, bm_r0, bm_r1, active, ms, diag, down, vals, dmask, pinv, cdown);
+}
 
 // z = T^-1 r per column; accumulates w.z (w = q for the PCG beta) per
 // member.  The forward sweep keeps y in z, the backward sweep overwrites it.
 template <class VT>
-__global__ void k_line_apply(const int32_t* bm_mem, const int32_t* bm_r0,
+__device__ __forceinline__ void k_line_apply_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* active,
                              const MemberScal* ms, const VT* __restrict__ pinv,
                              const VT* __restrict__ cdown, const VT* __restrict__ r,
                              VT* __restrict__ z, const VT* __restrict__ w,
                              double* acc, int acc_stride, int acc_off) {
-  const int m = bm_mem[blockIdx.x];
+  const int m = bm_mem[bid_];
   if (!active[m]) return;
-  const int top = bm_r0[blockIdx.x] + threadIdx.x;
+  const int top = bm_r0[bid_] + threadIdx.x;
   VT dot[1] = {0};
-  if (top < bm_r1[blockIdx.x]) {
+  if (top < bm_r1[bid_]) {
     const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
     VT yprev = 0, cprev = 0, pprev = 0;
     for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
@@ -885,6 +894,15 @@ __global__ void k_line_apply(const int32_t* bm_mem, const int32_t* bm_r0,
     }
   }
   if (w) block_accumulate_t<VT, 1>(dot, acc + (size_t)m * acc_stride + acc_off);
+}
+template <class VT>
+__global__ void k_line_apply(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* active,
+                             const MemberScal* ms, const VT* __restrict__ pinv,
+                             const VT* __restrict__ cdown, const VT* __restrict__ r,
+                             VT* __restrict__ z, const VT* __restrict__ w,
+                             double* acc, int acc_stride, int acc_off) {
+  k_line_apply_b<VT>(blockIdx.x, bm_mem, bm_r0, bm_r1, active, ms, pinv, cdown, r, z, w, acc, acc_stride, acc_off);
 }
 
 // IC(0) factor (left-looking row form of INCLDP), one thread per row of one
@@ -1107,28 +1125,41 @@ __global__ void k_pcg_update_rx(const int32_t* bm_mem, const int32_t* bm_r0,
 }
 
 template <class VT>
-__global__ void k_pcg_update_p(const int32_t* bm_mem, const int32_t* bm_r0,
+__device__ __forceinline__ void k_pcg_update_p_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
                                const int32_t* bm_r1, const uint8_t* active,
                                const double* sc, VT* p, const VT* z) {
-  const int m = bm_mem[blockIdx.x];
+  const int m = bm_mem[bid_];
   if (!active[m]) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
+  const int i = bm_r0[bid_] + threadIdx.x;
+  if (i >= bm_r1[bid_]) return;
   const VT beta = (VT)(-sc[m * SC_N + SC_QZ] / sc[m * SC_N + SC_PQ]);
   p[i] = z[i] + beta * p[i];
 }
+template <class VT>
+__global__ void k_pcg_update_p(const int32_t* bm_mem, const int32_t* bm_r0,
+                               const int32_t* bm_r1, const uint8_t* active,
+                               const double* sc, VT* p, const VT* z) {
+  k_pcg_update_p_b<VT>(blockIdx.x, bm_mem, bm_r0, bm_r1, active, sc, p, z);
+}
 
+template <class VT>
+__device__ __forceinline__ void k_dot_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
+                      const int32_t* bm_r1, const uint8_t* active, const VT* a,
+                      const VT* b, const uint8_t* mask, double* acc,
+                      int acc_stride, int acc_off) {
+  const int m = bm_mem[bid_];
+  if (!active[m]) return;
+  const int i = bm_r0[bid_] + threadIdx.x;
+  VT d[1] = {0};
+  if (i < bm_r1[bid_] && !(mask && mask[i])) d[0] = a[i] * b[i];
+  block_accumulate_t<VT, 1>(d, acc + (size_t)m * acc_stride + acc_off);
+}
 template <class VT>
 __global__ void k_dot(const int32_t* bm_mem, const int32_t* bm_r0,
                       const int32_t* bm_r1, const uint8_t* active, const VT* a,
                       const VT* b, const uint8_t* mask, double* acc,
                       int acc_stride, int acc_off) {
-  const int m = bm_mem[blockIdx.x];
-  if (!active[m]) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  VT d[1] = {0};
-  if (i < bm_r1[blockIdx.x] && !(mask && mask[i])) d[0] = a[i] * b[i];
-  block_accumulate_t<VT, 1>(d, acc + (size_t)m * acc_stride + acc_off);
+  k_dot_b<VT>(blockIdx.x, bm_mem, bm_r0, bm_r1, active, a, b, mask, acc, acc_stride, acc_off);
 }
 
 template <class VA, class VB>
@@ -1311,9 +1342,12 @@ k_krylov_decide_g(int nmem, uint8_t* active, double* sc, int32_t* niter, int itm
 }
 
 // niter[m] = 1 for the members in the Krylov solve
-__global__ void k_niter_init(int nmem, const uint8_t* active, int32_t* niter) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_niter_init_b(int bid_, int nmem, const uint8_t* active, int32_t* niter) {
+  const int m = bid_ * blockDim.x + threadIdx.x;
   if (m < nmem && active[m]) niter[m] = 1;
+}
+__global__ void k_niter_init(int nmem, const uint8_t* active, int32_t* niter) {
+  k_niter_init_b(blockIdx.x, nmem, active, niter);
 }
 
 // ============================================================================
@@ -1437,13 +1471,17 @@ __global__ void k_ikmax(const int32_t* bm_mem, const int32_t* bm_r0,
 }
 
 // per member: PNEW(IKMAX), POLD(IKMAX) gathered for the host
-__global__ void k_gather_ik(int nmem, const uint8_t* act, const int32_t* node_off,
+__device__ __forceinline__ void k_gather_ik_b(int bid_, int nmem, const uint8_t* act, const int32_t* node_off,
                             const int32_t* ikmax, Nodal nd, double* out) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = bid_ * blockDim.x + threadIdx.x;
   if (m >= nmem || !(act[m] & ACT_ITER)) return;
   const int i = node_off[m] + max(ikmax[m], 0);
   out[2 * m] = nd.pnew[i];
   out[2 * m + 1] = nd.pold[i];
+}
+__global__ void k_gather_ik(int nmem, const uint8_t* act, const int32_t* node_off,
+                            const int32_t* ikmax, Nodal nd, double* out) {
+  k_gather_ik_b(blockIdx.x, nmem, act, node_off, ikmax, nd, out);
 }
 
 // SWITCH_OLD after the norms when PINF (or PL2) <= TOLSWI
@@ -1485,9 +1523,12 @@ __global__ void k_store1(const int32_t* bm_mem, const int32_t* bm_r0,
 }
 
 // generic per-member flag kernel: out[m] = (in[m] & bits) != 0
-__global__ void k_flags(int nmem, const uint8_t* act, uint8_t bits, uint8_t* out) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_flags_b(int bid_, int nmem, const uint8_t* act, uint8_t bits, uint8_t* out) {
+  const int m = bid_ * blockDim.x + threadIdx.x;
   if (m < nmem) out[m] = (act[m] & bits) ? 1 : 0;
+}
+__global__ void k_flags(int nmem, const uint8_t* act, uint8_t bits, uint8_t* out) {
+  k_flags_b(blockIdx.x, nmem, act, bits, out);
 }
 
 
@@ -1570,16 +1611,21 @@ __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
 }
 
 // Element means of kr and Sw*Ss (NODELT) for the FP32 assembly.
-__global__ void k_elem_f32(const int32_t* ebm_mem, const int32_t* ebm_e0,
+__device__ __forceinline__ void k_elem_f32_b(int bid_, const int32_t* ebm_mem, const int32_t* ebm_e0,
                            const int32_t* ebm_e1, const uint8_t* act, const int4* tet,
                            NodalF nf) {
-  const int m = ebm_mem[blockIdx.x];
+  const int m = ebm_mem[bid_];
   if (!(act[m] & ACT_ITER)) return;
-  const int e = ebm_e0[blockIdx.x] + threadIdx.x;
-  if (e >= ebm_e1[blockIdx.x]) return;
+  const int e = ebm_e0[bid_] + threadIdx.x;
+  if (e >= ebm_e1[bid_]) return;
   const int4 t = tet[e];
   const float2 a = nf.ckr2[t.x], b = nf.ckr2[t.y], c = nf.ckr2[t.z], d = nf.ckr2[t.w];
   nf.krE[e] = make_float2(0.25f * (a.x + b.x + c.x + d.x), 0.25f * (a.y + b.y + c.y + d.y));
+}
+__global__ void k_elem_f32(const int32_t* ebm_mem, const int32_t* ebm_e0,
+                           const int32_t* ebm_e1, const uint8_t* act, const int4* tet,
+                           NodalF nf) {
+  k_elem_f32_b(blockIdx.x, ebm_mem, ebm_e0, ebm_e1, act, tet, nf);
 }
 
 // ---- compensated FP32 sums (TwoSum) for the mass-balance reductions ----
@@ -1732,12 +1778,12 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
 // FP32 boundary fluxes of the surface nodes for this iteration (BCPIC):
 // theta*ATMACT + (1-theta)*ATMOLD for Neumann atmospheric nodes, plus the
 // static non-atmospheric Neumann flux.
-__global__ void k_bcflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+__device__ __forceinline__ void k_bcflux_f32_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
                              const uint8_t* act, const MemberScal* ms, Nodal nd,
                              const float* qneu_f, float* bcf) {
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
-  const int m = bm_mem[blockIdx.x];
+  const int i = bm_r0[bid_] + threadIdx.x;
+  if (i >= bm_r1[bid_]) return;
+  const int m = bm_mem[bid_];
   if (!(act[m] & ACT_ITER)) return;
   float f = qneu_f[i];
   if (nd.ifatm[i] == 0) {
@@ -1746,6 +1792,11 @@ __global__ void k_bcflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const 
                      : (float)(th * nd.atmact[i] + (1.0 - th) * nd.atmold[i]);
   }
   bcf[i] = f;
+}
+__global__ void k_bcflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                             const uint8_t* act, const MemberScal* ms, Nodal nd,
+                             const float* qneu_f, float* bcf) {
+  k_bcflux_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, nd, qneu_f, bcf);
 }
 
 // Back-calculated flux at Dirichlet rows (BKPIC): SCR = A*PDIFF - XT5, then
@@ -1773,20 +1824,30 @@ __device__ __forceinline__ void bkflux_row(int i, bool valid, int lane, const ui
       nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
   }
 }
-__global__ void k_bkflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+__device__ __forceinline__ void k_bkflux_f32_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
                              const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
                              const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
-  const int i = bm_r0[blockIdx.x] + grp;
-  bkflux_row(i, i < bm_r1[blockIdx.x], lane, act, ms, rowptr, cols, vals, nd, nf);
+  const int i = bm_r0[bid_] + grp;
+  bkflux_row(i, i < bm_r1[bid_], lane, act, ms, rowptr, cols, vals, nd, nf);
+}
+__global__ void k_bkflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                             const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
+                             const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
+  k_bkflux_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, rowptr, cols, vals, nd, nf);
+}
+__device__ __forceinline__ void k_bkflux_list_f32_b(int bid_, int nrows, const int32_t* rows, const uint8_t* act,
+                                  const MemberScal* ms, const int32_t* rowptr,
+                                  const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
+  const int grp = (bid_ * blockDim.x + threadIdx.x) / kGroup;
+  const int lane = threadIdx.x % kGroup;
+  const bool ok = grp < nrows;
+  bkflux_row(ok ? rows[grp] : 0, ok, lane, act, ms, rowptr, cols, vals, nd, nf);
 }
 __global__ void k_bkflux_list_f32(int nrows, const int32_t* rows, const uint8_t* act,
                                   const MemberScal* ms, const int32_t* rowptr,
                                   const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
-  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
-  const int lane = threadIdx.x % kGroup;
-  const bool ok = grp < nrows;
-  bkflux_row(ok ? rows[grp] : 0, ok, lane, act, ms, rowptr, cols, vals, nd, nf);
+  k_bkflux_list_f32_b(blockIdx.x, nrows, rows, act, ms, rowptr, cols, vals, nd, nf);
 }
 
 // MASBAL sums (STORMB, FLUXMB), RELAX and NORMS for the FP32 path, one thread
@@ -1876,14 +1937,14 @@ __global__ void k_update_shl_f32(const int32_t* bm_mem, const int32_t* bm_r0,
 
 
 // STORE1 for the FP32 path: Sw(PNEW) in FP32, compensated sums.
-__global__ void k_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+__device__ __forceinline__ void k_store1_f32_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* mask, Nodal nd,
                              NodalF nf, double* red) {
-  const int m = bm_mem[blockIdx.x];
+  const int m = bm_mem[bid_];
   if (!mask[m]) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  const int i = bm_r0[bid_] + threadIdx.x;
   FF v[1] = {FF{0.0f, 0.0f}};
-  if (i < bm_r1[blockIdx.x]) {
+  if (i < bm_r1[bid_]) {
     const double p = nd.pnew[i];
     float se = 1.0f;
     if (p < -1.0e-14) se = expf(-nf.vgm[i] * log1pf(vgf_beta((float)p, nf.vgpsat[i], nf.vgn[i])));
@@ -1891,6 +1952,11 @@ __global__ void k_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
     v[0].hi = sw * nf.volnod[i] * nf.pnodi[i];
   }
   block_accumulate_ff<1>(v, red + (size_t)m * RD_NUM + RD_STORE1);
+}
+__global__ void k_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* mask, Nodal nd,
+                             NodalF nf, double* red) {
+  k_store1_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, mask, nd, nf, red);
 }
 
 // FP32 copies of the nodal van Genuchten parameters (after CHPARM)
@@ -1929,6 +1995,150 @@ __global__ void k_compact_map(int ntot, int nact, const int32_t* amem, const int
 // ============================================================================
 // host side
 // ============================================================================
+__device__ __forceinline__ void k_switch_flags_b(int bid_, int nmem, const uint8_t* act, const double* red,
+                               const double* redmax, const MemberScal* ms,
+                               int l2norm, uint8_t* out) {
+  const int m = bid_ * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  const double pinf = redmax[2 * m], pl2 = sqrt(red[(size_t)m * RD_NUM + RD_PL2]);
+  out[m] = (act[m] & ACT_ITER) && ((l2norm == 0 && pinf <= ms[m].tolswi) ||
+                                   (l2norm != 0 && pl2 <= ms[m].tolswi));
+}
+__global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
+                               const double* redmax, const MemberScal* ms,
+                               int l2norm, uint8_t* out) {
+  k_switch_flags_b(blockIdx.x, nmem, act, red, redmax, ms, l2norm, out);
+}
+
+// ============================================================================
+// Launch-fused kernels of the graph path: one launch runs the blocks of
+// several independent kernels (consecutive block ranges, one segment each),
+// or a kernel and the per-member decision that follows it.  They cut the
+// number of dependent graph nodes per Picard iteration; every segment is the
+// unchanged body of the corresponding kernel.
+// ============================================================================
+// element means | BC fluxes | Krylov member flags
+__global__ void __launch_bounds__(kThreads)
+k_pre2_f32(int ne, const int32_t* e_mem, const int32_t* e_r0, const int32_t* e_r1, int ns,
+           const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1, int nmem,
+           const uint8_t* act, const int4* tet, const MemberScal* ms, Nodal nd, NodalF nf,
+           uint8_t* active) {
+  int b = blockIdx.x;
+  if (b < ne) { k_elem_f32_b(b, e_mem, e_r0, e_r1, act, tet, nf); return; }
+  b -= ne;
+  if (b < ns) { k_bcflux_f32_b(b, s_mem, s_r0, s_r1, act, ms, nd, nf.qneu, nf.bcf); return; }
+  b -= ns;
+  k_flags_b(b, nmem, act, ACT_ITER, active);
+}
+
+// column-line factor | |b_masked|^2
+__global__ void __launch_bounds__(kThreads)
+k_pcg_setup1_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1,
+                 const int32_t* c_mem, const int32_t* c_r0, const int32_t* c_r1,
+                 const uint8_t* active, const MemberScal* ms, const int32_t* diag,
+                 const int32_t* down, const float* vals, const uint8_t* dmask, float* pinv,
+                 float* cdown, const float* b, double* sc) {
+  int bb = blockIdx.x;
+  if (bb < ns) {
+    k_line_setup_b<float, float>(bb, s_mem, s_r0, s_r1, active, ms, diag, down, vals, dmask,
+                                 pinv, cdown);
+    return;
+  }
+  bb -= ns;
+  k_dot_b<float>(bb, c_mem, c_r0, c_r1, active, b, b, dmask, sc, SC_N, SC_XL);
+}
+
+// p = M^-1 r | iteration counts
+__global__ void __launch_bounds__(kThreads)
+k_pcg_setup3_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1,
+                 const uint8_t* active, const MemberScal* ms, const float* pinv,
+                 const float* cdown, const float* r, float* p, int nmem, int32_t* niter) {
+  int bb = blockIdx.x;
+  if (bb < ns) {
+    k_line_apply_b<float>(bb, s_mem, s_r0, s_r1, active, ms, pinv, cdown, r, p, nullptr, nullptr,
+                          0, 0);
+    return;
+  }
+  bb -= ns;
+  k_niter_init_b(bb, nmem, active, niter);
+}
+
+// p = z + beta p, then the PCG decision by the last block to finish: the
+// per-member test of k_krylov_decide_g and the WHILE node's condition.
+__global__ void __launch_bounds__(kThreads)
+k_pcg_update_p_decide(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                      uint8_t* active, double* sc, float* p, const float* z, int nmem,
+                      int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
+                      unsigned int* done, cudaGraphConditionalHandle h) {
+  k_pcg_update_p_b<float>(blockIdx.x, bm_mem, bm_r0, bm_r1, active, sc, p, z);
+  __shared__ int s_last, s_cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    s_cnt = 0;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  int mine = 0;
+  for (int m = threadIdx.x; m < nmem; m += blockDim.x) {
+    if (!active[m]) continue;
+    double* S = sc + (size_t)m * SC_N;
+    const double xl = S[SC_XL];
+    const double err = (xl > 0.0) ? sqrt(S[SC_RR] / xl) : 0.0;
+    S[SC_ERR] = err;
+    if (err > tol && niter[m] < itmax) {
+      niter[m] += 1;
+      mine++;
+    } else {
+      active[m] = 0;
+    }
+    S[SC_PR] = S[SC_PQ] = S[SC_QZ] = S[SC_RR] = 0.0;
+  }
+  if (mine) atomicAdd(&s_cnt, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *done = 0u;
+    const int l = *loops + 1;
+    *loops = l;
+    cudaGraphSetConditional(h, (s_cnt > 0 && l < maxloops) ? 1u : 0u);
+  }
+}
+
+// back-calculated fluxes: surface rows | deep static Dirichlet rows
+__global__ void __launch_bounds__(kThreads)
+k_bkflux_all_f32(int ns16, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1,
+                 int ndeep, const int32_t* deep, const uint8_t* act, const MemberScal* ms,
+                 const int32_t* rowptr, const int32_t* cols, const float* vals, Nodal nd,
+                 NodalF nf) {
+  int bb = blockIdx.x;
+  if (bb < ns16) {
+    k_bkflux_f32_b(bb, s_mem, s_r0, s_r1, act, ms, rowptr, cols, vals, nd, nf);
+    return;
+  }
+  bb -= ns16;
+  k_bkflux_list_f32_b(bb, ndeep, deep, act, ms, rowptr, cols, vals, nd, nf);
+}
+
+// per member: PNEW/POLD at IKMAX, and whether SWITCH_OLD runs
+__global__ void k_member_post(int nmem, const uint8_t* act, const int32_t* node_off,
+                              const int32_t* ikmax, Nodal nd, double* ikval, const double* red,
+                              const double* redmax, const MemberScal* ms, int l2norm,
+                              uint8_t* sw) {
+  k_gather_ik_b(blockIdx.x, nmem, act, node_off, ikmax, nd, ikval);
+  k_switch_flags_b(blockIdx.x, nmem, act, red, redmax, ms, l2norm, sw);
+}
+
+// STORE1 of every member whose action bits include ACT_ITER
+__global__ void k_store1_iter_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                                  const int32_t* bm_r1, const uint8_t* act, Nodal nd, NodalF nf,
+                                  double* red) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  k_store1_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, act, nd, nf, red);
+}
+
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 // Host view of one member: mesh, inputs and time-stepping state.
@@ -2052,7 +2262,9 @@ struct Engine {
   void atm_setup_member(MemberHost& h, bool initial);
   void atm_advance(MemberHost& h);  // ATMNXT series advance
   void atm_back(MemberHost& h);     // ATMBAK
-  void push_scalars();
+  // member scalars to the device (to_pinned: into the pinned buffer that the
+  // graph of the macro-iteration copies)
+  void push_scalars(bool to_pinned = false);
   int macro_iteration();
   void picard_or_newton_iteration(const std::vector<int>& itm);
   // phase 0: whole solve with host checks every chk iterations; 1: set-up
@@ -2104,7 +2316,7 @@ struct Engine {
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
   void iteration_pre(int solve_phase);
-  void iteration_post();
+  void iteration_post(bool graph = false);
   void start_kernels();
   // CUDA graph of one macro-iteration (FP32 Picard path)
   cudaGraph_t g_graph = nullptr;
@@ -2114,9 +2326,18 @@ struct Engine {
   // host-side phase timers of macro-iterations (ms): preparation, waiting for
   // the device (launch + synchronise), decisions; macro-iteration count
   double tm_prep = 0, tm_dev = 0, tm_host = 0, tm_graph = 0;
+  // graph GPU time by the number of rows with work (log2 bins)
+  double bin_ms[32] = {}, bin_n[32] = {};
+  int64_t cur_rows = 0;
   int64_t n_macro = 0;
   cudaEvent_t gev0 = nullptr, gev1 = nullptr;  // around graph launches
   DBuf<int32_t> d_loops;
+  DBuf<uint8_t> d_inbuf;    // [member scalars | action bits]
+  DBuf<unsigned int> d_done;  // block counter of k_pcg_update_p_decide
+  DBuf<double> d_resbuf;    // [sc | loops | red | redmax | ikmax | ikval | niter]
+  size_t res_off[8] = {0, 0, 0, 0, 0, 0, 0, 0}, res_zero = 0;
+  uint8_t* hp_in = nullptr;  // pinned mirror of d_inbuf
+  double* hp_res = nullptr;  // pinned mirror of d_resbuf
   uint8_t* hp_act = nullptr;
   MemberScal* hp_ms = nullptr;
   double *hp_red = nullptr, *hp_redmax = nullptr, *hp_ikv = nullptr, *hp_sc = nullptr;
@@ -2630,12 +2851,38 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     if (precision == 0) { d_linv64.alloc(N); d_lc64.alloc(N); }
     else { d_linv32.alloc(N); d_lc32.alloc(N); }
   }
-  d_act.alloc(nmem); d_active.alloc(nmem); d_switch.alloc(nmem); d_mask2.alloc(nmem);
+  d_active.alloc(nmem); d_switch.alloc(nmem); d_mask2.alloc(nmem);
   d_outer.alloc(nmem);
-  d_ms.alloc(nmem);
-  d_red.alloc((size_t)nmem * RD_NUM); d_redmax.alloc((size_t)nmem * 2);
-  d_sc.alloc((size_t)nmem * SC_N); d_sc.zero(st);
-  d_ikmax.alloc(nmem); d_ikval.alloc((size_t)nmem * 2); d_niter.alloc(nmem); d_nact.alloc(1);
+  // per-macro-iteration inputs (member scalars, action bits) and per-member
+  // results packed in one buffer each, so a CUDA graph moves each with one
+  // copy; the results' zeroed part comes first
+  {
+    const size_t ims = sizeof(MemberScal) * nmem;
+    d_inbuf.alloc(ims + nmem);
+    d_ms.view(reinterpret_cast<MemberScal*>(d_inbuf.p), nmem);
+    d_act.view(d_inbuf.p + ims, nmem);
+    const size_t nm2 = (size_t)(nmem + 1) / 2;  // int32 counts padded to doubles
+    res_off[0] = 0;                                   // sc
+    res_off[1] = res_off[0] + (size_t)nmem * SC_N;    // loops (1 int32)
+    res_off[2] = res_off[1] + 1;                      // red
+    res_off[3] = res_off[2] + (size_t)nmem * RD_NUM;  // redmax
+    res_off[4] = res_off[3] + (size_t)2 * nmem;       // ikmax (int32)
+    res_off[5] = res_off[4] + nm2;                    // ikval
+    res_off[6] = res_off[5] + (size_t)2 * nmem;       // niter (int32)
+    res_off[7] = res_off[6] + nm2;                    // end
+    res_zero = res_off[5];
+    d_resbuf.alloc(res_off[7]);
+    d_resbuf.zero(st);
+    double* b = d_resbuf.p;
+    d_sc.view(b + res_off[0], (size_t)nmem * SC_N);
+    d_loops.view(reinterpret_cast<int32_t*>(b + res_off[1]), 1);
+    d_red.view(b + res_off[2], (size_t)nmem * RD_NUM);
+    d_redmax.view(b + res_off[3], (size_t)2 * nmem);
+    d_ikmax.view(reinterpret_cast<int32_t*>(b + res_off[4]), nmem);
+    d_ikval.view(b + res_off[5], (size_t)2 * nmem);
+    d_niter.view(reinterpret_cast<int32_t*>(b + res_off[6]), nmem);
+  }
+  d_nact.alloc(1);
   make_blockmap(bm1, kThreads);
   make_blockmap(bm16, kRowsPerBlock16);
   make_elem_blockmap(bme, kThreads);
@@ -2777,7 +3024,7 @@ void Engine::reset() {
   CG_TRY(cudaMemcpyAsync(nd.ifatmp, s_ifatmp.p, N, cudaMemcpyDeviceToDevice, st));
 }
 
-void Engine::push_scalars() {
+void Engine::push_scalars(bool to_pinned) {
   bool nodal_dirty = false;
   for (int m = 0; m < nmem; ++m) {
     MemberHost& h = *M[m];
@@ -2789,7 +3036,7 @@ void Engine::push_scalars() {
     S.nnod = h.meshp->nnod; S.nstr = h.meshp->nstr; S.iopt = iopt; S.pad = 0;
     if (h.atm_nodal_dirty) nodal_dirty = true;
   }
-  if (graphs_on()) std::memcpy(hp_ms, h_ms.data(), sizeof(MemberScal) * nmem);
+  if (to_pinned) std::memcpy(hp_ms, h_ms.data(), sizeof(MemberScal) * nmem);
   else d_ms.upload(h_ms.data(), nmem, st);
   if (nodal_dirty) {
     for (int m = 0; m < nmem; ++m) {
@@ -2919,6 +3166,39 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
     tmp = w32[6].p; dinv = w32[7].p; F = d_F32.p; linv = d_linv32.p; lc = d_lc32.p;
   }
   const int pc = precond;
+  if constexpr (sizeof(MT) == 4 && sizeof(VT) == 4) {
+    if (phase != 0 && pc == 2 && cbms.nblk && cbm1.nblk) {
+      if (phase == 1) {
+        // column-line factor | |b|^2 ; x0 = M^-1 b ; r = b - A x0 ;
+        // p = M^-1 r | iteration counts (sc and the loop counter were zeroed
+        // at the start of the graph)
+        k_pcg_setup1_f32<<<cbms.nblk + cbm1.nblk, kThreads, 0, st>>>(cbms.nblk, cbms.mem.p,
+            cbms.r0.p, cbms.r1.p, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, d_ms.p, d_diag.p,
+            d_down.p, vals, d_dmask.p, linv, lc, b, d_sc.p);
+        k_line_apply<VT><<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
+            d_active.p, d_ms.p, linv, lc, b, x, nullptr, d_sc.p, SC_N, SC_QZ);
+        k_resid<MT, VT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+            d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, x, b, r, nullptr, 0);
+        k_pcg_setup3_f32<<<cbms.nblk + cdiv(nmem, kThreads), kThreads, 0, st>>>(cbms.nblk,
+            cbms.mem.p, cbms.r0.p, cbms.r1.p, d_active.p, d_ms.p, linv, lc, r, p, nmem, d_niter.p);
+        count(4);
+      } else {
+        k_spmv<MT, VT><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
+            d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+        k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+            d_active.p, d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
+        k_line_apply<VT><<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
+            d_active.p, d_ms.p, linv, lc, r, z, q, d_sc.p, SC_N, SC_QZ);
+        k_pcg_update_p_decide<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+            d_active.p, d_sc.p, p, z, nmem, d_niter.p, itmax, tol, d_loops.p, itmax + 2, d_done.p,
+            gh);
+        count(4);
+      }
+      check_launch();
+      return;
+    }
+  }
   if (phase == 2) {
     // one PCG iteration of the graph's WHILE body (see below for the steps)
     k_spmv<MT, VT><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
@@ -3117,15 +3397,6 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
   }
 }
 
-__global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
-                               const double* redmax, const MemberScal* ms,
-                               int l2norm, uint8_t* out) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= nmem) return;
-  const double pinf = redmax[2 * m], pl2 = sqrt(red[(size_t)m * RD_NUM + RD_PL2]);
-  out[m] = (act[m] & ACT_ITER) && ((l2norm == 0 && pinf <= ms[m].tolswi) ||
-                                   (l2norm != 0 && pl2 <= ms[m].tolswi));
-}
 
 // One nonlinear iteration for every member flagged ACT_ITER, in three
 // phases: pre-solve (soil characteristics, assembly, BCs), the linear solve,
@@ -3140,16 +3411,25 @@ void Engine::iteration_pre(int solve_phase) {
     // correction to opts.inner_tol.
     k_vg_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd, nf,
                                             d_nodal[ND_Z].p);
-    k_elem_f32<<<cbme.nblk, kThreads, 0, st>>>(cbme.mem.p, cbme.r0.p, cbme.r1.p, d_act.p, d_tet.p, nf);
     count();
-    if (cbms.nblk)
-      k_bcflux_f32<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p,
-                                                   nd, nf.qneu, nf.bcf);
+    if (solve_phase == 1) {
+      // graph: element means | BC fluxes | Krylov flags in one launch
+      k_pre2_f32<<<cbme.nblk + cbms.nblk + cdiv(nmem, kThreads), kThreads, 0, st>>>(
+          cbme.nblk, cbme.mem.p, cbme.r0.p, cbme.r1.p, cbms.nblk, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+          nmem, d_act.p, d_tet.p, d_ms.p, nd, nf, d_active.p);
+      count();
+    } else {
+      k_elem_f32<<<cbme.nblk, kThreads, 0, st>>>(cbme.mem.p, cbme.r0.p, cbme.r1.p, d_act.p, d_tet.p, nf);
+      if (cbms.nblk)
+        k_bcflux_f32<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p,
+                                                     nd, nf.qneu, nf.bcf);
+      k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
+      count(3);
+    }
     k_assemble_picard_f32<<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
         d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, d_rec32.p, d_dmask.p,
         nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
-    k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
-    count(4);
+    count();
     check_launch();
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
                             std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1,
@@ -3167,9 +3447,30 @@ void Engine::iteration_pre(int solve_phase) {
   }
 }
 
-void Engine::iteration_post() {
+void Engine::iteration_post(bool graph) {
   const bool mixed = (precision == 1 && iopt == 1);
   const cathy_parm_t& P0 = M[0]->parm;
+  if (graph && mixed) {
+    // graph path: the result buffer was zeroed at the start of the graph
+    k_update_shl_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
+                                                    nf.pdiff);
+    const int nb = cbms16.nblk + cdiv((long)ndeep * kGroup, kThreads);
+    if (nb)
+      k_bkflux_all_f32<<<nb, kThreads, 0, st>>>(cbms16.nblk, cbms16.mem.p, cbms16.r0.p,
+          cbms16.r1.p, ndeep, d_deep.p, d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
+    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
+        d_ms.p, nd, nf, nf.volnod, nf.pnodi, d_red.p, d_redmax.p);
+    k_ikmax<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
+                                           d_redmax.p, d_ikmax.p, 1);
+    k_member_post<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_node_off.p, d_ikmax.p, nd,
+        d_ikval.p, d_red.p, d_redmax.p, d_ms.p, P0.l2norm, d_switch.p);
+    if (cbms.nblk)
+      k_switch<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p,
+                                               d_switch.p, d_ms.p, nd);
+    count(6);
+    check_launch();
+    return;
+  }
   if (mixed)
     k_update_shl_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
                                                     nf.pdiff);
@@ -3241,22 +3542,26 @@ void Engine::graph_free() {
 
 void Engine::pinned_alloc() {
   pinned_free();
-  CG_TRY(cudaMallocHost((void**)&hp_act, std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_ms, sizeof(MemberScal) * std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_red, sizeof(double) * RD_NUM * std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_redmax, sizeof(double) * 2 * std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_ikv, sizeof(double) * 2 * std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_sc, sizeof(double) * SC_N * std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_ikmax, sizeof(int32_t) * std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_nit, sizeof(int32_t) * std::max(nmem, 1)));
-  CG_TRY(cudaMallocHost((void**)&hp_loops, sizeof(int32_t)));
-  d_loops.alloc(1);
+  const size_t ims = sizeof(MemberScal) * nmem;
+  CG_TRY(cudaMallocHost((void**)&hp_in, ims + nmem));
+  CG_TRY(cudaMallocHost((void**)&hp_res, sizeof(double) * res_off[7]));
+  hp_ms = reinterpret_cast<MemberScal*>(hp_in);
+  hp_act = hp_in + ims;
+  hp_sc = hp_res + res_off[0];
+  hp_loops = reinterpret_cast<int32_t*>(hp_res + res_off[1]);
+  hp_red = hp_res + res_off[2];
+  hp_redmax = hp_res + res_off[3];
+  hp_ikmax = reinterpret_cast<int32_t*>(hp_res + res_off[4]);
+  hp_ikv = hp_res + res_off[5];
+  hp_nit = reinterpret_cast<int32_t*>(hp_res + res_off[6]);
+  d_done.alloc(1);
+  d_done.zero(st);
 }
 
 void Engine::pinned_free() {
-  void* ps[] = {hp_act, hp_ms, hp_red, hp_redmax, hp_ikv, hp_sc, hp_ikmax, hp_nit, hp_loops};
-  for (void* q : ps)
-    if (q) cudaFreeHost(q);
+  if (hp_in) cudaFreeHost(hp_in);
+  if (hp_res) cudaFreeHost(hp_res);
+  hp_in = nullptr; hp_res = nullptr;
   hp_act = nullptr; hp_ms = nullptr; hp_red = hp_redmax = hp_ikv = hp_sc = nullptr;
   hp_ikmax = hp_nit = hp_loops = nullptr;
 }
@@ -3271,8 +3576,8 @@ void Engine::graph_build() {
   // A
   int64_t c0 = launches;
   CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  CG_TRY(cudaMemcpyAsync(d_act.p, hp_act, nmem, cudaMemcpyHostToDevice, st));
-  CG_TRY(cudaMemcpyAsync(d_ms.p, hp_ms, sizeof(MemberScal) * nmem, cudaMemcpyHostToDevice, st));
+  CG_TRY(cudaMemcpyAsync(d_inbuf.p, hp_in, d_inbuf.n, cudaMemcpyHostToDevice, st));
+  CG_TRY(cudaMemsetAsync(d_resbuf.p, 0, sizeof(double) * res_zero, st));
   start_kernels();
   iteration_pre(1);
   cudaGraph_t gA = nullptr;
@@ -3301,17 +3606,11 @@ void Engine::graph_build() {
   // C
   c0 = launches;
   CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  iteration_post();
-  k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_mask2.p);
-  k_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, nf, d_red.p);
-  count(2);
-  CG_TRY(cudaMemcpyAsync(hp_red, d_red.p, sizeof(double) * nmem * RD_NUM, cudaMemcpyDeviceToHost, st));
-  CG_TRY(cudaMemcpyAsync(hp_redmax, d_redmax.p, sizeof(double) * nmem * 2, cudaMemcpyDeviceToHost, st));
-  CG_TRY(cudaMemcpyAsync(hp_ikv, d_ikval.p, sizeof(double) * nmem * 2, cudaMemcpyDeviceToHost, st));
-  CG_TRY(cudaMemcpyAsync(hp_ikmax, d_ikmax.p, sizeof(int32_t) * nmem, cudaMemcpyDeviceToHost, st));
-  CG_TRY(cudaMemcpyAsync(hp_nit, d_niter.p, sizeof(int32_t) * nmem, cudaMemcpyDeviceToHost, st));
-  CG_TRY(cudaMemcpyAsync(hp_sc, d_sc.p, sizeof(double) * nmem * SC_N, cudaMemcpyDeviceToHost, st));
-  CG_TRY(cudaMemcpyAsync(hp_loops, d_loops.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  iteration_post(true);
+  k_store1_iter_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
+                                                    nf, d_red.p);
+  count();
+  CG_TRY(cudaMemcpyAsync(hp_res, d_resbuf.p, sizeof(double) * res_off[7], cudaMemcpyDeviceToHost, st));
   cudaGraph_t gC = nullptr;
   CG_TRY(cudaStreamEndCapture(st, &gC));
   g_nC = launches - c0;
@@ -3345,8 +3644,8 @@ int Engine::macro_iteration() {
     h_act[m] = a;
     h.pend &= (uint8_t)~a;  // bits not executed now stay pending
   }
-  push_scalars();
   const bool graph = graphs_on() && niter_members > 0;
+  push_scalars(graph);
   if (!graph) d_act.upload(h_act.data(), nmem, st);
   else std::memcpy(hp_act, h_act.data(), nmem);
   {
@@ -3375,6 +3674,12 @@ int Engine::macro_iteration() {
       float gms = 0.0f;
       CG_TRY(cudaEventElapsedTime(&gms, gev0, gev1));
       tm_graph += gms;
+      int64_t rows = 0;
+      for (int m : itm) rows += node_off[m + 1] - node_off[m];
+      int b = 0;
+      while (b < 31 && (rows >> (b + 1)) > 0) ++b;
+      bin_ms[b] += gms;
+      bin_n[b] += 1.0;
     }
     g_launches++;
     launches += g_nA + g_nC + g_nB * (int64_t)(*hp_loops);
@@ -3805,6 +4110,8 @@ int engine_timers(Engine* e, double* out, int n) {
   const double v[8] = {(double)e->n_macro, (double)e->g_launches, (double)e->g_builds,
                        e->tm_prep, e->tm_dev, e->tm_host, e->gpu_ms, e->tm_graph};
   for (int q = 0; q < n && q < 8; ++q) out[q] = v[q];
+  for (int q = 8; q < n && q < 8 + 64; ++q)
+    out[q] = ((q - 8) & 1) ? e->bin_ms[(q - 8) / 2] : e->bin_n[(q - 8) / 2];
   return 0;
 }
 

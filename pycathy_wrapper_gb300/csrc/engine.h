@@ -28,10 +28,19 @@ template <class T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  bool owned = true;
   void alloc(size_t count) {
     free();
     n = count;
+    owned = true;
     if (count) CG_TRY(cudaMalloc((void**)&p, sizeof(T) * count));
+  }
+  // a non-owning window into another allocation
+  void view(T* ptr, size_t count) {
+    free();
+    p = ptr;
+    n = count;
+    owned = false;
   }
   void zero(cudaStream_t s) {
     if (n) CG_TRY(cudaMemsetAsync(p, 0, sizeof(T) * n, s));
@@ -43,9 +52,10 @@ struct DBuf {
     if (count) CG_TRY(cudaMemcpyAsync(h, p, sizeof(T) * count, cudaMemcpyDeviceToHost, s));
   }
   void free() {
-    if (p) cudaFree(p);
+    if (p && owned) cudaFree(p);
     p = nullptr;
     n = 0;
+    owned = true;
   }
   ~DBuf() { free(); }
 };
