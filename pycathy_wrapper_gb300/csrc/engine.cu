@@ -644,8 +644,9 @@ __device__ __forceinline__ uint64_t gtimer() {
 // lanes per row); per-member sums stay in registers while the entries belong
 // to the same member and are flushed (one block reduction, one FP64 atomic
 // per quantity) when the member changes.  Arithmetic in the vector type VT.
+constexpr int kSpmvThreads = 128;
 template <class MT, class VT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kSpmvThreads)
 k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
        const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
        const MT* vals, const uint8_t* dmask, const VT* x, VT* y, const VT* w,
@@ -661,16 +662,24 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
     __syncthreads();
     if (s_slot < 0) lt = nullptr;
   }
-  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  // 8 lanes per row (two slots per lane: rows have at most 15), 16 rows per
+  // map entry = one block of kSpmvThreads
+  const int grp = threadIdx.x >> 3, lane = threadIdx.x & 7;
   VT d[2] = {0, 0};
   int cur = -1;
   double bytes = 0.0;
   // each block takes a contiguous run of map entries (one or two members)
   const int chunk = (nblk + gridDim.x - 1) / gridDim.x;
   const int b0 = blockIdx.x * chunk, b1 = min(nblk, b0 + chunk);
-  for (int b = b0; b < b1; ++b) {
+  // two map entries of the same member per iteration: both entries' loads
+  // are in flight together
+  for (int b = b0; b < b1;) {
     const int m = bm_mem[b];
-    if (!active[m]) continue;  // block-uniform
+    const int nb = (b + 1 < b1 && bm_mem[b + 1] == m) ? 2 : 1;
+    if (!active[m]) {  // block-uniform
+      b += nb;
+      continue;
+    }
     if (acc && m != cur) {
       if (cur >= 0) {
         block_accumulate_t<VT, 2>(d, acc + (size_t)cur * acc_stride);
@@ -679,27 +688,68 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
       d[0] = d[1] = 0;
       cur = m;
     }
-    const int r0 = bm_r0[b], r1 = bm_r1[b];
-    const int i = r0 + grp;
-    const bool rowok = i < r1;
-    if (alg_bytes && threadIdx.x == 0) {
-      // values + column indices + row pointers + x read + y written (+ w read)
-      const double nz = (double)(rowptr[r1] - rowptr[r0]);
-      bytes += nz * (sizeof(MT) + 4) + (r1 - r0) * (4.0 + (w ? 3.0 : 2.0) * sizeof(VT));
+    int i[2];
+    bool rowok[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      rowok[u] = false;
+      i[u] = 0;
+      if (u < nb) {
+        const int r0 = bm_r0[b + u], r1 = bm_r1[b + u];
+        i[u] = r0 + grp;
+        rowok[u] = i[u] < r1;
+        if (alg_bytes && threadIdx.x == 0) {
+          // values + column indices + row pointers + x read + y written (+ w read)
+          const double nz = (double)(rowptr[r1] - rowptr[r0]);
+          bytes += nz * (sizeof(MT) + 4) + (r1 - r0) * (4.0 + (w ? 3.0 : 2.0) * sizeof(VT));
+        }
+      }
     }
-    VT s = 0;
-    if (rowok) {
-      const int s0 = rowptr[i] + lane;
-      if (s0 < rowptr[i + 1]) s = (VT)vals[s0] * x[cols[s0]];
+    int sa[2], se[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      sa[u] = 0;
+      se[u] = 0;
+      if (rowok[u]) {
+        sa[u] = rowptr[i[u]] + lane;
+        se[u] = rowptr[i[u] + 1];
+      }
     }
-    s = group_sum<VT>(s);
-    if (rowok && lane == 0) {
-      const VT xi = x[i];
-      const VT yi = dmask[i] ? xi : s;
-      y[i] = yi;
-      d[0] += xi * yi;
-      if (w) d[1] += xi * w[i];
+    MT va[2], vc[2];
+    int ca[2], cc[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const bool a = sa[u] < se[u], c = sa[u] + 8 < se[u];
+      va[u] = a ? vals[sa[u]] : (MT)0;
+      vc[u] = c ? vals[sa[u] + 8] : (MT)0;
+      ca[u] = a ? cols[sa[u]] : -1;
+      cc[u] = c ? cols[sa[u] + 8] : -1;
     }
+    VT sum[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const VT xa = ca[u] >= 0 ? x[ca[u]] : (VT)0, xc = cc[u] >= 0 ? x[cc[u]] : (VT)0;
+      VT t = 0;
+      if (ca[u] >= 0) t = (VT)va[u] * xa;
+      if (cc[u] >= 0) t += (VT)vc[u] * xc;
+      sum[u] = t;
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      sum[0] += __shfl_xor_sync(0xffffffffu, sum[0], o);
+      sum[1] += __shfl_xor_sync(0xffffffffu, sum[1], o);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (rowok[u] && lane == 0) {
+        const VT xi = x[i[u]];
+        const VT yi = dmask[i[u]] ? xi : sum[u];
+        y[i[u]] = yi;
+        d[0] += xi * yi;
+        if (w) d[1] += xi * w[i[u]];
+      }
+    }
+    b += nb;
   }
   if (acc && cur >= 0) block_accumulate_t<VT, 2>(d, acc + (size_t)cur * acc_stride);
   if (alg_bytes && threadIdx.x == 0 && bytes != 0.0) atomicAdd(alg_bytes, bytes);
@@ -1670,34 +1720,49 @@ __device__ __forceinline__ void block_accumulate_ff(FF (&v)[NV], double* acc) {
   }
 }
 
-// Row-owned Picard assembly in FP32.  One 16-lane group per row; the lanes
-// take the row's incident elements in parallel (lane j: incidences j, j+16,
-// ...) and compute each element's four local LHS entries and RHS terms.  The
-// diagonal entries are summed by a shuffle reduction; the off-diagonal ones
-// are written to shared memory at position q*4 + l (incidence q, local node
-// l) and each slot's owner lane adds its contributions through a gather list
-// precomputed from the mesh (the slot of (i, j) collects the incidences
-// whose element contains j, in incidence order): deterministic, no atomics,
-// no search.  RHS = -sum K (h_l - h_k) - mass terms, see the FP32 block
+// Compact FP32 element record for the assembly: S[10], |V|, |V|*porosity.
+__global__ void k_rec48(int nt, const TetRec<float>* rec, float4* out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nt) return;
+  const TetRec<float> R = rec[e];
+  out[3 * (size_t)e] = make_float4(R.S[0], R.S[1], R.S[2], R.S[3]);
+  out[3 * (size_t)e + 1] = make_float4(R.S[4], R.S[5], R.S[6], R.S[7]);
+  out[3 * (size_t)e + 2] = make_float4(R.S[8], R.S[9], R.vol, R.vpel);
+}
+
+// Row-owned Picard assembly in FP32.  One 16-lane group per row.  The lanes
+// first stage the row's column heads (total head as a float hi/lo pair, and
+// the head/saturation changes for a consistent mass matrix) in shared
+// memory, then take the row's incident elements in parallel (lane j:
+// incidences j, j+16, ...): each incidence reads its element record and the
+// row-local slots of the element's four nodes (precomputed, 4 bits each), so
+// no node id or nodal value is gathered from global memory per incidence.
+// The diagonal entries are summed by a shuffle reduction; the off-diagonal
+// ones are written to shared memory at position q*4 + l (incidence q, local
+// node l) and each slot's owner lane adds its contributions through a gather
+// list precomputed from the mesh (in incidence order): deterministic, no
+// atomics.  RHS = -sum K (h_l - h_k) - mass terms, see the FP32 block
 // comment; BC fluxes come precomputed in FP32 (bcf).
 __global__ void __launch_bounds__(kThreads)
 k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
                       const uint8_t* act, const MemberScal* ms,
                       const int32_t* rowptr, const int32_t* cols,
-                      const int32_t* inc_ptr, const int32_t* inc, const int4* tet,
-                      const TetRec<float>* rec, const uint8_t* dmask, NodalF nf,
-                      const float* bcf, float* vals, float lm_d, float lm_o,
-                      const int64_t* __restrict__ glrow, const uint8_t* __restrict__ gloff,
-                      const uint8_t* __restrict__ gl) {
+                      const int32_t* inc_ptr, const int32_t* inc,
+                      const uint16_t* __restrict__ islot, const float4* __restrict__ rec48,
+                      const uint8_t* dmask, NodalF nf, const float* bcf, float* vals,
+                      float lm_d, float lm_o, const int64_t* __restrict__ glrow,
+                      const uint8_t* __restrict__ gloff, const uint8_t* __restrict__ gl) {
   const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
   __shared__ float sval[kRowsPerBlock16][64 * 4];
+  __shared__ float2 sh2[kRowsPerBlock16][kGroup];
+  __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
   const int i = bm_r0[blockIdx.x] + grp;
   const bool rowok = i < bm_r1[blockIdx.x];
   const MemberScal& S = ms[m];
   const float rdt = (float)S.deltat_r, th = (float)S.tetaf;
-  int s0 = 0, rlen = 0, p0 = 0, p1 = 0;
+  int s0 = 0, rlen = 0, p0 = 0, p1 = 0, col = -1;
   float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f;
   if (rowok) {
     s0 = rowptr[i];
@@ -1705,7 +1770,16 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     p0 = inc_ptr[i];
     p1 = inc_ptr[i + 1];
     et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
+    if (lane < rlen) col = cols[s0 + lane];
   }
+  if (col >= 0) {
+    sh2[grp][lane] = nf.h2[col];
+    if (lm_o != 0.0f) {
+      sdp[grp][lane] = nf.dpsi[col];
+      sds[grp][lane] = nf.dsw[col];
+    }
+  }
+  __syncwarp();
   int ntrip = (p1 - p0 + kGroup - 1) / kGroup;
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
   float dacc = 0.0f, rp = 0.0f, msum = 0.0f, mssum = 0.0f;
@@ -1714,13 +1788,12 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     const int p = p0 + q;
     if (rowok && p < p1) {
       const int ek = inc[p];
+      const int isl = islot[p];
       const int e = ek >> 2, k = ek & 3;
-      const int4 t = tet[e];
-      const int tn[4] = {t.x, t.y, t.z, t.w};
-      const float4* rv = reinterpret_cast<const float4*>(rec + e);
-      const float4 r0 = rv[0], r1 = rv[1], r2 = rv[2], r3 = rv[3];
+      const float4* rv = rec48 + 3 * (size_t)e;
+      const float4 r0 = rv[0], r1 = rv[1], r2 = rv[2];
       const float Sv[10] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y};
-      const float vol = r3.z, vpel = r3.w;
+      const float vol = r2.z, vpel = r2.w;
       const float2 ke = nf.krE[e];
       const float kr = ke.x, e1 = ke.y;
       const float ve1 = vol * e1;
@@ -1735,15 +1808,15 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
         } else {
           sval[grp][q * 4 + l] = c;
         }
-        const int nl = tn[l];
-        const float2 hn = nf.h2[nl];
+        const int sl = (isl >> (4 * l)) & 15;
+        const float2 hn = sh2[grp][sl];
         const float dh = (hn.x - hh_i) + (hn.y - hl_i);
         rp -= kr * skl * dh;
         if (l == k) {
           msum += ve1 * lm_d;
           mssum += vpel * lm_d;
         } else if (lm_o != 0.0f) {
-          rp -= (ve1 * lm_o * nf.dpsi[nl] + vpel * lm_o * nf.dsw[nl]) * rdt;
+          rp -= (ve1 * lm_o * sdp[grp][sl] + vpel * lm_o * sds[grp][sl]) * rdt;
         }
       }
     }
@@ -1757,7 +1830,7 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   if (lane < rlen) {
     const int sl = s0 + lane;
     float lhs;
-    if (cols[sl] == i) {
+    if (col == i) {
       lhs = dsum;
     } else {
       const int64_t base = glrow[i];
@@ -2209,6 +2282,8 @@ struct Engine {
   // contribution positions q*4 + l
   DBuf<int64_t> d_glrow;
   DBuf<uint8_t> d_gloff, d_gl;
+  DBuf<uint16_t> d_islot;  // per incidence: row-local slots of the element's 4 nodes (4 bits each)
+  DBuf<float4> d_rec48;    // per element: S[10], volume, volume*porosity (3 x float4)
   DBuf<int32_t> d_srows, d_lev_f, d_lev_b;
   std::vector<int32_t> lev_f_ptr, lev_b_ptr;  // batched levels (host)
   DBuf<double> d_vals64;
@@ -2313,6 +2388,7 @@ struct Engine {
     lt_reset();
   }
   int grid_persist(int nblk) const { return std::max(1, std::min(nblk, persist_blocks)); }
+  int grid_spmv(int nblk) const { return std::max(1, std::min(nblk, 2 * persist_blocks)); }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
   void iteration_pre(int solve_phase);
@@ -2545,6 +2621,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   const bool glists = (precision == 1 && iopt == 1);
   std::vector<int64_t> h_glrow(glists ? N + 1 : 0, 0);
   std::vector<uint8_t> h_gloff(glists ? NNZ : 0, 0), h_gl;
+  std::vector<uint16_t> h_islot(glists ? (size_t)4 * NT : 0, 0);
   if (glists) h_gl.reserve((size_t)12 * NT);
   std::vector<int4> h_tet(NT);
   std::vector<double> h_x(N), h_y(N), h_z(N), h_arenod(N, 0.0);
@@ -2606,13 +2683,16 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         for (int sj = 0; sj < rl; ++sj) cnt[sj] = 0;
         for (int q = 0; q < ninc; ++q) {
           const int e = g.inc[p0 + q] >> 2, k = g.inc[p0 + q] & 3;
+          uint16_t packed = 0;
           for (int l = 0; l < 4; ++l) {
-            if (l == k) continue;
             const int j = g.tetra[5 * e + l] - 1;
             const int sj = (int)(std::lower_bound(g.cols.begin() + s0, g.cols.begin() + s0 + rl, j) -
                                  (g.cols.begin() + s0));
+            packed |= (uint16_t)(sj << (4 * l));
+            if (l == k) continue;
             lst[sj][cnt[sj]++] = (uint8_t)(q * 4 + l);
           }
+          h_islot[(size_t)h_incptr[no + i] + q] = packed;
         }
         h_glrow[no + i] = (int64_t)h_gl.size();
         int off = 0;
@@ -2753,6 +2833,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     d_glrow.alloc(N + 1); d_glrow.upload(h_glrow.data(), N + 1, st);
     d_gloff.alloc(NNZ); d_gloff.upload(h_gloff.data(), NNZ, st);
     d_gl.alloc(std::max<size_t>(h_gl.size(), 1)); d_gl.upload(h_gl.data(), h_gl.size(), st);
+    d_islot.alloc(h_islot.size()); d_islot.upload(h_islot.data(), h_islot.size(), st);
   }
   d_srows.alloc(nsurf); d_srows.upload(h_srows.data(), nsurf, st);
   {
@@ -2822,6 +2903,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     d_rec32.alloc(NT);
     k_geom<float><<<cdiv(NT, 128), 128, 0, st>>>((int)NT, d_tet.p, P(ND_X), P(ND_Y), P(ND_Z),
         d_tetsoil.p, d_tab[0].p, d_tab[1].p, d_tab[2].p, P(ND_PNODI), d_rec32.p, P(ND_VOLNOD), nullptr);
+    d_rec48.alloc((size_t)3 * NT);
+    k_rec48<<<cdiv(NT, 256), 256, 0, st>>>((int)NT, d_rec32.p, d_rec48.p);
   }
   check_launch();
   if (precision == 1 && iopt == 1) {
@@ -3183,7 +3266,7 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
             cbms.mem.p, cbms.r0.p, cbms.r1.p, d_active.p, d_ms.p, linv, lc, r, p, nmem, d_niter.p);
         count(4);
       } else {
-        k_spmv<MT, VT><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+        k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
             cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
             d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
         k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
@@ -3201,7 +3284,7 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
   }
   if (phase == 2) {
     // one PCG iteration of the graph's WHILE body (see below for the steps)
-    k_spmv<MT, VT><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+    k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
         cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
         d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
     k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
@@ -3242,7 +3325,7 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
   if (chk < 1) chk = 1;
   for (int it = 0; it < itmax + 2; ++it) {
     // q = A p, pq = p.q, pr = p.r
-    k_spmv<MT, VT><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+    k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
         cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
         d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
     count();
@@ -3300,7 +3383,7 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
     }
   };
   auto spmv = [&](const double* in, double* out) {
-    k_spmv<double, double><<<grid_persist(cbm16.nblk), kThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+    k_spmv<double, double><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
         cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out,
         nullptr, nullptr, 0, nullptr, nullptr, 0);
     count();
@@ -3427,8 +3510,8 @@ void Engine::iteration_pre(int solve_phase) {
       count(3);
     }
     k_assemble_picard_f32<<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, d_rec32.p, d_dmask.p,
-        nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
+        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_islot.p, d_rec48.p,
+        d_dmask.p, nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
     count();
     check_launch();
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
@@ -4042,8 +4125,8 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
     k_bcflux_f32<<<e->bms.nblk, kThreads, 0, e->st>>>(e->bms.mem.p, e->bms.r0.p, e->bms.r1.p, e->d_act.p,
         e->d_ms.p, e->nd, e->nf.qneu, e->nf.bcf);
     k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
-        e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_tet.p,
-        e->d_rec32.p, e->d_dmask.p, e->nf, e->nf.bcf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o,
+        e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_islot.p,
+        e->d_rec48.p, e->d_dmask.p, e->nf, e->nf.bcf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o,
         e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
   } else {
     k_vg<double><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->iopt == 2);
