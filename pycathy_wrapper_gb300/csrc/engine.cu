@@ -309,15 +309,10 @@ __global__ void k_geom(int nt, const int4* tet, const double* x, const double* y
 // step actions (per member masks)
 // ============================================================================
 // surface part: BKSTEP restore + COMMIT bookkeeping + ATM update + switching
-__global__ void k_start_surface(const int32_t* bm_mem, const int32_t* bm_r0,
-                                const int32_t* bm_r1, const uint8_t* act,
-                                const MemberScal* ms, Nodal nd) {
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
-  const int m = nd.mem[i];
-  const uint8_t a = act[m];
-  if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START))) return;
-  const MemberScal& S = ms[m];
+// surface part of the step actions for surface node i: BKSTEP restore +
+// COMMIT bookkeeping + ATM update + switching
+__device__ __forceinline__ void start_surface_node(int i, uint8_t a, const MemberScal& S,
+                                                   Nodal& nd) {
   int8_t f = nd.ifatm[i];
   if (a & ACT_COMMIT) {
     nd.ifatmp[i] = f;
@@ -361,30 +356,24 @@ __global__ void k_start_surface(const int32_t* bm_mem, const int32_t* bm_r0,
   nd.ifatm[i] = f;
 }
 
-// all nodes.  phase 0: COMMIT (ptimep <- pnew) and BACKSTEP restore;
-// phase 1 (after the surface kernel): Dirichlet mask, START / NEXT updates.
-__global__ void k_start_nodes(const int32_t* bm_mem, const int32_t* bm_r0,
-                              const int32_t* bm_r1, const uint8_t* act,
-                              const MemberScal* ms, Nodal nd, int phase, int need_sw) {
-  const int m = bm_mem[blockIdx.x];
-  const uint8_t a = act[m];
-  if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START | ACT_NEXT))) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
-  if (phase == 0) {
-    if (a & ACT_COMMIT) {
-      nd.qpold[i] = nd.qpnew[i];
-      nd.ptimep[i] = nd.pnew[i];
-    }
-    if (a & ACT_BACKSTEP) {
-      nd.pnew[i] = nd.ptimep[i];
-      nd.qpnew[i] = nd.qpold[i];
-    }
-    return;
+// node i, phase 0: COMMIT (ptimep <- pnew) and BACKSTEP restore
+__device__ __forceinline__ void start_phase0_node(int i, uint8_t a, Nodal& nd) {
+  if (a & ACT_COMMIT) {
+    nd.qpold[i] = nd.qpnew[i];
+    nd.ptimep[i] = nd.pnew[i];
   }
-  const double th = ms[m].tetaf;
+  if (a & ACT_BACKSTEP) {
+    nd.pnew[i] = nd.ptimep[i];
+    nd.qpnew[i] = nd.qpold[i];
+  }
+}
+
+// node i, phase 1 (after the surface part): Dirichlet mask, START / NEXT
+__device__ __forceinline__ void start_phase1_node(int i, uint8_t a, const MemberScal& S,
+                                                  Nodal& nd, int need_sw) {
+  const double th = S.tetaf;
   const int loc = nd.loc[i];
-  const bool surf = loc < ms[m].nnod;
+  const bool surf = loc < S.nnod;
   if (a & (ACT_START | ACT_BACKSTEP | ACT_COMMIT)) {
     uint8_t dm = nd.sdir[i];
     if (surf) dm |= (nd.ifatm[i] == 1 || nd.ifatm[i] == 2);
@@ -407,6 +396,32 @@ __global__ void k_start_nodes(const int32_t* bm_mem, const int32_t* bm_r0,
     nd.ptold[i] = nd.ptnew[i];
     nd.ptnew[i] = (th == 1.0) ? p : th * p + (1.0 - th) * nd.ptimep[i];
   }
+}
+
+// surface part: BKSTEP restore + COMMIT bookkeeping + ATM update + switching
+__global__ void k_start_surface(const int32_t* bm_mem, const int32_t* bm_r0,
+                                const int32_t* bm_r1, const uint8_t* act,
+                                const MemberScal* ms, Nodal nd) {
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const int m = nd.mem[i];
+  const uint8_t a = act[m];
+  if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START))) return;
+  start_surface_node(i, a, ms[m], nd);
+}
+
+// all nodes.  phase 0: COMMIT (ptimep <- pnew) and BACKSTEP restore;
+// phase 1 (after the surface kernel): Dirichlet mask, START / NEXT updates.
+__global__ void k_start_nodes(const int32_t* bm_mem, const int32_t* bm_r0,
+                              const int32_t* bm_r1, const uint8_t* act,
+                              const MemberScal* ms, Nodal nd, int phase, int need_sw) {
+  const int m = bm_mem[blockIdx.x];
+  const uint8_t a = act[m];
+  if (!(a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START | ACT_NEXT))) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  if (phase == 0) start_phase0_node(i, a, nd);
+  else start_phase1_node(i, a, ms[m], nd, need_sw);
 }
 
 // ============================================================================
@@ -1534,17 +1549,11 @@ __global__ void k_gather_ik(int nmem, const uint8_t* act, const int32_t* node_of
   k_gather_ik_b(blockIdx.x, nmem, act, node_off, ikmax, nd, out);
 }
 
-// SWITCH_OLD after the norms when PINF (or PL2) <= TOLSWI
-__global__ void k_switch(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                         const uint8_t* act, const uint8_t* do_switch, const MemberScal* ms,
-                         Nodal nd) {
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
-  const int m = bm_mem[blockIdx.x];
-  if (!(act[m] & ACT_ITER) || !do_switch[m]) return;
+// SWITCH_OLD after the norms when PINF (or PL2) <= TOLSWI, for surface node i
+__device__ __forceinline__ void switch_node(int i, double pmin, Nodal& nd) {
   int8_t f = nd.ifatm[i];
   if (f == -1) return;
-  const double pot = nd.atmpot[i], pmin = ms[m].pmin;
+  const double pot = nd.atmpot[i];
   double a = nd.atmact[i], p = nd.pnew[i];
   if (f == 1 && p >= 0.0 && (pot < 0.0 || a > pot)) { f = 0; a = pot; }
   else if (f == 1 && p <= pmin && (pot > 0.0 || a < pot)) { f = 0; a = pot; }
@@ -1554,6 +1563,15 @@ __global__ void k_switch(const int32_t* bm_mem, const int32_t* bm_r0, const int3
   nd.atmact[i] = a;
   nd.pnew[i] = p;
   nd.dmask[i] = nd.sdir[i] | (uint8_t)(f == 1 || f == 2);
+}
+__global__ void k_switch(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                         const uint8_t* act, const uint8_t* do_switch, const MemberScal* ms,
+                         Nodal nd) {
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER) || !do_switch[m]) return;
+  switch_node(i, ms[m].pmin, nd);
 }
 
 // STORE1 = sum Sw(PNEW) * VOLNOD * PNODI (storcal.f) for members in mask
@@ -1622,13 +1640,8 @@ __device__ __forceinline__ float vgf_dse(double psi1, double psi0, float psat,
   return se0 * expm1f(-m * log1pf(db / (1.0f + b0)));
 }
 
-__global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
-                         const int32_t* bm_r1, const uint8_t* act, Nodal nd,
-                         NodalF nf, const double* z) {
-  const int m = bm_mem[blockIdx.x];
-  if (!(act[m] & ACT_ITER)) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
+// FP32 soil characteristics of node i (see the FP32 block comment).
+__device__ __forceinline__ void vg_f32_node(int i, const Nodal& nd, NodalF& nf, const double* z) {
   const float psat = nf.vgpsat[i], n = nf.vgn[i], mm = nf.vgm[i], pnot = nf.vgpnot[i];
   const float rmcp = nf.rmcp[i];
   const double p = nd.pnew[i], pt = nd.ptnew[i], pn = nd.ptimep[i];
@@ -1658,6 +1671,37 @@ __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
   nf.hhi[i] = hh;
   nf.hlo[i] = hl;
   nf.h2[i] = make_float2(hh, hl);
+}
+
+__global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                         const int32_t* bm_r1, const uint8_t* act, Nodal nd,
+                         NodalF nf, const double* z) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  vg_f32_node(i, nd, nf, z);
+}
+
+// Step actions of every node (phase 0, the surface part for surface nodes,
+// phase 1) and the FP32 soil characteristics of iterating members, in one
+// pass: each of these reads and writes only its own node.
+__global__ void k_start_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                               const int32_t* bm_r1, const uint8_t* act,
+                               const MemberScal* ms, Nodal nd, NodalF nf, const double* z,
+                               int need_sw) {
+  const int m = bm_mem[blockIdx.x];
+  const uint8_t a = act[m];
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const MemberScal& S = ms[m];
+  if (a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START | ACT_NEXT)) {
+    start_phase0_node(i, a, nd);
+    if ((a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START)) && nd.loc[i] < S.nnod)
+      start_surface_node(i, a, S, nd);
+    start_phase1_node(i, a, S, nd, need_sw);
+  }
+  if (a & ACT_ITER) vg_f32_node(i, nd, nf, z);
 }
 
 // Element means of kr and Sw*Ss (NODELT) for the FP32 assembly.
@@ -1926,7 +1970,7 @@ __global__ void k_bkflux_list_f32(int nrows, const int32_t* rows, const uint8_t*
 // MASBAL sums (STORMB, FLUXMB), RELAX and NORMS for the FP32 path, one thread
 // per row; compensated FP32 block sums.
 __global__ void __launch_bounds__(kThreads)
-k_masbal_norms_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+k_masbal_norms_f32(int do_shl, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
                    const uint8_t* act, const MemberScal* ms, Nodal nd, NodalF nf,
                    const float* volnod_f, const float* pnodi_f, double* red,
                    double* redmax) {
@@ -1937,6 +1981,13 @@ k_masbal_norms_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* b
   FF v[RD_PL2];
   for (int q = 0; q < RD_PL2; ++q) v[q] = FF{0.0f, 0.0f};
   float pl2 = 0.0f, fl2 = 0.0f, pinf = 0.0f, finf = 0.0f;
+  if (do_shl && i < bm_r1[blockIdx.x]) {
+    // PNEW += PDIFF + SHLPIC (the head update of the graph path)
+    double p = nd.pnew[i] + (double)nf.pdiff[i];
+    if (nd.sdir[i]) p = nd.presc[i];
+    else if (nd.dmask[i]) p = nd.pold[i];
+    nd.pnew[i] = p;
+  }
   if (i < bm_r1[blockIdx.x]) {
     const bool surf = nd.loc[i] < S.nnod;
     const int8_t f = surf ? nd.ifatm[i] : (int8_t)-1;
@@ -2201,6 +2252,60 @@ __global__ void k_member_post(int nmem, const uint8_t* act, const int32_t* node_
                               uint8_t* sw) {
   k_gather_ik_b(blockIdx.x, nmem, act, node_off, ikmax, nd, ikval);
   k_switch_flags_b(blockIdx.x, nmem, act, red, redmax, ms, l2norm, sw);
+}
+
+// IKMAX of every iterating member, then (last block to finish) PNEW/POLD at
+// IKMAX and whether SWITCH_OLD runs, per member.
+__global__ void k_ikmax_post(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                             const uint8_t* act, Nodal nd, const double* redmax, int32_t* ikmax,
+                             int nmem, const int32_t* node_off, double* ikval, const double* red,
+                             const MemberScal* ms, int l2norm, uint8_t* sw, unsigned int* done) {
+  const int m = bm_mem[blockIdx.x];
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if ((act[m] & ACT_ITER) && i < bm_r1[blockIdx.x]) {
+    if (fabsf((float)(nd.pnew[i] - nd.pold[i])) == (float)redmax[(size_t)m * 2])
+      atomicMax(ikmax + m, nd.loc[i]);
+  }
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int q = threadIdx.x; q < nmem; q += blockDim.x) {
+    const bool it = (act[q] & ACT_ITER) != 0;
+    if (it) {
+      const int j = node_off[q] + max(ikmax[q], 0);
+      ikval[2 * q] = nd.pnew[j];
+      ikval[2 * q + 1] = nd.pold[j];
+    }
+    const double pinf = redmax[2 * q], pl2 = sqrt(red[(size_t)q * RD_NUM + RD_PL2]);
+    sw[q] = it && ((l2norm == 0 && pinf <= ms[q].tolswi) || (l2norm != 0 && pl2 <= ms[q].tolswi));
+  }
+  if (threadIdx.x == 0) *done = 0u;
+}
+
+// SWITCH_OLD on the surface nodes of the members that switch, then STORE1
+// (storcal.f) of every iterating member at the final heads.
+__global__ void k_switch_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                                    const int32_t* bm_r1, const uint8_t* act, const uint8_t* sw,
+                                    const MemberScal* ms, Nodal nd, NodalF nf, double* red) {
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  FF v[1] = {FF{0.0f, 0.0f}};
+  if (i < bm_r1[blockIdx.x]) {
+    if (sw[m] && nd.loc[i] < ms[m].nnod) switch_node(i, ms[m].pmin, nd);
+    const double p = nd.pnew[i];
+    float se = 1.0f;
+    if (p < -1.0e-14) se = expf(-nf.vgm[i] * log1pf(vgf_beta((float)p, nf.vgpsat[i], nf.vgn[i])));
+    const float swv = nf.vgpnot[i] * se + nf.rmcp[i];
+    v[0].hi = swv * nf.volnod[i] * nf.pnodi[i];
+  }
+  block_accumulate_ff<1>(v, red + (size_t)m * RD_NUM + RD_STORE1);
 }
 
 // STORE1 of every member whose action bits include ACT_ITER
@@ -3492,8 +3597,14 @@ void Engine::iteration_pre(int solve_phase) {
     // FP32 path: the Picard loop is the FP64 refinement loop (its residual is
     // FP64-grade, see the FP32 kernels); the inner FP32 PCG solves each
     // correction to opts.inner_tol.
-    k_vg_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd, nf,
-                                            d_nodal[ND_Z].p);
+    if (solve_phase == 1) {
+      // graph: step actions + soil characteristics in one pass
+      k_start_vg_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
+          d_ms.p, nd, nf, d_nodal[ND_Z].p, need_sw_flag());
+    } else {
+      k_vg_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd, nf,
+                                              d_nodal[ND_Z].p);
+    }
     count();
     if (solve_phase == 1) {
       // graph: element means | BC fluxes | Krylov flags in one launch
@@ -3534,23 +3645,19 @@ void Engine::iteration_post(bool graph) {
   const bool mixed = (precision == 1 && iopt == 1);
   const cathy_parm_t& P0 = M[0]->parm;
   if (graph && mixed) {
-    // graph path: the result buffer was zeroed at the start of the graph
-    k_update_shl_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
-                                                    nf.pdiff);
+    // graph path (the result buffer was zeroed at the start of the graph):
+    // back-fluxes | head update + mass balance + norms | IKMAX + per-member
+    // records and switch flags; switching and STORE1 follow in the graph
     const int nb = cbms16.nblk + cdiv((long)ndeep * kGroup, kThreads);
     if (nb)
       k_bkflux_all_f32<<<nb, kThreads, 0, st>>>(cbms16.nblk, cbms16.mem.p, cbms16.r0.p,
           cbms16.r1.p, ndeep, d_deep.p, d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
-    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
+    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(1, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
         d_ms.p, nd, nf, nf.volnod, nf.pnodi, d_red.p, d_redmax.p);
-    k_ikmax<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
-                                           d_redmax.p, d_ikmax.p, 1);
-    k_member_post<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_node_off.p, d_ikmax.p, nd,
-        d_ikval.p, d_red.p, d_redmax.p, d_ms.p, P0.l2norm, d_switch.p);
-    if (cbms.nblk)
-      k_switch<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p,
-                                               d_switch.p, d_ms.p, nd);
-    count(6);
+    k_ikmax_post<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
+        d_redmax.p, d_ikmax.p, nmem, d_node_off.p, d_ikval.p, d_red.p, d_ms.p, P0.l2norm,
+        d_switch.p, d_done.p + 1);
+    count(3);
     check_launch();
     return;
   }
@@ -3570,7 +3677,7 @@ void Engine::iteration_post(bool graph) {
     if (ndeep)
       k_bkflux_list_f32<<<cdiv((long)ndeep * kGroup, kThreads), kThreads, 0, st>>>(ndeep, d_deep.p,
           d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
-    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
+    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(0, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
         d_ms.p, nd, nf, nf.volnod, nf.pnodi, d_red.p, d_redmax.p);
     count();
   } else
@@ -3637,7 +3744,7 @@ void Engine::pinned_alloc() {
   hp_ikmax = reinterpret_cast<int32_t*>(hp_res + res_off[4]);
   hp_ikv = hp_res + res_off[5];
   hp_nit = reinterpret_cast<int32_t*>(hp_res + res_off[6]);
-  d_done.alloc(1);
+  d_done.alloc(2);
   d_done.zero(st);
 }
 
@@ -3661,7 +3768,6 @@ void Engine::graph_build() {
   CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   CG_TRY(cudaMemcpyAsync(d_inbuf.p, hp_in, d_inbuf.n, cudaMemcpyHostToDevice, st));
   CG_TRY(cudaMemsetAsync(d_resbuf.p, 0, sizeof(double) * res_zero, st));
-  start_kernels();
   iteration_pre(1);
   cudaGraph_t gA = nullptr;
   CG_TRY(cudaStreamEndCapture(st, &gA));
@@ -3690,8 +3796,8 @@ void Engine::graph_build() {
   c0 = launches;
   CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   iteration_post(true);
-  k_store1_iter_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
-                                                    nf, d_red.p);
+  k_switch_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
+                                                      d_switch.p, d_ms.p, nd, nf, d_red.p);
   count();
   CG_TRY(cudaMemcpyAsync(hp_res, d_resbuf.p, sizeof(double) * res_off[7], cudaMemcpyDeviceToHost, st));
   cudaGraph_t gC = nullptr;
