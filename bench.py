@@ -24,7 +24,7 @@ the whole ensemble day from the initial condition.
             bandwidth.
   cpu_baseline  the CPU oracle (serial C++ restatement of the reference
             Fortran) on a bounded sample: the first 16 members for their first
-            2 simulated hours, one process per host core.
+            30 simulated minutes, one process per host core.
 
 --impl reference runs the CPU restatement of the reference's solver on the
 host cores (the Fortran reference cannot be built: no Fortran compiler) on a
@@ -233,7 +233,7 @@ def main():
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--tmax", type=float, default=86400.0)
     ap.add_argument("--cpu-members", type=int, default=16)
-    ap.add_argument("--cpu-tmax", type=float, default=7200.0,
+    ap.add_argument("--cpu-tmax", type=float, default=1800.0,
                     help="simulated seconds per member in the bounded CPU sample")
     ap.add_argument("--plain-members", type=int, default=4)
     ap.add_argument("--no-graphs", action="store_true")

@@ -261,6 +261,21 @@ int32_t cathy_gb300_lp_eval(void* model, int32_t n, int32_t nnod,
                             int32_t train_steps, double* loss, float* dprime,
                             float* omega, float* grads);
 
+/* Attach a model to a handle (FP32 Picard path with the column-line
+ * preconditioner, parm.precond = 2).  mode 1: train -- every Picard solve
+ * stays plain, its first four Krylov pairs (p, q = A p) and matrices feed one
+ * Adam step; mode 2: use -- members solve with the learned factor, every 8th
+ * Picard iteration of a member is a plain probe, and a member keeps the
+ * learned factor only while its mean PCG iteration count is not above the
+ * plain one (plain column-line is the fallback; a column whose learned
+ * pivots are not all positive also keeps the plain factor).  mode 0 or
+ * model NULL detaches.  Kernel-by-kernel launches are used while a model is
+ * attached. */
+int32_t cathy_gb300_attach_learned(void* handle, void* model, int32_t mode);
+/* out[0..n), n <= 6: learned solves, their PCG iterations, plain solves,
+ * their PCG iterations (mode 2), training steps and last loss (mode 1) */
+int32_t cathy_gb300_learned_stats(void* handle, double* out, int32_t n);
+
 /* ---- allocation-free solve ----------------------------------------------- */
 /* No counterpart in the reference: an extra entry point of this library for
  * callers that may not allocate device memory while they run (a driver whose

@@ -129,6 +129,8 @@ EXPORTS = {
     "cathy_gb300_lp_eval": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, i32p, i32p, f32p,
                                         u8p, f32p, f32p, f32p, C.c_float, C.c_int32, f32p,
                                         f32p, C.c_int32, f64p, f32p, f32p, f32p]),
+    "cathy_gb300_attach_learned": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "cathy_gb300_learned_stats": (C.c_int32, [C.c_void_p, f64p, C.c_int32]),
     "cathy_gb300_nsyslv_noalloc": (C.c_int32, [i32p, i32p, C.c_void_p, i32p, i32p,
                                                C.c_void_p, C.c_void_p, f64p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, f64p, f64p,

@@ -194,6 +194,19 @@ class Simulation:
               "cathy_gb300_profile")
         return ms.value, n.value, bts.value
 
+    def attach_learned(self, model, mode: int = 2):
+        """Attach a :class:`~pycathy_wrapper_gb300.learned.LearnedPreconditioner`
+        (mode 1 train on the plain solves, 2 use with plain fallback, 0 detach)."""
+        h = model.handle if model is not None else None
+        check(self.L.cathy_gb300_attach_learned(self.h, h, int(mode)), "attach_learned")
+        self._lp = model
+
+    def learned_stats(self):
+        out = (C.c_double * 6)()
+        check(self.L.cathy_gb300_learned_stats(self.h, out, 6), "learned_stats")
+        return dict(learned_solves=out[0], learned_iters=out[1], plain_solves=out[2],
+                    plain_iters=out[3], train_steps=out[4], last_loss=out[5])
+
     def timers(self):
         """Host-side phase timers of the time stepping."""
         out = (C.c_double * 72)()

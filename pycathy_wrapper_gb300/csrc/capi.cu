@@ -141,6 +141,16 @@ int32_t cathy_gb300_stats(void* h, double* gpu_ms, int64_t* launches,
   return engine_stats((Engine*)h, gpu_ms, launches, lin_iters, nl_iters);
 }
 
+int32_t cathy_gb300_attach_learned(void* h, void* model, int32_t mode) {
+  if (!h || mode < 0 || mode > 2) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_attach_learned((Engine*)h, model, mode); });
+}
+
+int32_t cathy_gb300_learned_stats(void* h, double* out, int32_t n) {
+  if (!h || !out || n < 0) return CATHY_GB300_EINVAL;
+  return engine_learned_stats((Engine*)h, out, n);
+}
+
 int32_t cathy_gb300_timers(void* h, double* out, int32_t n) {
   if (!h || !out || n < 0) return CATHY_GB300_EINVAL;
   return engine_timers((Engine*)h, out, n);

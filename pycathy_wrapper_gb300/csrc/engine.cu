@@ -34,6 +34,7 @@
 
 #include "engine.h"
 #include "kernels.cuh"
+#include "learned.h"
 
 namespace cathy {
 
@@ -783,6 +784,115 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
   }
 }
 
+// FP32 y = A x as a stream over each map entry's slots: one warp per entry
+// (16 consecutive rows of one member, their slots contiguous in vals/cols),
+// the lanes read the entry's values and columns with 16-byte vector loads,
+// form the products with gathered x, stage them in shared memory, and lane r
+// adds row r's products.  All of an entry's loads are independent, so a warp
+// keeps 16 rows in flight.  Dirichlet rows are the identity; per-member dot
+// products d0 += x.y, d1 += x.w accumulate per warp and are flushed with one
+// FP64 atomic per quantity whenever the warp's member changes.  Timing and
+// byte accounting as in k_spmv.
+constexpr int kStreamWarps = 4;
+__global__ void __launch_bounds__(32 * kStreamWarps)
+k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+              const uint8_t* active, const int32_t* __restrict__ rowptr,
+              const int32_t* __restrict__ cols, const float* __restrict__ vals,
+              const uint8_t* __restrict__ dmask, const float* __restrict__ x, float* y,
+              const float* __restrict__ w, double* acc, int acc_stride, double* alg_bytes,
+              unsigned long long* lt, int lt_cap) {
+  __shared__ int s_slot;
+  __shared__ float sprod[kStreamWarps][16 * kGroup + 8];
+  if (lt) {
+    if (threadIdx.x == 0) {
+      const unsigned long long q = lt[LT_SEQ];
+      s_slot = q < (unsigned long long)lt_cap ? (int)q : -1;
+      if (s_slot >= 0) atomicMin(&lt[LT_HDR + 2 * s_slot], (unsigned long long)gtimer());
+    }
+    __syncthreads();
+    if (s_slot < 0) lt = nullptr;
+  }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  float* sp = sprod[wp];
+  float d0 = 0.0f, d1 = 0.0f;
+  int cur = -1;
+  double bytes = 0.0;
+  // each block takes a contiguous run of entries; its warps interleave
+  const int chunk = (nblk + gridDim.x - 1) / gridDim.x;
+  const int b0 = blockIdx.x * chunk, b1 = min(nblk, b0 + chunk);
+  for (int b = b0 + wp; b < b1; b += kStreamWarps) {
+    const int m = bm_mem[b];
+    if (!active[m]) continue;  // warp-uniform
+    if (acc && m != cur) {
+      if (cur >= 0) {
+        const float a0 = warp_sum_t<float>(d0), a1 = warp_sum_t<float>(d1);
+        if (lane == 0) {
+          if (a0 != 0.0f) atomicAdd(acc + (size_t)cur * acc_stride, (double)a0);
+          if (a1 != 0.0f) atomicAdd(acc + (size_t)cur * acc_stride + 1, (double)a1);
+        }
+      }
+      d0 = d1 = 0.0f;
+      cur = m;
+    }
+    const int r0 = bm_r0[b], r1 = bm_r1[b], nr = r1 - r0;
+    // row pointers of the entry (lanes 0..nr)
+    const int rp = lane <= nr ? rowptr[r0 + lane] : 0;
+    const int sbeg = __shfl_sync(0xffffffffu, rp, 0);
+    const int send = __shfl_sync(0xffffffffu, rp, nr);
+    if (alg_bytes && lane == 0)
+      bytes += (double)(send - sbeg) * 8.0 + nr * (4.0 + (w ? 3.0 : 2.0) * 4.0);
+    // 16-byte vectors covering [sbeg, send)
+    const int v0 = sbeg >> 2, v1 = (send + 3) >> 2;
+    for (int v = v0 + lane; v < v1; v += 32) {
+      const float4 va = reinterpret_cast<const float4*>(vals)[v];
+      const int4 ca = reinterpret_cast<const int4*>(cols)[v];
+      const int k0 = 4 * v;
+      const float vv[4] = {va.x, va.y, va.z, va.w};
+      const int cc[4] = {ca.x, ca.y, ca.z, ca.w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int k = k0 + t;
+        if (k >= sbeg && k < send) sp[k - sbeg] = vv[t] * x[cc[t]];
+      }
+    }
+    __syncwarp();
+    const int rlo = __shfl_down_sync(0xffffffffu, rp, 0);
+    const int rhi = __shfl_down_sync(0xffffffffu, rp, 1);
+    if (lane < nr) {
+      float sum = 0.0f;
+      for (int k = rlo; k < rhi; ++k) sum += sp[k - sbeg];
+      const int i = r0 + lane;
+      const float xi = x[i];
+      const float yi = dmask[i] ? xi : sum;
+      y[i] = yi;
+      d0 += xi * yi;
+      if (w) d1 += xi * w[i];
+    }
+    __syncwarp();
+  }
+  if (acc && cur >= 0) {
+    const float a0 = warp_sum_t<float>(d0), a1 = warp_sum_t<float>(d1);
+    if (lane == 0) {
+      if (a0 != 0.0f) atomicAdd(acc + (size_t)cur * acc_stride, (double)a0);
+      if (a1 != 0.0f) atomicAdd(acc + (size_t)cur * acc_stride + 1, (double)a1);
+    }
+  }
+  if (alg_bytes && lane == 0 && bytes != 0.0) atomicAdd(alg_bytes, bytes);
+  if (lt) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicMax(&lt[LT_HDR + 2 * s_slot + 1], (unsigned long long)gtimer());
+      const unsigned long long done = atomicAdd(&lt[LT_DONE], 1ull);
+      if (done == gridDim.x - 1) {
+        lt[LT_DONE] = 0;
+        __threadfence();
+        lt[LT_SEQ] = (unsigned long long)(s_slot + 1);
+      }
+    }
+  }
+}
+
 // r = b - A x (masked), r zero at Dirichlet rows
 template <class MT, class VT>
 __global__ void __launch_bounds__(kThreads)
@@ -884,6 +994,55 @@ __device__ __forceinline__ void k_line_setup_b(int bid_, const int32_t* bm_mem, 
     }
   }
 }
+// Column-line factor on the learned diagonal d' (members flagged in use):
+// overwrites the plain factor of those columns; a column whose pivots are
+// not all positive keeps the plain factor (the fallback).
+__global__ void k_line_setup_learned(const int32_t* bm_mem, const int32_t* bm_r0,
+                                     const int32_t* bm_r1, const uint8_t* active,
+                                     const uint8_t* use, const MemberScal* ms,
+                                     const int32_t* __restrict__ down, const float* __restrict__ vals,
+                                     const uint8_t* __restrict__ dmask,
+                                     const float* __restrict__ dl, float* __restrict__ pinv) {
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m] || !use[m]) return;
+  const int top = bm_r0[blockIdx.x] + threadIdx.x;
+  if (top >= bm_r1[blockIdx.x]) return;
+  const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
+  double piv_prev = 1.0, c_prev = 0.0;
+  bool ok = true;
+  for (int k = 0; k < nl && ok; ++k) {
+    const int i = top + k * nnod;
+    const bool di = dmask[i] != 0;
+    const double a = di ? 1.0 : (double)dl[i];
+    double c = 0.0;
+    if (k + 1 < nl && !di && !dmask[i + nnod] && down[i] >= 0) c = (double)vals[down[i]];
+    const double piv = a - c_prev * c_prev / piv_prev;
+    ok = piv > 0.0 && isfinite(piv);
+    piv_prev = piv;
+    c_prev = c;
+  }
+  if (!ok) return;
+  piv_prev = 1.0;
+  c_prev = 0.0;
+  for (int k = 0; k < nl; ++k) {
+    const int i = top + k * nnod;
+    const bool di = dmask[i] != 0;
+    const double a = di ? 1.0 : (double)dl[i];
+    double c = 0.0;
+    if (k + 1 < nl && !di && !dmask[i + nnod] && down[i] >= 0) c = (double)vals[down[i]];
+    const double piv = a - c_prev * c_prev / piv_prev;
+    pinv[i] = (float)(1.0 / piv);
+    piv_prev = piv;
+    c_prev = c;
+  }
+}
+
+// per-member time step in FP32 (input of the learned preconditioner)
+__global__ void k_member_dt(int nmem, const MemberScal* ms, float* dtf) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < nmem) dtf[m] = (float)ms[m].deltat;
+}
+
 template <class MT, class VT>
 __global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* active,
@@ -2347,6 +2506,7 @@ struct MemberHost {
   double red_last[RD_NUM];
   bool lsfail = false;
   bool paused = false;
+  int lp_fwd_step = -1;  // time step of the last learned-network evaluation
   int steps_done = 0;
   std::vector<cathy_iter_rec_t> iter_recs;
   std::vector<cathy_step_rec_t> step_recs;
@@ -2425,6 +2585,7 @@ struct Engine {
 
   ~Engine() {
     graph_free();
+    lp_work_free(lpw);
     if (gev0) cudaEventDestroy(gev0);
     if (gev1) cudaEventDestroy(gev1);
     pinned_free();
@@ -2494,9 +2655,35 @@ struct Engine {
   }
   int grid_persist(int nblk) const { return std::max(1, std::min(nblk, persist_blocks)); }
   int grid_spmv(int nblk) const { return std::max(1, std::min(nblk, 2 * persist_blocks)); }
+  // q = A p with the fused dots p.q, p.r (FP32 stream kernel)
+  void spmv_f32(const float* vals, const float* p, float* q, const float* r) {
+    const int g = std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps,
+                                       2 * persist_blocks));
+    k_spmv_stream<<<g, 32 * kStreamWarps, 0, st>>>(cbm16.nblk, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+        d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N,
+        prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+  }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
   void iteration_pre(int solve_phase);
+  // learned column-line preconditioner (mode 1: train on the plain solver's
+  // Krylov pairs; mode 2: use, with plain column-line as the fallback)
+  LpModel* lpm = nullptr;
+  int lp_mode = 0;
+  LpWork lpw;
+  DBuf<float> d_ksn, d_dtf, d_P, d_Q;
+  DBuf<uint8_t> d_lpact, d_lpuse, d_lpfwd, d_lpapp;
+  DBuf<int32_t> d_nnodm, d_ctop, d_cstr, d_cnl, d_cmem;
+  int lp_ncol = 0;
+  std::vector<float> h_ksn;
+  std::vector<uint8_t> lp_use_now;       // member used the learned factor this iteration
+  std::vector<double> lp_sum_l, lp_sum_p;
+  std::vector<int64_t> lp_n_l, lp_n_p, lp_k;
+  int64_t lp_train_calls = 0;
+  void lp_attach(LpModel* model, int mode);
+  LpGraph lp_graph(const uint8_t* active);
+  void lp_before_solve();
+  void lp_after_solve();
   void iteration_post(bool graph = false);
   void start_kernels();
   // CUDA graph of one macro-iteration (FP32 Picard path)
@@ -2523,7 +2710,9 @@ struct Engine {
   MemberScal* hp_ms = nullptr;
   double *hp_red = nullptr, *hp_redmax = nullptr, *hp_ikv = nullptr, *hp_sc = nullptr;
   int32_t *hp_ikmax = nullptr, *hp_nit = nullptr, *hp_loops = nullptr;
-  bool graphs_on() const { return opts.graphs != 0 && precision == 1 && iopt == 1; }
+  bool graphs_on() const {
+    return opts.graphs != 0 && precision == 1 && iopt == 1 && lp_mode == 0;
+  }
   void graph_free();
   void graph_build();
   void pinned_alloc();
@@ -2928,7 +3117,9 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_ifatmp.alloc(N); d_ifatmp.upload(h_ifatmp.data(), N, st);
   d_tet.alloc(NT); d_tet.upload(h_tet.data(), NT, st);
   d_rowptr.alloc(N + 1); d_rowptr.upload(h_rowptr.data(), N + 1, st);
-  d_cols.alloc(NNZ); d_cols.upload(h_cols.data(), NNZ, st);
+  // columns and FP32 values are padded by 4 so that 16-byte vector reads of
+  // the last slots stay inside the allocation
+  d_cols.alloc(NNZ + 4); d_cols.zero(st); d_cols.upload(h_cols.data(), NNZ, st);
   d_diag.alloc(N); d_diag.upload(h_diag.data(), N, st);
   d_down.alloc(N); d_down.upload(h_down.data(), N, st);
   d_tslot.alloc(NNZ); d_tslot.upload(h_tslot.data(), NNZ, st);
@@ -2974,6 +3165,15 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     };
     batch_levels(true, lev_f_ptr, d_lev_f);
     batch_levels(false, lev_b_ptr, d_lev_b);
+  }
+  // nodal saturated conductivity (mean PERMZ of the incident elements), an
+  // input of the learned preconditioner
+  h_ksn.assign(N, 0.0f);
+  for (int i = 0; i < N; ++i) {
+    double ks = 0.0;
+    const int p0 = h_incptr[i], p1 = h_incptr[i + 1];
+    for (int q = p0; q < p1; ++q) ks += tabs[2][h_tetsoil[h_inc[q] >> 2]];
+    h_ksn[i] = (float)(p1 > p0 ? ks / (p1 - p0) : 0.0);
   }
   // soil tables
   DBuf<double> d_tab[8];
@@ -3026,7 +3226,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   }
   // matrix and solver workspace
   if (precision == 0) { d_vals64.alloc(NNZ); d_vals64.zero(st); }
-  else { d_vals32.alloc(NNZ); d_vals32.zero(st); d_vals64.alloc(0); }
+  else { d_vals32.alloc(NNZ + 4); d_vals32.zero(st); d_vals64.alloc(0); }
   const int nw = 14;
   if (precision == 0 || iopt == 2) for (int k = 0; k < nw; ++k) { w64[k].alloc(N); w64[k].zero(st); }
   else for (int k = 0; k < 4; ++k) { w64[k].alloc(N); w64[k].zero(st); }
@@ -3319,6 +3519,14 @@ static void precond_setup(Engine& E, int pc, const MT* vals, FT* F, VT* dinv,
       k_line_setup<MT, VT><<<E.cbms.nblk, kThreads, 0, st>>>(E.cbms.mem.p, E.cbms.r0.p, E.cbms.r1.p,
           E.d_active.p, E.d_ms.p, E.d_diag.p, E.d_down.p, vals, E.d_dmask.p, linv, lc);
     E.count();
+    if constexpr (sizeof(MT) == 4 && sizeof(VT) == 4) {
+      if (E.lp_mode == 2 && E.cbms.nblk) {
+        k_line_setup_learned<<<E.cbms.nblk, kThreads, 0, st>>>(E.cbms.mem.p, E.cbms.r0.p,
+            E.cbms.r1.p, E.d_active.p, E.d_lpuse.p, E.d_ms.p, E.d_down.p, (const float*)vals,
+            E.d_dmask.p, E.lpw.dprime, (float*)linv);
+        E.count();
+      }
+    }
   } else {
     for (size_t l = 0; l + 1 < E.lev_f_ptr.size(); ++l) {
       const int nr = E.lev_f_ptr[l + 1] - E.lev_f_ptr[l];
@@ -3371,9 +3579,7 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
             cbms.mem.p, cbms.r0.p, cbms.r1.p, d_active.p, d_ms.p, linv, lc, r, p, nmem, d_niter.p);
         count(4);
       } else {
-        k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
-            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
-            d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+        spmv_f32(vals, p, q, r);
         k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
             d_active.p, d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
         k_line_apply<VT><<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
@@ -3389,9 +3595,11 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
   }
   if (phase == 2) {
     // one PCG iteration of the graph's WHILE body (see below for the steps)
-    k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
-        cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
-        d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+    if constexpr (sizeof(MT) == 4 && sizeof(VT) == 4) spmv_f32(vals, p, q, r);
+    else
+      k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+          cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
+          d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
     k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
         d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
     count(2);
@@ -3430,11 +3638,23 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
   if (chk < 1) chk = 1;
   for (int it = 0; it < itmax + 2; ++it) {
     // q = A p, pq = p.q, pr = p.r
-    k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
-        cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
-        d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+    if constexpr (sizeof(MT) == 4 && sizeof(VT) == 4) spmv_f32(vals, p, q, r);
+    else
+      k_spmv<MT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+          cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
+          d_sc.p + SC_PQ, SC_N, prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
     count();
     if (prof) lt_pending++;
+    if constexpr (sizeof(VT) == 4) {
+      if (lp_mode == 1 && it < kLpPairs) {
+        // Krylov pair (p, q = A p) of this iteration for the learned model
+        k_copy_cast<VT, float><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+            d_active.p, p, d_P.p + (size_t)it * N, nullptr, 0);
+        k_copy_cast<VT, float><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+            d_active.p, q, d_Q.p + (size_t)it * N, nullptr, 0);
+        count(2);
+      }
+    }
     k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p,
         d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
     count();
@@ -3625,9 +3845,11 @@ void Engine::iteration_pre(int solve_phase) {
         d_dmask.p, nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
     count();
     check_launch();
+    if (lp_mode && solve_phase == 0) lp_before_solve();
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
                             std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1,
                             solve_phase);
+    if (lp_mode == 1 && solve_phase == 0) lp_after_solve();
   } else {
     k_vg<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd,
                                                 iopt == 2);
@@ -3711,6 +3933,111 @@ void Engine::start_kernels() {
     k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 1, need_sw_flag());
   count(3);
   check_launch();
+}
+
+// ---- learned column-line preconditioner in the solver --------------------
+void Engine::lp_attach(LpModel* model, int mode) {
+  if (mode != 0 && !(precision == 1 && iopt == 1 && precond == 2))
+    throw std::string("the learned preconditioner needs the FP32 Picard path with the column-line preconditioner");
+  lpm = model;
+  lp_mode = model ? mode : 0;
+  if (!lp_mode) return;
+  graph_free();
+  lp_work_alloc(lpw, N, NNZ, nmem, lp_mode == 1);
+  d_ksn.alloc(N); d_ksn.upload(h_ksn.data(), N, st);
+  d_dtf.alloc(nmem);
+  d_lpact.alloc(nmem); d_lpuse.alloc(nmem); d_lpfwd.alloc(nmem); d_lpapp.alloc(nmem);
+  d_lpuse.zero(st);
+  if (lp_mode == 1) {
+    d_P.alloc((size_t)kLpPairs * N);
+    d_Q.alloc((size_t)kLpPairs * N);
+  }
+  std::vector<int32_t> nn(nmem), top, str, nl, cm;
+  for (int m = 0; m < nmem; ++m) {
+    const HostMesh& g = *M[m]->meshp;
+    nn[m] = g.nnod;
+    for (int c = 0; c < g.nnod; ++c) {
+      top.push_back(node_off[m] + c);
+      str.push_back(g.nnod);
+      nl.push_back(g.nstr + 1);
+      cm.push_back(m);
+    }
+  }
+  lp_ncol = (int)top.size();
+  d_nnodm.alloc(nmem); d_nnodm.upload(nn.data(), nmem, st);
+  d_ctop.alloc(lp_ncol); d_ctop.upload(top.data(), lp_ncol, st);
+  d_cstr.alloc(lp_ncol); d_cstr.upload(str.data(), lp_ncol, st);
+  d_cnl.alloc(lp_ncol); d_cnl.upload(nl.data(), lp_ncol, st);
+  d_cmem.alloc(lp_ncol); d_cmem.upload(cm.data(), lp_ncol, st);
+  lp_use_now.assign(nmem, 0);
+  lp_sum_l.assign(nmem, 0.0); lp_sum_p.assign(nmem, 0.0);
+  lp_n_l.assign(nmem, 0); lp_n_p.assign(nmem, 0); lp_k.assign(nmem, 0);
+  CG_TRY(cudaStreamSynchronize(st));
+}
+
+LpGraph Engine::lp_graph(const uint8_t* active) {
+  return LpGraph{N, d_rowptr.p, d_cols.p, d_vals32.p, d_diag.p, d_dmask.p, d_mem.p, d_nnodm.p,
+                 d_ksn.p, nf.pnodi, nf.et2, d_dtf.p, active};
+}
+
+// Mode 1: clear the Krylov pair buffers.  Mode 2: choose, per iterating
+// member, the learned or the plain column-line factor for this solve --
+// every 8th Picard iteration of a member is a plain probe, and the member
+// keeps the learned factor only while its mean PCG iteration count is not
+// above the plain one -- and evaluate the network (at the first learned
+// iteration of a time step; later iterations reuse the per-edge weights on
+// the current matrix).
+void Engine::lp_before_solve() {
+  k_member_dt<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_ms.p, d_dtf.p);
+  count();
+  if (lp_mode == 1) {
+    CG_TRY(cudaMemsetAsync(d_P.p, 0, sizeof(float) * d_P.n, st));
+    CG_TRY(cudaMemsetAsync(d_Q.p, 0, sizeof(float) * d_Q.n, st));
+    k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_lpact.p);
+    count();
+    return;
+  }
+  std::vector<uint8_t> fwd(nmem, 0), app(nmem, 0), use(nmem, 0);
+  bool anyf = false, anya = false;
+  for (int m = 0; m < nmem; ++m) {
+    if (!(h_act[m] & ACT_ITER)) continue;
+    const bool probe = (lp_k[m] % 8) == 7;
+    const bool better = lp_n_l[m] == 0 || lp_n_p[m] == 0 ||
+                        lp_sum_l[m] / lp_n_l[m] <= lp_sum_p[m] / lp_n_p[m];
+    lp_k[m]++;
+    use[m] = (!probe && better) ? 1 : 0;
+    if (!use[m]) continue;
+    if ((h_act[m] & ACT_START) || M[m]->lp_fwd_step != M[m]->nstep) {
+      fwd[m] = 1;
+      anyf = true;
+      M[m]->lp_fwd_step = M[m]->nstep;
+    } else {
+      app[m] = 1;
+      anya = true;
+    }
+  }
+  lp_use_now = use;
+  d_lpuse.upload(use.data(), nmem, st);
+  if (anyf) {
+    d_lpfwd.upload(fwd.data(), nmem, st);
+    lp_forward(*lpm, lp_graph(d_lpfwd.p), lpw, st);
+    count(3);
+  }
+  if (anya) {
+    d_lpapp.upload(app.data(), nmem, st);
+    lp_apply_omega(lp_graph(d_lpapp.p), lpw, st);
+    count();
+  }
+}
+
+// Mode 1: one Adam step on this iteration's matrices and Krylov pairs.
+void Engine::lp_after_solve() {
+  LpColumns c{lp_ncol, d_ctop.p, d_cstr.p, d_cnl.p, d_cmem.p};
+  double loss = 0.0;
+  int used = 0;
+  lp_train_step(*lpm, lp_graph(d_lpact.p), c, d_down.p, d_tslot.p, lpw, d_P.p, d_Q.p, st, &loss,
+                &used);
+  lp_train_calls++;
 }
 
 // ---- one macro-iteration of the FP32 Picard path as a CUDA graph ---------
@@ -3912,6 +4239,10 @@ int Engine::macro_iteration() {
     const cathy_parm_t& P = h.parm;
     const double* R = &red[(size_t)m * RD_NUM];
     const int niter = nit[m];
+    if (lp_mode == 2) {
+      if (lp_use_now[m]) { lp_sum_l[m] += niter; lp_n_l[m]++; }
+      else { lp_sum_p[m] += niter; lp_n_p[m]++; }
+    }
     h.itlin += niter; h.nitert += niter;
     lin_iters += niter;
     // FP32 inner solves stop at their own iteration cap; they count as a
@@ -4292,6 +4623,21 @@ int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launche
       CG_TRY(cudaStreamSynchronize(e->st));
     }
   }
+  return 0;
+}
+
+int engine_attach_learned(Engine* e, void* model, int mode) {
+  e->lp_attach(model ? lp_model_of(model) : nullptr, model ? mode : 0);
+  return 0;
+}
+
+int engine_learned_stats(Engine* e, double* out, int n) {
+  double v[6] = {0, 0, 0, 0, (double)e->lp_train_calls, e->lpm ? e->lpm->last_loss : 0.0};
+  for (int m = 0; m < (int)e->lp_n_l.size(); ++m) {
+    v[0] += (double)e->lp_n_l[m]; v[1] += e->lp_sum_l[m];
+    v[2] += (double)e->lp_n_p[m]; v[3] += e->lp_sum_p[m];
+  }
+  for (int q = 0; q < n && q < 6; ++q) out[q] = v[q];
   return 0;
 }
 

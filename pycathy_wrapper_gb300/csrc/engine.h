@@ -91,6 +91,8 @@ int engine_reset(Engine* e);
 int engine_profile(Engine* e, int enable, double* spmv_ms, int64_t* spmv_launches,
                    double* spmv_bytes);
 int engine_timers(Engine* e, double* out, int n);
+int engine_attach_learned(Engine* e, void* model, int mode);
+int engine_learned_stats(Engine* e, double* out, int n);
 int engine_stats(Engine* e, double* gpu_ms, int64_t* launches,
                  int64_t* lin_iters, int64_t* nl_iters);
 

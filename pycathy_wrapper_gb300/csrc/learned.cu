@@ -879,6 +879,7 @@ void lp_train_step(LpModel& m, const LpGraph& g, const LpColumns& c, const int32
   lp_loss_grad(m, g, c, down, tslot, w, P, Q, st, loss, &b);
   if (nused) *nused = b;
   if (b == 0) return;
+  if (loss) m.last_loss = *loss;
   m.steps += 1;
   const float bc1 = 1.0f - powf(0.9f, (float)m.steps);
   const float bc2 = 1.0f - powf(0.999f, (float)m.steps);
@@ -912,6 +913,10 @@ int lp_guard(F&& f) {
   }
 }
 }  // namespace
+
+namespace cathy {
+LpModel* lp_model_of(void* handle) { return handle ? &((LpHandle*)handle)->m : nullptr; }
+}  // namespace cathy
 
 extern "C" {
 

@@ -74,7 +74,11 @@ struct LpModel {
   uint16_t* wbf = nullptr;      // bf16: W1 (64x16) | W2 (64x64) | W2^T (64x64)
   int64_t steps = 0;
   double lr = 1e-3;
+  double last_loss = 0.0;
 };
+
+// The model behind a cathy_gb300_lp_create handle.
+LpModel* lp_model_of(void* handle);
 
 void lp_alloc(LpModel& m);
 void lp_free(LpModel& m);

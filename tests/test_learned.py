@@ -178,3 +178,60 @@ def test_trained_network_against_plain_line_on_held_out_systems():
             counts.append((_pcg_iters(ref, A, b, d_plain), _pcg_iters(ref, A, b, d_learn)))
     print("held-out PCG iterations (plain, learned):", counts)
     assert all(abs(nl - np_) <= 1 for np_, nl in counts), counts
+
+
+def _engine_cases(n=3):
+    from pycathy_wrapper_gb300.inputs import config1
+    cases = []
+    for k in range(n):
+        c = config1(ncell=8 + 2 * k, nstr=6, tmax=1800.0, sigma=1.0 + 0.5 * k, ks_seed=40 + k)
+        c.parm.precond = 2
+        cases.append(c)
+    return cases
+
+
+@pytest.mark.gpu
+def test_solver_training_mode_leaves_the_solution_unchanged():
+    """Mode 1: the solver trains the network on its own Krylov pairs while its
+    solves stay plain -- heads are identical to a run without a model."""
+    from pycathy_wrapper_gb300.api import Simulation
+    from pycathy_wrapper_gb300.learned import LearnedPreconditioner, init_params
+    cases = _engine_cases()
+    with Simulation(cases, precision=1, graphs=False) as s:
+        s.run()
+        ref = [s.state(m)[0] for m in range(len(cases))]
+    with LearnedPreconditioner(init_params(0), lr=1e-3) as lp, \
+            Simulation(cases, precision=1, graphs=False) as s:
+        s.attach_learned(lp, mode=1)
+        s.run()
+        st = s.learned_stats()
+        got = [s.state(m)[0] for m in range(len(cases))]
+        assert lp.steps() > 10
+    assert st["train_steps"] > 10 and np.isfinite(st["last_loss"])
+    for a, b in zip(ref, got):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_solver_use_mode_with_plain_fallback():
+    """Mode 2: members solve with the learned factor and probe the plain one
+    every 8th Picard iteration; heads stay within the Picard tolerance of the
+    plain run and the counters record both kinds of solves."""
+    from pycathy_wrapper_gb300.api import Simulation
+    from pycathy_wrapper_gb300.learned import LearnedPreconditioner, init_params
+    cases = _engine_cases()
+    with Simulation(cases, precision=1, graphs=False) as s:
+        s.run()
+        ref = [(s.state(m), len(s.records(m)[1])) for m in range(len(cases))]
+    p = init_params(0)
+    p[-65:-1] *= 5.0   # a visibly non-zero correction
+    with LearnedPreconditioner(p) as lp, Simulation(cases, precision=1, graphs=False) as s:
+        s.attach_learned(lp, mode=2)
+        s.run()
+        st = s.learned_stats()
+        got = [s.state(m) for m in range(len(cases))]
+    assert st["learned_solves"] > 0 and st["plain_solves"] > 0
+    for (r, _), g in zip(ref, got):
+        assert r[3] == g[3] == 1
+        assert abs(r[1] - g[1]) < 1e-9
+        assert np.max(np.abs(r[0] - g[0])) <= 1e-5
