@@ -372,7 +372,7 @@ def main():
         "nl_iterations": nl, "lin_iterations": lin,
         "members_finished": int(sum(1 for f in fin if f == 1)),
         "wall_s_timed": wall,
-        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,float>",
+        "roofline": {"bound": "hbm", "kernel": "k_spmv_stream",
                      "timing": "per launch on the device clock (first block start to last "
                                "block end), every SpMV of the timed region",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -26,11 +26,13 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <string>
 #include <vector>
+#include <type_traits>
 
 #include "engine.h"
 #include "kernels.cuh"
@@ -648,6 +650,26 @@ k_assemble_newton(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm
 // slot; slot = LT_SEQ advances when a launch completes.  Works inside CUDA
 // graphs (where event records are not allowed in conditional bodies).
 enum { LT_SEQ = 0, LT_DONE = 1, LT_HDR = 2 };
+
+// Per-member Krylov scalars sc[m*SC_N + ...] (the SpMV accumulates x.y, x.w
+// into two consecutive slots: PQ, PR; the r-update accumulates |r|^2 and q.z
+// into RR, QZ).
+enum {
+  SC_PQ = 0, SC_PR, SC_RR, SC_QZ, SC_XL, SC_ROJ, SC_SIG, SC_AA, SC_BB,
+  SC_ROJM1, SC_ALFJM1, SC_ETAJ, SC_ALF, SC_BETA, SC_ERR, SC_NB, SC_N
+};
+// Programmatic dependent launch.  Inside the Picard-iteration graph a kernel
+// may be launched while its predecessor is still running (its blocks become
+// resident once every block of the predecessor has started); it waits here,
+// before touching any global memory, until the predecessor grid has
+// completed and its writes are visible, then lets its own successor be
+// scheduled.  Both instructions return at once for a kernel launched
+// without the programmatic attribute.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ uint64_t gtimer() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -793,16 +815,29 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
 // products d0 += x.y, d1 += x.w accumulate per warp and are flushed with one
 // FP64 atomic per quantity whenever the warp's member changes.  Timing and
 // byte accounting as in k_spmv.
+//
+// kUpd (the PCG direction update fused into the product): x is the
+// preconditioned residual z, and for its own rows the kernel forms
+// p = z + beta p and q = A z + beta q (= A p, as q holds A p_old), beta per
+// member in sc[SC_BETA] (beta = 0: p = z, q = A z); the dots are then p.q
+// and p.w.
 constexpr int kStreamWarps = 4;
+template <bool kUpd>
 __global__ void __launch_bounds__(32 * kStreamWarps)
 k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
               const uint8_t* active, const int32_t* __restrict__ rowptr,
               const int32_t* __restrict__ cols, const float* __restrict__ vals,
               const uint8_t* __restrict__ dmask, const float* __restrict__ x, float* y,
-              const float* __restrict__ w, double* acc, int acc_stride, double* alg_bytes,
-              unsigned long long* lt, int lt_cap) {
+              const float* __restrict__ w, float* pv, const double* sc, double* acc,
+              int acc_stride, double* alg_bytes, unsigned long long* lt, int lt_cap) {
+  pdl_enter();
   __shared__ int s_slot;
+  __shared__ double s_bytes;
   __shared__ float sprod[kStreamWarps][16 * kGroup + 8];
+  if (alg_bytes) {
+    if (threadIdx.x == 0) s_bytes = 0.0;
+    __syncthreads();
+  }
   if (lt) {
     if (threadIdx.x == 0) {
       const unsigned long long q = lt[LT_SEQ];
@@ -840,7 +875,8 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
     const int sbeg = __shfl_sync(0xffffffffu, rp, 0);
     const int send = __shfl_sync(0xffffffffu, rp, nr);
     if (alg_bytes && lane == 0)
-      bytes += (double)(send - sbeg) * 8.0 + nr * (4.0 + (w ? 3.0 : 2.0) * 4.0);
+      bytes += (double)(send - sbeg) * 8.0 + nr * (kUpd ? 28.0 : 4.0 + (w ? 3.0 : 2.0) * 4.0);
+    const float beta = kUpd ? (float)sc[(size_t)m * SC_N + SC_BETA] : 0.0f;
     // 16-byte vectors covering [sbeg, send)
     const int v0 = sbeg >> 2, v1 = (send + 3) >> 2;
     for (int v = v0 + lane; v < v1; v += 32) {
@@ -863,10 +899,19 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
       for (int k = rlo; k < rhi; ++k) sum += sp[k - sbeg];
       const int i = r0 + lane;
       const float xi = x[i];
-      const float yi = dmask[i] ? xi : sum;
+      const bool dm = dmask[i] != 0;
+      float yi = dm ? xi : sum;
+      float pi = xi;
+      if (kUpd) {
+        if (beta != 0.0f) {
+          pi = xi + beta * pv[i];
+          yi = dm ? pi : yi + beta * y[i];
+        }
+        pv[i] = pi;
+      }
       y[i] = yi;
-      d0 += xi * yi;
-      if (w) d1 += xi * w[i];
+      d0 += pi * yi;
+      if (w) d1 += pi * w[i];
     }
     __syncwarp();
   }
@@ -877,7 +922,12 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
       if (a1 != 0.0f) atomicAdd(acc + (size_t)cur * acc_stride + 1, (double)a1);
     }
   }
-  if (alg_bytes && lane == 0 && bytes != 0.0) atomicAdd(alg_bytes, bytes);
+  if (alg_bytes) {
+    // one global atomic per block
+    if (lane == 0 && bytes != 0.0) atomicAdd(&s_bytes, bytes);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_bytes != 0.0) atomicAdd(alg_bytes, s_bytes);
+  }
   if (lt) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -900,6 +950,7 @@ k_resid(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
         const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
         const MT* vals, const uint8_t* dmask, const VT* x, const VT* b, VT* r,
         double* acc, int acc_stride) {
+  pdl_enter();
   const int m = bm_mem[blockIdx.x];
   if (!active[m]) return;
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
@@ -955,7 +1006,10 @@ __device__ __forceinline__ void k_line_setup_b(int bid_, const int32_t* bm_mem, 
   const int top = bm_r0[bid_] + threadIdx.x;
   if (top >= bm_r1[bid_]) return;
   const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
-  double piv_prev = 1.0, c_prev = 0.0;
+  // the FP32 factor pivots in FP32 (the recurrence of an M-matrix column is
+  // stable; FP64 divisions run at a small fraction of the FP32 rate here)
+  using CT = typename std::conditional<sizeof(MT) == 4, float, double>::type;
+  CT piv_prev = 1, c_prev = 0;
   for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
     int id[kLineChunk], iw[kLineChunk];
     bool dm[kLineChunk], dmb[kLineChunk];
@@ -970,14 +1024,14 @@ __device__ __forceinline__ void k_line_setup_b(int bid_, const int32_t* bm_mem, 
         if (k + 1 < nl) { iw[j] = down[i]; dmb[j] = dmask[i + nnod] != 0; }
       }
     }
-    double a[kLineChunk], c[kLineChunk];
+    CT a[kLineChunk], c[kLineChunk];
 #pragma unroll
     for (int j = 0; j < kLineChunk; ++j) {
-      a[j] = 1.0;
-      c[j] = 0.0;
+      a[j] = 1;
+      c[j] = 0;
       if (k0 + j < nl) {
-        if (!dm[j]) a[j] = (double)vals[id[j]];
-        if (!dm[j] && !dmb[j] && iw[j] >= 0) c[j] = (double)vals[iw[j]];
+        if (!dm[j]) a[j] = (CT)vals[id[j]];
+        if (!dm[j] && !dmb[j] && iw[j] >= 0) c[j] = (CT)vals[iw[j]];
       }
     }
 #pragma unroll
@@ -985,8 +1039,8 @@ __device__ __forceinline__ void k_line_setup_b(int bid_, const int32_t* bm_mem, 
       const int k = k0 + j;
       if (k < nl) {
         const int i = top + k * nnod;
-        const double piv = a[j] - c_prev * c_prev / piv_prev;
-        pinv[i] = (VT)(1.0 / piv);
+        const CT piv = a[j] - c_prev * c_prev / piv_prev;
+        pinv[i] = (VT)((CT)1 / piv);
         cdown[i] = (VT)c[j];
         piv_prev = piv;
         c_prev = c[j];
@@ -1126,6 +1180,7 @@ __global__ void k_line_apply(const int32_t* bm_mem, const int32_t* bm_r0,
                              const VT* __restrict__ cdown, const VT* __restrict__ r,
                              VT* __restrict__ z, const VT* __restrict__ w,
                              double* acc, int acc_stride, int acc_off) {
+  pdl_enter();
   k_line_apply_b<VT>(blockIdx.x, bm_mem, bm_r0, bm_r1, active, ms, pinv, cdown, r, z, w, acc, acc_stride, acc_off);
 }
 
@@ -1313,12 +1368,6 @@ __global__ void k_umul(const int32_t* bm_mem, const int32_t* bm_r0, const int32_
 }
 
 // ---- Krylov vector kernels (per member scalars in sc[m*SC_N + ...]) ------
-// (k_spmv accumulates x.y, x.w into two consecutive slots: PQ, PR; the
-// r-update accumulates |r|^2 and q.z into RR, QZ.)
-enum {
-  SC_PQ = 0, SC_PR, SC_RR, SC_QZ, SC_XL, SC_ROJ, SC_SIG, SC_AA, SC_BB,
-  SC_ROJM1, SC_ALFJM1, SC_ETAJ, SC_ALF, SC_BETA, SC_ERR, SC_NB, SC_N
-};
 
 // x0 = M^-1 b path helpers: generic axpby-style kernels
 template <class VT>
@@ -1327,6 +1376,7 @@ __global__ void k_pcg_update_rx(const int32_t* bm_mem, const int32_t* bm_r0,
                                 const double* sc, VT* r, VT* x, const VT* p,
                                 const VT* q, const uint8_t* dmask,
                                 const VT* dinv, VT* z, double* acc) {
+  pdl_enter();
   // alfa = (p.r)/(p.q); r -= alfa q; x += alfa p; rr += |r_masked|^2;
   // Jacobi (dinv != NULL): z = dinv*r, qz += q.z
   const int m = bm_mem[blockIdx.x];
@@ -1774,11 +1824,10 @@ __global__ void k_flags(int nmem, const uint8_t* act, uint8_t bits, uint8_t* out
 // ============================================================================
 struct NodalF {
   float *ckrw, *et1, *et2, *sw, *dsw, *dpsi, *hhi, *hlo, *rhs, *xt5, *pdiff;
-  float2 *krE;   // per element: (mean kr, mean Sw*Ss)
   float2 *ckr2;  // per node: (kr, Sw*Ss)
   float2 *h2;    // per node: total head (hi, lo)
   float *vgn, *vgm, *vgpsat, *vgn1, *vgnr, *vgpsn, *vgpnot, *ss;
-  float *rmcp, *bcf, *qneu, *volnod, *pnodi;
+  float *rmcp, *qneu, *volnod, *pnodi;
 };
 
 // Se(psi) and Se(psi1) - Se(psi0) in FP32 (fvgse.f semantics for the sign
@@ -1844,11 +1893,18 @@ __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
 
 // Step actions of every node (phase 0, the surface part for surface nodes,
 // phase 1) and the FP32 soil characteristics of iterating members, in one
-// pass: each of these reads and writes only its own node.
-__global__ void k_start_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+// pass: each of these reads and writes only its own node.  The blocks after
+// the node blocks set the Krylov flags of the members.
+__global__ void k_start_vg_f32(int nb1, const int32_t* bm_mem, const int32_t* bm_r0,
                                const int32_t* bm_r1, const uint8_t* act,
                                const MemberScal* ms, Nodal nd, NodalF nf, const double* z,
-                               int need_sw) {
+                               int need_sw, int nmem, uint8_t* active) {
+  pdl_enter();
+  if ((int)blockIdx.x >= nb1) {
+    // Krylov member flags (the blocks after the node blocks)
+    k_flags_b(blockIdx.x - nb1, nmem, act, ACT_ITER, active);
+    return;
+  }
   const int m = bm_mem[blockIdx.x];
   const uint8_t a = act[m];
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
@@ -1863,23 +1919,6 @@ __global__ void k_start_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
   if (a & ACT_ITER) vg_f32_node(i, nd, nf, z);
 }
 
-// Element means of kr and Sw*Ss (NODELT) for the FP32 assembly.
-__device__ __forceinline__ void k_elem_f32_b(int bid_, const int32_t* ebm_mem, const int32_t* ebm_e0,
-                           const int32_t* ebm_e1, const uint8_t* act, const int4* tet,
-                           NodalF nf) {
-  const int m = ebm_mem[bid_];
-  if (!(act[m] & ACT_ITER)) return;
-  const int e = ebm_e0[bid_] + threadIdx.x;
-  if (e >= ebm_e1[bid_]) return;
-  const int4 t = tet[e];
-  const float2 a = nf.ckr2[t.x], b = nf.ckr2[t.y], c = nf.ckr2[t.z], d = nf.ckr2[t.w];
-  nf.krE[e] = make_float2(0.25f * (a.x + b.x + c.x + d.x), 0.25f * (a.y + b.y + c.y + d.y));
-}
-__global__ void k_elem_f32(const int32_t* ebm_mem, const int32_t* ebm_e0,
-                           const int32_t* ebm_e1, const uint8_t* act, const int4* tet,
-                           NodalF nf) {
-  k_elem_f32_b(blockIdx.x, ebm_mem, ebm_e0, ebm_e1, act, tet, nf);
-}
 
 // ---- compensated FP32 sums (TwoSum) for the mass-balance reductions ----
 struct FF {
@@ -1945,20 +1984,28 @@ __global__ void k_rec48(int nt, const TetRec<float>* rec, float4* out) {
 // node l) and each slot's owner lane adds its contributions through a gather
 // list precomputed from the mesh (in incidence order): deterministic, no
 // atomics.  RHS = -sum K (h_l - h_k) - mass terms, see the FP32 block
-// comment; BC fluxes come precomputed in FP32 (bcf).
+// comment.  The element means of kr and Sw*Ss (NODELT) are formed per
+// incidence from the staged values of the element's four nodes, and the
+// row's boundary flux (BCPIC: static Neumann flux, plus
+// theta*ATMACT + (1-theta)*ATMOLD at atmospheric Neumann surface nodes) is
+// added by the row's first lane.
 __global__ void __launch_bounds__(kThreads)
 k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
                       const uint8_t* act, const MemberScal* ms,
                       const int32_t* rowptr, const int32_t* cols,
                       const int32_t* inc_ptr, const int32_t* inc,
                       const uint16_t* __restrict__ islot, const float4* __restrict__ rec48,
-                      const uint8_t* dmask, NodalF nf, const float* bcf, float* vals,
+                      const uint8_t* dmask, NodalF nf, const int32_t* __restrict__ loc,
+                      const int8_t* __restrict__ ifatm, const double* __restrict__ atmact,
+                      const double* __restrict__ atmold, float* vals,
                       float lm_d, float lm_o, const int64_t* __restrict__ glrow,
                       const uint8_t* __restrict__ gloff, const uint8_t* __restrict__ gl) {
+  pdl_enter();
   const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
   __shared__ float sval[kRowsPerBlock16][64 * 4];
   __shared__ float2 sh2[kRowsPerBlock16][kGroup];
+  __shared__ float2 sk2[kRowsPerBlock16][kGroup];
   __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
   const int i = bm_r0[blockIdx.x] + grp;
@@ -1977,6 +2024,7 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   }
   if (col >= 0) {
     sh2[grp][lane] = nf.h2[col];
+    sk2[grp][lane] = nf.ckr2[col];
     if (lm_o != 0.0f) {
       sdp[grp][lane] = nf.dpsi[col];
       sds[grp][lane] = nf.dsw[col];
@@ -1997,8 +2045,10 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
       const float4 r0 = rv[0], r1 = rv[1], r2 = rv[2];
       const float Sv[10] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y};
       const float vol = r2.z, vpel = r2.w;
-      const float2 ke = nf.krE[e];
-      const float kr = ke.x, e1 = ke.y;
+      const float2 n0 = sk2[grp][isl & 15], n1 = sk2[grp][(isl >> 4) & 15],
+                   n2 = sk2[grp][(isl >> 8) & 15], n3 = sk2[grp][(isl >> 12) & 15];
+      const float kr = 0.25f * (n0.x + n1.x + n2.x + n3.x);
+      const float e1 = 0.25f * (n0.y + n1.y + n2.y + n3.y);
       const float ve1 = vol * e1;
 #pragma unroll
       for (int l = 0; l < 4; ++l) {
@@ -2047,176 +2097,140 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   if (lane == 0) {
     rhs -= (msum * nf.dpsi[i] + mssum * nf.dsw[i]) * rdt;
     nf.xt5[i] = rhs;
-    nf.rhs[i] = dmask[i] ? 0.0f : rhs + bcf[i];
+    float f = nf.qneu[i];
+    if (loc[i] < S.nnod && ifatm[i] == 0) {
+      const double thd = S.tetaf;
+      f += (thd == 1.0) ? (float)atmact[i]
+                        : (float)(thd * atmact[i] + (1.0 - thd) * atmold[i]);
+    }
+    nf.rhs[i] = dmask[i] ? 0.0f : rhs + f;
   }
 }
 
-// FP32 boundary fluxes of the surface nodes for this iteration (BCPIC):
-// theta*ATMACT + (1-theta)*ATMOLD for Neumann atmospheric nodes, plus the
-// static non-atmospheric Neumann flux.
-__device__ __forceinline__ void k_bcflux_f32_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                             const uint8_t* act, const MemberScal* ms, Nodal nd,
-                             const float* qneu_f, float* bcf) {
-  const int i = bm_r0[bid_] + threadIdx.x;
-  if (i >= bm_r1[bid_]) return;
-  const int m = bm_mem[bid_];
-  if (!(act[m] & ACT_ITER)) return;
-  float f = qneu_f[i];
-  if (nd.ifatm[i] == 0) {
-    const double th = ms[m].tetaf;
-    f += (th == 1.0) ? (float)nd.atmact[i]
-                     : (float)(th * nd.atmact[i] + (1.0 - th) * nd.atmold[i]);
-  }
-  bcf[i] = f;
-}
-__global__ void k_bcflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                             const uint8_t* act, const MemberScal* ms, Nodal nd,
-                             const float* qneu_f, float* bcf) {
-  k_bcflux_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, nd, qneu_f, bcf);
-}
 
-// Back-calculated flux at Dirichlet rows (BKPIC): SCR = A*PDIFF - XT5, then
-// QPNEW (static Dirichlet) or ATMACT (atmospheric Dirichlet).  16 lanes per
-// candidate row: surface rows through a member block map (rows == nullptr)
-// or an explicit list of deep static Dirichlet rows.
-__device__ __forceinline__ void bkflux_row(int i, bool valid, int lane, const uint8_t* act,
-                                           const MemberScal* ms, const int32_t* rowptr,
-                                           const int32_t* cols, const float* vals,
-                                           Nodal& nd, NodalF& nf) {
-  bool dir = false;
-  if (valid) dir = (act[nd.mem[i]] & ACT_ITER) && nd.dmask[i];
-  float sp = 0.0f;
-  if (dir) {
-    const int sl = rowptr[i] + lane;
-    if (sl < rowptr[i + 1]) sp = vals[sl] * nf.pdiff[cols[sl]];
-  }
-  sp = group_sum<float>(sp);
-  if (dir && lane == 0) {
-    const int m = nd.mem[i];
-    const double th = ms[m].tetaf;
-    const double scr = (double)sp - (double)nf.xt5[i];
-    if (nd.sdir[i]) nd.qpnew[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.qpold[i]) / th;
-    else if (nd.loc[i] < ms[m].nnod)
-      nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
-  }
-}
-__device__ __forceinline__ void k_bkflux_f32_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                             const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
-                             const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
-  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
-  const int i = bm_r0[bid_] + grp;
-  bkflux_row(i, i < bm_r1[bid_], lane, act, ms, rowptr, cols, vals, nd, nf);
-}
-__global__ void k_bkflux_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                             const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
-                             const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
-  k_bkflux_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, rowptr, cols, vals, nd, nf);
-}
-__device__ __forceinline__ void k_bkflux_list_f32_b(int bid_, int nrows, const int32_t* rows, const uint8_t* act,
-                                  const MemberScal* ms, const int32_t* rowptr,
-                                  const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
-  const int grp = (bid_ * blockDim.x + threadIdx.x) / kGroup;
-  const int lane = threadIdx.x % kGroup;
-  const bool ok = grp < nrows;
-  bkflux_row(ok ? rows[grp] : 0, ok, lane, act, ms, rowptr, cols, vals, nd, nf);
-}
-__global__ void k_bkflux_list_f32(int nrows, const int32_t* rows, const uint8_t* act,
-                                  const MemberScal* ms, const int32_t* rowptr,
-                                  const int32_t* cols, const float* vals, Nodal nd, NodalF nf) {
-  k_bkflux_list_f32_b(blockIdx.x, nrows, rows, act, ms, rowptr, cols, vals, nd, nf);
-}
 
-// MASBAL sums (STORMB, FLUXMB), RELAX and NORMS for the FP32 path, one thread
-// per row; compensated FP32 block sums.
+// Post-solve pass of the FP32 Picard iteration, one thread per row:
+// PNEW += PDIFF + SHLPIC; at Dirichlet rows the back-calculated flux (BKPIC:
+// SCR = A*PDIFF - XT5 -> QPNEW or ATMACT); then the MASBAL sums, RELAX and
+// NORMS of k_masbal_norms_f32.  PINF and IKMAX (the largest node index
+// attaining PINF) come from one 64-bit maximum of (|dp| float bits, node
+// index) per member.  The last block to finish converts the maxima and
+// takes the per-member pass: PNEW/POLD at IKMAX and whether SWITCH_OLD runs.
 __global__ void __launch_bounds__(kThreads)
-k_masbal_norms_f32(int do_shl, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                   const uint8_t* act, const MemberScal* ms, Nodal nd, NodalF nf,
-                   const float* volnod_f, const float* pnodi_f, double* red,
-                   double* redmax) {
+k_masbal_post_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                  const uint8_t* act, const MemberScal* ms, Nodal nd, NodalF nf,
+                  const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
+                  const float* __restrict__ vals, double* red, double* redmax, int nmem,
+                  const int32_t* node_off, int32_t* ikmax, double* ikval, int l2norm,
+                  uint8_t* sw, unsigned int* done) {
+  pdl_enter();
   const int m = bm_mem[blockIdx.x];
-  if (!(act[m] & ACT_ITER)) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  const MemberScal& S = ms[m];
-  FF v[RD_PL2];
-  for (int q = 0; q < RD_PL2; ++q) v[q] = FF{0.0f, 0.0f};
-  float pl2 = 0.0f, fl2 = 0.0f, pinf = 0.0f, finf = 0.0f;
-  if (do_shl && i < bm_r1[blockIdx.x]) {
-    // PNEW += PDIFF + SHLPIC (the head update of the graph path)
-    double p = nd.pnew[i] + (double)nf.pdiff[i];
-    if (nd.sdir[i]) p = nd.presc[i];
-    else if (nd.dmask[i]) p = nd.pold[i];
-    nd.pnew[i] = p;
-  }
-  if (i < bm_r1[blockIdx.x]) {
-    const bool surf = nd.loc[i] < S.nnod;
-    const int8_t f = surf ? nd.ifatm[i] : (int8_t)-1;
-    if (nd.sdir[i]) {
-      const float qn = (float)nd.qpnew[i];
-      if (qn > 0.0f) v[RD_NDIN].hi = qn; else v[RD_NDOUT].hi = qn;
-    }
-    if (f != -1) {
-      const float aa = (float)nd.atmact[i];
-      if (f == 1 || f == 2) {
-        if (aa > 0.0f) v[RD_ADIN].hi = aa; else v[RD_ADOUT].hi = aa;
-      } else {
-        if (aa > 0.0f) v[RD_ANIN].hi = aa; else v[RD_ANOUT].hi = aa;
-      }
-    }
-    double p = nd.pnew[i];
-    if (S.nlrelx == 1) {
-      p = S.omega * p + (1.0 - S.omega) * nd.pold[i];
-      nd.pnew[i] = p;
-    }
-    const float dp = (float)(p - nd.ptimep[i]);
-    const float sw = nf.sw[i], dsw = nf.dsw[i];
-    v[RD_DSTORE].hi = volnod_f[i] * (nf.ss[i] * (2.0f * sw - dsw) * 0.5f * dp + pnodi_f[i] * dsw);
-    const float diff = (float)(p - nd.pold[i]);
-    pl2 = diff * diff;
-    pinf = fabsf(diff);
-    const float b = nf.rhs[i];
-    fl2 = b * b;
-    finf = fabsf(b);
-  }
-  block_accumulate_ff<RD_PL2>(v, red + (size_t)m * RD_NUM);
-  float sums[2] = {pl2, fl2};
-  block_accumulate_t<float, 2>(sums, red + (size_t)m * RD_NUM + RD_PL2);
-  __shared__ float shm[2][kThreads / 32];
   const int wl = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    pinf = fmaxf(pinf, __shfl_xor_sync(0xffffffffu, pinf, o));
-    finf = fmaxf(finf, __shfl_xor_sync(0xffffffffu, finf, o));
-  }
-  if (wl == 0) { shm[0][w] = pinf; shm[1][w] = finf; }
-  __syncthreads();
-  if (w == 0) {
-    float a = wl < (int)(blockDim.x >> 5) ? shm[0][wl] : 0.0f;
-    float b = wl < (int)(blockDim.x >> 5) ? shm[1][wl] : 0.0f;
+  if (act[m] & ACT_ITER) {  // block-uniform
+    const int i = bm_r0[blockIdx.x] + threadIdx.x;
+    const MemberScal& S = ms[m];
+    FF v[RD_PL2];
+    for (int q = 0; q < RD_PL2; ++q) v[q] = FF{0.0f, 0.0f};
+    float pl2 = 0.0f, fl2 = 0.0f, finf = 0.0f;
+    unsigned long long key = 0ull;
+    if (i < bm_r1[blockIdx.x]) {
+      double p = nd.pnew[i] + (double)nf.pdiff[i];
+      const bool dir = nd.dmask[i] != 0;
+      if (nd.sdir[i]) p = nd.presc[i];
+      else if (dir) p = nd.pold[i];
+      const bool surf = nd.loc[i] < S.nnod;
+      if (dir) {
+        const int s0 = rowptr[i], s1 = rowptr[i + 1];
+        float sp = 0.0f;
+        for (int sl = s0; sl < s1; ++sl) sp += vals[sl] * nf.pdiff[cols[sl]];
+        const double th = S.tetaf;
+        const double scr = (double)sp - (double)nf.xt5[i];
+        if (nd.sdir[i]) nd.qpnew[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.qpold[i]) / th;
+        else if (surf)
+          nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
+      }
+      const int8_t f = surf ? nd.ifatm[i] : (int8_t)-1;
+      if (nd.sdir[i]) {
+        const float qn = (float)nd.qpnew[i];
+        if (qn > 0.0f) v[RD_NDIN].hi = qn; else v[RD_NDOUT].hi = qn;
+      }
+      if (f != -1) {
+        const float aa = (float)nd.atmact[i];
+        if (f == 1 || f == 2) {
+          if (aa > 0.0f) v[RD_ADIN].hi = aa; else v[RD_ADOUT].hi = aa;
+        } else {
+          if (aa > 0.0f) v[RD_ANIN].hi = aa; else v[RD_ANOUT].hi = aa;
+        }
+      }
+      if (S.nlrelx == 1) p = S.omega * p + (1.0 - S.omega) * nd.pold[i];
+      nd.pnew[i] = p;
+      const float dp = (float)(p - nd.ptimep[i]);
+      const float swv = nf.sw[i], dsw = nf.dsw[i];
+      v[RD_DSTORE].hi = nf.volnod[i] * (nf.ss[i] * (2.0f * swv - dsw) * 0.5f * dp + nf.pnodi[i] * dsw);
+      const float diff = (float)(p - nd.pold[i]);
+      pl2 = diff * diff;
+      const float b = nf.rhs[i];
+      fl2 = b * b;
+      finf = fabsf(b);
+      key = ((unsigned long long)__float_as_uint(fabsf(diff)) << 32) |
+            (unsigned long long)(uint32_t)nd.loc[i];
+    }
+    block_accumulate_ff<RD_PL2>(v, red + (size_t)m * RD_NUM);
+    float sums[2] = {pl2, fl2};
+    block_accumulate_t<float, 2>(sums, red + (size_t)m * RD_NUM + RD_PL2);
+    __shared__ float shf[kThreads / 32];
+    __shared__ unsigned long long shk[kThreads / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
-      b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+      finf = fmaxf(finf, __shfl_xor_sync(0xffffffffu, finf, o));
+      const unsigned long long ko = __shfl_xor_sync(0xffffffffu, key, o);
+      key = ko > key ? ko : key;
     }
-    if (wl == 0) {
-      atomic_max_nonneg(redmax + (size_t)m * 2, (double)a);
-      atomic_max_nonneg(redmax + (size_t)m * 2 + 1, (double)b);
+    if (wl == 0) { shf[w] = finf; shk[w] = key; }
+    __syncthreads();
+    if (w == 0) {
+      float a = wl < (int)(blockDim.x >> 5) ? shf[wl] : 0.0f;
+      unsigned long long kk = wl < (int)(blockDim.x >> 5) ? shk[wl] : 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+        const unsigned long long ko = __shfl_xor_sync(0xffffffffu, kk, o);
+        kk = ko > kk ? ko : kk;
+      }
+      if (wl == 0) {
+        atomicMax(reinterpret_cast<unsigned long long*>(redmax + (size_t)m * 2), kk);
+        atomic_max_nonneg(redmax + (size_t)m * 2 + 1, (double)a);
+      }
     }
   }
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int q = threadIdx.x; q < nmem; q += blockDim.x) {
+    const bool it = (act[q] & ACT_ITER) != 0;
+    double pinf = 0.0;
+    if (it) {
+      const unsigned long long kk = reinterpret_cast<unsigned long long*>(redmax)[2 * q];
+      pinf = (double)__uint_as_float((unsigned int)(kk >> 32));
+      const int loc = (int)(uint32_t)(kk & 0xffffffffull);
+      redmax[2 * q] = pinf;
+      ikmax[q] = loc;
+      const int j = node_off[q] + loc;
+      ikval[2 * q] = nd.pnew[j];
+      ikval[2 * q + 1] = nd.pold[j];
+    }
+    const double pl2 = sqrt(red[(size_t)q * RD_NUM + RD_PL2]);
+    sw[q] = it && ((l2norm == 0 && pinf <= ms[q].tolswi) || (l2norm != 0 && pl2 <= ms[q].tolswi));
+  }
+  if (threadIdx.x == 0) *done = 0u;
 }
 
-// PNEW += PDIFF (FP32 correction into FP64 heads) + SHLPIC
-__global__ void k_update_shl_f32(const int32_t* bm_mem, const int32_t* bm_r0,
-                                 const int32_t* bm_r1, const uint8_t* act,
-                                 Nodal nd, const float* pdiff) {
-  const int m = bm_mem[blockIdx.x];
-  if (!(act[m] & ACT_ITER)) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
-  double p = nd.pnew[i] + (double)pdiff[i];
-  if (nd.sdir[i]) p = nd.presc[i];
-  else if (nd.dmask[i]) p = nd.pold[i];
-  nd.pnew[i] = p;
-}
 
 
 // STORE1 for the FP32 path: Sw(PNEW) in FP32, compensated sums.
@@ -2250,7 +2264,6 @@ __global__ void k_params_f32(int n, Nodal nd, NodalF nf) {
   nf.qneu[i] = (float)nd.qneu[i];
   nf.volnod[i] = (float)nd.volnod[i];
   nf.pnodi[i] = (float)nd.pnodi[i];
-  nf.bcf[i] = (float)nd.qneu[i];
   nf.vgn[i] = (float)nd.vgn[i]; nf.vgm[i] = (float)nd.vgm[i]; nf.vgpsat[i] = (float)nd.vgpsat[i];
   nf.vgn1[i] = (float)nd.vgn1[i]; nf.vgnr[i] = (float)nd.vgnr[i]; nf.vgpsn[i] = (float)nd.vgpsn[i];
   nf.vgpnot[i] = (float)nd.vgpnot[i]; nf.ss[i] = (float)nd.snodi[i];
@@ -2300,60 +2313,194 @@ __global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
 // number of dependent graph nodes per Picard iteration; every segment is the
 // unchanged body of the corresponding kernel.
 // ============================================================================
-// element means | BC fluxes | Krylov member flags
-__global__ void __launch_bounds__(kThreads)
-k_pre2_f32(int ne, const int32_t* e_mem, const int32_t* e_r0, const int32_t* e_r1, int ns,
-           const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1, int nmem,
-           const uint8_t* act, const int4* tet, const MemberScal* ms, Nodal nd, NodalF nf,
-           uint8_t* active) {
-  int b = blockIdx.x;
-  if (b < ne) { k_elem_f32_b(b, e_mem, e_r0, e_r1, act, tet, nf); return; }
-  b -= ne;
-  if (b < ns) { k_bcflux_f32_b(b, s_mem, s_r0, s_r1, act, ms, nd, nf.qneu, nf.bcf); return; }
-  b -= ns;
-  k_flags_b(b, nmem, act, ACT_ITER, active);
-}
 
-// column-line factor | |b_masked|^2
+// PCG set-up with x0 = 0, one launch: per vertical column the column-line
+// factor (pivot inverses and masked vertical couplings, as k_line_setup_b)
+// and, in the same sweeps, z = T^-1 b, r = b, x = 0 | |b_masked|^2 per
+// member | iteration counts = 1 and beta = 0 (first direction p = z).
 __global__ void __launch_bounds__(kThreads)
-k_pcg_setup1_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1,
-                 const int32_t* c_mem, const int32_t* c_r0, const int32_t* c_r1,
-                 const uint8_t* active, const MemberScal* ms, const int32_t* diag,
-                 const int32_t* down, const float* vals, const uint8_t* dmask, float* pinv,
-                 float* cdown, const float* b, double* sc) {
+k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1, int nc,
+                const int32_t* c_mem, const int32_t* c_r0, const int32_t* c_r1,
+                const uint8_t* active, const MemberScal* ms, const int32_t* __restrict__ diag,
+                const int32_t* __restrict__ down, const float* __restrict__ vals,
+                const uint8_t* __restrict__ dmask, float* pinv, float* cdown,
+                const float* __restrict__ b, float* r, float* x, float* z, double* sc, int nmem,
+                int32_t* niter) {
+  pdl_enter();
   int bb = blockIdx.x;
-  if (bb < ns) {
-    k_line_setup_b<float, float>(bb, s_mem, s_r0, s_r1, active, ms, diag, down, vals, dmask,
-                                 pinv, cdown);
+  if (bb >= ns) {
+    bb -= ns;
+    if (bb < nc) {
+      k_dot_b<float>(bb, c_mem, c_r0, c_r1, active, b, b, dmask, sc, SC_N, SC_XL);
+      return;
+    }
+    bb -= nc;
+    const int m = bb * blockDim.x + threadIdx.x;
+    if (m < nmem && active[m]) {
+      niter[m] = 1;
+      sc[(size_t)m * SC_N + SC_BETA] = 0.0;
+    }
     return;
   }
-  bb -= ns;
-  k_dot_b<float>(bb, c_mem, c_r0, c_r1, active, b, b, dmask, sc, SC_N, SC_XL);
-}
-
-// p = M^-1 r | iteration counts
-__global__ void __launch_bounds__(kThreads)
-k_pcg_setup3_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1,
-                 const uint8_t* active, const MemberScal* ms, const float* pinv,
-                 const float* cdown, const float* r, float* p, int nmem, int32_t* niter) {
-  int bb = blockIdx.x;
-  if (bb < ns) {
-    k_line_apply_b<float>(bb, s_mem, s_r0, s_r1, active, ms, pinv, cdown, r, p, nullptr, nullptr,
-                          0, 0);
-    return;
+  const int m = s_mem[bb];
+  if (!active[m]) return;
+  const int top = s_r0[bb] + threadIdx.x;
+  if (top >= s_r1[bb]) return;
+  const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
+  float piv_prev = 1.0f, c_prev = 0.0f, yprev = 0.0f, pv_prev = 0.0f;
+  for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
+    int id[kLineChunk], iw[kLineChunk];
+    bool dm[kLineChunk], dmb[kLineChunk];
+    float bv[kLineChunk];
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      const int k = k0 + j;
+      id[j] = -1; iw[j] = -1; dm[j] = true; dmb[j] = true; bv[j] = 0.0f;
+      if (k < nl) {
+        const int i = top + k * nnod;
+        dm[j] = dmask[i] != 0;
+        id[j] = diag[i];
+        bv[j] = b[i];
+        if (k + 1 < nl) { iw[j] = down[i]; dmb[j] = dmask[i + nnod] != 0; }
+      }
+    }
+    float a[kLineChunk], c[kLineChunk];
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      a[j] = 1.0f;
+      c[j] = 0.0f;
+      if (k0 + j < nl) {
+        if (!dm[j]) a[j] = vals[id[j]];
+        if (!dm[j] && !dmb[j] && iw[j] >= 0) c[j] = vals[iw[j]];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      const int k = k0 + j;
+      if (k < nl) {
+        const int i = top + k * nnod;
+        const float piv = a[j] - c_prev * c_prev / piv_prev;
+        const float pv = 1.0f / piv;
+        pinv[i] = pv;
+        cdown[i] = c[j];
+        // forward substitution with the previous layer's factor entries
+        const float yk = bv[j] - c_prev * yprev * pv_prev;
+        z[i] = yk;
+        r[i] = bv[j];
+        x[i] = 0.0f;
+        yprev = yk;
+        pv_prev = pv;
+        piv_prev = piv;
+        c_prev = c[j];
+      }
+    }
   }
-  bb -= ns;
-  k_niter_init_b(bb, nmem, active, niter);
+  float znext = 0.0f;
+  for (int k1 = nl - 1; k1 >= 0; k1 -= kLineChunk) {
+    float yy[kLineChunk], pv[kLineChunk], cd[kLineChunk];
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      const int k = k1 - j;
+      yy[j] = pv[j] = cd[j] = 0.0f;
+      if (k >= 0) {
+        const int i = top + k * nnod;
+        yy[j] = z[i]; pv[j] = pinv[i]; cd[j] = cdown[i];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kLineChunk; ++j) {
+      const int k = k1 - j;
+      if (k >= 0) {
+        const float zk = (yy[j] - cd[j] * znext) * pv[j];
+        z[top + k * nnod] = zk;
+        znext = zk;
+      }
+    }
+  }
 }
 
-// p = z + beta p, then the PCG decision by the last block to finish: the
-// per-member test of k_krylov_decide_g and the WHILE node's condition.
+// One column-line PCG step after the fused direction update + product
+// (k_spmv_stream<true>), one thread per vertical column: alpha = p.r / p.q;
+// r -= alpha q, x += alpha p; rr += |r_masked|^2; z = T^-1 r (forward and
+// backward sweeps along the column); qz += q.z.  The last block to finish
+// then takes the per-member decision of k_krylov_decide_g, stores
+// beta = -q.z / p.q for the next direction, and either sets the graph's
+// WHILE condition (use_cond) or stores the number of members still
+// iterating in *nact.
 __global__ void __launch_bounds__(kThreads)
-k_pcg_update_p_decide(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                      uint8_t* active, double* sc, float* p, const float* z, int nmem,
-                      int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
-                      unsigned int* done, cudaGraphConditionalHandle h) {
-  k_pcg_update_p_b<float>(blockIdx.x, bm_mem, bm_r0, bm_r1, active, sc, p, z);
+k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+             uint8_t* active, const MemberScal* ms, double* sc, const float* __restrict__ pinv,
+             const float* __restrict__ cdown, float* r, float* x, const float* __restrict__ p,
+             const float* __restrict__ q, float* z, const uint8_t* __restrict__ dmask, int nmem,
+             int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
+             unsigned int* done, int32_t* nact, int use_cond, cudaGraphConditionalHandle h) {
+  pdl_enter();
+  const int m = bm_mem[blockIdx.x];
+  if (active[m]) {  // block-uniform
+    float dd[2] = {0.0f, 0.0f};  // rr, qz
+    const int top = bm_r0[blockIdx.x] + threadIdx.x;
+    if (top < bm_r1[blockIdx.x]) {
+      const float alfa = (float)(sc[(size_t)m * SC_N + SC_PR] / sc[(size_t)m * SC_N + SC_PQ]);
+      const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
+      float yprev = 0.0f, cprev = 0.0f, pprev = 0.0f;
+      for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
+        float rr[kLineChunk], qq[kLineChunk], pp[kLineChunk], xx[kLineChunk], pv[kLineChunk],
+            cd[kLineChunk];
+        bool dm[kLineChunk];
+#pragma unroll
+        for (int j = 0; j < kLineChunk; ++j) {
+          const int k = k0 + j;
+          rr[j] = qq[j] = pp[j] = xx[j] = pv[j] = cd[j] = 0.0f;
+          dm[j] = true;
+          if (k < nl) {
+            const int i = top + k * nnod;
+            rr[j] = r[i]; qq[j] = q[i]; pp[j] = p[i]; xx[j] = x[i];
+            pv[j] = pinv[i]; cd[j] = cdown[i]; dm[j] = dmask[i] != 0;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < kLineChunk; ++j) {
+          const int k = k0 + j;
+          if (k < nl) {
+            const int i = top + k * nnod;
+            const float ri = rr[j] - alfa * qq[j];
+            r[i] = ri;
+            x[i] = xx[j] + alfa * pp[j];
+            if (!dm[j]) dd[0] += ri * ri;
+            const float yk = ri - cprev * yprev * pprev;
+            z[i] = yk;
+            yprev = yk;
+            cprev = cd[j];
+            pprev = pv[j];
+          }
+        }
+      }
+      float znext = 0.0f;
+      for (int k1 = nl - 1; k1 >= 0; k1 -= kLineChunk) {
+        float yy[kLineChunk], pv[kLineChunk], cd[kLineChunk], qq[kLineChunk];
+#pragma unroll
+        for (int j = 0; j < kLineChunk; ++j) {
+          const int k = k1 - j;
+          yy[j] = pv[j] = cd[j] = qq[j] = 0.0f;
+          if (k >= 0) {
+            const int i = top + k * nnod;
+            yy[j] = z[i]; pv[j] = pinv[i]; cd[j] = cdown[i]; qq[j] = q[i];
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < kLineChunk; ++j) {
+          const int k = k1 - j;
+          if (k >= 0) {
+            const float zk = (yy[j] - cd[j] * znext) * pv[j];
+            z[top + k * nnod] = zk;
+            dd[1] += qq[j] * zk;
+            znext = zk;
+          }
+        }
+      }
+    }
+    block_accumulate_t<float, 2>(dd, sc + (size_t)m * SC_N + SC_RR);
+  }
   __shared__ int s_last, s_cnt;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -2365,17 +2512,18 @@ k_pcg_update_p_decide(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   if (!s_last) return;
   __threadfence();
   int mine = 0;
-  for (int m = threadIdx.x; m < nmem; m += blockDim.x) {
-    if (!active[m]) continue;
-    double* S = sc + (size_t)m * SC_N;
+  for (int mm = threadIdx.x; mm < nmem; mm += blockDim.x) {
+    if (!active[mm]) continue;
+    double* S = sc + (size_t)mm * SC_N;
     const double xl = S[SC_XL];
     const double err = (xl > 0.0) ? sqrt(S[SC_RR] / xl) : 0.0;
     S[SC_ERR] = err;
-    if (err > tol && niter[m] < itmax) {
-      niter[m] += 1;
+    if (err > tol && niter[mm] < itmax) {
+      niter[mm] += 1;
+      S[SC_BETA] = -S[SC_QZ] / S[SC_PQ];
       mine++;
     } else {
-      active[m] = 0;
+      active[mm] = 0;
     }
     S[SC_PR] = S[SC_PQ] = S[SC_QZ] = S[SC_RR] = 0.0;
   }
@@ -2385,73 +2533,20 @@ k_pcg_update_p_decide(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     *done = 0u;
     const int l = *loops + 1;
     *loops = l;
-    cudaGraphSetConditional(h, (s_cnt > 0 && l < maxloops) ? 1u : 0u);
+    if (use_cond) cudaGraphSetConditional(h, (s_cnt > 0 && l < maxloops) ? 1u : 0u);
+    if (nact) *nact = s_cnt;
   }
 }
 
-// back-calculated fluxes: surface rows | deep static Dirichlet rows
-__global__ void __launch_bounds__(kThreads)
-k_bkflux_all_f32(int ns16, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1,
-                 int ndeep, const int32_t* deep, const uint8_t* act, const MemberScal* ms,
-                 const int32_t* rowptr, const int32_t* cols, const float* vals, Nodal nd,
-                 NodalF nf) {
-  int bb = blockIdx.x;
-  if (bb < ns16) {
-    k_bkflux_f32_b(bb, s_mem, s_r0, s_r1, act, ms, rowptr, cols, vals, nd, nf);
-    return;
-  }
-  bb -= ns16;
-  k_bkflux_list_f32_b(bb, ndeep, deep, act, ms, rowptr, cols, vals, nd, nf);
-}
 
-// per member: PNEW/POLD at IKMAX, and whether SWITCH_OLD runs
-__global__ void k_member_post(int nmem, const uint8_t* act, const int32_t* node_off,
-                              const int32_t* ikmax, Nodal nd, double* ikval, const double* red,
-                              const double* redmax, const MemberScal* ms, int l2norm,
-                              uint8_t* sw) {
-  k_gather_ik_b(blockIdx.x, nmem, act, node_off, ikmax, nd, ikval);
-  k_switch_flags_b(blockIdx.x, nmem, act, red, redmax, ms, l2norm, sw);
-}
 
-// IKMAX of every iterating member, then (last block to finish) PNEW/POLD at
-// IKMAX and whether SWITCH_OLD runs, per member.
-__global__ void k_ikmax_post(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                             const uint8_t* act, Nodal nd, const double* redmax, int32_t* ikmax,
-                             int nmem, const int32_t* node_off, double* ikval, const double* red,
-                             const MemberScal* ms, int l2norm, uint8_t* sw, unsigned int* done) {
-  const int m = bm_mem[blockIdx.x];
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if ((act[m] & ACT_ITER) && i < bm_r1[blockIdx.x]) {
-    if (fabsf((float)(nd.pnew[i] - nd.pold[i])) == (float)redmax[(size_t)m * 2])
-      atomicMax(ikmax + m, nd.loc[i]);
-  }
-  __shared__ int s_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  for (int q = threadIdx.x; q < nmem; q += blockDim.x) {
-    const bool it = (act[q] & ACT_ITER) != 0;
-    if (it) {
-      const int j = node_off[q] + max(ikmax[q], 0);
-      ikval[2 * q] = nd.pnew[j];
-      ikval[2 * q + 1] = nd.pold[j];
-    }
-    const double pinf = redmax[2 * q], pl2 = sqrt(red[(size_t)q * RD_NUM + RD_PL2]);
-    sw[q] = it && ((l2norm == 0 && pinf <= ms[q].tolswi) || (l2norm != 0 && pl2 <= ms[q].tolswi));
-  }
-  if (threadIdx.x == 0) *done = 0u;
-}
 
 // SWITCH_OLD on the surface nodes of the members that switch, then STORE1
 // (storcal.f) of every iterating member at the final heads.
 __global__ void k_switch_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
                                     const int32_t* bm_r1, const uint8_t* act, const uint8_t* sw,
                                     const MemberScal* ms, Nodal nd, NodalF nf, double* red) {
+  pdl_enter();
   const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
@@ -2531,8 +2626,8 @@ struct Engine {
   // device buffers
   DBuf<int32_t> d_mem, d_loc, d_node_off;
   DBuf<double> d_nodal[48];
-  DBuf<float> d_nodf[24];
-  DBuf<float2> d_krE, d_ckr2, d_h2;
+  DBuf<float> d_nodf[23];
+  DBuf<float2> d_ckr2, d_h2;
   BlockMap bme;  // element blocks per member
   DBuf<int32_t> d_drows;  // Dirichlet candidate rows (surface + static)
   int ndrows = 0;
@@ -2595,6 +2690,33 @@ struct Engine {
   }
   void count(int k = 1) { launches += k; }
   void check_launch() { CG_TRY(cudaPeekAtLastError()); }
+  // Kernel launch for the Picard-iteration graph.  With CATHY_GB300_PDL=1,
+  // while a graph is being captured, a kernel that directly follows another
+  // captured kernel gets a programmatic dependency on it (the kernel starts
+  // with pdl_enter()); outside capture, and after a copy or the start of a
+  // capture, it is an ordinary launch.  Off by default: on GB300 the
+  // programmatic edges did not shorten the graph (one 55,815-row member:
+  // 22.89 ms with, 22.71 ms without, for 147 Picard iterations).
+  bool pdl_enabled = std::getenv("CATHY_GB300_PDL") != nullptr &&
+                     std::getenv("CATHY_GB300_PDL")[0] == '1';
+  bool pdl_cap = false, pdl_prev = false;
+  template <class... KArgs, class... Args>
+  void launch(void (*k)(KArgs...), int grid, int block, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    if (pdl_enabled && pdl_cap && pdl_prev) {
+      at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      at[0].val.programmaticStreamSerializationAllowed = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+    }
+    CG_TRY(cudaLaunchKernelEx(&cfg, k, args...));
+    pdl_prev = pdl_cap;
+  }
   void build(int nmembers, const cathy_member_t* mem);
   void make_blockmap(BlockMap& bm, int rows_per_block);
   void make_elem_blockmap(BlockMap& bm, int elems_per_block);
@@ -2655,13 +2777,23 @@ struct Engine {
   }
   int grid_persist(int nblk) const { return std::max(1, std::min(nblk, persist_blocks)); }
   int grid_spmv(int nblk) const { return std::max(1, std::min(nblk, 2 * persist_blocks)); }
+  int grid_stream() const {
+    return std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps,
+                                2 * persist_blocks));
+  }
   // q = A p with the fused dots p.q, p.r (FP32 stream kernel)
   void spmv_f32(const float* vals, const float* p, float* q, const float* r) {
-    const int g = std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps,
-                                       2 * persist_blocks));
-    k_spmv_stream<<<g, 32 * kStreamWarps, 0, st>>>(cbm16.nblk, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-        d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r, d_sc.p + SC_PQ, SC_N,
-        prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+    launch(k_spmv_stream<false>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+           cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
+           (float*)nullptr, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
+           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+  }
+  // p = z + beta p, q = A z + beta q (= A p) with the fused dots p.q, p.r
+  void spmv_upd_f32(const float* vals, const float* z, float* p, float* q, const float* r) {
+    launch(k_spmv_stream<true>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+           cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, z, q, r,
+           p, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
+           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
   }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
@@ -2684,7 +2816,7 @@ struct Engine {
   LpGraph lp_graph(const uint8_t* active);
   void lp_before_solve();
   void lp_after_solve();
-  void iteration_post(bool graph = false);
+  void iteration_post(bool fused = false);
   void start_kernels();
   // CUDA graph of one macro-iteration (FP32 Picard path)
   cudaGraph_t g_graph = nullptr;
@@ -2701,7 +2833,7 @@ struct Engine {
   cudaEvent_t gev0 = nullptr, gev1 = nullptr;  // around graph launches
   DBuf<int32_t> d_loops;
   DBuf<uint8_t> d_inbuf;    // [member scalars | action bits]
-  DBuf<unsigned int> d_done;  // block counter of k_pcg_update_p_decide
+  DBuf<unsigned int> d_done;  // last-block counters (k_pcg_xz_f32, k_masbal_post_f32)
   DBuf<double> d_resbuf;    // [sc | loops | red | redmax | ikmax | ikval | niter]
   size_t res_off[8] = {0, 0, 0, 0, 0, 0, 0, 0}, res_zero = 0;
   uint8_t* hp_in = nullptr;  // pinned mirror of d_inbuf
@@ -3213,14 +3345,15 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   }
   check_launch();
   if (precision == 1 && iopt == 1) {
-    for (int k = 0; k < 24; ++k) { d_nodf[k].alloc(N); d_nodf[k].zero(st); }
-    float** fp[24] = {&nf.ckrw, &nf.et1, &nf.et2, &nf.sw, &nf.dsw, &nf.dpsi, &nf.hhi, &nf.hlo,
-                      &nf.rhs, &nf.xt5, &nf.pdiff, &nf.vgn, &nf.vgm, &nf.vgpsat, &nf.vgn1,
-                      &nf.vgnr, &nf.vgpsn, &nf.vgpnot, &nf.ss, &nf.rmcp, &nf.bcf, &nf.qneu,
-                      &nf.volnod, &nf.pnodi};
-    for (int k = 0; k < 24; ++k) *fp[k] = d_nodf[k].p;
-    d_krE.alloc(NT); d_ckr2.alloc(N); d_h2.alloc(N);
-    nf.krE = d_krE.p; nf.ckr2 = d_ckr2.p; nf.h2 = d_h2.p;
+    constexpr int kNodf = 23;
+    for (int k = 0; k < kNodf; ++k) { d_nodf[k].alloc(N); d_nodf[k].zero(st); }
+    float** fp[kNodf] = {&nf.ckrw, &nf.et1, &nf.et2, &nf.sw, &nf.dsw, &nf.dpsi, &nf.hhi, &nf.hlo,
+                         &nf.rhs, &nf.xt5, &nf.pdiff, &nf.vgn, &nf.vgm, &nf.vgpsat, &nf.vgn1,
+                         &nf.vgnr, &nf.vgpsn, &nf.vgpnot, &nf.ss, &nf.rmcp, &nf.qneu,
+                         &nf.volnod, &nf.pnodi};
+    for (int k = 0; k < kNodf; ++k) *fp[k] = d_nodf[k].p;
+    d_ckr2.alloc(N); d_h2.alloc(N);
+    nf.ckr2 = d_ckr2.p; nf.h2 = d_h2.p;
     k_params_f32<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, nd, nf);
     check_launch();
   }
@@ -3311,6 +3444,9 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_nact_dummy.alloc(1);
   d_prof_bytes.alloc(1);
   d_prof_bytes.zero(st);
+  // last-block counters of k_pcg_xz_f32 and k_masbal_post_f32 (both paths)
+  d_done.alloc(2);
+  d_done.zero(st);
   if (graphs_on()) pinned_alloc();
   CG_TRY(cudaStreamSynchronize(st));
 }
@@ -3563,33 +3699,82 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
   }
   const int pc = precond;
   if constexpr (sizeof(MT) == 4 && sizeof(VT) == 4) {
-    if (phase != 0 && pc == 2 && cbms.nblk && cbm1.nblk) {
-      if (phase == 1) {
-        // column-line factor | |b|^2 ; x0 = M^-1 b ; r = b - A x0 ;
-        // p = M^-1 r | iteration counts (sc and the loop counter were zeroed
-        // at the start of the graph)
-        k_pcg_setup1_f32<<<cbms.nblk + cbm1.nblk, kThreads, 0, st>>>(cbms.nblk, cbms.mem.p,
-            cbms.r0.p, cbms.r1.p, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, d_ms.p, d_diag.p,
-            d_down.p, vals, d_dmask.p, linv, lc, b, d_sc.p);
-        k_line_apply<VT><<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
-            d_active.p, d_ms.p, linv, lc, b, x, nullptr, d_sc.p, SC_N, SC_QZ);
-        k_resid<MT, VT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-            d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, x, b, r, nullptr, 0);
-        k_pcg_setup3_f32<<<cbms.nblk + cdiv(nmem, kThreads), kThreads, 0, st>>>(cbms.nblk,
-            cbms.mem.p, cbms.r0.p, cbms.r1.p, d_active.p, d_ms.p, linv, lc, r, p, nmem, d_niter.p);
-        count(4);
-      } else {
-        spmv_f32(vals, p, q, r);
-        k_pcg_update_rx<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
-            d_active.p, d_sc.p, r, x, p, q, d_dmask.p, nullptr, nullptr, nullptr);
-        k_line_apply<VT><<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
-            d_active.p, d_ms.p, linv, lc, r, z, q, d_sc.p, SC_N, SC_QZ);
-        k_pcg_update_p_decide<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
-            d_active.p, d_sc.p, p, z, nmem, d_niter.p, itmax, tol, d_loops.p, itmax + 2, d_done.p,
-            gh);
-        count(4);
+    if (pc == 2 && cbms.nblk && cbm1.nblk) {
+      // FP32 column-line PCG in two kernels per iteration: [p = z + beta p,
+      // q = A z + beta q, p.q, p.r] and [r, x update, z = T^-1 r, q.z, the
+      // decision and the next beta].  The same kernels run inside the
+      // Picard graph (phase 1: set-up, phase 2: the WHILE body) and launch
+      // by launch (phase 0).
+      if (!d_done.p || !d_loops.p || !d_niter.p || !d_nact.p || !d_nact_dummy.p)
+        throw std::string("PCG counters not allocated");
+      if (phase != 2) {
+        if (phase == 0) {
+          // (the graph path zeroes sc and the loop counter at its start)
+          CG_TRY(cudaMemsetAsync(d_sc.p, 0, sizeof(double) * nmem * SC_N, st));
+          CG_TRY(cudaMemsetAsync(d_loops.p, 0, sizeof(int32_t), st));
+          pdl_prev = false;
+        }
+        // x0 = 0: column-line factor with z = T^-1 b, r = b, x = 0 | |b|^2 |
+        // iteration counts, beta = 0
+        launch(k_pcg_setup_f32, cbms.nblk + cbm1.nblk + cdiv(nmem, kThreads), kThreads,
+               cbms.nblk, cbms.mem.p, cbms.r0.p, cbms.r1.p, cbm1.nblk, cbm1.mem.p, cbm1.r0.p,
+               cbm1.r1.p, (const uint8_t*)d_active.p, d_ms.p, d_diag.p, d_down.p, vals,
+               d_dmask.p, linv, lc, (const float*)b, r, x, z, d_sc.p, nmem, d_niter.p);
+        count();
+        if (lp_mode == 2) {
+          // learned factor for the members that use it, then z = T^-1 b again
+          k_line_setup_learned<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
+              d_active.p, d_lpuse.p, d_ms.p, d_down.p, (const float*)vals, d_dmask.p,
+              lpw.dprime, (float*)linv);
+          k_line_apply<VT><<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
+              d_active.p, d_ms.p, linv, lc, b, z, nullptr, d_sc.p, SC_N, SC_QZ);
+          count(2);
+        }
+        check_launch();
+        if (phase == 1) return;
       }
-      check_launch();
+      auto body = [&](int32_t* nact) {
+        spmv_upd_f32(vals, z, p, q, r);
+        launch(k_pcg_xz_f32, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p, d_active.p,
+               d_ms.p, d_sc.p, (const float*)linv, (const float*)lc, r, x, (const float*)p,
+               (const float*)q, z, (const uint8_t*)d_dmask.p, nmem, d_niter.p, itmax, tol,
+               d_loops.p, itmax + 2, d_done.p, nact, phase == 2 ? 1 : 0, gh);
+        count(2);
+      };
+      if (phase == 2) {
+        body(nullptr);
+        check_launch();
+        return;
+      }
+      if (chk < 1) chk = 1;
+      for (int it = 0; it < itmax + 2; ++it) {
+        const bool look = (it % chk == chk - 1 || it == itmax + 1);
+        if (lp_mode == 1 && it < kLpPairs) {
+          // Krylov pair (p, q = A p) of this iteration for the learned model
+          spmv_upd_f32(vals, z, p, q, r);
+          k_copy_cast<VT, float><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p,
+              cbm1.r1.p, d_active.p, p, d_P.p + (size_t)it * N, nullptr, 0);
+          k_copy_cast<VT, float><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p,
+              cbm1.r1.p, d_active.p, q, d_Q.p + (size_t)it * N, nullptr, 0);
+          launch(k_pcg_xz_f32, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+                 d_active.p, d_ms.p, d_sc.p, (const float*)linv, (const float*)lc, r, x,
+                 (const float*)p, (const float*)q, z, (const uint8_t*)d_dmask.p, nmem,
+                 d_niter.p, itmax, tol, d_loops.p, itmax + 2, d_done.p,
+                 look ? d_nact.p : d_nact_dummy.p, 0, gh);
+          count(4);
+        } else {
+          body(look ? d_nact.p : d_nact_dummy.p);
+        }
+        if (prof) lt_pending++;
+        check_launch();
+        if (look) {
+          int32_t nact = 0;
+          d_nact.download(&nact, 1, st);
+          CG_TRY(cudaStreamSynchronize(st));
+          if (prof && lt_pending > lt_cap - 2 * (itmax + 4)) prof_flush();
+          if (nact == 0) break;
+        }
+      }
       return;
     }
   }
@@ -3817,32 +4002,16 @@ void Engine::iteration_pre(int solve_phase) {
     // FP32 path: the Picard loop is the FP64 refinement loop (its residual is
     // FP64-grade, see the FP32 kernels); the inner FP32 PCG solves each
     // correction to opts.inner_tol.
-    if (solve_phase == 1) {
-      // graph: step actions + soil characteristics in one pass
-      k_start_vg_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
-          d_ms.p, nd, nf, d_nodal[ND_Z].p, need_sw_flag());
-    } else {
-      k_vg_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd, nf,
-                                              d_nodal[ND_Z].p);
-    }
+    // step actions + soil characteristics + Krylov member flags in one pass
+    launch(k_start_vg_f32, cbm1.nblk + cdiv(nmem, kThreads), kThreads, cbm1.nblk, cbm1.mem.p,
+           cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, nf, d_nodal[ND_Z].p, need_sw_flag(), nmem,
+           d_active.p);
     count();
-    if (solve_phase == 1) {
-      // graph: element means | BC fluxes | Krylov flags in one launch
-      k_pre2_f32<<<cbme.nblk + cbms.nblk + cdiv(nmem, kThreads), kThreads, 0, st>>>(
-          cbme.nblk, cbme.mem.p, cbme.r0.p, cbme.r1.p, cbms.nblk, cbms.mem.p, cbms.r0.p, cbms.r1.p,
-          nmem, d_act.p, d_tet.p, d_ms.p, nd, nf, d_active.p);
-      count();
-    } else {
-      k_elem_f32<<<cbme.nblk, kThreads, 0, st>>>(cbme.mem.p, cbme.r0.p, cbme.r1.p, d_act.p, d_tet.p, nf);
-      if (cbms.nblk)
-        k_bcflux_f32<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p,
-                                                     nd, nf.qneu, nf.bcf);
-      k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
-      count(3);
-    }
-    k_assemble_picard_f32<<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-        d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_islot.p, d_rec48.p,
-        d_dmask.p, nf, nf.bcf, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
+    launch(k_assemble_picard_f32, cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+           d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_islot.p, d_rec48.p,
+           d_dmask.p, nf, nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact,
+           (const double*)nd.atmold, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p,
+           d_gl.p);
     count();
     check_launch();
     if (lp_mode && solve_phase == 0) lp_before_solve();
@@ -3863,50 +4032,32 @@ void Engine::iteration_pre(int solve_phase) {
   }
 }
 
-void Engine::iteration_post(bool graph) {
+void Engine::iteration_post(bool fused) {
   const bool mixed = (precision == 1 && iopt == 1);
   const cathy_parm_t& P0 = M[0]->parm;
-  if (graph && mixed) {
-    // graph path (the result buffer was zeroed at the start of the graph):
-    // back-fluxes | head update + mass balance + norms | IKMAX + per-member
-    // records and switch flags; switching and STORE1 follow in the graph
-    const int nb = cbms16.nblk + cdiv((long)ndeep * kGroup, kThreads);
-    if (nb)
-      k_bkflux_all_f32<<<nb, kThreads, 0, st>>>(cbms16.nblk, cbms16.mem.p, cbms16.r0.p,
-          cbms16.r1.p, ndeep, d_deep.p, d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
-    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(1, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
-        d_ms.p, nd, nf, nf.volnod, nf.pnodi, d_red.p, d_redmax.p);
-    k_ikmax_post<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
-        d_redmax.p, d_ikmax.p, nmem, d_node_off.p, d_ikval.p, d_red.p, d_ms.p, P0.l2norm,
-        d_switch.p, d_done.p + 1);
-    count(3);
+  if (fused && mixed) {
+    // fused path (the result buffer was zeroed at the start of the
+    // iteration): head update + back-fluxes + mass balance + norms + IKMAX,
+    // the per-member pass by its last block; then switching and STORE1
+    launch(k_masbal_post_f32, cbm1.nblk, kThreads, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+           (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf, (const int32_t*)d_rowptr.p,
+           (const int32_t*)d_cols.p, (const float*)d_vals32.p, d_red.p, d_redmax.p, nmem,
+           (const int32_t*)d_node_off.p, d_ikmax.p, d_ikval.p, P0.l2norm, d_switch.p, d_done.p + 1);
+    launch(k_switch_store1_f32, cbm1.nblk, kThreads, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
+           d_switch.p, d_ms.p, nd, nf, d_red.p);
+    count(2);
     check_launch();
     return;
   }
-  if (mixed)
-    k_update_shl_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd,
-                                                    nf.pdiff);
-  else
-    k_update_shl<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd);
+  k_update_shl<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd);
   count();
   CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
   CG_TRY(cudaMemsetAsync(d_redmax.p, 0, sizeof(double) * nmem * 2, st));
   CG_TRY(cudaMemsetAsync(d_ikmax.p, 0, sizeof(int32_t) * nmem, st));
-  if (mixed) {
-    if (cbms16.nblk)
-      k_bkflux_f32<<<cbms16.nblk, kThreads, 0, st>>>(cbms16.mem.p, cbms16.r0.p, cbms16.r1.p,
-          d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
-    if (ndeep)
-      k_bkflux_list_f32<<<cdiv((long)ndeep * kGroup, kThreads), kThreads, 0, st>>>(ndeep, d_deep.p,
-          d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals32.p, nd, nf);
-    k_masbal_norms_f32<<<cbm1.nblk, kThreads, 0, st>>>(0, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
-        d_ms.p, nd, nf, nf.volnod, nf.pnodi, d_red.p, d_redmax.p);
-    count();
-  } else
-    k_masbal_norms<double><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_act.p,
-        d_ms.p, d_rowptr.p, d_cols.p, d_vals64.p, nd, d_red.p, d_redmax.p, iopt == 2);
+  k_masbal_norms<double><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+      d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_vals64.p, nd, d_red.p, d_redmax.p, iopt == 2);
   k_ikmax<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd, d_redmax.p,
-                                         d_ikmax.p, mixed ? 1 : 0);
+                                         d_ikmax.p, 0);
   k_gather_ik<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_node_off.p, d_ikmax.p, nd, d_ikval.p);
   k_switch_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, d_red.p, d_redmax.p, d_ms.p,
                                                   P0.l2norm, d_switch.p);
@@ -4071,8 +4222,6 @@ void Engine::pinned_alloc() {
   hp_ikmax = reinterpret_cast<int32_t*>(hp_res + res_off[4]);
   hp_ikv = hp_res + res_off[5];
   hp_nit = reinterpret_cast<int32_t*>(hp_res + res_off[6]);
-  d_done.alloc(2);
-  d_done.zero(st);
 }
 
 void Engine::pinned_free() {
@@ -4095,7 +4244,10 @@ void Engine::graph_build() {
   CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   CG_TRY(cudaMemcpyAsync(d_inbuf.p, hp_in, d_inbuf.n, cudaMemcpyHostToDevice, st));
   CG_TRY(cudaMemsetAsync(d_resbuf.p, 0, sizeof(double) * res_zero, st));
+  pdl_cap = true;
+  pdl_prev = false;
   iteration_pre(1);
+  pdl_cap = pdl_prev = false;
   cudaGraph_t gA = nullptr;
   CG_TRY(cudaStreamEndCapture(st, &gA));
   g_nA = launches - c0;
@@ -4114,18 +4266,21 @@ void Engine::graph_build() {
   CG_TRY(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   {
     const cathy_parm_t& P0 = M[0]->parm;
+    pdl_cap = true;
+    pdl_prev = false;
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
                             std::max(P0.tolcg, opts.inner_tol), true, 1, 2, h);
+    pdl_cap = pdl_prev = false;
   }
   CG_TRY(cudaStreamEndCapture(st, &body));
   g_nB = launches - c0;
   // C
   c0 = launches;
   CG_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  pdl_cap = true;
+  pdl_prev = false;
   iteration_post(true);
-  k_switch_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
-                                                      d_switch.p, d_ms.p, nd, nf, d_red.p);
-  count();
+  pdl_cap = pdl_prev = false;
   CG_TRY(cudaMemcpyAsync(hp_res, d_resbuf.p, sizeof(double) * res_off[7], cudaMemcpyDeviceToHost, st));
   cudaGraph_t gC = nullptr;
   CG_TRY(cudaStreamEndCapture(st, &gC));
@@ -4171,8 +4326,9 @@ int Engine::macro_iteration() {
   }
   const double *red, *redmax, *ikv, *scv;
   const int32_t *ikmax, *nit;
-  std::vector<double> v_red, v_redmax, v_ikv, v_scv;
+  std::vector<double> v_red, v_redmax, v_ikv, v_scv, v_res;
   std::vector<int32_t> v_ikmax, v_nit;
+  const bool mixed = (precision == 1 && iopt == 1);
   auto t1 = clk::now();
   if (graph) {
     const int key[6] = {cbm1.nblk, cbm16.nblk, cbme.nblk, cbms.nblk, cbms16.nblk, prof ? 1 : 0};
@@ -4204,6 +4360,23 @@ int Engine::macro_iteration() {
       if (lt_pending > lt_cap - 2 * (opts.inner_maxit + 8)) prof_flush();
     }
     red = hp_red; redmax = hp_redmax; ikv = hp_ikv; scv = hp_sc; ikmax = hp_ikmax; nit = hp_nit;
+  } else if (mixed && niter_members > 0) {
+    // the graph's kernels launched one by one (the same kernels, in the
+    // same order, with the PCG loop driven from the host)
+    CG_TRY(cudaMemsetAsync(d_resbuf.p, 0, sizeof(double) * res_zero, st));
+    pdl_cap = pdl_prev = false;
+    iteration_pre(0);
+    iteration_post(true);
+    v_res.resize(res_off[7]);
+    d_resbuf.download(v_res.data(), res_off[7], st);
+    CG_TRY(cudaStreamSynchronize(st));
+    const double* b = v_res.data();
+    scv = b + res_off[0];
+    red = b + res_off[2];
+    redmax = b + res_off[3];
+    ikmax = reinterpret_cast<const int32_t*>(b + res_off[4]);
+    ikv = b + res_off[5];
+    nit = reinterpret_cast<const int32_t*>(b + res_off[6]);
   } else {
     start_kernels();
     if (niter_members == 0) {
@@ -4292,7 +4465,7 @@ int Engine::macro_iteration() {
     // STORE1 (storcal.f) at the converged heads: the graph computed it for
     // every iterating member; the kernel-by-kernel path computes it now
     const double* st1 = red;
-    if (!graph) {
+    if (!graph && !mixed) {
       d_mask2.upload(conv_mask.data(), nmem, st);
       CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
       if (precision == 1 && iopt == 1)
@@ -4557,14 +4730,10 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   if (mixed) {
     k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->nd, e->nf,
                                                   e->d_nodal[ND_Z].p);
-    k_elem_f32<<<e->bme.nblk, kThreads, 0, e->st>>>(e->bme.mem.p, e->bme.r0.p, e->bme.r1.p, e->d_act.p,
-                                                    e->d_tet.p, e->nf);
-    k_bcflux_f32<<<e->bms.nblk, kThreads, 0, e->st>>>(e->bms.mem.p, e->bms.r0.p, e->bms.r1.p, e->d_act.p,
-        e->d_ms.p, e->nd, e->nf.qneu, e->nf.bcf);
     k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
         e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_islot.p,
-        e->d_rec48.p, e->d_dmask.p, e->nf, e->nf.bcf, e->d_vals32.p, (float)e->lm_d, (float)e->lm_o,
-        e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
+        e->d_rec48.p, e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold,
+        e->d_vals32.p, (float)e->lm_d, (float)e->lm_o, e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
   } else {
     k_vg<double><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->iopt == 2);
     e->assemble<double>();
