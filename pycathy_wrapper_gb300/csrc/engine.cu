@@ -821,7 +821,7 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
 // p = z + beta p and q = A z + beta q (= A p, as q holds A p_old), beta per
 // member in sc[SC_BETA] (beta = 0: p = z, q = A z); the dots are then p.q
 // and p.w.
-constexpr int kStreamWarps = 4;
+constexpr int kStreamWarps = 8;
 template <bool kUpd>
 __global__ void __launch_bounds__(32 * kStreamWarps)
 k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
@@ -915,11 +915,39 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
     }
     __syncwarp();
   }
-  if (acc && cur >= 0) {
+  if (acc) {
+    // the warps' last partial sums, merged per block: the warps take
+    // interleaved entries of the block's contiguous run and usually end on
+    // the same member, so a block issues one FP64 atomic per quantity (a
+    // small member otherwise sees thousands of same-address atomics)
+    __shared__ int s_cur[kStreamWarps];
+    __shared__ float s_a0[kStreamWarps], s_a1[kStreamWarps];
     const float a0 = warp_sum_t<float>(d0), a1 = warp_sum_t<float>(d1);
     if (lane == 0) {
-      if (a0 != 0.0f) atomicAdd(acc + (size_t)cur * acc_stride, (double)a0);
-      if (a1 != 0.0f) atomicAdd(acc + (size_t)cur * acc_stride + 1, (double)a1);
+      s_cur[wp] = cur;
+      s_a0[wp] = a0;
+      s_a1[wp] = a1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int mc = -1;
+      double t0 = 0.0, t1 = 0.0;
+      for (int q = 0; q <= kStreamWarps; ++q) {
+        const int mq = q < kStreamWarps ? s_cur[q] : -1;
+        if (q < kStreamWarps && mq < 0) continue;
+        if (mq != mc) {
+          if (mc >= 0) {
+            if (t0 != 0.0) atomicAdd(acc + (size_t)mc * acc_stride, t0);
+            if (t1 != 0.0) atomicAdd(acc + (size_t)mc * acc_stride + 1, t1);
+          }
+          mc = mq;
+          t0 = t1 = 0.0;
+        }
+        if (q < kStreamWarps) {
+          t0 += (double)s_a0[q];
+          t1 += (double)s_a1[q];
+        }
+      }
     }
   }
   if (alg_bytes) {
@@ -2778,8 +2806,9 @@ struct Engine {
   int grid_persist(int nblk) const { return std::max(1, std::min(nblk, persist_blocks)); }
   int grid_spmv(int nblk) const { return std::max(1, std::min(nblk, 2 * persist_blocks)); }
   int grid_stream() const {
+    // one warp per map entry up to one resident wave of 256-thread blocks
     return std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps,
-                                2 * persist_blocks));
+                                persist_blocks));
   }
   // q = A p with the fused dots p.q, p.r (FP32 stream kernel)
   void spmv_f32(const float* vals, const float* p, float* q, const float* r) {
