@@ -816,13 +816,15 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
 // FP64 atomic per quantity whenever the warp's member changes.  Timing and
 // byte accounting as in k_spmv.
 //
-// kUpd (the PCG direction update fused into the product): x is the
-// preconditioned residual z, and for its own rows the kernel forms
+// kMode kSpmvUpd (the PCG direction update fused into the product): x is
+// the preconditioned residual z, and for its own rows the kernel forms
 // p = z + beta p and q = A z + beta q (= A p, as q holds A p_old), beta per
 // member in sc[SC_BETA] (beta = 0: p = z, q = A z); the dots are then p.q
-// and p.w.
+// and p.w.  kSpmvResid: y = w - A x at the rows that are not Dirichlet rows
+// and 0 at those (the masked residual, w = b), no dots.
+enum { kSpmvPlain = 0, kSpmvUpd = 1, kSpmvResid = 2 };
 constexpr int kStreamWarps = 8;
-template <bool kUpd>
+template <int kMode>
 __global__ void __launch_bounds__(32 * kStreamWarps)
 k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
               const uint8_t* active, const int32_t* __restrict__ rowptr,
@@ -875,8 +877,9 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
     const int sbeg = __shfl_sync(0xffffffffu, rp, 0);
     const int send = __shfl_sync(0xffffffffu, rp, nr);
     if (alg_bytes && lane == 0)
-      bytes += (double)(send - sbeg) * 8.0 + nr * (kUpd ? 28.0 : 4.0 + (w ? 3.0 : 2.0) * 4.0);
-    const float beta = kUpd ? (float)sc[(size_t)m * SC_N + SC_BETA] : 0.0f;
+      bytes += (double)(send - sbeg) * 8.0 +
+               nr * (kMode == kSpmvUpd ? 28.0 : 4.0 + (w ? 3.0 : 2.0) * 4.0);
+    const float beta = kMode == kSpmvUpd ? (float)sc[(size_t)m * SC_N + SC_BETA] : 0.0f;
     // 16-byte vectors covering [sbeg, send)
     const int v0 = sbeg >> 2, v1 = (send + 3) >> 2;
     for (int v = v0 + lane; v < v1; v += 32) {
@@ -898,20 +901,24 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
       float sum = 0.0f;
       for (int k = rlo; k < rhi; ++k) sum += sp[k - sbeg];
       const int i = r0 + lane;
-      const float xi = x[i];
       const bool dm = dmask[i] != 0;
-      float yi = dm ? xi : sum;
-      float pi = xi;
-      if (kUpd) {
-        if (beta != 0.0f) {
-          pi = xi + beta * pv[i];
-          yi = dm ? pi : yi + beta * y[i];
+      if (kMode == kSpmvResid) {
+        y[i] = dm ? 0.0f : w[i] - sum;
+      } else {
+        const float xi = x[i];
+        float yi = dm ? xi : sum;
+        float pi = xi;
+        if (kMode == kSpmvUpd) {
+          if (beta != 0.0f) {
+            pi = xi + beta * pv[i];
+            yi = dm ? pi : yi + beta * y[i];
+          }
+          pv[i] = pi;
         }
-        pv[i] = pi;
+        y[i] = yi;
+        d0 += pi * yi;
+        if (w) d1 += pi * w[i];
       }
-      y[i] = yi;
-      d0 += pi * yi;
-      if (w) d1 += pi * w[i];
     }
     __syncwarp();
   }
@@ -2342,17 +2349,18 @@ __global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
 // unchanged body of the corresponding kernel.
 // ============================================================================
 
-// PCG set-up with x0 = 0, one launch: per vertical column the column-line
-// factor (pivot inverses and masked vertical couplings, as k_line_setup_b)
-// and, in the same sweeps, z = T^-1 b, r = b, x = 0 | |b_masked|^2 per
-// member | iteration counts = 1 and beta = 0 (first direction p = z).
+// PCG set-up, first launch: per vertical column the column-line factor
+// (pivot inverses and masked vertical couplings, as k_line_setup_b) and, in
+// the same sweeps, x0 = T^-1 b (the reference's starting guess M^-1 b) |
+// |b_masked|^2 per member | iteration counts = 1 and beta = 0 (first
+// direction p = z).  r = b - A x0 and z = T^-1 r follow.
 __global__ void __launch_bounds__(kThreads)
 k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1, int nc,
                 const int32_t* c_mem, const int32_t* c_r0, const int32_t* c_r1,
                 const uint8_t* active, const MemberScal* ms, const int32_t* __restrict__ diag,
                 const int32_t* __restrict__ down, const float* __restrict__ vals,
                 const uint8_t* __restrict__ dmask, float* pinv, float* cdown,
-                const float* __restrict__ b, float* r, float* x, float* z, double* sc, int nmem,
+                const float* __restrict__ b, float* x, double* sc, int nmem,
                 int32_t* niter) {
   pdl_enter();
   int bb = blockIdx.x;
@@ -2413,9 +2421,7 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
         cdown[i] = c[j];
         // forward substitution with the previous layer's factor entries
         const float yk = bv[j] - c_prev * yprev * pv_prev;
-        z[i] = yk;
-        r[i] = bv[j];
-        x[i] = 0.0f;
+        x[i] = yk;
         yprev = yk;
         pv_prev = pv;
         piv_prev = piv;
@@ -2432,7 +2438,7 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
       yy[j] = pv[j] = cd[j] = 0.0f;
       if (k >= 0) {
         const int i = top + k * nnod;
-        yy[j] = z[i]; pv[j] = pinv[i]; cd[j] = cdown[i];
+        yy[j] = x[i]; pv[j] = pinv[i]; cd[j] = cdown[i];
       }
     }
 #pragma unroll
@@ -2440,7 +2446,7 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
       const int k = k1 - j;
       if (k >= 0) {
         const float zk = (yy[j] - cd[j] * znext) * pv[j];
-        z[top + k * nnod] = zk;
+        x[top + k * nnod] = zk;
         znext = zk;
       }
     }
@@ -2812,14 +2818,21 @@ struct Engine {
   }
   // q = A p with the fused dots p.q, p.r (FP32 stream kernel)
   void spmv_f32(const float* vals, const float* p, float* q, const float* r) {
-    launch(k_spmv_stream<false>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+    launch(k_spmv_stream<kSpmvPlain>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
            (float*)nullptr, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
            prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
   }
+  // r = b - A x (masked)
+  void resid_f32(const float* vals, const float* x, const float* b, float* r) {
+    launch(k_spmv_stream<kSpmvResid>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+           cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, x, r, b,
+           (float*)nullptr, (const double*)d_sc.p, (double*)nullptr, (int)SC_N,
+           (double*)nullptr, (unsigned long long*)nullptr, 0);
+  }
   // p = z + beta p, q = A z + beta q (= A p) with the fused dots p.q, p.r
   void spmv_upd_f32(const float* vals, const float* z, float* p, float* q, const float* r) {
-    launch(k_spmv_stream<true>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+    launch(k_spmv_stream<kSpmvUpd>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, z, q, r,
            p, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
            prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
@@ -3743,22 +3756,27 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
           CG_TRY(cudaMemsetAsync(d_loops.p, 0, sizeof(int32_t), st));
           pdl_prev = false;
         }
-        // x0 = 0: column-line factor with z = T^-1 b, r = b, x = 0 | |b|^2 |
-        // iteration counts, beta = 0
+        // column-line factor with x0 = T^-1 b | |b|^2 | iteration counts,
+        // beta = 0; then r = b - A x0 and z = T^-1 r
         launch(k_pcg_setup_f32, cbms.nblk + cbm1.nblk + cdiv(nmem, kThreads), kThreads,
                cbms.nblk, cbms.mem.p, cbms.r0.p, cbms.r1.p, cbm1.nblk, cbm1.mem.p, cbm1.r0.p,
                cbm1.r1.p, (const uint8_t*)d_active.p, d_ms.p, d_diag.p, d_down.p, vals,
-               d_dmask.p, linv, lc, (const float*)b, r, x, z, d_sc.p, nmem, d_niter.p);
+               d_dmask.p, linv, lc, (const float*)b, x, d_sc.p, nmem, d_niter.p);
         count();
         if (lp_mode == 2) {
-          // learned factor for the members that use it, then z = T^-1 b again
+          // learned factor for the members that use it, then x0 = T^-1 b again
           k_line_setup_learned<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
               d_active.p, d_lpuse.p, d_ms.p, d_down.p, (const float*)vals, d_dmask.p,
               lpw.dprime, (float*)linv);
           k_line_apply<VT><<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p,
-              d_active.p, d_ms.p, linv, lc, b, z, nullptr, d_sc.p, SC_N, SC_QZ);
+              d_active.p, d_ms.p, linv, lc, b, x, nullptr, d_sc.p, SC_N, SC_QZ);
           count(2);
         }
+        resid_f32(vals, x, b, r);
+        launch(k_line_apply<VT>, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+               d_active.p, d_ms.p, linv, lc, (const VT*)r, z, (const VT*)nullptr, d_sc.p,
+               (int)SC_N, (int)SC_QZ);
+        count(2);
         check_launch();
         if (phase == 1) return;
       }
