@@ -2078,7 +2078,13 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
       const int e = ek >> 2, k = ek & 3;
       const float4* rv = rec48 + 3 * (size_t)e;
       const float4 r0 = rv[0], r1 = rv[1], r2 = rv[2];
-      const float Sv[10] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y};
+      // row k of the packed symmetric 4x4 stiffness shape (S[sym_idx(k, l)]),
+      // selected with constant indices
+      const float srow[4] = {
+          k == 0 ? r0.x : k == 1 ? r0.y : k == 2 ? r0.z : r0.w,
+          k == 0 ? r0.y : k == 1 ? r1.x : k == 2 ? r1.y : r1.z,
+          k == 0 ? r0.z : k == 1 ? r1.y : k == 2 ? r1.w : r2.x,
+          k == 0 ? r0.w : k == 1 ? r1.z : k == 2 ? r2.x : r2.y};
       const float vol = r2.z, vpel = r2.w;
       const float2 n0 = sk2[grp][isl & 15], n1 = sk2[grp][(isl >> 4) & 15],
                    n2 = sk2[grp][(isl >> 8) & 15], n3 = sk2[grp][(isl >> 12) & 15];
@@ -2088,7 +2094,7 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
 #pragma unroll
       for (int l = 0; l < 4; ++l) {
         const float lm = (l == k) ? lm_d : lm_o;
-        const float skl = Sv[sym_idx(k, l)];
+        const float skl = srow[l];
         float c = th * (kr * skl) + ve1 * lm * rdt;
         if (l == k) {
           c += vpel * lm_d * et2i * rdt;
