@@ -806,6 +806,57 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
   }
 }
 
+// Entry list of the members still in the Krylov solve, built by one block:
+// for the j-th member of the compacted maps (amem_cum: member ids, then per
+// map the cumulative entry counts, na at [nmem]) whose Krylov flag is set,
+// its run of 16-row map entries [cum16[j], cum16[j+1]) becomes one segment:
+// kfirst[s] = its first entry, kcum[s] = the entries before it.  The
+// product of the PCG loop spreads the listed entries evenly over its grid,
+// so members that are still iterating are not left to the few blocks that
+// hold their part of the map.
+__device__ void build_kact(const int32_t* amem_cum, int nmem, const uint8_t* active,
+                           int32_t* kact) {
+  const int32_t* amem = amem_cum;
+  const int na = min(max(amem_cum[nmem], 0), nmem);
+  const int32_t* cum16 = amem_cum + 2 * (nmem + 1);
+  int32_t* kcum = kact + 1;
+  int32_t* kfirst = kact + nmem + 2;
+  constexpr int kW = kThreads / 32;
+  __shared__ int s_ws[2 * kW];
+  __shared__ int s_base[2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) { s_base[0] = 0; s_base[1] = 0; }
+  __syncthreads();
+  for (int j0 = 0; j0 < na; j0 += kThreads) {
+    const int j = j0 + threadIdx.x;
+    int cnt = 0, f = 0;
+    if (j < na && active[amem[j]]) {
+      f = cum16[j];
+      cnt = cum16[j + 1] - f;
+    }
+    const int flag = cnt > 0 ? 1 : 0;
+    int sf = flag, sn = cnt;  // inclusive warp scans
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t1 = __shfl_up_sync(0xffffffffu, sf, o), t2 = __shfl_up_sync(0xffffffffu, sn, o);
+      if (lane >= o) { sf += t1; sn += t2; }
+    }
+    if (lane == 31) { s_ws[w] = sf; s_ws[kW + w] = sn; }
+    __syncthreads();
+    int pf = 0, pn = 0;
+    for (int q = 0; q < w; ++q) { pf += s_ws[q]; pn += s_ws[kW + q]; }
+    const int ef = s_base[0] + pf + sf - flag, en = s_base[1] + pn + sn - cnt;
+    if (flag) { kfirst[ef] = f; kcum[ef] = en; }
+    __syncthreads();
+    if (threadIdx.x == kThreads - 1) { s_base[0] = ef + flag; s_base[1] = en + cnt; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    kact[0] = s_base[0];
+    kcum[s_base[0]] = s_base[1];
+  }
+}
+
 // FP32 y = A x as a stream over each map entry's slots: one warp per entry
 // (16 consecutive rows of one member, their slots contiguous in vals/cols),
 // the lanes read the entry's values and columns with 16-byte vector loads,
@@ -825,13 +876,14 @@ k_spmv(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_
 enum { kSpmvPlain = 0, kSpmvUpd = 1, kSpmvResid = 2 };
 constexpr int kStreamWarps = 8;
 template <int kMode>
-__global__ void __launch_bounds__(32 * kStreamWarps)
+__global__ void __launch_bounds__(32 * kStreamWarps, 8)
 k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
               const uint8_t* active, const int32_t* __restrict__ rowptr,
               const int32_t* __restrict__ cols, const float* __restrict__ vals,
               const uint8_t* __restrict__ dmask, const float* __restrict__ x, float* y,
               const float* __restrict__ w, float* pv, const double* sc, double* acc,
-              int acc_stride, double* alg_bytes, unsigned long long* lt, int lt_cap) {
+              int acc_stride, double* alg_bytes, unsigned long long* lt, int lt_cap,
+              const int32_t* kact, const int32_t* kfirst) {
   pdl_enter();
   __shared__ int s_slot;
   __shared__ double s_bytes;
@@ -854,10 +906,40 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
   float d0 = 0.0f, d1 = 0.0f;
   int cur = -1;
   double bytes = 0.0;
-  // each block takes a contiguous run of entries; its warps interleave
-  const int chunk = (nblk + gridDim.x - 1) / gridDim.x;
-  const int b0 = blockIdx.x * chunk, b1 = min(nblk, b0 + chunk);
-  for (int b = b0 + wp; b < b1; b += kStreamWarps) {
+  // each block takes a contiguous run of entries (kSpmvUpd: of the listed
+  // entries of the members still in the Krylov solve); its warps interleave
+  int total = nblk, nseg = 0;
+  const int32_t* kcum = kact + 1;
+  if (kMode == kSpmvUpd) {
+    nseg = kact[0];
+    total = kcum[nseg];
+  }
+  // (the list is built before every product of the loop: nseg <= members)
+  const int chunk = (total + gridDim.x - 1) / gridDim.x;
+  const int b0 = blockIdx.x * chunk, b1 = min(total, b0 + chunk);
+  // the warp's current segment: its end and entry offset live in registers
+  int seg = 0, seg_end = 0, delta = 0;
+  if (kMode == kSpmvUpd && b0 + wp < b1) {
+    // last segment starting at or before the warp's first listed entry
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (kcum[mid] <= b0 + wp) lo = mid; else hi = mid - 1;
+    }
+    seg = lo;
+    seg_end = kcum[seg + 1];
+    delta = kfirst[seg] - kcum[seg];
+  }
+  for (int g = b0 + wp; g < b1; g += kStreamWarps) {
+    int b = g;
+    if (kMode == kSpmvUpd) {
+      while (g >= seg_end) {  // warp-uniform
+        ++seg;
+        seg_end = kcum[seg + 1];
+        delta = kfirst[seg] - kcum[seg];
+      }
+      b = g + delta;
+    }
     const int m = bm_mem[b];
     if (!active[m]) continue;  // warp-uniform
     if (acc && m != cur) {
@@ -2367,7 +2449,7 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
                 const int32_t* __restrict__ down, const float* __restrict__ vals,
                 const uint8_t* __restrict__ dmask, float* pinv, float* cdown,
                 const float* __restrict__ b, float* x, double* sc, int nmem,
-                int32_t* niter) {
+                int32_t* niter, const int32_t* amem_cum, int32_t* kact) {
   pdl_enter();
   int bb = blockIdx.x;
   if (bb >= ns) {
@@ -2382,6 +2464,7 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
       niter[m] = 1;
       sc[(size_t)m * SC_N + SC_BETA] = 0.0;
     }
+    if (bb == 0) build_kact(amem_cum, nmem, active, kact);  // the first block of this part
     return;
   }
   const int m = s_mem[bb];
@@ -2473,7 +2556,8 @@ k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
              const float* __restrict__ cdown, float* r, float* x, const float* __restrict__ p,
              const float* __restrict__ q, float* z, const uint8_t* __restrict__ dmask, int nmem,
              int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
-             unsigned int* done, int32_t* nact, int use_cond, cudaGraphConditionalHandle h) {
+             unsigned int* done, int32_t* nact, int use_cond, cudaGraphConditionalHandle h,
+             const int32_t* amem_cum, int32_t* kact) {
   pdl_enter();
   const int m = bm_mem[blockIdx.x];
   if (active[m]) {  // block-uniform
@@ -2569,6 +2653,7 @@ k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
   }
   if (mine) atomicAdd(&s_cnt, mine);
   __syncthreads();
+  build_kact(amem_cum, nmem, active, kact);
   if (threadIdx.x == 0) {
     *done = 0u;
     const int l = *loops + 1;
@@ -2706,6 +2791,9 @@ struct Engine {
   std::vector<int32_t> nblk1, nblk16, nblke, nblks, nblks16;  // blocks per member
   std::vector<int32_t> first1, first16, firste, firsts, firsts16;
   DBuf<int32_t> d_first, d_amem_cum;
+  // entry list of the members still in the Krylov solve: [0] segments,
+  // [1 .. nmem+1] cumulative entry counts, [nmem+2 ..] segment starts
+  DBuf<int32_t> d_kact;
   std::vector<uint8_t> last_active;
   DBuf<int32_t> d_deep;  // static Dirichlet rows below the surface
   int ndeep = 0;
@@ -2827,21 +2915,24 @@ struct Engine {
     launch(k_spmv_stream<kSpmvPlain>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
            (float*)nullptr, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
-           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap,
+           (const int32_t*)d_kact.p, (const int32_t*)d_kact.p);
   }
   // r = b - A x (masked)
   void resid_f32(const float* vals, const float* x, const float* b, float* r) {
     launch(k_spmv_stream<kSpmvResid>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, x, r, b,
            (float*)nullptr, (const double*)d_sc.p, (double*)nullptr, (int)SC_N,
-           (double*)nullptr, (unsigned long long*)nullptr, 0);
+           (double*)nullptr, (unsigned long long*)nullptr, 0, (const int32_t*)d_kact.p,
+           (const int32_t*)d_kact.p);
   }
   // p = z + beta p, q = A z + beta q (= A p) with the fused dots p.q, p.r
   void spmv_upd_f32(const float* vals, const float* z, float* p, float* q, const float* r) {
     launch(k_spmv_stream<kSpmvUpd>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, z, q, r,
            p, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
-           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap);
+           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap,
+           (const int32_t*)d_kact.p, (const int32_t*)(d_kact.p + nmem + 2));
   }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class MT> void assemble();
@@ -3529,7 +3620,14 @@ void Engine::init_compaction() {
   d_first.alloc(fst.size());
   d_first.upload(fst.data(), fst.size(), st);
   d_amem_cum.alloc((size_t)6 * (nmem + 1));
-  last_active.assign(nmem, 1);
+  d_amem_cum.zero(st);
+  d_kact.alloc((size_t)2 * nmem + 2);
+  d_kact.zero(st);
+  // compacted maps and per-member offsets for "every member has work" (the
+  // offsets are read on the device, so they are written here, not only when
+  // the set of members with work changes)
+  last_active.assign(nmem, 0);
+  compact_maps(std::vector<uint8_t>(nmem, 1));
 }
 
 void Engine::compact_maps(const std::vector<uint8_t>& memact) {
@@ -3552,8 +3650,10 @@ void Engine::compact_maps(const std::vector<uint8_t>& memact) {
       hostbuf[(size_t)(q + 1) * (nmem + 1) + j] = acc;
       acc += (*counts[q])[amem[j]];
     }
+    hostbuf[(size_t)(q + 1) * (nmem + 1) + na] = acc;
     tot[q] = acc;
   }
+  hostbuf[nmem] = na;  // read on the device (the Krylov entry lists)
   d_amem_cum.upload(hostbuf.data(), hostbuf.size(), st);
   const BlockMap* full[5] = {&bm1, &bm16, &bme, &bms, &bms16};
   BlockMap* comp[5] = {&cbm1, &cbm16, &cbme, &cbms, &cbms16};
@@ -3767,7 +3867,8 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
         launch(k_pcg_setup_f32, cbms.nblk + cbm1.nblk + cdiv(nmem, kThreads), kThreads,
                cbms.nblk, cbms.mem.p, cbms.r0.p, cbms.r1.p, cbm1.nblk, cbm1.mem.p, cbm1.r0.p,
                cbm1.r1.p, (const uint8_t*)d_active.p, d_ms.p, d_diag.p, d_down.p, vals,
-               d_dmask.p, linv, lc, (const float*)b, x, d_sc.p, nmem, d_niter.p);
+               d_dmask.p, linv, lc, (const float*)b, x, d_sc.p, nmem, d_niter.p,
+               (const int32_t*)d_amem_cum.p, d_kact.p);
         count();
         if (lp_mode == 2) {
           // learned factor for the members that use it, then x0 = T^-1 b again
@@ -3791,7 +3892,8 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
         launch(k_pcg_xz_f32, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p, d_active.p,
                d_ms.p, d_sc.p, (const float*)linv, (const float*)lc, r, x, (const float*)p,
                (const float*)q, z, (const uint8_t*)d_dmask.p, nmem, d_niter.p, itmax, tol,
-               d_loops.p, itmax + 2, d_done.p, nact, phase == 2 ? 1 : 0, gh);
+               d_loops.p, itmax + 2, d_done.p, nact, phase == 2 ? 1 : 0, gh,
+               (const int32_t*)d_amem_cum.p, d_kact.p);
         count(2);
       };
       if (phase == 2) {
@@ -3813,7 +3915,8 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
                  d_active.p, d_ms.p, d_sc.p, (const float*)linv, (const float*)lc, r, x,
                  (const float*)p, (const float*)q, z, (const uint8_t*)d_dmask.p, nmem,
                  d_niter.p, itmax, tol, d_loops.p, itmax + 2, d_done.p,
-                 look ? d_nact.p : d_nact_dummy.p, 0, gh);
+                 look ? d_nact.p : d_nact_dummy.p, 0, gh, (const int32_t*)d_amem_cum.p,
+                 d_kact.p);
           count(4);
         } else {
           body(look ? d_nact.p : d_nact_dummy.p);
