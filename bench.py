@@ -24,7 +24,10 @@ the whole ensemble day from the initial condition.
             bandwidth.
   cpu_baseline  the CPU oracle (serial C++ restatement of the reference
             Fortran) on a bounded sample: the first 16 members for their first
-            simulated hour, one process per host core.
+            2 simulated hours, one process per host core (about a minute on 16
+            Arm cores; the day's throughput varies strongly with simulated
+            time, and the first half hour or hour alone overstates the CPU's
+            whole-day throughput several-fold).
 
 --impl reference runs the CPU restatement of the reference's solver on the
 host cores (the Fortran reference cannot be built: no Fortran compiler) on a
@@ -199,8 +202,11 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     nsample = min(args.cpu_members, args.members)
     vals, walls = [], []
+    # warm-up steps (process start-up, page cache) run a short sample; the
+    # timed steps run the bounded sample itself
     for i in range(args.warmup + args.steps):
-        v, wall, sim = cpu_sample(args.members, 0, args.cpu_tmax, nsample, cores)
+        tmax = args.cpu_tmax if i >= args.warmup else min(args.cpu_tmax, 300.0)
+        v, wall, sim = cpu_sample(args.members, 0, tmax, nsample, cores)
         if i >= args.warmup:
             vals.append(v)
             walls.append(wall)
@@ -236,7 +242,7 @@ def main():
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--tmax", type=float, default=86400.0)
     ap.add_argument("--cpu-members", type=int, default=16)
-    ap.add_argument("--cpu-tmax", type=float, default=3600.0,
+    ap.add_argument("--cpu-tmax", type=float, default=7200.0,
                     help="simulated seconds per member in the bounded CPU sample")
     ap.add_argument("--plain-members", type=int, default=4)
     ap.add_argument("--no-graphs", action="store_true")
