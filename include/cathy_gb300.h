@@ -147,6 +147,10 @@ int32_t cathy_gb300_get_state(void* handle, int32_t m, double* pnew,
                               double* time, double* deltat, int32_t* status);
 int32_t cathy_gb300_set_state(void* handle, int32_t m, const double* ptimep,
                               double time, double deltat);
+/* water saturation of member m at its current heads (n values, FP64): the
+ * SW array that DETOUT writes to the sw output file (detout.f:44-45),
+ * VGPNOT*Se(PNEW) + VGRMC/PNODI as CHNEW forms it */
+int32_t cathy_gb300_get_saturation(void* handle, int32_t m, double* sw);
 int32_t cathy_gb300_num_records(void* handle, int32_t m, int32_t* niter_recs,
                                 int32_t* nstep_recs);
 int32_t cathy_gb300_get_records(void* handle, int32_t m,

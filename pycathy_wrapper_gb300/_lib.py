@@ -98,6 +98,7 @@ EXPORTS = {
     "cathy_gb300_step": (C.c_int32, [C.c_void_p, i32p]),
     "cathy_gb300_run": (C.c_int32, [C.c_void_p, C.c_int32, i32p]),
     "cathy_gb300_get_state": (C.c_int32, [C.c_void_p, C.c_int32, f64p, f64p, f64p, i32p]),
+    "cathy_gb300_get_saturation": (C.c_int32, [C.c_void_p, C.c_int32, f64p]),
     "cathy_gb300_set_state": (C.c_int32, [C.c_void_p, C.c_int32, f64p, C.c_double,
                                           C.c_double]),
     "cathy_gb300_num_records": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p]),

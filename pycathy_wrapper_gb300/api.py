@@ -148,6 +148,13 @@ class Simulation:
                                            C.byref(stt)), "get_state")
         return p, t.value, dt.value, stt.value
 
+    def saturation(self, m: int = 0):
+        """Water saturation of member m at its current heads (the SW array of
+        the reference's ``sw`` output, detout.f:44-45)."""
+        sw = np.zeros(self.sizes[m]["n"])
+        check(self.L.cathy_gb300_get_saturation(self.h, m, _ptr(sw, f64p)), "get_saturation")
+        return sw
+
     def set_state(self, m: int, ptimep, time: float, deltat: float):
         p = _f64(ptimep)
         check(self.L.cathy_gb300_set_state(self.h, m, _ptr(p, f64p), time, deltat), "set_state")

@@ -95,6 +95,11 @@ int32_t cathy_gb300_get_state(void* h, int32_t m, double* pnew, double* time,
   return guarded([&]() { return engine_get_state((Engine*)h, m, pnew, time, deltat, status); });
 }
 
+int32_t cathy_gb300_get_saturation(void* h, int32_t m, double* sw) {
+  if (!h || !sw) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_get_saturation((Engine*)h, m, sw); });
+}
+
 int32_t cathy_gb300_set_state(void* h, int32_t m, const double* ptimep, double time,
                               double deltat) {
   if (!h || !ptimep) return CATHY_GB300_EINVAL;

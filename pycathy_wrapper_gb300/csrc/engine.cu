@@ -2358,29 +2358,6 @@ k_masbal_post_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm
 
 
 
-// STORE1 for the FP32 path: Sw(PNEW) in FP32, compensated sums.
-__device__ __forceinline__ void k_store1_f32_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
-                             const int32_t* bm_r1, const uint8_t* mask, Nodal nd,
-                             NodalF nf, double* red) {
-  const int m = bm_mem[bid_];
-  if (!mask[m]) return;
-  const int i = bm_r0[bid_] + threadIdx.x;
-  FF v[1] = {FF{0.0f, 0.0f}};
-  if (i < bm_r1[bid_]) {
-    const double p = nd.pnew[i];
-    float se = 1.0f;
-    if (p < -1.0e-14) se = expf(-nf.vgm[i] * log1pf(vgf_beta((float)p, nf.vgpsat[i], nf.vgn[i])));
-    const float sw = nf.vgpnot[i] * se + nf.rmcp[i];
-    v[0].hi = sw * nf.volnod[i] * nf.pnodi[i];
-  }
-  block_accumulate_ff<1>(v, red + (size_t)m * RD_NUM + RD_STORE1);
-}
-__global__ void k_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
-                             const int32_t* bm_r1, const uint8_t* mask, Nodal nd,
-                             NodalF nf, double* red) {
-  k_store1_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, mask, nd, nf, red);
-}
-
 // FP32 copies of the nodal van Genuchten parameters (after CHPARM)
 __global__ void k_params_f32(int n, Nodal nd, NodalF nf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2687,15 +2664,6 @@ __global__ void k_switch_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
     v[0].hi = swv * nf.volnod[i] * nf.pnodi[i];
   }
   block_accumulate_ff<1>(v, red + (size_t)m * RD_NUM + RD_STORE1);
-}
-
-// STORE1 of every member whose action bits include ACT_ITER
-__global__ void k_store1_iter_f32(const int32_t* bm_mem, const int32_t* bm_r0,
-                                  const int32_t* bm_r1, const uint8_t* act, Nodal nd, NodalF nf,
-                                  double* red) {
-  const int m = bm_mem[blockIdx.x];
-  if (!(act[m] & ACT_ITER)) return;
-  k_store1_f32_b(blockIdx.x, bm_mem, bm_r0, bm_r1, act, nd, nf, red);
 }
 
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
@@ -4620,16 +4588,14 @@ int Engine::macro_iteration() {
     }
   }
   if (any_conv) {
-    // STORE1 (storcal.f) at the converged heads: the graph computed it for
-    // every iterating member; the kernel-by-kernel path computes it now
+    // STORE1 (storcal.f) at the converged heads: the FP32 path computed it
+    // for every iterating member (k_switch_store1_f32); the FP64 path
+    // computes it now
     const double* st1 = red;
     if (!graph && !mixed) {
       d_mask2.upload(conv_mask.data(), nmem, st);
       CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
-      if (precision == 1 && iopt == 1)
-        k_store1_f32<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, nf, d_red.p);
-      else
-        k_store1<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, d_red.p);
+      k_store1<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, d_red.p);
       count();
       check_launch();
       d_red.download(v_red.data(), v_red.size(), st);
@@ -4812,6 +4778,28 @@ int engine_get_state(Engine* e, int m, double* pnew, double* time,
   if (time) *time = h.step_recs.empty() ? 0.0 : h.step_recs.back().time;
   if (deltat) *deltat = h.step_recs.empty() ? h.deltat : h.step_recs.back().deltat;
   if (status) *status = h.status;
+  return 0;
+}
+
+// Sw(PNEW) of one member's nodes in FP64 (CHNEW's SWNEW, fvgse.f):
+// VGPNOT * Se(PNEW) + VGRMC / PNODI.
+__global__ void k_saturation(int n, int off, Nodal nd, double* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int i = off + k;
+  const double se = vg_se<double>(nd.pnew[i], nd.vgpsat[i], nd.vgn[i], nd.vgm[i]);
+  out[k] = nd.vgpnot[i] * se + nd.vgrmc[i] / nd.pnodi[i];
+}
+
+int engine_get_saturation(Engine* e, int m, double* sw) {
+  if (m < 0 || m >= e->nmem || !sw) return CATHY_GB300_EINVAL;
+  const int n = e->M[m]->meshp->n;
+  DBuf<double> out;
+  out.alloc(n);
+  k_saturation<<<cdiv(n, kThreads), kThreads, 0, e->st>>>(n, e->node_off[m], e->nd, out.p);
+  CG_TRY(cudaPeekAtLastError());
+  out.download(sw, n, e->st);
+  CG_TRY(cudaStreamSynchronize(e->st));
   return 0;
 }
 

@@ -9,10 +9,11 @@ here take the same project folders, read the same input files
 (:mod:`pycathy_wrapper_gb300.project`), run the subsurface solver on the GPU
 -- an ensemble as one batched solve -- and write the output files pyCATHY
 reads back: ``output/psi`` (pressure heads, read by
-pyCATHY/importers/cathy_outputs.py:480 ``read_psi``) and ``output/mbeconv``
-(mass balance and convergence per time step, read by
-pyCATHY/importers/cathy_outputs.py:607 ``read_mbeconv``; row format of
-cathy_main.f:3269-3273).
+pyCATHY/importers/cathy_outputs.py:480 ``read_psi``), ``output/sw`` (water
+saturation, ``read_sw`` at :418), ``output/mbeconv`` (mass balance and
+convergence per time step, read by pyCATHY/importers/cathy_outputs.py:607
+``read_mbeconv``; row format of cathy_main.f:3269-3273) and
+``output/iter`` (the nonlinear-iteration log, conver.f:44-45).
 """
 from __future__ import annotations
 
@@ -38,6 +39,47 @@ def write_psi(path: str, snapshots) -> None:
             p = np.asarray(p, float)
             for a in range(0, len(p), 5):
                 f.write("".join(_fmt_e(v, 15, 6) for v in p[a:a + 5]) + "\n")
+
+
+def write_sw(path: str, snapshots) -> None:
+    """``snapshots``: iterable of (nstep, time, saturation).  The file opens
+    with the reference's ``  0   HSPSW`` line (cathy_main.f:2821, format at
+    :4134); each block is laid out like ``psi`` (detout.f:44-45), which
+    pyCATHY's ``read_sw`` (importers/cathy_outputs.py:418) parses."""
+    with open(path, "w") as f:
+        f.write("  0   HSPSW\n")
+        for nstep, time, sw in snapshots:
+            f.write(f"{int(nstep):7d}{_fmt_e(float(time), 16, 8)}     NSTEP   TIME\n")
+            sw = np.asarray(sw, float)
+            for a in range(0, len(sw), 5):
+                f.write("".join(_fmt_e(v, 15, 6) for v in sw[a:a + 5]) + "\n")
+
+
+def write_iter(path: str, parm, iter_records) -> None:
+    """The nonlinear-iteration log: the parameter header of
+    cathy_main.f:3960-3972 (written at :2863), a ``(NSTEP: ...)`` line at the
+    start of every time-step attempt (format at :3973, written at :2985) and
+    one line per Picard/Newton iteration with the convergence and residual
+    norms and the heads at IKMAX (conver.f:44-45, format at :103)."""
+    with open(path, "w") as f:
+        f.write(f"     IOPT   (1 PICARD, 2 NEWTON)             = {int(parm.iopt):6d}\n")
+        f.write(f"     NLRELX (0 NORELX,1 CONS RELX,2 VAR RELX)= {int(parm.nlrelx):6d}\n")
+        f.write("     KSLOPE (0 ANA, 1 KSL/ANA, 2 KSL/C-DIFF,\n")
+        f.write(f"             3 LOC KSL/ANA, 4 LOC TAN-SLOPE) = {int(parm.kslope):6d}\n")
+        f.write(f"     TOLUNS (TOLERANCE FOR NONLINEAR ITER)   = {_fmt_e(parm.toluns, 15, 5)}\n")
+        f.write(f"     TOLSWI (TOLERANCE FOR BC SWITCHING)     = {_fmt_e(parm.tolswi, 15, 5)}\n")
+        f.write(f"     L2NORM (0 INFINITY NORM, ELSE L2 NORM)  = {int(parm.l2norm):6d}\n")
+        f.write("\n nlinr  linr converg error norms  node   PNEW at   POLD at   resid error norms\n")
+        f.write("  iter  iter       PL2      PINF IKMAX     IKMAX     IKMAX       FL2      FINF\n")
+        f.write(" " + "=" * 77 + "\n")
+        for r in iter_records:
+            if int(r["iter"]) == 1:
+                f.write(" " * 23 + f" (NSTEP: {int(r['nstep']):5d}  DELTAT: "
+                        f"{_fmt_e(r['deltat'], 12, 4)}  TIME: {_fmt_e(r['time'], 12, 4)})\n")
+            f.write(f"{int(r['iter']):6d}{int(r['niter']):6d}{_fmt_e(r['pl2'], 10, 3)}"
+                    f"{_fmt_e(r['pinf'], 10, 3)}{int(r['ikmax']):6d}"
+                    f"{_fmt_e(r['pnew_ik'], 10, 2)}{_fmt_e(r['pold_ik'], 10, 2)}"
+                    f"{_fmt_e(r['fl2'], 10, 3)}{_fmt_e(r['finf'], 10, 3)}\n")
 
 
 _MBE_HDR = (
@@ -69,14 +111,16 @@ def write_mbeconv(path: str, step_records, initial_volume: float) -> None:
             f.write(" ".join(vals) + "\n")
 
 
-def _write_member(prj: str, p0, result, recs) -> None:
+def _write_member(prj: str, parm, p0, sw0, result, sw, its, recs) -> None:
     out = os.path.join(prj, "output")
     os.makedirs(out, exist_ok=True)
     p, t, dt, status = result
     nstep = recs[-1]["nstep"] if recs else 0
     write_psi(os.path.join(out, "psi"), [(0, 0.0, p0), (nstep, t, p)])
+    write_sw(os.path.join(out, "sw"), [(0, 0.0, sw0), (nstep, t, sw)])
     v0 = (recs[0]["store2"] - recs[0]["cdstor"]) if recs else 0.0
     write_mbeconv(os.path.join(out, "mbeconv"), recs, v0)
+    write_iter(os.path.join(out, "iter"), parm, its)
 
 
 def run_project(prj: str, precision: int = 1, device: int = 0, write: bool = True) -> dict:
@@ -98,12 +142,13 @@ def run_ensemble(member_dirs: Sequence[str], precision: int = 1, device: int = 0
     out = []
     with Simulation(cases, precision=precision, device=device) as s:
         p0 = [s.state(m)[0].copy() for m in range(len(cases))]
+        sw0 = [s.saturation(m) for m in range(len(cases))]
         s.run()
         for m, d in enumerate(member_dirs):
             res = s.state(m)
-            _, recs = s.records(m)
+            its, recs = s.records(m)
             if write:
-                _write_member(d, p0[m], res, recs)
+                _write_member(d, cases[m].parm, p0[m], sw0[m], res, s.saturation(m), its, recs)
             out.append(dict(dir=d, pnew=res[0], time=res[1], deltat=res[2],
                             status=int(res[3]), steps=len(recs)))
     return out

@@ -1,6 +1,7 @@
 """pyCATHY-facing files: project folders written and read back, and the
-output files (psi, mbeconv) in the layouts pyCATHY's readers parse
-(pyCATHY/importers/cathy_outputs.py:480 read_psi, :607 read_mbeconv)."""
+output files (psi, sw, mbeconv, iter) in the layouts pyCATHY's readers parse
+(pyCATHY/importers/cathy_outputs.py:480 read_psi, :418 read_sw,
+:607 read_mbeconv) and the reference writes (iter: conver.f:44-45)."""
 import os
 
 import numpy as np
@@ -75,6 +76,81 @@ def test_output_files_parse_like_pycathy(tmp_path):
     np.testing.assert_allclose(a[:, 13], 1e-5 - 2e-6, rtol=1e-3)
 
 
+def _parse_sw(path):
+    """The block parsing of pyCATHY's read_sw: header lines hold the step and
+    the time; the file's first line is the HSPSW marker."""
+    lines = open(path).readlines()
+    assert lines[0] == "  0   HSPSW\n"
+    return _parse_psi(path)
+
+
+def _parse_iter(path):
+    """Fixed-width fields of the reference's iteration lines
+    (2I6, 2E10.3, I6, 2E10.2, 2E10.3) and the (NSTEP: ...) step lines."""
+    steps, rows = [], []
+    for ln in open(path).read().splitlines():
+        if "(NSTEP:" in ln:
+            w = ln.replace("(", " ").replace(")", " ").split()
+            steps.append((int(w[1]), float(w[3]), float(w[5])))
+        elif len(ln) == 78 and ln[:6].strip().isdigit():
+            cuts = [0, 6, 12, 22, 32, 38, 48, 58, 68, 78]
+            f = [ln[a:b] for a, b in zip(cuts[:-1], cuts[1:])]
+            rows.append(dict(iter=int(f[0]), niter=int(f[1]), pl2=float(f[2]), pinf=float(f[3]),
+                             ikmax=int(f[4]), pnew_ik=float(f[5]), pold_ik=float(f[6]),
+                             fl2=float(f[7]), finf=float(f[8])))
+    return steps, rows
+
+
+def test_sw_and_iter_files_from_oracle_records(tmp_path):
+    import oracle as O
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.pycathy import write_iter, write_sw
+    case = config0(tmax=3600.0, precond=0)
+    o = O.Oracle(case)
+    p0 = o.state()[0]
+    sw0 = o.vg_nodal(p0)["sw"]
+    for _ in range(4):
+        o.step()
+    p1, t1, _ = o.state()
+    sw1 = o.vg_nodal(p1)["sw"]
+    write_sw(str(tmp_path / "sw"), [(0, 0.0, sw0), (4, t1, sw1)])
+    times, blocks = _parse_sw(str(tmp_path / "sw"))
+    assert times == [0.0, pytest.approx(t1, rel=1e-8)]
+    np.testing.assert_allclose(blocks[0], sw0, rtol=1e-6)
+    np.testing.assert_allclose(blocks[1], sw1, rtol=1e-6)
+    its = o.iter_records()
+    write_iter(str(tmp_path / "iter"), case.parm, its)
+    head = open(str(tmp_path / "iter")).read().splitlines()
+    assert head[0] == "     IOPT   (1 PICARD, 2 NEWTON)             =      1"
+    assert head[10] == " " + "=" * 77
+    steps, rows = _parse_iter(str(tmp_path / "iter"))
+    assert len(rows) == len(its)
+    assert len(steps) == sum(1 for r in its if r["iter"] == 1)
+    for a, b in zip(rows, its):
+        assert (a["iter"], a["niter"], a["ikmax"]) == (b["iter"], b["niter"], b["ikmax"])
+        for k, rt in (("pl2", 1e-3), ("pinf", 1e-3), ("pnew_ik", 1e-2), ("pold_ik", 1e-2),
+                      ("fl2", 1e-3), ("finf", 1e-3)):
+            assert a[k] == pytest.approx(b[k], rel=rt, abs=1e-300), k
+
+
+@pytest.mark.gpu
+def test_saturation_matches_oracle():
+    """Sw at the current heads (the sw output's array) against the oracle's
+    van Genuchten restatement, FP64 and FP32 paths."""
+    import oracle as O
+    from pycathy_wrapper_gb300.api import Simulation
+    from pycathy_wrapper_gb300.inputs import config0
+    for precision in (0, 1):
+        case = config0(tmax=3600.0, precond=0 if precision == 0 else 2)
+        with Simulation([case], precision=precision) as s:
+            for _ in range(5):
+                s.step()
+            p = s.state(0)[0]
+            sw = s.saturation(0)
+        ref = O.Oracle(config0(tmax=3600.0, precond=0)).vg_nodal(p)["sw"]
+        np.testing.assert_allclose(sw, ref, rtol=1e-12, atol=1e-14)
+
+
 @pytest.mark.gpu
 def test_run_ensemble_on_project_folders_matches_api(tmp_path):
     from pycathy_wrapper_gb300.api import Simulation
@@ -100,3 +176,8 @@ def test_run_ensemble_on_project_folders_matches_api(tmp_path):
         np.testing.assert_allclose(blocks[-1], r["pnew"], rtol=1e-6, atol=1e-12)
         mb = np.loadtxt(os.path.join(dirs[m], "output", "mbeconv"), skiprows=2, usecols=range(19))
         assert mb[-1, 2] == pytest.approx(1800.0)
+        times, sws = _parse_sw(os.path.join(dirs[m], "output", "sw"))
+        assert times[-1] == pytest.approx(1800.0)
+        assert len(sws[-1]) == len(r["pnew"]) and np.all((sws[-1] > 0.0) & (sws[-1] <= 1.0))
+        steps, rows = _parse_iter(os.path.join(dirs[m], "output", "iter"))
+        assert rows and steps[-1][2] == pytest.approx(1800.0, rel=1e-4)
