@@ -2236,8 +2236,9 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
 
 // Post-solve pass of the FP32 Picard iteration, one thread per row:
 // PNEW += PDIFF + SHLPIC; at Dirichlet rows the back-calculated flux (BKPIC:
-// SCR = A*PDIFF - XT5 -> QPNEW or ATMACT); then the MASBAL sums, RELAX and
-// NORMS of k_masbal_norms_f32.  PINF and IKMAX (the largest node index
+// SCR = A*PDIFF - XT5 -> QPNEW or ATMACT); then the MASBAL sums (STORMB,
+// FLUXMB; compensated FP32 block sums), RELAX and NORMS (PL2, FL2, FINF in
+// FP32 per node, reduced in FP64).  PINF and IKMAX (the largest node index
 // attaining PINF) come from one 64-bit maximum of (|dp| float bits, node
 // index) per member.  The last block to finish converts the maxima and
 // takes the per-member pass: PNEW/POLD at IKMAX and whether SWITCH_OLD runs.
@@ -2409,11 +2410,12 @@ __global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
 }
 
 // ============================================================================
-// Launch-fused kernels of the graph path: one launch runs the blocks of
-// several independent kernels (consecutive block ranges, one segment each),
-// or a kernel and the per-member decision that follows it.  They cut the
-// number of dependent graph nodes per Picard iteration; every segment is the
-// unchanged body of the corresponding kernel.
+// Launch-fused kernels of the FP32 Picard iteration (run inside the
+// iteration's CUDA graph or launch by launch): one launch runs the blocks of
+// several independent pieces of work (consecutive block ranges, one segment
+// each), or fuses a pass with the per-member decision that follows it (by
+// the last block to finish).  They cut the number of dependent launches per
+// Picard iteration.
 // ============================================================================
 
 // PCG set-up, first launch: per vertical column the column-line factor
@@ -4118,9 +4120,10 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
 
 
 // One nonlinear iteration for every member flagged ACT_ITER, in three
-// phases: pre-solve (soil characteristics, assembly, BCs), the linear solve,
-// post-solve (head update, mass balance, norms, switching).  The FP32
-// Picard path can also run as one CUDA graph (graph_build).
+// phases: pre-solve (step actions and soil characteristics, assembly, BCs),
+// the linear solve, post-solve (head update, mass balance, norms,
+// switching).  The FP32 Picard path runs the same kernels either as one CUDA
+// graph (graph_build) or launch by launch.
 void Engine::iteration_pre(int solve_phase) {
   const bool mixed = (precision == 1 && iopt == 1);
   const cathy_parm_t& P0 = M[0]->parm;
