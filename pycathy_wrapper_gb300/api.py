@@ -159,6 +159,12 @@ class Simulation:
         p = _f64(ptimep)
         check(self.L.cathy_gb300_set_state(self.h, m, _ptr(p, f64p), time, deltat), "set_state")
 
+    def num_records(self, m: int = 0):
+        """(iteration records, accepted steps) of member m so far."""
+        ni, ns = C.c_int32(), C.c_int32()
+        check(self.L.cathy_gb300_num_records(self.h, m, C.byref(ni), C.byref(ns)), "records")
+        return ni.value, ns.value
+
     def records(self, m: int = 0):
         ni, ns = C.c_int32(), C.c_int32()
         check(self.L.cathy_gb300_num_records(self.h, m, C.byref(ni), C.byref(ns)), "records")

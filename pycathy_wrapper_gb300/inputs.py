@@ -135,6 +135,13 @@ class Parm:
     precond: int = 0
     kslope: int = 0
     tolksl: float = 0.01
+    # output control (not used by the solver): IPRT1 = 3 asks for the mesh
+    # files only; detailed output (psi, sw) at TIME=0 and at the first step
+    # reaching each TIMPRT; the water table at the NODVP columns every step
+    iprt1: int = 2
+    iprt: int = 4
+    timprt: List[float] = field(default_factory=list)
+    nodvp: List[int] = field(default_factory=list)
 
 
 @dataclass

@@ -62,6 +62,26 @@ def read_parm(path) -> Parm:
     p.deltat, p.dtmin, p.dtmax, p.tmax = v[11][:4]
     p.dtmaga, p.dtmagm, p.dtreds, p.dtredm = v[12][:4]
     p.tolksl = v[2][1]
+    p.iprt1 = int(v[0][0])
+    # IPRT VTKF NPRT (TIMPRT(I),I=1,NPRT) then NUMVP (NODVP(I),I=1,NUMVP):
+    # list-directed reads (datin.f:118-119), so a list may run on over
+    # several lines
+    k = 13
+    if len(v) > k and len(v[k]) >= 3:
+        p.iprt, nprt = int(v[k][0]), int(v[k][2])
+        vals = list(v[k][3:])
+        while len(vals) < nprt and k + 1 < len(v):
+            k += 1
+            vals += v[k]
+        p.timprt = [float(t) for t in vals[:nprt]]
+        k += 1
+        if k < len(v) and v[k]:
+            numvp = int(v[k][0])
+            ids = list(v[k][1:])
+            while len(ids) < numvp and k + 1 < len(v):
+                k += 1
+                ids += v[k]
+            p.nodvp = [int(i) for i in ids[:numvp]]
     return p
 
 

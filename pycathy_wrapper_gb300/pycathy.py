@@ -41,6 +41,68 @@ def write_psi(path: str, snapshots) -> None:
                 f.write("".join(_fmt_e(v, 15, 6) for v in p[a:a + 5]) + "\n")
 
 
+def write_grid3d(path: str, mesh) -> None:
+    """The 3-D mesh as GEN3D writes it for IPRT1 = 3 (gen3d.f:96-102,
+    formats 1030-1050): NNOD N NT, the NT tetrahedra (4 nodes + material, in
+    GEN3D's node order: the mesh of :func:`mesh_gen3d`), the N node
+    coordinates; pyCATHY's ``read_grid3d`` (importers/cathy_outputs.py:15)
+    parses it."""
+    x, y, z, tetra = mesh["x"], mesh["y"], mesh["z"], np.asarray(mesh["tetra"])
+    with open(path, "w") as f:
+        f.write(f"{int(mesh['nnod']):9d}{len(x):9d}{len(tetra):9d}\n")
+        for t in tetra:
+            f.write("".join(f"{int(v):7d}" for v in t[:5]) + "\n")
+        for a, b, c in zip(x, y, z):
+            f.write(_fmt_e(a, 15, 6) + _fmt_e(b, 15, 6) + _fmt_e(c, 15, 6) + "\n")
+
+
+def write_xyz(path: str, mesh) -> None:
+    """Node coordinates as GEN3D writes them for IPRT1 = 3 (gen3d.f:92-95,
+    formats 1010-1020); pyCATHY's ``read_xyz`` (:177) parses it."""
+    x, y, z = mesh["x"], mesh["y"], mesh["z"]
+    with open(path, "w") as f:
+        f.write(f"{int(mesh['nnod']):7d}{len(x):7d}  NNOD   N\n")
+        for i, (a, b, c) in enumerate(zip(x, y, z)):
+            f.write(f"{i + 1:7d}" + _fmt_e(a, 15, 6) + _fmt_e(b, 15, 6) + _fmt_e(c, 15, 6) + "\n")
+
+
+def water_table(p, z, nnod: int, nstr: int, nodvp) -> List[float]:
+    """Water-table elevation at the NODVP columns (wtdepth.f:18-46): from
+    the bottom layer up, the first pair of a saturated node below an
+    unsaturated one, interpolated linearly in the head; with no such pair,
+    the ponded surface level if the surface node is saturated, else the
+    bottom of the column.  Node k*nnod + c is column c, layer k (0 = top)."""
+    out = []
+    for nv in nodvp:
+        c = int(nv) - 1
+        wt, flag = z[c], 0
+        for j in range(nstr, 0, -1):
+            i1, i2 = c + j * nnod, c + (j - 1) * nnod
+            if p[i1] >= 0.0 and p[i2] < 0.0 and flag == 0:
+                rc = (z[i1] - z[i2]) / (p[i1] - p[i2])
+                wt, flag = z[i1] - rc * p[i1], 1
+            elif p[i1] >= 0.0 and p[i2] < 0.0 and flag == 1:
+                flag = 2
+            elif j == 1 and p[i2] >= 0.0 and flag == 0:
+                wt, flag = z[c] + p[i2], 3
+            elif j == 1 and flag == 0:
+                wt, flag = z[c + nstr * nnod], 4
+        out.append(float(wt))
+    return out
+
+
+def write_wtdepth(path: str, rows) -> None:
+    """``rows``: (time, [water table at each NODVP column]) per accepted
+    step; header of cathy_main.f:2872 (format :4042), rows in format 1020
+    of wtdepth.f (70 values of 1PE15.6 per line)."""
+    with open(path, "w") as f:
+        f.write("#TIME      <--- WTDEPTH(NODVP(I)), I=1,2,...,NUMVP --->\n")
+        for t, wt in rows:
+            vals = [float(t)] + [float(w) for w in wt]
+            for a in range(0, len(vals), 70):
+                f.write("".join(_fmt_e(v, 15, 6) for v in vals[a:a + 70]) + "\n")
+
+
 def write_sw(path: str, snapshots) -> None:
     """``snapshots``: iterable of (nstep, time, saturation).  The file opens
     with the reference's ``  0   HSPSW`` line (cathy_main.f:2821, format at
@@ -111,22 +173,108 @@ def write_mbeconv(path: str, step_records, initial_volume: float) -> None:
             f.write(" ".join(vals) + "\n")
 
 
-def _write_member(prj: str, parm, p0, sw0, result, sw, its, recs) -> None:
+def drive_outputs(sim, n: int, parms, meshes):
+    """Run every member to the end one accepted step at a time (``sim.step``
+    advances each running member by exactly one step, so the members'
+    trajectories are those of an uninterrupted run) and collect what the
+    reference writes along the way: detailed output (heads and saturation)
+    at TIME = 0 and at the first step reaching each TIMPRT
+    (cathy_main.f:3715-3738), and the water table at the NODVP columns after
+    every step (cathy_main.f:3628).  ``sim`` needs step(), state(m),
+    saturation(m) and num_steps(m)."""
+    snaps = [[(0, 0.0, sim.state(m)[0].copy(), sim.saturation(m))] for m in range(n)]
+    kprt, seen = [0] * n, [0] * n
+    wt = [[] for _ in range(n)]
+    while True:
+        nact = sim.step()
+        for m in range(n):
+            k = sim.num_steps(m)
+            if k == seen[m]:
+                continue
+            seen[m] = k
+            p, t = sim.state(m)[:2]
+            msh, parm = meshes[m], parms[m]
+            if parm.nodvp:
+                wt[m].append((t, water_table(p, msh["z"], msh["nnod"], msh["nstr"], parm.nodvp)))
+            if kprt[m] < len(parm.timprt) and t >= parm.timprt[kprt[m]]:
+                snaps[m].append((k, t, p.copy(), sim.saturation(m)))
+                kprt[m] += 1
+        if nact == 0:
+            break
+    for m in range(n):
+        k = sim.num_steps(m)
+        p, t = sim.state(m)[:2]
+        if snaps[m][-1][0] != k:  # the end of the run (TIME = TMAX)
+            snaps[m].append((k, t, p.copy(), sim.saturation(m)))
+    return snaps, wt
+
+
+def _write_member(prj: str, parm, mesh, snaps, wt, its, recs) -> None:
     out = os.path.join(prj, "output")
     os.makedirs(out, exist_ok=True)
-    p, t, dt, status = result
-    nstep = recs[-1]["nstep"] if recs else 0
-    write_psi(os.path.join(out, "psi"), [(0, 0.0, p0), (nstep, t, p)])
-    write_sw(os.path.join(out, "sw"), [(0, 0.0, sw0), (nstep, t, sw)])
+    write_psi(os.path.join(out, "psi"), [(k, t, p) for k, t, p, _ in snaps])
+    write_sw(os.path.join(out, "sw"), [(k, t, sw) for k, t, _, sw in snaps])
     v0 = (recs[0]["store2"] - recs[0]["cdstor"]) if recs else 0.0
     write_mbeconv(os.path.join(out, "mbeconv"), recs, v0)
     write_iter(os.path.join(out, "iter"), parm, its)
+    if parm.nodvp:
+        write_wtdepth(os.path.join(out, "wtdepth"), wt)
+    write_grid3d(os.path.join(out, "grid3d"), mesh)
+    write_xyz(os.path.join(out, "xyz"), mesh)
+
+
+def mesh_gen3d(case) -> dict:
+    """The host mesh with the tetrahedra in GEN3D's node order (the Picard
+    pattern builder sorts each tetrahedron's nodes after GEN3D has written
+    grid3d; the Newton mesh keeps GEN3D's order)."""
+    from .api import build_mesh
+    mesh = build_mesh(case, iopt=2)
+    mesh["nstr"] = case.dem.nstr
+    return mesh
+
+
+def write_mesh(prj: str) -> dict:
+    """The IPRT1 = 3 run of the reference (gen3d.f:89-111: write the mesh
+    and stop), on the host mesh builder: ``output/grid3d`` and
+    ``output/xyz``.  pyCATHY runs it to get the mesh
+    (pyCATHY/cathy_tools.py:729)."""
+    case = read_project(prj)
+    mesh = mesh_gen3d(case)
+    out = os.path.join(prj, "output")
+    os.makedirs(out, exist_ok=True)
+    write_grid3d(os.path.join(out, "grid3d"), mesh)
+    write_xyz(os.path.join(out, "xyz"), mesh)
+    return mesh
 
 
 def run_project(prj: str, precision: int = 1, device: int = 0, write: bool = True) -> dict:
     """Run one pyCATHY project folder to TMAX on the GPU (the replacement
-    of ``subprocess.run(["./cathy"])``).  Returns heads, time and status."""
+    of ``subprocess.run(["./cathy"])``; with IPRT1 = 3 in ``input/parm`` it
+    writes the mesh files and stops, as the reference does).  Returns heads,
+    time and status."""
+    if read_project(prj).parm.iprt1 == 3:
+        mesh = write_mesh(prj)
+        return dict(dir=prj, mesh=mesh, status=1, steps=0)
     return run_ensemble([prj], precision=precision, device=device, write=write)[0]
+
+
+class _Stepper:
+    """The engine seen through the calls of :func:`drive_outputs`."""
+
+    def __init__(self, sim):
+        self.sim = sim
+
+    def step(self):
+        return self.sim.step()
+
+    def state(self, m):
+        return self.sim.state(m)
+
+    def saturation(self, m):
+        return self.sim.saturation(m)
+
+    def num_steps(self, m):
+        return self.sim.num_records(m)[1]
 
 
 def run_ensemble(member_dirs: Sequence[str], precision: int = 1, device: int = 0,
@@ -134,21 +282,29 @@ def run_ensemble(member_dirs: Sequence[str], precision: int = 1, device: int = 0
     """Run every member folder of a DA ensemble as ONE batched GPU solve
     (the replacement of the process pool over ``./cathy``).  Members may
     differ in mesh, soil, forcing and initial state; they must share IOPT,
-    LUMP and the Picard preconditioner."""
+    LUMP and the Picard preconditioner.  With ``write`` the members step
+    together one accepted step at a time so that the detailed output and
+    the water table are taken where the reference takes them; without it
+    they run straight to the end.  (The FP32 dot products of the batched
+    SpMV are grouped over the members that are active at the time, so the
+    two schedules agree to the FP32 rounding of those sums, not bit for
+    bit.)"""
     cases = [read_project(d) for d in member_dirs]
     for c in cases:
         if c.parm.iopt == 1 and c.parm.precond == 0 and precision == 1:
             c.parm.precond = 2  # FP32 batched path: column-line preconditioner
     out = []
     with Simulation(cases, precision=precision, device=device) as s:
-        p0 = [s.state(m)[0].copy() for m in range(len(cases))]
-        sw0 = [s.saturation(m) for m in range(len(cases))]
-        s.run()
+        if write:
+            meshes = [mesh_gen3d(c) for c in cases]
+            snaps, wt = drive_outputs(_Stepper(s), len(cases), [c.parm for c in cases], meshes)
+        else:
+            s.run()
         for m, d in enumerate(member_dirs):
             res = s.state(m)
             its, recs = s.records(m)
             if write:
-                _write_member(d, cases[m].parm, p0[m], sw0[m], res, s.saturation(m), its, recs)
+                _write_member(d, cases[m].parm, meshes[m], snaps[m], wt[m], its, recs)
             out.append(dict(dir=d, pnew=res[0], time=res[1], deltat=res[2],
                             status=int(res[3]), steps=len(recs)))
     return out
@@ -177,7 +333,7 @@ def write_project(case, prj: str) -> None:
     os.makedirs(inp, exist_ok=True)
     os.makedirs(pre, exist_ok=True)
     with open(os.path.join(inp, "parm"), "w") as f:
-        f.write("2 0 0\tIPRT1 NCOUT TRAFLAG\n")
+        f.write(f"{p.iprt1} 0 0\tIPRT1 NCOUT TRAFLAG\n")
         f.write(f"{p.isimgr} {p.pondh_min!r} 0\tISIMGR PONDH_MIN VELREC\n")
         f.write(f"{p.kslope} {p.tolksl!r}\tKSLOPE TOLKSL\n")
         f.write("-3.0 -1.0 -3.0 -1.0\tPKRL PKRR PSEL PSER\n")
@@ -190,8 +346,13 @@ def write_project(case, prj: str) -> None:
         f.write(f"{p.isolv} {p.itmxcg} {p.tolcg!r}\tISOLV ITMXCG TOLCG\n")
         f.write(f"{p.deltat!r} {p.dtmin!r} {p.dtmax!r} {p.tmax!r}\tDELTAT DTMIN DTMAX TMAX\n")
         f.write(f"{p.dtmaga!r} {p.dtmagm!r} {p.dtreds!r} {p.dtredm!r}\tDTMAGA DTMAGM DTREDS DTREDM\n")
-        f.write(f"4 2 1 {p.tmax!r}\tIPRT VTKF NPRT (TIMPRT(I),I=1,NPRT)\n")
-        f.write("1 1\tNUMVP (NODVP(I),I=1,NUMVP)\n0\tNR\n0\tNUM_QOUT\n1\t(ID_QOUT(I),I=1,NUM_QOUT)\n")
+        timprt = list(p.timprt) or [p.tmax]
+        nodvp = list(p.nodvp) or [1]
+        f.write(f"{p.iprt} 2 {len(timprt)} " + " ".join(repr(float(t)) for t in timprt)
+                + "\tIPRT VTKF NPRT (TIMPRT(I),I=1,NPRT)\n")
+        f.write(f"{len(nodvp)} " + " ".join(str(int(i)) for i in nodvp)
+                + "\tNUMVP (NODVP(I),I=1,NUMVP)\n")
+        f.write("0\tNR\n0\tNUM_QOUT\n1\t(ID_QOUT(I),I=1,NUM_QOUT)\n")
     nzone, nstr = s.nzone, d.nstr
     with open(os.path.join(inp, "dem_parameters"), "w") as f:
         f.write(f"{d.delta_x!r}\n{d.delta_y!r}\n{d.factor!r}\n1\n{nzone}\t{nstr}\t25\n")

@@ -133,6 +133,118 @@ def test_sw_and_iter_files_from_oracle_records(tmp_path):
             assert a[k] == pytest.approx(b[k], rel=rt, abs=1e-300), k
 
 
+def test_mesh_files_match_reference_grid3d(tmp_path):
+    """grid3d and xyz from the host mesh builder against the reference's own
+    grid3d of the weill example (parsed as pyCATHY's read_grid3d does)."""
+    from conftest import GOLDEN, load_golden_case
+    from pycathy_wrapper_gb300.pycathy import mesh_gen3d, write_grid3d, write_xyz
+    g = np.load(os.path.join(GOLDEN, "weill_grid3d.npz"))
+    mesh = mesh_gen3d(load_golden_case("weill"))
+    write_grid3d(str(tmp_path / "grid3d"), mesh)
+    nnod, n, nt = np.loadtxt(str(tmp_path / "grid3d"), max_rows=1).astype(int)
+    assert (nnod, n, nt) == (int(g["nnod"]), g["xyz"].shape[0], g["tetra"].shape[0])
+    tet = np.loadtxt(str(tmp_path / "grid3d"), skiprows=1, max_rows=nt).astype(int)
+    xyz = np.loadtxt(str(tmp_path / "grid3d"), skiprows=1 + nt)
+    np.testing.assert_array_equal(tet, g["tetra"])
+    np.testing.assert_allclose(xyz, g["xyz"], rtol=1e-6, atol=1e-6)
+    write_xyz(str(tmp_path / "xyz"), mesh)
+    a = np.loadtxt(str(tmp_path / "xyz"), skiprows=1)
+    assert open(str(tmp_path / "xyz")).readline().split()[:2] == [str(nnod), str(n)]
+    np.testing.assert_array_equal(a[:, 0], np.arange(1, n + 1))
+    np.testing.assert_allclose(a[:, 1:], g["xyz"], rtol=1e-6, atol=1e-6)
+
+
+def test_water_table_rules():
+    """wtdepth.f's cases on one 3-layer column (nnod = 1, top node first)."""
+    from pycathy_wrapper_gb300.pycathy import water_table
+    z = np.array([3.0, 2.0, 1.0, 0.0])
+    # saturated below 1.5 m: crossing between the nodes at z = 1 (p = 0.5)
+    # and z = 2 (p = -0.5), interpolated to z = 1.5
+    assert water_table(np.array([-1.5, -0.5, 0.5, 1.5]), z, 1, 3, [1]) == [pytest.approx(1.5)]
+    # fully unsaturated: the bottom of the column
+    assert water_table(np.array([-4.0, -3.0, -2.0, -1.0]), z, 1, 3, [1]) == [0.0]
+    # fully saturated with ponding: surface elevation + surface head
+    assert water_table(np.array([0.2, 1.2, 2.2, 3.2]), z, 1, 3, [1]) == [pytest.approx(3.2)]
+
+
+def test_parm_output_controls_round_trip(tmp_path):
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.project import read_project
+    from pycathy_wrapper_gb300.pycathy import write_project
+    c = config0(tmax=7200.0)
+    c.parm.iprt1, c.parm.timprt, c.parm.nodvp = 3, [1800.0, 3600.0, 7200.0], [5, 17]
+    write_project(c, str(tmp_path))
+    r = read_project(str(tmp_path))
+    assert (r.parm.iprt1, r.parm.timprt, r.parm.nodvp) == (3, [1800.0, 3600.0, 7200.0], [5, 17])
+
+
+def test_mesh_only_run_writes_grid3d_without_a_gpu(tmp_path):
+    """IPRT1 = 3: the mesh files and nothing else (gen3d.f:89-111)."""
+    from pycathy_wrapper_gb300.api import build_mesh
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.pycathy import run_project, write_project
+    c = config0(tmax=600.0)
+    c.parm.iprt1 = 3
+    write_project(c, str(tmp_path))
+    res = run_project(str(tmp_path))
+    assert res["steps"] == 0
+    out = tmp_path / "output"
+    assert sorted(os.listdir(out)) == ["grid3d", "xyz"]
+    m = build_mesh(c)
+    nnod, n, nt = np.loadtxt(str(out / "grid3d"), max_rows=1).astype(int)
+    assert (nnod, n, nt) == (m["nnod"], m["n"], m["nt"])
+
+
+class _OracleStepper:
+    """The oracle behind the calls of drive_outputs (one member)."""
+
+    def __init__(self, case):
+        import oracle as O
+        self.o, self.tmax = O.Oracle(case), case.parm.tmax
+
+    def _t(self):
+        # the time of the last accepted step (the oracle's TIME has already
+        # moved on to the next step, as after TIMUPD)
+        r = self.o.step_records()
+        return r[-1]["time"] if r else 0.0
+
+    def step(self):
+        self.o.step()
+        return 0 if self._t() >= self.tmax - 1e-9 else 1
+
+    def state(self, m):
+        p, _, dt = self.o.state()
+        return p, self._t(), dt, 0
+
+    def saturation(self, m):
+        return self.o.vg_nodal(self.o.state()[0])["sw"]
+
+    def num_steps(self, m):
+        return len(self.o.step_records())
+
+
+def test_drive_outputs_print_times_and_water_table():
+    """Detailed output at TIME = 0 and at the first step reaching each
+    TIMPRT, a water-table row per accepted step."""
+    from pycathy_wrapper_gb300.api import build_mesh
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.pycathy import drive_outputs, water_table
+    c = config0(tmax=1200.0)
+    c.parm.timprt, c.parm.nodvp = [300.0, 1200.0], [1, 7]
+    mesh = build_mesh(c)
+    mesh["nstr"] = c.dem.nstr
+    st = _OracleStepper(c)
+    snaps, wt = drive_outputs(st, 1, [c.parm], [mesh])
+    recs = st.o.step_records()
+    times = [r["time"] for r in recs]
+    assert [s[1] for s in snaps[0]] == [0.0, next(t for t in times if t >= 300.0), times[-1]]
+    assert snaps[0][-1][1] == pytest.approx(1200.0)
+    assert [r[0] for r in wt[0]] == times
+    p_end = st.o.state()[0]
+    assert wt[0][-1][1] == water_table(p_end, mesh["z"], mesh["nnod"], c.dem.nstr, [1, 7])
+    np.testing.assert_array_equal(snaps[0][-1][2], p_end)
+
+
 @pytest.mark.gpu
 def test_saturation_matches_oracle():
     """Sw at the current heads (the sw output's array) against the oracle's
@@ -166,8 +278,11 @@ def test_run_ensemble_on_project_folders_matches_api(tmp_path):
     for c in cases:
         c.parm.precond = 2
     with Simulation(cases, precision=1) as s:
-        s.run()
+        # the same step-by-step schedule as run_ensemble's output driver
+        while s.step() > 0:
+            pass
         direct = [s.state(m) for m in range(len(cases))]
+        nsteps = [s.num_records(m)[1] for m in range(len(cases))]
     for m, r in enumerate(res):
         assert r["status"] == 1
         np.testing.assert_array_equal(r["pnew"], direct[m][0])
@@ -181,3 +296,7 @@ def test_run_ensemble_on_project_folders_matches_api(tmp_path):
         assert len(sws[-1]) == len(r["pnew"]) and np.all((sws[-1] > 0.0) & (sws[-1] <= 1.0))
         steps, rows = _parse_iter(os.path.join(dirs[m], "output", "iter"))
         assert rows and steps[-1][2] == pytest.approx(1800.0, rel=1e-4)
+        wt = np.loadtxt(os.path.join(dirs[m], "output", "wtdepth"), ndmin=2)
+        assert wt.shape[0] == nsteps[m] and wt[-1, 0] == pytest.approx(1800.0)
+        assert sorted(os.listdir(os.path.join(dirs[m], "output"))) == [
+            "grid3d", "iter", "mbeconv", "psi", "sw", "wtdepth", "xyz"]
