@@ -195,6 +195,46 @@ def test_mesh_only_run_writes_grid3d_without_a_gpu(tmp_path):
     assert (nnod, n, nt) == (m["nnod"], m["n"], m["nt"])
 
 
+def test_cathy_cli_mesh_only_run(tmp_path):
+    """The ``./cathy`` replacement in a project folder (IPRT1 = 3: the mesh
+    files, no GPU)."""
+    import subprocess
+    import sys
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.pycathy import write_project
+    c = config0(tmax=600.0)
+    c.parm.iprt1 = 3
+    write_project(c, str(tmp_path))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, PYTHONPATH=root + os.pathsep + os.environ.get("PYTHONPATH", ""))
+    r = subprocess.run([sys.executable, "-m", "pycathy_wrapper_gb300.cathy_cli"],
+                       cwd=str(tmp_path), env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "mesh written" in r.stdout
+    assert sorted(os.listdir(tmp_path / "output")) == ["grid3d", "xyz"]
+
+
+def test_parm_lists_continued_on_next_lines(tmp_path):
+    """TIMPRT and NODVP are list-directed reads (datin.f:118-119): their
+    values may run on over several lines."""
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.project import read_parm
+    from pycathy_wrapper_gb300.pycathy import write_project
+    write_project(config0(tmax=7200.0), str(tmp_path))
+    path = tmp_path / "input" / "parm"
+    ls = open(path).read().splitlines()
+    k = next(i for i, ln in enumerate(ls) if "TIMPRT" in ln)
+    ls[k] = "4 2 4 600.0 1200.0\tIPRT VTKF NPRT (TIMPRT(I),I=1,NPRT)"
+    ls.insert(k + 1, "3600.0")
+    ls.insert(k + 2, "7200.0")
+    ls[k + 3] = "3 1 2\tNUMVP (NODVP(I),I=1,NUMVP)"
+    ls.insert(k + 4, "9")
+    open(path, "w").write("\n".join(ls) + "\n")
+    p = read_parm(str(path))
+    assert p.timprt == [600.0, 1200.0, 3600.0, 7200.0]
+    assert p.nodvp == [1, 2, 9]
+
+
 class _OracleStepper:
     """The oracle behind the calls of drive_outputs (one member)."""
 
