@@ -131,6 +131,10 @@ int32_t cathy_gb300_mesh(const cathy_dem_t* dem, int32_t iopt, int32_t* out5,
                          int32_t* rowptr, int32_t* cols);
 
 /* ---- handle API --------------------------------------------------------- */
+/* The handle runs the reference's time loop around FLOW3D
+ * (cathy_main.f:2882-3843: time-step control TIMUPD/BKSTEP, one FLOW3D call
+ * per step at :3101, mass balance and output records) for one project or a
+ * whole ensemble batched on one GPU. */
 int32_t cathy_gb300_create(int32_t nmembers, const cathy_member_t* members,
                            const cathy_opts_t* opts, void** handle);
 int32_t cathy_gb300_destroy(void* handle);
@@ -151,6 +155,9 @@ int32_t cathy_gb300_set_state(void* handle, int32_t m, const double* ptimep,
  * SW array that DETOUT writes to the sw output file (detout.f:44-45),
  * VGPNOT*Se(PNEW) + VGRMC/PNODI as CHNEW forms it */
 int32_t cathy_gb300_get_saturation(void* handle, int32_t m, double* sw);
+/* iteration records (one per Picard/Newton iteration: the `iter` file's
+ * lines, conver.f:44-45) and step records (one per accepted step: the
+ * `mbeconv` rows, cathy_main.f:3269-3273) of member m */
 int32_t cathy_gb300_num_records(void* handle, int32_t m, int32_t* niter_recs,
                                 int32_t* nstep_recs);
 int32_t cathy_gb300_get_records(void* handle, int32_t m,
@@ -170,8 +177,10 @@ int32_t cathy_gb300_picard_system(void* handle, int32_t m, double* vals,
 int32_t cathy_gb300_reset(void* handle);
 /* live timing of the SpMV kernel: enable (1) / disable (0) resets the
  * counters; -1 only reads them.  Outputs: total device time of the timed
- * launches (ms, CUDA events on the solver stream), launches, and their
- * algorithmic bytes (values+columns+row pointers+vectors). */
+ * launches (ms; each launch timed on the device clock from its first
+ * block's start to its last block's end, which also works inside the
+ * graph's conditional PCG loop), launches, and their algorithmic bytes
+ * (values+columns+row pointers+vectors). */
 int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
                             int64_t* spmv_launches, double* spmv_bytes);
 /* GPU time spent in the hot path (ms) since creation, and kernel launches */
