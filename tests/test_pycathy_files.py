@@ -165,6 +165,15 @@ def test_water_table_rules():
     assert water_table(np.array([-4.0, -3.0, -2.0, -1.0]), z, 1, 3, [1]) == [0.0]
     # fully saturated with ponding: surface elevation + surface head
     assert water_table(np.array([0.2, 1.2, 2.2, 3.2]), z, 1, 3, [1]) == [pytest.approx(3.2)]
+    # a perched saturated layer above an unsaturated one: the scan from the
+    # bottom keeps the lower crossing (z = 0.5 between p = 0.5 and -0.5)
+    z5 = np.array([4.0, 3.0, 2.0, 1.0, 0.0])
+    p5 = np.array([-0.5, 0.5, -1.0, -0.5, 0.5])
+    assert water_table(p5, z5, 1, 4, [1]) == [pytest.approx(0.5)]
+    # two columns side by side (nnod = 2): column 2's nodes are 1, 3, 5, 7
+    zz = np.repeat(z, 2)
+    pp = np.stack([[-1.5, -0.5, 0.5, 1.5], [-4.0, -3.0, -2.0, -1.0]], 1).ravel()
+    assert water_table(pp, zz, 2, 3, [1, 2]) == [pytest.approx(1.5), 0.0]
 
 
 def test_parm_output_controls_round_trip(tmp_path):
