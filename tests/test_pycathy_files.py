@@ -294,6 +294,48 @@ def test_drive_outputs_print_times_and_water_table():
     np.testing.assert_array_equal(snaps[0][-1][2], p_end)
 
 
+class _ScriptedStepper:
+    """Two members on a 1-column, 3-layer mesh: member 0 accepts a step of
+    100 s per call up to 500 s, member 1 fails after two steps."""
+
+    def __init__(self):
+        self.k = [0, 0]
+        self.dead = [False, False]
+
+    def step(self):
+        for m in (0, 1):
+            if self.dead[m] or (m == 0 and self.k[0] == 5):
+                continue
+            if m == 1 and self.k[1] == 2:
+                self.dead[1] = True  # the failed member accepts no more steps
+                continue
+            self.k[m] += 1
+        return sum(1 for m in (0, 1) if not self.dead[m] and not (m == 0 and self.k[0] == 5))
+
+    def state(self, m):
+        p = np.array([-1.0, -0.5, 0.5, 1.0]) + 0.01 * self.k[m]
+        return p, 100.0 * self.k[m], 100.0, (2 if self.dead[m] else 0)
+
+    def saturation(self, m):
+        return np.full(4, 0.5 + 0.01 * self.k[m])
+
+    def num_steps(self, m):
+        return self.k[m]
+
+
+def test_drive_outputs_with_a_failing_member():
+    from pycathy_wrapper_gb300.inputs import Parm
+    from pycathy_wrapper_gb300.pycathy import drive_outputs
+    mesh = dict(z=np.array([3.0, 2.0, 1.0, 0.0]), nnod=1, nstr=3)
+    parms = [Parm(timprt=[250.0, 500.0], nodvp=[1]), Parm(timprt=[250.0], nodvp=[1])]
+    snaps, wt = drive_outputs(_ScriptedStepper(), 2, parms, [mesh, mesh])
+    assert [(k, t) for k, t, _, _ in snaps[0]] == [(0, 0.0), (3, 300.0), (5, 500.0)]
+    # the failed member: its start and the last step it accepted
+    assert [(k, t) for k, t, _, _ in snaps[1]] == [(0, 0.0), (2, 200.0)]
+    assert [t for t, _ in wt[0]] == [100.0, 200.0, 300.0, 400.0, 500.0]
+    assert [t for t, _ in wt[1]] == [100.0, 200.0]
+
+
 @pytest.mark.gpu
 def test_saturation_matches_oracle():
     """Sw at the current heads (the sw output's array) against the oracle's
