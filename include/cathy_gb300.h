@@ -305,9 +305,11 @@ int32_t cathy_gb300_learned_stats(void* handle, double* out, int32_t n);
  * call.  That array is held on every GPU that loads the library until the
  * process exits, and it bounds n at CATHY_GB300_NOALLOC_MAXN rows; larger
  * systems are rejected with CATHY_GB300_EINVAL.  The first call on a device
- * looks up the array's device address (make that first call before any
- * stream capture).  Every call reuses the same array, so calls that overlap
- * on the GPU (from two streams or two host threads) race on it. */
+ * looks up the array's device address.  The function waits for `stream` at
+ * every iteration (it reads the convergence test back into host memory), so
+ * it must not be called while that stream is being captured into a CUDA
+ * graph.  Every call reuses the same array, so calls that overlap on the GPU
+ * (from two streams or two host threads) race on it. */
 #define CATHY_GB300_NOALLOC_MAXN 131072
 int32_t cathy_gb300_nsyslv_noalloc(const int32_t* n, const int32_t* numdir,
                                    const int32_t* noddir_dev,

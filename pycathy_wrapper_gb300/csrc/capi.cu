@@ -172,7 +172,7 @@ int32_t cathy_gb300_symslv(const int32_t* iout, const int32_t* n,
                            double* res) {
   (void)iout; (void)scr;
   if (!n || !nterm || !numdir || !niter || !itmxcg || !tolcg || !ja || !topol ||
-      !pnew || !tnoti || !coef1 || *n <= 0)
+      !pnew || !tnoti || !coef1 || *n <= 0 || *numdir < 0 || (*numdir > 0 && !noddir))
     return CATHY_GB300_EINVAL;
   if (!have_device()) return CATHY_GB300_ENODEV;
   return guarded([&]() {
@@ -192,7 +192,8 @@ int32_t cathy_gb300_nsyslv(const int32_t* isolv, const int32_t* iout,
                            double* err, double* res) {
   (void)iout; (void)ia;
   if (!isolv || !n || !nterm || !numdir || !itmxcg || !niter || !ja || !topol ||
-      !tolcg || !coef1 || !pnew || !tnoti || *n <= 0)
+      !tolcg || !coef1 || !pnew || !tnoti || *n <= 0 || *numdir < 0 ||
+      (*numdir > 0 && !noddir))
     return CATHY_GB300_EINVAL;
   if (!have_device()) return CATHY_GB300_ENODEV;
   return guarded([&]() {

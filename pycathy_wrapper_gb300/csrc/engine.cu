@@ -5073,7 +5073,10 @@ int dropin_symslv(int n, int nterm, int numdir, const int32_t* noddir,
   std::vector<double> vals(cols.size());
   for (size_t s = 0; s < cols.size(); ++s) vals[s] = coef1[up[s]];
   std::vector<uint8_t> dm(n, 0);
-  for (int k = 0; k < numdir; ++k) dm[noddir[k] - 1] = 1;
+  for (int k = 0; k < numdir; ++k) {
+    if (noddir[k] < 1 || noddir[k] > n) throw std::string("NODDIR entry outside 1..N");
+    dm[noddir[k] - 1] = 1;
+  }
   std::vector<double> b(tnoti, tnoti + n);
   for (int i = 0; i < n; ++i) if (dm[i]) b[i] = 0.0;
   Engine E;
@@ -5114,7 +5117,10 @@ int dropin_nsyslv(int isolv, int n, int nterm, int numdir, const int32_t* noddir
   for (int s = 0; s < nterm; ++s) cols[s] = ja[s] - 1;
   std::vector<double> vals(coef1, coef1 + nterm);
   std::vector<uint8_t> dm(n, 0);
-  for (int k = 0; k < numdir; ++k) dm[noddir[k] - 1] = 1;
+  for (int k = 0; k < numdir; ++k) {
+    if (noddir[k] < 1 || noddir[k] > n) throw std::string("NODDIR entry outside 1..N");
+    dm[noddir[k] - 1] = 1;
+  }
   std::vector<double> b(tnoti, tnoti + n);
   double bn = 0.0;
   for (int i = 0; i < n; ++i) { if (dm[i]) b[i] = 0.0; bn += tnoti[i] * tnoti[i]; }

@@ -39,7 +39,7 @@ static __device__ __align__(256) double g_scratch[kScratchDoubles];
 // scalar slots (after the vectors and the mask)
 enum {
   S_XL = 0, S_ROJ, S_SIG, S_AA, S_BB, S_RR, S_ROJM1, S_ALFJM1, S_ETAJ, S_ERR,
-  S_TRR, S_TBB, S_NITER, S_ACTIVE
+  S_TRR, S_TBB, S_NITER, S_ACTIVE, S_BN
 };
 
 struct Work {
@@ -136,11 +136,13 @@ __global__ void k_mark(int numdir, const int32_t* noddir, int n, Work w) {
   }
 }
 
-// dinv = 1/a_ii (1 at Dirichlet rows); x0 = dinv*b; xl = |b_masked|^2
+// dinv = 1/a_ii (1 at Dirichlet rows); x0 = dinv*b; xl = |b_masked|^2 (the
+// error norm's denominator) and, in its own slot, the sum of TNOTI^2 over
+// every row, Dirichlet rows included (NSYSLV's zero right-hand-side test)
 __global__ void k_setup(int n, const int32_t* topol, const int32_t* ja, const double* a,
                         const double* tnoti, double* x, Work w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[1] = {0.0};
+  double v[1] = {0.0}, u[1] = {0.0};
   if (i < n) {
     double d = 1.0;
     if (!w.dm[i]) {
@@ -152,8 +154,10 @@ __global__ void k_setup(int n, const int32_t* topol, const int32_t* ja, const do
     const double b = w.dm[i] ? 0.0 : tnoti[i];
     x[i] = d * b;
     v[0] = b * b;
+    u[0] = tnoti[i] * tnoti[i];
   }
   block_sum<1>(v, w.sc + S_XL);
+  block_sum<1>(u, w.sc + S_BN);
 }
 
 // out = dinv * (A in) with Dirichlet rows as identity (16 lanes per row);
@@ -318,11 +322,15 @@ extern "C" int32_t cathy_gb300_nsyslv_noalloc(
   k_clear<<<blocks(n > kNumScal ? n : kNumScal, kThreads), kThreads, 0, st>>>(n, w);
   if (numdir > 0) k_mark<<<blocks(numdir, kThreads), kThreads, 0, st>>>(numdir, noddir_d, n, w);
   k_setup<<<gn, kThreads, 0, st>>>(n, topol_d, ja_d, coef1_d, tnoti_d, pnew_d, w);
-  double xl = 0.0;
-  if ((e = cudaMemcpyAsync(&xl, w.sc + S_XL, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+  // a launch that failed without a sticky error (no kernel image for the
+  // device, say) would otherwise leave the copy below reading a slot that
+  // nothing wrote
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "set-up launch");
+  double bn = 0.0;
+  if ((e = cudaMemcpyAsync(&bn, w.sc + S_BN, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return fail(e, "set-up");
-  if (xl == 0.0) {  // NSYSLV returns PNEW = 0 for a zero right-hand side
+  if (bn == 0.0) {  // NSYSLV returns PNEW = 0 when every TNOTI is zero
     if ((e = cudaMemsetAsync(pnew_d, 0, sizeof(double) * n, st)) != cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess)
       return fail(e, "zero solution");

@@ -80,16 +80,28 @@ def test_noalloc_matches_allocating_nsyslv_twice():
     t_nod = torch.from_numpy(noddir).to(dev)
     torch.cuda.synchronize()
     scale = np.max(np.abs(x_ref))
+    # the second call runs on a stream of its own: the entry point must
+    # launch on the stream it is given
+    side = torch.cuda.Stream(device=dev)
+    outs = [torch.full((n,), float("nan"), dtype=torch.float64, device=dev) for _ in range(2)]
+    torch.cuda.synchronize()
     for call in range(2):
-        t_x = torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
-        torch.cuda.synchronize()
+        t_x = outs[call]
+        stream = None if call == 0 else C.c_void_p(side.cuda_stream)
+        free_before = torch.cuda.mem_get_info(dev)[0]
         niter, err, res = C.c_int32(), C.c_double(), C.c_double()
         rc = L.cathy_gb300_nsyslv_noalloc(
             _ci(n), _ci(len(noddir)), C.c_void_p(t_nod.data_ptr()), _ci(500), C.byref(niter),
             C.c_void_p(t_ja.data_ptr()), C.c_void_p(t_topol.data_ptr()), _cd(1e-10),
             C.c_void_p(t_vals.data_ptr()), C.c_void_p(t_x.data_ptr()),
-            C.c_void_p(t_tn.data_ptr()), C.byref(err), C.byref(res), None)
+            C.c_void_p(t_tn.data_ptr()), C.byref(err), C.byref(res), stream)
         assert rc == _lib.OK, (call, rc)
+        if call == 1:
+            # after the first call (which loads the library's device code and
+            # its fixed workspace) a call takes no device memory
+            side.synchronize()
+            assert torch.cuda.mem_get_info(dev)[0] == free_before
+        torch.cuda.synchronize()
         x = t_x.cpu().numpy()
         # same tolerance as the NSYSLV drop-in's own parity test
         assert np.all(np.isfinite(x)), call
