@@ -444,6 +444,43 @@ int nsyslv(int isolv, int n, int numdir, const int* noddir, int itmxcg,
 // ---------------------------------------------------------------------------
 // The oracle state
 // ---------------------------------------------------------------------------
+// ASSPIC (asspic.f:9-54) on the reference's own arrays: 1-based TETRA(5,NT)
+// and TETJA(4,4,NT) contents, column-major LMASS(4,4), BI/CI/DI(4,NT) and
+// PERMX/PERMY/PERMZ(MAXSTR,*); COEF1/COEF2/COEF4 (C pointers to the Fortran
+// arrays, 1-based contents) are accumulated in the reference's element order
+// with its left-to-right sums: COEF1(IND) + PVKB*BI(L) + PVKC*CI(L) + PVKD*DI(L).
+void asspic(int nt, int ntri, const int* tetra, const int* tetja, const double* lmass,
+            double* coef1, double* coef2, double* coef4, const double* et1e,
+            const double* pel, const double* permx, const double* permy,
+            const double* permz, const double* ckrwe, const double* volu,
+            const double* volur, const double* bi, const double* ci, const double* di,
+            int maxstr) {
+  for (int iel = 1; iel <= nt; ++iel) {
+    int istr = 1 + iel / (ntri * 3);
+    const int ir = iel % (ntri * 3);
+    if (ir == 0) istr -= 1;
+    const int mtype = tetra[5 * (iel - 1) + 4];
+    const int id = (istr - 1) + maxstr * (mtype - 1);
+    const int e = iel - 1;
+    const double vk = volur[e] * ckrwe[e];
+    const double ve1 = volu[e] * et1e[e];
+    const double ve = volu[e] * pel[e];
+    const double pvk1 = permx[id] * vk, pvk2 = permy[id] * vk, pvk3 = permz[id] * vk;
+    for (int k = 1; k <= 4; ++k) {
+      const double pvkb = pvk1 * bi[4 * e + k - 1], pvkc = pvk2 * ci[4 * e + k - 1],
+                   pvkd = pvk3 * di[4 * e + k - 1];
+      for (int l = k; l <= 4; ++l) {
+        const int ind = tetja[16 * e + 4 * (l - 1) + (k - 1)] - 1;
+        const double lm = lmass[4 * (l - 1) + (k - 1)];
+        coef1[ind] = coef1[ind] + pvkb * bi[4 * e + l - 1] + pvkc * ci[4 * e + l - 1] +
+                     pvkd * di[4 * e + l - 1];
+        coef2[ind] = coef2[ind] + ve1 * lm;
+        coef4[ind] = coef4[ind] + ve * lm;
+      }
+    }
+  }
+}
+
 struct Oracle {
   // sizes
   int nrow = 0, ncol = 0, nnod = 0, ntri = 0, nstr = 0, n = 0, nt = 0,
@@ -553,6 +590,17 @@ struct Oracle {
              b1r * b1r;
     }
     return 0.0;
+  }
+
+  // ASSPIC on the oracle's state (element arrays are 1-based vectors)
+  void asspic_state() {
+    double lm[16];
+    for (int k = 1; k <= 4; ++k)
+      for (int l = 1; l <= 4; ++l) lm[4 * (l - 1) + (k - 1)] = lmass[k][l];
+    asspic(nt, ntri, tetra.data(), tetja.data(), lm, coef1.data() + 1, coef2.data() + 1,
+           coef4.data() + 1, et1e.data() + 1, pel.data() + 1, permx.data(), permy.data(),
+           permz.data(), ckrwe.data() + 1, volu.data() + 1, volur.data() + 1, bi.data(),
+           ci.data(), di.data(), nstr);
   }
 
   // NODELT (nodelt.f:9-29)
@@ -1113,24 +1161,7 @@ void Oracle::picard() {
   std::fill(coef4.begin(), coef4.end(), 0.0);
   std::fill(coef5.begin(), coef5.end(), 0.0);
   // ASSPIC (asspic.f:26-51)
-  for (int iel = 1; iel <= nt; ++iel) {
-    int istr = istr_of(iel);
-    int mtype = T(5, iel);
-    int id = idx(istr, mtype);
-    double vk = volur[iel] * ckrwe[iel];
-    double ve1 = volu[iel] * et1e[iel];
-    double ve = volu[iel] * pel[iel];
-    double pvk1 = permx[id] * vk, pvk2 = permy[id] * vk, pvk3 = permz[id] * vk;
-    for (int k = 1; k <= 4; ++k) {
-      double pvkb = pvk1 * B(k, iel), pvkc = pvk2 * C(k, iel), pvkd = pvk3 * D(k, iel);
-      for (int l = k; l <= 4; ++l) {
-        int ind = TJ(k, l, iel);
-        coef1[ind] = coef1[ind] + pvkb * B(l, iel) + pvkc * C(l, iel) + pvkd * D(l, iel);
-        coef2[ind] = coef2[ind] + ve1 * lmass[k][l];
-        coef4[ind] = coef4[ind] + ve * lmass[k][l];
-      }
-    }
-  }
+  asspic_state();
   // RHSPIC (rhspic.f:22-38)
   for (int k = 1; k <= n; ++k) tnoti[k] = 0.0;
   double rdt = 1.0 / deltat;
@@ -1771,21 +1802,7 @@ void orc_picard_system(void* h, double* coef1, double* tnoti, double* xt5,
   std::fill(r.coef2.begin(), r.coef2.end(), 0.0);
   std::fill(r.coef4.begin(), r.coef4.end(), 0.0);
   std::fill(r.coef5.begin(), r.coef5.end(), 0.0);
-  for (int iel = 1; iel <= r.nt; ++iel) {
-    int id = r.idx(r.istr_of(iel), r.T(5, iel));
-    double vk = r.volur[iel] * r.ckrwe[iel];
-    double ve1 = r.volu[iel] * r.et1e[iel], ve = r.volu[iel] * r.pel[iel];
-    double pvk1 = r.permx[id] * vk, pvk2 = r.permy[id] * vk, pvk3 = r.permz[id] * vk;
-    for (int k = 1; k <= 4; ++k) {
-      double pvkb = pvk1 * r.B(k, iel), pvkc = pvk2 * r.C(k, iel), pvkd = pvk3 * r.D(k, iel);
-      for (int l = k; l <= 4; ++l) {
-        int ind = r.TJ(k, l, iel);
-        r.coef1[ind] += pvkb * r.B(l, iel) + pvkc * r.C(l, iel) + pvkd * r.D(l, iel);
-        r.coef2[ind] += ve1 * r.lmass[k][l];
-        r.coef4[ind] += ve * r.lmass[k][l];
-      }
-    }
-  }
+  r.asspic_state();
   double rdt = 1.0 / r.deltat;
   for (int k = 1; k <= r.n; ++k) r.tnoti[k] = 0.0;
   for (int k = 1; k <= r.n; ++k) {
@@ -1819,6 +1836,35 @@ void orc_picard_system(void* h, double* coef1, double* tnoti, double* xt5,
       r.tnoti[k] += r.parm.tetaf * r.atmact[k] + (1.0 - r.parm.tetaf) * r.atmold[k];
   for (int k = 1; k <= r.n; ++k) tnoti[k - 1] = r.tnoti[k];
   for (int k = 1; k <= r.nterm; ++k) coef1[k - 1] = r.coef1[k];
+}
+
+void orc_asspic(int32_t nt, int32_t ntri, const int32_t* tetra, const int32_t* tetja,
+                const double* lmass, double* coef1, double* coef2, double* coef4,
+                const double* et1e, const double* pel, const double* permx,
+                const double* permy, const double* permz, const double* ckrwe,
+                const double* volu, const double* volur, const double* bi,
+                const double* ci, const double* di, int32_t maxstr) {
+  asspic(nt, ntri, tetra, tetja, lmass, coef1, coef2, coef4, et1e, pel, permx, permy, permz,
+         ckrwe, volu, volur, bi, ci, di, maxstr);
+}
+
+void orc_asspic_inputs(void* h, int32_t* tetja, double* lmass, double* et1e, double* pel,
+                       double* permx, double* permy, double* permz, double* ckrwe,
+                       double* volu, double* volur, double* bi, double* ci, double* di) {
+  Oracle* o = (Oracle*)h;
+  std::copy(o->tetja.begin(), o->tetja.begin() + 16 * (size_t)o->nt, tetja);
+  for (int k = 1; k <= 4; ++k)
+    for (int l = 1; l <= 4; ++l) lmass[4 * (l - 1) + (k - 1)] = o->lmass[k][l];
+  for (int e = 1; e <= o->nt; ++e) {
+    et1e[e - 1] = o->et1e[e]; pel[e - 1] = o->pel[e]; ckrwe[e - 1] = o->ckrwe[e];
+    volu[e - 1] = o->volu[e]; volur[e - 1] = o->volur[e];
+  }
+  std::copy(o->permx.begin(), o->permx.end(), permx);
+  std::copy(o->permy.begin(), o->permy.end(), permy);
+  std::copy(o->permz.begin(), o->permz.end(), permz);
+  std::copy(o->bi.begin(), o->bi.begin() + 4 * (size_t)o->nt, bi);
+  std::copy(o->ci.begin(), o->ci.begin() + 4 * (size_t)o->nt, ci);
+  std::copy(o->di.begin(), o->di.begin() + 4 * (size_t)o->nt, di);
 }
 
 void orc_vg_nodal(void* h, const double* psi, double* sw, double* ckrw,

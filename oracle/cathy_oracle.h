@@ -110,6 +110,21 @@ void orc_set_state(void* h, const double* ptimep, double time, double deltat);
  * storage (topol/ja of IOPT=1). */
 void orc_picard_system(void* h, double* coef1, double* tnoti, double* xt5,
                        int32_t* dirmask);
+/* ASSPIC (asspic.f:9) with the reference's argument list: TETRA(5,NT) and
+ * TETJA(4,4,NT) with 1-based contents, column-major LMASS(4,4), BI/CI/DI(4,NT),
+ * PERMX/PERMY/PERMZ(MAXSTR,*); COEF1/COEF2/COEF4 are accumulated in place. */
+void orc_asspic(int32_t nt, int32_t ntri, const int32_t* tetra, const int32_t* tetja,
+                const double* lmass, double* coef1, double* coef2, double* coef4,
+                const double* et1e, const double* pel, const double* permx,
+                const double* permy, const double* permz, const double* ckrwe,
+                const double* volu, const double* volur, const double* bi,
+                const double* ci, const double* di, int32_t maxstr);
+/* ASSPIC's inputs at the current state (after orc_picard_system): TETJA
+ * (16*nt), LMASS (16), ET1E/PEL/CKRWE/VOLU/VOLUR (nt), PERMX/PERMY/PERMZ
+ * (nstr*nzone, leading dimension nstr), BI/CI/DI (4*nt) */
+void orc_asspic_inputs(void* h, int32_t* tetja, double* lmass, double* et1e, double* pel,
+                       double* permx, double* permy, double* permz, double* ckrwe,
+                       double* volu, double* volur, double* bi, double* ci, double* di);
 /* nodal soil characteristics at heads psi (n): sw, ckrw, etai, et2 */
 void orc_vg_nodal(void* h, const double* psi, double* sw, double* ckrw,
                   double* etai, double* et2);

@@ -100,6 +100,8 @@ def lib():
         L.orc_set_state.argtypes = [C.c_void_p, f64p, C.c_double, C.c_double]
         L.orc_picard_system.argtypes = [C.c_void_p, f64p, f64p, f64p, i32p]
         L.orc_vg_nodal.argtypes = [C.c_void_p, f64p, f64p, f64p, f64p, f64p]
+        L.orc_asspic.argtypes = [C.c_int32, C.c_int32, i32p, i32p] + [f64p] * 15 + [C.c_int32]
+        L.orc_asspic_inputs.argtypes = [C.c_void_p, i32p] + [f64p] * 12
         L.orc_symslv.restype = C.c_int32
         L.orc_symslv.argtypes = [C.c_int32, C.c_int32, C.c_int32, i32p, i32p, i32p,
                                  f64p, f64p, f64p, C.c_int32, C.c_double, C.c_int32, f64p]
@@ -225,6 +227,25 @@ class Oracle:
         lib().orc_picard_system(self.h, _f64(c1)[1], _f64(tn)[1], _f64(xt5)[1], _i32(dm)[1])
         return c1, tn, xt5, dm
 
+    def asspic_inputs(self):
+        """ASSPIC's arguments at the current state (call after picard_system):
+        the reference's arrays in memory order."""
+        nt = self.nt
+        tetja = np.zeros(16 * nt, np.int32)
+        lmass = np.zeros(16)
+        e = [np.zeros(nt) for _ in range(5)]
+        nzs = len(self.case.soil.permx.reshape(-1))
+        p = [np.zeros(nzs) for _ in range(3)]
+        g = [np.zeros(4 * nt) for _ in range(3)]
+        et1e, pel, ckrwe, volu, volur = e
+        lib().orc_asspic_inputs(self.h, _i32(tetja)[1], _f64(lmass)[1], _f64(et1e)[1],
+                                _f64(pel)[1], *[_f64(a)[1] for a in p], _f64(ckrwe)[1],
+                                _f64(volu)[1], _f64(volur)[1], *[_f64(a)[1] for a in g])
+        return dict(tetra=self.mesh()["tetra"], tetja=tetja, lmass=lmass, et1e=et1e, pel=pel,
+                    permx=p[0], permy=p[1], permz=p[2], ckrwe=ckrwe, volu=volu, volur=volur,
+                    bi=g[0], ci=g[1], di=g[2], ntri=self.ntri,
+                    maxstr=self.case.dem.nstr)
+
     def vg_nodal(self, psi):
         psi, pp = _f64(psi)
         out = [np.zeros(self.n) for _ in range(4)]
@@ -255,3 +276,20 @@ def nsyslv(topol, ja, coef1, b, noddir, isolv=0, itmxcg=500, tolcg=1e-10):
                              _i32(topol)[1], _f64(x)[1], _f64(b)[1], _f64(coef1)[1],
                              itmxcg, tolcg, _f64(er)[1])
     return x, int(niter), float(er[0]), float(er[1])
+
+
+def asspic(tetra, tetja, lmass, coef1, coef2, coef4, et1e, pel, permx, permy, permz,
+           ckrwe, volu, volur, bi, ci, di, ntri, maxstr):
+    """Reference ASSPIC on the caller's arrays (same layout as the drop-in);
+    returns accumulated copies of COEF1, COEF2, COEF4."""
+    tetra = np.ascontiguousarray(tetra, np.int32).reshape(-1)
+    tetja = np.ascontiguousarray(tetja, np.int32).reshape(-1)
+    c1, c2, c4 = (np.array(a, np.float64) for a in (coef1, coef2, coef4))
+    arrs = [np.ascontiguousarray(a, np.float64).reshape(-1)
+            for a in (lmass, et1e, pel, permx, permy, permz, ckrwe, volu, volur, bi, ci, di)]
+    lm, a1, a2, px, py, pz, kr, vo, vr, b, c, d = arrs
+    lib().orc_asspic(len(tetra) // 5, ntri, _i32(tetra)[1], _i32(tetja)[1], _f64(lm)[1],
+                     _f64(c1)[1], _f64(c2)[1], _f64(c4)[1], _f64(a1)[1], _f64(a2)[1],
+                     _f64(px)[1], _f64(py)[1], _f64(pz)[1], _f64(kr)[1], _f64(vo)[1],
+                     _f64(vr)[1], _f64(b)[1], _f64(c)[1], _f64(d)[1], maxstr)
+    return c1, c2, c4

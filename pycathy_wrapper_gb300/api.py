@@ -309,3 +309,32 @@ def nsyslv(topol, ja, coef1, tnoti, noddir, isolv=0, itmxcg=500, tolcg=1e-10,
                                _ptr(tnoti, f64p), C.byref(err), C.byref(res)),
           "cathy_gb300_nsyslv")
     return pnew, niter.value, err.value, res.value
+
+
+def asspic(tetra, tetja, lmass, coef1, coef2, coef4, et1e, pel, permx, permy, permz,
+           ckrwe, volu, volur, bi, ci, di, ntri, maxstr, etae=None):
+    """ASSPIC drop-in (asspic.f:9): element assembly of the Picard stiffness
+    (COEF1) and mass (COEF2, COEF4) arrays on the GPU.
+
+    Arguments carry the reference's contents: ``tetra`` (nt, 5) and ``tetja``
+    (nt, 4, 4) hold 1-based node ids / slot indices, ``tetja[e, l, k]`` being
+    TETJA(K,L,IEL) (the Fortran array in memory order); ``lmass`` is LMASS
+    (4, 4) in memory order; ``permx/permy/permz`` are PERMX(MAXSTR, NZONE)
+    flattened in memory order; ``bi/ci/di`` are BI(4, NT) in memory order.
+    The COEF arrays are accumulated (copies are returned)."""
+    L = _lib.load()
+    tetra, tetja = _i32(tetra).reshape(-1), _i32(tetja).reshape(-1)
+    nt = len(tetra) // 5
+    c1, c2, c4 = _f64(coef1).copy(), _f64(coef2).copy(), _f64(coef4).copy()
+    nterm = len(c1)
+    keep = [_f64(a).reshape(-1) for a in (lmass, et1e, pel, permx, permy, permz, ckrwe,
+                                          volu, volur, bi, ci, di)]
+    lm, a1, a2, px, py, pz, kr, vo, vr, b, c, d = keep
+    et = _f64(etae) if etae is not None else np.zeros(nt)
+    check(L.cathy_gb300_asspic(_ci(nt), _ci(ntri), _ptr(tetra, i32p), _ptr(tetja, i32p),
+                               _ptr(lm, f64p), _ptr(c1, f64p), _ptr(c2, f64p), _ptr(c4, f64p),
+                               _ptr(a1, f64p), _ptr(a2, f64p), _ptr(px, f64p), _ptr(py, f64p),
+                               _ptr(pz, f64p), _ptr(kr, f64p), _ptr(et, f64p), _ptr(vo, f64p),
+                               _ptr(vr, f64p), _ptr(b, f64p), _ptr(c, f64p), _ptr(d, f64p),
+                               _ci(maxstr), _ci(nterm)), "cathy_gb300_asspic")
+    return c1, c2, c4

@@ -5149,35 +5149,46 @@ int dropin_nsyslv(int isolv, int n, int nterm, int numdir, const int32_t* noddir
   return 0;
 }
 
-// ASSPIC drop-in: element-parallel assembly into the caller's upper CSR
-// arrays through TETJA (atomic accumulation).
-__global__ void k_asspic(int nt, int ntri, int maxstr, const int32_t* tetra,
-                         const int32_t* tetja, const double* lmass,
-                         double* coef1, double* coef2, double* coef4,
-                         const double* et1e, const double* pel,
-                         const double* permx, const double* permy,
-                         const double* permz, const double* ckrwe,
-                         const double* volur, const double* volu,
-                         const double* bi, const double* ci, const double* di) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nt) return;
-  const int iel = e + 1;
-  int istr = 1 + iel / (ntri * 3);
-  if (iel % (ntri * 3) == 0) istr -= 1;
-  const int mtype = tetra[5 * e + 4];
-  const int id = (mtype - 1) * maxstr + (istr - 1);
-  const double vk = volur[e] * ckrwe[e];
-  const double ve1 = volu[e] * et1e[e], ve = volu[e] * pel[e];
-  const double pvk1 = permx[id] * vk, pvk2 = permy[id] * vk, pvk3 = permz[id] * vk;
-  for (int k = 0; k < 4; ++k) {
-    const double pvkb = pvk1 * bi[4 * e + k], pvkc = pvk2 * ci[4 * e + k], pvkd = pvk3 * di[4 * e + k];
-    for (int l = k; l < 4; ++l) {
-      const int ind = tetja[16 * e + 4 * l + k] - 1;
-      atomicAdd(coef1 + ind, pvkb * bi[4 * e + l] + pvkc * ci[4 * e + l] + pvkd * di[4 * e + l]);
-      atomicAdd(coef2 + ind, ve1 * lmass[4 * l + k]);
-      atomicAdd(coef4 + ind, ve * lmass[4 * l + k]);
-    }
+// ASSPIC drop-in (asspic.f:9-54), row-owned: one thread per COEF slot.  The
+// slot's contributions come from an inverse TETJA map (slot -> element*16 +
+// K*4 + L, elements in increasing order, built on the host), so each slot
+// receives them in the reference's element order.  Every product and sum is
+// rounded on its own (no fused multiply-add) and the three terms of COEF1
+// are added left to right, COEF1(IND) + PVKB*BI(L) + PVKC*CI(L) +
+// PVKD*DI(L): the result equals the reference's serial loop bit for bit and
+// does not depend on the launch.
+__global__ void k_asspic_gather(int nterm, int ntri, int maxstr, const int32_t* cptr,
+                                const int32_t* code, const int32_t* tetra,
+                                const double* lmass, double* coef1, double* coef2,
+                                double* coef4, const double* et1e, const double* pel,
+                                const double* permx, const double* permy,
+                                const double* permz, const double* ckrwe,
+                                const double* volur, const double* volu,
+                                const double* bi, const double* ci, const double* di) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nterm) return;
+  double a1 = coef1[s], a2 = coef2[s], a4 = coef4[s];
+  for (int q = cptr[s]; q < cptr[s + 1]; ++q) {
+    const int c = code[q];
+    const int e = c >> 4, k = (c >> 2) & 3, l = c & 3;
+    const int iel = e + 1;
+    int istr = 1 + iel / (ntri * 3);
+    if (iel % (ntri * 3) == 0) istr -= 1;
+    const int id = (istr - 1) + maxstr * (tetra[5 * e + 4] - 1);
+    const double vk = __dmul_rn(volur[e], ckrwe[e]);
+    const double pvkb = __dmul_rn(__dmul_rn(permx[id], vk), bi[4 * e + k]);
+    const double pvkc = __dmul_rn(__dmul_rn(permy[id], vk), ci[4 * e + k]);
+    const double pvkd = __dmul_rn(__dmul_rn(permz[id], vk), di[4 * e + k]);
+    a1 = __dadd_rn(a1, __dmul_rn(pvkb, bi[4 * e + l]));
+    a1 = __dadd_rn(a1, __dmul_rn(pvkc, ci[4 * e + l]));
+    a1 = __dadd_rn(a1, __dmul_rn(pvkd, di[4 * e + l]));
+    const double lm = lmass[4 * l + k];
+    a2 = __dadd_rn(a2, __dmul_rn(__dmul_rn(volu[e], et1e[e]), lm));
+    a4 = __dadd_rn(a4, __dmul_rn(__dmul_rn(volu[e], pel[e]), lm));
   }
+  coef1[s] = a1;
+  coef2[s] = a2;
+  coef4[s] = a4;
 }
 
 int dropin_asspic(int nt, int ntri, const int32_t* tetra, const int32_t* tetja,
@@ -5187,15 +5198,48 @@ int dropin_asspic(int nt, int ntri, const int32_t* tetra, const int32_t* tetja,
                   const double* permz, const double* ckrwe,
                   const double* volur, const double* volu, const double* bi,
                   const double* ci, const double* di, int maxstr, int nterm) {
+  if (ntri <= 0 || maxstr <= 0 || nterm <= 0) return CATHY_GB300_EINVAL;
+  if ((long)nt >= (1L << 27)) throw std::string("too many elements for the ASSPIC drop-in");
+  int nzone = 0;
+  for (int e = 0; e < nt; ++e) {
+    if (tetra[5 * e + 4] < 1) throw std::string("TETRA zone id below 1");
+    nzone = std::max(nzone, (int)tetra[5 * e + 4]);
+    const int iel = e + 1;
+    const int istr = 1 + iel / (ntri * 3) - (iel % (ntri * 3) == 0 ? 1 : 0);
+    if (istr < 1 || istr > maxstr) throw std::string("element layer outside 1..MAXSTR");
+  }
+  // inverse TETJA map: counting sort of the (K <= L) pairs by slot, stable in
+  // element order
+  std::vector<int32_t> cptr((size_t)nterm + 1, 0), code((size_t)10 * nt);
+  for (int e = 0; e < nt; ++e)
+    for (int k = 0; k < 4; ++k)
+      for (int l = k; l < 4; ++l) {
+        const int ind = tetja[16 * (size_t)e + 4 * l + k];
+        if (ind < 1 || ind > nterm) throw std::string("TETJA entry outside 1..NTERM");
+        cptr[ind]++;
+      }
+  for (int q = 0; q < nterm; ++q) cptr[q + 1] += cptr[q];
+  {
+    std::vector<int32_t> fill(cptr.begin(), cptr.end() - 1);
+    for (int e = 0; e < nt; ++e)
+      for (int k = 0; k < 4; ++k)
+        for (int l = k; l < 4; ++l) {
+          const int ind = tetja[16 * (size_t)e + 4 * l + k] - 1;
+          code[fill[ind]++] = (e << 4) | (k << 2) | l;
+        }
+  }
   cudaStream_t st;
   CG_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  int nzone = 0;
-  for (int e = 0; e < nt; ++e) nzone = std::max(nzone, (int)tetra[5 * e + 4]);
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
+  } guard{st};
   const size_t tsz = (size_t)maxstr * nzone;
-  DBuf<int32_t> t, tj;
+  DBuf<int32_t> t, cp, cd;
   DBuf<double> lm, c1, c2, c4, a1, a2, px, py, pz, kr, vr, vo, b, c, d;
   t.alloc(5 * (size_t)nt); t.upload(tetra, 5 * (size_t)nt, st);
-  tj.alloc(16 * (size_t)nt); tj.upload(tetja, 16 * (size_t)nt, st);
+  cp.alloc(cptr.size()); cp.upload(cptr.data(), cptr.size(), st);
+  cd.alloc(code.size()); cd.upload(code.data(), code.size(), st);
   lm.alloc(16); lm.upload(lmass, 16, st);
   c1.alloc(nterm); c1.upload(coef1, nterm, st);
   c2.alloc(nterm); c2.upload(coef2, nterm, st);
@@ -5211,14 +5255,14 @@ int dropin_asspic(int nt, int ntri, const int32_t* tetra, const int32_t* tetja,
   b.alloc(4 * (size_t)nt); b.upload(bi, 4 * (size_t)nt, st);
   c.alloc(4 * (size_t)nt); c.upload(ci, 4 * (size_t)nt, st);
   d.alloc(4 * (size_t)nt); d.upload(di, 4 * (size_t)nt, st);
-  k_asspic<<<cdiv(nt, 128), 128, 0, st>>>(nt, ntri, maxstr, t.p, tj.p, lm.p, c1.p, c2.p, c4.p,
-                                          a1.p, a2.p, px.p, py.p, pz.p, kr.p, vr.p, vo.p, b.p, c.p, d.p);
+  k_asspic_gather<<<cdiv(nterm, 128), 128, 0, st>>>(nterm, ntri, maxstr, cp.p, cd.p, t.p, lm.p,
+                                                    c1.p, c2.p, c4.p, a1.p, a2.p, px.p, py.p, pz.p,
+                                                    kr.p, vr.p, vo.p, b.p, c.p, d.p);
   CG_TRY(cudaPeekAtLastError());
   c1.download(coef1, nterm, st);
   c2.download(coef2, nterm, st);
   c4.download(coef4, nterm, st);
   CG_TRY(cudaStreamSynchronize(st));
-  cudaStreamDestroy(st);
   return 0;
 }
 
