@@ -57,7 +57,9 @@ typedef struct cathy_soil {
   int32_t nzone;
   const double *permx, *permy, *permz, *elstor, *poros, *vgn, *vgrmc, *vgpsat;
   double pmin, scf;
-  int32_t kslope;              /* 0 only                                   */
+  int32_t kslope;              /* 0 analytical slopes; 1 chord slopes
+                                  between PTOLD and PTNEW once they differ
+                                  by TOLKSL (chpic1.f, chnew1.f)           */
   double tolksl;
 } cathy_soil_t;
 

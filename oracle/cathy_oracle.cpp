@@ -1242,17 +1242,31 @@ void Oracle::picard() {
 // NEWTON (newton.f) with NEWUNS/CHNEW0, ASSNEW, RHSNEW, CFMATN, RHSGRV, BCNEW,
 // NSYSLV, SHLNEW.  KSLOPE=0 only.
 void Oracle::newton() {
-  // NEWUNS -> CHNEW0 (chnew0.f IVGHU=0) + NODELT
+  // NEWUNS -> CHNEW0 (chnew0.f IVGHU=0) or, for KSLOPE=1, CHNEW1
+  // (chnew1.f:27-53: chord slopes between PTOLD and PTNEW once they differ by
+  // TOLKSL or more) + NODELT
   for (int i = 1; i <= n; ++i) {
     double psi = ptnew[i];
     double se = fvgse(psi, i);
-    double dsedp = fvgdse(psi, i);
-    double dswdp = vgpnot[i] * dsedp;
     sw[i] = vgpnot[i] * se + vgrmc[i] / pnodi[i];
-    etai[i] = sw[i] * snodi[i] + pnodi[i] * dswdp;
-    detai[i] = dswdp * snodi[i] + pnodi[i] * vgpnot[i] * fvgdds(psi, i);
     ckrw[i] = fvgkr(psi, se, i);
-    dckrw[i] = fvgdkr(psi, i);
+    const double dp = psi - ptold[i];
+    if (kslope == 0 || std::fabs(dp) < tolksl) {
+      double dsedp = fvgdse(psi, i);
+      double dswdp = vgpnot[i] * dsedp;
+      etai[i] = sw[i] * snodi[i] + pnodi[i] * dswdp;
+      detai[i] = dswdp * snodi[i] + pnodi[i] * vgpnot[i] * fvgdds(psi, i);
+      dckrw[i] = fvgdkr(psi, i);
+    } else {
+      const double pold = ptold[i];
+      const double seold = fvgse(pold, i);
+      const double dsenew = fvgdse(psi, i), dseold = fvgdse(pold, i);
+      const double dswdp = vgpnot[i] * ((se - seold) / dp);
+      const double krold = fvgkr(pold, seold, i);
+      etai[i] = sw[i] * snodi[i] + pnodi[i] * dswdp;
+      detai[i] = dswdp * snodi[i] + pnodi[i] * vgpnot[i] * ((dsenew - dseold) / dp);
+      dckrw[i] = (ckrw[i] - krold) / dp;
+    }
   }
   nodelt(ckrw, ckrwe);
   nodelt(etai, etae);

@@ -460,9 +460,18 @@ __global__ void k_vg(const int32_t* bm_mem, const int32_t* bm_r0,
       se_c = (CT)se_t;
     }
     nd.et1[i] = sw * ss;
-    CT dse = vg_dse<CT>((CT)pt, (CT)psat, (CT)n, (CT)nd.vgn1[i], (CT)nd.vgpsn[i],
-                        (CT)nd.vgnr[i]);
-    nd.et2[i] = (double)((CT)pnot * dse);
+    const MemberScal& S = ms[m];
+    const double dpo = pt - nd.ptold[i];
+    if (S.kslope == 1 && fabs(dpo) >= S.tolksl) {
+      // CHPIC1 (chpic1.f:25-48): chord slope of Se between PTOLD and PTNEW
+      const double se_t = vg_se<double>(pt, psat, n, mm);
+      const double se_o = vg_se<double>(nd.ptold[i], psat, n, mm);
+      nd.et2[i] = pnot * ((se_t - se_o) / dpo);
+    } else {
+      CT dse = vg_dse<CT>((CT)pt, (CT)psat, (CT)n, (CT)nd.vgn1[i], (CT)nd.vgpsn[i],
+                          (CT)nd.vgnr[i]);
+      nd.et2[i] = (double)((CT)pnot * dse);
+    }
     if constexpr (sizeof(CT) == 8) {
       nd.ckrw[i] = vg_kr<double>(pt, se_c, nd.vgmr[i], mm);
     } else {
@@ -482,14 +491,29 @@ __global__ void k_vg(const int32_t* bm_mem, const int32_t* bm_r0,
     nd.sw[i] = sw;
   } else {
     const double se = vg_se<double>(pt, psat, n, mm);
-    const double dsedp = vg_dse<double>(pt, psat, n, nd.vgn1[i], nd.vgpsn[i], nd.vgnr[i]);
-    const double dswdp = pnot * dsedp;
     const double sw = pnot * se + rmc / por;
+    const double kr = vg_kr<double>(pt, se, nd.vgmr[i], mm);
     nd.sw[i] = sw;
-    nd.etai[i] = sw * ss + por * dswdp;
-    nd.detai[i] = dswdp * ss + por * pnot * vg_dds(pt, psat, n, mm, nd.vgn1[i]);
-    nd.ckrw[i] = vg_kr<double>(pt, se, nd.vgmr[i], mm);
-    nd.dckrw[i] = vg_dkr(pt, psat, n, mm, nd.vgn1[i], nd.vgm52[i], nd.vgmm1[i]);
+    nd.ckrw[i] = kr;
+    const MemberScal& S = ms[m];
+    const double po = nd.ptold[i], dp = pt - po;
+    if (S.kslope == 1 && fabs(dp) >= S.tolksl) {
+      // CHNEW1 (chnew1.f:27-53): chord slopes between PTOLD and PTNEW
+      const double seo = vg_se<double>(po, psat, n, mm);
+      const double dsen = vg_dse<double>(pt, psat, n, nd.vgn1[i], nd.vgpsn[i], nd.vgnr[i]);
+      const double dseo = vg_dse<double>(po, psat, n, nd.vgn1[i], nd.vgpsn[i], nd.vgnr[i]);
+      const double dswdp = pnot * ((se - seo) / dp);
+      const double kro = vg_kr<double>(po, seo, nd.vgmr[i], mm);
+      nd.etai[i] = sw * ss + por * dswdp;
+      nd.detai[i] = dswdp * ss + por * pnot * ((dsen - dseo) / dp);
+      nd.dckrw[i] = (kr - kro) / dp;
+    } else {
+      const double dsedp = vg_dse<double>(pt, psat, n, nd.vgn1[i], nd.vgpsn[i], nd.vgnr[i]);
+      const double dswdp = pnot * dsedp;
+      nd.etai[i] = sw * ss + por * dswdp;
+      nd.detai[i] = dswdp * ss + por * pnot * vg_dds(pt, psat, n, mm, nd.vgn1[i]);
+      nd.dckrw[i] = vg_dkr(pt, psat, n, mm, nd.vgn1[i], nd.vgm52[i], nd.vgmm1[i]);
+    }
   }
 }
 
@@ -1965,8 +1989,11 @@ __device__ __forceinline__ float vgf_dse(double psi1, double psi0, float psat,
   return se0 * expm1f(-m * log1pf(db / (1.0f + b0)));
 }
 
-// FP32 soil characteristics of node i (see the FP32 block comment).
-__device__ __forceinline__ void vg_f32_node(int i, const Nodal& nd, NodalF& nf, const double* z) {
+// FP32 soil characteristics of node i (see the FP32 block comment); with
+// KSLOPE=1 the storage coefficient is the chord slope of Se between PTOLD
+// and PTNEW once they differ by TOLKSL or more (CHPIC1, chpic1.f:25-48).
+__device__ __forceinline__ void vg_f32_node(int i, const Nodal& nd, NodalF& nf, const double* z,
+                                            const MemberScal& S) {
   const float psat = nf.vgpsat[i], n = nf.vgn[i], mm = nf.vgm[i], pnot = nf.vgpnot[i];
   const float rmcp = nf.rmcp[i];
   const double p = nd.pnew[i], pt = nd.ptnew[i], pn = nd.ptimep[i];
@@ -1981,6 +2008,10 @@ __device__ __forceinline__ void vg_f32_node(int i, const Nodal& nd, NodalF& nf, 
     const float b1 = beta + 1.0f, b1r = 1.0f / b1;
     dse = nf.vgn1[i] * (__powf(fabsf(ptf), nf.vgn1[i]) / nf.vgpsn[i]) *
           __powf(fabsf(b1), nf.vgnr[i]) * b1r * b1r;
+  }
+  if (S.kslope == 1) {
+    const double dpo = pt - nd.ptold[i];
+    if (fabs(dpo) >= S.tolksl) dse = vgf_dse(pt, nd.ptold[i], psat, n, mm) / (float)dpo;
   }
   const float sw = pnot * se + rmcp;
   nf.ckrw[i] = kr;
@@ -1999,13 +2030,13 @@ __device__ __forceinline__ void vg_f32_node(int i, const Nodal& nd, NodalF& nf, 
 }
 
 __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
-                         const int32_t* bm_r1, const uint8_t* act, Nodal nd,
-                         NodalF nf, const double* z) {
+                         const int32_t* bm_r1, const uint8_t* act, const MemberScal* ms,
+                         Nodal nd, NodalF nf, const double* z) {
   const int m = bm_mem[blockIdx.x];
   if (!(act[m] & ACT_ITER)) return;
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
   if (i >= bm_r1[blockIdx.x]) return;
-  vg_f32_node(i, nd, nf, z);
+  vg_f32_node(i, nd, nf, z, ms[m]);
 }
 
 // Step actions of every node (phase 0, the surface part for surface nodes,
@@ -2033,7 +2064,7 @@ __global__ void k_start_vg_f32(int nb1, const int32_t* bm_mem, const int32_t* bm
       start_surface_node(i, a, S, nd);
     start_phase1_node(i, a, S, nd, need_sw);
   }
-  if (a & ACT_ITER) vg_f32_node(i, nd, nf, z);
+  if (a & ACT_ITER) vg_f32_node(i, nd, nf, z, S);
 }
 
 
@@ -2675,6 +2706,8 @@ struct MemberHost {
   std::shared_ptr<HostMesh> meshp = std::make_shared<HostMesh>();
   cathy_parm_t parm;
   double pmin = -5, scf = 0, pondh_min = 1e10;
+  int kslope = 0;
+  double tolksl = 0.01;
   // atmospheric series (atmone.f/atmnxt.f/atmbak.f state)
   int hspatm = 1, ieto = 0, natm = 0, atm_next = 0, htiatm = 0;
   std::vector<double> atm_t, atm_v;
@@ -3121,7 +3154,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     if (mem[m].parm.iopt != iopt || mem[m].parm.lump != lump ||
         mem[m].parm.precond != precond)
       throw std::string("members must share IOPT, LUMP and the preconditioner");
-    if (mem[m].soil.kslope != 0) throw std::string("KSLOPE != 0 not supported");
+    if (mem[m].soil.kslope != 0 && mem[m].soil.kslope != 1)
+      throw std::string("KSLOPE 2..4 (chord slope with centred or local differences) not supported");
   }
   // meshes (topology cached per identical DEM activity/size)
   M.resize(nmem);
@@ -3272,6 +3306,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       }
     h.pmin = S.pmin;
     h.scf = S.scf;
+    h.kslope = S.kslope;
+    h.tolksl = S.tolksl;
     h.pondh_min = (h.parm.isimgr <= 1) ? 1.0e10 : h.parm.pondh_min;
     h.hspatm = B.hspatm; h.ieto = B.ieto; h.natm = B.natm;
     h.atm_t.assign(B.atmtim, B.atmtim + B.natm);
@@ -3677,7 +3713,8 @@ void Engine::push_scalars(bool to_pinned) {
     S.pmin = h.pmin; S.omega = h.parm.omega; S.tolswi = h.parm.tolswi;
     S.atm_ta = h.atm_ta; S.atm_tb = h.atm_tb; S.atm_va = h.atm_va; S.atm_vb = h.atm_vb;
     S.atm_mode = h.atm_mode; S.hspatm = h.hspatm; S.ieto = h.ieto; S.nlrelx = h.parm.nlrelx;
-    S.nnod = h.meshp->nnod; S.nstr = h.meshp->nstr; S.iopt = iopt; S.pad = 0;
+    S.nnod = h.meshp->nnod; S.nstr = h.meshp->nstr; S.iopt = iopt;
+    S.kslope = h.kslope; S.tolksl = h.tolksl;
     if (h.atm_nodal_dirty) nodal_dirty = true;
   }
   if (to_pinned) std::memcpy(hp_ms, h_ms.data(), sizeof(MemberScal) * nmem);
@@ -4877,8 +4914,8 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   e->d_act.upload(act.data(), e->nmem, e->st);
   const bool mixed = (e->precision == 1 && e->iopt == 1);
   if (mixed) {
-    k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->nd, e->nf,
-                                                  e->d_nodal[ND_Z].p);
+    k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p,
+                                                  e->d_ms.p, e->nd, e->nf, e->d_nodal[ND_Z].p);
     k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
         e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_islot.p,
         e->d_rec48.p, e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold,

@@ -39,7 +39,8 @@ struct MemberScal {
   double atm_va, atm_vb;   // homogeneous rates (hspatm != 0)
   int32_t atm_mode;        // 0 keep, 1 interpolate, 2 constant vb
   int32_t hspatm, ieto, nlrelx;
-  int32_t nnod, nstr, iopt, pad;
+  int32_t nnod, nstr, iopt, kslope;  // KSLOPE 0 (analytical) or 1 (chord slope)
+  double tolksl;                      // chord slope once |PTNEW - PTOLD| >= TOLKSL
 };
 
 // per-member reduction accumulators (zeroed before use)

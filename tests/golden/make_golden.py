@@ -1,8 +1,8 @@
 """Generate the golden fixtures from the reference's stored CATHY runs.
 
-Run in a container where the reference checkout is mounted:
+Run where the reference checkout is available, giving its path:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the reference checkout>
 
 For each example project it stores (a) the project inputs as parsed by
 ``pycathy_wrapper_gb300.project.read_project`` and (b) the values the
@@ -87,4 +87,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path to the reference checkout>")
+    main(sys.argv[1])
