@@ -33,9 +33,11 @@ the whole ensemble day from the initial condition.
 host cores (the Fortran reference cannot be built: no Fortran compiler) on a
 bounded sample of the same ensemble and prints the same metric.
 
-Multi-GPU (torchrun): each rank runs its own 256-member shard (seeds offset
-by 256 per rank), no collective on the data path; value = all members'
-simulated seconds / max rank time (weak scaling).
+Multi-GPU (torchrun): the ensemble holds 256 members per rank (seeds 1000..)
+and is split into one shard per rank, greedy by mesh size
+(pycathy_wrapper_gb300.shard); each rank runs its shard as one batched
+solve, no collective on the data path; value = all members' simulated
+seconds / max rank time (weak scaling).
 """
 from __future__ import annotations
 
@@ -56,9 +58,15 @@ METRIC = "simulated s per wall s at 1e-6 m head tol: learned+batched vs plain GP
 UNIT = "sim-s/wall-s"
 
 
-def _cases(nmem, rank, tmax, precond):
+def _cases(nmem, rank, tmax, precond, world=1):
+    """This rank's members: the ensemble holds nmem * world members (seeds
+    1000..), split across the ranks greedy by mesh size (one shard per GPU,
+    no collective on the data path)."""
     from pycathy_wrapper_gb300.inputs import config2_members
-    cases = config2_members(nmem, tmax=tmax, base_seed=1000 + 256 * rank)
+    cases = config2_members(nmem * world, tmax=tmax, base_seed=1000)
+    if world > 1:
+        from pycathy_wrapper_gb300.shard import member_nodes, shard_of
+        cases = [cases[m] for m in shard_of(member_nodes(cases), rank, world)]
     for c in cases:
         c.parm.precond = precond
     return cases
@@ -263,7 +271,7 @@ def main():
                          f"one process per core, {wall:.1f} s wall"}
     import numpy as np
     from pycathy_wrapper_gb300.api import Simulation
-    cases = _cases(args.members, rank, args.tmax, precond=2)
+    cases = _cases(args.members, rank, args.tmax, precond=2, world=ws)
     sim = Simulation(cases, precision=1, device=int(os.environ.get("LOCAL_RANK", "0")),
                      graphs=not args.no_graphs)
     nodes_total = int(sum(s["n"] for s in sim.sizes))

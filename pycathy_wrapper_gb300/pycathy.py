@@ -278,7 +278,7 @@ class _Stepper:
 
 
 def run_ensemble(member_dirs: Sequence[str], precision: int = 1, device: int = 0,
-                 write: bool = True) -> List[dict]:
+                 write: bool = True, rank: int = 0, world: int = 1) -> List[dict]:
     """Run every member folder of a DA ensemble as ONE batched GPU solve
     (the replacement of the process pool over ``./cathy``).  Members may
     differ in mesh, soil, forcing and initial state; they must share IOPT,
@@ -288,7 +288,16 @@ def run_ensemble(member_dirs: Sequence[str], precision: int = 1, device: int = 0
     they run straight to the end.  (The FP32 dot products of the batched
     SpMV are grouped over the members that are active at the time, so the
     two schedules agree to the FP32 rounding of those sums, not bit for
-    bit.)"""
+    bit.)
+
+    With ``world`` > 1 the call runs only rank ``rank``'s shard of the
+    members (one process per GPU; shards balanced by mesh size, see
+    :mod:`pycathy_wrapper_gb300.shard`) and returns that shard's results."""
+    if world > 1:
+        from .shard import member_nodes, shard_of
+        allc = [read_project(d) for d in member_dirs]
+        mine = shard_of(member_nodes(allc), rank, world)
+        member_dirs = [member_dirs[m] for m in mine]
     cases = [read_project(d) for d in member_dirs]
     for c in cases:
         if c.parm.iopt == 1 and c.parm.precond == 0 and precision == 1:
