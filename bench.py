@@ -23,11 +23,14 @@ the whole ensemble day from the initial condition.
             graph's conditional body), against the measured HBM copy
             bandwidth.
   cpu_baseline  the CPU oracle (serial C++ restatement of the reference
-            Fortran) on a bounded sample: the first 16 members for their first
-            2 simulated hours, one process per host core (about a minute on 16
-            Arm cores; the day's throughput varies strongly with simulated
-            time, and the first half hour or hour alone overstates the CPU's
-            whole-day throughput several-fold).
+            Fortran) on a bounded sample: members 1000..1014 and 1036 for
+            their first 30 simulated minutes, one process per host core;
+            also with pyCATHY's default pool of cpu_count() - 5 workers.
+  same_sample_gpu_vs_cpu  the GPU path on exactly that sample (same
+            members, same window, device-timed) beside the CPU figure: the
+            like-for-like ratio.  The day's throughput varies with simulated
+            time (the first minutes run at the smallest time steps), so the
+            whole-day value and the sample are different workloads.
 
 --impl reference runs the CPU restatement of the reference's solver on the
 host cores (the Fortran reference cannot be built: no Fortran compiler) on a
@@ -73,14 +76,26 @@ def _cases(nmem, rank, tmax, precond, world=1):
 
 
 # ---------------------------------------------------------------------------
-# CPU oracle sample (spawned worker processes)
+# Bounded sample for the CPU baseline, the reference arm and the GPU run on
+# the same sample: the first 15 members and member 36 (seed 1036, which fails
+# later in the day: a hard member), each for its first SAMPLE_TMAX simulated
+# seconds.
 # ---------------------------------------------------------------------------
+SAMPLE = list(range(15)) + [36]
+SAMPLE_TMAX = 1800.0
+
+
+def _sample_cases(nmem, tmax, precond):
+    allc = _cases(nmem, 0, tmax, precond=precond)
+    return [allc[i] for i in SAMPLE if i < len(allc)]
+
+
 def _oracle_member(args):
-    seed_index, nmem, rank, tmax = args
+    k, nmem, tmax = args
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    c = _cases(nmem, rank, tmax, precond=0)[seed_index]
+    c = _sample_cases(nmem, tmax, precond=0)[k]
     o = O.Oracle(c)
     t0 = time.perf_counter()
     o.run()
@@ -89,18 +104,36 @@ def _oracle_member(args):
     return (sr[-1]["time"] if sr else 0.0), el
 
 
-def cpu_sample(nmem, rank, tmax, nsample, cores):
+def cpu_sample(nmem, tmax, cores):
+    """The CPU restatement of the reference solver on the sample, one member
+    per worker process (pyCATHY's DA runs one ./cathy per member in a
+    process pool); returns simulated s per wall s, wall s, simulated s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     ctx = mp.get_context("spawn")
-    jobs = [(i, nmem, rank, tmax) for i in range(nsample)]
+    n = len(_sample_cases(nmem, tmax, precond=0))
+    jobs = [(k, nmem, tmax) for k in range(n)]
     t0 = time.perf_counter()
-    with ctx.Pool(processes=cores) as pool:
+    with ctx.Pool(processes=max(1, cores)) as pool:
         res = pool.map(_oracle_member, jobs)
     wall = time.perf_counter() - t0
     sim = sum(r[0] for r in res)
     return sim / wall, wall, sim
+
+
+def gpu_sample(nmem, tmax, device, graphs):
+    """The GPU path on the same sample (device-timed, one batched solve)."""
+    from pycathy_wrapper_gb300.api import Simulation
+    cases = _sample_cases(nmem, tmax, precond=2)
+    with Simulation(cases, precision=1, device=device, graphs=graphs) as s:
+        s.run(20)  # warm-up: the first steps of every member
+        s.reset()
+        a = s.stats()["gpu_ms"]
+        s.run()
+        dev = (s.stats()["gpu_ms"] - a) / 1000.0
+        sim = sum(s.state(m)[1] for m in range(s.nmembers))
+    return sim / dev, dev, sim
 
 
 # ---------------------------------------------------------------------------
@@ -208,13 +241,12 @@ def run_reference(args):
         barrier(ws)
         return
     cores = os.cpu_count() or 1
-    nsample = min(args.cpu_members, args.members)
     vals, walls = [], []
     # warm-up steps (process start-up, page cache) run a short sample; the
     # timed steps run the bounded sample itself
     for i in range(args.warmup + args.steps):
-        tmax = args.cpu_tmax if i >= args.warmup else min(args.cpu_tmax, 300.0)
-        v, wall, sim = cpu_sample(args.members, 0, tmax, nsample, cores)
+        tmax = args.cpu_tmax if i >= args.warmup else min(args.cpu_tmax, 120.0)
+        v, wall, sim = cpu_sample(args.members, tmax, cores)
         if i >= args.warmup:
             vals.append(v)
             walls.append(wall)
@@ -225,11 +257,11 @@ def run_reference(args):
         "ms_per_step": 1000.0 * sum(walls) / len(walls), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"ensemble{args.members}_day", "members": args.members,
-                   "tmax_s": args.tmax, "sample_members": nsample},
+                   "tmax_s": args.tmax, "sample_members": [1000 + i for i in SAMPLE]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{nsample} of {args.members} members, first "
+                         "sample": f"members {[1000 + i for i in SAMPLE]}, first "
                                    f"{args.cpu_tmax:g} simulated s each, one process per core "
-                                   f"(CPU restatement of the reference Fortran; gfortran "
+                                   f"(CPU restatement of the reference Fortran, -O2; gfortran "
                                    f"absent)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -249,8 +281,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--tmax", type=float, default=86400.0)
-    ap.add_argument("--cpu-members", type=int, default=16)
-    ap.add_argument("--cpu-tmax", type=float, default=7200.0,
+    ap.add_argument("--cpu-tmax", type=float, default=SAMPLE_TMAX,
                     help="simulated seconds per member in the bounded CPU sample")
     ap.add_argument("--plain-members", type=int, default=4)
     ap.add_argument("--no-graphs", action="store_true")
@@ -261,19 +292,30 @@ def main():
         return run_reference(args)
     rank, ws = dist_init()
     # CPU baseline first (spawned pool, before any GPU context)
-    cpu = None
+    cpu = cpu_pyc = None
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
-        ns = min(args.cpu_members, args.members)
-        v, wall, sim = cpu_sample(args.members, 0, args.cpu_tmax, ns, cores)
+        v, wall, sim = cpu_sample(args.members, args.cpu_tmax, cores)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{ns} of {args.members} members x first {args.cpu_tmax:g} simulated s, "
-                         f"one process per core, {wall:.1f} s wall"}
+               "sample": f"members {[1000 + i for i in SAMPLE]} x first {args.cpu_tmax:g} "
+                         f"simulated s, one process per core, {wall:.1f} s wall"}
+        # pyCATHY's default DA pool size (cathy_DA.py: cpu_count() - 5)
+        wk = max(1, cores - 5)
+        v2, wall2, _ = cpu_sample(args.members, args.cpu_tmax, wk)
+        cpu_pyc = {"value": v2, "unit": UNIT, "cores": wk,
+                   "sample": f"same sample, {wk} worker processes, {wall2:.1f} s wall"}
     import numpy as np
     from pycathy_wrapper_gb300.api import Simulation
+    dev_id = int(os.environ.get("LOCAL_RANK", "0"))
+    # the GPU path on the CPU baseline's sample (same members, same window)
+    like = None
+    if rank == 0 and cpu is not None:
+        vg, devs, _ = gpu_sample(args.members, args.cpu_tmax, dev_id, not args.no_graphs)
+        like = {"sample": cpu["sample"].split(", one process")[0], "gpu": vg, "cpu": cpu["value"],
+                "cpu_cores": cpu["cores"], "gpu_over_cpu": vg / cpu["value"], "unit": UNIT,
+                "gpu_s": devs}
     cases = _cases(args.members, rank, args.tmax, precond=2, world=ws)
-    sim = Simulation(cases, precision=1, device=int(os.environ.get("LOCAL_RANK", "0")),
-                     graphs=not args.no_graphs)
+    sim = Simulation(cases, precision=1, device=dev_id, graphs=not args.no_graphs)
     nodes_total = int(sum(s["n"] for s in sim.sizes))
     nnz_total = int(sum(s["nnz"] for s in sim.sizes))
     # warm-up: partial passes of the same workload (every member's first
@@ -282,6 +324,10 @@ def main():
     for _ in range(args.warmup):
         sim.reset()
         sim.run(args.warmup_member_steps)
+    # the assembly (the dominant kernel of the full-batch iterations) on the
+    # whole ensemble as it stands after the warm-up: mean of 20 launches
+    # between CUDA events, inputs far larger than L2 (no flush needed)
+    asm_ms, asm_bytes, asm_rows = sim.time_assembly(20)
 
     def reached():
         # simulated seconds actually covered (members that fail stop early)
@@ -393,7 +439,15 @@ def main():
                      "frac": (achieved / peak) if achieved else None,
                      "peak_source": peak_kind, "traffic": traffic,
                      "launches": spmv_n, "alg_bytes_per_launch": spmv_bytes / max(spmv_n, 1)},
+        "roofline_assembly": {
+            "bound": "hbm", "kernel": "k_assemble_picard_f32",
+            "timing": "20 launches over all 256 members after the warm-up, CUDA events",
+            "achieved": asm_bytes / 1e9 / (asm_ms / 1e3), "peak": peak, "unit": "GB/s",
+            "frac": asm_bytes / 1e9 / (asm_ms / 1e3) / peak, "peak_source": peak_kind,
+            "alg_bytes_per_launch": asm_bytes, "rows": asm_rows, "ms_per_launch": asm_ms},
         "cpu_baseline": cpu,
+        "cpu_baseline_pycathy_workers": cpu_pyc,
+        "same_sample_gpu_vs_cpu": like,
         "plain_gpu": plain,
         "speedup_vs_plain_gpu": (value / plain["value"]) if plain else None,
         "clocks": ck,

@@ -185,6 +185,27 @@ int32_t cathy_gb300_reset(void* handle);
  * (values+columns+row pointers+vectors). */
 int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
                             int64_t* spmv_launches, double* spmv_bytes);
+/* Phase timers of the nonlinear iterations in the nine buckets of the
+ * reference's CPU summary (risul, cathy_main.f:3913-3950; accumulated in
+ * picard.f:66-202): unsat characteristics, init of system matrices, local
+ * assembly, RHS, global LHS, BC contributions, linear solver & residual,
+ * Dirichlet resetting & DIFMAX, fluxes/mass balance/switching.  enable 1
+ * starts them (zeroed) -- macro-iterations then run kernel by kernel with
+ * CUDA events between the phases and NVTX ranges named after the buckets;
+ * 0 stops them; -1 only reads.  out[0..n), n <= 9: GPU ms per bucket
+ * (buckets whose work is fused into another kernel stay 0: the FP32 path
+ * assembles matrix, RHS and BC terms in one kernel, bucket 3). */
+int32_t cathy_gb300_phase_timers(void* handle, int32_t enable, double* out, int32_t n);
+/* Times the FP32 Picard assembly (ASSPIC + RHSPIC + CFMATP + RHSGRV + BCPIC
+ * fused, asspic.f:26-51) on the handle's current state: nrep launches over
+ * the members that iterated in the last macro-iteration, between CUDA
+ * events; the launches recompute the same system from unchanged inputs.
+ * Outputs: mean ms per launch, the launch's algorithmic bytes (per row 74 B,
+ * per surface row 16 B, per incidence 21 B (+4 B with a consistent mass
+ * matrix), per matrix slot 9 B) and the rows assembled.  FP32 Picard path
+ * only (CATHY_GB300_EUNSUP otherwise). */
+int32_t cathy_gb300_time_assembly(void* handle, int32_t nrep, double* ms, double* bytes,
+                                  int64_t* rows);
 /* GPU time spent in the hot path (ms) since creation, and kernel launches */
 int32_t cathy_gb300_stats(void* handle, double* gpu_ms, int64_t* launches,
                           int64_t* lin_iters, int64_t* nl_iters);

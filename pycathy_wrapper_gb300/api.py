@@ -231,6 +231,27 @@ class Simulation:
                              if out[8 + 2 * b] > 0}
         return d
 
+    PHASES = ("UNSAT CHARACTERISTICS", "INIT. OF SYSTEM MATRICES", "LOCAL SYSTEM ASSEMBLY",
+              "RHS CALCULATION W/O BC'S", "GLOBAL LHS SYSTEM MATRIX", "BC CONTRIBUTIONS TO RHS",
+              "LINEAR SOLVER & RESIDUAL", "DIR. RESETTING AND DIFMAX",
+              "B-FLX, M-BAL, SW, & EX-PT")
+
+    def phase_timers(self, enable: int = -1):
+        """GPU ms per phase bucket of the reference's risul summary (enable 1
+        starts timing, 0 stops it, -1 reads); a dict name -> ms."""
+        out = (C.c_double * 9)()
+        check(self.L.cathy_gb300_phase_timers(self.h, int(enable), out, 9), "phase_timers")
+        return {k: out[i] for i, k in enumerate(self.PHASES)}
+
+    def time_assembly(self, nrep: int = 10):
+        """Mean device time (ms) of the FP32 assembly over the members that
+        iterated last, its algorithmic bytes and rows (see the C header)."""
+        ms, b = C.c_double(), C.c_double()
+        r = C.c_int64()
+        check(self.L.cathy_gb300_time_assembly(self.h, int(nrep), C.byref(ms), C.byref(b),
+                                               C.byref(r)), "time_assembly")
+        return ms.value, b.value, r.value
+
     def stats(self):
         ms = C.c_double()
         la, li, nl = C.c_int64(), C.c_int64(), C.c_int64()

@@ -140,6 +140,17 @@ int32_t cathy_gb300_profile(void* h, int32_t enable, double* spmv_ms,
   return engine_profile((Engine*)h, enable, spmv_ms, spmv_launches, spmv_bytes);
 }
 
+int32_t cathy_gb300_phase_timers(void* h, int32_t enable, double* out, int32_t n) {
+  if (!h || (n > 0 && !out) || n < 0) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_phase_timers((Engine*)h, enable, out, n); });
+}
+
+int32_t cathy_gb300_time_assembly(void* h, int32_t nrep, double* ms, double* bytes,
+                                  int64_t* rows) {
+  if (!h || !ms || !bytes || !rows) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_time_assembly((Engine*)h, nrep, ms, bytes, rows); });
+}
+
 int32_t cathy_gb300_stats(void* h, double* gpu_ms, int64_t* launches,
                           int64_t* lin_iters, int64_t* nl_iters) {
   if (!h) return CATHY_GB300_EINVAL;

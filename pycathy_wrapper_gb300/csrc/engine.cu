@@ -21,6 +21,7 @@
 // nonlinear convergence decision (flow3d.f:212-294) run per member on the
 // host from a few scalars copied back each nonlinear iteration.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -194,6 +195,10 @@ struct Nodal {  // per node
   double *pnew, *pold, *ptnew, *ptold, *ptimep, *pdiff, *swnew, *swtimep;
   double *rhs, *xt5, *qneu, *presc, *qpnew, *qpold;
   double *sw, *et1, *et2, *ckrw, *etai, *dckrw, *detai;
+  // FP32 path, FP64 mass balance: head at the mass balance of the last
+  // iteration (before relaxation and switching), and van Genuchten beta and
+  // Se carried at PTIMEP from step to step
+  double *pmb, *bet, *set;
   uint8_t *sdir;             // static (non-atmospheric) Dirichlet node
   uint8_t *dmask;            // current Dirichlet mask (static | atm 1,2)
   // surface nodes (valid for loc < nnod)
@@ -899,32 +904,18 @@ __device__ void build_kact(const int32_t* amem_cum, int nmem, const uint8_t* act
 // and 0 at those (the masked residual, w = b), no dots.
 enum { kSpmvPlain = 0, kSpmvUpd = 1, kSpmvResid = 2 };
 constexpr int kStreamWarps = 8;
+// FP32 y = A x as a stream over the map entries that virtual block vbid of
+// vgrid takes (see k_spmv_stream).  s_bytes: a zeroed shared slot for the
+// byte count (used only with alg_bytes).  Arrays written by other phases of
+// the fused Picard iteration carry no __restrict__.
 template <int kMode>
-__global__ void __launch_bounds__(32 * kStreamWarps, 8)
-k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-              const uint8_t* active, const int32_t* __restrict__ rowptr,
-              const int32_t* __restrict__ cols, const float* __restrict__ vals,
-              const uint8_t* __restrict__ dmask, const float* __restrict__ x, float* y,
-              const float* __restrict__ w, float* pv, const double* sc, double* acc,
-              int acc_stride, double* alg_bytes, unsigned long long* lt, int lt_cap,
-              const int32_t* kact, const int32_t* kfirst) {
-  pdl_enter();
-  __shared__ int s_slot;
-  __shared__ double s_bytes;
+__device__ __forceinline__ void spmv_stream_run(
+    int vbid, int vgrid, int nblk, const int32_t* bm_mem, const int32_t* bm_r0,
+    const int32_t* bm_r1, const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
+    const float* vals, const uint8_t* dmask, const float* x, float* y, const float* w, float* pv,
+    const double* sc, double* acc, int acc_stride, double* alg_bytes, double* s_bytes,
+    const int32_t* kact, const int32_t* kfirst) {
   __shared__ float sprod[kStreamWarps][16 * kGroup + 8];
-  if (alg_bytes) {
-    if (threadIdx.x == 0) s_bytes = 0.0;
-    __syncthreads();
-  }
-  if (lt) {
-    if (threadIdx.x == 0) {
-      const unsigned long long q = lt[LT_SEQ];
-      s_slot = q < (unsigned long long)lt_cap ? (int)q : -1;
-      if (s_slot >= 0) atomicMin(&lt[LT_HDR + 2 * s_slot], (unsigned long long)gtimer());
-    }
-    __syncthreads();
-    if (s_slot < 0) lt = nullptr;
-  }
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   float* sp = sprod[wp];
   float d0 = 0.0f, d1 = 0.0f;
@@ -939,8 +930,8 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
     total = kcum[nseg];
   }
   // (the list is built before every product of the loop: nseg <= members)
-  const int chunk = (total + gridDim.x - 1) / gridDim.x;
-  const int b0 = blockIdx.x * chunk, b1 = min(total, b0 + chunk);
+  const int chunk = (total + vgrid - 1) / vgrid;
+  const int b0 = vbid * chunk, b1 = min(total, b0 + chunk);
   // the warp's current segment: its end and entry offset live in registers
   int seg = 0, seg_end = 0, delta = 0;
   if (kMode == kSpmvUpd && b0 + wp < b1) {
@@ -1065,10 +1056,40 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
   }
   if (alg_bytes) {
     // one global atomic per block
-    if (lane == 0 && bytes != 0.0) atomicAdd(&s_bytes, bytes);
+    if (lane == 0 && bytes != 0.0) atomicAdd(s_bytes, bytes);
     __syncthreads();
-    if (threadIdx.x == 0 && s_bytes != 0.0) atomicAdd(alg_bytes, s_bytes);
+    if (threadIdx.x == 0 && *s_bytes != 0.0) atomicAdd(alg_bytes, *s_bytes);
   }
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(32 * kStreamWarps, 8)
+k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+              const uint8_t* active, const int32_t* __restrict__ rowptr,
+              const int32_t* __restrict__ cols, const float* __restrict__ vals,
+              const uint8_t* __restrict__ dmask, const float* __restrict__ x, float* y,
+              const float* __restrict__ w, float* pv, const double* sc, double* acc,
+              int acc_stride, double* alg_bytes, unsigned long long* lt, int lt_cap,
+              const int32_t* kact, const int32_t* kfirst) {
+  pdl_enter();
+  __shared__ int s_slot;
+  __shared__ double s_bytes;
+  if (alg_bytes) {
+    if (threadIdx.x == 0) s_bytes = 0.0;
+    __syncthreads();
+  }
+  if (lt) {
+    if (threadIdx.x == 0) {
+      const unsigned long long q = lt[LT_SEQ];
+      s_slot = q < (unsigned long long)lt_cap ? (int)q : -1;
+      if (s_slot >= 0) atomicMin(&lt[LT_HDR + 2 * s_slot], (unsigned long long)gtimer());
+    }
+    __syncthreads();
+    if (s_slot < 0) lt = nullptr;
+  }
+  spmv_stream_run<kMode>(blockIdx.x, gridDim.x, nblk, bm_mem, bm_r0, bm_r1, active, rowptr, cols,
+                         vals, dmask, x, y, w, pv, sc, acc, acc_stride, alg_bytes, &s_bytes, kact,
+                         kfirst);
   if (lt) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1250,13 +1271,13 @@ __global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
 
 // z = T^-1 r per column; accumulates w.z (w = q for the PCG beta) per
 // member.  The forward sweep keeps y in z, the backward sweep overwrites it.
+// (No __restrict__ here: in the fused Picard iteration other phases of the
+// same launch write these arrays.)
 template <class VT>
 __device__ __forceinline__ void k_line_apply_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* active,
-                             const MemberScal* ms, const VT* __restrict__ pinv,
-                             const VT* __restrict__ cdown, const VT* __restrict__ r,
-                             VT* __restrict__ z, const VT* __restrict__ w,
-                             double* acc, int acc_stride, int acc_off) {
+                             const MemberScal* ms, const VT* pinv, const VT* cdown, const VT* r,
+                             VT* z, const VT* w, double* acc, int acc_stride, int acc_off) {
   const int m = bm_mem[bid_];
   if (!active[m]) return;
   const int top = bm_r0[bid_] + threadIdx.x;
@@ -1989,6 +2010,103 @@ __device__ __forceinline__ float vgf_dse(double psi1, double psi0, float psat,
   return se0 * expm1f(-m * log1pf(db / (1.0f + b0)));
 }
 
+// ---- FP64 mass balance of the FP32 path ----------------------------------
+// DSTORE needs Sw at the start of the accepted iteration and at PTIMEP in
+// FP64 (the reference sums V [Ss (Sw + Sw_t)/2 (P - P_t) + phi (Sw - Sw_t)]
+// in double precision, masbal.f:36-109).  A double-precision pow costs
+// about 40 times the FP32 one on this GPU, so Se and beta = |psi/psat|^n are
+// carried in FP64 at PTIMEP from step to step and moved to a nearby head by
+// increments: with r = psi/psi_t - 1,
+//   beta - beta_t = beta_t expm1(n log1p(r)),
+//   Se / Se_t - 1 = expm1(-m log1p((beta - beta_t)/(1 + beta_t))).
+// For arguments t with |t| <= 1/16 log1p(t) = t + t^2 P(t) and expm1(t) =
+// t + t^2 Q(t) (Taylor series to t^9); the tails t^2 P, t^2 Q are at most
+// |t|/30 of the result and are evaluated in FP32, the leading term and the
+// sums in FP64, so each increment is accurate to about 1e-9 relative (1e-11
+// for |t| <= 1e-3).  Quotients use one FP32 division refined by an FP64
+// residual.  Larger moves and moves across saturation use FP64 pow.
+__device__ __forceinline__ double log1p_near0(double t) {
+  const float f = (float)t;
+  float c = 1.0f / 9.0f;
+  c = fmaf(c, f, -1.0f / 8.0f);
+  c = fmaf(c, f, 1.0f / 7.0f);
+  c = fmaf(c, f, -1.0f / 6.0f);
+  c = fmaf(c, f, 1.0f / 5.0f);
+  c = fmaf(c, f, -1.0f / 4.0f);
+  c = fmaf(c, f, 1.0f / 3.0f);
+  c = fmaf(c, f, -1.0f / 2.0f);
+  return t + (double)(f * f * c);
+}
+__device__ __forceinline__ double expm1_near0(double t) {
+  const float f = (float)t;
+  float c = 1.0f / 362880.0f;
+  c = fmaf(c, f, 1.0f / 40320.0f);
+  c = fmaf(c, f, 1.0f / 5040.0f);
+  c = fmaf(c, f, 1.0f / 720.0f);
+  c = fmaf(c, f, 1.0f / 120.0f);
+  c = fmaf(c, f, 1.0f / 24.0f);
+  c = fmaf(c, f, 1.0f / 6.0f);
+  c = fmaf(c, f, 1.0f / 2.0f);
+  return t + (double)(f * f * c);
+}
+// a / b to about 1e-14 relative (|a/b| well inside the FP32 range)
+__device__ __forceinline__ double div_refined(double a, double b) {
+  const float q = (float)a / (float)b;
+  const double e = fma(-(double)q, b, a);
+  return (double)q + (double)((float)e / (float)b);
+}
+// Se and beta at head psi from their values se_t, b_t at psi_t (FP64).
+__device__ __forceinline__ void vg_move64(double psi, double psi_t, double b_t, double se_t,
+                                          double psat, double n, double m, double& se,
+                                          double& b) {
+  const bool u = psi < -1.0e-14, ut = psi_t < -1.0e-14;
+  if (!u) { se = 1.0; b = 0.0; return; }
+  if (ut && psi != psi_t) {
+    const double r = div_refined(psi - psi_t, psi_t);
+    if (fabs(r) <= 1.0 / 64.0) {
+      const double x = n * log1p_near0(r);
+      if (fabs(x) <= 1.0 / 16.0) {
+        const double db = b_t * expm1_near0(x);
+        const double y = div_refined(db, 1.0 + b_t);
+        if (fabs(y) <= 1.0 / 16.0) {
+          const double z = -m * log1p_near0(y);
+          if (fabs(z) <= 1.0 / 16.0) {
+            se = se_t + se_t * expm1_near0(z);
+            b = b_t + db;
+            return;
+          }
+        }
+      }
+    }
+  } else if (ut) {
+    se = se_t; b = b_t;
+    return;
+  }
+  b = pow(fabs(psi / psat), n);
+  se = pow(fabs(1.0 / (b + 1.0)), m);
+}
+// Node i's share of the accepted step's FP64 storage change and of the new
+// storage, then beta/Se moved to the accepted head (the next PTIMEP).
+// POLD is the head at the start of the accepted iteration (where CHPIC took
+// SWNEW), PMB the head at its mass balance, PNEW the accepted head.
+__device__ __forceinline__ void commit_mass_node(int i, const Nodal& nd, double& dstore,
+                                                 double& store) {
+  const double psat = nd.vgpsat[i], n = nd.vgn[i], m = nd.vgm[i];
+  const double pt = nd.ptimep[i], bt = nd.bet[i], st = nd.set[i];
+  double so, bo, sn, bn;
+  vg_move64(nd.pold[i], pt, bt, st, psat, n, m, so, bo);
+  const double pn = nd.pnew[i];
+  if (pn == nd.pold[i]) { sn = so; bn = bo; }
+  else vg_move64(pn, pt, bt, st, psat, n, m, sn, bn);
+  const double pnot = nd.vgpnot[i], por = nd.pnodi[i], rmp = nd.vgrmc[i] / por;
+  const double swo = pnot * so + rmp, swt = pnot * st + rmp;
+  const double v = nd.volnod[i];
+  dstore = v * (nd.snodi[i] * (swo + swt) * 0.5 * (nd.pmb[i] - pt) + por * (pnot * (so - st)));
+  store = (pnot * sn + rmp) * v * por;
+  nd.bet[i] = bn;
+  nd.set[i] = sn;
+}
+
 // FP32 soil characteristics of node i (see the FP32 block comment); with
 // KSLOPE=1 the storage coefficient is the chord slope of Se between PTOLD
 // and PTNEW once they differ by TOLKSL or more (CHPIC1, chpic1.f:25-48).
@@ -2043,20 +2161,25 @@ __global__ void k_vg_f32(const int32_t* bm_mem, const int32_t* bm_r0,
 // phase 1) and the FP32 soil characteristics of iterating members, in one
 // pass: each of these reads and writes only its own node.  The blocks after
 // the node blocks set the Krylov flags of the members.
-__global__ void k_start_vg_f32(int nb1, const int32_t* bm_mem, const int32_t* bm_r0,
-                               const int32_t* bm_r1, const uint8_t* act,
-                               const MemberScal* ms, Nodal nd, NodalF nf, const double* z,
-                               int need_sw, int nmem, uint8_t* active) {
-  pdl_enter();
-  if ((int)blockIdx.x >= nb1) {
-    // Krylov member flags (the blocks after the node blocks)
-    k_flags_b(blockIdx.x - nb1, nmem, act, ACT_ITER, active);
-    return;
-  }
-  const int m = bm_mem[blockIdx.x];
+// ACT_COMMIT first forms the committed step's FP64 storage change and
+// storage (commit_mass_node, one FP64 atomic per block and quantity into
+// red[RD_DSTORE_C], red[RD_STORE1_C]) before PTIMEP moves to the accepted
+// heads.
+__device__ __forceinline__ void start_vg_entry(int bid, const int32_t* bm_mem,
+                                               const int32_t* bm_r0, const int32_t* bm_r1,
+                                               const uint8_t* act, const MemberScal* ms,
+                                               Nodal& nd, NodalF& nf, const double* z,
+                                               int need_sw, double* red) {
+  const int m = bm_mem[bid];
   const uint8_t a = act[m];
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  if (i >= bm_r1[blockIdx.x]) return;
+  const int i = bm_r0[bid] + threadIdx.x;
+  const bool ok = i < bm_r1[bid];
+  if (a & ACT_COMMIT) {  // block-uniform
+    double mb[2] = {0.0, 0.0};
+    if (ok) commit_mass_node(i, nd, mb[0], mb[1]);
+    block_accumulate<2>(mb, red + (size_t)m * RD_NUM + RD_DSTORE_C);
+  }
+  if (!ok) return;
   const MemberScal& S = ms[m];
   if (a & (ACT_COMMIT | ACT_BACKSTEP | ACT_START | ACT_NEXT)) {
     start_phase0_node(i, a, nd);
@@ -2066,100 +2189,139 @@ __global__ void k_start_vg_f32(int nb1, const int32_t* bm_mem, const int32_t* bm
   }
   if (a & ACT_ITER) vg_f32_node(i, nd, nf, z, S);
 }
-
-
-// ---- compensated FP32 sums (TwoSum) for the mass-balance reductions ----
-struct FF {
-  float hi, lo;
-};
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  const float s = a.hi + b.hi;
-  const float bb = s - a.hi;
-  const float err = (a.hi - (s - bb)) + (b.hi - bb);
-  return FF{s, err + a.lo + b.lo};
-}
-// Block sum of NV compensated values, one FP64 atomic per value.
-template <int NV>
-__device__ __forceinline__ void block_accumulate_ff(FF (&v)[NV], double* acc) {
-  __shared__ float shh[NV][kThreads / 32], shl[NV][kThreads / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    FF s = v[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      FF t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
-      s = ff_add(s, t);
-    }
-    if (lane == 0) { shh[i][w] = s.hi; shl[i][w] = s.lo; }
+__global__ void k_start_vg_f32(int nb1, const int32_t* bm_mem, const int32_t* bm_r0,
+                               const int32_t* bm_r1, const uint8_t* act,
+                               const MemberScal* ms, Nodal nd, NodalF nf, const double* z,
+                               int need_sw, int nmem, uint8_t* active, double* red) {
+  pdl_enter();
+  if ((int)blockIdx.x >= nb1) {
+    // Krylov member flags (the blocks after the node blocks)
+    k_flags_b(blockIdx.x - nb1, nmem, act, ACT_ITER, active);
+    return;
   }
-  __syncthreads();
-  if (w == 0) {
-    const int nw = blockDim.x >> 5;
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-      FF s{lane < nw ? shh[i][lane] : 0.0f, lane < nw ? shl[i][lane] : 0.0f};
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        FF t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
-        s = ff_add(s, t);
-      }
-      if (lane == 0 && (s.hi != 0.0f || s.lo != 0.0f))
-        atomicAdd(acc + i, (double)s.hi + (double)s.lo);
-    }
-  }
+  start_vg_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, nd, nf, z, need_sw, red);
 }
 
-// Compact FP32 element record for the assembly: S[10], |V|, |V|*porosity.
-__global__ void k_rec48(int nt, const TetRec<float>* rec, float4* out) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nt) return;
+// beta and Se at PTIMEP in FP64 of nodes [i0, i1) (the carried values of
+// the FP32 path's mass balance)
+__global__ void k_init_carry(int i0, int i1, Nodal nd) {
+  const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= i1) return;
+  const double p = nd.ptimep[i];
+  double b = 0.0, se = 1.0;
+  if (p < -1.0e-14) {
+    b = pow(fabs(p / nd.vgpsat[i]), nd.vgn[i]);
+    se = pow(fabs(1.0 / (b + 1.0)), nd.vgm[i]);
+  }
+  nd.bet[i] = b;
+  nd.set[i] = se;
+}
+
+
+// Per-incidence FP32 assembly records.  Incidence p of row i is element e
+// with i as its local node k; its record holds row k of the element's
+// stiffness shape for the other three local nodes a < b < c (S_ka, S_kb,
+// S_kc; S_kk = -(S_ka + S_kb + S_kc): P1 stiffness rows sum to zero) and
+// the element volume.  vpi[p] (consistent mass only) holds |V| * porosity.
+__global__ void k_rec16(long ninc, const int32_t* inc, const TetRec<float>* rec, float4* out,
+                        float* vpi) {
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= ninc) return;
+  const int e = inc[p] >> 2, k = inc[p] & 3;
   const TetRec<float> R = rec[e];
-  out[3 * (size_t)e] = make_float4(R.S[0], R.S[1], R.S[2], R.S[3]);
-  out[3 * (size_t)e + 1] = make_float4(R.S[4], R.S[5], R.S[6], R.S[7]);
-  out[3 * (size_t)e + 2] = make_float4(R.S[8], R.S[9], R.vol, R.vpel);
+  float o[3];
+  int t = 0;
+#pragma unroll
+  for (int l = 0; l < 4; ++l)
+    if (l != k) o[t++] = R.S[sym_idx(k, l)];
+  out[p] = make_float4(o[0], o[1], o[2], R.vol);
+  if (vpi) vpi[p] = R.vpel;
+}
+
+// Per node: the sum of |V| * porosity over its incident elements (the
+// lumped storage-coefficient weight of CFMATP and of RHSPIC's Sw term).
+__global__ void k_vps(int n, const int32_t* inc_ptr, const int32_t* inc,
+                      const TetRec<float>* rec, float* vps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = 0.0;
+  for (int q = inc_ptr[i]; q < inc_ptr[i + 1]; ++q) v += (double)rec[inc[q] >> 2].vpel;
+  vps[i] = (float)v;
 }
 
 // Row-owned Picard assembly in FP32.  One 16-lane group per row.  The lanes
 // first stage the row's column heads (total head as a float hi/lo pair, and
-// the head/saturation changes for a consistent mass matrix) in shared
-// memory, then take the row's incident elements in parallel (lane j:
-// incidences j, j+16, ...): each incidence reads its element record and the
-// row-local slots of the element's four nodes (precomputed, 4 bits each), so
-// no node id or nodal value is gathered from global memory per incidence.
-// The diagonal entries are summed by a shuffle reduction; the off-diagonal
-// ones are written to shared memory at position q*4 + l (incidence q, local
-// node l) and each slot's owner lane adds its contributions through a gather
-// list precomputed from the mesh (in incidence order): deterministic, no
-// atomics.  RHS = -sum K (h_l - h_k) - mass terms, see the FP32 block
-// comment.  The element means of kr and Sw*Ss (NODELT) are formed per
-// incidence from the staged values of the element's four nodes, and the
-// row's boundary flux (BCPIC: static Neumann flux, plus
+// the head/saturation changes for a consistent mass matrix) and the
+// columns' (kr, Sw*Ss) in shared memory, then take the row's incidences in
+// parallel (lane j: incidences j, j+16, ...; the first two rounds' records
+// are loaded together): each reads its own 16-byte record (three stiffness
+// entries and the volume, contiguous per row, no element indirection) and
+// the row-local slots of the element's nodes in the order k, a, b, c (4
+// bits each), so no node id or nodal value is gathered from global memory
+// per incidence.  The diagonal entries are summed by a shuffle reduction;
+// the off-diagonal ones are written to shared memory at position q*4 + t
+// (incidence q, t = 1..3 for a, b, c) and each slot's owner lane adds its
+// contributions through a gather list precomputed from the mesh (in
+// incidence order): deterministic, no atomics.  RHS = -sum K (h_l - h_k) -
+// mass terms, see the FP32 block comment; the storage-coefficient terms use
+// the row's sum of |V| * porosity (vps).  The element means of kr and Sw*Ss
+// (NODELT) are formed per incidence from the staged values of the element's
+// four nodes, and the row's boundary flux (BCPIC: static Neumann flux, plus
 // theta*ATMACT + (1-theta)*ATMOLD at atmospheric Neumann surface nodes) is
 // added by the row's first lane.
-// 6 resident blocks per SM (40 registers; 8 B of spill): measured faster on
-// the full batch than the 5 blocks that 48 registers allow
-__global__ void __launch_bounds__(kThreads, 6)
-k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                      const uint8_t* act, const MemberScal* ms,
-                      const int32_t* rowptr, const int32_t* cols,
-                      const int32_t* inc_ptr, const int32_t* inc,
-                      const uint16_t* __restrict__ islot, const float4* __restrict__ rec48,
-                      const uint8_t* dmask, NodalF nf, const int32_t* __restrict__ loc,
-                      const int8_t* __restrict__ ifatm, const double* __restrict__ atmact,
-                      const double* __restrict__ atmold, float* vals,
-                      float lm_d, float lm_o, const int64_t* __restrict__ glrow,
-                      const uint8_t* __restrict__ gloff, const uint8_t* __restrict__ gl) {
-  pdl_enter();
-  const int m = bm_mem[blockIdx.x];
+//
+// The device function is one 16-row map entry bid (block-uniform early
+// exits, no block barrier); arrays that other phases of the fused Picard
+// iteration write (IFATM, ATMACT, ATMOLD, the nodal fields) carry no
+// __restrict__ so that they are never read through the non-coherent path.
+struct AsmInc {  // one incidence's contribution to its row
+  float dacc, rp, msum;
+};
+__device__ __forceinline__ void asm_incidence(int q, float4 r, int isl, float vp, int grp,
+                                              float th, float rdt, float lm_d, float lm_o,
+                                              float hh_i, float hl_i,
+                                              float (*sval)[64 * 4], float2 (*sh2)[kGroup],
+                                              float2 (*sk2)[kGroup], float (*sdp)[kGroup],
+                                              float (*sds)[kGroup], AsmInc& a) {
+  const int s0 = isl & 15, sa = (isl >> 4) & 15, sb = (isl >> 8) & 15, sc = (isl >> 12) & 15;
+  const float2 n0 = sk2[grp][s0], n1 = sk2[grp][sa], n2 = sk2[grp][sb], n3 = sk2[grp][sc];
+  const float kr = 0.25f * (n0.x + n1.x + n2.x + n3.x);
+  const float e1 = 0.25f * (n0.y + n1.y + n2.y + n3.y);
+  const float ve1 = r.w * e1;
+  const float tk = th * kr;
+  const float mo = ve1 * lm_o * rdt;
+  sval[grp][q * 4 + 1] = tk * r.x + mo;
+  sval[grp][q * 4 + 2] = tk * r.y + mo;
+  sval[grp][q * 4 + 3] = tk * r.z + mo;
+  a.dacc += -tk * ((r.x + r.y) + r.z) + ve1 * lm_d * rdt;
+  const float2 ha = sh2[grp][sa], hb = sh2[grp][sb], hc = sh2[grp][sc];
+  const float da = (ha.x - hh_i) + (ha.y - hl_i);
+  const float db = (hb.x - hh_i) + (hb.y - hl_i);
+  const float dc = (hc.x - hh_i) + (hc.y - hl_i);
+  a.rp -= kr * ((r.x * da + r.y * db) + r.z * dc);
+  a.msum += ve1 * lm_d;
+  if (lm_o != 0.0f) {
+    a.rp -= (ve1 * lm_o * (sdp[grp][sa] + sdp[grp][sb] + sdp[grp][sc]) +
+             vp * lm_o * (sds[grp][sa] + sds[grp][sb] + sds[grp][sc])) * rdt;
+  }
+}
+
+__device__ __forceinline__ void assemble_f32_entry(
+    int bid, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+    const uint8_t* act, const MemberScal* ms, const int32_t* rowptr, const int32_t* cols,
+    const int32_t* inc_ptr, const float4* rec16, const uint16_t* islot, const float* vpi,
+    const float* vps, const uint8_t* dmask, const NodalF& nf, const int32_t* loc,
+    const int8_t* ifatm, const double* atmact, const double* atmold, float* vals, float lm_d,
+    float lm_o, const int64_t* glrow, const uint8_t* gloff, const uint8_t* gl) {
+  const int m = bm_mem[bid];
   if (!(act[m] & ACT_ITER)) return;
   __shared__ float sval[kRowsPerBlock16][64 * 4];
   __shared__ float2 sh2[kRowsPerBlock16][kGroup];
   __shared__ float2 sk2[kRowsPerBlock16][kGroup];
   __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
-  const int i = bm_r0[blockIdx.x] + grp;
-  const bool rowok = i < bm_r1[blockIdx.x];
+  const int i = bm_r0[bid] + grp;
+  const bool rowok = i < bm_r1[bid];
   const MemberScal& S = ms[m];
   const float rdt = (float)S.deltat_r, th = (float)S.tetaf;
   int s0 = 0, rlen = 0, p0 = 0, p1 = 0, col = -1;
@@ -2172,6 +2334,20 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
     if (lane < rlen) col = cols[s0 + lane];
   }
+  // the first two rounds of incidence records, in flight with the staging
+  float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+  int i0 = -1, i1 = -1;
+  float v0 = 0.0f, v1 = 0.0f;
+  if (rowok && p0 + lane < p1) {
+    r0 = rec16[p0 + lane];
+    i0 = islot[p0 + lane];
+    if (lm_o != 0.0f) v0 = vpi[p0 + lane];
+  }
+  if (rowok && p0 + kGroup + lane < p1) {
+    r1 = rec16[p0 + kGroup + lane];
+    i1 = islot[p0 + kGroup + lane];
+    if (lm_o != 0.0f) v1 = vpi[p0 + kGroup + lane];
+  }
   if (col >= 0) {
     sh2[grp][lane] = nf.h2[col];
     sk2[grp][lane] = nf.ckr2[col];
@@ -2183,75 +2359,41 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   __syncwarp();
   int ntrip = (p1 - p0 + kGroup - 1) / kGroup;
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
-  float dacc = 0.0f, rp = 0.0f, msum = 0.0f, mssum = 0.0f;
-  for (int trip = 0; trip < ntrip; ++trip) {
+  AsmInc a{0.0f, 0.0f, 0.0f};
+  if (i0 >= 0)
+    asm_incidence(lane, r0, i0, v0, grp, th, rdt, lm_d, lm_o, hh_i, hl_i, sval, sh2, sk2, sdp,
+                  sds, a);
+  if (i1 >= 0)
+    asm_incidence(kGroup + lane, r1, i1, v1, grp, th, rdt, lm_d, lm_o, hh_i, hl_i, sval, sh2, sk2,
+                  sdp, sds, a);
+  for (int trip = 2; trip < ntrip; ++trip) {  // nodes with more than 32 incident elements
     const int q = trip * kGroup + lane;
-    const int p = p0 + q;
-    if (rowok && p < p1) {
-      const int ek = inc[p];
-      const int isl = islot[p];
-      const int e = ek >> 2, k = ek & 3;
-      const float4* rv = rec48 + 3 * (size_t)e;
-      const float4 r0 = rv[0], r1 = rv[1], r2 = rv[2];
-      // row k of the packed symmetric 4x4 stiffness shape (S[sym_idx(k, l)]),
-      // selected with constant indices
-      const float srow[4] = {
-          k == 0 ? r0.x : k == 1 ? r0.y : k == 2 ? r0.z : r0.w,
-          k == 0 ? r0.y : k == 1 ? r1.x : k == 2 ? r1.y : r1.z,
-          k == 0 ? r0.z : k == 1 ? r1.y : k == 2 ? r1.w : r2.x,
-          k == 0 ? r0.w : k == 1 ? r1.z : k == 2 ? r2.x : r2.y};
-      const float vol = r2.z, vpel = r2.w;
-      const float2 n0 = sk2[grp][isl & 15], n1 = sk2[grp][(isl >> 4) & 15],
-                   n2 = sk2[grp][(isl >> 8) & 15], n3 = sk2[grp][(isl >> 12) & 15];
-      const float kr = 0.25f * (n0.x + n1.x + n2.x + n3.x);
-      const float e1 = 0.25f * (n0.y + n1.y + n2.y + n3.y);
-      const float ve1 = vol * e1;
-#pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        const float lm = (l == k) ? lm_d : lm_o;
-        const float skl = srow[l];
-        float c = th * (kr * skl) + ve1 * lm * rdt;
-        if (l == k) {
-          c += vpel * lm_d * et2i * rdt;
-          dacc += c;
-        } else {
-          sval[grp][q * 4 + l] = c;
-        }
-        const int sl = (isl >> (4 * l)) & 15;
-        const float2 hn = sh2[grp][sl];
-        const float dh = (hn.x - hh_i) + (hn.y - hl_i);
-        rp -= kr * skl * dh;
-        if (l == k) {
-          msum += ve1 * lm_d;
-          mssum += vpel * lm_d;
-        } else if (lm_o != 0.0f) {
-          rp -= (ve1 * lm_o * sdp[grp][sl] + vpel * lm_o * sds[grp][sl]) * rdt;
-        }
-      }
-    }
+    if (rowok && p0 + q < p1)
+      asm_incidence(q, rec16[p0 + q], islot[p0 + q], lm_o != 0.0f ? vpi[p0 + q] : 0.0f, grp, th,
+                    rdt, lm_d, lm_o, hh_i, hl_i, sval, sh2, sk2, sdp, sds, a);
   }
   __syncwarp();
-  const float dsum = group_sum<float>(dacc);
-  float rhs = group_sum<float>(rp);
-  msum = group_sum<float>(msum);
-  mssum = group_sum<float>(mssum);
+  const float dsum = group_sum<float>(a.dacc);
+  float rhs = group_sum<float>(a.rp);
+  const float msum = group_sum<float>(a.msum);
   if (!rowok) return;
+  const float vpl = vps[i] * lm_d;  // sum over the row's elements of |V| porosity LM_kk
   if (lane < rlen) {
     const int sl = s0 + lane;
     float lhs;
     if (col == i) {
-      lhs = dsum;
+      lhs = dsum + vpl * et2i * rdt;
     } else {
       const int64_t base = glrow[i];
-      const int a = gloff[sl];
-      const int b = (lane + 1 < rlen) ? (int)gloff[sl + 1] : (int)(glrow[i + 1] - base);
+      const int ga = gloff[sl];
+      const int gb = (lane + 1 < rlen) ? (int)gloff[sl + 1] : (int)(glrow[i + 1] - base);
       lhs = 0.0f;
-      for (int u = a; u < b; ++u) lhs += sval[grp][gl[base + u]];
+      for (int u = ga; u < gb; ++u) lhs += sval[grp][gl[base + u]];
     }
     vals[sl] = lhs;
   }
   if (lane == 0) {
-    rhs -= (msum * nf.dpsi[i] + mssum * nf.dsw[i]) * rdt;
+    rhs -= (msum * nf.dpsi[i] + vpl * nf.dsw[i]) * rdt;
     nf.xt5[i] = rhs;
     float f = nf.qneu[i];
     if (loc[i] < S.nnod && ifatm[i] == 0) {
@@ -2261,6 +2403,25 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     }
     nf.rhs[i] = dmask[i] ? 0.0f : rhs + f;
   }
+}
+
+// 6 resident blocks per SM (40 registers; 8 B of spill): measured faster on
+// the full batch than the 5 blocks that 48 registers allow
+__global__ void __launch_bounds__(kThreads, 6)
+k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                      const uint8_t* act, const MemberScal* ms,
+                      const int32_t* rowptr, const int32_t* cols, const int32_t* inc_ptr,
+                      const float4* __restrict__ rec16, const uint16_t* __restrict__ islot,
+                      const float* __restrict__ vpi, const float* __restrict__ vps,
+                      const uint8_t* dmask, NodalF nf, const int32_t* __restrict__ loc,
+                      const int8_t* __restrict__ ifatm, const double* __restrict__ atmact,
+                      const double* __restrict__ atmold, float* vals,
+                      float lm_d, float lm_o, const int64_t* __restrict__ glrow,
+                      const uint8_t* __restrict__ gloff, const uint8_t* __restrict__ gl) {
+  pdl_enter();
+  assemble_f32_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, rowptr, cols, inc_ptr, rec16,
+                     islot, vpi, vps, dmask, nf, loc, ifatm, atmact, atmold, vals, lm_d, lm_o,
+                     glrow, gloff, gl);
 }
 
 
@@ -2273,102 +2434,96 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
 // attaining PINF) come from one 64-bit maximum of (|dp| float bits, node
 // index) per member.  The last block to finish converts the maxima and
 // takes the per-member pass: PNEW/POLD at IKMAX and whether SWITCH_OLD runs.
-__global__ void __launch_bounds__(kThreads)
-k_masbal_post_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-                  const uint8_t* act, const MemberScal* ms, Nodal nd, NodalF nf,
-                  const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
-                  const float* __restrict__ vals, double* red, double* redmax, int nmem,
-                  const int32_t* node_off, int32_t* ikmax, double* ikval, int l2norm,
-                  uint8_t* sw, unsigned int* done) {
-  pdl_enter();
-  const int m = bm_mem[blockIdx.x];
+__device__ __forceinline__ void masbal_post_entry(int bid, const int32_t* bm_mem,
+                                                  const int32_t* bm_r0, const int32_t* bm_r1,
+                                                  const uint8_t* act, const MemberScal* ms,
+                                                  Nodal& nd, NodalF& nf, const int32_t* rowptr,
+                                                  const int32_t* cols, const float* vals,
+                                                  double* red, double* redmax) {
+  const int m = bm_mem[bid];
   const int wl = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (act[m] & ACT_ITER) {  // block-uniform
-    const int i = bm_r0[blockIdx.x] + threadIdx.x;
-    const MemberScal& S = ms[m];
-    FF v[RD_PL2];
-    for (int q = 0; q < RD_PL2; ++q) v[q] = FF{0.0f, 0.0f};
-    float pl2 = 0.0f, fl2 = 0.0f, finf = 0.0f;
-    unsigned long long key = 0ull;
-    if (i < bm_r1[blockIdx.x]) {
-      double p = nd.pnew[i] + (double)nf.pdiff[i];
-      const bool dir = nd.dmask[i] != 0;
-      if (nd.sdir[i]) p = nd.presc[i];
-      else if (dir) p = nd.pold[i];
-      const bool surf = nd.loc[i] < S.nnod;
-      if (dir) {
-        const int s0 = rowptr[i], s1 = rowptr[i + 1];
-        float sp = 0.0f;
-        for (int sl = s0; sl < s1; ++sl) sp += vals[sl] * nf.pdiff[cols[sl]];
-        const double th = S.tetaf;
-        const double scr = (double)sp - (double)nf.xt5[i];
-        if (nd.sdir[i]) nd.qpnew[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.qpold[i]) / th;
-        else if (surf)
-          nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
-      }
-      const int8_t f = surf ? nd.ifatm[i] : (int8_t)-1;
-      if (nd.sdir[i]) {
-        const float qn = (float)nd.qpnew[i];
-        if (qn > 0.0f) v[RD_NDIN].hi = qn; else v[RD_NDOUT].hi = qn;
-      }
-      if (f != -1) {
-        const float aa = (float)nd.atmact[i];
-        if (f == 1 || f == 2) {
-          if (aa > 0.0f) v[RD_ADIN].hi = aa; else v[RD_ADOUT].hi = aa;
-        } else {
-          if (aa > 0.0f) v[RD_ANIN].hi = aa; else v[RD_ANOUT].hi = aa;
-        }
-      }
-      if (S.nlrelx == 1) p = S.omega * p + (1.0 - S.omega) * nd.pold[i];
-      nd.pnew[i] = p;
-      const float dp = (float)(p - nd.ptimep[i]);
-      const float swv = nf.sw[i], dsw = nf.dsw[i];
-      v[RD_DSTORE].hi = nf.volnod[i] * (nf.ss[i] * (2.0f * swv - dsw) * 0.5f * dp + nf.pnodi[i] * dsw);
-      const float diff = (float)(p - nd.pold[i]);
-      pl2 = diff * diff;
-      const float b = nf.rhs[i];
-      fl2 = b * b;
-      finf = fabsf(b);
-      key = ((unsigned long long)__float_as_uint(fabsf(diff)) << 32) |
-            (unsigned long long)(uint32_t)nd.loc[i];
+  if (!(act[m] & ACT_ITER)) return;  // block-uniform
+  const int i = bm_r0[bid] + threadIdx.x;
+  const MemberScal& S = ms[m];
+  double v[RD_PL2];  // FP64 boundary-flux sums (FLUXMB); DSTORE comes at the commit
+  for (int q = 0; q < RD_PL2; ++q) v[q] = 0.0;
+  float pl2 = 0.0f, fl2 = 0.0f, finf = 0.0f;
+  unsigned long long key = 0ull;
+  if (i < bm_r1[bid]) {
+    double p = nd.pnew[i] + (double)nf.pdiff[i];
+    const bool dir = nd.dmask[i] != 0;
+    if (nd.sdir[i]) p = nd.presc[i];
+    else if (dir) p = nd.pold[i];
+    const bool surf = nd.loc[i] < S.nnod;
+    if (dir) {
+      const int s0 = rowptr[i], s1 = rowptr[i + 1];
+      float sp = 0.0f;
+      for (int sl = s0; sl < s1; ++sl) sp += vals[sl] * nf.pdiff[cols[sl]];
+      const double th = S.tetaf;
+      const double scr = (double)sp - (double)nf.xt5[i];
+      if (nd.sdir[i]) nd.qpnew[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.qpold[i]) / th;
+      else if (surf)
+        nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
     }
-    block_accumulate_ff<RD_PL2>(v, red + (size_t)m * RD_NUM);
-    float sums[2] = {pl2, fl2};
-    block_accumulate_t<float, 2>(sums, red + (size_t)m * RD_NUM + RD_PL2);
-    __shared__ float shf[kThreads / 32];
-    __shared__ unsigned long long shk[kThreads / 32];
+    const int8_t f = surf ? nd.ifatm[i] : (int8_t)-1;
+    if (nd.sdir[i]) {
+      const double qn = nd.qpnew[i];
+      if (qn > 0.0) v[RD_NDIN] = qn; else v[RD_NDOUT] = qn;
+    }
+    if (f != -1) {
+      const double aa = nd.atmact[i];
+      if (f == 1 || f == 2) {
+        if (aa > 0.0) v[RD_ADIN] = aa; else v[RD_ADOUT] = aa;
+      } else {
+        if (aa > 0.0) v[RD_ANIN] = aa; else v[RD_ANOUT] = aa;
+      }
+    }
+    nd.pmb[i] = p;  // the mass balance's head (masbal.f runs before RELAX)
+    if (S.nlrelx == 1) p = S.omega * p + (1.0 - S.omega) * nd.pold[i];
+    nd.pnew[i] = p;
+    const float diff = (float)(p - nd.pold[i]);
+    pl2 = diff * diff;
+    const float b = nf.rhs[i];
+    fl2 = b * b;
+    finf = fabsf(b);
+    key = ((unsigned long long)__float_as_uint(fabsf(diff)) << 32) |
+          (unsigned long long)(uint32_t)nd.loc[i];
+  }
+  block_accumulate<RD_PL2>(v, red + (size_t)m * RD_NUM);
+  float sums[2] = {pl2, fl2};
+  block_accumulate_t<float, 2>(sums, red + (size_t)m * RD_NUM + RD_PL2);
+  __shared__ float shf[kThreads / 32];
+  __shared__ unsigned long long shk[kThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    finf = fmaxf(finf, __shfl_xor_sync(0xffffffffu, finf, o));
+    const unsigned long long ko = __shfl_xor_sync(0xffffffffu, key, o);
+    key = ko > key ? ko : key;
+  }
+  if (wl == 0) { shf[w] = finf; shk[w] = key; }
+  __syncthreads();
+  if (w == 0) {
+    float a = wl < (int)(blockDim.x >> 5) ? shf[wl] : 0.0f;
+    unsigned long long kk = wl < (int)(blockDim.x >> 5) ? shk[wl] : 0ull;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      finf = fmaxf(finf, __shfl_xor_sync(0xffffffffu, finf, o));
-      const unsigned long long ko = __shfl_xor_sync(0xffffffffu, key, o);
-      key = ko > key ? ko : key;
+      a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+      const unsigned long long ko = __shfl_xor_sync(0xffffffffu, kk, o);
+      kk = ko > kk ? ko : kk;
     }
-    if (wl == 0) { shf[w] = finf; shk[w] = key; }
-    __syncthreads();
-    if (w == 0) {
-      float a = wl < (int)(blockDim.x >> 5) ? shf[wl] : 0.0f;
-      unsigned long long kk = wl < (int)(blockDim.x >> 5) ? shk[wl] : 0ull;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
-        const unsigned long long ko = __shfl_xor_sync(0xffffffffu, kk, o);
-        kk = ko > kk ? ko : kk;
-      }
-      if (wl == 0) {
-        atomicMax(reinterpret_cast<unsigned long long*>(redmax + (size_t)m * 2), kk);
-        atomic_max_nonneg(redmax + (size_t)m * 2 + 1, (double)a);
-      }
+    if (wl == 0) {
+      atomicMax(reinterpret_cast<unsigned long long*>(redmax + (size_t)m * 2), kk);
+      atomic_max_nonneg(redmax + (size_t)m * 2 + 1, (double)a);
     }
   }
-  __shared__ int s_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
+}
+
+// The per-member pass after the mass-balance blocks: PINF and IKMAX from
+// the packed maxima, PNEW/POLD at IKMAX, and whether SWITCH_OLD runs.
+__device__ __forceinline__ void masbal_members(int nmem, const uint8_t* act, const MemberScal* ms,
+                                               Nodal& nd, double* red, double* redmax,
+                                               const int32_t* node_off, int32_t* ikmax,
+                                               double* ikval, int l2norm, uint8_t* sw) {
   for (int q = threadIdx.x; q < nmem; q += blockDim.x) {
     const bool it = (act[q] & ACT_ITER) != 0;
     double pinf = 0.0;
@@ -2385,10 +2540,38 @@ k_masbal_post_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm
     const double pl2 = sqrt(red[(size_t)q * RD_NUM + RD_PL2]);
     sw[q] = it && ((l2norm == 0 && pinf <= ms[q].tolswi) || (l2norm != 0 && pl2 <= ms[q].tolswi));
   }
-  if (threadIdx.x == 0) *done = 0u;
 }
 
 
+
+
+__global__ void __launch_bounds__(kThreads)
+k_masbal_post_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                  const uint8_t* act, const MemberScal* ms, Nodal nd, NodalF nf,
+                  const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
+                  const float* __restrict__ vals, double* red, double* redmax, int nmem,
+                  const int32_t* node_off, int32_t* ikmax, double* ikval, int l2norm,
+                  uint8_t* sw, unsigned int* done) {
+  pdl_enter();
+  masbal_post_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, nd, nf, rowptr, cols, vals, red,
+                    redmax);
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  masbal_members(nmem, act, ms, nd, red, redmax, node_off, ikmax, ikval, l2norm, sw);
+  if (threadIdx.x == 0) *done = 0u;
+}
+
+__global__ void k_cast_f64_f32(long n, const double* a, float* b) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
 
 // FP32 copies of the nodal van Genuchten parameters (after CHPARM)
 __global__ void k_params_f32(int n, Nodal nd, NodalF nf) {
@@ -2454,31 +2637,14 @@ __global__ void k_switch_flags(int nmem, const uint8_t* act, const double* red,
 // the same sweeps, x0 = T^-1 b (the reference's starting guess M^-1 b) |
 // |b_masked|^2 per member | iteration counts = 1 and beta = 0 (first
 // direction p = z).  r = b - A x0 and z = T^-1 r follow.
-__global__ void __launch_bounds__(kThreads)
-k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1, int nc,
-                const int32_t* c_mem, const int32_t* c_r0, const int32_t* c_r1,
-                const uint8_t* active, const MemberScal* ms, const int32_t* __restrict__ diag,
-                const int32_t* __restrict__ down, const float* __restrict__ vals,
-                const uint8_t* __restrict__ dmask, float* pinv, float* cdown,
-                const float* __restrict__ b, float* x, double* sc, int nmem,
-                int32_t* niter, const int32_t* amem_cum, int32_t* kact) {
-  pdl_enter();
-  int bb = blockIdx.x;
-  if (bb >= ns) {
-    bb -= ns;
-    if (bb < nc) {
-      k_dot_b<float>(bb, c_mem, c_r0, c_r1, active, b, b, dmask, sc, SC_N, SC_XL);
-      return;
-    }
-    bb -= nc;
-    const int m = bb * blockDim.x + threadIdx.x;
-    if (m < nmem && active[m]) {
-      niter[m] = 1;
-      sc[(size_t)m * SC_N + SC_BETA] = 0.0;
-    }
-    if (bb == 0) build_kact(amem_cum, nmem, active, kact);  // the first block of this part
-    return;
-  }
+// Column part of the set-up for the column block bb (no block barrier).
+__device__ __forceinline__ void pcg_setup_col_entry(int bb, const int32_t* s_mem,
+                                                    const int32_t* s_r0, const int32_t* s_r1,
+                                                    const uint8_t* active, const MemberScal* ms,
+                                                    const int32_t* diag, const int32_t* down,
+                                                    const float* vals, const uint8_t* dmask,
+                                                    float* pinv, float* cdown, const float* b,
+                                                    float* x) {
   const int m = s_mem[bb];
   if (!active[m]) return;
   const int top = s_r0[bb] + threadIdx.x;
@@ -2554,6 +2720,42 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
   }
 }
 
+// Per-member part: iteration counts 1 and beta = 0 for the members of
+// block bb's slice of members; block 0 also builds the Krylov entry list.
+__device__ __forceinline__ void pcg_setup_members(int bb, int nmem, const uint8_t* active,
+                                                  int32_t* niter, double* sc,
+                                                  const int32_t* amem_cum, int32_t* kact) {
+  const int m = bb * blockDim.x + threadIdx.x;
+  if (m < nmem && active[m]) {
+    niter[m] = 1;
+    sc[(size_t)m * SC_N + SC_BETA] = 0.0;
+  }
+  if (bb == 0) build_kact(amem_cum, nmem, active, kact);
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1, int nc,
+                const int32_t* c_mem, const int32_t* c_r0, const int32_t* c_r1,
+                const uint8_t* active, const MemberScal* ms, const int32_t* __restrict__ diag,
+                const int32_t* __restrict__ down, const float* __restrict__ vals,
+                const uint8_t* __restrict__ dmask, float* pinv, float* cdown,
+                const float* __restrict__ b, float* x, double* sc, int nmem,
+                int32_t* niter, const int32_t* amem_cum, int32_t* kact) {
+  pdl_enter();
+  int bb = blockIdx.x;
+  if (bb >= ns) {
+    bb -= ns;
+    if (bb < nc) {
+      k_dot_b<float>(bb, c_mem, c_r0, c_r1, active, b, b, dmask, sc, SC_N, SC_XL);
+      return;
+    }
+    pcg_setup_members(bb - nc, nmem, active, niter, sc, amem_cum, kact);
+    return;
+  }
+  pcg_setup_col_entry(bb, s_mem, s_r0, s_r1, active, ms, diag, down, vals, dmask, pinv, cdown, b,
+                      x);
+}
+
 // One column-line PCG step after the fused direction update + product
 // (k_spmv_stream<true>), one thread per vertical column: alpha = p.r / p.q;
 // r -= alpha q, x += alpha p; rr += |r_masked|^2; z = T^-1 r (forward and
@@ -2562,91 +2764,92 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
 // beta = -q.z / p.q for the next direction, and either sets the graph's
 // WHILE condition (use_cond) or stores the number of members still
 // iterating in *nact.
-__global__ void __launch_bounds__(kThreads)
-k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
-             uint8_t* active, const MemberScal* ms, double* sc, const float* __restrict__ pinv,
-             const float* __restrict__ cdown, float* r, float* x, const float* __restrict__ p,
-             const float* __restrict__ q, float* z, const uint8_t* __restrict__ dmask, int nmem,
-             int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
-             unsigned int* done, int32_t* nact, int use_cond, cudaGraphConditionalHandle h,
-             const int32_t* amem_cum, int32_t* kact) {
-  pdl_enter();
-  const int m = bm_mem[blockIdx.x];
-  if (active[m]) {  // block-uniform
-    float dd[2] = {0.0f, 0.0f};  // rr, qz
-    const int top = bm_r0[blockIdx.x] + threadIdx.x;
-    if (top < bm_r1[blockIdx.x]) {
-      const float alfa = (float)(sc[(size_t)m * SC_N + SC_PR] / sc[(size_t)m * SC_N + SC_PQ]);
-      const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
-      float yprev = 0.0f, cprev = 0.0f, pprev = 0.0f;
-      for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
-        float rr[kLineChunk], qq[kLineChunk], pp[kLineChunk], xx[kLineChunk], pv[kLineChunk],
-            cd[kLineChunk];
-        bool dm[kLineChunk];
+// One column block bid of the column-line PCG step: r, x update, z =
+// T^-1 r, and the block's rr and qz into the member's Krylov scalars.
+__device__ __forceinline__ void pcg_xz_entry(int bid, const int32_t* bm_mem, const int32_t* bm_r0,
+                                             const int32_t* bm_r1, const uint8_t* active,
+                                             const MemberScal* ms, double* sc, const float* pinv,
+                                             const float* cdown, float* r, float* x,
+                                             const float* p, const float* q, float* z,
+                                             const uint8_t* dmask) {
+  const int m = bm_mem[bid];
+  if (!active[m]) return;  // block-uniform
+  float dd[2] = {0.0f, 0.0f};  // rr, qz
+  const int top = bm_r0[bid] + threadIdx.x;
+  if (top < bm_r1[bid]) {
+    const float alfa = (float)(sc[(size_t)m * SC_N + SC_PR] / sc[(size_t)m * SC_N + SC_PQ]);
+    const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
+    float yprev = 0.0f, cprev = 0.0f, pprev = 0.0f;
+    for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
+      float rr[kLineChunk], qq[kLineChunk], pp[kLineChunk], xx[kLineChunk], pv[kLineChunk],
+          cd[kLineChunk];
+      bool dm[kLineChunk];
 #pragma unroll
-        for (int j = 0; j < kLineChunk; ++j) {
-          const int k = k0 + j;
-          rr[j] = qq[j] = pp[j] = xx[j] = pv[j] = cd[j] = 0.0f;
-          dm[j] = true;
-          if (k < nl) {
-            const int i = top + k * nnod;
-            rr[j] = r[i]; qq[j] = q[i]; pp[j] = p[i]; xx[j] = x[i];
-            pv[j] = pinv[i]; cd[j] = cdown[i]; dm[j] = dmask[i] != 0;
-          }
-        }
-#pragma unroll
-        for (int j = 0; j < kLineChunk; ++j) {
-          const int k = k0 + j;
-          if (k < nl) {
-            const int i = top + k * nnod;
-            const float ri = rr[j] - alfa * qq[j];
-            r[i] = ri;
-            x[i] = xx[j] + alfa * pp[j];
-            if (!dm[j]) dd[0] += ri * ri;
-            const float yk = ri - cprev * yprev * pprev;
-            z[i] = yk;
-            yprev = yk;
-            cprev = cd[j];
-            pprev = pv[j];
-          }
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k0 + j;
+        rr[j] = qq[j] = pp[j] = xx[j] = pv[j] = cd[j] = 0.0f;
+        dm[j] = true;
+        if (k < nl) {
+          const int i = top + k * nnod;
+          rr[j] = r[i]; qq[j] = q[i]; pp[j] = p[i]; xx[j] = x[i];
+          pv[j] = pinv[i]; cd[j] = cdown[i]; dm[j] = dmask[i] != 0;
         }
       }
-      float znext = 0.0f;
-      for (int k1 = nl - 1; k1 >= 0; k1 -= kLineChunk) {
-        float yy[kLineChunk], pv[kLineChunk], cd[kLineChunk], qq[kLineChunk];
 #pragma unroll
-        for (int j = 0; j < kLineChunk; ++j) {
-          const int k = k1 - j;
-          yy[j] = pv[j] = cd[j] = qq[j] = 0.0f;
-          if (k >= 0) {
-            const int i = top + k * nnod;
-            yy[j] = z[i]; pv[j] = pinv[i]; cd[j] = cdown[i]; qq[j] = q[i];
-          }
-        }
-#pragma unroll
-        for (int j = 0; j < kLineChunk; ++j) {
-          const int k = k1 - j;
-          if (k >= 0) {
-            const float zk = (yy[j] - cd[j] * znext) * pv[j];
-            z[top + k * nnod] = zk;
-            dd[1] += qq[j] * zk;
-            znext = zk;
-          }
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k0 + j;
+        if (k < nl) {
+          const int i = top + k * nnod;
+          const float ri = rr[j] - alfa * qq[j];
+          r[i] = ri;
+          x[i] = xx[j] + alfa * pp[j];
+          if (!dm[j]) dd[0] += ri * ri;
+          const float yk = ri - cprev * yprev * pprev;
+          z[i] = yk;
+          yprev = yk;
+          cprev = cd[j];
+          pprev = pv[j];
         }
       }
     }
-    block_accumulate_t<float, 2>(dd, sc + (size_t)m * SC_N + SC_RR);
+    float znext = 0.0f;
+    for (int k1 = nl - 1; k1 >= 0; k1 -= kLineChunk) {
+      float yy[kLineChunk], pv[kLineChunk], cd[kLineChunk], qq[kLineChunk];
+#pragma unroll
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k1 - j;
+        yy[j] = pv[j] = cd[j] = qq[j] = 0.0f;
+        if (k >= 0) {
+          const int i = top + k * nnod;
+          yy[j] = z[i]; pv[j] = pinv[i]; cd[j] = cdown[i]; qq[j] = q[i];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kLineChunk; ++j) {
+        const int k = k1 - j;
+        if (k >= 0) {
+          const float zk = (yy[j] - cd[j] * znext) * pv[j];
+          z[top + k * nnod] = zk;
+          dd[1] += qq[j] * zk;
+          znext = zk;
+        }
+      }
+    }
   }
-  __shared__ int s_last, s_cnt;
+  block_accumulate_t<float, 2>(dd, sc + (size_t)m * SC_N + SC_RR);
+}
+
+// The per-member PCG decision after a step (GRADDP's stopping test: the
+// masked recursive residual against TOLCG, and the iteration cap), the next
+// beta = -q.z / p.q, the Krylov scalars cleared for the next step, and the
+// entry list of the members still iterating.  One block; returns the number
+// of members still iterating (to thread 0).
+__device__ __forceinline__ int pcg_decide(int nmem, uint8_t* active, double* sc, int32_t* niter,
+                                          int itmax, double tol, const int32_t* amem_cum,
+                                          int32_t* kact) {
+  __shared__ int s_cnt;
+  if (threadIdx.x == 0) s_cnt = 0;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
-    s_cnt = 0;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
   int mine = 0;
   for (int mm = threadIdx.x; mm < nmem; mm += blockDim.x) {
     if (!active[mm]) continue;
@@ -2666,37 +2869,57 @@ k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
   if (mine) atomicAdd(&s_cnt, mine);
   __syncthreads();
   build_kact(amem_cum, nmem, active, kact);
+  return s_cnt;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+             uint8_t* active, const MemberScal* ms, double* sc, const float* __restrict__ pinv,
+             const float* __restrict__ cdown, float* r, float* x, const float* __restrict__ p,
+             const float* __restrict__ q, float* z, const uint8_t* __restrict__ dmask, int nmem,
+             int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
+             unsigned int* done, int32_t* nact, int use_cond, cudaGraphConditionalHandle h,
+             const int32_t* amem_cum, int32_t* kact) {
+  pdl_enter();
+  pcg_xz_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, active, ms, sc, pinv, cdown, r, x, p, q, z, dmask);
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int cnt = pcg_decide(nmem, active, sc, niter, itmax, tol, amem_cum, kact);
   if (threadIdx.x == 0) {
     *done = 0u;
     const int l = *loops + 1;
     *loops = l;
-    if (use_cond) cudaGraphSetConditional(h, (s_cnt > 0 && l < maxloops) ? 1u : 0u);
-    if (nact) *nact = s_cnt;
+    if (use_cond) cudaGraphSetConditional(h, (cnt > 0 && l < maxloops) ? 1u : 0u);
+    if (nact) *nact = cnt;
   }
 }
 
 
 
 
-// SWITCH_OLD on the surface nodes of the members that switch, then STORE1
-// (storcal.f) of every iterating member at the final heads.
-__global__ void k_switch_store1_f32(const int32_t* bm_mem, const int32_t* bm_r0,
-                                    const int32_t* bm_r1, const uint8_t* act, const uint8_t* sw,
-                                    const MemberScal* ms, Nodal nd, NodalF nf, double* red) {
+// SWITCH_OLD on the surface nodes of the members whose norms allow it (the
+// storage STORE1 of an accepted step is formed in FP64 when it is
+// committed, k_start_vg_f32).
+__device__ __forceinline__ void switch_entry(int bid, const int32_t* bm_mem, const int32_t* bm_r0,
+                                             const int32_t* bm_r1, const uint8_t* act,
+                                             const uint8_t* sw, const MemberScal* ms, Nodal& nd) {
+  const int m = bm_mem[bid];
+  if (!(act[m] & ACT_ITER) || !sw[m]) return;
+  const int i = bm_r0[bid] + threadIdx.x;
+  if (i < bm_r1[bid] && nd.loc[i] < ms[m].nnod) switch_node(i, ms[m].pmin, nd);
+}
+__global__ void k_switch_f32(const int32_t* bm_mem, const int32_t* bm_r0,
+                             const int32_t* bm_r1, const uint8_t* act, const uint8_t* sw,
+                             const MemberScal* ms, Nodal nd) {
   pdl_enter();
-  const int m = bm_mem[blockIdx.x];
-  if (!(act[m] & ACT_ITER)) return;
-  const int i = bm_r0[blockIdx.x] + threadIdx.x;
-  FF v[1] = {FF{0.0f, 0.0f}};
-  if (i < bm_r1[blockIdx.x]) {
-    if (sw[m] && nd.loc[i] < ms[m].nnod) switch_node(i, ms[m].pmin, nd);
-    const double p = nd.pnew[i];
-    float se = 1.0f;
-    if (p < -1.0e-14) se = expf(-nf.vgm[i] * log1pf(vgf_beta((float)p, nf.vgpsat[i], nf.vgn[i])));
-    const float swv = nf.vgpnot[i] * se + nf.rmcp[i];
-    v[0].hi = swv * nf.volnod[i] * nf.pnodi[i];
-  }
-  block_accumulate_ff<1>(v, red + (size_t)m * RD_NUM + RD_STORE1);
+  switch_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, act, sw, ms, nd);
 }
 
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
@@ -2735,6 +2958,10 @@ struct MemberHost {
   int steps_done = 0;
   std::vector<cathy_iter_rec_t> iter_recs;
   std::vector<cathy_step_rec_t> step_recs;
+  // FP32 path: the accepted step whose FP64 storage change and storage come
+  // back with the macro-iteration that commits it
+  bool rec_pending = false;
+  cathy_step_rec_t prec{};
   // atm interpolation to push to the device
   int atm_mode = 0;
   double atm_ta = 0, atm_tb = 0, atm_va = 0, atm_vb = 0;
@@ -2773,7 +3000,9 @@ struct Engine {
   DBuf<int64_t> d_glrow;
   DBuf<uint8_t> d_gloff, d_gl;
   DBuf<uint16_t> d_islot;  // per incidence: row-local slots of the element's 4 nodes (4 bits each)
-  DBuf<float4> d_rec48;    // per element: S[10], volume, volume*porosity (3 x float4)
+  DBuf<float4> d_rec16;    // per incidence: three stiffness entries of its row, volume
+  DBuf<float> d_vpi;       // per incidence: volume * porosity (consistent mass only)
+  DBuf<float> d_vps;       // per node: sum of volume * porosity over its elements
   DBuf<int32_t> d_srows, d_lev_f, d_lev_b;
   std::vector<int32_t> lev_f_ptr, lev_b_ptr;  // batched levels (host)
   DBuf<double> d_vals64;
@@ -2812,6 +3041,7 @@ struct Engine {
   std::vector<uint8_t> h_act;
 
   ~Engine() {
+    for (cudaEvent_t ev : pev) cudaEventDestroy(ev);
     graph_free();
     lp_work_free(lpw);
     if (gev0) cudaEventDestroy(gev0);
@@ -2862,6 +3092,7 @@ struct Engine {
   // graph of the macro-iteration copies)
   void push_scalars(bool to_pinned = false);
   int macro_iteration();
+  void flush_commits();
   void picard_or_newton_iteration(const std::vector<int>& itm);
   // phase 0: whole solve with host checks every chk iterations; 1: set-up
   // only; 2: one iteration + graph decision (the body of a WHILE node)
@@ -2876,6 +3107,42 @@ struct Engine {
   int lt_cap = 1 << 16;
   int64_t lt_pending = 0;     // launches written since the last flush
   int persist_blocks = 1216;  // grid of the persistent kernels (8 per SM)
+  // Phase timers in the reference's CPUVEC buckets (picard.f:66-202, the
+  // risul summary at cathy_main.f:3913-3950) with NVTX ranges of the same
+  // names.  When enabled, macro-iterations run kernel by kernel (the same
+  // kernels as the graph) with CUDA events between the phases.
+  bool phase_timing = false;
+  double phase_ms[9] = {};
+  std::vector<cudaEvent_t> pev;
+  std::vector<std::pair<int, int>> pmarks;  // (event index, bucket or -1)
+  bool nvtx_open = false;
+  void phase(int bucket) {
+    if (!phase_timing || pdl_cap) return;
+    static const char* kNames[9] = {
+        "UNSAT CHARACTERISTICS", "INIT. OF SYSTEM MATRICES", "LOCAL SYSTEM ASSEMBLY",
+        "RHS CALCULATION W/O BC'S", "GLOBAL LHS SYSTEM MATRIX", "BC CONTRIBUTIONS TO RHS",
+        "LINEAR SOLVER & RESIDUAL", "DIR. RESETTING AND DIFMAX", "B-FLX, M-BAL, SW, & EX-PT"};
+    if (nvtx_open) nvtxRangePop();
+    nvtx_open = bucket >= 0;
+    if (nvtx_open) nvtxRangePushA(kNames[bucket]);
+    const int k = (int)pmarks.size();
+    if (k >= (int)pev.size()) {
+      cudaEvent_t ev;
+      CG_TRY(cudaEventCreate(&ev));
+      pev.push_back(ev);
+    }
+    CG_TRY(cudaEventRecord(pev[k], st));
+    pmarks.emplace_back(k, bucket);
+  }
+  void phase_collect() {  // after the stream has been synchronised
+    for (size_t k = 0; k + 1 < pmarks.size(); ++k) {
+      if (pmarks[k].second < 0) continue;
+      float ms = 0.0f;
+      CG_TRY(cudaEventElapsedTime(&ms, pev[pmarks[k].first], pev[pmarks[k + 1].first]));
+      phase_ms[pmarks[k].second] += ms;
+    }
+    pmarks.clear();
+  }
   void lt_reset() {
     std::vector<unsigned long long> h((size_t)LT_HDR + 2 * (size_t)lt_cap);
     h[LT_SEQ] = 0;
@@ -2940,6 +3207,9 @@ struct Engine {
            (const int32_t*)d_kact.p, (const int32_t*)(d_kact.p + nmem + 2));
   }
   void solve_bicgstab(int isolv, int itmax, double tol);
+  template <class VT>
+  void bicgstab_t(int isolv, int itmax, double tol, const VT* vals, const VT* b, VT* x,
+                  DBuf<VT>* w, VT* F, VT* G);
   template <class MT> void assemble();
   void iteration_pre(int solve_phase);
   // learned column-line preconditioner (mode 1: train on the plain solver's
@@ -3019,7 +3289,7 @@ enum {
   ND_PTNEW, ND_PTOLD, ND_PTIMEP, ND_PDIFF, ND_SWNEW, ND_SWTIMEP, ND_RHS, ND_XT5,
   ND_QNEU, ND_PRESC, ND_QPNEW, ND_QPOLD, ND_SW, ND_ET1, ND_ET2, ND_CKRW, ND_ETAI,
   ND_DCKRW, ND_DETAI, ND_ARENOD, ND_ATMPOT, ND_ATMACT, ND_ATMOLD, ND_ATMA, ND_ATMB,
-  ND_X, ND_Y, ND_Z, ND_NUM
+  ND_X, ND_Y, ND_Z, ND_PMB, ND_BET, ND_SET, ND_NUM
 };
 
 void Engine::make_elem_blockmap(BlockMap& bm, int epb) {
@@ -3254,14 +3524,18 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         for (int sj = 0; sj < rl; ++sj) cnt[sj] = 0;
         for (int q = 0; q < ninc; ++q) {
           const int e = g.inc[p0 + q] >> 2, k = g.inc[p0 + q] & 3;
+          // local nodes in the order k, then the others ascending (the
+          // order of the incidence record's stiffness entries)
+          int ord[4] = {k, 0, 0, 0}, t = 1;
+          for (int l = 0; l < 4; ++l)
+            if (l != k) ord[t++] = l;
           uint16_t packed = 0;
-          for (int l = 0; l < 4; ++l) {
-            const int j = g.tetra[5 * e + l] - 1;
+          for (t = 0; t < 4; ++t) {
+            const int j = g.tetra[5 * e + ord[t]] - 1;
             const int sj = (int)(std::lower_bound(g.cols.begin() + s0, g.cols.begin() + s0 + rl, j) -
                                  (g.cols.begin() + s0));
-            packed |= (uint16_t)(sj << (4 * l));
-            if (l == k) continue;
-            lst[sj][cnt[sj]++] = (uint8_t)(q * 4 + l);
+            packed |= (uint16_t)(sj << (4 * t));
+            if (t > 0) lst[sj][cnt[sj]++] = (uint8_t)(q * 4 + t);
           }
           h_islot[(size_t)h_incptr[no + i] + q] = packed;
         }
@@ -3474,12 +3748,13 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   nd.dckrw = P(ND_DCKRW); nd.detai = P(ND_DETAI); nd.arenod = P(ND_ARENOD);
   nd.atmpot = P(ND_ATMPOT); nd.atmact = P(ND_ATMACT); nd.atmold = P(ND_ATMOLD);
   nd.atm_a = P(ND_ATMA); nd.atm_b = P(ND_ATMB);
+  nd.pmb = P(ND_PMB); nd.bet = P(ND_BET); nd.set = P(ND_SET);
   nd.sdir = d_sdir.p; nd.dmask = d_dmask.p; nd.ifatm = d_ifatm.p; nd.ifatmp = d_ifatmp.p;
   // TPNODI/CHPARM then geometry
   k_tpnodi<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, d_inc_ptr.p, d_inc.p, d_tetsoil.p,
       d_tab[4].p, d_tab[3].p, d_tab[5].p, d_tab[6].p, d_tab[7].p, nd);
   check_launch();
-  if (precision == 0) {
+  if (precision == 0 || iopt == 2) {  // Newton assembles in FP64 at both precisions
     d_rec64.alloc(NT);
     k_geom<double><<<cdiv(NT, 128), 128, 0, st>>>((int)NT, d_tet.p, P(ND_X), P(ND_Y), P(ND_Z),
         d_tetsoil.p, d_tab[0].p, d_tab[1].p, d_tab[2].p, P(ND_PNODI), d_rec64.p, P(ND_VOLNOD), nullptr);
@@ -3487,8 +3762,17 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     d_rec32.alloc(NT);
     k_geom<float><<<cdiv(NT, 128), 128, 0, st>>>((int)NT, d_tet.p, P(ND_X), P(ND_Y), P(ND_Z),
         d_tetsoil.p, d_tab[0].p, d_tab[1].p, d_tab[2].p, P(ND_PNODI), d_rec32.p, P(ND_VOLNOD), nullptr);
-    d_rec48.alloc((size_t)3 * NT);
-    k_rec48<<<cdiv(NT, 256), 256, 0, st>>>((int)NT, d_rec32.p, d_rec48.p);
+    if (iopt == 1) {
+      const long ninc = (long)d_inc.n;
+      d_rec16.alloc(ninc);
+      if (lump == 0) d_vpi.alloc(ninc);
+      d_vps.alloc(N);
+      k_rec16<<<cdiv(ninc, 256), 256, 0, st>>>(ninc, d_inc.p, d_rec32.p, d_rec16.p,
+                                               lump == 0 ? d_vpi.p : nullptr);
+      k_vps<<<cdiv(N, 256), 256, 0, st>>>(N, d_inc_ptr.p, d_inc.p, d_rec32.p, d_vps.p);
+      CG_TRY(cudaStreamSynchronize(st));
+      d_rec32.free();  // the FP32 Picard path reads only the per-incidence records
+    }
   }
   check_launch();
   if (precision == 1 && iopt == 1) {
@@ -3502,18 +3786,22 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     d_ckr2.alloc(N); d_h2.alloc(N);
     nf.ckr2 = d_ckr2.p; nf.h2 = d_h2.p;
     k_params_f32<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, nd, nf);
+    k_init_carry<<<cdiv(N, kThreads), kThreads, 0, st>>>(0, N, nd);
     check_launch();
   }
   // matrix and solver workspace
-  if (precision == 0) { d_vals64.alloc(NNZ); d_vals64.zero(st); }
-  else { d_vals32.alloc(NNZ + 4); d_vals32.zero(st); d_vals64.alloc(0); }
+  // FP32 Newton: FP64 Jacobian and residual, FP32 copy of the Jacobian for
+  // the BiCGSTAB correction solve
+  if (precision == 0 || iopt == 2) { d_vals64.alloc(NNZ); d_vals64.zero(st); }
+  if (precision == 1) { d_vals32.alloc(NNZ + 4); d_vals32.zero(st); }
   const int nw = 14;
   if (precision == 0 || iopt == 2) for (int k = 0; k < nw; ++k) { w64[k].alloc(N); w64[k].zero(st); }
   else for (int k = 0; k < 4; ++k) { w64[k].alloc(N); w64[k].zero(st); }
-  if (precision == 1) for (int k = 0; k < 8; ++k) { w32[k].alloc(N); w32[k].zero(st); }
+  if (precision == 1)
+    for (int k = 0; k < (iopt == 2 ? nw : 8); ++k) { w32[k].alloc(N); w32[k].zero(st); }
   if (precond == 0 || iopt == 2) {
-    if (precision == 0 || iopt == 2) { d_F64.alloc(NNZ); if (iopt == 2) d_G64.alloc(NNZ); }
-    else d_F32.alloc(NNZ);
+    if (precision == 0) { d_F64.alloc(NNZ); if (iopt == 2) d_G64.alloc(NNZ); }
+    else { d_F32.alloc(NNZ); if (iopt == 2) d_G32.alloc(NNZ); }
   }
   if (precond == 2) {
     if (precision == 0) { d_linv64.alloc(N); d_lc64.alloc(N); }
@@ -3702,6 +3990,10 @@ void Engine::reset() {
   cp(nd.qpold, s_qpnew);
   CG_TRY(cudaMemcpyAsync(nd.ifatm, s_ifatm.p, N, cudaMemcpyDeviceToDevice, st));
   CG_TRY(cudaMemcpyAsync(nd.ifatmp, s_ifatmp.p, N, cudaMemcpyDeviceToDevice, st));
+  if (precision == 1 && iopt == 1) {
+    k_init_carry<<<cdiv(N, kThreads), kThreads, 0, st>>>(0, N, nd);
+    check_launch();
+  }
 }
 
 void Engine::push_scalars(bool to_pinned) {
@@ -4027,46 +4319,50 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
   }
 }
 
-// ---- BiCGSTAB (Newton), FP64, GCSTAS (isolv 0) / GCSTAD (isolv -5) ----
-void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
-  const double* vals = d_vals64.p;
-  double *x = nd.pdiff, *b = nd.rhs;
-  double *r = w64[2].p, *rt = w64[3].p, *p = w64[4].p, *v = w64[5].p, *s = w64[6].p,
-         *t = w64[7].p, *pjm = w64[8].p, *vjm = w64[9].p, *scr1 = w64[10].p,
-         *scr2 = w64[11].p, *dd = w64[12].p, *tmp = w64[13].p;
+// ---- BiCGSTAB (Newton), GCSTAS (isolv 0) / GCSTAD (isolv -5) ----
+// VT = double: the reference's FP64 solve on the FP64 Jacobian.  VT = float:
+// the correction solve of the FP32 Newton path on an FP32 copy of the
+// Jacobian (the residual, the Newton update and the convergence test stay
+// FP64); the scalar recurrences are FP64 in both.
+template <class VT>
+void Engine::bicgstab_t(int isolv, int itmax, double tol, const VT* vals, const VT* b, VT* x,
+                        DBuf<VT>* w, VT* F, VT* G) {
+  VT *r = w[2].p, *rt = w[3].p, *p = w[4].p, *v = w[5].p, *s = w[6].p, *t = w[7].p,
+     *pjm = w[8].p, *vjm = w[9].p, *scr1 = w[10].p, *scr2 = w[11].p, *dd = w[12].p,
+     *tmp = w[13].p;
   const bool jac = (isolv == -5);
   auto E1 = [&](auto kern, auto... args) {
     kern<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, args...);
     count();
   };
-  auto lsolve = [&](const double* in, double* out) {
+  auto lsolve = [&](const VT* in, VT* out) {
     for (size_t l = 0; l + 1 < lev_f_ptr.size(); ++l) {
       const int nr = lev_f_ptr[l + 1] - lev_f_ptr[l];
       if (!nr) continue;
-      k_lsolve_level<double, double><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
-          d_lev_f.p + lev_f_ptr[l], d_rowptr.p, d_cols.p, d_diag.p, d_G64.p, d_active.p, d_mem.p, in, out);
+      k_lsolve_level<VT, VT><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
+          d_lev_f.p + lev_f_ptr[l], d_rowptr.p, d_cols.p, d_diag.p, G, d_active.p, d_mem.p, in, out);
       count();
     }
   };
-  auto usolve = [&](const double* in, double* out) {
+  auto usolve = [&](const VT* in, VT* out) {
     for (size_t l = 0; l + 1 < lev_b_ptr.size(); ++l) {
       const int nr = lev_b_ptr[l + 1] - lev_b_ptr[l];
       if (!nr) continue;
-      k_usolve_level<double, double><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
-          d_lev_b.p + lev_b_ptr[l], d_rowptr.p, d_cols.p, d_diag.p, d_G64.p, d_active.p, d_mem.p, in, out);
+      k_usolve_level<VT, VT><<<cdiv((long)nr * kGroup, kThreads), kThreads, 0, st>>>(nr,
+          d_lev_b.p + lev_b_ptr[l], d_rowptr.p, d_cols.p, d_diag.p, G, d_active.p, d_mem.p, in, out);
       count();
     }
   };
-  auto spmv = [&](const double* in, double* out) {
-    k_spmv<double, double><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
+  auto spmv = [&](const VT* in, VT* out) {
+    k_spmv<VT, VT><<<grid_spmv(cbm16.nblk), kSpmvThreads, 0, st>>>(cbm16.nblk, cbm16.mem.p,
         cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, in, out,
         nullptr, nullptr, 0, nullptr, nullptr, 0);
     count();
   };
-  auto applyB = [&](const double* in, double* out) {
+  auto applyB = [&](const VT* in, VT* out) {
     if (jac) {
       spmv(in, out);
-      E1(k_scale_vec<double>, out, (const double*)dd);
+      E1(k_scale_vec<VT>, out, (const VT*)dd);
     } else {
       usolve(in, scr1);
       spmv(scr1, scr2);
@@ -4081,66 +4377,66 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
     scv[(size_t)m * SC_N + SC_ETAJ] = 1.0;
   }
   d_sc.upload(scv.data(), scv.size(), st);
-  k_dot<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, b, b,
+  k_dot<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, b, b,
       d_dmask.p, d_sc.p, SC_N, SC_XL);
   count();
   if (jac) {
-    k_jacobi_setup<double, double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+    k_jacobi_setup<VT, VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
         d_active.p, d_diag.p, vals, d_dmask.p, dd);
     count();
-    E1(k_copy_cast<double, double>, (const double*)b, x, (const double*)nullptr, 0);
-    E1(k_scale_vec<double>, x, (const double*)dd);
+    E1(k_copy_cast<VT, VT>, (const VT*)b, x, (const double*)nullptr, 0);
+    E1(k_scale_vec<VT>, x, (const VT*)dd);
     spmv(x, scr1);
-    E1(k_sub_vec<double>, scr1, (const double*)b, (const double*)scr1);
-    E1(k_copy_cast<double, double>, (const double*)scr1, r, (const double*)nullptr, 0);
-    E1(k_scale_vec<double>, r, (const double*)dd);
+    E1(k_sub_vec<VT>, scr1, (const VT*)b, (const VT*)scr1);
+    E1(k_copy_cast<VT, VT>, (const VT*)scr1, r, (const double*)nullptr, 0);
+    E1(k_scale_vec<VT>, r, (const VT*)dd);
   } else {
     for (size_t l = 0; l + 1 < lev_f_ptr.size(); ++l) {
       const int nr = lev_f_ptr[l + 1] - lev_f_ptr[l];
       if (!nr) continue;
-      k_ilu0_level<double, double><<<cdiv(nr, 128), 128, 0, st>>>(nr, d_lev_f.p + lev_f_ptr[l],
-          d_rowptr.p, d_cols.p, d_diag.p, vals, d_dmask.p, d_active.p, d_mem.p, d_F64.p);
+      k_ilu0_level<VT, VT><<<cdiv(nr, 128), 128, 0, st>>>(nr, d_lev_f.p + lev_f_ptr[l],
+          d_rowptr.p, d_cols.p, d_diag.p, vals, d_dmask.p, d_active.p, d_mem.p, F);
       count();
     }
-    k_ilu0_split<double><<<cdiv(N, 256), 256, 0, st>>>(N, d_rowptr.p, d_cols.p, d_diag.p,
-        d_active.p, d_mem.p, d_F64.p, d_G64.p);
+    k_ilu0_split<VT><<<cdiv(N, 256), 256, 0, st>>>(N, d_rowptr.p, d_cols.p, d_diag.p,
+        d_active.p, d_mem.p, F, G);
     count();
     lsolve(b, tmp);
     usolve(tmp, x);              // x0 = (LU)^-1 b   (PROD1)
     spmv(x, scr1);
-    E1(k_sub_vec<double>, scr1, (const double*)b, (const double*)scr1);
+    E1(k_sub_vec<VT>, scr1, (const VT*)b, (const VT*)scr1);
     lsolve(scr1, r);             // r0 = L^-1 (b - A x0)
-    k_umul<double, double><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-        d_active.p, d_rowptr.p, d_cols.p, d_diag.p, d_G64.p, x, scr1);
+    k_umul<VT, VT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+        d_active.p, d_rowptr.p, d_cols.p, d_diag.p, G, x, scr1);
     count();
-    E1(k_copy_cast<double, double>, (const double*)scr1, x, (const double*)nullptr, 0);  // y0 = U x0
+    E1(k_copy_cast<VT, VT>, (const VT*)scr1, x, (const double*)nullptr, 0);  // y0 = U x0
   }
-  E1(k_copy_cast<double, double>, (const double*)r, rt, (const double*)nullptr, 0);
-  E1(k_set_vec<double>, pjm, (const double*)nullptr, 0.0);
-  E1(k_set_vec<double>, vjm, (const double*)nullptr, 0.0);
+  E1(k_copy_cast<VT, VT>, (const VT*)r, rt, (const double*)nullptr, 0);
+  E1(k_set_vec<VT>, pjm, (const VT*)nullptr, (VT)0);
+  E1(k_set_vec<VT>, vjm, (const VT*)nullptr, (VT)0);
   std::vector<int32_t> ones(nmem, 1);
   d_niter.upload(ones.data(), nmem, st);
   check_launch();
   for (int it = 0; it < itmax + 3; ++it) {
-    k_dot<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, rt, r,
+    k_dot<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, rt, r,
         nullptr, d_sc.p, SC_N, SC_ROJ);
     count();
-    E1(k_bicg_p<double>, (const double*)d_sc.p, p, (const double*)r, (const double*)pjm, (const double*)vjm);
+    E1(k_bicg_p<VT>, (const double*)d_sc.p, p, (const VT*)r, (const VT*)pjm, (const VT*)vjm);
     applyB(p, v);
-    k_dot<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, rt, v,
+    k_dot<VT><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_active.p, rt, v,
         nullptr, d_sc.p, SC_N, SC_SIG);
     count();
-    E1(k_bicg_s<double>, (const double*)d_sc.p, s, (const double*)r, (const double*)v);
+    E1(k_bicg_s<VT>, (const double*)d_sc.p, s, (const VT*)r, (const VT*)v);
     applyB(s, t);
-    E1(k_bicg_st<double>, d_sc.p, (const double*)s, (const double*)t);
-    E1(k_bicg_xr<double>, d_sc.p, x, r, (const double*)p, (const double*)s, (const double*)t,
+    E1(k_bicg_st<VT>, d_sc.p, (const VT*)s, (const VT*)t);
+    E1(k_bicg_xr<VT>, d_sc.p, x, r, (const VT*)p, (const VT*)s, (const VT*)t,
        (const uint8_t*)d_dmask.p);
     CG_TRY(cudaMemsetAsync(d_nact.p, 0, sizeof(int32_t), st));
     k_krylov_decide<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_active.p, d_sc.p, d_niter.p, itmax,
         tol, 1, d_nact.p);
     count();
-    E1(k_copy_cast<double, double>, (const double*)p, pjm, (const double*)nullptr, 0);
-    E1(k_copy_cast<double, double>, (const double*)v, vjm, (const double*)nullptr, 0);
+    E1(k_copy_cast<VT, VT>, (const VT*)p, pjm, (const double*)nullptr, 0);
+    E1(k_copy_cast<VT, VT>, (const VT*)v, vjm, (const double*)nullptr, 0);
     check_launch();
     int32_t nact = 0;
     d_nact.download(&nact, 1, st);
@@ -4150,11 +4446,33 @@ void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
   if (!jac) {
     // x = U^-1 y for every member that iterated
     k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
-    E1(k_copy_cast<double, double>, (const double*)x, tmp, (const double*)nullptr, 0);
+    E1(k_copy_cast<VT, VT>, (const VT*)x, tmp, (const double*)nullptr, 0);
     usolve(tmp, x);
   }
 }
 
+
+void Engine::solve_bicgstab(int isolv, int itmax, double tol) {
+  if (precision == 0) {
+    bicgstab_t<double>(isolv, itmax, tol, d_vals64.p, nd.rhs, nd.pdiff, w64, d_F64.p, d_G64.p);
+    return;
+  }
+  // FP32 correction solve: Jacobian and residual rounded to FP32, the
+  // correction back to FP64 (inner tolerance and cap as the Picard path's)
+  k_cast_f64_f32<<<cdiv(NNZ, 256), 256, 0, st>>>(NNZ, d_vals64.p, d_vals32.p);
+  k_copy_cast<double, float><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+      d_active.p, (const double*)nd.rhs, w32[0].p, (const double*)nullptr, 0);
+  count(2);
+  bicgstab_t<float>(isolv, std::min(itmax, opts.inner_maxit), std::max(tol, opts.inner_tol),
+                    d_vals32.p, w32[0].p, w32[1].p, w32, d_F32.p, d_G32.p);
+  // every member that iterated takes its correction (the Krylov flags are
+  // cleared as members converge)
+  k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
+  k_copy_cast<float, double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
+      d_active.p, (const float*)w32[1].p, nd.pdiff, (const double*)nullptr, 0);
+  count(2);
+  check_launch();
+}
 
 // One nonlinear iteration for every member flagged ACT_ITER, in three
 // phases: pre-solve (step actions and soil characteristics, assembly, BCs),
@@ -4169,30 +4487,38 @@ void Engine::iteration_pre(int solve_phase) {
     // FP64-grade, see the FP32 kernels); the inner FP32 PCG solves each
     // correction to opts.inner_tol.
     // step actions + soil characteristics + Krylov member flags in one pass
+    phase(0);
     launch(k_start_vg_f32, cbm1.nblk + cdiv(nmem, kThreads), kThreads, cbm1.nblk, cbm1.mem.p,
            cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, nf, d_nodal[ND_Z].p, need_sw_flag(), nmem,
-           d_active.p);
+           d_active.p, d_red.p);
     count();
+    // ASSPIC + RHSPIC + CFMATP + BC contributions fused: the CPUVEC buckets
+    // of system initialisation, assembly, RHS, LHS and BC in one kernel
+    phase(2);
     launch(k_assemble_picard_f32, cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-           d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_islot.p, d_rec48.p,
-           d_dmask.p, nf, nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact,
-           (const double*)nd.atmold, d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p,
-           d_gl.p);
+           d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, (const float4*)d_rec16.p,
+           (const uint16_t*)d_islot.p, (const float*)d_vpi.p, (const float*)d_vps.p, d_dmask.p, nf,
+           nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact, (const double*)nd.atmold,
+           d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
     count();
     check_launch();
     if (lp_mode && solve_phase == 0) lp_before_solve();
+    phase(6);
     solve_pcg<float, float>(std::min(P0.itmxcg, opts.inner_maxit),
                             std::max(P0.tolcg, opts.inner_tol), true, precond == 2 ? 3 : 1,
                             solve_phase);
     if (lp_mode == 1 && solve_phase == 0) lp_after_solve();
   } else {
+    phase(0);
     k_vg<double><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd,
                                                 iopt == 2);
     count();
     check_launch();
+    phase(2);
     assemble<double>();
     k_flags<<<cdiv(nmem, 128), 128, 0, st>>>(nmem, d_act.p, ACT_ITER, d_active.p);
     count();
+    phase(6);
     if (iopt == 1) solve_pcg<double, double>(P0.itmxcg, P0.tolcg, true, 1);
     else solve_bicgstab(P0.isolv, P0.itmxcg, P0.tolcg);
   }
@@ -4204,19 +4530,26 @@ void Engine::iteration_post(bool fused) {
   if (fused && mixed) {
     // fused path (the result buffer was zeroed at the start of the
     // iteration): head update + back-fluxes + mass balance + norms + IKMAX,
-    // the per-member pass by its last block; then switching and STORE1
+    // the per-member pass by its last block; then switching on the surface
+    phase(8);
     launch(k_masbal_post_f32, cbm1.nblk, kThreads, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p,
            (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf, (const int32_t*)d_rowptr.p,
            (const int32_t*)d_cols.p, (const float*)d_vals32.p, d_red.p, d_redmax.p, nmem,
            (const int32_t*)d_node_off.p, d_ikmax.p, d_ikval.p, P0.l2norm, d_switch.p, d_done.p + 1);
-    launch(k_switch_store1_f32, cbm1.nblk, kThreads, cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p,
-           d_switch.p, d_ms.p, nd, nf, d_red.p);
-    count(2);
+    count();
+    if (cbms.nblk) {
+      launch(k_switch_f32, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+             (const uint8_t*)d_act.p, (const uint8_t*)d_switch.p, (const MemberScal*)d_ms.p, nd);
+      count();
+    }
+    phase(-1);
     check_launch();
     return;
   }
+  phase(7);
   k_update_shl<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, nd);
   count();
+  phase(8);
   CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
   CG_TRY(cudaMemsetAsync(d_redmax.p, 0, sizeof(double) * nmem * 2, st));
   CG_TRY(cudaMemsetAsync(d_ikmax.p, 0, sizeof(int32_t) * nmem, st));
@@ -4230,6 +4563,7 @@ void Engine::iteration_post(bool fused) {
   if (cbms.nblk)
     k_switch<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_switch.p, d_ms.p, nd);
   count(5);
+  phase(-1);
   check_launch();
 }
 
@@ -4461,6 +4795,42 @@ void Engine::graph_build() {
   g_builds++;
 }
 
+// Completes member h's pending step record with the step's storage change
+// and storage: ERRAS = VIN + VOUT - DSTORE, ERREL and the cumulative sums
+// of the reference's time loop (cathy_main.f:3259-3273, masbal.f:98-109).
+static void finish_step_record(MemberHost& h, double dstore, double store1) {
+  cathy_step_rec_t& sr = h.prec;
+  const double vin = sr.vin, vout = sr.vout;
+  const double erras = vin + vout - dstore;
+  double errel;
+  if (sr.deltat >= 1.0e15) errel = vin != 0.0 ? 100.0 * erras / vin : 0.0;
+  else errel = (vin + vout) != 0.0 ? 100.0 * erras / (vin + vout) : 0.0;
+  h.store1 = store1;
+  h.store2 += dstore;
+  h.vtot += vin + vout;
+  h.cvin += vin; h.cvout += vout; h.cdstor += dstore; h.cerras += erras;
+  h.caeras += std::fabs(erras);
+  h.dstore = dstore; h.vin = vin; h.vout = vout; h.erras = erras; h.errel = errel;
+  sr.store1 = h.store1; sr.store2 = h.store2; sr.dstore = dstore; sr.cdstor = h.cdstor;
+  sr.cvin = h.cvin; sr.cvout = h.cvout; sr.erras = erras; sr.errel = errel;
+  sr.cerras = h.cerras; sr.caeras = h.caeras;
+  h.step_recs.push_back(sr);
+  h.rec_pending = false;
+}
+
+// Runs the pending commits of accepted steps now (one macro-iteration in
+// which no member iterates), so that every accepted step is recorded when a
+// run returns.
+void Engine::flush_commits() {
+  bool any = false;
+  for (int m = 0; m < nmem; ++m) any |= (M[m]->pend & ACT_COMMIT) != 0;
+  if (!any) return;
+  std::vector<bool> was(nmem);
+  for (int m = 0; m < nmem; ++m) { was[m] = M[m]->paused; M[m]->paused = true; }
+  macro_iteration();
+  for (int m = 0; m < nmem; ++m) M[m]->paused = was[m];
+}
+
 // ---- macro-iteration: device step actions, one nonlinear iteration, host
 // decisions (flow3d.f:212-294, TIMUPD, BKSTEP) ----
 int Engine::macro_iteration() {
@@ -4481,7 +4851,7 @@ int Engine::macro_iteration() {
     h_act[m] = a;
     h.pend &= (uint8_t)~a;  // bits not executed now stay pending
   }
-  const bool graph = graphs_on() && niter_members > 0;
+  const bool graph = graphs_on() && niter_members > 0 && !phase_timing;
   push_scalars(graph);
   if (!graph) d_act.upload(h_act.data(), nmem, st);
   else std::memcpy(hp_act, h_act.data(), nmem);
@@ -4526,13 +4896,23 @@ int Engine::macro_iteration() {
       if (lt_pending > lt_cap - 2 * (opts.inner_maxit + 8)) prof_flush();
     }
     red = hp_red; redmax = hp_redmax; ikv = hp_ikv; scv = hp_sc; ikmax = hp_ikmax; nit = hp_nit;
-  } else if (mixed && niter_members > 0) {
+  } else if (mixed) {
     // the graph's kernels launched one by one (the same kernels, in the
-    // same order, with the PCG loop driven from the host)
+    // same order, with the PCG loop driven from the host); with no member
+    // iterating only the step actions run (the commits of accepted steps,
+    // whose FP64 storage terms come back in the result buffer)
     CG_TRY(cudaMemsetAsync(d_resbuf.p, 0, sizeof(double) * res_zero, st));
     pdl_cap = pdl_prev = false;
-    iteration_pre(0);
-    iteration_post(true);
+    if (niter_members > 0) {
+      iteration_pre(0);
+      iteration_post(true);
+    } else if (cbm1.nblk) {
+      launch(k_start_vg_f32, cbm1.nblk + cdiv(nmem, kThreads), kThreads, cbm1.nblk, cbm1.mem.p,
+             cbm1.r0.p, cbm1.r1.p, (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf,
+             (const double*)d_nodal[ND_Z].p, need_sw_flag(), nmem, d_active.p, d_red.p);
+      count();
+      check_launch();
+    }
     v_res.resize(res_off[7]);
     d_resbuf.download(v_res.data(), res_off[7], st);
     CG_TRY(cudaStreamSynchronize(st));
@@ -4562,6 +4942,7 @@ int Engine::macro_iteration() {
     red = v_red.data(); redmax = v_redmax.data(); ikv = v_ikv.data(); scv = v_scv.data();
     ikmax = v_ikmax.data(); nit = v_nit.data();
   }
+  phase_collect();
   const auto t2 = clk::now();
   tm_prep += std::chrono::duration<double, std::milli>(t1 - t0).count();
   tm_dev += std::chrono::duration<double, std::milli>(t2 - t1).count();
@@ -4571,6 +4952,17 @@ int Engine::macro_iteration() {
     ~HostTimer() { e->tm_host += std::chrono::duration<double, std::milli>(clk::now() - t).count(); }
   } host_timer{this, t2};
   nl_iters += niter_members;
+  // FP32 path: steps committed in this macro-iteration get their FP64
+  // storage change and storage (formed at the commit) and are recorded
+  if (mixed) {
+    for (int m = 0; m < nmem; ++m) {
+      MemberHost& h = *M[m];
+      if (!h.rec_pending || !(h_act[m] & ACT_COMMIT)) continue;
+      const double* R = &red[(size_t)m * RD_NUM];
+      finish_step_record(h, R[RD_DSTORE_C], R[RD_STORE1_C]);
+    }
+  }
+  if (niter_members == 0) return 0;
   std::vector<uint8_t> conv_mask(nmem, 0);
   bool any_conv = false;
   for (int m : itm) {
@@ -4628,11 +5020,10 @@ int Engine::macro_iteration() {
     }
   }
   if (any_conv) {
-    // STORE1 (storcal.f) at the converged heads: the FP32 path computed it
-    // for every iterating member (k_switch_store1_f32); the FP64 path
-    // computes it now
+    // STORE1 (storcal.f) at the converged heads: the FP64 path computes it
+    // now; the FP32 path forms it with DSTORE when the step is committed
     const double* st1 = red;
-    if (!graph && !mixed) {
+    if (!mixed) {
       d_mask2.upload(conv_mask.data(), nmem, st);
       CG_TRY(cudaMemsetAsync(d_red.p, 0, sizeof(double) * nmem * RD_NUM, st));
       k_store1<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_mask2.p, nd, d_red.p);
@@ -4648,30 +5039,18 @@ int Engine::macro_iteration() {
       const cathy_parm_t& P = h.parm;
       const double* R = h.red_last;
       const double deltam = (h.deltat < 1.0e15) ? 0.5 * h.deltat : 1.0;
-      const double dstore = R[RD_DSTORE];
       const double vadin = (R[RD_ADIN] + h.adinp) * deltam, vadout = (R[RD_ADOUT] + h.adoutp) * deltam;
       const double vndin = (R[RD_NDIN] + h.ndinp) * deltam, vndout = (R[RD_NDOUT] + h.ndoutp) * deltam;
       const double vanin = (R[RD_ANIN] + h.aninp) * deltam, vanout = (R[RD_ANOUT] + h.anoutp) * deltam;
       const double vnnin = (h.nnin + h.nninp) * deltam, vnnout = (h.nnout + h.nnoutp) * deltam;
-      const double vin = vadin + vndin + vanin + vnnin;
-      const double vout = vadout + vndout + vanout + vnnout;
-      const double erras = vin + vout - dstore;
-      double errel;
-      if (h.deltat >= 1.0e15) errel = vin != 0.0 ? 100.0 * erras / vin : 0.0;
-      else errel = (vin + vout) != 0.0 ? 100.0 * erras / (vin + vout) : 0.0;
-      h.store1 = st1[(size_t)m * RD_NUM + RD_STORE1];
-      h.store2 += dstore;
-      h.vtot += vin + vout;
-      h.cvin += vin; h.cvout += vout; h.cdstor += dstore; h.cerras += erras;
-      h.caeras += std::fabs(erras);
-      h.dstore = dstore; h.vin = vin; h.vout = vout; h.erras = erras; h.errel = errel;
-      cathy_step_rec_t sr;
+      cathy_step_rec_t& sr = h.prec;
+      sr = cathy_step_rec_t{};
       sr.nstep = h.nstep; sr.iter = h.iter; sr.nitert = h.nitert; sr.nback = h.kbackt;
-      sr.deltat = h.deltat; sr.time = h.time; sr.store1 = h.store1; sr.store2 = h.store2;
-      sr.dstore = dstore; sr.cdstor = h.cdstor; sr.vin = vin; sr.cvin = h.cvin; sr.vout = vout;
-      sr.cvout = h.cvout; sr.erras = erras; sr.errel = errel; sr.cerras = h.cerras;
-      sr.caeras = h.caeras;
-      h.step_recs.push_back(sr);
+      sr.deltat = h.deltat; sr.time = h.time;
+      sr.vin = vadin + vndin + vanin + vnnin;
+      sr.vout = vadout + vndout + vanout + vnnout;
+      h.rec_pending = true;
+      if (!mixed) finish_step_record(h, R[RD_DSTORE], st1[(size_t)m * RD_NUM + RD_STORE1]);
       h.adinp = R[RD_ADIN]; h.adoutp = R[RD_ADOUT]; h.ndinp = R[RD_NDIN]; h.ndoutp = R[RD_NDOUT];
       h.aninp = R[RD_ANIN]; h.anoutp = R[RD_ANOUT]; h.nninp = h.nnin; h.nnoutp = h.nnout;
       h.steps_done++;
@@ -4750,6 +5129,7 @@ static int run_until(Engine* e, int target_mode, int max_macro) {
     if (e->macro_iteration() == 0 && ++idle > 2)
       throw std::string("no member made progress (internal state error)");
   }
+  e->flush_commits();
   for (int m = 0; m < e->nmem; ++m) e->M[m]->paused = false;
   CG_TRY(cudaEventRecord(e->ev1, e->st));
   CG_TRY(cudaEventSynchronize(e->ev1));
@@ -4786,6 +5166,7 @@ int engine_run(Engine* e, int max_steps, int* nsteps) {
     if (e->macro_iteration() == 0 && ++idle > 2)
       throw std::string("no member made progress (internal state error)");
   }
+  e->flush_commits();
   for (int m = 0; m < e->nmem; ++m) {
     e->M[m]->paused = false;
     done = std::max(done, e->M[m]->steps_done - start[m]);
@@ -4852,7 +5233,13 @@ int engine_set_state(Engine* e, int m, const double* ptimep, double time,
                          cudaMemcpyHostToDevice, e->st));
   CG_TRY(cudaMemcpyAsync(e->nd.ptimep + e->node_off[m], ptimep, sizeof(double) * n,
                          cudaMemcpyHostToDevice, e->st));
+  if (e->precision == 1 && e->iopt == 1) {
+    k_init_carry<<<cdiv((long)n, kThreads), kThreads, 0, e->st>>>(e->node_off[m],
+                                                                 e->node_off[m + 1], e->nd);
+    CG_TRY(cudaPeekAtLastError());
+  }
   CG_TRY(cudaStreamSynchronize(e->st));
+  h.rec_pending = false;
   h.time = time;
   h.deltat = deltat;
   h.timep = time - deltat;
@@ -4897,6 +5284,7 @@ int engine_get_mesh(Engine* e, int m, double* x, double* y, double* z,
 int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt5,
                          int32_t* dirmask) {
   if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  e->flush_commits();  // the FP32 path records a step when it commits it
   MemberHost& h = *e->M[m];
   // apply pending START so that pold/ptnew/swtimep are current
   std::vector<uint8_t> act(e->nmem, 0);
@@ -4917,8 +5305,9 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
     k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p,
                                                   e->d_ms.p, e->nd, e->nf, e->d_nodal[ND_Z].p);
     k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
-        e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_inc.p, e->d_islot.p,
-        e->d_rec48.p, e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold,
+        e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_rec16.p,
+        e->d_islot.p, e->d_vpi.p, e->d_vps.p, e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm,
+        e->nd.atmact, e->nd.atmold,
         e->d_vals32.p, (float)e->lm_d, (float)e->lm_o, e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
   } else {
     k_vg<double><<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->iopt == 2);
@@ -5002,6 +5391,67 @@ int engine_timers(Engine* e, double* out, int n) {
   for (int q = 0; q < n && q < 8; ++q) out[q] = v[q];
   for (int q = 8; q < n && q < 8 + 64; ++q)
     out[q] = ((q - 8) & 1) ? e->bin_ms[(q - 8) / 2] : e->bin_n[(q - 8) / 2];
+  return 0;
+}
+
+// Times the FP32 Picard assembly (k_assemble_picard_f32) on the current
+// state: nrep launches over every running member, between CUDA events on
+// the engine stream.  The launches rebuild the matrix, right-hand side and
+// XT5 from the nodal fields of each member's last iteration; the next
+// Picard iteration assembles again before it uses them.  Returns the mean launch time (ms) and
+// the launch's algorithmic bytes (asm_bytes: per row 74 B of row data, row
+// and column pointers, nodal inputs and outputs and the row's own nodal
+// values gathered once; per surface row 16 B of ATMACT/ATMOLD; per
+// incidence 16 B record + 2 B slots + 3 B gather entries (+4 B porosity
+// volume with a consistent mass matrix); per matrix slot 4 B column + 4 B
+// value written + 1 B gather offset), and the rows assembled.
+int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t* rows) {
+  if (!(e->precision == 1 && e->iopt == 1)) return CATHY_GB300_EUNSUP;
+  double b = 0.0;
+  int64_t r = 0;
+  std::vector<uint8_t> act(e->nmem, 0), memact(e->nmem, 0);
+  for (int m = 0; m < e->nmem; ++m)
+    if (e->M[m]->status == 0) act[m] = ACT_ITER, memact[m] = 1;
+  e->h_act = act;
+  e->d_act.upload(act.data(), e->nmem, e->st);
+  e->compact_maps(memact);
+  for (int m = 0; m < e->nmem; ++m) {
+    if (!act[m]) continue;
+    const HostMesh& g = *e->M[m]->meshp;
+    const double inc = 4.0 * g.nt;
+    b += 74.0 * g.n + 16.0 * g.nnod + (e->lm_o != 0.0 ? 25.0 : 21.0) * inc + 9.0 * (double)g.nnz();
+    r += g.n;
+  }
+  if (r == 0 || nrep < 1) return CATHY_GB300_EINVAL;
+  auto go = [&]() {
+    k_assemble_picard_f32<<<e->cbm16.nblk, kThreads, 0, e->st>>>(
+        e->cbm16.mem.p, e->cbm16.r0.p, e->cbm16.r1.p, e->d_act.p, e->d_ms.p, e->d_rowptr.p,
+        e->d_cols.p, e->d_inc_ptr.p, e->d_rec16.p, e->d_islot.p, e->d_vpi.p, e->d_vps.p,
+        e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold, e->d_vals32.p,
+        (float)e->lm_d, (float)e->lm_o, e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
+  };
+  go();  // warm
+  CG_TRY(cudaEventRecord(e->ev0, e->st));
+  for (int k = 0; k < nrep; ++k) go();
+  CG_TRY(cudaEventRecord(e->ev1, e->st));
+  CG_TRY(cudaEventSynchronize(e->ev1));
+  CG_TRY(cudaPeekAtLastError());
+  float t = 0.0f;
+  CG_TRY(cudaEventElapsedTime(&t, e->ev0, e->ev1));
+  *ms = t / nrep;
+  *bytes = b;
+  *rows = r;
+  return 0;
+}
+
+// Phase timers (enable 1: on and zeroed, 0: off, -1: read only): out[0..9)
+// the GPU ms of the nine CPUVEC buckets of the reference's risul summary.
+int engine_phase_timers(Engine* e, int enable, double* out, int n) {
+  for (int q = 0; q < n && q < 9; ++q) out[q] = e->phase_ms[q];
+  if (enable >= 0) {
+    e->phase_timing = enable != 0;
+    for (double& v : e->phase_ms) v = 0.0;
+  }
   return 0;
 }
 

@@ -43,10 +43,13 @@ struct MemberScal {
   double tolksl;                      // chord slope once |PTNEW - PTOLD| >= TOLKSL
 };
 
-// per-member reduction accumulators (zeroed before use)
+// per-member reduction accumulators (zeroed before use).  RD_DSTORE_C and
+// RD_STORE1_C hold the FP64 storage change and storage of the step accepted
+// in the previous macro-iteration (the FP32 path forms them when the step
+// is committed, see k_start_vg_f32).
 enum {
   RD_DSTORE = 0, RD_NDIN, RD_NDOUT, RD_ADIN, RD_ADOUT, RD_ANIN, RD_ANOUT,
-  RD_PL2, RD_FL2, RD_STORE1, RD_NUM
+  RD_PL2, RD_FL2, RD_STORE1, RD_DSTORE_C, RD_STORE1_C, RD_NUM
 };
 
 template <class MT>

@@ -18,6 +18,7 @@ convergence per time step, read by pyCATHY/importers/cathy_outputs.py:607
 from __future__ import annotations
 
 import os
+import time
 from typing import List, Sequence
 
 import numpy as np
@@ -173,6 +174,70 @@ def write_mbeconv(path: str, step_records, initial_volume: float) -> None:
             f.write(" ".join(vals) + "\n")
 
 
+_PHASE_LINES = (
+    " TOT CPU FOR UNSAT CHARACTERISTICS    = ", " TOT CPU FOR INIT. OF SYSTEM MATRICES = ",
+    " TOT CPU FOR LOCAL SYSTEM ASSEMBLY    = ", " TOT CPU FOR RHS CALCULATION W/O BC'S = ",
+    " TOT CPU FOR GLOBAL LHS SYSTEM MATRIX = ", " TOT CPU FOR BC CONTRIBUTIONS TO RHS  = ",
+    " TOT CPU FOR LINEAR SOLVER & RESIDUAL = ", " TOT CPU FOR DIR. RESETTING AND DIFMAX= ",
+    " TOT CPU FOR B-FLX, M-BAL, SW, & EX-PT= ")
+
+
+def write_risul(path: str, step_records, iter_records, phase_s, total_s) -> None:
+    """The closing summary of the reference's ``risul`` file
+    (cathy_main.f:3880-3950, formats 1215, 1400, 1420, 1440, 1450): the
+    cumulative mass-balance error, the back-step and linear-failure counts,
+    the time spent per phase (here GPU seconds of the nonlinear iterations,
+    in the reference's nine CPUVEC buckets, picard.f:66-202; ``phase_s``
+    holds them in that order) and the time-step statistics (DTSTAT,
+    dtstat.f:8-24)."""
+    recs, its = list(step_records), list(iter_records)
+    total = max(float(total_s), 1e-30)
+    nl = sum(phase_s)
+    with open(path, "w") as f:
+        if recs:
+            r = recs[-1]
+            vtot = r["cvin"] + r["cvout"]
+            if vtot != 0.0:
+                f.write(f"\n  CUMULATIVE (TOTAL) MBE BASED ON CERRAS         : {r['cerras']:12.5E}\n")
+                f.write(f"  CUMULATIVE (TOTAL) RELATIVE MBE BASED ON CERRAS: "
+                        f"{100.0 * r['cerras'] / vtot:12.5E} %\n")
+        nback = sum(int(r["nback"]) for r in recs)
+        f.write(f"\n  TOTAL NUMBER OF BACK-STEPPING OCCURRENCES      : {nback:6d}\n")
+        f.write("  TOTAL NUMBER OF LINEAR SOLVER FAILURES         :      0\n\n")
+        f.write(f"\n  TOT CPU FOR THE SIMULATION           = {total:15.2f} SECONDS  {100.0:6.2f} %\n")
+        f.write(f"  TOT CPU FOR NONLINEAR SCHEME         = {nl:15.2f} SECONDS  "
+                f"{100.0 * nl / total:6.2f} %\n")
+        f.write(f"  TOT CPU FOR OVERHEAD (SEE CODE DESC.)= {total - nl:15.2f} SECONDS  "
+                f"{100.0 * (total - nl) / total:6.2f} %\n\n")
+        for name, v in zip(_PHASE_LINES, phase_s):
+            f.write(f" {name}{v:15.2f} SECONDS  {100.0 * v / total:6.2f} %\n")
+        f.write(" " * 41 + "-----------" + " " * 9 + "-------\n")
+        f.write(" " * 41 + f"{nl:11.2f} SECONDS  {100.0 * nl / total:6.2f} %\n\n")
+        ns = len(recs)
+        dts = [r["deltat"] for r in recs]
+        ksm = int(np.argmin(dts)) if dts else 0
+        kbg = int(np.argmax(dts)) if dts else 0
+        nli = len(its)
+        lin = sum(int(r["niter"]) for r in its)
+        per = lambda a, b: a / b if b else 0.0
+        f.write(f"  TOTAL NUMBER OF TIME STEPS           = {ns:8d}\n")
+        if dts:
+            f.write(f"  SMALLEST TIME STEP SIZE              = {dts[ksm]:11.3E}  AT TIME "
+                    f"{recs[ksm]['time']:11.3E}\n")
+            f.write(f"  LARGEST  TIME STEP SIZE              = {dts[kbg]:11.3E}  AT TIME "
+                    f"{recs[kbg]['time']:11.3E}\n")
+            f.write(f"  AVERAGE  TIME STEP SIZE              = {sum(dts) / ns:11.3E}\n")
+        f.write(f"  TOTAL NUMBER OF NONLINEAR ITERATIONS = {nli:8d}\n")
+        f.write(f"  TOTAL NUMBER OF LINEAR ITERATIONS    = {lin:8d}  (= 0 FOR NONSYM)\n")
+        f.write(f"  AVG NL ITERATIONS PER TIME STEP      = {per(nli, ns):8.2f}\n")
+        f.write(f"  AVG LINEAR ITERATIONS PER TIME STEP  = {per(lin, ns):8.2f}\n")
+        f.write(f"  AVG LIN ITERATIONS PER NL ITERATION  = {per(lin, nli):8.2f}\n")
+        f.write(f"  AVG TOT CPU PER TIME STEP            = {per(total, ns):8.2f} SECONDS\n")
+        f.write(f"  AVG TOT CPU PER NL ITERATION         = {per(total, nli):8.2f} SECONDS\n")
+        f.write(f"  AVG TOT NL CPU PER TIME STEP         = {per(nl, ns):8.2f} SECONDS\n")
+        f.write(f"  AVG TOT NL CPU PER NL ITERATION      = {per(nl, nli):8.2f} SECONDS\n")
+
+
 def drive_outputs(sim, n: int, parms, meshes):
     """Run every member to the end one accepted step at a time (``sim.step``
     advances each running member by exactly one step, so the members'
@@ -209,7 +274,8 @@ def drive_outputs(sim, n: int, parms, meshes):
     return snaps, wt
 
 
-def _write_member(prj: str, parm, mesh, snaps, wt, its, recs) -> None:
+def _write_member(prj: str, parm, mesh, snaps, wt, its, recs, phase_s=None,
+                  total_s=0.0) -> None:
     out = os.path.join(prj, "output")
     os.makedirs(out, exist_ok=True)
     write_psi(os.path.join(out, "psi"), [(k, t, p) for k, t, p, _ in snaps])
@@ -221,6 +287,8 @@ def _write_member(prj: str, parm, mesh, snaps, wt, its, recs) -> None:
         write_wtdepth(os.path.join(out, "wtdepth"), wt)
     write_grid3d(os.path.join(out, "grid3d"), mesh)
     write_xyz(os.path.join(out, "xyz"), mesh)
+    if phase_s is not None:
+        write_risul(os.path.join(out, "risul"), recs, its, phase_s, total_s)
 
 
 def mesh_gen3d(case) -> dict:
@@ -305,15 +373,26 @@ def run_ensemble(member_dirs: Sequence[str], precision: int = 1, device: int = 0
     out = []
     with Simulation(cases, precision=precision, device=device) as s:
         if write:
+            # the phase table of risul needs per-phase timing (kernel by
+            # kernel, CUDA events between the phases)
+            s.phase_timers(1)
+            t0 = time.perf_counter()
             meshes = [mesh_gen3d(c) for c in cases]
             snaps, wt = drive_outputs(_Stepper(s), len(cases), [c.parm for c in cases], meshes)
+            total = time.perf_counter() - t0
+            ph = [v / 1000.0 for v in s.phase_timers(0).values()]
+            # a batch shares the phase times: each member's share is its
+            # rows' share of the batch
+            rows = np.array([float(sz["n"]) for sz in s.sizes])
+            share = rows / rows.sum()
         else:
             s.run()
         for m, d in enumerate(member_dirs):
             res = s.state(m)
             its, recs = s.records(m)
             if write:
-                _write_member(d, cases[m].parm, meshes[m], snaps[m], wt[m], its, recs)
+                _write_member(d, cases[m].parm, meshes[m], snaps[m], wt[m], its, recs,
+                              [v * share[m] for v in ph], total * share[m])
             out.append(dict(dir=d, pnew=res[0], time=res[1], deltat=res[2],
                             status=int(res[3]), steps=len(recs)))
     return out

@@ -133,6 +133,33 @@ def test_sw_and_iter_files_from_oracle_records(tmp_path):
             assert a[k] == pytest.approx(b[k], rel=rt, abs=1e-300), k
 
 
+def test_risul_summary_from_oracle_records(tmp_path):
+    """The risul closing summary (cathy_main.f:3880-3950): step statistics
+    recomputed from the records, the phase table adding up to the
+    nonlinear-scheme total, and the cumulative relative MBE."""
+    import re
+    import oracle as O
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.pycathy import write_risul
+    case = config0(tmax=3600.0, precond=0)
+    o = O.Oracle(case)
+    for _ in range(12):
+        o.step()
+    recs, its = o.step_records(), o.iter_records()
+    phases = [0.5, 0.0, 1.25, 0.0, 0.0, 0.0, 3.0, 0.0, 0.25]
+    write_risul(str(tmp_path / "risul"), recs, its, phases, 6.0)
+    txt = open(str(tmp_path / "risul")).read()
+    num = lambda key: float(re.search(re.escape(key) + r"\s*=?\s*(-?[0-9.E+-]+)", txt).group(1))
+    assert num("TOTAL NUMBER OF TIME STEPS") == len(recs)
+    assert num("TOTAL NUMBER OF NONLINEAR ITERATIONS") == len(its)
+    assert num("TOTAL NUMBER OF LINEAR ITERATIONS") == sum(r["niter"] for r in its)
+    assert num("TOT CPU FOR NONLINEAR SCHEME") == pytest.approx(5.0)
+    assert num("TOT CPU FOR LINEAR SOLVER & RESIDUAL") == pytest.approx(3.0)
+    assert num("SMALLEST TIME STEP SIZE") == pytest.approx(min(r["deltat"] for r in recs), rel=1e-3)
+    rel = 100.0 * recs[-1]["cerras"] / (recs[-1]["cvin"] + recs[-1]["cvout"])
+    assert num("CUMULATIVE (TOTAL) RELATIVE MBE BASED ON CERRAS:") == pytest.approx(rel, rel=1e-4)
+
+
 def test_mesh_files_match_reference_grid3d(tmp_path):
     """grid3d and xyz from the host mesh builder against the reference's own
     grid3d of the weill example (parsed as pyCATHY's read_grid3d does)."""
