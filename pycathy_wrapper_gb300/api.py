@@ -84,10 +84,14 @@ class Simulation:
     and soil but share IOPT, LUMP and the preconditioner).  ``precision`` 0
     runs FP64 everywhere (the reference's arithmetic); 1 assembles and runs
     the Krylov iterations in FP32 inside an FP64 residual/refinement loop.
+    ``inner_tol`` is the FP32 Krylov solve's relative tolerance (the larger
+    of it and TOLCG is used): at 1e-8 the FP32 path takes the oracle's time
+    steps on every tested member; at 1e-6 some members drift to different
+    (equally converged) iterates and, over a day, a different step sequence.
     """
 
     def __init__(self, cases: Union[Case, Sequence[Case]], precision: int = 0,
-                 device: int = 0, inner_maxit: int = 200, inner_tol: float = 1e-6,
+                 device: int = 0, inner_maxit: int = 200, inner_tol: float = 1e-8,
                  graphs: bool = True):
         self.L = _lib.load()
         self.cases: List[Case] = [cases] if isinstance(cases, Case) else list(cases)
@@ -230,6 +234,20 @@ class Simulation:
         d["by_log2_rows"] = {b: (out[8 + 2 * b], out[9 + 2 * b]) for b in range(32)
                              if out[8 + 2 * b] > 0}
         return d
+
+    def autotune(self, nrep: int = 10):
+        """Time the assembly and stream-SpMV schedules on the running members
+        and keep the fastest (cached per GPU and size class; nrep <= 0 reuses
+        a cached choice).  Returns dict(asm_blocks, spmv_blocks, asm_ms,
+        spmv_ms)."""
+        sc = (C.c_int32 * 2)()
+        ms = (C.c_double * 2)()
+        check(self.L.cathy_gb300_autotune(self.h, int(nrep), sc, ms), "autotune")
+        return dict(asm_blocks=sc[0], spmv_blocks=sc[1], asm_ms=ms[0], spmv_ms=ms[1])
+
+    def set_schedule(self, asm_blocks: int, spmv_blocks: int):
+        check(self.L.cathy_gb300_set_schedule(self.h, int(asm_blocks), int(spmv_blocks)),
+              "set_schedule")
 
     PHASES = ("UNSAT CHARACTERISTICS", "INIT. OF SYSTEM MATRICES", "LOCAL SYSTEM ASSEMBLY",
               "RHS CALCULATION W/O BC'S", "GLOBAL LHS SYSTEM MATRIX", "BC CONTRIBUTIONS TO RHS",

@@ -140,6 +140,16 @@ int32_t cathy_gb300_profile(void* h, int32_t enable, double* spmv_ms,
   return engine_profile((Engine*)h, enable, spmv_ms, spmv_launches, spmv_bytes);
 }
 
+int32_t cathy_gb300_autotune(void* h, int32_t nrep, int32_t* sched, double* ms) {
+  if (!h || !sched || !ms) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_autotune((Engine*)h, nrep, sched, ms); });
+}
+
+int32_t cathy_gb300_set_schedule(void* h, int32_t asm_blocks, int32_t spmv_blocks) {
+  if (!h) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_set_schedule((Engine*)h, asm_blocks, spmv_blocks); });
+}
+
 int32_t cathy_gb300_phase_timers(void* h, int32_t enable, double* out, int32_t n) {
   if (!h || (n > 0 && !out) || n < 0) return CATHY_GB300_EINVAL;
   return guarded([&]() { return engine_phase_timers((Engine*)h, enable, out, n); });

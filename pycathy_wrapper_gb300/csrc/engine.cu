@@ -31,6 +31,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 #include <type_traits>
@@ -906,8 +907,7 @@ enum { kSpmvPlain = 0, kSpmvUpd = 1, kSpmvResid = 2 };
 constexpr int kStreamWarps = 8;
 // FP32 y = A x as a stream over the map entries that virtual block vbid of
 // vgrid takes (see k_spmv_stream).  s_bytes: a zeroed shared slot for the
-// byte count (used only with alg_bytes).  Arrays written by other phases of
-// the fused Picard iteration carry no __restrict__.
+// byte count (used only with alg_bytes).
 template <int kMode>
 __device__ __forceinline__ void spmv_stream_run(
     int vbid, int vgrid, int nblk, const int32_t* bm_mem, const int32_t* bm_r0,
@@ -1271,8 +1271,6 @@ __global__ void k_line_setup(const int32_t* bm_mem, const int32_t* bm_r0,
 
 // z = T^-1 r per column; accumulates w.z (w = q for the PCG beta) per
 // member.  The forward sweep keeps y in z, the backward sweep overwrites it.
-// (No __restrict__ here: in the fused Picard iteration other phases of the
-// same launch write these arrays.)
 template <class VT>
 __device__ __forceinline__ void k_line_apply_b(int bid_, const int32_t* bm_mem, const int32_t* bm_r0,
                              const int32_t* bm_r1, const uint8_t* active,
@@ -2271,9 +2269,7 @@ __global__ void k_vps(int n, const int32_t* inc_ptr, const int32_t* inc,
 // added by the row's first lane.
 //
 // The device function is one 16-row map entry bid (block-uniform early
-// exits, no block barrier); arrays that other phases of the fused Picard
-// iteration write (IFATM, ATMACT, ATMOLD, the nodal fields) carry no
-// __restrict__ so that they are never read through the non-coherent path.
+// exits, no block barrier).
 struct AsmInc {  // one incidence's contribution to its row
   float dacc, rp, msum;
 };
@@ -2313,28 +2309,44 @@ __device__ __forceinline__ void assemble_f32_entry(
     const float* vps, const uint8_t* dmask, const NodalF& nf, const int32_t* loc,
     const int8_t* ifatm, const double* atmact, const double* atmold, float* vals, float lm_d,
     float lm_o, const int64_t* glrow, const uint8_t* gloff, const uint8_t* gl) {
-  const int m = bm_mem[bid];
-  if (!(act[m] & ACT_ITER)) return;
   __shared__ float sval[kRowsPerBlock16][64 * 4];
   __shared__ float2 sh2[kRowsPerBlock16][kGroup];
   __shared__ float2 sk2[kRowsPerBlock16][kGroup];
   __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
+  // The loads are issued in four dependent rounds: the map entry; the row's
+  // pointers and nodal inputs together with the member's flag; the row's
+  // columns, gather offsets and incidence records; the columns' nodal
+  // values and the slots' gather lists.
+  const int m = bm_mem[bid];
+  const int rbeg = bm_r0[bid], rend = bm_r1[bid];
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
-  const int i = bm_r0[bid] + grp;
-  const bool rowok = i < bm_r1[bid];
+  const int i = rbeg + grp;
+  const bool rowok = i < rend;
+  const uint8_t am = act[m];
   const MemberScal& S = ms[m];
   const float rdt = (float)S.deltat_r, th = (float)S.tetaf;
-  int s0 = 0, rlen = 0, p0 = 0, p1 = 0, col = -1;
-  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f;
+  int s0 = 0, s1 = 0, p0 = 0, p1 = 0;
+  int64_t gbase = 0, gend = 0;
+  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f;
   if (rowok) {
     s0 = rowptr[i];
-    rlen = rowptr[i + 1] - s0;
+    s1 = rowptr[i + 1];
     p0 = inc_ptr[i];
     p1 = inc_ptr[i + 1];
+    gbase = glrow[i];
+    gend = glrow[i + 1];
     et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
-    if (lane < rlen) col = cols[s0 + lane];
+    vpl = vps[i] * lm_d;  // sum over the row's elements of |V| porosity LM_kk
   }
-  // the first two rounds of incidence records, in flight with the staging
+  if (!(am & ACT_ITER)) return;  // block-uniform
+  const int rlen = s1 - s0;
+  int col = -1, ga = 0, gb = 0;
+  if (rowok && lane < rlen) {
+    col = cols[s0 + lane];
+    ga = gloff[s0 + lane];
+    gb = (lane + 1 < rlen) ? (int)gloff[s0 + lane + 1] : (int)(gend - gbase);
+  }
+  // the first two rounds of incidence records
   float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
   int i0 = -1, i1 = -1;
   float v0 = 0.0f, v1 = 0.0f;
@@ -2348,6 +2360,12 @@ __device__ __forceinline__ void assemble_f32_entry(
     i1 = islot[p0 + kGroup + lane];
     if (lm_o != 0.0f) v1 = vpi[p0 + kGroup + lane];
   }
+  // the slot's gather list (its first eight entries in registers)
+  constexpr int kPre = 8;
+  uint8_t gq[kPre];
+  const bool offd = col >= 0 && col != i;
+#pragma unroll
+  for (int u = 0; u < kPre; ++u) gq[u] = (offd && ga + u < gb) ? gl[gbase + ga + u] : 0;
   if (col >= 0) {
     sh2[grp][lane] = nf.h2[col];
     sk2[grp][lane] = nf.ckr2[col];
@@ -2377,20 +2395,18 @@ __device__ __forceinline__ void assemble_f32_entry(
   float rhs = group_sum<float>(a.rp);
   const float msum = group_sum<float>(a.msum);
   if (!rowok) return;
-  const float vpl = vps[i] * lm_d;  // sum over the row's elements of |V| porosity LM_kk
-  if (lane < rlen) {
-    const int sl = s0 + lane;
+  if (col >= 0) {
     float lhs;
     if (col == i) {
       lhs = dsum + vpl * et2i * rdt;
     } else {
-      const int64_t base = glrow[i];
-      const int ga = gloff[sl];
-      const int gb = (lane + 1 < rlen) ? (int)gloff[sl + 1] : (int)(glrow[i + 1] - base);
       lhs = 0.0f;
-      for (int u = ga; u < gb; ++u) lhs += sval[grp][gl[base + u]];
+#pragma unroll
+      for (int u = 0; u < kPre; ++u)
+        if (ga + u < gb) lhs += sval[grp][gq[u]];
+      for (int u = ga + kPre; u < gb; ++u) lhs += sval[grp][gl[gbase + u]];
     }
-    vals[sl] = lhs;
+    vals[s0 + lane] = lhs;
   }
   if (lane == 0) {
     rhs -= (msum * nf.dpsi[i] + vpl * nf.dsw[i]) * rdt;
@@ -2405,9 +2421,10 @@ __device__ __forceinline__ void assemble_f32_entry(
   }
 }
 
-// 6 resident blocks per SM (40 registers; 8 B of spill): measured faster on
-// the full batch than the 5 blocks that 48 registers allow
-__global__ void __launch_bounds__(kThreads, 6)
+// kMinBlocks: resident blocks per SM the compiler must fit (registers); the
+// autotuner picks the variant (the arithmetic is the same in all of them).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
 k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
                       const uint8_t* act, const MemberScal* ms,
                       const int32_t* rowptr, const int32_t* cols, const int32_t* inc_ptr,
@@ -2423,8 +2440,12 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
                      islot, vpi, vps, dmask, nf, loc, ifatm, atmact, atmold, vals, lm_d, lm_o,
                      glrow, gloff, gl);
 }
-
-
+using AsmKernel = decltype(&k_assemble_picard_f32<6>);
+constexpr int kAsmVariants = 4;
+constexpr int kAsmBlocks[kAsmVariants] = {4, 5, 6, 8};
+static const AsmKernel kAsmKernel[kAsmVariants] = {
+    &k_assemble_picard_f32<4>, &k_assemble_picard_f32<5>, &k_assemble_picard_f32<6>,
+    &k_assemble_picard_f32<8>};
 
 // Post-solve pass of the FP32 Picard iteration, one thread per row:
 // PNEW += PDIFF + SHLPIC; at Dirichlet rows the back-calculated flux (BKPIC:
@@ -3107,6 +3128,12 @@ struct Engine {
   int lt_cap = 1 << 16;
   int64_t lt_pending = 0;     // launches written since the last flush
   int persist_blocks = 1216;  // grid of the persistent kernels (8 per SM)
+  // schedules chosen by the autotuner (engine_autotune): the assembly
+  // variant (resident blocks per SM kAsmBlocks[asm_variant]) and the stream
+  // SpMV's resident blocks per SM (its grid = stream_per_sm * SMs)
+  int asm_variant = 2;
+  int stream_per_sm = 8;
+  int nsm = 152;
   // Phase timers in the reference's CPUVEC buckets (picard.f:66-202, the
   // risul summary at cathy_main.f:3913-3950) with NVTX ranges of the same
   // names.  When enabled, macro-iterations run kernel by kernel (the same
@@ -3180,7 +3207,7 @@ struct Engine {
   int grid_stream() const {
     // one warp per map entry up to one resident wave of 256-thread blocks
     return std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps,
-                                persist_blocks));
+                                stream_per_sm * nsm));
   }
   // q = A p with the fused dots p.q, p.r (FP32 stream kernel)
   void spmv_f32(const float* vals, const float* p, float* q, const float* r) {
@@ -3875,6 +3902,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     CG_TRY(cudaGetDevice(&dev));
     CG_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     persist_blocks = std::max(1, nsm) * 8;
+    this->nsm = std::max(1, nsm);
   }
   d_nact_dummy.alloc(1);
   d_prof_bytes.alloc(1);
@@ -4495,7 +4523,7 @@ void Engine::iteration_pre(int solve_phase) {
     // ASSPIC + RHSPIC + CFMATP + BC contributions fused: the CPUVEC buckets
     // of system initialisation, assembly, RHS, LHS and BC in one kernel
     phase(2);
-    launch(k_assemble_picard_f32, cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+    launch(kAsmKernel[asm_variant], cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
            d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, (const float4*)d_rec16.p,
            (const uint16_t*)d_islot.p, (const float*)d_vpi.p, (const float*)d_vps.p, d_dmask.p, nf,
            nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact, (const double*)nd.atmold,
@@ -5094,7 +5122,7 @@ Engine* engine_create(int nmembers, const cathy_member_t* members,
   Engine* e = new Engine();
   e->opts = opts;
   if (e->opts.inner_maxit <= 0) e->opts.inner_maxit = 200;
-  if (e->opts.inner_tol <= 0) e->opts.inner_tol = 1e-5;
+  if (e->opts.inner_tol <= 0) e->opts.inner_tol = 1e-8;
   try {
     e->build(nmembers, members);
     // the first time level: ATMNXT at TIME (cathy_main.f:2938) for every member
@@ -5304,7 +5332,7 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   if (mixed) {
     k_vg_f32<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p,
                                                   e->d_ms.p, e->nd, e->nf, e->d_nodal[ND_Z].p);
-    k_assemble_picard_f32<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
+    kAsmKernel[e->asm_variant]<<<e->bm16.nblk, kThreads, 0, e->st>>>(e->bm16.mem.p, e->bm16.r0.p, e->bm16.r1.p,
         e->d_act.p, e->d_ms.p, e->d_rowptr.p, e->d_cols.p, e->d_inc_ptr.p, e->d_rec16.p,
         e->d_islot.p, e->d_vpi.p, e->d_vps.p, e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm,
         e->nd.atmact, e->nd.atmold,
@@ -5424,7 +5452,7 @@ int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t
   }
   if (r == 0 || nrep < 1) return CATHY_GB300_EINVAL;
   auto go = [&]() {
-    k_assemble_picard_f32<<<e->cbm16.nblk, kThreads, 0, e->st>>>(
+    kAsmKernel[e->asm_variant]<<<e->cbm16.nblk, kThreads, 0, e->st>>>(
         e->cbm16.mem.p, e->cbm16.r0.p, e->cbm16.r1.p, e->d_act.p, e->d_ms.p, e->d_rowptr.p,
         e->d_cols.p, e->d_inc_ptr.p, e->d_rec16.p, e->d_islot.p, e->d_vpi.p, e->d_vps.p,
         e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold, e->d_vals32.p,
@@ -5441,6 +5469,125 @@ int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t
   *ms = t / nrep;
   *bytes = b;
   *rows = r;
+  return 0;
+}
+
+// ---- schedule autotuner ----------------------------------------------------
+// Per (GPU, size class) cache of the schedules chosen by engine_autotune.
+static std::mutex g_tune_mu;
+static std::map<std::string, std::pair<int, int>> g_tune_cache;
+
+static std::string tune_key(Engine* e, int64_t rows) {
+  cudaDeviceProp prop;
+  CG_TRY(cudaGetDeviceProperties(&prop, e->opts.device));
+  int cls = 0;
+  while (cls < 62 && (rows >> (cls + 1)) > 0) ++cls;
+  return std::string(prop.name) + "/" + std::to_string(prop.multiProcessorCount) + "/rows2^" +
+         std::to_string(cls);
+}
+
+// Flags every running member as iterating (and in the Krylov solve) and
+// compacts the maps over them; returns the rows.
+static int64_t flag_running(Engine* e) {
+  std::vector<uint8_t> act(e->nmem, 0), on(e->nmem, 0);
+  int64_t rows = 0;
+  for (int m = 0; m < e->nmem; ++m)
+    if (e->M[m]->status == 0) {
+      act[m] = ACT_ITER;
+      on[m] = 1;
+      rows += e->M[m]->meshp->n;
+    }
+  e->h_act = act;
+  e->d_act.upload(act.data(), e->nmem, e->st);
+  e->d_active.upload(on.data(), e->nmem, e->st);
+  e->compact_maps(on);
+  return rows;
+}
+
+// The autotuner of the FP32 Picard path.  On the handle's current state
+// (every running member, so call it once the members have run a few steps)
+// it times each assembly variant (resident blocks per SM 4, 5, 6, 8) and
+// the stream SpMV at 4, 6 and 8 resident blocks per SM (nrep launches each
+// between CUDA events, after one untimed launch) and keeps the fastest of
+// each.  The choice is cached per (GPU, rows size class): nrep <= 0 takes
+// the cached schedule when there is one.  The launches rebuild the matrix
+// from the current nodal fields and multiply Krylov work vectors; the next
+// Picard iteration overwrites both.  Assembly variants give bit-identical
+// systems; the SpMV grid only regroups the FP32 dot products.
+int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
+  if (!(e->precision == 1 && e->iopt == 1 && e->precond == 2)) return CATHY_GB300_EUNSUP;
+  const int64_t rows = flag_running(e);
+  if (rows == 0) return CATHY_GB300_EINVAL;
+  const std::string key = tune_key(e, rows);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (nrep <= 0 && it != g_tune_cache.end()) {
+      e->asm_variant = it->second.first;
+      e->stream_per_sm = it->second.second;
+      e->graph_free();
+      sched[0] = kAsmBlocks[e->asm_variant];
+      sched[1] = e->stream_per_sm;
+      ms[0] = ms[1] = 0.0;
+      return 0;
+    }
+  }
+  if (nrep <= 0) nrep = 10;
+  auto timed = [&](auto&& go) {
+    go();
+    CG_TRY(cudaEventRecord(e->ev0, e->st));
+    for (int k = 0; k < nrep; ++k) go();
+    CG_TRY(cudaEventRecord(e->ev1, e->st));
+    CG_TRY(cudaEventSynchronize(e->ev1));
+    CG_TRY(cudaPeekAtLastError());
+    float t = 0.0f;
+    CG_TRY(cudaEventElapsedTime(&t, e->ev0, e->ev1));
+    return (double)t / nrep;
+  };
+  double best_a = 1e300, best_s = 1e300;
+  int va = e->asm_variant, vs = e->stream_per_sm;
+  for (int v = 0; v < kAsmVariants; ++v) {
+    const double t = timed([&]() {
+      kAsmKernel[v]<<<e->cbm16.nblk, kThreads, 0, e->st>>>(
+          e->cbm16.mem.p, e->cbm16.r0.p, e->cbm16.r1.p, e->d_act.p, e->d_ms.p, e->d_rowptr.p,
+          e->d_cols.p, e->d_inc_ptr.p, e->d_rec16.p, e->d_islot.p, e->d_vpi.p, e->d_vps.p,
+          e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold,
+          e->d_vals32.p, (float)e->lm_d, (float)e->lm_o, e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
+    });
+    if (t < best_a) { best_a = t; va = v; }
+  }
+  const bool was_prof = e->prof;
+  e->prof = false;
+  for (int per : {4, 6, 8}) {
+    e->stream_per_sm = per;
+    const double t = timed([&]() { e->spmv_f32(e->d_vals32.p, e->w32[3].p, e->w32[4].p, e->w32[2].p); });
+    if (t < best_s) { best_s = t; vs = per; }
+  }
+  e->prof = was_prof;
+  e->asm_variant = va;
+  e->stream_per_sm = vs;
+  e->graph_free();
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = {va, vs};
+  }
+  sched[0] = kAsmBlocks[va];
+  sched[1] = vs;
+  ms[0] = best_a;
+  ms[1] = best_s;
+  return 0;
+}
+
+// Forces a schedule (assembly resident blocks per SM: 4, 5, 6 or 8; stream
+// SpMV resident blocks per SM: 1..8).
+int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm) {
+  int v = -1;
+  for (int k = 0; k < kAsmVariants; ++k)
+    if (kAsmBlocks[k] == asm_blocks) v = k;
+  if (v < 0 || spmv_per_sm < 1 || spmv_per_sm > 8) return CATHY_GB300_EINVAL;
+  e->asm_variant = v;
+  e->stream_per_sm = spmv_per_sm;
+  e->graph_free();
   return 0;
 }
 

@@ -4,11 +4,12 @@ The bench runs the 256-member ensemble (seeds 1000+m) for one simulated day
 on the FP32 batched path: FP32 assembly and column-line-preconditioned FP32
 PCG inside the FP64 residual loop, one CUDA graph per Picard iteration.
 These tests run that exact path (``Simulation(cases, precision=1,
-graphs=True)``, ``precond=2``) on real ensemble draws -- the four smallest
-members (1007, 1046, 1153, 1223) and two members that fail within the day
-(1115, 1036: DTMIN reached without Picard convergence) -- for the full day,
+graphs=True)``, ``precond=2``) on real ensemble draws -- four members that finish (1007, 1046, 1053,
+1123) and two that fail within the day (1115, 1036: DTMIN reached without
+Picard convergence) -- for the full day,
 batched together, and compare every member with the CPU oracle running the
-reference's method (FP64, IC(0)-PCG) on the same inputs.  A config-1-style
+reference's method (FP64, IC(0)-PCG) on the same inputs, with the default
+FP32 inner tolerance (1e-8).  A config-1-style
 member (40x40 fractal DEM, 15 layers, per-cell lognormal Ks) is checked for
 the 6-hour rain pulse the same way.  The FP64 path (``precision=0``, IC(0))
 is checked iterate for iterate on two of the members.

@@ -417,4 +417,4 @@ def test_run_ensemble_on_project_folders_matches_api(tmp_path):
         wt = np.loadtxt(os.path.join(dirs[m], "output", "wtdepth"), ndmin=2)
         assert wt.shape[0] == nsteps[m] and wt[-1, 0] == pytest.approx(1800.0)
         assert sorted(os.listdir(os.path.join(dirs[m], "output"))) == [
-            "grid3d", "iter", "mbeconv", "psi", "sw", "wtdepth", "xyz"]
+            "grid3d", "iter", "mbeconv", "psi", "risul", "sw", "wtdepth", "xyz"]
