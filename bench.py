@@ -16,6 +16,11 @@ the whole ensemble day from the initial condition.
             (set_state), runs, and reads every member's final heads back.
   plain_gpu the reference's method on the GPU (FP64, IC(0)-PCG), one member
             at a time, over a sample of members.
+  learned_preconditioner  the learned column-line factor on the CPU
+            sample's members and window (train pass, then solve pass with
+            plain fallback) beside the same launch-by-launch path without it.
+  schedule  the autotuner's choice (assembly resident blocks per SM, SpMV
+            blocks per SM), timed on the warmed-up ensemble.
   roofline  the SpMV kernel (dominant Krylov kernel): algorithmic bytes of
             every launch in the timed region / the launches' durations, each
             taken on the device clock from its first block's start to its
@@ -134,6 +139,45 @@ def gpu_sample(nmem, tmax, device, graphs):
         dev = (s.stats()["gpu_ms"] - a) / 1000.0
         sim = sum(s.state(m)[1] for m in range(s.nmembers))
     return sim / dev, dev, sim
+
+
+def learned_sample(nmem, tmax, device):
+    """The learned column-line preconditioner on the bounded sample, against
+    the same launch-by-launch path without it: one pass in training mode
+    (mode 1: the network learns from the plain solver's Krylov pairs; heads
+    are the plain ones), then a pass that solves with the trained factor
+    (mode 2, plain factor as fallback).  Device-timed; returns both
+    throughputs and the mean PCG iterations per solve."""
+    from pycathy_wrapper_gb300.api import Simulation
+    from pycathy_wrapper_gb300.learned import LearnedPreconditioner, init_params
+    cases = _sample_cases(nmem, tmax, precond=2)
+
+    def one(lp, mode):
+        with Simulation(cases, precision=1, device=device, graphs=False) as s:
+            if lp is not None:
+                s.attach_learned(lp, mode=mode)
+            a = s.stats()
+            s.run()
+            b = s.stats()
+            dev = (b["gpu_ms"] - a["gpu_ms"]) / 1000.0
+            sim = sum(s.state(m)[1] for m in range(s.nmembers))
+            lin = b["lin_iters"] - a["lin_iters"]
+            nl = b["nl_iters"] - a["nl_iters"]
+            st = s.learned_stats() if lp is not None else None
+        return dict(value=sim / dev, device_s=dev, lin_per_nl=lin / max(nl, 1)), st
+
+    plain, _ = one(None, 0)
+    with LearnedPreconditioner(init_params(0), device=device, lr=1e-3) as lp:
+        train, tst = one(lp, 1)
+        use, ust = one(lp, 2)
+    return {"unit": UNIT, "sample": "the CPU sample's members and window, launch by launch",
+            "plain": plain, "training_pass": dict(train, train_steps=tst["train_steps"],
+                                                  last_loss=tst["last_loss"]),
+            "learned": dict(use, learned_solves=ust["learned_solves"],
+                            plain_solves=ust["plain_solves"],
+                            learned_iters_per_solve=ust["learned_iters"] / max(ust["learned_solves"], 1),
+                            plain_iters_per_solve=ust["plain_iters"] / max(ust["plain_solves"], 1)),
+            "learned_over_plain": use["value"] / plain["value"]}
 
 
 # ---------------------------------------------------------------------------
@@ -287,6 +331,7 @@ def main():
     ap.add_argument("--no-graphs", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -325,8 +370,15 @@ def main():
         sim.reset()
         sim.run(args.warmup_member_steps)
     # the assembly (the dominant kernel of the full-batch iterations) on the
-    # whole ensemble as it stands after the warm-up: mean of 20 launches
-    # between CUDA events, inputs far larger than L2 (no flush needed)
+    # whole ensemble: mean of 20 launches between CUDA events, inputs far
+    # larger than L2 (no flush needed)
+    # the schedule: resident blocks per SM of the assembly, stream-SpMV grid
+    # (project autotuner, cached per GPU), then the assembly's own timing:
+    # both on every member after its first 5 accepted steps (all members
+    # still running)
+    sim.reset()
+    sim.run(5)
+    sched = sim.autotune(10)
     asm_ms, asm_bytes, asm_rows = sim.time_assembly(20)
 
     def reached():
@@ -404,6 +456,9 @@ def main():
                 tot_s += s1.state(0)[1]
         plain = {"value": tot_s / tot_t, "unit": UNIT,
                  "sample": f"members {pick} one at a time, FP64 IC(0)-PCG, 1 simulated day"}
+    learned = None
+    if rank == 0 and not args.no_learned:
+        learned = learned_sample(args.members, args.cpu_tmax, dev_id)
     if rank != 0:
         return
     peak, peak_kind = _peaks()
@@ -426,7 +481,8 @@ def main():
                    "cuda_graphs": not args.no_graphs,
                    "preconditioner": "column-line (vertical tridiagonal) block Jacobi",
                    "l2": "inputs larger than L2 (ensemble matrix > 1.5 GB)",
-                   "parallelism": f"members sharded per rank x{ws}"},
+                   "parallelism": f"members sharded per rank x{ws}",
+                   "schedule": sched},
         "e2e": e2e,
         "gpu_launches": launches,
         "nl_iterations": nl, "lin_iterations": lin,
@@ -450,6 +506,7 @@ def main():
         "same_sample_gpu_vs_cpu": like,
         "plain_gpu": plain,
         "speedup_vs_plain_gpu": (value / plain["value"]) if plain else None,
+        "learned_preconditioner": learned,
         "clocks": ck,
     }
     print(json.dumps(line), flush=True)

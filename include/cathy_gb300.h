@@ -197,7 +197,7 @@ int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
  * its FP32 dot products.  CATHY_GB300_EUNSUP outside the FP32 Picard path
  * with the column-line preconditioner. */
 int32_t cathy_gb300_autotune(void* handle, int32_t nrep, int32_t* sched, double* ms);
-/* Forces a schedule: assembly blocks/SM in {4, 5, 6, 8}, SpMV blocks/SM in
+/* Forces a schedule: assembly blocks/SM in {5, 6, 7, 8}, SpMV blocks/SM in
  * 1..8 (defaults 6 and 8). */
 int32_t cathy_gb300_set_schedule(void* handle, int32_t asm_blocks, int32_t spmv_blocks);
 /* Phase timers of the nonlinear iterations in the nine buckets of the

@@ -79,13 +79,18 @@ __device__ __forceinline__ double warp_max(double v) {
 }
 
 // Block-level sum of NV values, one atomicAdd per value into acc[0..NV).
+// FP64 adds run at a small fraction of the FP32 rate on this GPU, so a warp
+// whose values are all zero (most warps for boundary-flux sums) skips its
+// shuffle tree: the sums are the same (a zero partial changes no nonzero
+// sum, and zero sums are not added).
 template <int NV>
 __device__ __forceinline__ void block_accumulate(double (&v)[NV], double* acc) {
   __shared__ double sh[NV][kThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
-    double s = warp_sum(v[i]);
+    double s = 0.0;
+    if (__ballot_sync(0xffffffffu, v[i] != 0.0)) s = warp_sum(v[i]);  // warp-uniform
     if (lane == 0) sh[i][w] = s;
   }
   __syncthreads();
@@ -93,8 +98,10 @@ __device__ __forceinline__ void block_accumulate(double (&v)[NV], double* acc) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
       double s = (lane < (int)(blockDim.x >> 5)) ? sh[i][lane] : 0.0;
-      s = warp_sum(s);
-      if (lane == 0 && s != 0.0) atomicAdd(acc + i, s);
+      if (__ballot_sync(0xffffffffu, s != 0.0)) {
+        s = warp_sum(s);
+        if (lane == 0 && s != 0.0) atomicAdd(acc + i, s);
+      }
     }
   }
 }
@@ -2270,6 +2277,7 @@ __global__ void k_vps(int n, const int32_t* inc_ptr, const int32_t* inc,
 //
 // The device function is one 16-row map entry bid (block-uniform early
 // exits, no block barrier).
+constexpr int kGlWords = 3 * 64 / 4;  // gather-list words of a row (<= 64 incidences)
 struct AsmInc {  // one incidence's contribution to its row
   float dacc, rp, msum;
 };
@@ -2313,10 +2321,12 @@ __device__ __forceinline__ void assemble_f32_entry(
   __shared__ float2 sh2[kRowsPerBlock16][kGroup];
   __shared__ float2 sk2[kRowsPerBlock16][kGroup];
   __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
+  __shared__ uint32_t sgl[kRowsPerBlock16][kGlWords];  // the row's gather list
   // The loads are issued in four dependent rounds: the map entry; the row's
-  // pointers and nodal inputs together with the member's flag; the row's
-  // columns, gather offsets and incidence records; the columns' nodal
-  // values and the slots' gather lists.
+  // pointers and every per-row input (nodal values, boundary data) with the
+  // member's flag; the row's columns, gather offsets, incidence records and
+  // its whole gather list (4-byte aligned per row, loaded as words); the
+  // columns' nodal values.
   const int m = bm_mem[bid];
   const int rbeg = bm_r0[bid], rend = bm_r1[bid];
   const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
@@ -2326,46 +2336,48 @@ __device__ __forceinline__ void assemble_f32_entry(
   const MemberScal& S = ms[m];
   const float rdt = (float)S.deltat_r, th = (float)S.tetaf;
   int s0 = 0, s1 = 0, p0 = 0, p1 = 0;
-  int64_t gbase = 0, gend = 0;
-  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f;
+  int64_t gbase = 0;
+  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f;
+  bool atm_i = false, dm_i = false;
   if (rowok) {
     s0 = rowptr[i];
     s1 = rowptr[i + 1];
     p0 = inc_ptr[i];
     p1 = inc_ptr[i + 1];
     gbase = glrow[i];
-    gend = glrow[i + 1];
     et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
     vpl = vps[i] * lm_d;  // sum over the row's elements of |V| porosity LM_kk
+    dp_i = nf.dpsi[i]; ds_i = nf.dsw[i]; qn_i = nf.qneu[i];
+    atm_i = loc[i] < S.nnod && ifatm[i] == 0;  // atmospheric Neumann surface node
+    dm_i = dmask[i] != 0;
   }
   if (!(am & ACT_ITER)) return;  // block-uniform
-  const int rlen = s1 - s0;
+  const int rlen = s1 - s0, ninc = p1 - p0;
+  const int nglw = (3 * ninc + 3) / 4;  // gather-list words: 3 entries per incidence
   int col = -1, ga = 0, gb = 0;
   if (rowok && lane < rlen) {
     col = cols[s0 + lane];
     ga = gloff[s0 + lane];
-    gb = (lane + 1 < rlen) ? (int)gloff[s0 + lane + 1] : (int)(gend - gbase);
+    gb = (lane + 1 < rlen) ? (int)gloff[s0 + lane + 1] : 3 * ninc;
   }
   // the first two rounds of incidence records
   float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
   int i0 = -1, i1 = -1;
   float v0 = 0.0f, v1 = 0.0f;
-  if (rowok && p0 + lane < p1) {
+  if (rowok && lane < ninc) {
     r0 = rec16[p0 + lane];
     i0 = islot[p0 + lane];
     if (lm_o != 0.0f) v0 = vpi[p0 + lane];
   }
-  if (rowok && p0 + kGroup + lane < p1) {
+  if (rowok && kGroup + lane < ninc) {
     r1 = rec16[p0 + kGroup + lane];
     i1 = islot[p0 + kGroup + lane];
     if (lm_o != 0.0f) v1 = vpi[p0 + kGroup + lane];
   }
-  // the slot's gather list (its first eight entries in registers)
-  constexpr int kPre = 8;
-  uint8_t gq[kPre];
-  const bool offd = col >= 0 && col != i;
-#pragma unroll
-  for (int u = 0; u < kPre; ++u) gq[u] = (offd && ga + u < gb) ? gl[gbase + ga + u] : 0;
+  const uint32_t* glw = reinterpret_cast<const uint32_t*>(gl + gbase);
+  uint32_t w0 = 0, w1 = 0;
+  if (rowok && lane < nglw) w0 = glw[lane];
+  if (rowok && kGroup + lane < nglw) w1 = glw[kGroup + lane];
   if (col >= 0) {
     sh2[grp][lane] = nf.h2[col];
     sk2[grp][lane] = nf.ckr2[col];
@@ -2374,8 +2386,11 @@ __device__ __forceinline__ void assemble_f32_entry(
       sds[grp][lane] = nf.dsw[col];
     }
   }
+  sgl[grp][lane] = w0;
+  sgl[grp][kGroup + lane] = w1;
+  for (int w = 2 * kGroup + lane; rowok && w < nglw; w += kGroup) sgl[grp][w] = glw[w];
   __syncwarp();
-  int ntrip = (p1 - p0 + kGroup - 1) / kGroup;
+  int ntrip = (ninc + kGroup - 1) / kGroup;
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
   AsmInc a{0.0f, 0.0f, 0.0f};
   if (i0 >= 0)
@@ -2386,7 +2401,7 @@ __device__ __forceinline__ void assemble_f32_entry(
                   sdp, sds, a);
   for (int trip = 2; trip < ntrip; ++trip) {  // nodes with more than 32 incident elements
     const int q = trip * kGroup + lane;
-    if (rowok && p0 + q < p1)
+    if (rowok && q < ninc)
       asm_incidence(q, rec16[p0 + q], islot[p0 + q], lm_o != 0.0f ? vpi[p0 + q] : 0.0f, grp, th,
                     rdt, lm_d, lm_o, hh_i, hl_i, sval, sh2, sk2, sdp, sds, a);
   }
@@ -2401,23 +2416,21 @@ __device__ __forceinline__ void assemble_f32_entry(
       lhs = dsum + vpl * et2i * rdt;
     } else {
       lhs = 0.0f;
-#pragma unroll
-      for (int u = 0; u < kPre; ++u)
-        if (ga + u < gb) lhs += sval[grp][gq[u]];
-      for (int u = ga + kPre; u < gb; ++u) lhs += sval[grp][gl[gbase + u]];
+      const uint8_t* g8 = reinterpret_cast<const uint8_t*>(sgl[grp]);
+      for (int u = ga; u < gb; ++u) lhs += sval[grp][g8[u]];
     }
     vals[s0 + lane] = lhs;
   }
   if (lane == 0) {
-    rhs -= (msum * nf.dpsi[i] + vpl * nf.dsw[i]) * rdt;
+    rhs -= (msum * dp_i + vpl * ds_i) * rdt;
     nf.xt5[i] = rhs;
-    float f = nf.qneu[i];
-    if (loc[i] < S.nnod && ifatm[i] == 0) {
+    float f = qn_i;
+    if (atm_i) {
       const double thd = S.tetaf;
       f += (thd == 1.0) ? (float)atmact[i]
                         : (float)(thd * atmact[i] + (1.0 - thd) * atmold[i]);
     }
-    nf.rhs[i] = dmask[i] ? 0.0f : rhs + f;
+    nf.rhs[i] = dm_i ? 0.0f : rhs + f;
   }
 }
 
@@ -2442,9 +2455,9 @@ k_assemble_picard_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
 }
 using AsmKernel = decltype(&k_assemble_picard_f32<6>);
 constexpr int kAsmVariants = 4;
-constexpr int kAsmBlocks[kAsmVariants] = {4, 5, 6, 8};
+constexpr int kAsmBlocks[kAsmVariants] = {5, 6, 7, 8};
 static const AsmKernel kAsmKernel[kAsmVariants] = {
-    &k_assemble_picard_f32<4>, &k_assemble_picard_f32<5>, &k_assemble_picard_f32<6>,
+    &k_assemble_picard_f32<5>, &k_assemble_picard_f32<6>, &k_assemble_picard_f32<7>,
     &k_assemble_picard_f32<8>};
 
 // Post-solve pass of the FP32 Picard iteration, one thread per row:
@@ -3131,7 +3144,7 @@ struct Engine {
   // schedules chosen by the autotuner (engine_autotune): the assembly
   // variant (resident blocks per SM kAsmBlocks[asm_variant]) and the stream
   // SpMV's resident blocks per SM (its grid = stream_per_sm * SMs)
-  int asm_variant = 2;
+  int asm_variant = 1;
   int stream_per_sm = 8;
   int nsm = 152;
   // Phase timers in the reference's CPUVEC buckets (picard.f:66-202, the
@@ -3540,7 +3553,9 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     // FP32 assembly gather lists: for every off-diagonal slot (i, j), the
     // positions q*4 + l of the contributions of row i's incidences q (local
     // node l of the element is j), in incidence order.  Per row: base offset
-    // (int32); per slot: start relative to the row base (uint8).
+    // (int64, a multiple of 4: the kernel loads a row's list as words; a row
+    // holds 3 entries per incidence); per slot: start relative to the row
+    // base (uint8).
     if (precision == 1 && iopt == 1) {
       uint8_t lst[kGroup][3 * 64];
       int cnt[kGroup];
@@ -3566,6 +3581,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
           }
           h_islot[(size_t)h_incptr[no + i] + q] = packed;
         }
+        while (h_gl.size() & 3) h_gl.push_back(0);  // rows start on a 4-byte boundary
         h_glrow[no + i] = (int64_t)h_gl.size();
         int off = 0;
         for (int sj = 0; sj < rl; ++sj) {
@@ -3708,7 +3724,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   if (glists) {
     d_glrow.alloc(N + 1); d_glrow.upload(h_glrow.data(), N + 1, st);
     d_gloff.alloc(NNZ); d_gloff.upload(h_gloff.data(), NNZ, st);
-    d_gl.alloc(std::max<size_t>(h_gl.size(), 1)); d_gl.upload(h_gl.data(), h_gl.size(), st);
+    while (h_gl.size() & 3) h_gl.push_back(0);  // whole words for the last row
+    d_gl.alloc(std::max<size_t>(h_gl.size(), 4)); d_gl.upload(h_gl.data(), h_gl.size(), st);
     d_islot.alloc(h_islot.size()); d_islot.upload(h_islot.data(), h_islot.size(), st);
   }
   d_srows.alloc(nsurf); d_srows.upload(h_srows.data(), nsurf, st);
@@ -5506,7 +5523,7 @@ static int64_t flag_running(Engine* e) {
 
 // The autotuner of the FP32 Picard path.  On the handle's current state
 // (every running member, so call it once the members have run a few steps)
-// it times each assembly variant (resident blocks per SM 4, 5, 6, 8) and
+// it times each assembly variant (resident blocks per SM 5, 6, 7, 8) and
 // the stream SpMV at 4, 6 and 8 resident blocks per SM (nrep launches each
 // between CUDA events, after one untimed launch) and keeps the fastest of
 // each.  The choice is cached per (GPU, rows size class): nrep <= 0 takes
