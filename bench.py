@@ -497,7 +497,8 @@ def main():
                      "launches": spmv_n, "alg_bytes_per_launch": spmv_bytes / max(spmv_n, 1)},
         "roofline_assembly": {
             "bound": "hbm", "kernel": "k_assemble_picard_f32",
-            "timing": "20 launches over all 256 members after the warm-up, CUDA events",
+            "timing": f"mean of 20 launches over all {args.members} members after their first "
+                      f"5 steps, CUDA events",
             "achieved": asm_bytes / 1e9 / (asm_ms / 1e3), "peak": peak, "unit": "GB/s",
             "frac": asm_bytes / 1e9 / (asm_ms / 1e3) / peak, "peak_source": peak_kind,
             "alg_bytes_per_launch": asm_bytes, "rows": asm_rows, "ms_per_launch": asm_ms},

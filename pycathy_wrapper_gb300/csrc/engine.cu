@@ -24,6 +24,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -102,6 +103,27 @@ __device__ __forceinline__ void block_accumulate(double (&v)[NV], double* acc) {
         s = warp_sum(s);
         if (lane == 0 && s != 0.0) atomicAdd(acc + i, s);
       }
+    }
+  }
+}
+
+// Block sum of NV FP64 values through shared memory: warp 0 adds the
+// block's values in a fixed order (8 per lane, then a shuffle tree), so
+// the block does 13 FP64 adds per value in one warp instead of 5 in every
+// warp -- for values that are nonzero in every thread.
+template <int NV>
+__device__ __forceinline__ void block_accumulate_smem(double (&v)[NV], double* acc) {
+  __shared__ double sh[NV][kThreads];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) sh[i][threadIdx.x] = v[i];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double s = 0.0;
+      for (int k = threadIdx.x; k < (int)blockDim.x; k += 32) s += sh[i][k];
+      s = warp_sum(s);
+      if (threadIdx.x == 0 && s != 0.0) atomicAdd(acc + i, s);
     }
   }
 }
@@ -207,6 +229,8 @@ struct Nodal {  // per node
   // iteration (before relaxation and switching), and van Genuchten beta and
   // Se carried at PTIMEP from step to step
   double *pmb, *bet, *set;
+  // per-node FP64 constants of the storage terms (k_mb_consts)
+  double *mba, *mbb, *mbc, *mbd;
   uint8_t *sdir;             // static (non-atmospheric) Dirichlet node
   uint8_t *dmask;            // current Dirichlet mask (static | atm 1,2)
   // surface nodes (valid for loc < nnod)
@@ -695,6 +719,17 @@ enum {
   SC_PQ = 0, SC_PR, SC_RR, SC_QZ, SC_XL, SC_ROJ, SC_SIG, SC_AA, SC_BB,
   SC_ROJM1, SC_ALFJM1, SC_ETAJ, SC_ALF, SC_BETA, SC_ERR, SC_NB, SC_N
 };
+// The FP32 PCG direction coefficient beta is stored as a float in the first
+// four bytes of the SC_BETA slot: the decision converts it once per member,
+// and the SpMV entries that read it do no FP64 conversion (an FP64
+// instruction costs about 16 FP32 ones on this GPU).
+__device__ __forceinline__ float sc_beta_f32(const double* S) {
+  return reinterpret_cast<const float*>(S + SC_BETA)[0];
+}
+__device__ __forceinline__ void set_sc_beta_f32(double* S, float b) {
+  S[SC_BETA] = 0.0;
+  reinterpret_cast<float*>(S + SC_BETA)[0] = b;
+}
 // Programmatic dependent launch.  Inside the Picard-iteration graph a kernel
 // may be launched while its predecessor is still running (its blocks become
 // resident once every block of the predecessor has started); it waits here,
@@ -927,7 +962,7 @@ __device__ __forceinline__ void spmv_stream_run(
   float* sp = sprod[wp];
   float d0 = 0.0f, d1 = 0.0f;
   int cur = -1;
-  double bytes = 0.0;
+  long long bytes = 0;  // algorithmic bytes (integer: no FP64 work per entry)
   // each block takes a contiguous run of entries (kSpmvUpd: of the listed
   // entries of the members still in the Krylov solve); its warps interleave
   int total = nblk, nseg = 0;
@@ -981,9 +1016,8 @@ __device__ __forceinline__ void spmv_stream_run(
     const int sbeg = __shfl_sync(0xffffffffu, rp, 0);
     const int send = __shfl_sync(0xffffffffu, rp, nr);
     if (alg_bytes && lane == 0)
-      bytes += (double)(send - sbeg) * 8.0 +
-               nr * (kMode == kSpmvUpd ? 28.0 : 4.0 + (w ? 3.0 : 2.0) * 4.0);
-    const float beta = kMode == kSpmvUpd ? (float)sc[(size_t)m * SC_N + SC_BETA] : 0.0f;
+      bytes += (long long)(send - sbeg) * 8 + nr * (kMode == kSpmvUpd ? 28 : (w ? 16 : 12));
+    const float beta = kMode == kSpmvUpd ? sc_beta_f32(sc + (size_t)m * SC_N) : 0.0f;
     // 16-byte vectors covering [sbeg, send)
     const int v0 = sbeg >> 2, v1 = (send + 3) >> 2;
     for (int v = v0 + lane; v < v1; v += 32) {
@@ -1063,7 +1097,7 @@ __device__ __forceinline__ void spmv_stream_run(
   }
   if (alg_bytes) {
     // one global atomic per block
-    if (lane == 0 && bytes != 0.0) atomicAdd(s_bytes, bytes);
+    if (lane == 0 && bytes != 0) atomicAdd(s_bytes, (double)bytes);
     __syncthreads();
     if (threadIdx.x == 0 && *s_bytes != 0.0) atomicAdd(alg_bytes, *s_bytes);
   }
@@ -2090,24 +2124,48 @@ __device__ __forceinline__ void vg_move64(double psi, double psi_t, double b_t, 
   b = pow(fabs(psi / psat), n);
   se = pow(fabs(1.0 / (b + 1.0)), m);
 }
+// Se at psi = pn + d from Se (sn) and beta (bn) at pn, for a small move
+// |d| <= 1e-5 |pn| on the unsaturated branch: second-order Taylor series,
+// Se' = -m n g Se / psi and Se'' = Se' (n (1 - g) - m n g - 1) / psi with
+// g = beta / (1 + beta), the increment in FP32 (its third-order remainder
+// is below 1e-14 of Se).  Returns false (and leaves so) otherwise.
+__device__ __forceinline__ bool se_near(double pn, double d, double sn, double bn, float n,
+                                        float m, double& so) {
+  if (!(pn < -1.0e-14) || !(pn + d < -1.0e-14)) return false;
+  const float df = (float)d, pf = (float)pn;
+  if (fabsf(df) > 1.0e-5f * fabsf(pf)) return false;
+  const float b = (float)bn, g = b / (1.0f + b);
+  const float s1 = -m * n * g * (float)sn / pf;
+  const float s2 = s1 * (n * (1.0f - g) - m * n * g - 1.0f) / pf;
+  so = sn + (double)(df * fmaf(0.5f * df, s2, s1));
+  return true;
+}
+
 // Node i's share of the accepted step's FP64 storage change and of the new
 // storage, then beta/Se moved to the accepted head (the next PTIMEP).
 // POLD is the head at the start of the accepted iteration (where CHPIC took
-// SWNEW), PMB the head at its mass balance, PNEW the accepted head.
+// SWNEW), PMB the head at its mass balance, PNEW the accepted head.  Se at
+// PNEW is moved from PTIMEP (it is carried to the next step); Se at POLD,
+// which differs from PNEW by the last Picard correction, from PNEW.  With
+// A = V phi pnot, B = V thr, C = V Ss pnot / 2, D = V Ss thr / phi
+// (k_mb_consts) the storage terms of masbal.f are
+//   DSTORE_i = (C (Se + Se_t) + D) (PMB - P_t) + A (Se - Se_t),
+//   STORE_i = A Se' + B.
 __device__ __forceinline__ void commit_mass_node(int i, const Nodal& nd, double& dstore,
                                                  double& store) {
   const double psat = nd.vgpsat[i], n = nd.vgn[i], m = nd.vgm[i];
   const double pt = nd.ptimep[i], bt = nd.bet[i], st = nd.set[i];
-  double so, bo, sn, bn;
-  vg_move64(nd.pold[i], pt, bt, st, psat, n, m, so, bo);
-  const double pn = nd.pnew[i];
-  if (pn == nd.pold[i]) { sn = so; bn = bo; }
-  else vg_move64(pn, pt, bt, st, psat, n, m, sn, bn);
-  const double pnot = nd.vgpnot[i], por = nd.pnodi[i], rmp = nd.vgrmc[i] / por;
-  const double swo = pnot * so + rmp, swt = pnot * st + rmp;
-  const double v = nd.volnod[i];
-  dstore = v * (nd.snodi[i] * (swo + swt) * 0.5 * (nd.pmb[i] - pt) + por * (pnot * (so - st)));
-  store = (pnot * sn + rmp) * v * por;
+  const double po = nd.pold[i], pn = nd.pnew[i];
+  double sn, bn, so;
+  vg_move64(pn, pt, bt, st, psat, n, m, sn, bn);
+  if (po == pn) {
+    so = sn;
+  } else if (!se_near(pn, po - pn, sn, bn, (float)n, (float)m, so)) {
+    double bo;
+    vg_move64(po, pt, bt, st, psat, n, m, so, bo);
+  }
+  dstore = fma(nd.mba[i], so - st, fma(nd.mbc[i], so + st, nd.mbd[i]) * (nd.pmb[i] - pt));
+  store = fma(nd.mba[i], sn, nd.mbb[i]);
   nd.bet[i] = bn;
   nd.set[i] = sn;
 }
@@ -2182,7 +2240,7 @@ __device__ __forceinline__ void start_vg_entry(int bid, const int32_t* bm_mem,
   if (a & ACT_COMMIT) {  // block-uniform
     double mb[2] = {0.0, 0.0};
     if (ok) commit_mass_node(i, nd, mb[0], mb[1]);
-    block_accumulate<2>(mb, red + (size_t)m * RD_NUM + RD_DSTORE_C);
+    block_accumulate_smem<2>(mb, red + (size_t)m * RD_NUM + RD_DSTORE_C);
   }
   if (!ok) return;
   const MemberScal& S = ms[m];
@@ -2205,6 +2263,21 @@ __global__ void k_start_vg_f32(int nb1, const int32_t* bm_mem, const int32_t* bm
     return;
   }
   start_vg_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, act, ms, nd, nf, z, need_sw, red);
+}
+
+// The per-node FP64 constants of the FP32 path's storage terms (see
+// commit_mass_node): A = V phi pnot, B = V thr, C = V Ss pnot / 2,
+// D = V Ss thr / phi (V nodal volume, phi porosity, thr residual moisture,
+// pnot = 1 - thr / phi, Ss specific storage).
+__global__ void k_mb_consts(int n, Nodal nd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = nd.volnod[i], por = nd.pnodi[i], pnot = nd.vgpnot[i];
+  const double thr = nd.vgrmc[i], ss = nd.snodi[i];
+  nd.mba[i] = v * por * pnot;
+  nd.mbb[i] = v * thr;
+  nd.mbc[i] = 0.5 * v * ss * pnot;
+  nd.mbd[i] = v * ss * (thr / por);
 }
 
 // beta and Se at PTIMEP in FP64 of nodes [i0, i1) (the carried values of
@@ -2334,7 +2407,7 @@ __device__ __forceinline__ void assemble_f32_entry(
   const bool rowok = i < rend;
   const uint8_t am = act[m];
   const MemberScal& S = ms[m];
-  const float rdt = (float)S.deltat_r, th = (float)S.tetaf;
+  const float rdt = S.deltat_rf, th = S.tetaf_f;  // no FP64 conversion per warp
   int s0 = 0, s1 = 0, p0 = 0, p1 = 0;
   int64_t gbase = 0;
   float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f;
@@ -2459,6 +2532,203 @@ constexpr int kAsmBlocks[kAsmVariants] = {5, 6, 7, 8};
 static const AsmKernel kAsmKernel[kAsmVariants] = {
     &k_assemble_picard_f32<5>, &k_assemble_picard_f32<6>, &k_assemble_picard_f32<7>,
     &k_assemble_picard_f32<8>};
+
+// ---- staged assembly: TMA bulk copies into shared memory ------------------
+// A block's 16 rows own contiguous ranges of incidence records, slot
+// nibbles, columns, gather offsets and gather-list bytes; thread 0 copies
+// each range whole into shared memory with one cp.async.bulk (the async
+// copy engine, completion counted in bytes on an mbarrier) as soon as the
+// map entry is read, while every thread loads its row's own inputs.  The
+// loads of the unstaged kernel's third round thus go out with its second,
+// and the lanes read the records, slots and lists from shared memory.
+// Bulk copies need 16-byte aligned addresses and sizes: each range is
+// widened to whole 16-byte units (the arrays are padded by 16 bytes).
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// try_wait suspends for a bounded time per call; this many calls (far more
+// than any copy of a few KB needs) and the block gives up and flags it
+constexpr int kStageSpin = 1 << 20;
+
+__host__ __device__ inline long long align16ll(long long x) { return (x + 15) & ~15LL; }
+// byte offsets of the staged arrays in dynamic shared memory, for the
+// largest ranges of any entry; off[5] is the total
+__host__ __device__ inline void asm_stage_layout(int cap_inc, int cap_slot, int cap_gl, int* off) {
+  off[0] = 0;                                            // records, 16 B each
+  off[1] = off[0] + cap_inc * 16;                        // slot nibbles
+  off[2] = off[1] + (int)align16ll(cap_inc * 2 + 32);    // columns
+  off[3] = off[2] + (int)align16ll(cap_slot * 4 + 32);   // gather offsets
+  off[4] = off[3] + (int)align16ll(cap_slot + 32);       // gather lists
+  off[5] = off[4] + (int)align16ll(cap_gl + 32);
+}
+
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                      const int4* __restrict__ bm_ent, const longlong2* __restrict__ bm_eg,
+                      const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
+                      const int32_t* cols, const int32_t* inc_ptr,
+                      const float4* __restrict__ rec16, const uint16_t* __restrict__ islot,
+                      const float* __restrict__ vpi, const float* __restrict__ vps,
+                      const uint8_t* dmask, NodalF nf, const int32_t* __restrict__ loc,
+                      const int8_t* __restrict__ ifatm, const double* __restrict__ atmact,
+                      const double* __restrict__ atmold, float* vals, float lm_d, float lm_o,
+                      const int64_t* __restrict__ glrow, const uint8_t* __restrict__ gloff,
+                      const uint8_t* __restrict__ gl, int cap_inc, int cap_slot, int cap_gl,
+                      int32_t* stage_err) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ float sval[kRowsPerBlock16][64 * 4];
+  __shared__ float2 sh2[kRowsPerBlock16][kGroup];
+  __shared__ float2 sk2[kRowsPerBlock16][kGroup];
+  __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
+  __shared__ __align__(8) uint64_t mbar;
+  pdl_enter();
+  const int bid = blockIdx.x;
+  int off[6];
+  asm_stage_layout(cap_inc, cap_slot, cap_gl, off);
+  float4* srec = reinterpret_cast<float4*>(dsm + off[0]);
+  uint16_t* sisl = reinterpret_cast<uint16_t*>(dsm + off[1]);
+  int32_t* scol = reinterpret_cast<int32_t*>(dsm + off[2]);
+  uint8_t* sglo = dsm + off[3];
+  uint8_t* sgl = dsm + off[4];
+  if (threadIdx.x == 0) mbar_init(&mbar, 1);
+  __syncthreads();
+  const int m = bm_mem[bid];
+  const int rbeg = bm_r0[bid], rend = bm_r1[bid];
+  const int4 e4 = bm_ent[bid];        // incidences [x, y), slots [z, w)
+  const longlong2 eg = bm_eg[bid];    // gather-list bytes [x, y)
+  const uint8_t am = act[m];
+  const bool iter = (am & ACT_ITER) != 0;
+  // 16-byte aligned starts of the staged ranges, in elements
+  const int isl0 = e4.x & ~7, col0 = e4.z & ~3, glo0 = e4.z & ~15;
+  const long long gl0 = eg.x & ~15LL;
+  if (threadIdx.x == 0 && iter) {
+    const uint32_t b0 = (uint32_t)(e4.y - e4.x) * 16u;
+    const uint32_t b1 = (uint32_t)(align16ll(2LL * e4.y) - 2LL * isl0);
+    const uint32_t b2 = (uint32_t)(align16ll(4LL * e4.w) - 4LL * col0);
+    const uint32_t b3 = (uint32_t)(align16ll((long long)e4.w) - glo0);
+    const uint32_t b4 = (uint32_t)(align16ll(eg.y) - gl0);
+    mbar_expect_tx(&mbar, b0 + b1 + b2 + b3 + b4);
+    if (b0) bulk_g2s(srec, rec16 + e4.x, b0, &mbar);
+    if (b1) bulk_g2s(sisl, islot + isl0, b1, &mbar);
+    if (b2) bulk_g2s(scol, cols + col0, b2, &mbar);
+    if (b3) bulk_g2s(sglo, gloff + glo0, b3, &mbar);
+    if (b4) bulk_g2s(sgl, gl + gl0, b4, &mbar);
+  }
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = rbeg + grp;
+  const bool rowok = i < rend;
+  const MemberScal& S = ms[m];
+  const float rdt = S.deltat_rf, th = S.tetaf_f;
+  int s0 = 0, s1 = 0, p0 = 0, p1 = 0;
+  int64_t gbase = 0;
+  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f;
+  bool atm_i = false, dm_i = false;
+  if (rowok) {
+    s0 = rowptr[i];
+    s1 = rowptr[i + 1];
+    p0 = inc_ptr[i];
+    p1 = inc_ptr[i + 1];
+    gbase = glrow[i];
+    et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
+    vpl = vps[i] * lm_d;
+    dp_i = nf.dpsi[i]; ds_i = nf.dsw[i]; qn_i = nf.qneu[i];
+    atm_i = loc[i] < S.nnod && ifatm[i] == 0;
+    dm_i = dmask[i] != 0;
+  }
+  if (!iter) return;  // block-uniform; no copy was issued
+  bool ready = false;
+  for (int k = 0; k < kStageSpin && !ready; ++k) ready = mbar_try_wait(&mbar, 0);
+  if (!ready) {
+    if (threadIdx.x == 0) atomicExch(stage_err, 1);
+    return;
+  }
+  const int rlen = s1 - s0, ninc = p1 - p0;
+  int col = -1, ga = 0, gb = 0;
+  if (rowok && lane < rlen) {
+    col = scol[s0 + lane - col0];
+    ga = sglo[s0 + lane - glo0];
+    gb = (lane + 1 < rlen) ? (int)sglo[s0 + lane + 1 - glo0] : 3 * ninc;
+  }
+  if (col >= 0) {
+    sh2[grp][lane] = nf.h2[col];
+    sk2[grp][lane] = nf.ckr2[col];
+    if (lm_o != 0.0f) {
+      sdp[grp][lane] = nf.dpsi[col];
+      sds[grp][lane] = nf.dsw[col];
+    }
+  }
+  __syncwarp();
+  int ntrip = (ninc + kGroup - 1) / kGroup;
+  ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
+  AsmInc a{0.0f, 0.0f, 0.0f};
+  for (int trip = 0; trip < ntrip; ++trip) {
+    const int q = trip * kGroup + lane;
+    if (rowok && q < ninc)
+      asm_incidence(q, srec[p0 - e4.x + q], sisl[p0 + q - isl0],
+                    lm_o != 0.0f ? vpi[p0 + q] : 0.0f, grp, th, rdt, lm_d, lm_o, hh_i, hl_i,
+                    sval, sh2, sk2, sdp, sds, a);
+  }
+  __syncwarp();
+  const float dsum = group_sum<float>(a.dacc);
+  float rhs = group_sum<float>(a.rp);
+  const float msum = group_sum<float>(a.msum);
+  if (!rowok) return;
+  if (col >= 0) {
+    float lhs;
+    if (col == i) {
+      lhs = dsum + vpl * et2i * rdt;
+    } else {
+      lhs = 0.0f;
+      const uint8_t* g8 = sgl + (gbase - gl0);
+      for (int u = ga; u < gb; ++u) lhs += sval[grp][g8[u]];
+    }
+    vals[s0 + lane] = lhs;
+  }
+  if (lane == 0) {
+    rhs -= (msum * dp_i + vpl * ds_i) * rdt;
+    nf.xt5[i] = rhs;
+    float f = qn_i;
+    if (atm_i) {
+      const double thd = S.tetaf;
+      f += (thd == 1.0) ? (float)atmact[i]
+                        : (float)(thd * atmact[i] + (1.0 - thd) * atmold[i]);
+    }
+    nf.rhs[i] = dm_i ? 0.0f : rhs + f;
+  }
+}
+using StagedKernel = decltype(&k_assemble_staged_f32<6>);
+static const StagedKernel kStagedKernel[kAsmVariants] = {
+    &k_assemble_staged_f32<5>, &k_assemble_staged_f32<6>, &k_assemble_staged_f32<7>,
+    &k_assemble_staged_f32<8>};
 
 // Post-solve pass of the FP32 Picard iteration, one thread per row:
 // PNEW += PDIFF + SHLPIC; at Dirichlet rows the back-calculated flux (BKPIC:
@@ -2625,7 +2895,9 @@ __global__ void k_params_f32(int n, Nodal nd, NodalF nf) {
 // the active member slot holding block b (binary search over cum).
 __global__ void k_compact_map(int ntot, int nact, const int32_t* amem, const int32_t* cum,
                               const int32_t* first, const int32_t* fmem, const int32_t* fr0,
-                              const int32_t* fr1, int32_t* omem, int32_t* or0, int32_t* or1) {
+                              const int32_t* fr1, int32_t* omem, int32_t* or0, int32_t* or1,
+                              const int4* fent, const longlong2* feg, int4* oent,
+                              longlong2* oeg) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= ntot) return;
   int lo = 0, hi = nact - 1;
@@ -2637,6 +2909,10 @@ __global__ void k_compact_map(int ntot, int nact, const int32_t* amem, const int
   omem[b] = fmem[src];
   or0[b] = fr0[src];
   or1[b] = fr1[src];
+  if (fent) {
+    oent[b] = fent[src];
+    oeg[b] = feg[src];
+  }
 }
 
 // ============================================================================
@@ -2762,7 +3038,7 @@ __device__ __forceinline__ void pcg_setup_members(int bb, int nmem, const uint8_
   const int m = bb * blockDim.x + threadIdx.x;
   if (m < nmem && active[m]) {
     niter[m] = 1;
-    sc[(size_t)m * SC_N + SC_BETA] = 0.0;
+    set_sc_beta_f32(sc + (size_t)m * SC_N, 0.0f);
   }
   if (bb == 0) build_kact(amem_cum, nmem, active, kact);
 }
@@ -2802,16 +3078,23 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
 // T^-1 r, and the block's rr and qz into the member's Krylov scalars.
 __device__ __forceinline__ void pcg_xz_entry(int bid, const int32_t* bm_mem, const int32_t* bm_r0,
                                              const int32_t* bm_r1, const uint8_t* active,
-                                             const MemberScal* ms, double* sc, const float* pinv,
-                                             const float* cdown, float* r, float* x,
-                                             const float* p, const float* q, float* z,
-                                             const uint8_t* dmask) {
+                                             const MemberScal* ms, double* sc,
+                                             const float* __restrict__ pinv,
+                                             const float* __restrict__ cdown,
+                                             float* __restrict__ r, float* __restrict__ x,
+                                             const float* __restrict__ p,
+                                             const float* __restrict__ q, float* __restrict__ z,
+                                             const uint8_t* __restrict__ dmask) {
   const int m = bm_mem[bid];
   if (!active[m]) return;  // block-uniform
   float dd[2] = {0.0f, 0.0f};  // rr, qz
   const int top = bm_r0[bid] + threadIdx.x;
+  // alfa = p.r / p.q: one FP64 division per warp (lane 0), broadcast
+  float alfa = 0.0f;
+  if ((threadIdx.x & 31) == 0)
+    alfa = (float)(sc[(size_t)m * SC_N + SC_PR] / sc[(size_t)m * SC_N + SC_PQ]);
+  alfa = __shfl_sync(0xffffffffu, alfa, 0);
   if (top < bm_r1[bid]) {
-    const float alfa = (float)(sc[(size_t)m * SC_N + SC_PR] / sc[(size_t)m * SC_N + SC_PQ]);
     const int nnod = ms[m].nnod, nl = ms[m].nstr + 1;
     float yprev = 0.0f, cprev = 0.0f, pprev = 0.0f;
     for (int k0 = 0; k0 < nl; k0 += kLineChunk) {
@@ -2893,7 +3176,7 @@ __device__ __forceinline__ int pcg_decide(int nmem, uint8_t* active, double* sc,
     S[SC_ERR] = err;
     if (err > tol && niter[mm] < itmax) {
       niter[mm] += 1;
-      S[SC_BETA] = -S[SC_QZ] / S[SC_PQ];
+      set_sc_beta_f32(S, (float)(-S[SC_QZ] / S[SC_PQ]));
       mine++;
     } else {
       active[mm] = 0;
@@ -2909,8 +3192,9 @@ __device__ __forceinline__ int pcg_decide(int nmem, uint8_t* active, double* sc,
 __global__ void __launch_bounds__(kThreads)
 k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
              uint8_t* active, const MemberScal* ms, double* sc, const float* __restrict__ pinv,
-             const float* __restrict__ cdown, float* r, float* x, const float* __restrict__ p,
-             const float* __restrict__ q, float* z, const uint8_t* __restrict__ dmask, int nmem,
+             const float* __restrict__ cdown, float* __restrict__ r, float* __restrict__ x,
+             const float* __restrict__ p, const float* __restrict__ q, float* __restrict__ z,
+             const uint8_t* __restrict__ dmask, int nmem,
              int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
              unsigned int* done, int32_t* nact, int use_cond, cudaGraphConditionalHandle h,
              const int32_t* amem_cum, int32_t* kact) {
@@ -3003,6 +3287,16 @@ struct MemberHost {
   std::vector<double> atm_a_nodal, atm_b_nodal;
 };
 
+// nodal FP64 arrays of the engine (d_nodal[ND_*])
+enum {
+  ND_VOLNOD = 0, ND_PNODI, ND_SNODI, ND_VGN, ND_VGM, ND_VGRMC, ND_VGPSAT, ND_VGN1,
+  ND_VGNR, ND_VGPSN, ND_VGMR, ND_VGM52, ND_VGMM1, ND_VGPNOT, ND_PNEW, ND_POLD,
+  ND_PTNEW, ND_PTOLD, ND_PTIMEP, ND_PDIFF, ND_SWNEW, ND_SWTIMEP, ND_RHS, ND_XT5,
+  ND_QNEU, ND_PRESC, ND_QPNEW, ND_QPOLD, ND_SW, ND_ET1, ND_ET2, ND_CKRW, ND_ETAI,
+  ND_DCKRW, ND_DETAI, ND_ARENOD, ND_ATMPOT, ND_ATMACT, ND_ATMOLD, ND_ATMA, ND_ATMB,
+  ND_X, ND_Y, ND_Z, ND_PMB, ND_BET, ND_SET, ND_MBA, ND_MBB, ND_MBC, ND_MBD, ND_NUM
+};
+
 struct Engine {
   cathy_opts_t opts;
   int nmem = 0;
@@ -3016,7 +3310,7 @@ struct Engine {
   std::vector<int32_t> node_off, tet_off, nnz_off;
   // device buffers
   DBuf<int32_t> d_mem, d_loc, d_node_off;
-  DBuf<double> d_nodal[48];
+  DBuf<double> d_nodal[ND_NUM];
   DBuf<float> d_nodf[23];
   DBuf<float2> d_ckr2, d_h2;
   BlockMap bme;  // element blocks per member
@@ -3097,12 +3391,14 @@ struct Engine {
   bool pdl_enabled = std::getenv("CATHY_GB300_PDL") != nullptr &&
                      std::getenv("CATHY_GB300_PDL")[0] == '1';
   bool pdl_cap = false, pdl_prev = false;
+  size_t next_smem = 0;  // dynamic shared memory of the next launch()
   template <class... KArgs, class... Args>
   void launch(void (*k)(KArgs...), int grid, int block, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3((unsigned)block);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = next_smem;
+    next_smem = 0;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     if (pdl_enabled && pdl_cap && pdl_prev) {
@@ -3145,6 +3441,15 @@ struct Engine {
   // variant (resident blocks per SM kAsmBlocks[asm_variant]) and the stream
   // SpMV's resident blocks per SM (its grid = stream_per_sm * SMs)
   int asm_variant = 1;
+  // staged assembly: largest incidence, slot and gather-list ranges of a
+  // 16-row entry, and the device flag a block sets if its staging wait
+  // runs out
+  int stage_inc = 0, stage_slot = 0, stage_gl = 0;
+  DBuf<int32_t> d_stage_err;
+  bool asm_staged = false;  // the autotuner's choice between the two assemblies
+  size_t stage_smem = 0;    // dynamic shared memory of the staged assembly (0: unavailable)
+  void launch_assembly(int variant, bool staged);
+  void check_stage_err();
   int stream_per_sm = 8;
   int nsm = 152;
   // Phase timers in the reference's CPUVEC buckets (picard.f:66-202, the
@@ -3323,14 +3628,6 @@ struct Engine {
 };
 
 // ---- member input -> host mesh + device arrays ---------------------------
-enum {
-  ND_VOLNOD = 0, ND_PNODI, ND_SNODI, ND_VGN, ND_VGM, ND_VGRMC, ND_VGPSAT, ND_VGN1,
-  ND_VGNR, ND_VGPSN, ND_VGMR, ND_VGM52, ND_VGMM1, ND_VGPNOT, ND_PNEW, ND_POLD,
-  ND_PTNEW, ND_PTOLD, ND_PTIMEP, ND_PDIFF, ND_SWNEW, ND_SWTIMEP, ND_RHS, ND_XT5,
-  ND_QNEU, ND_PRESC, ND_QPNEW, ND_QPOLD, ND_SW, ND_ET1, ND_ET2, ND_CKRW, ND_ETAI,
-  ND_DCKRW, ND_DETAI, ND_ARENOD, ND_ATMPOT, ND_ATMACT, ND_ATMOLD, ND_ATMA, ND_ATMB,
-  ND_X, ND_Y, ND_Z, ND_PMB, ND_BET, ND_SET, ND_NUM
-};
 
 void Engine::make_elem_blockmap(BlockMap& bm, int epb) {
   std::vector<int32_t> mm, r0, r1;
@@ -3723,10 +4020,12 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_inc.alloc(h_inc.size()); d_inc.upload(h_inc.data(), h_inc.size(), st);
   if (glists) {
     d_glrow.alloc(N + 1); d_glrow.upload(h_glrow.data(), N + 1, st);
-    d_gloff.alloc(NNZ); d_gloff.upload(h_gloff.data(), NNZ, st);
+    // (+16 bytes: the staged assembly copies whole 16-byte units)
+    d_gloff.alloc(NNZ + 16); d_gloff.zero(st); d_gloff.upload(h_gloff.data(), NNZ, st);
     while (h_gl.size() & 3) h_gl.push_back(0);  // whole words for the last row
-    d_gl.alloc(std::max<size_t>(h_gl.size(), 4)); d_gl.upload(h_gl.data(), h_gl.size(), st);
-    d_islot.alloc(h_islot.size()); d_islot.upload(h_islot.data(), h_islot.size(), st);
+    d_gl.alloc(h_gl.size() + 16); d_gl.zero(st); d_gl.upload(h_gl.data(), h_gl.size(), st);
+    d_islot.alloc(h_islot.size() + 8); d_islot.zero(st);
+    d_islot.upload(h_islot.data(), h_islot.size(), st);
   }
   d_srows.alloc(nsurf); d_srows.upload(h_srows.data(), nsurf, st);
   {
@@ -3793,6 +4092,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   nd.atmpot = P(ND_ATMPOT); nd.atmact = P(ND_ATMACT); nd.atmold = P(ND_ATMOLD);
   nd.atm_a = P(ND_ATMA); nd.atm_b = P(ND_ATMB);
   nd.pmb = P(ND_PMB); nd.bet = P(ND_BET); nd.set = P(ND_SET);
+  nd.mba = P(ND_MBA); nd.mbb = P(ND_MBB); nd.mbc = P(ND_MBC); nd.mbd = P(ND_MBD);
   nd.sdir = d_sdir.p; nd.dmask = d_dmask.p; nd.ifatm = d_ifatm.p; nd.ifatmp = d_ifatmp.p;
   // TPNODI/CHPARM then geometry
   k_tpnodi<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, d_inc_ptr.p, d_inc.p, d_tetsoil.p,
@@ -3830,6 +4130,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     d_ckr2.alloc(N); d_h2.alloc(N);
     nf.ckr2 = d_ckr2.p; nf.h2 = d_h2.p;
     k_params_f32<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, nd, nf);
+    k_mb_consts<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, nd);
     k_init_carry<<<cdiv(N, kThreads), kThreads, 0, st>>>(0, N, nd);
     check_launch();
   }
@@ -3885,6 +4186,44 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_nact.alloc(1);
   make_blockmap(bm1, kThreads);
   make_blockmap(bm16, kRowsPerBlock16);
+  if (precision == 1 && iopt == 1) {
+    // staged assembly: each 16-row entry's ranges of incidence records,
+    // matrix slots and gather-list bytes, and the largest of each (the
+    // shared-memory staging area of a block)
+    std::vector<int4> ent;
+    std::vector<longlong2> eg;
+    stage_inc = stage_slot = stage_gl = 0;
+    for (int m = 0; m < nmem; ++m)
+      for (int a = node_off[m]; a < node_off[m + 1]; a += kRowsPerBlock16) {
+        const int b = std::min(a + kRowsPerBlock16, node_off[m + 1]);
+        ent.push_back(make_int4(h_incptr[a], h_incptr[b], h_rowptr[a], h_rowptr[b]));
+        const long long g1 = h_glrow[b - 1] + 3LL * (h_incptr[b] - h_incptr[b - 1]);
+        eg.push_back(make_longlong2(h_glrow[a], g1));
+        stage_inc = std::max(stage_inc, h_incptr[b] - h_incptr[a]);
+        stage_slot = std::max(stage_slot, h_rowptr[b] - h_rowptr[a]);
+        stage_gl = std::max(stage_gl, (int)(g1 - h_glrow[a]));
+      }
+    if ((int)ent.size() != bm16.nblk) throw std::string("staged assembly: entry count mismatch");
+    bm16.ent.alloc(ent.size()); bm16.ent.upload(ent.data(), ent.size(), st);
+    bm16.eg.alloc(eg.size()); bm16.eg.upload(eg.data(), eg.size(), st);
+    d_stage_err.alloc(1);
+    d_stage_err.zero(st);
+    int off[6];
+    asm_stage_layout(stage_inc, stage_slot, stage_gl, off);
+    stage_smem = (size_t)off[5];
+    if (stage_smem > (size_t)48 * 1024) {
+      // above the default dynamic limit: opt in, or leave the staged
+      // assembly off if it does not fit next to the static arrays
+      bool ok = stage_smem <= (size_t)180 * 1024;
+      for (int k = 0; ok && k < kAsmVariants; ++k)
+        ok = cudaFuncSetAttribute(kStagedKernel[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)stage_smem) == cudaSuccess;
+      if (!ok) {
+        cudaGetLastError();
+        stage_smem = 0;
+      }
+    }
+  }
   make_elem_blockmap(bme, kThreads);
   make_surface_blockmap(bms, kThreads);
   make_surface_blockmap(bms16, kRowsPerBlock16);
@@ -3949,6 +4288,14 @@ void Engine::init_compaction() {
       CG_TRY(cudaMemcpyAsync(dst.r0.p, src.r0.p, 4 * src.nblk, cudaMemcpyDeviceToDevice, st));
       CG_TRY(cudaMemcpyAsync(dst.r1.p, src.r1.p, 4 * src.nblk, cudaMemcpyDeviceToDevice, st));
     }
+    if (src.ent.p) {
+      dst.ent.alloc(std::max(src.nblk, 1));
+      dst.eg.alloc(std::max(src.nblk, 1));
+      CG_TRY(cudaMemcpyAsync(dst.ent.p, src.ent.p, sizeof(int4) * src.nblk,
+                             cudaMemcpyDeviceToDevice, st));
+      CG_TRY(cudaMemcpyAsync(dst.eg.p, src.eg.p, sizeof(longlong2) * src.nblk,
+                             cudaMemcpyDeviceToDevice, st));
+    }
   };
   per_member_counts(host_mem(bm1), nmem, nblk1, first1);
   per_member_counts(host_mem(bm16), nmem, nblk16, first16);
@@ -4003,7 +4350,8 @@ void Engine::compact_maps(const std::vector<uint8_t>& memact) {
     if (!tot[q]) continue;
     k_compact_map<<<cdiv(tot[q], 256), 256, 0, st>>>(tot[q], na, d_amem_cum.p,
         d_amem_cum.p + (size_t)(q + 1) * (nmem + 1), d_first.p + (size_t)q * nmem, full[q]->mem.p,
-        full[q]->r0.p, full[q]->r1.p, comp[q]->mem.p, comp[q]->r0.p, comp[q]->r1.p);
+        full[q]->r0.p, full[q]->r1.p, comp[q]->mem.p, comp[q]->r0.p, comp[q]->r1.p,
+        full[q]->ent.p, full[q]->eg.p, comp[q]->ent.p, comp[q]->eg.p);
     count();
   }
   check_launch();
@@ -4047,6 +4395,7 @@ void Engine::push_scalars(bool to_pinned) {
     MemberHost& h = *M[m];
     MemberScal& S = h_ms[m];
     S.deltat = h.deltat; S.deltat_r = 1.0 / h.deltat; S.time = h.time; S.tetaf = h.parm.tetaf; S.scf = h.scf;
+    S.deltat_rf = (float)S.deltat_r; S.tetaf_f = (float)S.tetaf;
     S.pmin = h.pmin; S.omega = h.parm.omega; S.tolswi = h.parm.tolswi;
     S.atm_ta = h.atm_ta; S.atm_tb = h.atm_tb; S.atm_va = h.atm_va; S.atm_vb = h.atm_vb;
     S.atm_mode = h.atm_mode; S.hspatm = h.hspatm; S.ieto = h.ieto; S.nlrelx = h.parm.nlrelx;
@@ -4540,11 +4889,7 @@ void Engine::iteration_pre(int solve_phase) {
     // ASSPIC + RHSPIC + CFMATP + BC contributions fused: the CPUVEC buckets
     // of system initialisation, assembly, RHS, LHS and BC in one kernel
     phase(2);
-    launch(kAsmKernel[asm_variant], cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
-           d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, (const float4*)d_rec16.p,
-           (const uint16_t*)d_islot.p, (const float*)d_vpi.p, (const float*)d_vps.p, d_dmask.p, nf,
-           nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact, (const double*)nd.atmold,
-           d_vals32.p, (float)lm_d, (float)lm_o, d_glrow.p, d_gloff.p, d_gl.p);
+    launch_assembly(asm_variant, asm_staged);
     count();
     check_launch();
     if (lp_mode && solve_phase == 0) lp_before_solve();
@@ -5186,6 +5531,7 @@ static int run_until(Engine* e, int target_mode, int max_macro) {
 
 int engine_step(Engine* e, int* nactive) {
   run_until(e, 1, 1 << 30);
+  e->check_stage_err();
   int a = 0;
   for (int m = 0; m < e->nmem; ++m) a += (e->M[m]->status == 0);
   if (nactive) *nactive = a;
@@ -5221,6 +5567,7 @@ int engine_run(Engine* e, int max_steps, int* nsteps) {
   float ms = 0;
   CG_TRY(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
   e->gpu_ms += ms;
+  e->check_stage_err();
   if (nsteps) *nsteps = done;
   return 0;
 }
@@ -5469,11 +5816,7 @@ int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t
   }
   if (r == 0 || nrep < 1) return CATHY_GB300_EINVAL;
   auto go = [&]() {
-    kAsmKernel[e->asm_variant]<<<e->cbm16.nblk, kThreads, 0, e->st>>>(
-        e->cbm16.mem.p, e->cbm16.r0.p, e->cbm16.r1.p, e->d_act.p, e->d_ms.p, e->d_rowptr.p,
-        e->d_cols.p, e->d_inc_ptr.p, e->d_rec16.p, e->d_islot.p, e->d_vpi.p, e->d_vps.p,
-        e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold, e->d_vals32.p,
-        (float)e->lm_d, (float)e->lm_o, e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
+    e->launch_assembly(e->asm_variant, e->asm_staged);
   };
   go();  // warm
   CG_TRY(cudaEventRecord(e->ev0, e->st));
@@ -5492,7 +5835,7 @@ int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t
 // ---- schedule autotuner ----------------------------------------------------
 // Per (GPU, size class) cache of the schedules chosen by engine_autotune.
 static std::mutex g_tune_mu;
-static std::map<std::string, std::pair<int, int>> g_tune_cache;
+static std::map<std::string, std::array<int, 3>> g_tune_cache;
 
 static std::string tune_key(Engine* e, int64_t rows) {
   cudaDeviceProp prop;
@@ -5540,11 +5883,13 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
     if (nrep <= 0 && it != g_tune_cache.end()) {
-      e->asm_variant = it->second.first;
-      e->stream_per_sm = it->second.second;
+      e->asm_variant = it->second[0];
+      e->stream_per_sm = it->second[1];
+      e->asm_staged = it->second[2] != 0 && e->stage_smem > 0;
       e->graph_free();
       sched[0] = kAsmBlocks[e->asm_variant];
       sched[1] = e->stream_per_sm;
+      sched[2] = e->asm_staged ? 1 : 0;
       ms[0] = ms[1] = 0.0;
       return 0;
     }
@@ -5563,16 +5908,13 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
   };
   double best_a = 1e300, best_s = 1e300;
   int va = e->asm_variant, vs = e->stream_per_sm;
-  for (int v = 0; v < kAsmVariants; ++v) {
-    const double t = timed([&]() {
-      kAsmKernel[v]<<<e->cbm16.nblk, kThreads, 0, e->st>>>(
-          e->cbm16.mem.p, e->cbm16.r0.p, e->cbm16.r1.p, e->d_act.p, e->d_ms.p, e->d_rowptr.p,
-          e->d_cols.p, e->d_inc_ptr.p, e->d_rec16.p, e->d_islot.p, e->d_vpi.p, e->d_vps.p,
-          e->d_dmask.p, e->nf, e->nd.loc, e->nd.ifatm, e->nd.atmact, e->nd.atmold,
-          e->d_vals32.p, (float)e->lm_d, (float)e->lm_o, e->d_glrow.p, e->d_gloff.p, e->d_gl.p);
-    });
-    if (t < best_a) { best_a = t; va = v; }
-  }
+  bool sa = e->asm_staged;
+  for (int staged = 0; staged < (e->stage_smem > 0 ? 2 : 1); ++staged)
+    for (int v = 0; v < kAsmVariants; ++v) {
+      const double t = timed([&]() { e->launch_assembly(v, staged != 0); });
+      if (t < best_a) { best_a = t; va = v; sa = staged != 0; }
+    }
+  e->check_stage_err();
   const bool was_prof = e->prof;
   e->prof = false;
   for (int per : {4, 6, 8}) {
@@ -5582,30 +5924,70 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
   }
   e->prof = was_prof;
   e->asm_variant = va;
+  e->asm_staged = sa;
   e->stream_per_sm = vs;
   e->graph_free();
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[key] = {va, vs};
+    g_tune_cache[key] = {va, vs, sa ? 1 : 0};
   }
   sched[0] = kAsmBlocks[va];
   sched[1] = vs;
+  sched[2] = sa ? 1 : 0;
   ms[0] = best_a;
   ms[1] = best_s;
   return 0;
 }
 
-// Forces a schedule (assembly resident blocks per SM: 4, 5, 6 or 8; stream
-// SpMV resident blocks per SM: 1..8).
-int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm) {
+// Forces a schedule (assembly resident blocks per SM: 5, 6, 7 or 8, staged
+// or not; stream SpMV resident blocks per SM: 1..8).
+int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged) {
   int v = -1;
   for (int k = 0; k < kAsmVariants; ++k)
     if (kAsmBlocks[k] == asm_blocks) v = k;
   if (v < 0 || spmv_per_sm < 1 || spmv_per_sm > 8) return CATHY_GB300_EINVAL;
+  if (asm_staged && e->stage_smem == 0) return CATHY_GB300_EUNSUP;
   e->asm_variant = v;
+  e->asm_staged = asm_staged != 0;
   e->stream_per_sm = spmv_per_sm;
   e->graph_free();
   return 0;
+}
+
+// The FP32 Picard assembly, unstaged or staged, at variant v (resident
+// blocks per SM kAsmBlocks[v]) over the compacted 16-row map.
+void Engine::launch_assembly(int v, bool staged) {
+  if (staged && stage_smem > 0) {
+    next_smem = stage_smem;
+    launch(kStagedKernel[v], cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+           (const int4*)cbm16.ent.p, (const longlong2*)cbm16.eg.p, (const uint8_t*)d_act.p,
+           (const MemberScal*)d_ms.p, (const int32_t*)d_rowptr.p, (const int32_t*)d_cols.p,
+           (const int32_t*)d_inc_ptr.p, (const float4*)d_rec16.p, (const uint16_t*)d_islot.p,
+           (const float*)d_vpi.p, (const float*)d_vps.p, (const uint8_t*)d_dmask.p, nf,
+           (const int32_t*)nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact,
+           (const double*)nd.atmold, d_vals32.p, (float)lm_d, (float)lm_o,
+           (const int64_t*)d_glrow.p, (const uint8_t*)d_gloff.p, (const uint8_t*)d_gl.p,
+           stage_inc, stage_slot, stage_gl, d_stage_err.p);
+  } else {
+    launch(kAsmKernel[v], cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+           (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, (const int32_t*)d_rowptr.p,
+           (const int32_t*)d_cols.p, (const int32_t*)d_inc_ptr.p, (const float4*)d_rec16.p,
+           (const uint16_t*)d_islot.p, (const float*)d_vpi.p, (const float*)d_vps.p,
+           (const uint8_t*)d_dmask.p, nf, (const int32_t*)nd.loc, (const int8_t*)nd.ifatm,
+           (const double*)nd.atmact, (const double*)nd.atmold, d_vals32.p, (float)lm_d,
+           (float)lm_o, (const int64_t*)d_glrow.p, (const uint8_t*)d_gloff.p,
+           (const uint8_t*)d_gl.p);
+  }
+}
+
+// A staged-assembly block whose copies did not arrive in time set a flag
+// (its rows were not assembled): report it as an error.
+void Engine::check_stage_err() {
+  if (!d_stage_err.p) return;
+  int32_t f = 0;
+  d_stage_err.download(&f, 1, st);
+  CG_TRY(cudaStreamSynchronize(st));
+  if (f) throw std::string("staged assembly: a block's shared-memory copies did not complete");
 }
 
 // Phase timers (enable 1: on and zeroed, 0: off, -1: read only): out[0..9)

@@ -66,6 +66,12 @@ struct DBuf {
 struct BlockMap {
   int nblk = 0;
   DBuf<int32_t> mem, r0, r1;
+  // 16-row map of the FP32 Picard path only: per entry the ranges of its
+  // rows' incidence records [x, y) and matrix slots [z, w), and of their
+  // gather-list bytes [eg.x, eg.y) (copied whole into shared memory by the
+  // staged assembly)
+  DBuf<int4> ent;
+  DBuf<longlong2> eg;
 };
 
 class Engine;  // defined in engine.cu
@@ -95,7 +101,7 @@ int engine_timers(Engine* e, double* out, int n);
 int engine_attach_learned(Engine* e, void* model, int mode);
 int engine_learned_stats(Engine* e, double* out, int n);
 int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms);
-int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm);
+int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged);
 int engine_phase_timers(Engine* e, int enable, double* out, int n);
 int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t* rows);
 int engine_stats(Engine* e, double* gpu_ms, int64_t* launches,

@@ -41,6 +41,7 @@ struct MemberScal {
   int32_t hspatm, ieto, nlrelx;
   int32_t nnod, nstr, iopt, kslope;  // KSLOPE 0 (analytical) or 1 (chord slope)
   double tolksl;                      // chord slope once |PTNEW - PTOLD| >= TOLKSL
+  float deltat_rf, tetaf_f;           // 1/DELTAT and TETAF rounded to FP32 by the host
 };
 
 // per-member reduction accumulators (zeroed before use).  RD_DSTORE_C and

@@ -12,7 +12,8 @@ reference's method (FP64, IC(0)-PCG) on the same inputs, with the default
 FP32 inner tolerance (1e-8).  A config-1-style
 member (40x40 fractal DEM, 15 layers, per-cell lognormal Ks) is checked for
 the 6-hour rain pulse the same way.  The FP64 path (``precision=0``, IC(0))
-is checked iterate for iterate on two of the members.
+is checked iterate for iterate on two of the members, and the CPU-runnable
+hillslope configuration for its full simulated day on both paths.
 
 Tolerances, written where they are asserted:
   * heads: max |psi_gpu - psi_oracle| <= 1e-6 m at the end of the run;
@@ -151,3 +152,23 @@ def test_fp64_path_matches_oracle_iterate_for_iterate(oracle_runs):
         assert np.max(np.abs(g["p"] - o["p"])) <= 1e-8
         assert abs(g["steps"][-1]["cerras"] - o["steps"][-1]["cerras"]) <= \
             1e-8 * abs(o["steps"][-1]["cvin"])
+
+
+def test_config0_hillslope_full_day_matches_oracle():
+    """The CPU-runnable configuration for its stated simulated day (20x20
+    hillslope, 10 layers, constant rain, Picard + Jacobi-PCG, dt 1..600 s):
+    the FP64 path with the reference's preconditioner iterate for iterate,
+    and the benchmarked FP32 column-line path step for step."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from pycathy_wrapper_gb300.inputs import config0
+    o = O.Oracle(config0(tmax=DAY, precond=1))
+    assert o.run() > 0
+    orc = dict(rc=len(o.step_records()), p=o.state()[0], steps=o.step_records(),
+               iters=[r["iter"] for r in o.step_records()],
+               niter=[r["niter"] for r in o.iter_records()])
+    g64 = _gpu([config0(tmax=DAY, precond=1)], precision=0)[0]
+    assert g64["iters"] == orc["iters"] and g64["niter"] == orc["niter"]
+    _check_finished(g64, orc, head_tol=1e-8, mbe_tol=1e-8, iter_frac=1.0)
+    g32 = _gpu([config0(tmax=DAY, precond=2)], precision=1, graphs=True)[0]
+    _check_finished(g32, orc, head_tol=1e-6, mbe_tol=1e-7, iter_frac=0.99)

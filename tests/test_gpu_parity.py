@@ -342,22 +342,26 @@ def test_newton_chord_slope_kslope1_matches_oracle():
 
 def test_every_autotuner_schedule_gives_the_same_heads():
     """The autotuner picks the assembly kernel's resident blocks per SM (5,
-    6, 7, 8: the same arithmetic, so bit-identical systems) and the stream
-    SpMV's grid (which only regroups its FP32 dot products).  Every schedule
-    must reach the same heads; the tuner returns one of its candidates and
-    reuses its cached choice."""
+    6, 7, 8), whether its records, columns and gather lists are staged in
+    shared memory by bulk copies or read directly (the same arithmetic in
+    the same order, so bit-identical systems), and the stream SpMV's grid
+    (which only regroups its FP32 dot products).  Every schedule must reach
+    the same heads; the tuner returns one of its candidates and reuses its
+    cached choice."""
     from pycathy_wrapper_gb300.inputs import config2_members
     cases = config2_members(3, tmax=1800.0, min_cells=8, max_cells=14)
     for c in cases:
         c.parm.precond = 2
     runs = {}
-    for asm, spmv in ((5, 8), (6, 8), (7, 8), (8, 8), (6, 4), (6, 6)):
+    scheds = [(a, 8, st) for st in (False, True) for a in (5, 6, 7, 8)] + \
+        [(6, 4, False), (6, 6, False)]
+    for asm, spmv, staged in scheds:
         with _sim(cases, precision=1, graphs=True) as s:
-            s.set_schedule(asm, spmv)
+            s.set_schedule(asm, spmv, staged)
             s.run()
-            runs[(asm, spmv)] = [(s.state(m)[0], [r["iter"] for r in s.records(m)[1]])
-                                 for m in range(len(cases))]
-    base = runs[(6, 8)]
+            runs[(asm, spmv, staged)] = [(s.state(m)[0], [r["iter"] for r in s.records(m)[1]])
+                                         for m in range(len(cases))]
+    base = runs[(6, 8, False)]
     for key, got in runs.items():
         for (pa, ia), (pb, ib) in zip(base, got):
             assert ia == ib, key
@@ -371,6 +375,7 @@ def test_every_autotuner_schedule_gives_the_same_heads():
         assert t["asm_blocks"] in (5, 6, 7, 8) and t["spmv_blocks"] in (4, 6, 8)
         assert t["asm_ms"] > 0 and t["spmv_ms"] > 0
         again = s.autotune(0)  # the cached choice
-        assert (again["asm_blocks"], again["spmv_blocks"]) == (t["asm_blocks"], t["spmv_blocks"])
+        assert (again["asm_blocks"], again["spmv_blocks"], again["asm_staged"]) == \
+            (t["asm_blocks"], t["spmv_blocks"], t["asm_staged"])
         s.run()
         assert all(s.state(m)[3] == 1 for m in range(len(cases)))
