@@ -332,6 +332,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--only", default="",
+                    help="comma-separated member indices: run only these (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -360,6 +362,10 @@ def main():
                 "cpu_cores": cpu["cores"], "gpu_over_cpu": vg / cpu["value"], "unit": UNIT,
                 "gpu_s": devs}
     cases = _cases(args.members, rank, args.tmax, precond=2, world=ws)
+    if args.only:
+        # a profiling run on chosen members of the ensemble (e.g. one tail
+        # member), not a bench line
+        cases = [cases[int(k)] for k in args.only.split(",")]
     sim = Simulation(cases, precision=1, device=dev_id, graphs=not args.no_graphs)
     nodes_total = int(sum(s["n"] for s in sim.sizes))
     nnz_total = int(sum(s["nnz"] for s in sim.sizes))
@@ -473,7 +479,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded ensemble: fractal DEMs, sampled van Genuchten soils)",
-        "config": {"workload": f"ensemble{args.members}_day", "members": args.members,
+        "config": {"workload": (f"ensemble{args.members}_day" if not args.only else
+                                f"ensemble{args.members}_members_{args.only}_day"),
+                   "members": args.members,
                    "tmax_s": args.tmax, "nodes_total": nodes_total, "nnz_total": nnz_total,
                    "warmup": f"{args.warmup} partial passes ({args.warmup_member_steps} accepted "
                              f"steps per member)",

@@ -200,7 +200,8 @@ int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
  * preconditioner. */
 int32_t cathy_gb300_autotune(void* handle, int32_t nrep, int32_t* sched, double* ms);
 /* Forces a schedule: assembly blocks/SM in {5, 6, 7, 8}, SpMV blocks/SM in
- * 1..8, assembly staged (1) or not (0) (defaults 6, 8, 0);
+ * 1..8, assembly staged (1) or not (0) (defaults 6, 8, and staged on the
+ * FP32 Picard path);
  * CATHY_GB300_EUNSUP if staging is asked for and unavailable. */
 int32_t cathy_gb300_set_schedule(void* handle, int32_t asm_blocks, int32_t spmv_blocks,
                                  int32_t asm_staged);

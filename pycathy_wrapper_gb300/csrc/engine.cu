@@ -956,7 +956,7 @@ __device__ __forceinline__ void spmv_stream_run(
     const int32_t* bm_r1, const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
     const float* vals, const uint8_t* dmask, const float* x, float* y, const float* w, float* pv,
     const double* sc, double* acc, int acc_stride, double* alg_bytes, double* s_bytes,
-    const int32_t* kact, const int32_t* kfirst) {
+    const int32_t* kact, const int32_t* kfirst, const int4* ent) {
   __shared__ float sprod[kStreamWarps][16 * kGroup + 8];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   float* sp = sprod[wp];
@@ -997,8 +997,37 @@ __device__ __forceinline__ void spmv_stream_run(
       }
       b = g + delta;
     }
+    // The entry's member, rows and (with ent) slot range; then every load
+    // of the entry -- row pointers, the rows' own inputs, the slot vectors
+    // -- goes out in one round (the member's flag is checked before any
+    // result is formed).
     const int m = bm_mem[b];
-    if (!active[m]) continue;  // warp-uniform
+    const int r0 = bm_r0[b], r1 = bm_r1[b], nr = r1 - r0;
+    int sbeg = 0, send = 0;
+    if (ent) {
+      const int4 e4 = ent[b];
+      sbeg = e4.z;
+      send = e4.w;
+    }
+    const bool act_m = active[m] != 0;
+    const int rp = lane <= nr ? rowptr[r0 + lane] : 0;
+    if (!ent) {
+      sbeg = __shfl_sync(0xffffffffu, rp, 0);
+      send = __shfl_sync(0xffffffffu, rp, nr);
+    }
+    const int i = r0 + lane;
+    bool dm = false;
+    float xi = 0.0f, pold = 0.0f, yold = 0.0f, wi = 0.0f;
+    if (lane < nr) {
+      dm = dmask[i] != 0;
+      if (kMode != kSpmvResid) xi = x[i];
+      if (kMode == kSpmvUpd) {
+        pold = pv[i];
+        yold = y[i];
+      }
+      if (w) wi = w[i];
+    }
+    if (!act_m) continue;  // warp-uniform
     if (acc && m != cur) {
       if (cur >= 0) {
         const float a0 = warp_sum_t<float>(d0), a1 = warp_sum_t<float>(d1);
@@ -1010,11 +1039,6 @@ __device__ __forceinline__ void spmv_stream_run(
       d0 = d1 = 0.0f;
       cur = m;
     }
-    const int r0 = bm_r0[b], r1 = bm_r1[b], nr = r1 - r0;
-    // row pointers of the entry (lanes 0..nr)
-    const int rp = lane <= nr ? rowptr[r0 + lane] : 0;
-    const int sbeg = __shfl_sync(0xffffffffu, rp, 0);
-    const int send = __shfl_sync(0xffffffffu, rp, nr);
     if (alg_bytes && lane == 0)
       bytes += (long long)(send - sbeg) * 8 + nr * (kMode == kSpmvUpd ? 28 : (w ? 16 : 12));
     const float beta = kMode == kSpmvUpd ? sc_beta_f32(sc + (size_t)m * SC_N) : 0.0f;
@@ -1038,24 +1062,21 @@ __device__ __forceinline__ void spmv_stream_run(
     if (lane < nr) {
       float sum = 0.0f;
       for (int k = rlo; k < rhi; ++k) sum += sp[k - sbeg];
-      const int i = r0 + lane;
-      const bool dm = dmask[i] != 0;
       if (kMode == kSpmvResid) {
-        y[i] = dm ? 0.0f : w[i] - sum;
+        y[i] = dm ? 0.0f : wi - sum;
       } else {
-        const float xi = x[i];
         float yi = dm ? xi : sum;
         float pi = xi;
         if (kMode == kSpmvUpd) {
           if (beta != 0.0f) {
-            pi = xi + beta * pv[i];
-            yi = dm ? pi : yi + beta * y[i];
+            pi = xi + beta * pold;
+            yi = dm ? pi : yi + beta * yold;
           }
           pv[i] = pi;
         }
         y[i] = yi;
         d0 += pi * yi;
-        if (w) d1 += pi * w[i];
+        if (w) d1 += pi * wi;
       }
     }
     __syncwarp();
@@ -1103,15 +1124,19 @@ __device__ __forceinline__ void spmv_stream_run(
   }
 }
 
-template <int kMode>
-__global__ void __launch_bounds__(32 * kStreamWarps, 8)
+// kMinBlocks: resident blocks per SM the register budget must allow (8 for
+// the full batch, where a resident wave of 8 blocks per SM keeps the most
+// entries in flight; 2 for small work sets, which fill few SMs and run
+// faster without the spills of the 32-register budget)
+template <int kMode, int kMinBlocks = 8>
+__global__ void __launch_bounds__(32 * kStreamWarps, kMinBlocks)
 k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
               const uint8_t* active, const int32_t* __restrict__ rowptr,
               const int32_t* __restrict__ cols, const float* __restrict__ vals,
               const uint8_t* __restrict__ dmask, const float* __restrict__ x, float* y,
               const float* __restrict__ w, float* pv, const double* sc, double* acc,
               int acc_stride, double* alg_bytes, unsigned long long* lt, int lt_cap,
-              const int32_t* kact, const int32_t* kfirst) {
+              const int32_t* kact, const int32_t* kfirst, const int4* ent) {
   pdl_enter();
   __shared__ int s_slot;
   __shared__ double s_bytes;
@@ -1130,7 +1155,7 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
   }
   spmv_stream_run<kMode>(blockIdx.x, gridDim.x, nblk, bm_mem, bm_r0, bm_r1, active, rowptr, cols,
                          vals, dmask, x, y, w, pv, sc, acc, acc_stride, alg_bytes, &s_bytes, kact,
-                         kfirst);
+                         kfirst, ent);
   if (lt) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -2357,7 +2382,7 @@ struct AsmInc {  // one incidence's contribution to its row
 __device__ __forceinline__ void asm_incidence(int q, float4 r, int isl, float vp, int grp,
                                               float th, float rdt, float lm_d, float lm_o,
                                               float hh_i, float hl_i,
-                                              float (*sval)[64 * 4], float2 (*sh2)[kGroup],
+                                              float* sv, float2 (*sh2)[kGroup],
                                               float2 (*sk2)[kGroup], float (*sdp)[kGroup],
                                               float (*sds)[kGroup], AsmInc& a) {
   const int s0 = isl & 15, sa = (isl >> 4) & 15, sb = (isl >> 8) & 15, sc = (isl >> 12) & 15;
@@ -2367,9 +2392,9 @@ __device__ __forceinline__ void asm_incidence(int q, float4 r, int isl, float vp
   const float ve1 = r.w * e1;
   const float tk = th * kr;
   const float mo = ve1 * lm_o * rdt;
-  sval[grp][q * 4 + 1] = tk * r.x + mo;
-  sval[grp][q * 4 + 2] = tk * r.y + mo;
-  sval[grp][q * 4 + 3] = tk * r.z + mo;
+  sv[q * 4 + 1] = tk * r.x + mo;
+  sv[q * 4 + 2] = tk * r.y + mo;
+  sv[q * 4 + 3] = tk * r.z + mo;
   a.dacc += -tk * ((r.x + r.y) + r.z) + ve1 * lm_d * rdt;
   const float2 ha = sh2[grp][sa], hb = sh2[grp][sb], hc = sh2[grp][sc];
   const float da = (ha.x - hh_i) + (ha.y - hl_i);
@@ -2467,16 +2492,16 @@ __device__ __forceinline__ void assemble_f32_entry(
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
   AsmInc a{0.0f, 0.0f, 0.0f};
   if (i0 >= 0)
-    asm_incidence(lane, r0, i0, v0, grp, th, rdt, lm_d, lm_o, hh_i, hl_i, sval, sh2, sk2, sdp,
+    asm_incidence(lane, r0, i0, v0, grp, th, rdt, lm_d, lm_o, hh_i, hl_i, sval[grp], sh2, sk2, sdp,
                   sds, a);
   if (i1 >= 0)
-    asm_incidence(kGroup + lane, r1, i1, v1, grp, th, rdt, lm_d, lm_o, hh_i, hl_i, sval, sh2, sk2,
+    asm_incidence(kGroup + lane, r1, i1, v1, grp, th, rdt, lm_d, lm_o, hh_i, hl_i, sval[grp], sh2, sk2,
                   sdp, sds, a);
   for (int trip = 2; trip < ntrip; ++trip) {  // nodes with more than 32 incident elements
     const int q = trip * kGroup + lane;
     if (rowok && q < ninc)
       asm_incidence(q, rec16[p0 + q], islot[p0 + q], lm_o != 0.0f ? vpi[p0 + q] : 0.0f, grp, th,
-                    rdt, lm_d, lm_o, hh_i, hl_i, sval, sh2, sk2, sdp, sds, a);
+                    rdt, lm_d, lm_o, hh_i, hl_i, sval[grp], sh2, sk2, sdp, sds, a);
   }
   __syncwarp();
   const float dsum = group_sum<float>(a.dacc);
@@ -2574,20 +2599,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// try_wait suspends for a bounded time per call; this many calls (far more
-// than any copy of a few KB needs) and the block gives up and flags it
-constexpr int kStageSpin = 1 << 20;
+// A block waits at most this long (global timer, ns) for its copies of a
+// few KB, which land within microseconds; after that it flags the failure
+// and returns, and blocks that start after a failure do not wait at all.
+constexpr unsigned long long kStageWaitNs = 200000000ull;
 
 __host__ __device__ inline long long align16ll(long long x) { return (x + 15) & ~15LL; }
 // byte offsets of the staged arrays in dynamic shared memory, for the
-// largest ranges of any entry; off[5] is the total
-__host__ __device__ inline void asm_stage_layout(int cap_inc, int cap_slot, int cap_gl, int* off) {
+// largest ranges of any entry, then the rows' contribution arrays (4 floats
+// per incidence of the row with the most); off[6] is the total
+__host__ __device__ inline void asm_stage_layout(int cap_inc, int cap_slot, int cap_gl,
+                                                 int row_inc, int* off) {
   off[0] = 0;                                            // records, 16 B each
   off[1] = off[0] + cap_inc * 16;                        // slot nibbles
   off[2] = off[1] + (int)align16ll(cap_inc * 2 + 32);    // columns
   off[3] = off[2] + (int)align16ll(cap_slot * 4 + 32);   // gather offsets
   off[4] = off[3] + (int)align16ll(cap_slot + 32);       // gather lists
-  off[5] = off[4] + (int)align16ll(cap_gl + 32);
+  off[5] = off[4] + (int)align16ll(cap_gl + 32);         // contributions
+  off[6] = off[5] + kRowsPerBlock16 * row_inc * 4 * 4;
 }
 
 template <int kMinBlocks>
@@ -2603,22 +2632,27 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
                       const double* __restrict__ atmold, float* vals, float lm_d, float lm_o,
                       const int64_t* __restrict__ glrow, const uint8_t* __restrict__ gloff,
                       const uint8_t* __restrict__ gl, int cap_inc, int cap_slot, int cap_gl,
-                      int32_t* stage_err) {
+                      int row_inc, int32_t* stage_err) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ float sval[kRowsPerBlock16][64 * 4];
   __shared__ float2 sh2[kRowsPerBlock16][kGroup];
   __shared__ float2 sk2[kRowsPerBlock16][kGroup];
   __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
   __shared__ __align__(8) uint64_t mbar;
+  // the row's inputs that only its lane 0 (or its diagonal lane) uses, parked
+  // in shared memory once loaded so that they hold no registers meanwhile
+  __shared__ float srow[kRowsPerBlock16][6];
   pdl_enter();
   const int bid = blockIdx.x;
-  int off[6];
-  asm_stage_layout(cap_inc, cap_slot, cap_gl, off);
+  int off[7];
+  asm_stage_layout(cap_inc, cap_slot, cap_gl, row_inc, off);
   float4* srec = reinterpret_cast<float4*>(dsm + off[0]);
   uint16_t* sisl = reinterpret_cast<uint16_t*>(dsm + off[1]);
   int32_t* scol = reinterpret_cast<int32_t*>(dsm + off[2]);
   uint8_t* sglo = dsm + off[3];
   uint8_t* sgl = dsm + off[4];
+  // the rows' contributions at positions q*4 + t (incidence q, local node t),
+  // 4 * row_inc floats per row (row_inc = most incidences of any row)
+  float* svrow = reinterpret_cast<float*>(dsm + off[5]);
   if (threadIdx.x == 0) mbar_init(&mbar, 1);
   __syncthreads();
   const int m = bm_mem[bid];
@@ -2650,26 +2684,41 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   const float rdt = S.deltat_rf, th = S.tetaf_f;
   int s0 = 0, s1 = 0, p0 = 0, p1 = 0;
   int64_t gbase = 0;
-  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f;
-  bool atm_i = false, dm_i = false;
+  float hh_i = 0.0f, hl_i = 0.0f;
+  float et2i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f, fl_i = 0.0f;
   if (rowok) {
     s0 = rowptr[i];
     s1 = rowptr[i + 1];
     p0 = inc_ptr[i];
     p1 = inc_ptr[i + 1];
     gbase = glrow[i];
-    et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
-    vpl = vps[i] * lm_d;
-    dp_i = nf.dpsi[i]; ds_i = nf.dsw[i]; qn_i = nf.qneu[i];
-    atm_i = loc[i] < S.nnod && ifatm[i] == 0;
-    dm_i = dmask[i] != 0;
+    hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
+    if (lane == 0) {
+      et2i = nf.et2[i];
+      vpl = vps[i] * lm_d;
+      dp_i = nf.dpsi[i]; ds_i = nf.dsw[i]; qn_i = nf.qneu[i];
+      // 1: atmospheric Neumann surface node, 2: Dirichlet
+      fl_i = (float)((loc[i] < S.nnod && ifatm[i] == 0 ? 1 : 0) | (dmask[i] != 0 ? 2 : 0));
+    }
   }
   if (!iter) return;  // block-uniform; no copy was issued
-  bool ready = false;
-  for (int k = 0; k < kStageSpin && !ready; ++k) ready = mbar_try_wait(&mbar, 0);
+  bool ready = mbar_try_wait(&mbar, 0);
+  if (!ready) {
+    const unsigned long long t0 = gtimer();
+    while (!ready && *(volatile int32_t*)stage_err == 0 && gtimer() - t0 < kStageWaitNs)
+      ready = mbar_try_wait(&mbar, 0);
+  }
   if (!ready) {
     if (threadIdx.x == 0) atomicExch(stage_err, 1);
     return;
+  }
+  if (lane == 0) {
+    srow[grp][0] = vpl * et2i * rdt;  // the lumped storage term of the diagonal
+    srow[grp][1] = vpl;
+    srow[grp][2] = dp_i;
+    srow[grp][3] = ds_i;
+    srow[grp][4] = qn_i;
+    srow[grp][5] = fl_i;
   }
   const int rlen = s1 - s0, ninc = p1 - p0;
   int col = -1, ga = 0, gb = 0;
@@ -2695,7 +2744,7 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     if (rowok && q < ninc)
       asm_incidence(q, srec[p0 - e4.x + q], sisl[p0 + q - isl0],
                     lm_o != 0.0f ? vpi[p0 + q] : 0.0f, grp, th, rdt, lm_d, lm_o, hh_i, hl_i,
-                    sval, sh2, sk2, sdp, sds, a);
+                    svrow + grp * 4 * row_inc, sh2, sk2, sdp, sds, a);
   }
   __syncwarp();
   const float dsum = group_sum<float>(a.dacc);
@@ -2705,24 +2754,26 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   if (col >= 0) {
     float lhs;
     if (col == i) {
-      lhs = dsum + vpl * et2i * rdt;
+      lhs = dsum + srow[grp][0];
     } else {
       lhs = 0.0f;
       const uint8_t* g8 = sgl + (gbase - gl0);
-      for (int u = ga; u < gb; ++u) lhs += sval[grp][g8[u]];
+      const float* sv = svrow + grp * 4 * row_inc;
+      for (int u = ga; u < gb; ++u) lhs += sv[g8[u]];
     }
     vals[s0 + lane] = lhs;
   }
   if (lane == 0) {
-    rhs -= (msum * dp_i + vpl * ds_i) * rdt;
+    rhs -= (msum * srow[grp][2] + srow[grp][1] * srow[grp][3]) * rdt;
     nf.xt5[i] = rhs;
-    float f = qn_i;
-    if (atm_i) {
+    float f = srow[grp][4];
+    const int fl = (int)srow[grp][5];
+    if (fl & 1) {
       const double thd = S.tetaf;
       f += (thd == 1.0) ? (float)atmact[i]
                         : (float)(thd * atmact[i] + (1.0 - thd) * atmold[i]);
     }
-    nf.rhs[i] = dm_i ? 0.0f : rhs + f;
+    nf.rhs[i] = (fl & 2) ? 0.0f : rhs + f;
   }
 }
 using StagedKernel = decltype(&k_assemble_staged_f32<6>);
@@ -3444,9 +3495,11 @@ struct Engine {
   // staged assembly: largest incidence, slot and gather-list ranges of a
   // 16-row entry, and the device flag a block sets if its staging wait
   // runs out
-  int stage_inc = 0, stage_slot = 0, stage_gl = 0;
+  int stage_inc = 0, stage_slot = 0, stage_gl = 0, stage_row_inc = 0;
   DBuf<int32_t> d_stage_err;
-  bool asm_staged = false;  // the autotuner's choice between the two assemblies
+  // the autotuner's choice between the two assemblies; staged by default
+  // where it is available (measured faster at 6 blocks/SM on the ensembles)
+  bool asm_staged = true;
   size_t stage_smem = 0;    // dynamic shared memory of the staged assembly (0: unavailable)
   void launch_assembly(int variant, bool staged);
   void check_stage_err();
@@ -3522,6 +3575,9 @@ struct Engine {
   }
   int grid_persist(int nblk) const { return std::max(1, std::min(nblk, persist_blocks)); }
   int grid_spmv(int nblk) const { return std::max(1, std::min(nblk, 2 * persist_blocks)); }
+  // work sets of at most two map entries per warp of one resident wave
+  // take the stream SpMV with the larger register budget
+  bool small_stream() const { return cbm16.nblk <= 2 * kStreamWarps * nsm; }
   int grid_stream() const {
     // one warp per map entry up to one resident wave of 256-thread blocks
     return std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps,
@@ -3529,27 +3585,31 @@ struct Engine {
   }
   // q = A p with the fused dots p.q, p.r (FP32 stream kernel)
   void spmv_f32(const float* vals, const float* p, float* q, const float* r) {
-    launch(k_spmv_stream<kSpmvPlain>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+    launch(small_stream() ? k_spmv_stream<kSpmvPlain, 2> : k_spmv_stream<kSpmvPlain, 8>,
+           grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
            (float*)nullptr, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
            prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap,
-           (const int32_t*)d_kact.p, (const int32_t*)d_kact.p);
+           (const int32_t*)d_kact.p, (const int32_t*)d_kact.p, (const int4*)cbm16.ent.p);
   }
   // r = b - A x (masked)
   void resid_f32(const float* vals, const float* x, const float* b, float* r) {
-    launch(k_spmv_stream<kSpmvResid>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+    launch(small_stream() ? k_spmv_stream<kSpmvResid, 2> : k_spmv_stream<kSpmvResid, 8>,
+           grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, x, r, b,
            (float*)nullptr, (const double*)d_sc.p, (double*)nullptr, (int)SC_N,
            (double*)nullptr, (unsigned long long*)nullptr, 0, (const int32_t*)d_kact.p,
-           (const int32_t*)d_kact.p);
+           (const int32_t*)d_kact.p, (const int4*)cbm16.ent.p);
   }
   // p = z + beta p, q = A z + beta q (= A p) with the fused dots p.q, p.r
   void spmv_upd_f32(const float* vals, const float* z, float* p, float* q, const float* r) {
-    launch(k_spmv_stream<kSpmvUpd>, grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
+    launch(small_stream() ? k_spmv_stream<kSpmvUpd, 2> : k_spmv_stream<kSpmvUpd, 8>,
+           grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
            cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, z, q, r,
            p, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
            prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap,
-           (const int32_t*)d_kact.p, (const int32_t*)(d_kact.p + nmem + 2));
+           (const int32_t*)d_kact.p, (const int32_t*)(d_kact.p + nmem + 2),
+           (const int4*)cbm16.ent.p);
   }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class VT>
@@ -4202,15 +4262,16 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         stage_inc = std::max(stage_inc, h_incptr[b] - h_incptr[a]);
         stage_slot = std::max(stage_slot, h_rowptr[b] - h_rowptr[a]);
         stage_gl = std::max(stage_gl, (int)(g1 - h_glrow[a]));
+        for (int r = a; r < b; ++r) stage_row_inc = std::max(stage_row_inc, h_incptr[r + 1] - h_incptr[r]);
       }
     if ((int)ent.size() != bm16.nblk) throw std::string("staged assembly: entry count mismatch");
     bm16.ent.alloc(ent.size()); bm16.ent.upload(ent.data(), ent.size(), st);
     bm16.eg.alloc(eg.size()); bm16.eg.upload(eg.data(), eg.size(), st);
     d_stage_err.alloc(1);
     d_stage_err.zero(st);
-    int off[6];
-    asm_stage_layout(stage_inc, stage_slot, stage_gl, off);
-    stage_smem = (size_t)off[5];
+    int off[7];
+    asm_stage_layout(stage_inc, stage_slot, stage_gl, stage_row_inc, off);
+    stage_smem = (size_t)off[6];
     if (stage_smem > (size_t)48 * 1024) {
       // above the default dynamic limit: opt in, or leave the staged
       // assembly off if it does not fit next to the static arrays
@@ -5967,7 +6028,7 @@ void Engine::launch_assembly(int v, bool staged) {
            (const int32_t*)nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact,
            (const double*)nd.atmold, d_vals32.p, (float)lm_d, (float)lm_o,
            (const int64_t*)d_glrow.p, (const uint8_t*)d_gloff.p, (const uint8_t*)d_gl.p,
-           stage_inc, stage_slot, stage_gl, d_stage_err.p);
+           stage_inc, stage_slot, stage_gl, stage_row_inc, d_stage_err.p);
   } else {
     launch(kAsmKernel[v], cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
            (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, (const int32_t*)d_rowptr.p,
