@@ -369,6 +369,9 @@ def main():
     sim = Simulation(cases, precision=1, device=dev_id, graphs=not args.no_graphs)
     nodes_total = int(sum(s["n"] for s in sim.sizes))
     nnz_total = int(sum(s["nnz"] for s in sim.sizes))
+    # q = A p with the dots p.q, p.r: values and columns, then per row its
+    # pointer, p, q and r
+    spmv_full_bytes = 8.0 * nnz_total + 16.0 * nodes_total
     # warm-up: partial passes of the same workload (every member's first
     # time steps: every kernel runs, the graphs of the early member sets are
     # built); untimed
@@ -495,6 +498,7 @@ def main():
         "gpu_launches": launches,
         "nl_iterations": nl, "lin_iterations": lin,
         "members_finished": int(sum(1 for f in fin if f == 1)),
+        "members_failed": [i for i, f in enumerate(fin) if f == 2],
         "wall_s_timed": wall,
         "roofline": {"bound": "hbm", "kernel": "k_spmv_stream",
                      "timing": "per launch on the device clock (first block start to last "
@@ -510,6 +514,14 @@ def main():
             "achieved": asm_bytes / 1e9 / (asm_ms / 1e3), "peak": peak, "unit": "GB/s",
             "frac": asm_bytes / 1e9 / (asm_ms / 1e3) / peak, "peak_source": peak_kind,
             "alg_bytes_per_launch": asm_bytes, "rows": asm_rows, "ms_per_launch": asm_ms},
+        "roofline_spmv_full_batch": {
+            "bound": "hbm", "kernel": "k_spmv_stream<kSpmvPlain>",
+            "timing": f"the autotuner's best mean over 10 launches on all {args.members} members "
+                      f"after their first 5 steps, CUDA events",
+            "achieved": spmv_full_bytes / 1e9 / (sched["spmv_ms"] / 1e3), "peak": peak,
+            "unit": "GB/s", "frac": spmv_full_bytes / 1e9 / (sched["spmv_ms"] / 1e3) / peak,
+            "peak_source": peak_kind, "alg_bytes_per_launch": spmv_full_bytes,
+            "ms_per_launch": sched["spmv_ms"]},
         "cpu_baseline": cpu,
         "cpu_baseline_pycathy_workers": cpu_pyc,
         "same_sample_gpu_vs_cpu": like,

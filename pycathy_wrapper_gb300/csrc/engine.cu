@@ -2376,6 +2376,16 @@ __global__ void k_vps(int n, const int32_t* inc_ptr, const int32_t* inc,
 // The device function is one 16-row map entry bid (block-uniform early
 // exits, no block barrier).
 constexpr int kGlWords = 3 * 64 / 4;  // gather-list words of a row (<= 64 incidences)
+// The row's diagonal (slot sum + lumped storage term) and its RHS after the
+// storage-change terms, in explicit fused operations: both assemblies
+// round them the same way.
+__device__ __forceinline__ float asm_diag(float dsum, float vpl_et2, float rdt) {
+  return fmaf(vpl_et2, rdt, dsum);
+}
+__device__ __forceinline__ float asm_rhs(float rhs, float msum, float dp, float vpl, float ds,
+                                         float rdt) {
+  return fmaf(-fmaf(msum, dp, vpl * ds), rdt, rhs);
+}
 struct AsmInc {  // one incidence's contribution to its row
   float dacc, rp, msum;
 };
@@ -2511,7 +2521,7 @@ __device__ __forceinline__ void assemble_f32_entry(
   if (col >= 0) {
     float lhs;
     if (col == i) {
-      lhs = dsum + vpl * et2i * rdt;
+      lhs = asm_diag(dsum, vpl * et2i, rdt);
     } else {
       lhs = 0.0f;
       const uint8_t* g8 = reinterpret_cast<const uint8_t*>(sgl[grp]);
@@ -2520,7 +2530,7 @@ __device__ __forceinline__ void assemble_f32_entry(
     vals[s0 + lane] = lhs;
   }
   if (lane == 0) {
-    rhs -= (msum * dp_i + vpl * ds_i) * rdt;
+    rhs = asm_rhs(rhs, msum, dp_i, vpl, ds_i, rdt);
     nf.xt5[i] = rhs;
     float f = qn_i;
     if (atm_i) {
@@ -2589,13 +2599,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// (the suspend-time hint, in ns, lets a waiting thread sleep until the
+// phase completes instead of spinning on issue slots)
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
       "selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(1000000u)
       : "memory");
   return ok != 0;
 }
@@ -2638,9 +2650,6 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   __shared__ float2 sk2[kRowsPerBlock16][kGroup];
   __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
   __shared__ __align__(8) uint64_t mbar;
-  // the row's inputs that only its lane 0 (or its diagonal lane) uses, parked
-  // in shared memory once loaded so that they hold no registers meanwhile
-  __shared__ float srow[kRowsPerBlock16][6];
   pdl_enter();
   const int bid = blockIdx.x;
   int off[7];
@@ -2684,22 +2693,19 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   const float rdt = S.deltat_rf, th = S.tetaf_f;
   int s0 = 0, s1 = 0, p0 = 0, p1 = 0;
   int64_t gbase = 0;
-  float hh_i = 0.0f, hl_i = 0.0f;
-  float et2i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f, fl_i = 0.0f;
+  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f;
+  bool atm_i = false, dm_i = false;
   if (rowok) {
     s0 = rowptr[i];
     s1 = rowptr[i + 1];
     p0 = inc_ptr[i];
     p1 = inc_ptr[i + 1];
     gbase = glrow[i];
-    hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
-    if (lane == 0) {
-      et2i = nf.et2[i];
-      vpl = vps[i] * lm_d;
-      dp_i = nf.dpsi[i]; ds_i = nf.dsw[i]; qn_i = nf.qneu[i];
-      // 1: atmospheric Neumann surface node, 2: Dirichlet
-      fl_i = (float)((loc[i] < S.nnod && ifatm[i] == 0 ? 1 : 0) | (dmask[i] != 0 ? 2 : 0));
-    }
+    et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
+    vpl = vps[i] * lm_d;
+    dp_i = nf.dpsi[i]; ds_i = nf.dsw[i]; qn_i = nf.qneu[i];
+    atm_i = loc[i] < S.nnod && ifatm[i] == 0;
+    dm_i = dmask[i] != 0;
   }
   if (!iter) return;  // block-uniform; no copy was issued
   bool ready = mbar_try_wait(&mbar, 0);
@@ -2711,14 +2717,6 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   if (!ready) {
     if (threadIdx.x == 0) atomicExch(stage_err, 1);
     return;
-  }
-  if (lane == 0) {
-    srow[grp][0] = vpl * et2i * rdt;  // the lumped storage term of the diagonal
-    srow[grp][1] = vpl;
-    srow[grp][2] = dp_i;
-    srow[grp][3] = ds_i;
-    srow[grp][4] = qn_i;
-    srow[grp][5] = fl_i;
   }
   const int rlen = s1 - s0, ninc = p1 - p0;
   int col = -1, ga = 0, gb = 0;
@@ -2754,7 +2752,7 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
   if (col >= 0) {
     float lhs;
     if (col == i) {
-      lhs = dsum + srow[grp][0];
+      lhs = asm_diag(dsum, vpl * et2i, rdt);
     } else {
       lhs = 0.0f;
       const uint8_t* g8 = sgl + (gbase - gl0);
@@ -2764,16 +2762,15 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     vals[s0 + lane] = lhs;
   }
   if (lane == 0) {
-    rhs -= (msum * srow[grp][2] + srow[grp][1] * srow[grp][3]) * rdt;
+    rhs = asm_rhs(rhs, msum, dp_i, vpl, ds_i, rdt);
     nf.xt5[i] = rhs;
-    float f = srow[grp][4];
-    const int fl = (int)srow[grp][5];
-    if (fl & 1) {
+    float f = qn_i;
+    if (atm_i) {
       const double thd = S.tetaf;
       f += (thd == 1.0) ? (float)atmact[i]
                         : (float)(thd * atmact[i] + (1.0 - thd) * atmold[i]);
     }
-    nf.rhs[i] = (fl & 2) ? 0.0f : rhs + f;
+    nf.rhs[i] = dm_i ? 0.0f : rhs + f;
   }
 }
 using StagedKernel = decltype(&k_assemble_staged_f32<6>);
