@@ -2616,6 +2616,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // and returns, and blocks that start after a failure do not wait at all.
 constexpr unsigned long long kStageWaitNs = 200000000ull;
 
+// Waits (all 32 lanes of the calling warp together) for the given phase of
+// bar, at most kStageWaitNs or until another block has flagged a failure;
+// the result is the same in every lane.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity,
+                                               const int32_t* stage_err) {
+  bool ready = mbar_try_wait(bar, parity);
+  if (__all_sync(0xffffffffu, ready)) return true;
+  const unsigned long long t0 = gtimer();
+  for (;;) {
+    if (!ready) ready = mbar_try_wait(bar, parity);
+    if (__all_sync(0xffffffffu, ready)) return true;
+    const bool stop = *(volatile const int32_t*)stage_err != 0 || gtimer() - t0 >= kStageWaitNs;
+    if (__any_sync(0xffffffffu, stop)) return false;
+  }
+}
+
 __host__ __device__ inline long long align16ll(long long x) { return (x + 15) & ~15LL; }
 // byte offsets of the staged arrays in dynamic shared memory, for the
 // largest ranges of any entry, then the rows' contribution arrays (4 floats
@@ -2708,13 +2724,8 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     dm_i = dmask[i] != 0;
   }
   if (!iter) return;  // block-uniform; no copy was issued
-  bool ready = mbar_try_wait(&mbar, 0);
-  if (!ready) {
-    const unsigned long long t0 = gtimer();
-    while (!ready && *(volatile int32_t*)stage_err == 0 && gtimer() - t0 < kStageWaitNs)
-      ready = mbar_try_wait(&mbar, 0);
-  }
-  if (!ready) {
+  const bool ready = mbar_wait_warp(&mbar, 0, stage_err);
+  if (__syncthreads_or(!ready)) {
     if (threadIdx.x == 0) atomicExch(stage_err, 1);
     return;
   }
@@ -3494,11 +3505,12 @@ struct Engine {
   // runs out
   int stage_inc = 0, stage_slot = 0, stage_gl = 0, stage_row_inc = 0;
   DBuf<int32_t> d_stage_err;
-  // the autotuner's choice between the two assemblies; staged by default
-  // where it is available (measured faster at 6 blocks/SM on the ensembles)
-  bool asm_staged = true;
+  // the autotuner's choice between the assemblies (0 direct loads, 1
+  // staged); staged by default where it is available (measured faster at 6
+  // blocks/SM on the ensembles)
+  int asm_staged = 1;
   size_t stage_smem = 0;    // dynamic shared memory of the staged assembly (0: unavailable)
-  void launch_assembly(int variant, bool staged);
+  void launch_assembly(int variant, int mode);
   void check_stage_err();
   int stream_per_sm = 8;
   int nsm = 152;
@@ -4062,8 +4074,9 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_nodal[ND_ATMACT].upload(h_atmact.data(), N, st);
   d_nodal[ND_ATMOLD].upload(h_atmold.data(), N, st);
   d_sdir.alloc(N); d_sdir.upload(h_sdir.data(), N, st);
-  d_dmask.alloc(N); d_dmask.zero(st);
-  d_ifatm.alloc(N); d_ifatm.upload(h_ifatm.data(), N, st);
+  // (+4: the pipelined assembly copies these byte arrays as aligned words)
+  d_dmask.alloc(N + 4); d_dmask.zero(st);
+  d_ifatm.alloc(N + 4); d_ifatm.zero(st); d_ifatm.upload(h_ifatm.data(), N, st);
   d_ifatmp.alloc(N); d_ifatmp.upload(h_ifatmp.data(), N, st);
   d_tet.alloc(NT); d_tet.upload(h_tet.data(), NT, st);
   d_rowptr.alloc(N + 1); d_rowptr.upload(h_rowptr.data(), N + 1, st);
@@ -5894,6 +5907,11 @@ int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t
 // Per (GPU, size class) cache of the schedules chosen by engine_autotune.
 static std::mutex g_tune_mu;
 static std::map<std::string, std::array<int, 3>> g_tune_cache;
+// resident blocks per SM of assembly variant v (either mode)
+static int asm_blocks_of(int v, int mode) {
+  (void)mode;
+  return kAsmBlocks[v];
+}
 
 static std::string tune_key(Engine* e, int64_t rows) {
   cudaDeviceProp prop;
@@ -5943,11 +5961,11 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
     if (nrep <= 0 && it != g_tune_cache.end()) {
       e->asm_variant = it->second[0];
       e->stream_per_sm = it->second[1];
-      e->asm_staged = it->second[2] != 0 && e->stage_smem > 0;
+      e->asm_staged = it->second[2];
       e->graph_free();
-      sched[0] = kAsmBlocks[e->asm_variant];
+      sched[0] = asm_blocks_of(e->asm_variant, e->asm_staged);
       sched[1] = e->stream_per_sm;
-      sched[2] = e->asm_staged ? 1 : 0;
+      sched[2] = e->asm_staged;
       ms[0] = ms[1] = 0.0;
       return 0;
     }
@@ -5965,12 +5983,12 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
     return (double)t / nrep;
   };
   double best_a = 1e300, best_s = 1e300;
-  int va = e->asm_variant, vs = e->stream_per_sm;
-  bool sa = e->asm_staged;
-  for (int staged = 0; staged < (e->stage_smem > 0 ? 2 : 1); ++staged)
+  int va = e->asm_variant, vs = e->stream_per_sm, sa = e->asm_staged;
+  const int modes = e->stage_smem > 0 ? 2 : 1;
+  for (int mode = 0; mode < modes; ++mode)
     for (int v = 0; v < kAsmVariants; ++v) {
-      const double t = timed([&]() { e->launch_assembly(v, staged != 0); });
-      if (t < best_a) { best_a = t; va = v; sa = staged != 0; }
+      const double t = timed([&]() { e->launch_assembly(v, mode); });
+      if (t < best_a) { best_a = t; va = v; sa = mode; }
     }
   e->check_stage_err();
   const bool was_prof = e->prof;
@@ -5987,26 +6005,27 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
   e->graph_free();
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[key] = {va, vs, sa ? 1 : 0};
+    g_tune_cache[key] = {va, vs, sa};
   }
-  sched[0] = kAsmBlocks[va];
+  sched[0] = asm_blocks_of(va, sa);
   sched[1] = vs;
-  sched[2] = sa ? 1 : 0;
+  sched[2] = sa;
   ms[0] = best_a;
   ms[1] = best_s;
   return 0;
 }
 
-// Forces a schedule (assembly resident blocks per SM: 5, 6, 7 or 8, staged
-// or not; stream SpMV resident blocks per SM: 1..8).
+// Forces a schedule (assembly mode 0 direct loads or 1 staged, resident
+// blocks per SM 5, 6, 7 or 8; stream SpMV resident blocks per SM: 1..8).
 int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged) {
   int v = -1;
+  if (asm_staged < 0 || asm_staged > 1) return CATHY_GB300_EINVAL;
   for (int k = 0; k < kAsmVariants; ++k)
     if (kAsmBlocks[k] == asm_blocks) v = k;
   if (v < 0 || spmv_per_sm < 1 || spmv_per_sm > 8) return CATHY_GB300_EINVAL;
-  if (asm_staged && e->stage_smem == 0) return CATHY_GB300_EUNSUP;
+  if (asm_staged == 1 && e->stage_smem == 0) return CATHY_GB300_EUNSUP;
   e->asm_variant = v;
-  e->asm_staged = asm_staged != 0;
+  e->asm_staged = asm_staged;
   e->stream_per_sm = spmv_per_sm;
   e->graph_free();
   return 0;
@@ -6014,8 +6033,8 @@ int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_stag
 
 // The FP32 Picard assembly, unstaged or staged, at variant v (resident
 // blocks per SM kAsmBlocks[v]) over the compacted 16-row map.
-void Engine::launch_assembly(int v, bool staged) {
-  if (staged && stage_smem > 0) {
+void Engine::launch_assembly(int v, int mode) {
+  if (mode == 1 && stage_smem > 0) {
     next_smem = stage_smem;
     launch(kStagedKernel[v], cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
            (const int4*)cbm16.ent.p, (const longlong2*)cbm16.eg.p, (const uint8_t*)d_act.p,

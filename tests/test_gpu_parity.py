@@ -341,10 +341,10 @@ def test_newton_chord_slope_kslope1_matches_oracle():
 
 
 def test_every_autotuner_schedule_gives_the_same_heads():
-    """The autotuner picks the assembly kernel's resident blocks per SM (5,
-    6, 7, 8), whether its records, columns and gather lists are staged in
-    shared memory by bulk copies or read directly (the same arithmetic in
-    the same order, so bit-identical systems), and the stream SpMV's grid
+    """The autotuner picks the assembly kernel's resident blocks per SM and
+    whether its records, columns and gather lists are read directly or
+    staged in shared memory by bulk copies (the same arithmetic in the same
+    order, so bit-identical systems), and the stream SpMV's grid
     (which only regroups its FP32 dot products).  Every schedule must reach
     the same heads; the tuner returns one of its candidates and reuses its
     cached choice."""
@@ -353,15 +353,15 @@ def test_every_autotuner_schedule_gives_the_same_heads():
     for c in cases:
         c.parm.precond = 2
     runs = {}
-    scheds = [(a, 8, st) for st in (False, True) for a in (5, 6, 7, 8)] + \
-        [(6, 4, False), (6, 6, False)]
+    scheds = [(a, 8, st) for st in (0, 1) for a in (5, 6, 7, 8)] + \
+        [(6, 4, 0), (6, 6, 0)]
     for asm, spmv, staged in scheds:
         with _sim(cases, precision=1, graphs=True) as s:
             s.set_schedule(asm, spmv, staged)
             s.run()
             runs[(asm, spmv, staged)] = [(s.state(m)[0], [r["iter"] for r in s.records(m)[1]])
                                          for m in range(len(cases))]
-    base = runs[(6, 8, False)]
+    base = runs[(6, 8, 0)]
     for key, got in runs.items():
         for (pa, ia), (pb, ib) in zip(base, got):
             assert ia == ib, key
