@@ -237,9 +237,10 @@ class Simulation:
 
     def autotune(self, nrep: int = 10):
         """Time the assembly (mode 0: inputs read directly, 1: staged in
-        shared memory by bulk copies; resident blocks per SM) and
-        stream-SpMV schedules on the running members and keep the fastest
-        (cached per GPU and size class; nrep <= 0 reuses a cached choice).
+        shared memory by bulk copies, 2: staged with 8 lanes per row;
+        resident blocks per SM) and stream-SpMV schedules on the running
+        members and keep the fastest (cached per GPU and size class;
+        nrep <= 0 reuses a cached choice).
         Returns dict(asm_blocks, spmv_blocks, asm_staged (the mode), asm_ms,
         spmv_ms)."""
         sc = (C.c_int32 * 3)()

@@ -2784,6 +2784,185 @@ k_assemble_staged_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t
     nf.rhs[i] = dm_i ? 0.0f : rhs + f;
   }
 }
+// The staged assembly with 8 lanes per row (128 threads, one 16-row entry
+// per block, 4 rows per warp): a row's ~24 incidences take 3 full rounds of
+// 8 lanes instead of 2 rounds of 16 at 75 % use, each lane owns the slots
+// lane and lane + 8, and the per-warp work (entry read, staging wait, row
+// epilogue, 3-level shuffle sums) is shared by 4 rows instead of 2.  Same
+// arithmetic in the same order as the 16-lane kernels: bit-identical.
+constexpr int kLanes8 = 8;
+constexpr int kThreads8 = kRowsPerBlock16 * kLanes8;
+template <class T>
+__device__ __forceinline__ T group8_sum(T v) {
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kThreads8, kMinBlocks)
+k_assemble_staged8_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                       const int4* __restrict__ bm_ent, const longlong2* __restrict__ bm_eg,
+                       const uint8_t* act, const MemberScal* ms, const int32_t* rowptr,
+                       const int32_t* cols, const int32_t* inc_ptr,
+                       const float4* __restrict__ rec16, const uint16_t* __restrict__ islot,
+                       const float* __restrict__ vpi, const float* __restrict__ vps,
+                       const uint8_t* dmask, NodalF nf, const int32_t* __restrict__ loc,
+                       const int8_t* __restrict__ ifatm, const double* __restrict__ atmact,
+                       const double* __restrict__ atmold, float* vals, float lm_d, float lm_o,
+                       const int64_t* __restrict__ glrow, const uint8_t* __restrict__ gloff,
+                       const uint8_t* __restrict__ gl, int cap_inc, int cap_slot, int cap_gl,
+                       int row_inc, int32_t* stage_err) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ float2 sh2[kRowsPerBlock16][kGroup];
+  __shared__ float2 sk2[kRowsPerBlock16][kGroup];
+  __shared__ float sdp[kRowsPerBlock16][kGroup], sds[kRowsPerBlock16][kGroup];
+  __shared__ __align__(8) uint64_t mbar;
+  pdl_enter();
+  const int bid = blockIdx.x;
+  int off[7];
+  asm_stage_layout(cap_inc, cap_slot, cap_gl, row_inc, off);
+  const float4* srec = reinterpret_cast<const float4*>(dsm + off[0]);
+  const uint16_t* sisl = reinterpret_cast<const uint16_t*>(dsm + off[1]);
+  const int32_t* scol = reinterpret_cast<const int32_t*>(dsm + off[2]);
+  const uint8_t* sglo = dsm + off[3];
+  const uint8_t* sgl = dsm + off[4];
+  float* svrow = reinterpret_cast<float*>(dsm + off[5]);
+  if (threadIdx.x == 0) mbar_init(&mbar, 1);
+  __syncthreads();
+  const int m = bm_mem[bid];
+  const int rbeg = bm_r0[bid], rend = bm_r1[bid];
+  const int4 e4 = bm_ent[bid];
+  const longlong2 eg = bm_eg[bid];
+  const uint8_t am = act[m];
+  const bool iter = (am & ACT_ITER) != 0;
+  const int isl0 = e4.x & ~7, col0 = e4.z & ~3, glo0 = e4.z & ~15;
+  const long long gl0 = eg.x & ~15LL;
+  if (threadIdx.x == 0 && iter) {
+    const uint32_t b0 = (uint32_t)(e4.y - e4.x) * 16u;
+    const uint32_t b1 = (uint32_t)(align16ll(2LL * e4.y) - 2LL * isl0);
+    const uint32_t b2 = (uint32_t)(align16ll(4LL * e4.w) - 4LL * col0);
+    const uint32_t b3 = (uint32_t)(align16ll((long long)e4.w) - glo0);
+    const uint32_t b4 = (uint32_t)(align16ll(eg.y) - gl0);
+    mbar_expect_tx(&mbar, b0 + b1 + b2 + b3 + b4);
+    if (b0) bulk_g2s(dsm + off[0], rec16 + e4.x, b0, &mbar);
+    if (b1) bulk_g2s(dsm + off[1], islot + isl0, b1, &mbar);
+    if (b2) bulk_g2s(dsm + off[2], cols + col0, b2, &mbar);
+    if (b3) bulk_g2s(dsm + off[3], gloff + glo0, b3, &mbar);
+    if (b4) bulk_g2s(dsm + off[4], gl + gl0, b4, &mbar);
+  }
+  const int grp = threadIdx.x / kLanes8, lane = threadIdx.x % kLanes8;
+  const int i = rbeg + grp;
+  const bool rowok = i < rend;
+  const MemberScal& S = ms[m];
+  const float rdt = S.deltat_rf, th = S.tetaf_f;
+  int s0 = 0, s1 = 0, p0 = 0, p1 = 0;
+  int64_t gbase = 0;
+  float et2i = 0.0f, hh_i = 0.0f, hl_i = 0.0f, vpl = 0.0f, dp_i = 0.0f, ds_i = 0.0f, qn_i = 0.0f;
+  bool atm_i = false, dm_i = false;
+  if (rowok) {
+    s0 = rowptr[i];
+    s1 = rowptr[i + 1];
+    p0 = inc_ptr[i];
+    p1 = inc_ptr[i + 1];
+    gbase = glrow[i];
+    et2i = nf.et2[i]; hh_i = nf.hhi[i]; hl_i = nf.hlo[i];
+    vpl = vps[i] * lm_d;
+    dp_i = nf.dpsi[i]; ds_i = nf.dsw[i]; qn_i = nf.qneu[i];
+    atm_i = loc[i] < S.nnod && ifatm[i] == 0;
+    dm_i = dmask[i] != 0;
+  }
+  if (!iter) return;  // block-uniform; no copy was issued
+  const bool ready = mbar_wait_warp(&mbar, 0, stage_err);
+  if (__syncthreads_or(!ready)) {
+    if (threadIdx.x == 0) atomicExch(stage_err, 1);
+    return;
+  }
+  const int rlen = s1 - s0, ninc = p1 - p0;
+  // slots lane and lane + 8 of the row
+  int colA = -1, colB = -1, gaA = 0, gbA = 0, gaB = 0, gbB = 0;
+  if (rowok && lane < rlen) {
+    colA = scol[s0 + lane - col0];
+    gaA = sglo[s0 + lane - glo0];
+    gbA = (lane + 1 < rlen) ? (int)sglo[s0 + lane + 1 - glo0] : 3 * ninc;
+  }
+  if (rowok && lane + kLanes8 < rlen) {
+    colB = scol[s0 + lane + kLanes8 - col0];
+    gaB = sglo[s0 + lane + kLanes8 - glo0];
+    gbB = (lane + kLanes8 + 1 < rlen) ? (int)sglo[s0 + lane + kLanes8 + 1 - glo0] : 3 * ninc;
+  }
+  if (colA >= 0) {
+    sh2[grp][lane] = nf.h2[colA];
+    sk2[grp][lane] = nf.ckr2[colA];
+    if (lm_o != 0.0f) {
+      sdp[grp][lane] = nf.dpsi[colA];
+      sds[grp][lane] = nf.dsw[colA];
+    }
+  }
+  if (colB >= 0) {
+    sh2[grp][lane + kLanes8] = nf.h2[colB];
+    sk2[grp][lane + kLanes8] = nf.ckr2[colB];
+    if (lm_o != 0.0f) {
+      sdp[grp][lane + kLanes8] = nf.dpsi[colB];
+      sds[grp][lane + kLanes8] = nf.dsw[colB];
+    }
+  }
+  __syncwarp();
+  int ntrip = (ninc + kLanes8 - 1) / kLanes8;
+  ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 8));
+  ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
+  AsmInc a{0.0f, 0.0f, 0.0f};
+  float* sv = svrow + grp * 4 * row_inc;
+  for (int trip = 0; trip < ntrip; ++trip) {
+    const int q = trip * kLanes8 + lane;
+    if (rowok && q < ninc)
+      asm_incidence(q, srec[p0 - e4.x + q], sisl[p0 + q - isl0],
+                    lm_o != 0.0f ? vpi[p0 + q] : 0.0f, grp, th, rdt, lm_d, lm_o, hh_i, hl_i,
+                    sv, sh2, sk2, sdp, sds, a);
+  }
+  __syncwarp();
+  const float dsum = group8_sum<float>(a.dacc);
+  float rhs = group8_sum<float>(a.rp);
+  const float msum = group8_sum<float>(a.msum);
+  if (!rowok) return;
+  const uint8_t* g8 = sgl + (gbase - gl0);
+  if (colA >= 0) {
+    float lhs;
+    if (colA == i) {
+      lhs = asm_diag(dsum, vpl * et2i, rdt);
+    } else {
+      lhs = 0.0f;
+      for (int u = gaA; u < gbA; ++u) lhs += sv[g8[u]];
+    }
+    vals[s0 + lane] = lhs;
+  }
+  if (colB >= 0) {
+    float lhs;
+    if (colB == i) {
+      lhs = asm_diag(dsum, vpl * et2i, rdt);
+    } else {
+      lhs = 0.0f;
+      for (int u = gaB; u < gbB; ++u) lhs += sv[g8[u]];
+    }
+    vals[s0 + lane + kLanes8] = lhs;
+  }
+  if (lane == 0) {
+    rhs = asm_rhs(rhs, msum, dp_i, vpl, ds_i, rdt);
+    nf.xt5[i] = rhs;
+    float f = qn_i;
+    if (atm_i) {
+      const double thd = S.tetaf;
+      f += (thd == 1.0) ? (float)atmact[i]
+                        : (float)(thd * atmact[i] + (1.0 - thd) * atmold[i]);
+    }
+    nf.rhs[i] = dm_i ? 0.0f : rhs + f;
+  }
+}
+using Staged8Kernel = decltype(&k_assemble_staged8_f32<12>);
+constexpr int kAsm8Blocks[kAsmVariants] = {6, 8, 10, 12};
+static const Staged8Kernel kStaged8Kernel[kAsmVariants] = {
+    &k_assemble_staged8_f32<6>, &k_assemble_staged8_f32<8>, &k_assemble_staged8_f32<10>,
+    &k_assemble_staged8_f32<12>};
+
 using StagedKernel = decltype(&k_assemble_staged_f32<6>);
 static const StagedKernel kStagedKernel[kAsmVariants] = {
     &k_assemble_staged_f32<5>, &k_assemble_staged_f32<6>, &k_assemble_staged_f32<7>,
@@ -3505,9 +3684,10 @@ struct Engine {
   // runs out
   int stage_inc = 0, stage_slot = 0, stage_gl = 0, stage_row_inc = 0;
   DBuf<int32_t> d_stage_err;
-  // the autotuner's choice between the assemblies (0 direct loads, 1
-  // staged); staged by default where it is available (measured faster at 6
-  // blocks/SM on the ensembles)
+  // the autotuner's choice among the assemblies (0 direct loads, 1 staged
+  // with 16 lanes per row, 2 staged with 8 lanes per row); staged by
+  // default where it is available (measured faster at 6 blocks/SM on the
+  // ensembles)
   int asm_staged = 1;
   size_t stage_smem = 0;    // dynamic shared memory of the staged assembly (0: unavailable)
   void launch_assembly(int variant, int mode);
@@ -4288,6 +4468,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       bool ok = stage_smem <= (size_t)180 * 1024;
       for (int k = 0; ok && k < kAsmVariants; ++k)
         ok = cudaFuncSetAttribute(kStagedKernel[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)stage_smem) == cudaSuccess &&
+             cudaFuncSetAttribute(kStaged8Kernel[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)stage_smem) == cudaSuccess;
       if (!ok) {
         cudaGetLastError();
@@ -5907,10 +6089,10 @@ int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t
 // Per (GPU, size class) cache of the schedules chosen by engine_autotune.
 static std::mutex g_tune_mu;
 static std::map<std::string, std::array<int, 3>> g_tune_cache;
-// resident blocks per SM of assembly variant v (either mode)
+// resident blocks per SM of assembly variant v in mode (0 direct, 1
+// staged, 2 staged with 8 lanes per row)
 static int asm_blocks_of(int v, int mode) {
-  (void)mode;
-  return kAsmBlocks[v];
+  return mode == 2 ? kAsm8Blocks[v] : kAsmBlocks[v];
 }
 
 static std::string tune_key(Engine* e, int64_t rows) {
@@ -5984,7 +6166,7 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
   };
   double best_a = 1e300, best_s = 1e300;
   int va = e->asm_variant, vs = e->stream_per_sm, sa = e->asm_staged;
-  const int modes = e->stage_smem > 0 ? 2 : 1;
+  const int modes = e->stage_smem > 0 ? 3 : 1;
   for (int mode = 0; mode < modes; ++mode)
     for (int v = 0; v < kAsmVariants; ++v) {
       const double t = timed([&]() { e->launch_assembly(v, mode); });
@@ -6015,15 +6197,17 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
   return 0;
 }
 
-// Forces a schedule (assembly mode 0 direct loads or 1 staged, resident
-// blocks per SM 5, 6, 7 or 8; stream SpMV resident blocks per SM: 1..8).
+// Forces a schedule (assembly mode 0 direct loads or 1 staged, 16 lanes per
+// row, resident blocks per SM 5, 6, 7 or 8; mode 2 staged, 8 lanes per
+// row, 6, 8, 10 or 12 blocks of 128 threads; stream SpMV resident blocks
+// per SM: 1..8).
 int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged) {
   int v = -1;
-  if (asm_staged < 0 || asm_staged > 1) return CATHY_GB300_EINVAL;
+  if (asm_staged < 0 || asm_staged > 2) return CATHY_GB300_EINVAL;
   for (int k = 0; k < kAsmVariants; ++k)
-    if (kAsmBlocks[k] == asm_blocks) v = k;
+    if (asm_blocks_of(k, asm_staged) == asm_blocks) v = k;
   if (v < 0 || spmv_per_sm < 1 || spmv_per_sm > 8) return CATHY_GB300_EINVAL;
-  if (asm_staged == 1 && e->stage_smem == 0) return CATHY_GB300_EUNSUP;
+  if (asm_staged >= 1 && e->stage_smem == 0) return CATHY_GB300_EUNSUP;
   e->asm_variant = v;
   e->asm_staged = asm_staged;
   e->stream_per_sm = spmv_per_sm;
@@ -6034,7 +6218,18 @@ int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_stag
 // The FP32 Picard assembly, unstaged or staged, at variant v (resident
 // blocks per SM kAsmBlocks[v]) over the compacted 16-row map.
 void Engine::launch_assembly(int v, int mode) {
-  if (mode == 1 && stage_smem > 0) {
+  if (mode == 2 && stage_smem > 0) {
+    next_smem = stage_smem;
+    launch(kStaged8Kernel[v], cbm16.nblk, kThreads8, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
+           (const int4*)cbm16.ent.p, (const longlong2*)cbm16.eg.p, (const uint8_t*)d_act.p,
+           (const MemberScal*)d_ms.p, (const int32_t*)d_rowptr.p, (const int32_t*)d_cols.p,
+           (const int32_t*)d_inc_ptr.p, (const float4*)d_rec16.p, (const uint16_t*)d_islot.p,
+           (const float*)d_vpi.p, (const float*)d_vps.p, (const uint8_t*)d_dmask.p, nf,
+           (const int32_t*)nd.loc, (const int8_t*)nd.ifatm, (const double*)nd.atmact,
+           (const double*)nd.atmold, d_vals32.p, (float)lm_d, (float)lm_o,
+           (const int64_t*)d_glrow.p, (const uint8_t*)d_gloff.p, (const uint8_t*)d_gl.p,
+           stage_inc, stage_slot, stage_gl, stage_row_inc, d_stage_err.p);
+  } else if (mode == 1 && stage_smem > 0) {
     next_smem = stage_smem;
     launch(kStagedKernel[v], cbm16.nblk, kThreads, cbm16.mem.p, cbm16.r0.p, cbm16.r1.p,
            (const int4*)cbm16.ent.p, (const longlong2*)cbm16.eg.p, (const uint8_t*)d_act.p,

@@ -343,8 +343,9 @@ def test_newton_chord_slope_kslope1_matches_oracle():
 def test_every_autotuner_schedule_gives_the_same_heads():
     """The autotuner picks the assembly kernel's resident blocks per SM and
     whether its records, columns and gather lists are read directly or
-    staged in shared memory by bulk copies (the same arithmetic in the same
-    order, so bit-identical systems), and the stream SpMV's grid
+    staged in shared memory by bulk copies, with 16 or 8 lanes per row (the
+    same arithmetic in the same order, so bit-identical systems), and the
+    stream SpMV's grid
     (which only regroups its FP32 dot products).  Every schedule must reach
     the same heads; the tuner returns one of its candidates and reuses its
     cached choice."""
@@ -354,7 +355,7 @@ def test_every_autotuner_schedule_gives_the_same_heads():
         c.parm.precond = 2
     runs = {}
     scheds = [(a, 8, st) for st in (0, 1) for a in (5, 6, 7, 8)] + \
-        [(6, 4, 0), (6, 6, 0)]
+        [(a, 8, 2) for a in (6, 8, 10, 12)] + [(6, 4, 0), (6, 6, 0)]
     for asm, spmv, staged in scheds:
         with _sim(cases, precision=1, graphs=True) as s:
             s.set_schedule(asm, spmv, staged)
