@@ -192,21 +192,27 @@ int32_t cathy_gb300_profile(void* handle, int32_t enable, double* spmv_ms,
  * into shared memory by bulk copies (mode 1), 16 lanes per row, at 5, 6, 7
  * and 8 resident blocks per SM, and staged with 8 lanes per row (mode 2)
  * at 6, 8, 10 and 12 blocks of 128 threads, and the stream SpMV at 4, 6
- * and 8 resident blocks per SM, nrep launches each,
+ * and 8 resident blocks per SM or in its staged form (each warp's next
+ * entry copied into shared memory while it multiplies the current one, 5
+ * blocks per SM), nrep launches each,
  * and keeps the fastest; the choice is cached per (GPU, rows size class),
- * and nrep <= 0 reuses a cached choice when there is one.  sched[3]
- * receives (assembly blocks/SM, SpMV blocks/SM, assembly mode 0/1/2),
+ * and nrep <= 0 reuses a cached choice when there is one.  sched[4]
+ * receives (assembly blocks/SM, SpMV blocks/SM, assembly mode 0/1/2, SpMV
+ * staged 0/1),
  * ms[2] their best mean ms.  The assembly variants give bit-identical
  * systems; the SpMV grid only regroups its FP32 dot products.
  * CATHY_GB300_EUNSUP outside the FP32 Picard path with the column-line
  * preconditioner. */
 int32_t cathy_gb300_autotune(void* handle, int32_t nrep, int32_t* sched, double* ms);
 /* Forces a schedule: assembly mode asm_staged 0 or 1 with blocks/SM in
- * {5, 6, 7, 8}, or 2 with {6, 8, 10, 12}; SpMV blocks/SM in 1..8 (defaults
- * 6, 8, mode 1 on the FP32 Picard path); CATHY_GB300_EUNSUP if a staged
- * mode is asked for and unavailable. */
+ * {5, 6, 7, 8}, or 2 with {6, 8, 10, 12}; SpMV blocks/SM in 1..8 and
+ * spmv_staged 0/1 (the staged form, which runs at 5 blocks/SM, is used for
+ * work sets of more than two map entries per warp of a resident wave)
+ * (defaults: mode 2 at 10 blocks/SM, SpMV 8, staged, on the FP32 Picard
+ * path); CATHY_GB300_EUNSUP if a staged assembly is asked for and
+ * unavailable. */
 int32_t cathy_gb300_set_schedule(void* handle, int32_t asm_blocks, int32_t spmv_blocks,
-                                 int32_t asm_staged);
+                                 int32_t asm_staged, int32_t spmv_staged);
 /* Phase timers of the nonlinear iterations in the nine buckets of the
  * reference's CPU summary (risul, cathy_main.f:3913-3950; accumulated in
  * picard.f:66-202): unsat characteristics, init of system matrices, local

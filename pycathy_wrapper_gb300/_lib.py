@@ -112,7 +112,8 @@ EXPORTS = {
     "cathy_gb300_profile": (C.c_int32, [C.c_void_p, C.c_int32, f64p, C.POINTER(C.c_int64),
                                         f64p]),
     "cathy_gb300_autotune": (C.c_int32, [C.c_void_p, C.c_int32, i32p, f64p]),
-    "cathy_gb300_set_schedule": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "cathy_gb300_set_schedule": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                             C.c_int32]),
     "cathy_gb300_phase_timers": (C.c_int32, [C.c_void_p, C.c_int32, f64p, C.c_int32]),
     "cathy_gb300_time_assembly": (C.c_int32, [C.c_void_p, C.c_int32, f64p, f64p,
                                               C.POINTER(C.c_int64)]),

@@ -241,17 +241,19 @@ class Simulation:
         resident blocks per SM) and stream-SpMV schedules on the running
         members and keep the fastest (cached per GPU and size class;
         nrep <= 0 reuses a cached choice).
-        Returns dict(asm_blocks, spmv_blocks, asm_staged (the mode), asm_ms,
-        spmv_ms)."""
-        sc = (C.c_int32 * 3)()
+        Returns dict(asm_blocks, spmv_blocks, asm_staged (the mode),
+        spmv_staged, asm_ms, spmv_ms)."""
+        sc = (C.c_int32 * 4)()
         ms = (C.c_double * 2)()
         check(self.L.cathy_gb300_autotune(self.h, int(nrep), sc, ms), "autotune")
-        return dict(asm_blocks=sc[0], spmv_blocks=sc[1], asm_staged=int(sc[2]), asm_ms=ms[0],
-                    spmv_ms=ms[1])
+        return dict(asm_blocks=sc[0], spmv_blocks=sc[1], asm_staged=int(sc[2]),
+                    spmv_staged=int(sc[3]), asm_ms=ms[0], spmv_ms=ms[1])
 
-    def set_schedule(self, asm_blocks: int, spmv_blocks: int, asm_staged: int = 0):
+    def set_schedule(self, asm_blocks: int, spmv_blocks: int, asm_staged: int = 0,
+                     spmv_staged: int = 0):
         check(self.L.cathy_gb300_set_schedule(self.h, int(asm_blocks), int(spmv_blocks),
-                                              int(asm_staged)), "set_schedule")
+                                              int(asm_staged), int(spmv_staged)),
+              "set_schedule")
 
     PHASES = ("UNSAT CHARACTERISTICS", "INIT. OF SYSTEM MATRICES", "LOCAL SYSTEM ASSEMBLY",
               "RHS CALCULATION W/O BC'S", "GLOBAL LHS SYSTEM MATRIX", "BC CONTRIBUTIONS TO RHS",

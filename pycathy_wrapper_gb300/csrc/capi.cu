@@ -146,10 +146,10 @@ int32_t cathy_gb300_autotune(void* h, int32_t nrep, int32_t* sched, double* ms) 
 }
 
 int32_t cathy_gb300_set_schedule(void* h, int32_t asm_blocks, int32_t spmv_blocks,
-                                 int32_t asm_staged) {
+                                 int32_t asm_staged, int32_t spmv_staged) {
   if (!h) return CATHY_GB300_EINVAL;
   return guarded([&]() {
-    return engine_set_schedule((Engine*)h, asm_blocks, spmv_blocks, asm_staged);
+    return engine_set_schedule((Engine*)h, asm_blocks, spmv_blocks, asm_staged, spmv_staged);
   });
 }
 

@@ -748,6 +748,63 @@ __device__ __forceinline__ uint64_t gtimer() {
   return t;
 }
 
+// ---- bulk copies into shared memory (cp.async.bulk + mbarrier) -----------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// (the suspend-time hint, in ns, lets a waiting thread sleep until the
+// phase completes instead of spinning on issue slots)
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(1000000u)
+      : "memory");
+  return ok != 0;
+}
+// A block waits at most this long (global timer, ns) for its copies of a
+// few KB, which land within microseconds; after that it flags the failure
+// and returns, and blocks that start after a failure do not wait at all.
+constexpr unsigned long long kStageWaitNs = 200000000ull;
+
+// Waits (all 32 lanes of the calling warp together) for the given phase of
+// bar, at most kStageWaitNs or until another block has flagged a failure;
+// the result is the same in every lane.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity,
+                                               const int32_t* stage_err) {
+  bool ready = mbar_try_wait(bar, parity);
+  if (__all_sync(0xffffffffu, ready)) return true;
+  const unsigned long long t0 = gtimer();
+  for (;;) {
+    if (!ready) ready = mbar_try_wait(bar, parity);
+    if (__all_sync(0xffffffffu, ready)) return true;
+    const bool stop = *(volatile const int32_t*)stage_err != 0 || gtimer() - t0 >= kStageWaitNs;
+    if (__any_sync(0xffffffffu, stop)) return false;
+  }
+}
+
+__host__ __device__ inline long long align16ll(long long x) { return (x + 15) & ~15LL; }
+
 // y = A x with Dirichlet rows as identity; optionally accumulates per-member
 // dot products d0 += x.y and d1 += x.w (w optional).  Persistent grid: each
 // block walks a contiguous run of block-map entries (16 rows per entry, 16
@@ -947,17 +1004,20 @@ __device__ void build_kact(const int32_t* amem_cum, int nmem, const uint8_t* act
 // and 0 at those (the masked residual, w = b), no dots.
 enum { kSpmvPlain = 0, kSpmvUpd = 1, kSpmvResid = 2 };
 constexpr int kStreamWarps = 8;
+constexpr int kSpmvStagedBlocks = 5;  // resident blocks per SM of the staged SpMV
 // FP32 y = A x as a stream over the map entries that virtual block vbid of
 // vgrid takes (see k_spmv_stream).  s_bytes: a zeroed shared slot for the
 // byte count (used only with alg_bytes).
-template <int kMode>
+template <int kMode, bool kStaged = false>
 __device__ __forceinline__ void spmv_stream_run(
     int vbid, int vgrid, int nblk, const int32_t* bm_mem, const int32_t* bm_r0,
     const int32_t* bm_r1, const uint8_t* active, const int32_t* rowptr, const int32_t* cols,
     const float* vals, const uint8_t* dmask, const float* x, float* y, const float* w, float* pv,
     const double* sc, double* acc, int acc_stride, double* alg_bytes, double* s_bytes,
-    const int32_t* kact, const int32_t* kfirst, const int4* ent) {
+    const int32_t* kact, const int32_t* kfirst, const int4* ent, unsigned char* stage = nullptr,
+    int stage_bytes = 0, int32_t* stage_err = nullptr) {
   __shared__ float sprod[kStreamWarps][16 * kGroup + 8];
+  __shared__ __align__(8) uint64_t sbar[kStaged ? kStreamWarps : 1][2];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   float* sp = sprod[wp];
   float d0 = 0.0f, d1 = 0.0f;
@@ -987,15 +1047,52 @@ __device__ __forceinline__ void spmv_stream_run(
     seg_end = kcum[seg + 1];
     delta = kfirst[seg] - kcum[seg];
   }
-  for (int g = b0 + wp; g < b1; g += kStreamWarps) {
-    int b = g;
-    if (kMode == kSpmvUpd) {
-      while (g >= seg_end) {  // warp-uniform
-        ++seg;
-        seg_end = kcum[seg + 1];
-        delta = kfirst[seg] - kcum[seg];
-      }
-      b = g + delta;
+  // map entry of the warp's g-th listed entry (g increasing: the segment
+  // cursor only moves forward)
+  auto entry_of = [&](int g) {
+    if (kMode != kSpmvUpd) return g;
+    while (g >= seg_end) {  // warp-uniform
+      ++seg;
+      seg_end = kcum[seg + 1];
+      delta = kfirst[seg] - kcum[seg];
+    }
+    return g + delta;
+  };
+  // Staged form: each warp copies its next entry's values and columns into
+  // the other of its two shared-memory stages (two bulk copies, completion
+  // on the stage's mbarrier) while it multiplies the current one, so two
+  // entries per warp are in flight.
+  // stage t of this warp: values, then columns
+  auto st_val = [&](int t) {
+    return reinterpret_cast<float*>(stage + (size_t)(2 * wp + t) * 2 * stage_bytes);
+  };
+  auto st_col = [&](int t) {
+    return reinterpret_cast<int*>(stage + (size_t)(2 * wp + t) * 2 * stage_bytes + stage_bytes);
+  };
+  if (kStaged) {
+    if (lane == 0) {
+      mbar_init(&sbar[wp][0], 1);
+      mbar_init(&sbar[wp][1], 1);
+    }
+    __syncwarp();
+  }
+  auto stage_entry = [&](int b, int t) {  // lane 0
+    const int4 e4 = ent[b];
+    const int v0 = e4.z & ~3, v1 = (e4.w + 3) & ~3;
+    const uint32_t nb = (uint32_t)(v1 - v0) * 4u;
+    mbar_expect_tx(&sbar[wp][t], 2u * nb);
+    bulk_g2s(st_val(t), vals + v0, nb, &sbar[wp][t]);
+    bulk_g2s(st_col(t), cols + v0, nb, &sbar[wp][t]);
+  };
+  int g = b0 + wp;
+  int bnext = g < b1 ? entry_of(g) : 0;
+  if (kStaged && g < b1 && lane == 0) stage_entry(bnext, 0);
+  for (int it = 0; g < b1; ++it, g += kStreamWarps) {
+    const int b = bnext;
+    const int t = it & 1;
+    if (g + kStreamWarps < b1) {
+      bnext = entry_of(g + kStreamWarps);
+      if (kStaged && lane == 0) stage_entry(bnext, t ^ 1);
     }
     // The entry's member, rows and (with ent) slot range; then every load
     // of the entry -- row pointers, the rows' own inputs, the slot vectors
@@ -1027,6 +1124,14 @@ __device__ __forceinline__ void spmv_stream_run(
       }
       if (w) wi = w[i];
     }
+    if (kStaged) {
+      // every staged entry is waited for, so that its stage is free for the
+      // entry after next
+      if (!mbar_wait_warp(&sbar[wp][t], (it >> 1) & 1, stage_err)) {
+        if (lane == 0) atomicExch(stage_err, 1);
+        break;
+      }
+    }
     if (!act_m) continue;  // warp-uniform
     if (acc && m != cur) {
       if (cur >= 0) {
@@ -1045,15 +1150,22 @@ __device__ __forceinline__ void spmv_stream_run(
     // 16-byte vectors covering [sbeg, send)
     const int v0 = sbeg >> 2, v1 = (send + 3) >> 2;
     for (int v = v0 + lane; v < v1; v += 32) {
-      const float4 va = reinterpret_cast<const float4*>(vals)[v];
-      const int4 ca = reinterpret_cast<const int4*>(cols)[v];
+      float4 va;
+      int4 ca;
+      if (kStaged) {
+        va = reinterpret_cast<const float4*>(st_val(t))[v - v0];
+        ca = reinterpret_cast<const int4*>(st_col(t))[v - v0];
+      } else {
+        va = reinterpret_cast<const float4*>(vals)[v];
+        ca = reinterpret_cast<const int4*>(cols)[v];
+      }
       const int k0 = 4 * v;
       const float vv[4] = {va.x, va.y, va.z, va.w};
       const int cc[4] = {ca.x, ca.y, ca.z, ca.w};
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int k = k0 + t;
-        if (k >= sbeg && k < send) sp[k - sbeg] = vv[t] * x[cc[t]];
+      for (int tt = 0; tt < 4; ++tt) {
+        const int k = k0 + tt;
+        if (k >= sbeg && k < send) sp[k - sbeg] = vv[tt] * x[cc[tt]];
       }
     }
     __syncwarp();
@@ -1128,7 +1240,10 @@ __device__ __forceinline__ void spmv_stream_run(
 // the full batch, where a resident wave of 8 blocks per SM keeps the most
 // entries in flight; 2 for small work sets, which fill few SMs and run
 // faster without the spills of the 32-register budget)
-template <int kMode, int kMinBlocks = 8>
+// kStaged: each warp stages its next entry's values and columns in shared
+// memory by bulk copies (dynamic shared memory: 2 stages x 2 arrays of
+// stage_bytes per warp).
+template <int kMode, int kMinBlocks = 8, bool kStaged = false>
 __global__ void __launch_bounds__(32 * kStreamWarps, kMinBlocks)
 k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
               const uint8_t* active, const int32_t* __restrict__ rowptr,
@@ -1136,7 +1251,9 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
               const uint8_t* __restrict__ dmask, const float* __restrict__ x, float* y,
               const float* __restrict__ w, float* pv, const double* sc, double* acc,
               int acc_stride, double* alg_bytes, unsigned long long* lt, int lt_cap,
-              const int32_t* kact, const int32_t* kfirst, const int4* ent) {
+              const int32_t* kact, const int32_t* kfirst, const int4* ent, int stage_bytes,
+              int32_t* stage_err) {
+  extern __shared__ __align__(16) unsigned char dsm_sp[];
   pdl_enter();
   __shared__ int s_slot;
   __shared__ double s_bytes;
@@ -1153,9 +1270,10 @@ k_spmv_stream(int nblk, const int32_t* bm_mem, const int32_t* bm_r0, const int32
     __syncthreads();
     if (s_slot < 0) lt = nullptr;
   }
-  spmv_stream_run<kMode>(blockIdx.x, gridDim.x, nblk, bm_mem, bm_r0, bm_r1, active, rowptr, cols,
-                         vals, dmask, x, y, w, pv, sc, acc, acc_stride, alg_bytes, &s_bytes, kact,
-                         kfirst, ent);
+  spmv_stream_run<kMode, kStaged>(blockIdx.x, gridDim.x, nblk, bm_mem, bm_r0, bm_r1, active,
+                                  rowptr, cols, vals, dmask, x, y, w, pv, sc, acc, acc_stride,
+                                  alg_bytes, &s_bytes, kact, kfirst, ent,
+                                  kStaged ? dsm_sp : nullptr, stage_bytes, stage_err);
   if (lt) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -2578,61 +2696,6 @@ static const AsmKernel kAsmKernel[kAsmVariants] = {
 // and the lanes read the records, slots and lists from shared memory.
 // Bulk copies need 16-byte aligned addresses and sizes: each range is
 // widened to whole 16-byte units (the arrays are padded by 16 bytes).
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-               : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-// (the suspend-time hint, in ns, lets a waiting thread sleep until the
-// phase completes instead of spinning on issue slots)
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
-      "selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity), "r"(1000000u)
-      : "memory");
-  return ok != 0;
-}
-// A block waits at most this long (global timer, ns) for its copies of a
-// few KB, which land within microseconds; after that it flags the failure
-// and returns, and blocks that start after a failure do not wait at all.
-constexpr unsigned long long kStageWaitNs = 200000000ull;
-
-// Waits (all 32 lanes of the calling warp together) for the given phase of
-// bar, at most kStageWaitNs or until another block has flagged a failure;
-// the result is the same in every lane.
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity,
-                                               const int32_t* stage_err) {
-  bool ready = mbar_try_wait(bar, parity);
-  if (__all_sync(0xffffffffu, ready)) return true;
-  const unsigned long long t0 = gtimer();
-  for (;;) {
-    if (!ready) ready = mbar_try_wait(bar, parity);
-    if (__all_sync(0xffffffffu, ready)) return true;
-    const bool stop = *(volatile const int32_t*)stage_err != 0 || gtimer() - t0 >= kStageWaitNs;
-    if (__any_sync(0xffffffffu, stop)) return false;
-  }
-}
-
-__host__ __device__ inline long long align16ll(long long x) { return (x + 15) & ~15LL; }
 // byte offsets of the staged arrays in dynamic shared memory, for the
 // largest ranges of any entry, then the rows' contribution arrays (4 floats
 // per incidence of the row with the most); off[6] is the total
@@ -2910,19 +2973,23 @@ k_assemble_staged8_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_
   int ntrip = (ninc + kLanes8 - 1) / kLanes8;
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 8));
   ntrip = max(ntrip, __shfl_xor_sync(0xffffffffu, ntrip, 16));
-  AsmInc a{0.0f, 0.0f, 0.0f};
+  // two partial sums per lane, for the incidences the 16-lane kernels give
+  // to lanes lane and lane + 8 (q mod 16), added in the same order, so that
+  // the first butterfly level (lane + lane^8) becomes aA + aB and the sums
+  // round exactly as there
+  AsmInc aA{0.0f, 0.0f, 0.0f}, aB{0.0f, 0.0f, 0.0f};
   float* sv = svrow + grp * 4 * row_inc;
   for (int trip = 0; trip < ntrip; ++trip) {
     const int q = trip * kLanes8 + lane;
     if (rowok && q < ninc)
       asm_incidence(q, srec[p0 - e4.x + q], sisl[p0 + q - isl0],
                     lm_o != 0.0f ? vpi[p0 + q] : 0.0f, grp, th, rdt, lm_d, lm_o, hh_i, hl_i,
-                    sv, sh2, sk2, sdp, sds, a);
+                    sv, sh2, sk2, sdp, sds, (trip & 1) ? aB : aA);
   }
   __syncwarp();
-  const float dsum = group8_sum<float>(a.dacc);
-  float rhs = group8_sum<float>(a.rp);
-  const float msum = group8_sum<float>(a.msum);
+  const float dsum = group8_sum<float>(aA.dacc + aB.dacc);
+  float rhs = group8_sum<float>(aA.rp + aB.rp);
+  const float msum = group8_sum<float>(aA.msum + aB.msum);
   if (!rowok) return;
   const uint8_t* g8 = sgl + (gbase - gl0);
   if (colA >= 0) {
@@ -3678,17 +3745,22 @@ struct Engine {
   // schedules chosen by the autotuner (engine_autotune): the assembly
   // variant (resident blocks per SM kAsmBlocks[asm_variant]) and the stream
   // SpMV's resident blocks per SM (its grid = stream_per_sm * SMs)
-  int asm_variant = 1;
+  int asm_variant = 2;
   // staged assembly: largest incidence, slot and gather-list ranges of a
   // 16-row entry, and the device flag a block sets if its staging wait
   // runs out
   int stage_inc = 0, stage_slot = 0, stage_gl = 0, stage_row_inc = 0;
+  // staged SpMV: bytes of one array of one stage (values or columns of the
+  // entry with the most slots, widened to 16-byte units), and whether to use it
+  int spmv_stage_bytes = 0;
+  bool spmv_staged = false;
   DBuf<int32_t> d_stage_err;
   // the autotuner's choice among the assemblies (0 direct loads, 1 staged
-  // with 16 lanes per row, 2 staged with 8 lanes per row); staged by
-  // default where it is available (measured faster at 6 blocks/SM on the
-  // ensembles)
-  int asm_staged = 1;
+  // with 16 lanes per row, 2 staged with 8 lanes per row); by default the
+  // 8-lane staged kernel at 10 blocks/SM (variant 2) where staging is
+  // available (the fastest on the GB300 ensembles), else the direct one at
+  // 6 blocks/SM (set at build)
+  int asm_staged = 2;
   size_t stage_smem = 0;    // dynamic shared memory of the staged assembly (0: unavailable)
   void launch_assembly(int variant, int mode);
   void check_stage_err();
@@ -3765,40 +3837,51 @@ struct Engine {
   int grid_persist(int nblk) const { return std::max(1, std::min(nblk, persist_blocks)); }
   int grid_spmv(int nblk) const { return std::max(1, std::min(nblk, 2 * persist_blocks)); }
   // work sets of at most two map entries per warp of one resident wave
-  // take the stream SpMV with the larger register budget
+  // take the stream SpMV with the larger register budget; larger ones the
+  // staged form (5 blocks/SM, two entries in flight per warp) when the
+  // entry ranges are there and the schedule asks for it
   bool small_stream() const { return cbm16.nblk <= 2 * kStreamWarps * nsm; }
+  bool staged_stream() const {
+    return spmv_staged && !small_stream() && cbm16.ent.p && spmv_stage_bytes > 0;
+  }
   int grid_stream() const {
     // one warp per map entry up to one resident wave of 256-thread blocks
-    return std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps,
-                                stream_per_sm * nsm));
+    const int per_sm = staged_stream() ? kSpmvStagedBlocks : stream_per_sm;
+    return std::max(1, std::min((cbm16.nblk + kStreamWarps - 1) / kStreamWarps, per_sm * nsm));
+  }
+  size_t spmv_smem() const {
+    return staged_stream() ? (size_t)kStreamWarps * 4 * spmv_stage_bytes : 0;
+  }
+  template <int kMode>
+  void launch_stream(const float* vals, const float* x, float* y, const float* w, float* pv,
+                     double* acc, double* ab, unsigned long long* lt, const int32_t* kfirst) {
+    auto k = small_stream() ? k_spmv_stream<kMode, 2, false>
+             : staged_stream() ? k_spmv_stream<kMode, kSpmvStagedBlocks, true>
+                               : k_spmv_stream<kMode, 8, false>;
+    next_smem = spmv_smem();
+    launch(k, grid_stream(), 32 * kStreamWarps, cbm16.nblk, (const int32_t*)cbm16.mem.p,
+           (const int32_t*)cbm16.r0.p, (const int32_t*)cbm16.r1.p, (const uint8_t*)d_active.p,
+           (const int32_t*)d_rowptr.p, (const int32_t*)d_cols.p, vals,
+           (const uint8_t*)d_dmask.p, x, y, w, pv, (const double*)d_sc.p, acc, (int)SC_N, ab,
+           lt, lt ? lt_cap : 0, (const int32_t*)d_kact.p, kfirst, (const int4*)cbm16.ent.p,
+           spmv_stage_bytes, d_stage_err.p);
   }
   // q = A p with the fused dots p.q, p.r (FP32 stream kernel)
   void spmv_f32(const float* vals, const float* p, float* q, const float* r) {
-    launch(small_stream() ? k_spmv_stream<kSpmvPlain, 2> : k_spmv_stream<kSpmvPlain, 8>,
-           grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
-           cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, p, q, r,
-           (float*)nullptr, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
-           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap,
-           (const int32_t*)d_kact.p, (const int32_t*)d_kact.p, (const int4*)cbm16.ent.p);
+    launch_stream<kSpmvPlain>(vals, p, q, r, (float*)nullptr, d_sc.p + SC_PQ,
+                              prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr,
+                              (const int32_t*)d_kact.p);
   }
   // r = b - A x (masked)
   void resid_f32(const float* vals, const float* x, const float* b, float* r) {
-    launch(small_stream() ? k_spmv_stream<kSpmvResid, 2> : k_spmv_stream<kSpmvResid, 8>,
-           grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
-           cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, x, r, b,
-           (float*)nullptr, (const double*)d_sc.p, (double*)nullptr, (int)SC_N,
-           (double*)nullptr, (unsigned long long*)nullptr, 0, (const int32_t*)d_kact.p,
-           (const int32_t*)d_kact.p, (const int4*)cbm16.ent.p);
+    launch_stream<kSpmvResid>(vals, x, r, b, (float*)nullptr, (double*)nullptr,
+                              (double*)nullptr, (unsigned long long*)nullptr,
+                              (const int32_t*)d_kact.p);
   }
   // p = z + beta p, q = A z + beta q (= A p) with the fused dots p.q, p.r
   void spmv_upd_f32(const float* vals, const float* z, float* p, float* q, const float* r) {
-    launch(small_stream() ? k_spmv_stream<kSpmvUpd, 2> : k_spmv_stream<kSpmvUpd, 8>,
-           grid_stream(), 32 * kStreamWarps, cbm16.nblk, cbm16.mem.p,
-           cbm16.r0.p, cbm16.r1.p, d_active.p, d_rowptr.p, d_cols.p, vals, d_dmask.p, z, q, r,
-           p, (const double*)d_sc.p, d_sc.p + SC_PQ, (int)SC_N,
-           prof ? d_prof_bytes.p : nullptr, prof ? d_lt.p : nullptr, lt_cap,
-           (const int32_t*)d_kact.p, (const int32_t*)(d_kact.p + nmem + 2),
-           (const int4*)cbm16.ent.p);
+    launch_stream<kSpmvUpd>(vals, z, q, r, p, d_sc.p + SC_PQ, prof ? d_prof_bytes.p : nullptr,
+                            prof ? d_lt.p : nullptr, (const int32_t*)(d_kact.p + nmem + 2));
   }
   void solve_bicgstab(int isolv, int itmax, double tol);
   template <class VT>
@@ -4459,10 +4542,11 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     bm16.eg.alloc(eg.size()); bm16.eg.upload(eg.data(), eg.size(), st);
     d_stage_err.alloc(1);
     d_stage_err.zero(st);
+    spmv_stage_bytes = (int)align16ll(4LL * stage_slot + 32);
     int off[7];
     asm_stage_layout(stage_inc, stage_slot, stage_gl, stage_row_inc, off);
     stage_smem = (size_t)off[6];
-    if (stage_smem > (size_t)48 * 1024) {
+    if (stage_smem > (size_t)48 * 1024) {  // (staged kernels opt in above 48 KB)
       // above the default dynamic limit: opt in, or leave the staged
       // assembly off if it does not fit next to the static arrays
       bool ok = stage_smem <= (size_t)180 * 1024;
@@ -4476,6 +4560,10 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         stage_smem = 0;
       }
     }
+  }
+  if (stage_smem == 0) {  // no staging: the direct-load assembly at 6 blocks/SM
+    asm_staged = 0;
+    asm_variant = 1;
   }
   make_elem_blockmap(bme, kThreads);
   make_surface_blockmap(bms, kThreads);
@@ -6088,7 +6176,7 @@ int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t
 // ---- schedule autotuner ----------------------------------------------------
 // Per (GPU, size class) cache of the schedules chosen by engine_autotune.
 static std::mutex g_tune_mu;
-static std::map<std::string, std::array<int, 3>> g_tune_cache;
+static std::map<std::string, std::array<int, 4>> g_tune_cache;
 // resident blocks per SM of assembly variant v in mode (0 direct, 1
 // staged, 2 staged with 8 lanes per row)
 static int asm_blocks_of(int v, int mode) {
@@ -6144,10 +6232,12 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
       e->asm_variant = it->second[0];
       e->stream_per_sm = it->second[1];
       e->asm_staged = it->second[2];
+      e->spmv_staged = it->second[3] != 0;
       e->graph_free();
       sched[0] = asm_blocks_of(e->asm_variant, e->asm_staged);
-      sched[1] = e->stream_per_sm;
+      sched[1] = e->spmv_staged ? kSpmvStagedBlocks : e->stream_per_sm;
       sched[2] = e->asm_staged;
+      sched[3] = e->spmv_staged ? 1 : 0;
       ms[0] = ms[1] = 0.0;
       return 0;
     }
@@ -6175,23 +6265,32 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
   e->check_stage_err();
   const bool was_prof = e->prof;
   e->prof = false;
-  for (int per : {4, 6, 8}) {
-    e->stream_per_sm = per;
-    const double t = timed([&]() { e->spmv_f32(e->d_vals32.p, e->w32[3].p, e->w32[4].p, e->w32[2].p); });
-    if (t < best_s) { best_s = t; vs = per; }
-  }
+  bool ss = e->spmv_staged;
+  for (int staged = 0; staged < 2; ++staged)
+    for (int per : {4, 6, 8}) {
+      if (staged && per != 4) continue;  // the staged form has one grid (5 blocks/SM)
+      e->spmv_staged = staged != 0;
+      e->stream_per_sm = per;
+      const double t = timed([&]() {
+        e->spmv_f32(e->d_vals32.p, e->w32[3].p, e->w32[4].p, e->w32[2].p);
+      });
+      if (t < best_s) { best_s = t; vs = per; ss = staged != 0; }
+    }
+  e->check_stage_err();
   e->prof = was_prof;
+  e->spmv_staged = ss;
   e->asm_variant = va;
   e->asm_staged = sa;
   e->stream_per_sm = vs;
   e->graph_free();
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[key] = {va, vs, sa};
+    g_tune_cache[key] = {va, vs, sa, ss ? 1 : 0};
   }
   sched[0] = asm_blocks_of(va, sa);
-  sched[1] = vs;
+  sched[1] = ss ? kSpmvStagedBlocks : vs;
   sched[2] = sa;
+  sched[3] = ss ? 1 : 0;
   ms[0] = best_a;
   ms[1] = best_s;
   return 0;
@@ -6200,8 +6299,9 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
 // Forces a schedule (assembly mode 0 direct loads or 1 staged, 16 lanes per
 // row, resident blocks per SM 5, 6, 7 or 8; mode 2 staged, 8 lanes per
 // row, 6, 8, 10 or 12 blocks of 128 threads; stream SpMV resident blocks
-// per SM: 1..8).
-int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged) {
+// per SM: 1..8, or its staged form for large work sets).
+int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged,
+                        int spmv_staged) {
   int v = -1;
   if (asm_staged < 0 || asm_staged > 2) return CATHY_GB300_EINVAL;
   for (int k = 0; k < kAsmVariants; ++k)
@@ -6210,6 +6310,7 @@ int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_stag
   if (asm_staged >= 1 && e->stage_smem == 0) return CATHY_GB300_EUNSUP;
   e->asm_variant = v;
   e->asm_staged = asm_staged;
+  e->spmv_staged = spmv_staged != 0;
   e->stream_per_sm = spmv_per_sm;
   e->graph_free();
   return 0;

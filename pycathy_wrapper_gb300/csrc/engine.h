@@ -101,7 +101,8 @@ int engine_timers(Engine* e, double* out, int n);
 int engine_attach_learned(Engine* e, void* model, int mode);
 int engine_learned_stats(Engine* e, double* out, int n);
 int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms);
-int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged);
+int engine_set_schedule(Engine* e, int asm_blocks, int spmv_per_sm, int asm_staged,
+                        int spmv_staged);
 int engine_phase_timers(Engine* e, int enable, double* out, int n);
 int engine_time_assembly(Engine* e, int nrep, double* ms, double* bytes, int64_t* rows);
 int engine_stats(Engine* e, double* gpu_ms, int64_t* launches,

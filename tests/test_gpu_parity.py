@@ -340,6 +340,30 @@ def test_newton_chord_slope_kslope1_matches_oracle():
     assert np.max(np.abs(p - po)) <= 1e-6
 
 
+def test_staged_spmv_gives_the_same_heads():
+    """The stream SpMV's staged form (each warp copies its next map entry's
+    values and columns into shared memory while it multiplies the current
+    one) runs for work sets of more than two entries per warp of a resident
+    wave; at the same grid (5 blocks per SM) its products and dot products
+    are formed in the same order as the direct form's, so the heads are
+    bit-identical."""
+    from pycathy_wrapper_gb300.inputs import config2_members
+    cases = config2_members(4, tmax=900.0, min_cells=40, max_cells=50)
+    for c in cases:
+        c.parm.precond = 2
+    runs = []
+    for staged in (0, 1):
+        with _sim(cases, precision=1, graphs=True) as s:
+            assert sum(z["n"] for z in s.sizes) > 2 * 8 * 152 * 16  # the large-set path
+            s.set_schedule(10, 5, 2, staged)
+            s.run()
+            runs.append([(s.state(m)[0], [r["iter"] for r in s.records(m)[1]])
+                         for m in range(len(cases))])
+    for (pa, ia), (pb, ib) in zip(*runs):
+        assert ia == ib
+        np.testing.assert_array_equal(pa, pb)
+
+
 def test_every_autotuner_schedule_gives_the_same_heads():
     """The autotuner picks the assembly kernel's resident blocks per SM and
     whether its records, columns and gather lists are read directly or
