@@ -6266,9 +6266,11 @@ int engine_autotune(Engine* e, int nrep, int32_t* sched, double* ms) {
   const bool was_prof = e->prof;
   e->prof = false;
   bool ss = e->spmv_staged;
-  for (int staged = 0; staged < 2; ++staged)
+  // (the staged form only runs for large work sets, at one grid)
+  const bool can_stage = e->cbm16.ent.p && e->spmv_stage_bytes > 0 && !e->small_stream();
+  for (int staged = 0; staged < (can_stage ? 2 : 1); ++staged)
     for (int per : {4, 6, 8}) {
-      if (staged && per != 4) continue;  // the staged form has one grid (5 blocks/SM)
+      if (staged && per != 4) continue;
       e->spmv_staged = staged != 0;
       e->stream_per_sm = per;
       const double t = timed([&]() {

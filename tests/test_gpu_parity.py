@@ -397,10 +397,11 @@ def test_every_autotuner_schedule_gives_the_same_heads():
     with _sim(cases, precision=1, graphs=True) as s:
         s.run(5)
         t = s.autotune(5)
-        assert t["asm_blocks"] in (5, 6, 7, 8) and t["spmv_blocks"] in (4, 6, 8)
+        assert t["asm_blocks"] in (5, 6, 7, 8, 10, 12) and t["spmv_blocks"] in (4, 5, 6, 8)
         assert t["asm_ms"] > 0 and t["spmv_ms"] > 0
         again = s.autotune(0)  # the cached choice
-        assert (again["asm_blocks"], again["spmv_blocks"], again["asm_staged"]) == \
-            (t["asm_blocks"], t["spmv_blocks"], t["asm_staged"])
+        assert (again["asm_blocks"], again["spmv_blocks"], again["asm_staged"],
+                again["spmv_staged"]) == (t["asm_blocks"], t["spmv_blocks"], t["asm_staged"],
+                                          t["spmv_staged"])
         s.run()
         assert all(s.state(m)[3] == 1 for m in range(len(cases)))
