@@ -782,6 +782,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// 4-byte asynchronous copy global -> shared (no register holds the value);
+// the issuing thread sees its copies after cp_async_wait_all().
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
 // A block waits at most this long (global timer, ns) for its copies of a
 // few KB, which land within microseconds; after that it flags the failure
 // and returns, and blocks that start after a failure do not wait at all.
@@ -3461,6 +3470,74 @@ __device__ __forceinline__ void pcg_xz_entry(int bid, const int32_t* bm_mem, con
   block_accumulate_t<float, 2>(dd, sc + (size_t)m * SC_N + SC_RR);
 }
 
+// The same PCG step for small work sets (at most one block per SM): each
+// thread first copies every layer of its column -- r, q, p, x, the factor
+// and the Dirichlet word -- into shared memory with 4-byte cp.async copies,
+// all in flight at once, then runs both sweeps on shared memory (y kept
+// there for the backward sweep).  The arithmetic and its order are those
+// of pcg_xz_entry; only the loads are issued differently (one round instead
+// of one per chunk of layers and sweep).  stg: 7 * nls * blockDim.x words.
+__device__ __forceinline__ void pcg_xz_entry_staged(
+    int bid, const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+    const uint8_t* active, const MemberScal* ms, double* sc, const float* __restrict__ pinv,
+    const float* __restrict__ cdown, float* __restrict__ r, float* __restrict__ x,
+    const float* __restrict__ p, const float* __restrict__ q, float* __restrict__ z,
+    const uint8_t* __restrict__ dmask, float* stg, int nls) {
+  const int m = bm_mem[bid];
+  if (!active[m]) return;  // block-uniform
+  float dd[2] = {0.0f, 0.0f};  // rr, qz
+  const int top = bm_r0[bid] + threadIdx.x;
+  float alfa = 0.0f;
+  if ((threadIdx.x & 31) == 0)
+    alfa = (float)(sc[(size_t)m * SC_N + SC_PR] / sc[(size_t)m * SC_N + SC_PQ]);
+  alfa = __shfl_sync(0xffffffffu, alfa, 0);
+  const int T = blockDim.x, t = threadIdx.x;
+  float* sr = stg;
+  float* sq = stg + (size_t)nls * T;
+  float* spp = stg + (size_t)2 * nls * T;
+  float* sx = stg + (size_t)3 * nls * T;
+  float* spv = stg + (size_t)4 * nls * T;
+  float* scd = stg + (size_t)5 * nls * T;
+  uint32_t* sdm = reinterpret_cast<uint32_t*>(stg + (size_t)6 * nls * T);
+  if (top < bm_r1[bid]) {
+    const int nnod = ms[m].nnod, nl = min(ms[m].nstr + 1, nls);
+    for (int k = 0; k < nl; ++k) {
+      const int i = top + k * nnod, o = k * T + t;
+      cp_async4(sr + o, r + i);
+      cp_async4(sq + o, q + i);
+      cp_async4(spp + o, p + i);
+      cp_async4(sx + o, x + i);
+      cp_async4(spv + o, pinv + i);
+      cp_async4(scd + o, cdown + i);
+      cp_async4(sdm + o, reinterpret_cast<const uint32_t*>(dmask) + (i >> 2));
+    }
+    cp_async_wait_all();
+    float yprev = 0.0f, cprev = 0.0f, pprev = 0.0f;
+    for (int k = 0; k < nl; ++k) {
+      const int i = top + k * nnod, o = k * T + t;
+      const float ri = sr[o] - alfa * sq[o];
+      r[i] = ri;
+      x[i] = sx[o] + alfa * spp[o];
+      const bool dm = ((sdm[o] >> (8 * (i & 3))) & 0xffu) != 0u;
+      if (!dm) dd[0] += ri * ri;
+      const float yk = ri - cprev * yprev * pprev;
+      sr[o] = yk;
+      yprev = yk;
+      cprev = scd[o];
+      pprev = spv[o];
+    }
+    float znext = 0.0f;
+    for (int k = nl - 1; k >= 0; --k) {
+      const int o = k * T + t;
+      const float zk = (sr[o] - scd[o] * znext) * spv[o];
+      z[top + k * nnod] = zk;
+      dd[1] += sq[o] * zk;
+      znext = zk;
+    }
+  }
+  block_accumulate_t<float, 2>(dd, sc + (size_t)m * SC_N + SC_RR);
+}
+
 // The per-member PCG decision after a step (GRADDP's stopping test: the
 // masked recursive residual against TOLCG, and the iteration cap), the next
 // beta = -q.z / p.q, the Krylov scalars cleared for the next step, and the
@@ -3494,6 +3571,9 @@ __device__ __forceinline__ int pcg_decide(int nmem, uint8_t* active, double* sc,
   return s_cnt;
 }
 
+// kStaged: the shared-memory form of the column pass (small work sets;
+// dynamic shared memory of 7 * nls * blockDim.x words)
+template <bool kStaged = false>
 __global__ void __launch_bounds__(kThreads)
 k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
              uint8_t* active, const MemberScal* ms, double* sc, const float* __restrict__ pinv,
@@ -3502,9 +3582,15 @@ k_pcg_xz_f32(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
              const uint8_t* __restrict__ dmask, int nmem,
              int32_t* niter, int itmax, double tol, int32_t* loops, int maxloops,
              unsigned int* done, int32_t* nact, int use_cond, cudaGraphConditionalHandle h,
-             const int32_t* amem_cum, int32_t* kact) {
+             const int32_t* amem_cum, int32_t* kact, int nls) {
+  extern __shared__ __align__(16) float dsm_xz[];
   pdl_enter();
-  pcg_xz_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, active, ms, sc, pinv, cdown, r, x, p, q, z, dmask);
+  if (kStaged)
+    pcg_xz_entry_staged(blockIdx.x, bm_mem, bm_r0, bm_r1, active, ms, sc, pinv, cdown, r, x, p,
+                        q, z, dmask, dsm_xz, nls);
+  else
+    pcg_xz_entry(blockIdx.x, bm_mem, bm_r0, bm_r1, active, ms, sc, pinv, cdown, r, x, p, q, z,
+                 dmask);
   __shared__ int s_last;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -3754,6 +3840,10 @@ struct Engine {
   // entry with the most slots, widened to 16-byte units), and whether to use it
   int spmv_stage_bytes = 0;
   bool spmv_staged = false;
+  // staged column pass: layers of the deepest member and its dynamic
+  // shared memory (0: unavailable)
+  int xz_layers = 0;
+  size_t xz_smem = 0;
   DBuf<int32_t> d_stage_err;
   // the autotuner's choice among the assemblies (0 direct loads, 1 staged
   // with 16 lanes per row, 2 staged with 8 lanes per row); by default the
@@ -3841,6 +3931,9 @@ struct Engine {
   // staged form (5 blocks/SM, two entries in flight per warp) when the
   // entry ranges are there and the schedule asks for it
   bool small_stream() const { return cbm16.nblk <= 2 * kStreamWarps * nsm; }
+  // the column pass in shared memory: small work sets (one block per SM at
+  // most) whose columns fit the staging area
+  bool staged_columns() const { return xz_smem > 0 && cbms.nblk <= nsm; }
   bool staged_stream() const {
     return spmv_staged && !small_stream() && cbm16.ent.p && spmv_stage_bytes > 0;
   }
@@ -4543,6 +4636,14 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     d_stage_err.alloc(1);
     d_stage_err.zero(st);
     spmv_stage_bytes = (int)align16ll(4LL * stage_slot + 32);
+    for (int m = 0; m < nmem; ++m) xz_layers = std::max(xz_layers, M[m]->meshp->nstr + 1);
+    xz_smem = (size_t)7 * xz_layers * kThreads * 4;
+    if (xz_smem > (size_t)200 * 1024 ||
+        cudaFuncSetAttribute(k_pcg_xz_f32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)xz_smem) != cudaSuccess) {
+      cudaGetLastError();
+      xz_smem = 0;
+    }
     int off[7];
     asm_stage_layout(stage_inc, stage_slot, stage_gl, stage_row_inc, off);
     stage_smem = (size_t)off[6];
@@ -4925,11 +5026,14 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
       }
       auto body = [&](int32_t* nact) {
         spmv_upd_f32(vals, z, p, q, r);
-        launch(k_pcg_xz_f32, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p, d_active.p,
-               d_ms.p, d_sc.p, (const float*)linv, (const float*)lc, r, x, (const float*)p,
-               (const float*)q, z, (const uint8_t*)d_dmask.p, nmem, d_niter.p, itmax, tol,
-               d_loops.p, itmax + 2, d_done.p, nact, phase == 2 ? 1 : 0, gh,
-               (const int32_t*)d_amem_cum.p, d_kact.p);
+        const bool xs = staged_columns();
+        next_smem = xs ? xz_smem : 0;
+        launch(xs ? k_pcg_xz_f32<true> : k_pcg_xz_f32<false>, cbms.nblk, kThreads, cbms.mem.p,
+               cbms.r0.p, cbms.r1.p, d_active.p, d_ms.p, d_sc.p, (const float*)linv,
+               (const float*)lc, r, x, (const float*)p, (const float*)q, z,
+               (const uint8_t*)d_dmask.p, nmem, d_niter.p, itmax, tol, d_loops.p, itmax + 2,
+               d_done.p, nact, phase == 2 ? 1 : 0, gh, (const int32_t*)d_amem_cum.p, d_kact.p,
+               xz_layers);
         count(2);
       };
       if (phase == 2) {
@@ -4947,12 +5051,12 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
               cbm1.r1.p, d_active.p, p, d_P.p + (size_t)it * N, nullptr, 0);
           k_copy_cast<VT, float><<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p,
               cbm1.r1.p, d_active.p, q, d_Q.p + (size_t)it * N, nullptr, 0);
-          launch(k_pcg_xz_f32, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+          launch(k_pcg_xz_f32<false>, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
                  d_active.p, d_ms.p, d_sc.p, (const float*)linv, (const float*)lc, r, x,
                  (const float*)p, (const float*)q, z, (const uint8_t*)d_dmask.p, nmem,
                  d_niter.p, itmax, tol, d_loops.p, itmax + 2, d_done.p,
                  look ? d_nact.p : d_nact_dummy.p, 0, gh, (const int32_t*)d_amem_cum.p,
-                 d_kact.p);
+                 d_kact.p, 0);
           count(4);
         } else {
           body(look ? d_nact.p : d_nact_dummy.p);
