@@ -3344,6 +3344,126 @@ __device__ __forceinline__ void pcg_setup_col_entry(int bb, const int32_t* s_mem
   }
 }
 
+// pcg_setup_col_entry in shared memory (small work sets): every layer's
+// Dirichlet word, slot indices and b in one round of cp.async copies, then
+// the two matrix entries per layer in a second, then both sweeps on shared
+// memory; the same arithmetic in the same order.  stg: 7 * nls * blockDim.x
+// words.
+__device__ __forceinline__ void pcg_setup_col_entry_staged(
+    int bb, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1,
+    const uint8_t* active, const MemberScal* ms, const int32_t* diag, const int32_t* down,
+    const float* vals, const uint8_t* dmask, float* pinv, float* cdown, const float* b,
+    float* x, float* stg, int nls) {
+  const int m = s_mem[bb];
+  if (!active[m]) return;
+  const int top = s_r0[bb] + threadIdx.x;
+  if (top >= s_r1[bb]) return;
+  const int T = blockDim.x, t = threadIdx.x;
+  uint32_t* sdm = reinterpret_cast<uint32_t*>(stg);
+  int32_t* sid = reinterpret_cast<int32_t*>(stg + (size_t)nls * T);
+  int32_t* siw = reinterpret_cast<int32_t*>(stg + (size_t)2 * nls * T);
+  float* sb = stg + (size_t)3 * nls * T;
+  float* sa = stg + (size_t)4 * nls * T;
+  float* sc_ = stg + (size_t)5 * nls * T;
+  float* sy = stg + (size_t)6 * nls * T;
+  const int nnod = ms[m].nnod, nl = min(ms[m].nstr + 1, nls);
+  for (int k = 0; k < nl; ++k) {
+    const int i = top + k * nnod, o = k * T + t;
+    cp_async4(sdm + o, reinterpret_cast<const uint32_t*>(dmask) + (i >> 2));
+    cp_async4(sid + o, diag + i);
+    cp_async4(sb + o, b + i);
+    if (k + 1 < nl) cp_async4(siw + o, down + i);
+  }
+  cp_async_wait_all();
+  auto dmk = [&](int k) {
+    const int i = top + k * nnod;
+    return ((sdm[k * T + t] >> (8 * (i & 3))) & 0xffu) != 0u;
+  };
+  for (int k = 0; k < nl; ++k) {
+    const int o = k * T + t;
+    const bool dm = dmk(k), dmb = k + 1 < nl ? dmk(k + 1) : true;
+    if (!dm) cp_async4(sa + o, vals + sid[o]);
+    if (!dm && !dmb && k + 1 < nl && siw[o] >= 0) cp_async4(sc_ + o, vals + siw[o]);
+  }
+  cp_async_wait_all();
+  float piv_prev = 1.0f, c_prev = 0.0f, yprev = 0.0f, pv_prev = 0.0f;
+  for (int k = 0; k < nl; ++k) {
+    const int i = top + k * nnod, o = k * T + t;
+    const bool dm = dmk(k), dmb = k + 1 < nl ? dmk(k + 1) : true;
+    const float a = dm ? 1.0f : sa[o];
+    const float c = (!dm && !dmb && k + 1 < nl && siw[o] >= 0) ? sc_[o] : 0.0f;
+    const float piv = a - c_prev * c_prev / piv_prev;
+    const float pv = 1.0f / piv;
+    pinv[i] = pv;
+    cdown[i] = c;
+    const float yk = sb[o] - c_prev * yprev * pv_prev;
+    sy[o] = yk;
+    sa[o] = pv;  // the factor, kept for the backward sweep
+    sc_[o] = c;
+    yprev = yk;
+    pv_prev = pv;
+    piv_prev = piv;
+    c_prev = c;
+  }
+  float znext = 0.0f;
+  for (int k = nl - 1; k >= 0; --k) {
+    const int o = k * T + t;
+    const float zk = (sy[o] - sc_[o] * znext) * sa[o];
+    x[top + k * nnod] = zk;
+    znext = zk;
+  }
+}
+
+// z = T^-1 r in shared memory for small work sets (the FP32 form of
+// k_line_apply_b: r, the factor and w in one round of cp.async copies, both
+// sweeps on shared memory, the same arithmetic in the same order).
+__global__ void __launch_bounds__(kThreads)
+k_line_apply_staged(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                    const uint8_t* active, const MemberScal* ms, const float* pinv,
+                    const float* cdown, const float* r, float* z, const float* w, double* acc,
+                    int acc_stride, int acc_off, int nls) {
+  extern __shared__ __align__(16) float dsm_la[];
+  pdl_enter();
+  const int m = bm_mem[blockIdx.x];
+  if (!active[m]) return;
+  const int top = bm_r0[blockIdx.x] + threadIdx.x;
+  const int T = blockDim.x, t = threadIdx.x;
+  float* sr = dsm_la;
+  float* spv = dsm_la + (size_t)nls * T;
+  float* scd = dsm_la + (size_t)2 * nls * T;
+  float* sw = dsm_la + (size_t)3 * nls * T;
+  float dot[1] = {0.0f};
+  if (top < bm_r1[blockIdx.x]) {
+    const int nnod = ms[m].nnod, nl = min(ms[m].nstr + 1, nls);
+    for (int k = 0; k < nl; ++k) {
+      const int i = top + k * nnod, o = k * T + t;
+      cp_async4(sr + o, r + i);
+      cp_async4(spv + o, pinv + i);
+      cp_async4(scd + o, cdown + i);
+      if (w) cp_async4(sw + o, w + i);
+    }
+    cp_async_wait_all();
+    float yprev = 0.0f, cprev = 0.0f, pprev = 0.0f;
+    for (int k = 0; k < nl; ++k) {
+      const int o = k * T + t;
+      const float yk = sr[o] - cprev * yprev * pprev;
+      sr[o] = yk;
+      yprev = yk;
+      cprev = scd[o];
+      pprev = spv[o];
+    }
+    float znext = 0.0f;
+    for (int k = nl - 1; k >= 0; --k) {
+      const int o = k * T + t;
+      const float zk = (sr[o] - scd[o] * znext) * spv[o];
+      z[top + k * nnod] = zk;
+      if (w) dot[0] += sw[o] * zk;
+      znext = zk;
+    }
+  }
+  if (w) block_accumulate_t<float, 1>(dot, acc + (size_t)m * acc_stride + acc_off);
+}
+
 // Per-member part: iteration counts 1 and beta = 0 for the members of
 // block bb's slice of members; block 0 also builds the Krylov entry list.
 __device__ __forceinline__ void pcg_setup_members(int bb, int nmem, const uint8_t* active,
@@ -3357,6 +3477,7 @@ __device__ __forceinline__ void pcg_setup_members(int bb, int nmem, const uint8_
   if (bb == 0) build_kact(amem_cum, nmem, active, kact);
 }
 
+template <bool kStaged = false>
 __global__ void __launch_bounds__(kThreads)
 k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t* s_r1, int nc,
                 const int32_t* c_mem, const int32_t* c_r0, const int32_t* c_r1,
@@ -3364,7 +3485,8 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
                 const int32_t* __restrict__ down, const float* __restrict__ vals,
                 const uint8_t* __restrict__ dmask, float* pinv, float* cdown,
                 const float* __restrict__ b, float* x, double* sc, int nmem,
-                int32_t* niter, const int32_t* amem_cum, int32_t* kact) {
+                int32_t* niter, const int32_t* amem_cum, int32_t* kact, int nls) {
+  extern __shared__ __align__(16) float dsm_su[];
   pdl_enter();
   int bb = blockIdx.x;
   if (bb >= ns) {
@@ -3376,8 +3498,12 @@ k_pcg_setup_f32(int ns, const int32_t* s_mem, const int32_t* s_r0, const int32_t
     pcg_setup_members(bb - nc, nmem, active, niter, sc, amem_cum, kact);
     return;
   }
-  pcg_setup_col_entry(bb, s_mem, s_r0, s_r1, active, ms, diag, down, vals, dmask, pinv, cdown, b,
-                      x);
+  if (kStaged)
+    pcg_setup_col_entry_staged(bb, s_mem, s_r0, s_r1, active, ms, diag, down, vals, dmask, pinv,
+                               cdown, b, x, dsm_su, nls);
+  else
+    pcg_setup_col_entry(bb, s_mem, s_r0, s_r1, active, ms, diag, down, vals, dmask, pinv, cdown,
+                        b, x);
 }
 
 // One column-line PCG step after the fused direction update + product
@@ -4640,6 +4766,10 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     xz_smem = (size_t)7 * xz_layers * kThreads * 4;
     if (xz_smem > (size_t)200 * 1024 ||
         cudaFuncSetAttribute(k_pcg_xz_f32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)xz_smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_pcg_setup_f32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)xz_smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_line_apply_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)xz_smem) != cudaSuccess) {
       cudaGetLastError();
       xz_smem = 0;
@@ -5001,11 +5131,14 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
         }
         // column-line factor with x0 = T^-1 b | |b|^2 | iteration counts,
         // beta = 0; then r = b - A x0 and z = T^-1 r
-        launch(k_pcg_setup_f32, cbms.nblk + cbm1.nblk + cdiv(nmem, kThreads), kThreads,
+        const bool xs = staged_columns();
+        next_smem = xs ? xz_smem : 0;
+        launch(xs ? k_pcg_setup_f32<true> : k_pcg_setup_f32<false>,
+               cbms.nblk + cbm1.nblk + cdiv(nmem, kThreads), kThreads,
                cbms.nblk, cbms.mem.p, cbms.r0.p, cbms.r1.p, cbm1.nblk, cbm1.mem.p, cbm1.r0.p,
                cbm1.r1.p, (const uint8_t*)d_active.p, d_ms.p, d_diag.p, d_down.p, vals,
                d_dmask.p, linv, lc, (const float*)b, x, d_sc.p, nmem, d_niter.p,
-               (const int32_t*)d_amem_cum.p, d_kact.p);
+               (const int32_t*)d_amem_cum.p, d_kact.p, xs ? xz_layers : 0);
         count();
         if (lp_mode == 2) {
           // learned factor for the members that use it, then x0 = T^-1 b again
@@ -5017,9 +5150,17 @@ void Engine::solve_pcg(int itmax, double tol, bool ref_mode, int chk, int phase,
           count(2);
         }
         resid_f32(vals, x, b, r);
-        launch(k_line_apply<VT>, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
-               d_active.p, d_ms.p, linv, lc, (const VT*)r, z, (const VT*)nullptr, d_sc.p,
-               (int)SC_N, (int)SC_QZ);
+        if (xs) {
+          next_smem = xz_smem;
+          launch(k_line_apply_staged, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+                 (const uint8_t*)d_active.p, (const MemberScal*)d_ms.p, (const float*)linv,
+                 (const float*)lc, (const float*)r, (float*)z, (const float*)nullptr, d_sc.p,
+                 (int)SC_N, (int)SC_QZ, xz_layers);
+        } else {
+          launch(k_line_apply<VT>, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+                 d_active.p, d_ms.p, linv, lc, (const VT*)r, z, (const VT*)nullptr, d_sc.p,
+                 (int)SC_N, (int)SC_QZ);
+        }
         count(2);
         check_launch();
         if (phase == 1) return;
