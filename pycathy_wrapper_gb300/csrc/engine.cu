@@ -3672,10 +3672,10 @@ __device__ __forceinline__ void pcg_xz_entry_staged(
 __device__ __forceinline__ int pcg_decide(int nmem, uint8_t* active, double* sc, int32_t* niter,
                                           int itmax, double tol, const int32_t* amem_cum,
                                           int32_t* kact) {
-  __shared__ int s_cnt;
-  if (threadIdx.x == 0) s_cnt = 0;
+  __shared__ int s_cnt, s_left;
+  if (threadIdx.x == 0) s_cnt = s_left = 0;
   __syncthreads();
-  int mine = 0;
+  int mine = 0, left = 0;
   for (int mm = threadIdx.x; mm < nmem; mm += blockDim.x) {
     if (!active[mm]) continue;
     double* S = sc + (size_t)mm * SC_N;
@@ -3688,12 +3688,15 @@ __device__ __forceinline__ int pcg_decide(int nmem, uint8_t* active, double* sc,
       mine++;
     } else {
       active[mm] = 0;
+      left++;
     }
     S[SC_PR] = S[SC_PQ] = S[SC_QZ] = S[SC_RR] = 0.0;
   }
   if (mine) atomicAdd(&s_cnt, mine);
+  if (left) atomicAdd(&s_left, left);
   __syncthreads();
-  build_kact(amem_cum, nmem, active, kact);
+  // the entry list changes only when a member leaves the solve
+  if (s_left) build_kact(amem_cum, nmem, active, kact);
   return s_cnt;
 }
 
@@ -4556,7 +4559,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   d_nodal[ND_ATMACT].upload(h_atmact.data(), N, st);
   d_nodal[ND_ATMOLD].upload(h_atmold.data(), N, st);
   d_sdir.alloc(N); d_sdir.upload(h_sdir.data(), N, st);
-  // (+4: the pipelined assembly copies these byte arrays as aligned words)
+  // (+4: the shared-memory column passes copy these byte arrays as aligned words)
   d_dmask.alloc(N + 4); d_dmask.zero(st);
   d_ifatm.alloc(N + 4); d_ifatm.zero(st); d_ifatm.upload(h_ifatm.data(), N, st);
   d_ifatmp.alloc(N); d_ifatmp.upload(h_ifatmp.data(), N, st);
