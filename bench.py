@@ -329,7 +329,8 @@ def run_large(args):
         cases[0].parm.precond = 2
         steps = 0
     else:
-        cases = [config4_member(300, 25, seed=k, tmax=43200.0) for k in range(32)]
+        nm = min(args.members, 32)  # 32 members by default; fewer for a profiling run
+        cases = [config4_member(300, 25, seed=k, tmax=43200.0) for k in range(nm)]
         steps = max(args.steps, 1)
     free0 = torch.cuda.mem_get_info()[0]
     t0 = time.perf_counter()
