@@ -700,6 +700,101 @@ k_assemble_newton(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm
   }
 }
 
+// The Newton assembly with the row's incidences spread over its 16 lanes:
+// in rounds of 16 incidences each lane forms one incidence's contributions
+// (to the row's four element-node slots and its five right-hand-side
+// terms) and parks them in shared memory; then each slot's lane adds the
+// round's contributions to its slot, and lanes 0..4 their RHS terms, in
+// incidence order.  Every term and every sum is formed as in
+// k_assemble_newton, which walks all of the row's incidences in every lane
+// (16 times the loads and a chain of dependent gathers per incidence).
+template <class MT>
+__global__ void __launch_bounds__(kThreads)
+k_assemble_newton_par(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                      const uint8_t* act, const MemberScal* ms,
+                      const int32_t* rowptr, const int32_t* cols,
+                      const int32_t* inc_ptr, const int32_t* inc, const int4* tet,
+                      const TetRec<MT>* rec, Nodal nd, MT* vals, double lm_d,
+                      double lm_o) {
+  __shared__ double sc_[kRowsPerBlock16][kGroup][4];  // slot contributions per incidence
+  __shared__ double sr_[kRowsPerBlock16][kGroup][5];  // RHS terms per incidence (4: kr)
+  __shared__ double sg_[kRowsPerBlock16][kGroup];     // gravity term g_k
+  __shared__ int sn_[kRowsPerBlock16][kGroup][4];     // the element's node ids
+  const int m = bm_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  const int grp = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int i = bm_r0[blockIdx.x] + grp;
+  const bool rowok = i < bm_r1[blockIdx.x];
+  const MemberScal& S = ms[m];
+  const double rdt = 1.0 / S.deltat, th = S.tetaf;
+  int s0 = 0, s1 = 0, col = -1;
+  if (rowok) {
+    s0 = rowptr[i]; s1 = rowptr[i + 1];
+    if (s0 + lane < s1) col = cols[s0 + lane];
+  }
+  double lhs = 0.0, rpart = 0.0;
+  const int p0 = rowok ? inc_ptr[i] : 0, p1 = rowok ? inc_ptr[i + 1] : 0;
+  int nround = (p1 - p0 + kGroup - 1) / kGroup;
+  nround = max(nround, __shfl_xor_sync(0xffffffffu, nround, 16));
+  for (int rd = 0; rd < nround; ++rd) {
+    const int q = rd * kGroup + lane;
+    if (p0 + q < p1) {
+      const int ek = inc[p0 + q];
+      const int e = ek >> 2, k = ek & 3;
+      const int4 t = tet[e];
+      const int tn[4] = {t.x, t.y, t.z, t.w};
+      const TetRec<MT> R = rec[e];
+      const double kr = 0.25 * (nd.ckrw[t.x] + nd.ckrw[t.y] + nd.ckrw[t.z] + nd.ckrw[t.w]);
+      const double ee = 0.25 * (nd.etai[t.x] + nd.etai[t.y] + nd.etai[t.z] + nd.etai[t.w]);
+      const double ve = (double)R.vol * ee;
+      double sum = 0.0, sum1 = 0.0;
+#pragma unroll
+      for (int qq = 0; qq < 4; ++qq) {
+        sum += (double)R.S[sym_idx(k, qq)] * nd.ptnew[tn[qq]];
+        sum1 += ((qq == k) ? lm_d : lm_o) * (nd.pnew[tn[qq]] - nd.ptimep[tn[qq]]);
+      }
+      const double tsumtd = th * sum + th * (double)R.g[k];
+      const double sum1tv = sum1 * th * (double)R.vol * rdt;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const double lm = (l == k) ? lm_d : lm_o;
+        sc_[grp][lane][l] = th * (kr * (double)R.S[sym_idx(k, l)]) + ve * lm * rdt +
+                            nd.dckrw[tn[l]] * tsumtd + nd.detai[tn[l]] * sum1tv;
+        sr_[grp][lane][l] = kr * (double)R.S[sym_idx(k, l)] * nd.ptnew[tn[l]] +
+                            ve * lm * rdt * (nd.pnew[tn[l]] - nd.ptimep[tn[l]]);
+        sn_[grp][lane][l] = tn[l];
+      }
+      sr_[grp][lane][4] = kr;
+      sg_[grp][lane] = (double)R.g[k];
+    }
+    __syncwarp();
+    const int nq = min(kGroup, p1 - p0 - rd * kGroup);
+    for (int qq = 0; qq < nq; ++qq) {
+      if (col >= 0) {
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+          if (sn_[grp][qq][l] == col) lhs += sc_[grp][qq][l];
+      }
+      if (lane < 4) rpart -= sr_[grp][qq][lane];
+      else if (lane == 4) rpart -= sr_[grp][qq][4] * sg_[grp][qq];
+    }
+    __syncwarp();
+  }
+  const double rhs = group_sum16(rpart);
+  if (!rowok) return;
+  if (col >= 0) vals[s0 + lane] = (MT)lhs;
+  if (lane == 0) {
+    nd.xt5[i] = rhs;
+    double b = rhs;
+    const int loc = nd.loc[i];
+    if (nd.dmask[i]) b = 0.0;
+    else if (loc < S.nnod && nd.ifatm[i] == 0)
+      b += th * nd.atmact[i] + (1.0 - th) * nd.atmold[i];
+    b += nd.qneu[i];
+    nd.rhs[i] = b;
+  }
+}
+
 // ============================================================================
 // sparse kernels
 // ============================================================================
@@ -5006,8 +5101,9 @@ void Engine::assemble() {
     k_assemble_picard<MT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_act.p,
         d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, rec, nd, vals, lm_d, lm_o);
   else
-    k_assemble_newton<MT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p, cbm16.r1.p, d_act.p,
-        d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, rec, nd, vals, lm_d, lm_o);
+    k_assemble_newton_par<MT><<<cbm16.nblk, kThreads, 0, st>>>(cbm16.mem.p, cbm16.r0.p,
+        cbm16.r1.p, d_act.p, d_ms.p, d_rowptr.p, d_cols.p, d_inc_ptr.p, d_inc.p, d_tet.p, rec, nd,
+        vals, lm_d, lm_o);
   check_launch();
   count();
 }

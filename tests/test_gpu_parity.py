@@ -297,49 +297,6 @@ def test_newton_chord_slope_kslope1_matches_oracle():
     assert np.max(np.abs(p - po)) <= 1e-6
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_chord_slope_kslope1_matches_oracle(precision):
-    """KSLOPE=1 (CHPIC1, chpic1.f:25-48): the storage coefficient is the
-    chord slope of Se between PTOLD and PTNEW.  TOLKSL is lowered so that
-    the chord branch is taken at most nodes of the hillslope's iterations."""
-    from pycathy_wrapper_gb300.inputs import config0
-    import oracle as O
-    case = config0(tmax=3600.0, precond=0)
-    case.soil.kslope, case.soil.tolksl = 1, 1e-7
-    o = O.Oracle(case)
-    for _ in range(20):
-        o.step()
-    base = config0(tmax=3600.0, precond=0)
-    o0 = O.Oracle(base)
-    for _ in range(20):
-        o0.step()
-    gcase = config0(tmax=3600.0, precond=0 if precision == 0 else 2)
-    gcase.soil.kslope, gcase.soil.tolksl = 1, 1e-7
-    with _sim(gcase, precision=precision) as s:
-        for _ in range(20):
-            s.step()
-        p, t, dt, st = s.state(0)
-        its, sts = s.records(0)
-    po, to, _ = o.state()
-    # the chord branch changes the solution path (else the test is vacuous)
-    assert np.max(np.abs(po - o0.state()[0])) > 1e-9 or \
-        [r["iter"] for r in o.step_records()] != [r["iter"] for r in o0.step_records()]
-    assert abs(sts[-1]["time"] - o.step_records()[-1]["time"]) < 1e-9
-    assert [r["iter"] for r in sts] == [r["iter"] for r in o.step_records()]
-    assert np.max(np.abs(p - po)) <= 1e-6
-
-
-def test_newton_chord_slope_kslope1_matches_oracle():
-    """KSLOPE=1 on the Newton branch (CHNEW1, chnew1.f:27-53): chord slopes
-    of the storage, its derivative and kr under ponded infiltration."""
-    from pycathy_wrapper_gb300.inputs import config4_member
-    case = config4_member(ncell=12, nstr=8, tmax=600.0)
-    case.soil.kslope, case.soil.tolksl = 1, 1e-3
-    o, (p, t, sts, its), (po, osr, oir) = _run_both(case, 8)
-    assert [r["iter"] for r in sts] == [r["iter"] for r in osr]
-    assert np.max(np.abs(p - po)) <= 1e-6
-
-
 def test_staged_spmv_gives_the_same_heads():
     """The stream SpMV's staged form (each warp copies its next map entry's
     values and columns into shared memory while it multiplies the current
