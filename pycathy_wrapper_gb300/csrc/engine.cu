@@ -1740,19 +1740,21 @@ __global__ void k_ilu0_level(int nrows, const int32_t* rows, const int32_t* rowp
     return;
   }
   for (int s = s0; s < s1; ++s) F[s] = dmask[cols[s]] ? (FT)0 : (FT)vals[s];
+  // (in the factor's own type: an FP64 division or update costs about 16
+  // FP32 ones on this GPU, and the FP32 factor preconditions an FP32 solve)
   for (int s = s0; s < sd; ++s) {
     const int k = cols[s];
     if (dmask[k]) continue;
-    const double l = (double)F[s] / (double)F[diag[k]];
-    F[s] = (FT)l;
+    const FT l = F[s] / F[diag[k]];
+    F[s] = l;
     int pi = s + 1;
     for (int t = diag[k] + 1; t < rowptr[k + 1]; ++t) {
       const int j = cols[t];
       while (pi < s1 && cols[pi] < j) ++pi;
-      if (pi < s1 && cols[pi] == j) F[pi] = (FT)((double)F[pi] - l * (double)F[t]);
+      if (pi < s1 && cols[pi] == j) F[pi] = F[pi] - l * F[t];
     }
   }
-  if ((double)F[sd] == 0.0) F[sd] = (FT)1;
+  if (F[sd] == (FT)0) F[sd] = (FT)1;
 }
 
 template <class FT>
