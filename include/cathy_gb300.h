@@ -61,6 +61,14 @@ typedef struct cathy_soil {
                                   between PTOLD and PTNEW once they differ
                                   by TOLKSL (chpic1.f, chnew1.f)           */
   double tolksl;
+  /* Feddes root-water uptake, ETRAN (etran.f:6-81), used when scf > 0:
+     nveg rows of PCANA PCREF PCWLT ZROOT PZ OMGC (datin.f:424-428) and the
+     input/root_map raster (nrow*ncol like the DEM, datin.f:221-233; NULL =
+     vegetation type 1 everywhere).  The Picard right-hand side loses
+     QTRANIE (bcpic.f:84-86); the Newton one does not (bcnew.f).           */
+  int32_t nveg;
+  const double* feddes;
+  const double* root_map;
 } cathy_soil_t;
 
 /* input/parm keys (datin.f:81-117) */

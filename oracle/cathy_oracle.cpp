@@ -495,6 +495,10 @@ struct Oracle {
   dvec permx, permy, permz, elstor, poros, vgncell, vgrmccell, vgpsatcell;
   double pmin = -5.0, scf = 0.0, tolksl = 0.01;
   int kslope = 0;
+  // Feddes root-water uptake (SOILCHAR.H /FEDDES/): VEG_TYPE per surface
+  // node and 6 parameters per type (PCANA, PCREF, PCWLT, ZROOT, PZ, OMGC)
+  ivec veg_type;
+  dvec feddes;
   // nodal soil parameters (SOILCHAR.H) and element porosity
   dvec pnodi, snodi, vgn, vgm, vgrmc, vgpsat, vgn1, vgm52, vgnr, vgmm1, vgmr,
       vgpsn, vgpnot, pel;
@@ -624,6 +628,7 @@ struct Oracle {
   void masbal(void);
   void conver(void);
   void switch_old(void);
+  void etran(void);
   bool flow3d(bool first_only);
   void atm_read_next(double& t, dvec& v, bool& ok);
   void atmone(void);
@@ -1572,6 +1577,52 @@ void Oracle::bkstep() {
   ptold = ptnew;
 }
 
+// ETRAN (etran.f:6-81): root water uptake QTRANIE of the new time step
+// from PNEW before SWITCH_OLD and the new ATMPOT; with SCF = 0 the potential
+// transpiration ETP is zero and so is QTRANIE.  The reference stops when a
+// root zone reaches the bottom node (etran.f:60-65); orc_create rejects such
+// a mesh instead.
+void Oracle::etran() {
+  for (int k = 1; k <= n; ++k) qtranie[k] = 0.0;
+  if (scf <= 0.0) return;
+  dvec btrani(n + 1, 0.0);
+  dvec btran(nnod + 1, 0.0), omg(nnod + 1, 0.0), etp(nnod + 1, 0.0);
+  for (int i = 1; i <= nnod; ++i) {
+    const double* fp = &feddes[6 * (veg_type[i] - 1)];
+    const double pcana = fp[0], pcref = fp[1], pcwlt = fp[2], zroot = fp[3], pz = fp[4];
+    int j = 1;
+    const double zsurf = z[i];
+    double depth = 0.0;
+    etp[i] = (atmpot[i] < 0.0) ? -1.0 * scf * atmpot[i] : 0.0;
+    while (depth <= zroot) {
+      const int k = (j - 1) * nnod + i;
+      const double s1 = pcana, s2 = pcana + 1.0e-3;
+      const double dz = (j == 1) ? (zsurf - z[k + nnod]) / 2.0 : (z[k - nnod] - z[k + nnod]) / 2.0;
+      const double sh2o = pnew[k];
+      double gx1 = (sh2o - pcwlt) / (pcref - pcwlt);
+      gx1 = std::min(1.0, std::max(0.0, gx1));
+      double gx2 = 1.0 - (sh2o - s1) / (s2 - s1);
+      gx2 = std::min(1.0, std::max(0.0, gx2));
+      const double gx = std::min(gx1, gx2);
+      const double beta = (1 - depth / zroot) * std::exp(-1.0 * pz * depth / zroot);
+      btrani[k] = std::max(0.0, beta * dz * gx);
+      btran[i] = btran[i] + beta * dz;
+      omg[i] = omg[i] + gx * beta * dz;
+      j = j + 1;
+      depth = zsurf - z[(j - 1) * nnod + i];  // in range: checked in orc_create
+    }
+    btran[i] = std::max(0.0, btran[i]);
+    omg[i] = omg[i] / btran[i];
+  }
+  for (int i = 1; i <= nnod; ++i) {
+    const double omgc = feddes[6 * (veg_type[i] - 1) + 5];
+    for (int j = 1; j <= nstr + 1; ++j) {
+      const int k = (j - 1) * nnod + i;
+      qtranie[k] = etp[i] * btrani[k] / btran[i] / std::max(omg[i], omgc);
+    }
+  }
+}
+
 // One pass of the main time loop (cathy_main.f:2882-3843) for FL3D, no
 // surface routing.  Returns 0 = step accepted, 1 = abort (no back-step
 // possible), 2 = finished.
@@ -1579,7 +1630,7 @@ int Oracle::step() {
   if (finished) return 2;
   // input/interpolate BCs for the new time level, switching (cathy_main.f:2886-2945)
   atmnxt();
-  for (int k = 1; k <= n; ++k) qtranie[k] = 0.0;  // ETRAN with ATMPOT >= 0
+  etran();
   switch_old();
   pold = pnew;
   for (int k = 1; k <= n; ++k)
@@ -1650,6 +1701,42 @@ void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,
   o->pmin = soil->pmin; o->scf = soil->scf; o->kslope = soil->kslope;
   o->tolksl = soil->tolksl;
   o->pondh_min = (parm->isimgr <= 1) ? 1.0e10 : parm->pondh_min;  // datin.f:123
+  // VEG_TYPE (datin.f:221-233): TRIANGOLI + TPNODI2D applied to the root
+  // map, i.e. the mean of FACTOR * map over the triangles of each surface
+  // node, truncated; the map must be active on the DEM's cells
+  o->veg_type.assign(o->nnod + 1, 1);
+  if (soil->scf > 0.0) {
+    if (soil->nveg < 1 || !soil->feddes) { delete o; return nullptr; }
+    o->feddes.assign(soil->feddes, soil->feddes + 6 * (size_t)soil->nveg);
+    if (soil->root_map) {
+      dvec sum(o->nnod + 1, 0.0);
+      ivec cnt(o->nnod + 1, 0);
+      int itria = 0;
+      for (int i = 0; i < dem->nrow; ++i)
+        for (int j = 0; j < dem->ncol; ++j) {
+          const size_t c = (size_t)i * dem->ncol + j;
+          if (dem->dem[c] == 0.0) continue;
+          if (soil->root_map[c] == 0.0) { delete o; return nullptr; }
+          const double e = soil->root_map[c] * dem->factor;
+          for (int t = 0; t < 2; ++t) {
+            ++itria;
+            for (int v = 0; v < 3; ++v) {
+              const int nd = o->triang[itria * 4 + v];
+              sum[nd] += e;
+              cnt[nd] += 1;
+            }
+          }
+        }
+      for (int i = 1; i <= o->nnod; ++i) o->veg_type[i] = (int)(sum[i] / cnt[i]);
+    }
+    for (int i = 1; i <= o->nnod; ++i) {
+      const int vt = o->veg_type[i];
+      if (vt < 1 || vt > soil->nveg) { delete o; return nullptr; }
+      // the root zone must end above the bottom node (etran.f:60-65)
+      const double zroot = o->feddes[6 * (vt - 1) + 3];
+      if (o->z[i] - o->z[nstr * nnod + i] <= zroot) { delete o; return nullptr; }
+    }
+  }
   auto z0 = [&](dvec& v, size_t s) { v.assign(s, 0.0); };
   for (dvec* v : {&o->pnew, &o->pold, &o->ptnew, &o->ptold, &o->ptimep, &o->pdiff,
                   &o->swnew, &o->swtimep, &o->sw, &o->ckrw, &o->etai, &o->et1,
@@ -1769,7 +1856,7 @@ int32_t orc_run(void* h, int32_t max_steps) {
 void orc_first_iteration(void* h, orc_iter_rec_t* rec) {
   Oracle* o = (Oracle*)h;
   o->atmnxt();
-  for (int k = 1; k <= o->n; ++k) o->qtranie[k] = 0.0;
+  o->etran();
   o->switch_old();
   o->pold = o->pnew;
   for (int k = 1; k <= o->n; ++k)
@@ -1777,6 +1864,12 @@ void orc_first_iteration(void* h, orc_iter_rec_t* rec) {
   o->ptold = o->ptnew;
   o->flow3d(true);
   *rec = o->iter_recs.back();
+}
+
+void orc_get_qtranie(void* h, double* qtranie, int32_t* veg_type) {
+  Oracle* o = (Oracle*)h;
+  for (int k = 1; k <= o->n; ++k) qtranie[k - 1] = o->qtranie[k];
+  for (int i = 1; i <= o->nnod; ++i) veg_type[i - 1] = o->veg_type[i];
 }
 
 int32_t orc_num_iter_recs(void* h) { return (int32_t)((Oracle*)h)->iter_recs.size(); }

@@ -41,6 +41,13 @@ typedef struct orc_soil {
   double pmin, scf;
   int32_t kslope;   /* 0 or 1 */
   double tolksl;
+  /* Feddes root-water uptake (datin.f:424-428, etran.f): nveg rows of
+   * PCANA, PCREF, PCWLT, ZROOT, PZ, OMGC; root_map = input/root_map
+   * (nrow*ncol, row-major like the DEM) or NULL for vegetation type 1
+   * everywhere.  Needed only when scf > 0. */
+  int32_t nveg;
+  const double* feddes;
+  const double* root_map;
 } orc_soil_t;
 
 typedef struct orc_parm {
@@ -101,6 +108,9 @@ int32_t orc_num_step_recs(void* h);
 void orc_get_step_recs(void* h, orc_step_rec_t* out);
 
 void orc_get_state(void* h, double* pnew, double* time_dt2);  /* time, deltat */
+/* QTRANIE (n values, 1-based node k at out[k-1]) of the current time step
+ * and VEG_TYPE of the surface nodes (nnod values) */
+void orc_get_qtranie(void* h, double* qtranie, int32_t* veg_type);
 void orc_set_state(void* h, const double* ptimep, double time, double deltat);
 
 /* ---- fine-grained kernels on the current state (for unit parity) ---- */

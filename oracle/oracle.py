@@ -34,7 +34,8 @@ class OrcSoil(C.Structure):
         (k, f64p) for k in ("permx", "permy", "permz", "elstor", "poros", "vgn",
                             "vgrmc", "vgpsat")] + [
         ("pmin", C.c_double), ("scf", C.c_double), ("kslope", C.c_int32),
-        ("tolksl", C.c_double)]
+        ("tolksl", C.c_double), ("nveg", C.c_int32), ("feddes", f64p),
+        ("root_map", f64p)]
 
 
 class OrcParm(C.Structure):
@@ -97,6 +98,7 @@ def lib():
         L.orc_num_step_recs.argtypes = [C.c_void_p]
         L.orc_get_step_recs.argtypes = [C.c_void_p, C.POINTER(StepRec)]
         L.orc_get_state.argtypes = [C.c_void_p, f64p, f64p]
+        L.orc_get_qtranie.argtypes = [C.c_void_p, f64p, i32p]
         L.orc_set_state.argtypes = [C.c_void_p, f64p, C.c_double, C.c_double]
         L.orc_picard_system.argtypes = [C.c_void_p, f64p, f64p, f64p, i32p]
         L.orc_vg_nodal.argtypes = [C.c_void_p, f64p, f64p, f64p, f64p, f64p]
@@ -149,6 +151,14 @@ class Oracle:
                        tolksl=s.tolksl)
         for k in ("permx", "permy", "permz", "elstor", "poros", "vgn", "vgrmc", "vgpsat"):
             setattr(soil, k, F(getattr(s, k).reshape(-1)))
+        fed = getattr(s, "feddes", None)
+        if fed is not None:
+            fed = np.asarray(fed, dtype=np.float64).reshape(-1, 6)
+            soil.nveg = fed.shape[0]
+            soil.feddes = F(fed.reshape(-1))
+        rmap = getattr(s, "root_map", None)
+        if rmap is not None:
+            soil.root_map = F(np.asarray(rmap, dtype=np.float64).reshape(-1))
         parm = OrcParm(**{k: getattr(p, k) for k, _ in OrcParm._fields_})
         pinit = b.pinit if b.pinit is not None else np.zeros(1)
         bc = OrcBC(hspatm=b.hspatm, ieto=b.ieto, natm=len(b.atmtim),
@@ -215,6 +225,13 @@ class Oracle:
         td = np.zeros(2)
         lib().orc_get_state(self.h, _f64(p)[1], _f64(td)[1])
         return p, float(td[0]), float(td[1])
+
+    def qtranie(self):
+        """QTRANIE of the current time step (n) and VEG_TYPE (nnod)."""
+        q = np.zeros(self.n)
+        vt = np.zeros(self.nnod, dtype=np.int32)
+        lib().orc_get_qtranie(self.h, _f64(q)[1], vt.ctypes.data_as(i32p))
+        return q, vt
 
     def set_state(self, ptimep, time, deltat):
         a, ptr = _f64(ptimep)

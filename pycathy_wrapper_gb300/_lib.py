@@ -42,7 +42,8 @@ class Soil(C.Structure):
         (k, f64p) for k in ("permx", "permy", "permz", "elstor", "poros", "vgn",
                             "vgrmc", "vgpsat")] + [
         ("pmin", C.c_double), ("scf", C.c_double), ("kslope", C.c_int32),
-        ("tolksl", C.c_double)]
+        ("tolksl", C.c_double), ("nveg", C.c_int32), ("feddes", f64p),
+        ("root_map", f64p)]
 
 
 class Parm(C.Structure):

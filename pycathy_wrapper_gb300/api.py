@@ -63,6 +63,12 @@ def _member(case: Case, keep: _Keep) -> _lib.Member:
     soil = _lib.Soil(nzone=s.nzone, pmin=s.pmin, scf=s.scf, kslope=s.kslope, tolksl=s.tolksl)
     for k in ("permx", "permy", "permz", "elstor", "poros", "vgn", "vgrmc", "vgpsat"):
         setattr(soil, k, keep.f(getattr(s, k).reshape(-1)))
+    if s.feddes is not None:
+        fed = np.asarray(s.feddes, dtype=np.float64).reshape(-1, 6)
+        soil.nveg = fed.shape[0]
+        soil.feddes = keep.f(fed.reshape(-1))
+    if s.root_map is not None:
+        soil.root_map = keep.f(np.asarray(s.root_map, dtype=np.float64).reshape(-1))
     mem.soil = soil
     mem.parm = _lib.Parm(**{k: getattr(p, k) for k, _ in _lib.Parm._fields_})
     pinit = b.pinit if b.pinit is not None else np.zeros(1)

@@ -236,6 +236,12 @@ struct Nodal {  // per node
   // surface nodes (valid for loc < nnod)
   int8_t *ifatm, *ifatmp;
   double *arenod, *atmpot, *atmact, *atmold, *atm_a, *atm_b;
+  // Feddes root-water uptake (members with SCF > 0; null when no member has
+  // it): row of the Feddes table per surface node, the table (PCANA PCREF
+  // PCWLT ZROOT PZ OMGC per row), node elevations and QTRANIE of the step
+  const int32_t* vegi;
+  const double *fed, *zc;
+  double* qtran;
 };
 
 // ============================================================================
@@ -351,6 +357,66 @@ __global__ void k_geom(int nt, const int4* tet, const double* x, const double* y
 // surface part: BKSTEP restore + COMMIT bookkeeping + ATM update + switching
 // surface part of the step actions for surface node i: BKSTEP restore +
 // COMMIT bookkeeping + ATM update + switching
+// ETRAN (etran.f:21-79) for the column below surface node i: root water
+// uptake QTRANIE of the new time step from PNEW before SWITCH_OLD and the
+// new ATMPOT.  Column node j (0 = surface) is i + j * NNOD.  QTRANIE holds
+// BTRANI during the root-zone pass.  The host checked that every root zone
+// ends above the bottom node.  qn32: the FP32 Picard path's Neumann term,
+// Q - QTRANIE (bcpic.f:73-86), or null.
+__device__ __noinline__ void etran_column(int i, double pot, const MemberScal& S, Nodal& nd,
+                                          float* qn32) {
+  const int nnod = S.nnod;
+  const double* fp = nd.fed + 6 * nd.vegi[i];
+  const double pcana = fp[0], pcref = fp[1], pcwlt = fp[2], zroot = fp[3], pz = fp[4];
+  const double omgc = fp[5];
+  const double zsurf = nd.zc[i];
+  const double etp = (pot < 0.0) ? -1.0 * S.scf * pot : 0.0;
+  const double s1 = pcana, s2 = pcana + 1.0e-3;
+  double btran = 0.0, omg = 0.0, depth = 0.0;
+  int j = 0;
+  while (depth <= zroot) {
+    const int k = i + j * nnod;
+    const double dz = (j == 0) ? (zsurf - nd.zc[k + nnod]) / 2.0
+                               : (nd.zc[k - nnod] - nd.zc[k + nnod]) / 2.0;
+    const double sh2o = nd.pnew[k];
+    const double gx1 = fmin(1.0, fmax(0.0, (sh2o - pcwlt) / (pcref - pcwlt)));
+    const double gx2 = fmin(1.0, fmax(0.0, 1.0 - (sh2o - s1) / (s2 - s1)));
+    const double gx = fmin(gx1, gx2);
+    const double beta = (1 - depth / zroot) * exp(-1.0 * pz * depth / zroot);
+    nd.qtran[k] = fmax(0.0, beta * dz * gx);
+    btran = btran + beta * dz;
+    omg = omg + gx * beta * dz;
+    ++j;
+    depth = zsurf - nd.zc[i + j * nnod];
+  }
+  const int jr = j;
+  btran = fmax(0.0, btran);
+  omg = omg / btran;
+  const double den = fmax(omg, omgc);
+  for (j = 0; j <= S.nstr; ++j) {
+    const int k = i + j * nnod;
+    const double q = (j < jr) ? etp * nd.qtran[k] / btran / den : 0.0;
+    nd.qtran[k] = q;
+    if (qn32) qn32[k] = (float)(nd.qneu[k] - q);
+  }
+}
+
+// ATMNXT for surface node i: the potential flux of the new time level
+__device__ __forceinline__ double atm_pot_new(int i, const MemberScal& S, const Nodal& nd) {
+  double pot = nd.atmpot[i];
+  const double area = nd.arenod[i];
+  if (S.atm_mode == 1) {
+    double va = S.hspatm ? S.atm_va : nd.atm_a[i];
+    double vb = S.hspatm ? S.atm_vb : nd.atm_b[i];
+    double slope = (S.ieto != 0) ? 0.0 : (vb - va) / (S.atm_tb - S.atm_ta);
+    pot = (va + slope * (S.time - S.atm_ta)) * area;
+  } else if (S.atm_mode == 2) {
+    double vb = S.hspatm ? S.atm_vb : nd.atm_b[i];
+    pot = vb * area;
+  }
+  return pot;
+}
+
 __device__ __forceinline__ void start_surface_node(int i, uint8_t a, const MemberScal& S,
                                                    Nodal& nd) {
   int8_t f = nd.ifatm[i];
@@ -363,17 +429,7 @@ __device__ __forceinline__ void start_surface_node(int i, uint8_t a, const Membe
     nd.atmact[i] = nd.atmold[i];
   }
   if (a & ACT_START) {
-    double pot = nd.atmpot[i];
-    const double area = nd.arenod[i];
-    if (S.atm_mode == 1) {
-      double va = S.hspatm ? S.atm_va : nd.atm_a[i];
-      double vb = S.hspatm ? S.atm_vb : nd.atm_b[i];
-      double slope = (S.ieto != 0) ? 0.0 : (vb - va) / (S.atm_tb - S.atm_ta);
-      pot = (va + slope * (S.time - S.atm_ta)) * area;
-    } else if (S.atm_mode == 2) {
-      double vb = S.hspatm ? S.atm_vb : nd.atm_b[i];
-      pot = vb * area;
-    }
+    const double pot = atm_pot_new(i, S, nd);
     nd.atmpot[i] = pot;
     double act_ = nd.atmact[i];
     if (S.atm_mode != 0 && f == 0) act_ = (pot >= 0.0) ? pot : (1.0 - S.scf) * pot;
@@ -622,6 +678,7 @@ k_assemble_picard(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm
       b += th * nd.atmact[i] + (1.0 - th) * nd.atmold[i];
     }
     b += nd.qneu[i];
+    if (nd.qtran) b -= nd.qtran[i];  // root water uptake (bcpic.f:84-86)
     nd.rhs[i] = b;
   }
 }
@@ -2501,6 +2558,22 @@ __device__ __forceinline__ void start_vg_entry(int bid, const int32_t* bm_mem,
   }
   if (a & ACT_ITER) vg_f32_node(i, nd, nf, z, S);
 }
+// ETRAN once per time step, before the step actions of the surface nodes
+// (it reads PNEW before SWITCH_OLD) and not again after a back-step
+// (bkstep.f returns to the solver, cathy_main.f:3176 -> :2980).  Launched
+// only when some member has SCF > 0.
+__global__ void k_etran(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1,
+                        const uint8_t* act, const MemberScal* ms, Nodal nd, float* qn32) {
+  pdl_enter();
+  const int i = bm_r0[blockIdx.x] + threadIdx.x;
+  if (i >= bm_r1[blockIdx.x]) return;
+  const int m = bm_mem[blockIdx.x];
+  const uint8_t a = act[m];
+  const MemberScal& S = ms[m];
+  if (!(a & ACT_START) || (a & ACT_BACKSTEP) || !(S.scf > 0.0)) return;
+  etran_column(i, atm_pot_new(i, S, nd), S, nd, qn32);
+}
+
 __global__ void k_start_vg_f32(int nb1, const int32_t* bm_mem, const int32_t* bm_r0,
                                const int32_t* bm_r1, const uint8_t* act,
                                const MemberScal* ms, Nodal nd, NodalF nf, const double* z,
@@ -3926,6 +3999,8 @@ struct Engine {
   double lm_d = 0.25, lm_o = 0.0;
   std::vector<int32_t> node_off, tet_off, nnz_off;
   // device buffers
+  DBuf<int32_t> d_vegi;          // Feddes row per node (surface nodes)
+  DBuf<double> d_fed, d_qtran;    // Feddes table, QTRANIE
   DBuf<int32_t> d_mem, d_loc, d_node_off;
   DBuf<double> d_nodal[ND_NUM];
   DBuf<float> d_nodf[23];
@@ -3981,7 +4056,7 @@ struct Engine {
   // stats
   double gpu_ms = 0;
   int64_t launches = 0, lin_iters = 0, nl_iters = 0;
-  Nodal nd;
+  Nodal nd{};
   std::vector<MemberScal> h_ms;
   std::vector<uint8_t> h_act;
 
@@ -4456,6 +4531,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   std::vector<double> h_x(N), h_y(N), h_z(N), h_arenod(N, 0.0);
   std::vector<uint8_t> h_sdir(N, 0);
   std::vector<double> h_presc(N, 0.0), h_qneu(N, 0.0), h_pinit(N, 0.0);
+  std::vector<double> h_fed;     // Feddes rows of the members with SCF > 0
+  std::vector<int32_t> h_vegi;   // per node: row of h_fed (surface nodes)
   std::vector<double> tabs[8];
   std::vector<int32_t> soil_off(nmem + 1, 0);
   h_inc.reserve(4 * NT);
@@ -4573,6 +4650,25 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     h.scf = S.scf;
     h.kslope = S.kslope;
     h.tolksl = S.tolksl;
+    // Feddes root-water uptake (etran.f; VEG_TYPE as datin.f:221-233)
+    if (S.scf > 0.0) {
+      if (S.nveg < 1 || !S.feddes)
+        throw std::string("SCF > 0 needs the Feddes table (PCANA PCREF PCWLT ZROOT PZ OMGC)");
+      std::vector<int32_t> vt;
+      if (!node_map_types(mem[m].dem, S.root_map, g, vt))
+        throw std::string("root_map is 0 on an active DEM cell");
+      const int row0 = (int)(h_fed.size() / 6);
+      h_fed.insert(h_fed.end(), S.feddes, S.feddes + 6 * (size_t)S.nveg);
+      if (h_vegi.empty()) h_vegi.assign(N, 0);
+      for (int i = 0; i < g.nnod; ++i) {
+        if (vt[i] < 1 || vt[i] > S.nveg) throw std::string("vegetation type outside 1..NVEG");
+        const double zroot = S.feddes[6 * (vt[i] - 1) + 3];
+        // the reference stops here (etran.f:60-65: DECREASE ZROOT)
+        if (!(g.z[i] - g.z[(size_t)g.nstr * g.nnod + i] > zroot))
+          throw std::string("ZROOT reaches the bottom node of a column");
+        h_vegi[no + i] = row0 + vt[i] - 1;
+      }
+    }
     h.pondh_min = (h.parm.isimgr <= 1) ? 1.0e10 : h.parm.pondh_min;
     h.hspatm = B.hspatm; h.ieto = B.ieto; h.natm = B.natm;
     h.atm_t.assign(B.atmtim, B.atmtim + B.natm);
@@ -4746,6 +4842,12 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   nd.pmb = P(ND_PMB); nd.bet = P(ND_BET); nd.set = P(ND_SET);
   nd.mba = P(ND_MBA); nd.mbb = P(ND_MBB); nd.mbc = P(ND_MBC); nd.mbd = P(ND_MBD);
   nd.sdir = d_sdir.p; nd.dmask = d_dmask.p; nd.ifatm = d_ifatm.p; nd.ifatmp = d_ifatmp.p;
+  if (!h_fed.empty()) {
+    d_vegi.alloc(N); d_vegi.upload(h_vegi.data(), N, st);
+    d_fed.alloc(h_fed.size()); d_fed.upload(h_fed.data(), h_fed.size(), st);
+    d_qtran.alloc(N); d_qtran.zero(st);
+    nd.vegi = d_vegi.p; nd.fed = d_fed.p; nd.zc = P(ND_Z); nd.qtran = d_qtran.p;
+  }
   // TPNODI/CHPARM then geometry
   k_tpnodi<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, d_inc_ptr.p, d_inc.p, d_tetsoil.p,
       d_tab[4].p, d_tab[3].p, d_tab[5].p, d_tab[6].p, d_tab[7].p, nd);
@@ -5569,6 +5671,11 @@ void Engine::iteration_pre(int solve_phase) {
     // correction to opts.inner_tol.
     // step actions + soil characteristics + Krylov member flags in one pass
     phase(0);
+    if (cbms.nblk && nd.qtran) {
+      launch(k_etran, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+             (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf.qneu);
+      count();
+    }
     launch(k_start_vg_f32, cbm1.nblk + cdiv(nmem, kThreads), kThreads, cbm1.nblk, cbm1.mem.p,
            cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, nf, d_nodal[ND_Z].p, need_sw_flag(), nmem,
            d_active.p, d_red.p);
@@ -5655,6 +5762,11 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
 void Engine::start_kernels() {
   if (cbm1.nblk)
     k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 0, need_sw_flag());
+  if (cbms.nblk)
+  if (cbms.nblk && nd.qtran) {
+    k_etran<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p, nd, nf.qneu);
+    count();
+  }
   if (cbms.nblk)
     k_start_surface<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p, nd);
   if (cbm1.nblk)
@@ -5984,6 +6096,11 @@ int Engine::macro_iteration() {
       iteration_pre(0);
       iteration_post(true);
     } else if (cbm1.nblk) {
+      if (cbms.nblk && nd.qtran) {
+        launch(k_etran, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
+               (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf.qneu);
+        count();
+      }
       launch(k_start_vg_f32, cbm1.nblk + cdiv(nmem, kThreads), kThreads, cbm1.nblk, cbm1.mem.p,
              cbm1.r0.p, cbm1.r1.p, (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf,
              (const double*)d_nodal[ND_Z].p, need_sw_flag(), nmem, d_active.p, d_red.p);
@@ -6375,6 +6492,8 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   e->d_act.upload(act.data(), e->nmem, e->st);
   e->compact_maps(std::vector<uint8_t>(e->nmem, 1));
   k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0, e->need_sw_flag());
+  if (e->nd.qtran)
+    k_etran<<<e->bms.nblk, kThreads, 0, e->st>>>(e->bms.mem.p, e->bms.r0.p, e->bms.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->nf.qneu);
   k_start_surface<<<e->bms.nblk, kThreads, 0, e->st>>>(e->bms.mem.p, e->bms.r0.p, e->bms.r1.p, e->d_act.p, e->d_ms.p, e->nd);
   k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 1, e->need_sw_flag());
   act[m] = ACT_ITER;

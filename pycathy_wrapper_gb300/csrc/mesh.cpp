@@ -87,6 +87,31 @@ static bool surface_mesh(const cathy_dem_t& d, HostMesh& m,
   return true;
 }
 
+bool node_map_types(const cathy_dem_t& d, const double* map, const HostMesh& m,
+                    std::vector<int32_t>& out) {
+  out.assign(m.nnod, 1);
+  if (!map) return true;
+  std::vector<double> sum(m.nnod, 0.0);
+  std::vector<int> cnt(m.nnod, 0);
+  // triangles come two per active cell in row-major cell order (build_mesh)
+  int t = 0;
+  for (int i = 0; i < d.nrow; ++i)
+    for (int j = 0; j < d.ncol; ++j) {
+      const size_t c = (size_t)i * d.ncol + j;
+      if (d.dem[c] == 0.0) continue;
+      if (map[c] == 0.0) return false;
+      const double e = map[c] * d.factor;
+      for (int h = 0; h < 2; ++h, ++t)
+        for (int q = 0; q < 3; ++q) {
+          const int nd = m.triang[4 * t + q] - 1;
+          sum[nd] += e;
+          cnt[nd] += 1;
+        }
+    }
+  for (int k = 0; k < m.nnod; ++k) out[k] = (int32_t)(sum[k] / cnt[k]);
+  return true;
+}
+
 bool build_mesh(const cathy_dem_t& d, int iopt, HostMesh& m) {
   m.nrow = d.nrow; m.ncol = d.ncol; m.nstr = d.nstr; m.iopt = iopt;
   std::vector<double> zs;

@@ -40,6 +40,14 @@ struct HostMesh {
 // without elements or a zero-area/zero-volume element).
 bool build_mesh(const cathy_dem_t& dem, int iopt, HostMesh& m);
 
+// Vegetation type of each surface node (datin.f:221-233): TRIANGOLI and
+// TPNODI2D applied to a per-cell map -- the mean of FACTOR * map over the
+// node's triangles -- truncated to an integer.  map == NULL gives 1.
+// Returns false when the map is 0 on an active DEM cell (the reference would
+// number the nodes of the two triangulations differently).
+bool node_map_types(const cathy_dem_t& dem, const double* map, const HostMesh& m,
+                    std::vector<int32_t>& out);
+
 // Shared topology helpers (also used by the Fortran drop-ins):
 // full CSR from a symmetric upper CSR (1-based TOPOL/JA, diag first).
 void upper_to_full(int n, const int32_t* topol, const int32_t* ja,

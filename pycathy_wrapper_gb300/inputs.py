@@ -68,6 +68,13 @@ class Soil:
     ``permy``, ``permz`` (saturated conductivity), ``elstor`` (specific
     storage), ``poros`` (porosity), ``vgn`` (VG n), ``vgrmc`` (residual
     moisture content) and ``vgpsat`` (VGPSATCELL = -1/alpha).
+
+    ``feddes`` holds one row per vegetation type of the Feddes root-water
+    uptake parameters PCANA, PCREF, PCWLT, ZROOT, PZ, OMGC (datin.f:424-428)
+    and ``root_map`` the vegetation type of each DEM cell (``input/root_map``;
+    None = type 1 everywhere).  ETRAN (etran.f) removes SCF times the
+    potential evaporation through the root zone, so both are needed when
+    ``scf`` > 0.
     """
 
     permx: np.ndarray
@@ -82,6 +89,8 @@ class Soil:
     scf: float = 0.0
     kslope: int = 0
     tolksl: float = 0.01
+    feddes: Optional[np.ndarray] = None
+    root_map: Optional[np.ndarray] = None
 
     @property
     def nzone(self) -> int:

@@ -105,14 +105,17 @@ def read_project(prj: str) -> Case:
     dem = Dem(dem=dem_map, delta_x=delta_x, delta_y=delta_y, zratio=zr,
               base=base, ivert=ivert, zone=zone_map, factor=factor,
               west=hdr.get("west", 0.0), south=hdr.get("south", 0.0))
-    # vegetation types: number of Feddes lines in the soil file
+    # vegetation types (datin.f:221-233): the root map's largest type is
+    # the number of Feddes lines in the soil file (datin.f:424-428)
     nveg = 1
+    root_map = None
     if os.path.exists(inp("root_map")):
-        rm, _ = read_raster(inp("root_map"))
-        nveg = max(1, int(np.max(rm)))
+        root_map, _ = read_raster(inp("root_map"))
+        nveg = max(1, int(np.max(root_map)))
     sl = [ln for ln in _lines(inp("soil")) if _nums(ln)]
     pmin = _nums(sl[0])[0]
     scf = _nums(sl[1])[1]
+    feddes = np.array([_nums(sl[3 + v])[:6] for v in range(nveg)], dtype=float)
     ivghu = int(_nums(sl[3 + nveg])[0])
     if ivghu != 0:
         raise ValueError("only IVGHU=0 (van Genuchten) soils are supported")
@@ -122,7 +125,8 @@ def read_project(prj: str) -> Case:
                 permz=rows[..., 2].copy(), elstor=rows[..., 3].copy(),
                 poros=rows[..., 4].copy(), vgn=rows[..., 5].copy(),
                 vgrmc=rows[..., 6].copy(), vgpsat=rows[..., 7].copy(),
-                pmin=pmin, scf=scf, kslope=parm.kslope, tolksl=parm.tolksl)
+                pmin=pmin, scf=scf, kslope=parm.kslope, tolksl=parm.tolksl,
+                feddes=feddes, root_map=root_map)
     # initial conditions
     il = [ln for ln in _lines(inp("ic")) if ln.strip()]
     indp = int(_nums(il[0])[0])

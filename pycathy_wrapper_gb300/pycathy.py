@@ -448,7 +448,10 @@ def write_project(case, prj: str) -> None:
         f.write("\t".join(repr(float(z)) for z in d.zratio) + "\n")
     with open(os.path.join(inp, "soil"), "w") as f:
         f.write(f"{s.pmin!r}\tPMIN\n0 {s.scf!r}\tIPEAT SCF\n0.4 0.225\tCBETA0,CANG\n")
-        f.write("0.0 -4.0 -150.0 1.0 1.0 1.0\tPCANA,PCREF,PCWLT,ZROOT,PZ,OMGC\n")
+        fed = (np.array([[0.0, -4.0, -150.0, 1.0, 1.0, 1.0]]) if s.feddes is None
+               else np.asarray(s.feddes, float).reshape(-1, 6))
+        for row in fed:
+            f.write(" ".join(repr(float(v)) for v in row) + "\tPCANA,PCREF,PCWLT,ZROOT,PZ,OMGC\n")
         f.write("0\tIVGHU\n0.02 2 2 0 0.333\tHUALFA,HUBETA,HUGAMA,HUPSIA,HUSWR\n1\tHUN\n")
         f.write("-5 1\tHUA,HUB\n1.2 0 -0.345\tBCBETA,BCRMC,BCPSAT\n")
         keys = ("permx", "permy", "permz", "elstor", "poros", "vgn", "vgrmc", "vgpsat")
@@ -486,3 +489,6 @@ def write_project(case, prj: str) -> None:
     if d.zone is not None:
         _raster(os.path.join(pre, "zone"), np.asarray(d.zone, float), d.west, d.south,
                 d.delta_x, d.delta_y)
+    if s.root_map is not None:
+        _raster(os.path.join(inp, "root_map"), np.asarray(s.root_map, float), d.west,
+                d.south, d.delta_x, d.delta_y)

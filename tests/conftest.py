@@ -28,7 +28,9 @@ def load_golden_case(key):
     soil = Soil(**{k: z["soil_" + k] for k in ("permx", "permy", "permz", "elstor",
                                                "poros", "vgn", "vgrmc", "vgpsat")},
                 pmin=meta["pmin"], scf=meta["scf"], kslope=meta["kslope"],
-                tolksl=meta["tolksl"])
+                tolksl=meta["tolksl"],
+                feddes=z["soil_feddes"] if "soil_feddes" in z else None,
+                root_map=z["soil_root_map"] if "soil_root_map" in z else None)
     parm = Parm(**meta["parm"])
     bc = BC(atmtim=z["atmtim"], atminp=z["atminp"], hspatm=meta["hspatm"],
             ieto=meta["ieto"], indp=meta["indp"], wtposition=meta["wtposition"])

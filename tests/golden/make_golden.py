@@ -55,6 +55,10 @@ def case_to_npz(case, path):
                 zone=d.zone if d.zone is not None else np.ones_like(d.dem, np.int32))
     for k in ("permx", "permy", "permz", "elstor", "poros", "vgn", "vgrmc", "vgpsat"):
         arrs["soil_" + k] = getattr(s, k)
+    if s.feddes is not None:
+        arrs["soil_feddes"] = np.asarray(s.feddes, float)
+    if s.root_map is not None:
+        arrs["soil_root_map"] = np.asarray(s.root_map, float)
     arrs["atmtim"] = b.atmtim
     arrs["atminp"] = b.atminp
     meta = dict(delta_x=d.delta_x, delta_y=d.delta_y, base=d.base, ivert=d.ivert,
