@@ -499,13 +499,22 @@ struct Oracle {
   // node and 6 parameters per type (PCANA, PCREF, PCWLT, ZROOT, PZ, OMGC)
   ivec veg_type;
   dvec feddes;
+  // seepage faces (sfvone.f, sfinit.f, extall.f): one entry per face node,
+  // the faces' lists one after another; SFEXIT equals SFEX at the start of
+  // every iteration, so KSF counts the exit flags EXTALL changes
+  int nsfn = 0;
+  ivec sfnode, sfex, sfexp;
+  dvec sfq, sfqp;
+  double sfflw = 0.0, sfflwp = 0.0;
+  int ksf = 0;
+  bool sfchek = false, ksfzer = true;
   // nodal soil parameters (SOILCHAR.H) and element porosity
   dvec pnodi, snodi, vgn, vgm, vgrmc, vgpsat, vgn1, vgm52, vgnr, vgmm1, vgmr,
       vgpsn, vgpnot, pel;
   // state vectors
   dvec pnew, pold, ptnew, ptold, ptimep, pdiff, swnew, swtimep, sw, ckrw, etai,
       et1, et2, ckrwe, etae, et1e, dckrw, detai, swp;
-  dvec coef1, coef2, coef3, coef4, coef5, tnoti, xt5, scr, lhsp, lhsatm;
+  dvec coef1, coef2, coef3, coef4, coef5, tnoti, xt5, scr, lhsp, lhsatm, lhssf;
   // boundary conditions
   int np = 0, nq = 0, numdir = 0;
   ivec contp, contq, noddir, ifatm, ifatmp;
@@ -629,6 +638,7 @@ struct Oracle {
   void conver(void);
   void switch_old(void);
   void etran(void);
+  void extall(void);
   bool flow3d(bool first_only);
   void atm_read_next(double& t, dvec& v, bool& ok);
   void atmone(void);
@@ -1044,6 +1054,8 @@ void Oracle::atmone() {
     if (contp[i] <= nnod) { ifatm[contp[i]] = -1; ifatmp[contp[i]] = -1; }
   for (int i = 1; i <= nq; ++i)
     if (contq[i] <= nnod) { ifatm[contq[i]] = -1; ifatmp[contq[i]] = -1; }
+  for (int e = 0; e < nsfn; ++e)  // atmone.f:112-119
+    if (sfnode[e] <= nnod) { ifatm[sfnode[e]] = -1; ifatmp[sfnode[e]] = -1; }
   for (int i = 1; i <= nnod; ++i) {
     if (ifatm[i] == -1) continue;
     if (pnew[i] >= pondh_min) { ifatm[i] = 2; ifatmp[i] = 2; continue; }
@@ -1085,6 +1097,8 @@ void Oracle::atmnxt() {
   }
   for (int i = 1; i <= np; ++i) if (contp[i] <= nnod) ifatm[contp[i]] = -1;
   for (int i = 1; i <= nq; ++i) if (contq[i] <= nnod) ifatm[contq[i]] = -1;
+  for (int e = 0; e < nsfn; ++e)  // atmnxt.f:94-101
+    if (sfnode[e] <= nnod) ifatm[sfnode[e]] = -1;
 }
 
 void Oracle::atmbak() {
@@ -1207,6 +1221,16 @@ void Oracle::picard() {
   }
   numdir = np;
   for (int k = 1; k <= np; ++k) noddir[k] = contp[k];
+  for (int e = 0; e < nsfn; ++e)
+    if (sfex[e] == 1) {
+      const int inod = sfnode[e];
+      numdir++;
+      noddir[numdir] = inod;
+      int ind = topol[inod];
+      tnoti[inod] = 0.0;
+      lhssf[e] = coef1[ind];
+      coef1[ind] = 1.0e-9 * RMAX;
+    }
   for (int k = 1; k <= nnod; ++k) {
     if (ifatm[k] == 1 || ifatm[k] == 2) {
       numdir++;
@@ -1237,6 +1261,11 @@ void Oracle::picard() {
     pnew[j] = presc[i];
     coef1[topol[j]] = lhsp[i];
   }
+  for (int e = 0; e < nsfn; ++e)
+    if (sfex[e] == 1) {
+      pnew[sfnode[e]] = 0.0;
+      coef1[topol[sfnode[e]]] = lhssf[e];
+    }
   for (int i = 1; i <= nnod; ++i)
     if (ifatm[i] == 1 || ifatm[i] == 2) {
       pnew[i] = pold[i];
@@ -1358,6 +1387,16 @@ void Oracle::newton() {
   }
   numdir = np;
   for (int k = 1; k <= np; ++k) noddir[k] = contp[k];
+  for (int e = 0; e < nsfn; ++e)
+    if (sfex[e] == 1) {
+      const int inod = sfnode[e];
+      numdir++;
+      noddir[numdir] = inod;
+      tnoti[inod] = 0.0;
+      int ind = diagpos(inod);
+      lhssf[e] = coef1[ind];
+      coef1[ind] = 1.0e-9 * RMAX;
+    }
   for (int k = 1; k <= nnod; ++k)
     if (ifatm[k] == 1 || ifatm[k] == 2) {
       numdir++;
@@ -1386,6 +1425,11 @@ void Oracle::newton() {
     pnew[j] = presc[i];
     coef1[diagpos(j)] = lhsp[i];
   }
+  for (int e = 0; e < nsfn; ++e)
+    if (sfex[e] == 1) {
+      pnew[sfnode[e]] = 0.0;
+      coef1[diagpos(sfnode[e])] = lhssf[e];
+    }
   for (int i = 1; i <= nnod; ++i)
     if (ifatm[i] == 1 || ifatm[i] == 2) {
       pnew[i] = pold[i];
@@ -1421,6 +1465,8 @@ void Oracle::masbal() {
   }
   for (int i = 1; i <= np; ++i)
     qpnew[i] = (scr[contp[i]] - (1.0 - tetaf) * qpold[i]) * tetafr;
+  for (int e = 0; e < nsfn; ++e)  // bkpic.f:44-51
+    if (sfex[e] == 1) sfq[e] = (scr[sfnode[e]] - (1.0 - tetaf) * sfqp[e]) * tetafr;
   for (int k = 1; k <= nnod; ++k)
     if (ifatm[k] == 1 || ifatm[k] == 2)
       atmact[k] = (scr[k] - (1.0 - tetaf) * atmold[k]) * tetafr;
@@ -1453,6 +1499,9 @@ void Oracle::masbal() {
     if (q[k] > 0.0) nnin += q[k];
     else nnout += q[k];
   }
+  sfflw = 0.0;  // fluxmb.f:46-60 (SFFLAG(5) is a diagnostic only)
+  for (int e = 0; e < nsfn; ++e)
+    if (sfex[e] == 1) sfflw = sfflw + sfq[e];
   adin = adout = anin = anout = 0.0;
   for (int k = 1; k <= nnod; ++k) {
     if (ifatm[k] == -1) continue;
@@ -1468,8 +1517,9 @@ void Oracle::masbal() {
   double vndin = (ndin + ndinp) * deltam, vndout = (ndout + ndoutp) * deltam;
   double vanin = (anin + aninp) * deltam, vanout = (anout + anoutp) * deltam;
   double vnnin = (nnin + nninp) * deltam, vnnout = (nnout + nnoutp) * deltam;
+  const double vsfflw = (sfflw + sfflwp) * deltam;
   vin = vadin + vndin + vanin + vnnin;
-  vout = vadout + vndout + vanout + vnnout;
+  vout = vadout + vndout + vanout + vnnout + vsfflw;
   erras = vin + vout - dstore;
   if (deltat >= 1.0e15) errel = (vin != 0.0) ? 100.0 * erras / vin : 0.0;
   else errel = ((vin + vout) != 0.0) ? 100.0 * erras / (vin + vout) : 0.0;
@@ -1498,6 +1548,29 @@ void Oracle::conver() {
   if ((parm.l2norm == 0 && pinf <= parm.tolswi) ||
       (parm.l2norm != 0 && pl2 <= parm.tolswi))
     switch_old();
+  if (nsfn > 0) {  // conver.f:82-104
+    extall();
+    ksfzer = (ksf == 0);
+  }
+}
+
+// EXTALL (extall.f:27-55) + EXTCVG (extcvg.f): an exit node whose
+// back-calculated flux is an inflow (SFQ >= 0) leaves the seepage face; a
+// potential node with PNEW > 1e-8 becomes an exit node at PNEW = 0
+// (DUPUIT = 0).  KSF counts the changed flags (SFEXIT = SFEX before).
+void Oracle::extall() {
+  ksf = 0;
+  for (int e = 0; e < nsfn; ++e) {
+    const int inod = sfnode[e];
+    const int before = sfex[e];
+    if (sfex[e] == 1) {
+      if (sfq[e] >= 0.0) { sfex[e] = 0; sfq[e] = 0.0; }
+    } else if (pnew[inod] > 1.0e-8) {
+      pnew[inod] = 0.0;
+      sfex[e] = 1;
+    }
+    if (sfex[e] != before) ksf++;
+  }
 }
 
 // FLOW3D (flow3d.f:93-294); returns true when BCKSTP or NOBACK is set.
@@ -1519,7 +1592,8 @@ bool Oracle::flow3d(bool first_only) {
     bool errgmx = (pl2 >= parm.ernlmx || pinf >= parm.ernlmx ||
                    fl2 >= parm.ernlmx || finf >= parm.ernlmx);
     bool normcv = (parm.l2norm == 0) ? (pinf <= parm.toluns) : (pl2 <= parm.toluns);
-    if (!lsfail && !errgmx && !normcv && itagen) {
+    if ((!lsfail && !errgmx && !normcv && itagen) ||
+        (!lsfail && !errgmx && itagen && sfchek && !ksfzer)) {
       pold = pnew;
       ptold = ptnew;
       for (int k = 1; k <= n; ++k)
@@ -1528,7 +1602,9 @@ bool Oracle::flow3d(bool first_only) {
       continue;
     }
     itrtot += iter;
-    if (!lsfail && !errgmx && normcv) return false;  // converged
+    if ((!sfchek && !lsfail && !errgmx && normcv) ||
+        (sfchek && !lsfail && !errgmx && normcv && ksfzer))
+      return false;  // converged
     return true;  // back-step (DTGMIN) or abort (!DTGMIN)
   }
 }
@@ -1557,6 +1633,7 @@ void Oracle::timupd() {
 // BKSTEP (bkstep.f:54-166) for the subsurface-only case
 void Oracle::bkstep() {
   pnew = ptimep;
+  for (int e = 0; e < nsfn; ++e) { sfex[e] = sfexp[e]; sfq[e] = sfqp[e]; }  // bkstep.f:56-66
   for (int i = 1; i <= np; ++i) qpnew[i] = qpold[i];
   for (int i = 1; i <= nnod; ++i) { ifatm[i] = ifatmp[i]; atmact[i] = atmold[i]; }
   time = timep;
@@ -1660,9 +1737,12 @@ int Oracle::step() {
   rec.dstore = dstore; rec.cdstor = cdstor; rec.vin = vin; rec.cvin = cvin;
   rec.vout = vout; rec.cvout = cvout; rec.erras = erras; rec.errel = errel;
   rec.cerras = cerras; rec.caeras = caeras;
+  rec.sfflw = sfflw;
   step_recs.push_back(rec);
   adinp = adin; adoutp = adout; ndinp = ndin; ndoutp = ndout;
   aninp = anin; anoutp = anout; nninp = nnin; nnoutp = nnout;
+  sfflwp = sfflw;  // cathy_main.f:3282, :3294-3300
+  for (int e = 0; e < nsfn; ++e) { sfexp[e] = sfex[e]; sfqp[e] = sfq[e]; }
   for (int i = 1; i <= np; ++i) qpold[i] = qpnew[i];
   for (int i = 1; i <= nnod; ++i) { ifatmp[i] = ifatm[i]; atmold[i] = atmact[i]; }
   ptimep = pnew;
@@ -1786,6 +1866,32 @@ void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,
   else o->dtgmin = true;
   o->timep = 0.0;
   o->time = o->deltat;
+  // seepage faces (sfvone.f: elevations descending along each face) and
+  // SFINIT (sfinit.f:22-50): nodes at PTIMEP >= 1e-8 start as exit points
+  // at zero head
+  if (bc->nsf > 0) {
+    std::vector<char> seen(n + 1, 0);
+    for (int i = 1; i <= o->np; ++i) seen[o->contp[i]] = 1;
+    for (int i = 1; i <= o->nq; ++i) seen[o->contq[i]] = 1;
+    int e = 0;
+    for (int f = 0; f < bc->nsf; ++f) {
+      for (int j = 0; j < bc->sfnum[f]; ++j, ++e) {
+        const int nd = bc->sfnod[e];
+        if (nd < 1 || nd > n || seen[nd]) { delete o; return nullptr; }
+        seen[nd] = 1;
+        if (j > 0 && o->z[bc->sfnod[e - 1]] < o->z[nd]) { delete o; return nullptr; }
+        o->sfnode.push_back(nd);
+      }
+    }
+    o->nsfn = e;
+    o->sfex.assign(e, 0); o->sfq.assign(e, 0.0); o->sfqp.assign(e, 0.0);
+    o->lhssf.assign(e, 0.0);
+    o->noddir.assign(o->np + e + nnod + 2, 0);
+    for (int k = 0; k < e; ++k)
+      if (o->ptimep[o->sfnode[k]] >= 1.0e-8) { o->sfex[k] = 1; o->ptimep[o->sfnode[k]] = 0.0; }
+    o->sfexp = o->sfex;
+    o->sfchek = (parm->isfcvg == 1);
+  }
   o->pnew = o->ptimep;
   o->atmone();
   // POLD, PTNEW, PTOLD (inital.f)
@@ -1864,6 +1970,11 @@ void orc_first_iteration(void* h, orc_iter_rec_t* rec) {
   o->ptold = o->ptnew;
   o->flow3d(true);
   *rec = o->iter_recs.back();
+}
+
+void orc_get_seepage(void* h, int32_t* sfex, double* sfq) {
+  Oracle* o = (Oracle*)h;
+  for (int e = 0; e < o->nsfn; ++e) { sfex[e] = o->sfex[e]; sfq[e] = o->sfq[e]; }
 }
 
 void orc_get_qtranie(void* h, double* qtranie, int32_t* veg_type) {

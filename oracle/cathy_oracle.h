@@ -57,6 +57,8 @@ typedef struct orc_parm {
   double deltat, dtmin, dtmax, tmax, dtmaga, dtmagm, dtreds, dtredm;
   double pondh_min;
   int32_t precond;  /* Picard linear solver: 0 = IC(0)-PCG (SYMSLV), 1 = Jacobi-PCG */
+  int32_t isfcvg;   /* 1: nonlinear convergence also needs the seepage-face
+                       exit points to stay put (ISFCVG, datin.f:110) */
 } orc_parm_t;
 
 typedef struct orc_bc {
@@ -66,6 +68,10 @@ typedef struct orc_bc {
   int32_t np; const int32_t* contp; const double* presc; /* non-atm Dirichlet */
   int32_t nq; const int32_t* contq; const double* q;     /* non-atm Neumann   */
   int32_t indp; double wtposition; const double* pinit;  /* initial condition */
+  /* seepage faces (input/sfbc, sfvone.f): nsf faces, sfnum[f] nodes each,
+   * sfnod = the faces' 1-based node lists one after another, each face
+   * ordered by descending elevation */
+  int32_t nsf; const int32_t* sfnum; const int32_t* sfnod;
 } orc_bc_t;
 
 /* One record per nonlinear iteration (the reference's `iter` file). */
@@ -79,6 +85,7 @@ typedef struct orc_step_rec {
   int32_t nstep, iter, nitert, nback;
   double deltat, time, store1, store2, dstore, cdstor, vin, cvin, vout, cvout,
          erras, errel, cerras, caeras;
+  double sfflw;    /* seepage-face flux SFFLW of the step (fluxmb.f:46-60) */
 } orc_step_rec_t;
 
 void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,
@@ -111,6 +118,9 @@ void orc_get_state(void* h, double* pnew, double* time_dt2);  /* time, deltat */
 /* QTRANIE (n values, 1-based node k at out[k-1]) of the current time step
  * and VEG_TYPE of the surface nodes (nnod values) */
 void orc_get_qtranie(void* h, double* qtranie, int32_t* veg_type);
+/* seepage-face state, one entry per face node in input order: SFEX (exit
+ * point flags) and SFQ (back-calculated fluxes) */
+void orc_get_seepage(void* h, int32_t* sfex, double* sfq);
 void orc_set_state(void* h, const double* ptimep, double time, double deltat);
 
 /* ---- fine-grained kernels on the current state (for unit parity) ---- */

@@ -45,7 +45,8 @@ class OrcParm(C.Structure):
         (k, C.c_double) for k in ("tetaf", "toluns", "tolswi", "ernlmx", "tolcg",
                                    "omega", "deltat", "dtmin", "dtmax", "tmax",
                                    "dtmaga", "dtmagm", "dtreds", "dtredm",
-                                   "pondh_min")] + [("precond", C.c_int32)]
+                                   "pondh_min")] + [("precond", C.c_int32),
+                                                    ("isfcvg", C.c_int32)]
 
 
 class OrcBC(C.Structure):
@@ -53,7 +54,8 @@ class OrcBC(C.Structure):
                 ("atmtim", f64p), ("atminp", f64p),
                 ("np", C.c_int32), ("contp", i32p), ("presc", f64p),
                 ("nq", C.c_int32), ("contq", i32p), ("q", f64p),
-                ("indp", C.c_int32), ("wtposition", C.c_double), ("pinit", f64p)]
+                ("indp", C.c_int32), ("wtposition", C.c_double), ("pinit", f64p),
+                ("nsf", C.c_int32), ("sfnum", i32p), ("sfnod", i32p)]
 
 
 class IterRec(C.Structure):
@@ -66,7 +68,7 @@ class StepRec(C.Structure):
     _fields_ = [(k, C.c_int32) for k in ("nstep", "iter", "nitert", "nback")] + [
         (k, C.c_double) for k in ("deltat", "time", "store1", "store2", "dstore",
                                    "cdstor", "vin", "cvin", "vout", "cvout",
-                                   "erras", "errel", "cerras", "caeras")]
+                                   "erras", "errel", "cerras", "caeras", "sfflw")]
 
 
 def build(force: bool = False) -> str:
@@ -99,6 +101,7 @@ def lib():
         L.orc_get_step_recs.argtypes = [C.c_void_p, C.POINTER(StepRec)]
         L.orc_get_state.argtypes = [C.c_void_p, f64p, f64p]
         L.orc_get_qtranie.argtypes = [C.c_void_p, f64p, i32p]
+        L.orc_get_seepage.argtypes = [C.c_void_p, i32p, f64p]
         L.orc_set_state.argtypes = [C.c_void_p, f64p, C.c_double, C.c_double]
         L.orc_picard_system.argtypes = [C.c_void_p, f64p, f64p, f64p, i32p]
         L.orc_vg_nodal.argtypes = [C.c_void_p, f64p, f64p, f64p, f64p, f64p]
@@ -168,6 +171,12 @@ class Oracle:
                    nq=len(b.contq), contq=I(b.contq if len(b.contq) else np.zeros(1)),
                    q=F(b.q if len(b.q) else np.zeros(1)),
                    indp=b.indp, wtposition=b.wtposition, pinit=F(pinit))
+        faces = [np.asarray(f, dtype=np.int32).reshape(-1) for f in getattr(b, "sfnod", [])]
+        if faces:
+            bc.nsf = len(faces)
+            bc.sfnum = I(np.array([len(f) for f in faces], np.int32))
+            bc.sfnod = I(np.concatenate(faces))
+        self.nsfn = int(sum(len(f) for f in faces))
         self.h = lib().orc_create(C.byref(dem), C.byref(soil), C.byref(parm), C.byref(bc))
         if not self.h:
             raise RuntimeError("oracle: mesh construction failed")
@@ -225,6 +234,13 @@ class Oracle:
         td = np.zeros(2)
         lib().orc_get_state(self.h, _f64(p)[1], _f64(td)[1])
         return p, float(td[0]), float(td[1])
+
+    def seepage(self):
+        """SFEX and SFQ, one entry per seepage-face node in input order."""
+        ex = np.zeros(max(self.nsfn, 1), dtype=np.int32)
+        q = np.zeros(max(self.nsfn, 1))
+        lib().orc_get_seepage(self.h, ex.ctypes.data_as(i32p), _f64(q)[1])
+        return ex[: self.nsfn], q[: self.nsfn]
 
     def qtranie(self):
         """QTRANIE of the current time step (n) and VEG_TYPE (nnod)."""

@@ -113,7 +113,8 @@ class Parm:
     Defaults are the values of the CATHY project template that pyCATHY
     clones (e.g. examples/SSHydro/weill_exemple/input/parm).
     ``precond`` selects the Picard linear solver: 0 = IC(0)-PCG (the
-    reference's SYMSLV), 1 = Jacobi-PCG.
+    reference's SYMSLV), 1 = Jacobi-PCG.  ``isfcvg`` = 1 makes nonlinear
+    convergence also wait for the seepage-face exit points (ISFCVG).
     """
 
     iopt: int = 1
@@ -142,6 +143,9 @@ class Parm:
     dtredm: float = 0.5
     pondh_min: float = 0.0
     precond: int = 0
+    isfcvg: int = 0
+    isfone: int = 0
+    dupuit: int = 0
     kslope: int = 0
     tolksl: float = 0.01
     # output control (not used by the solver): IPRT1 = 3 asks for the mesh
@@ -164,7 +168,9 @@ class BC:
     non-atmospheric Dirichlet and Neumann node lists (1-based) with constant
     values.  ``indp`` selects the initial condition (0 uniform ``pinit[0]``,
     1 nodal ``pinit``, 2 water table at the surface, 4 water table at depth
-    ``wtposition``).
+    ``wtposition``).  ``sfnod`` lists the seepage faces (``input/sfbc``),
+    one array of 1-based node numbers per face, ordered by descending
+    elevation (sfvone.f).
     """
 
     atmtim: np.ndarray = field(default_factory=lambda: np.array([0.0, 1e30]))
@@ -178,6 +184,7 @@ class BC:
     indp: int = 4
     wtposition: float = 1.0
     pinit: Optional[np.ndarray] = None
+    sfnod: List[np.ndarray] = field(default_factory=list)
 
 
 @dataclass

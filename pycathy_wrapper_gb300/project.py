@@ -62,6 +62,7 @@ def read_parm(path) -> Parm:
     p.deltat, p.dtmin, p.dtmax, p.tmax = v[11][:4]
     p.dtmaga, p.dtmagm, p.dtreds, p.dtredm = v[12][:4]
     p.tolksl = v[2][1]
+    p.isfone, p.isfcvg, p.dupuit = (int(x) for x in v[5][:3])
     p.iprt1 = int(v[0][0])
     # IPRT VTKF NPRT (TIMPRT(I),I=1,NPRT) then NUMVP (NODVP(I),I=1,NUMVP):
     # list-directed reads (datin.f:118-119), so a list may run on over
@@ -165,7 +166,58 @@ def read_project(prj: str) -> Case:
     neu = _read_bc_list(inp("nansfneubc"))
     if neu is not None:
         bc.contq, bc.q = neu
+    if os.path.exists(inp("sfbc")):
+        bc.sfnod = read_sfbc(inp("sfbc"), parm.tmax)
+    if bc.sfnod and (parm.isfone != 0 or parm.dupuit != 0):
+        # conver.f:88-99 and sfinit.f:35-41 stop on these
+        raise ValueError("seepage faces need ISFONE = 0 and DUPUIT = 0")
     return Case(dem, soil, parm, bc, name=os.path.basename(os.path.normpath(prj)))
+
+
+def read_sfbc(path, tmax=np.inf):
+    """``input/sfbc`` as SFVONE/SFVNXT read it (sfvone.f, sfvnxt.f): blocks
+    of TIME, NSF and per face a line with its node count followed by the
+    node list (list-directed: it may run over several lines, the rest of its
+    last line is skipped).  A block takes effect once TIME exceeds its time;
+    blocks at or after TMAX never do.  Only a time-invariant set of faces is
+    supported: every effective block must repeat the first one."""
+    rows = [_nums(ln) for ln in _lines(path)]
+    rows = [r for r in rows if r]
+    k = 0
+
+    def first():
+        nonlocal k
+        v = rows[k][0]
+        k += 1
+        return v
+
+    blocks = []
+    while k < len(rows):
+        t = first()
+        if k >= len(rows):
+            break
+        nsf = int(first())
+        faces = []
+        for _ in range(nsf):
+            cnt = int(first())
+            ids = []
+            while len(ids) < cnt:
+                ids += rows[k]
+                k += 1
+            faces.append(np.array(ids[:cnt], dtype=np.int32))
+        blocks.append((t, faces))
+    if not blocks:
+        return []
+    if blocks[0][0] > 0.0:
+        raise ValueError("input/sfbc: the first block must start at TIME = 0")
+    ref = blocks[0][1]
+    for t, faces in blocks[1:]:
+        if t >= tmax:
+            continue
+        same = len(faces) == len(ref) and all(np.array_equal(a, b) for a, b in zip(faces, ref))
+        if not same:
+            raise ValueError("input/sfbc: time-varying seepage faces are not supported")
+    return ref
 
 
 def _count_nodes(dem_map):

@@ -426,7 +426,7 @@ def write_project(case, prj: str) -> None:
         f.write(f"{p.kslope} {p.tolksl!r}\tKSLOPE TOLKSL\n")
         f.write("-3.0 -1.0 -3.0 -1.0\tPKRL PKRR PSEL PSER\n")
         f.write("-3.0 -2.5 -1.5 -1.0\tPDSE1L PDSE1R PDSE2L PDSE2R\n")
-        f.write("0 0 0\tISFONE ISFCVG DUPUIT\n")
+        f.write(f"{p.isfone} {p.isfcvg} {p.dupuit}\tISFONE ISFCVG DUPUIT\n")
         f.write(f"{p.tetaf!r} {p.lump} {p.iopt}\tTETAF LUMP IOPT\n")
         f.write(f"{p.nlrelx} {p.omega!r}\tNLRELX OMEGA\n")
         f.write(f"{p.l2norm} {p.toluns!r} {p.tolswi!r} {p.ernlmx!r}\tL2NORM TOLUNS TOLSWI ERNLMX\n")
@@ -484,6 +484,14 @@ def write_project(case, prj: str) -> None:
                 f.write(f"{int(a)}\n")
             for v in vals:
                 f.write(f"{float(v)!r}\n")
+    # seepage faces: one block at TIME 0 and the same faces again at a time
+    # no run reaches (SFVONE reads two blocks)
+    with open(os.path.join(inp, "sfbc"), "w") as f:
+        for t in (0.0, 1.0e30):
+            f.write(f"{t!r}\tTIME\n{len(b.sfnod)}\tNSF\n")
+            for face in b.sfnod:
+                face = np.ravel(face)
+                f.write(f"{len(face)}\tNNOD\n" + " ".join(str(int(i)) for i in face) + "\n")
     _raster(os.path.join(pre, "dem"), np.asarray(d.dem, float), d.west, d.south,
             d.delta_x, d.delta_y)
     if d.zone is not None:
