@@ -79,6 +79,9 @@ typedef struct cathy_parm {
   double deltat, dtmin, dtmax, tmax, dtmaga, dtmagm, dtreds, dtredm;
   double pondh_min;
   int32_t precond;             /* Picard: 0 IC(0), 1 Jacobi, 2 column line */
+  int32_t isfcvg;              /* 1: nonlinear convergence also needs the
+                                  seepage-face exit points to stay put
+                                  (ISFCVG, datin.f:110; flow3d.f:238-271) */
 } cathy_parm_t;
 
 /* input/atmbc, nansfdirbc, nansfneubc, ic */
@@ -89,6 +92,13 @@ typedef struct cathy_bc {
   int32_t np; const int32_t* contp; const double* presc;
   int32_t nq; const int32_t* contq; const double* q;
   int32_t indp; double wtposition; const double* pinit;
+  /* seepage faces (input/sfbc as sfvone.f reads it, time-invariant): nsf
+     faces of sfnum[f] nodes, sfnod = the 1-based node lists one after the
+     other, each face by descending elevation.  Exit points start where the
+     initial head is >= 1e-8 (sfinit.f) and move after every nonlinear
+     iteration (extall.f); their back-calculated outflow enters VOUT
+     (fluxmb.f, masbal.f).                                                  */
+  int32_t nsf; const int32_t* sfnum; const int32_t* sfnod;
 } cathy_bc_t;
 
 typedef struct cathy_member {
@@ -123,6 +133,7 @@ typedef struct cathy_step_rec {
   int32_t nstep, iter, nitert, nback;
   double deltat, time, store1, store2, dstore, cdstor, vin, cvin, vout, cvout,
          erras, errel, cerras, caeras;
+  double sfflw;                /* seepage-face flux SFFLW (fluxmb.f:46-60)  */
 } cathy_step_rec_t;
 
 /* ---- library ----------------------------------------------------------- */
@@ -165,6 +176,10 @@ int32_t cathy_gb300_set_state(void* handle, int32_t m, const double* ptimep,
  * SW array that DETOUT writes to the sw output file (detout.f:44-45),
  * VGPNOT*Se(PNEW) + VGRMC/PNODI as CHNEW forms it */
 int32_t cathy_gb300_get_saturation(void* handle, int32_t m, double* sw);
+/* seepage faces of member m, one entry per face node in the order of
+ * cathy_bc_t.sfnod: SFEX (1 = exit point) and the back-calculated flux SFQ
+ * of the last iteration (extall.f, bkpic.f); EINVAL without faces */
+int32_t cathy_gb300_get_seepage(void* handle, int32_t m, int32_t* sfex, double* sfq);
 /* iteration records (one per Picard/Newton iteration: the `iter` file's
  * lines, conver.f:44-45) and step records (one per accepted step: the
  * `mbeconv` rows, cathy_main.f:3269-3273) of member m */

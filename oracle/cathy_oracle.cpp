@@ -2003,6 +2003,14 @@ void orc_get_state(void* h, double* pnew, double* td) {
 void orc_set_state(void* h, const double* ptimep, double time, double deltat) {
   Oracle* o = (Oracle*)h;
   for (int i = 0; i < o->n; ++i) { o->ptimep[i + 1] = ptimep[i]; o->pnew[i + 1] = ptimep[i]; }
+  for (int e = 0; e < o->nsfn; ++e) {  // SFINIT on the new heads
+    const int nd = o->sfnode[e];
+    o->sfex[e] = o->ptimep[nd] >= 1.0e-8 ? 1 : 0;
+    if (o->sfex[e]) { o->ptimep[nd] = 0.0; o->pnew[nd] = 0.0; }
+    o->sfq[e] = 0.0; o->sfqp[e] = 0.0;
+  }
+  o->sfexp = o->sfex;
+  o->sfflwp = 0.0;
   o->time = time; o->deltat = deltat;
 }
 

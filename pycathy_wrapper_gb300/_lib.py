@@ -53,7 +53,8 @@ class Parm(C.Structure):
         (k, C.c_double) for k in ("tetaf", "toluns", "tolswi", "ernlmx", "tolcg",
                                    "omega", "deltat", "dtmin", "dtmax", "tmax",
                                    "dtmaga", "dtmagm", "dtreds", "dtredm",
-                                   "pondh_min")] + [("precond", C.c_int32)]
+                                   "pondh_min")] + [("precond", C.c_int32),
+                                                    ("isfcvg", C.c_int32)]
 
 
 class BC(C.Structure):
@@ -61,7 +62,8 @@ class BC(C.Structure):
                 ("atmtim", f64p), ("atminp", f64p),
                 ("np", C.c_int32), ("contp", i32p), ("presc", f64p),
                 ("nq", C.c_int32), ("contq", i32p), ("q", f64p),
-                ("indp", C.c_int32), ("wtposition", C.c_double), ("pinit", f64p)]
+                ("indp", C.c_int32), ("wtposition", C.c_double), ("pinit", f64p),
+                ("nsf", C.c_int32), ("sfnum", i32p), ("sfnod", i32p)]
 
 
 class Member(C.Structure):
@@ -84,7 +86,7 @@ class StepRec(C.Structure):
     _fields_ = [(k, C.c_int32) for k in ("nstep", "iter", "nitert", "nback")] + [
         (k, C.c_double) for k in ("deltat", "time", "store1", "store2", "dstore",
                                    "cdstor", "vin", "cvin", "vout", "cvout",
-                                   "erras", "errel", "cerras", "caeras")]
+                                   "erras", "errel", "cerras", "caeras", "sfflw")]
 
 
 EXPORTS = {
@@ -100,6 +102,7 @@ EXPORTS = {
     "cathy_gb300_run": (C.c_int32, [C.c_void_p, C.c_int32, i32p]),
     "cathy_gb300_get_state": (C.c_int32, [C.c_void_p, C.c_int32, f64p, f64p, f64p, i32p]),
     "cathy_gb300_get_saturation": (C.c_int32, [C.c_void_p, C.c_int32, f64p]),
+    "cathy_gb300_get_seepage": (C.c_int32, [C.c_void_p, C.c_int32, i32p, f64p]),
     "cathy_gb300_set_state": (C.c_int32, [C.c_void_p, C.c_int32, f64p, C.c_double,
                                           C.c_double]),
     "cathy_gb300_num_records": (C.c_int32, [C.c_void_p, C.c_int32, i32p, i32p]),

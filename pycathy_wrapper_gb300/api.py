@@ -80,6 +80,11 @@ def _member(case: Case, keep: _Keep) -> _lib.Member:
                      nq=len(b.contq), contq=keep.i(b.contq if len(b.contq) else z1),
                      q=keep.f(b.q if len(b.q) else z1),
                      indp=b.indp, wtposition=b.wtposition, pinit=keep.f(pinit))
+    faces = [np.asarray(f, dtype=np.int32).reshape(-1) for f in b.sfnod]
+    if faces:
+        mem.bc.nsf = len(faces)
+        mem.bc.sfnum = keep.i(np.array([len(f) for f in faces], np.int32))
+        mem.bc.sfnod = keep.i(np.concatenate(faces))
     return mem
 
 
@@ -164,6 +169,16 @@ class Simulation:
         sw = np.zeros(self.sizes[m]["n"])
         check(self.L.cathy_gb300_get_saturation(self.h, m, _ptr(sw, f64p)), "get_saturation")
         return sw
+
+    def seepage(self, m: int = 0):
+        """SFEX (exit-point flags) and SFQ (back-calculated fluxes) of member
+        m's seepage-face nodes, in the order of its ``bc.sfnod`` faces."""
+        k = int(sum(len(f) for f in self.cases[m].bc.sfnod))
+        ex = np.zeros(max(k, 1), np.int32)
+        q = np.zeros(max(k, 1))
+        check(self.L.cathy_gb300_get_seepage(self.h, m, _ptr(ex, i32p), _ptr(q, f64p)),
+              "get_seepage")
+        return ex[:k], q[:k]
 
     def set_state(self, m: int, ptimep, time: float, deltat: float):
         p = _f64(ptimep)

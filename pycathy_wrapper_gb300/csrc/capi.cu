@@ -100,6 +100,11 @@ int32_t cathy_gb300_get_saturation(void* h, int32_t m, double* sw) {
   return guarded([&]() { return engine_get_saturation((Engine*)h, m, sw); });
 }
 
+int32_t cathy_gb300_get_seepage(void* h, int32_t m, int32_t* sfex, double* sfq) {
+  if (!h || !sfex || !sfq) return CATHY_GB300_EINVAL;
+  return guarded([&]() { return engine_get_seepage((Engine*)h, m, sfex, sfq); });
+}
+
 int32_t cathy_gb300_set_state(void* h, int32_t m, const double* ptimep, double time,
                               double deltat) {
   if (!h || !ptimep) return CATHY_GB300_EINVAL;

@@ -242,6 +242,12 @@ struct Nodal {  // per node
   const int32_t* vegi;
   const double *fed, *zc;
   double* qtran;
+  // seepage faces (null when no member has one): per node bit 0 = node of a
+  // seepage face, bit 1 = exit point SFEX, bit 2 = SFEXP of the previous
+  // time level; back-calculated flux SFQ and its previous-level SFQP.  An
+  // exit point carries dmask 2 (Dirichlet at zero head).
+  uint8_t* sfx;
+  double *sfq, *sfqp;
 };
 
 // ============================================================================
@@ -473,6 +479,7 @@ __device__ __forceinline__ void start_phase1_node(int i, uint8_t a, const Member
   if (a & (ACT_START | ACT_BACKSTEP | ACT_COMMIT)) {
     uint8_t dm = nd.sdir[i];
     if (surf) dm |= (nd.ifatm[i] == 1 || nd.ifatm[i] == 2);
+    if (nd.sfx) dm |= (uint8_t)(nd.sfx[i] & 2);
     nd.dmask[i] = dm;
   }
   if (a & ACT_START) {
@@ -2144,8 +2151,10 @@ __global__ void k_update_shl(const int32_t* bm_mem, const int32_t* bm_r0,
   const int i = bm_r0[blockIdx.x] + threadIdx.x;
   if (i >= bm_r1[blockIdx.x]) return;
   double p = nd.pnew[i] + nd.pdiff[i];
+  const uint8_t dm = nd.dmask[i];
   if (nd.sdir[i]) p = nd.presc[i];
-  else if (nd.dmask[i]) p = nd.pold[i];
+  else if (dm & 2) p = 0.0;  // seepage-face exit point (shlpic.f:36-48)
+  else if (dm) p = nd.pold[i];
   nd.pnew[i] = p;
 }
 
@@ -2164,7 +2173,8 @@ k_masbal_norms(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1
   const int i = bm_r0[blockIdx.x] + grp;
   const bool rowok = i < bm_r1[blockIdx.x];
   const MemberScal& S = ms[m];
-  bool dir = rowok && nd.dmask[i];
+  const uint8_t dmv = rowok ? nd.dmask[i] : (uint8_t)0;
+  const bool dir = dmv != 0;
   double sp = 0.0;
   if (dir) {
     const int sl = rowptr[i] + lane;
@@ -2191,6 +2201,8 @@ k_masbal_norms(const int32_t* bm_mem, const int32_t* bm_r0, const int32_t* bm_r1
         const double qn = (scr - (1.0 - th) * nd.qpold[i]) * thr;
         nd.qpnew[i] = qn;
         if (qn > 0.0) v[RD_NDIN] += qn; else v[RD_NDOUT] += qn;
+      } else if (dmv & 2) {  // seepage-face exit point (bkpic.f:44-51)
+        nd.sfq[i] = (scr - (1.0 - th) * nd.sfqp[i]) * thr;
       } else if (surf) {
         const double aa = (scr - (1.0 - th) * nd.atmold[i]) * thr;
         nd.atmact[i] = aa;
@@ -2558,6 +2570,89 @@ __device__ __forceinline__ void start_vg_entry(int bid, const int32_t* bm_mem,
   }
   if (a & ACT_ITER) vg_f32_node(i, nd, nf, z, S);
 }
+// Step actions of the seepage-face nodes, one member per block, before the
+// other step actions (which rebuild DMASK from SFEX): COMMIT keeps SFEX and
+// SFQ as the previous level's (cathy_main.f:3294-3300), BACKSTEP restores
+// them (bkstep.f:56-66).
+__global__ void k_sf_start(const int32_t* sf_mem, const int32_t* sf_off,
+                           const int32_t* sf_node, const uint8_t* act, Nodal nd) {
+  pdl_enter();
+  const uint8_t a = act[sf_mem[blockIdx.x]];
+  if (!(a & (ACT_COMMIT | ACT_BACKSTEP))) return;
+  for (int c = sf_off[blockIdx.x] + threadIdx.x; c < sf_off[blockIdx.x + 1]; c += blockDim.x) {
+    const int i = sf_node[c];
+    uint8_t x = nd.sfx[i];
+    if (a & ACT_COMMIT) {
+      x = (uint8_t)((x & ~4) | ((x & 2) << 1));
+      nd.sfqp[i] = nd.sfq[i];
+    }
+    if (a & ACT_BACKSTEP) {
+      x = (uint8_t)((x & ~2) | ((x & 4) >> 1));
+      nd.sfq[i] = nd.sfqp[i];
+    }
+    nd.sfx[i] = x;
+  }
+}
+
+// EXTALL (extall.f:27-55) + EXTCVG (extcvg.f) for the seepage-face nodes of
+// one member per block, after the iteration's norms, IKMAX and SWITCH_OLD
+// (conver.f:57-104): an exit point with SFQ >= 0 (inflow) leaves the face,
+// a potential node with PNEW > 1e-8 becomes an exit point at PNEW = 0.
+// Before that, SFFLW (fluxmb.f:46-60) sums SFQ over the exit points as the
+// mass balance saw them; KSF counts the flags that change (SFEXIT = SFEX at
+// the start of every iteration).  Both are block sums in a fixed order.
+__global__ void k_extall(const int32_t* sf_mem, const int32_t* sf_off, const int32_t* sf_node,
+                         const uint8_t* act, Nodal nd, double* red) {
+  pdl_enter();
+  const int m = sf_mem[blockIdx.x];
+  if (!(act[m] & ACT_ITER)) return;
+  double flw = 0.0;
+  int ksf = 0;
+  for (int c = sf_off[blockIdx.x] + threadIdx.x; c < sf_off[blockIdx.x + 1]; c += blockDim.x) {
+    const int i = sf_node[c];
+    const uint8_t x = nd.sfx[i];
+    uint8_t ex = x & 2;
+    if (ex) {
+      const double q = nd.sfq[i];
+      flw += q;
+      if (q >= 0.0) {
+        ex = 0;
+        nd.sfq[i] = 0.0;
+      }
+    } else if (nd.pnew[i] > 1.0e-8) {
+      nd.pnew[i] = 0.0;
+      ex = 2;
+    }
+    if (ex != (x & 2)) {
+      ++ksf;
+      nd.sfx[i] = (uint8_t)((x & ~2) | ex);
+      nd.dmask[i] = (uint8_t)(nd.sdir[i] | ex);
+    }
+  }
+  __shared__ double s_flw[kThreads / 32];
+  __shared__ int s_ksf[kThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    flw += __shfl_xor_sync(0xffffffffu, flw, o);
+    ksf += __shfl_xor_sync(0xffffffffu, ksf, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_flw[threadIdx.x >> 5] = flw;
+    s_ksf[threadIdx.x >> 5] = ksf;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double f = 0.0;
+    int k = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      f += s_flw[w];
+      k += s_ksf[w];
+    }
+    red[(size_t)m * RD_NUM + RD_SFFLW] = f;
+    red[(size_t)m * RD_NUM + RD_KSF] = (double)k;
+  }
+}
+
 // ETRAN once per time step, before the step actions of the surface nodes
 // (it reads PNEW before SWITCH_OLD) and not again after a back-step
 // (bkstep.f returns to the solver, cathy_main.f:3176 -> :2980).  Launched
@@ -3239,8 +3334,10 @@ __device__ __forceinline__ void masbal_post_entry(int bid, const int32_t* bm_mem
   unsigned long long key = 0ull;
   if (i < bm_r1[bid]) {
     double p = nd.pnew[i] + (double)nf.pdiff[i];
-    const bool dir = nd.dmask[i] != 0;
+    const uint8_t dmv = nd.dmask[i];
+    const bool dir = dmv != 0;
     if (nd.sdir[i]) p = nd.presc[i];
+    else if (dmv & 2) p = 0.0;  // seepage-face exit point
     else if (dir) p = nd.pold[i];
     const bool surf = nd.loc[i] < S.nnod;
     if (dir) {
@@ -3250,6 +3347,7 @@ __device__ __forceinline__ void masbal_post_entry(int bid, const int32_t* bm_mem
       const double th = S.tetaf;
       const double scr = (double)sp - (double)nf.xt5[i];
       if (nd.sdir[i]) nd.qpnew[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.qpold[i]) / th;
+      else if (dmv & 2) nd.sfq[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.sfqp[i]) / th;
       else if (surf)
         nd.atmact[i] = (th == 1.0) ? scr : (scr - (1.0 - th) * nd.atmold[i]) / th;
     }
@@ -3959,6 +4057,9 @@ struct MemberHost {
          caeras = 0, vtot = 0;
   // last step
   double dstore = 0, vin = 0, vout = 0, erras = 0, errel = 0;
+  bool sfchek = false;    // ISFCVG = 1 with seepage faces
+  double sfflwp = 0;      // SFFLW of the previous time level
+  int sf_first = 0, sf_count = 0;  // its face nodes in the engine's list
   double red_last[RD_NUM];
   bool lsfail = false;
   bool paused = false;
@@ -4000,6 +4101,16 @@ struct Engine {
   std::vector<int32_t> node_off, tet_off, nnz_off;
   // device buffers
   DBuf<int32_t> d_vegi;          // Feddes row per node (surface nodes)
+  // seepage faces: per-node state, and the face nodes grouped by member
+  // (block b of k_extall / k_sf_start: member sf_mem[b], nodes
+  // sf_node[sf_off[b] .. sf_off[b+1]))
+  DBuf<uint8_t> d_sfx, s_sfx;
+  DBuf<double> d_sfq, d_sfqp;
+  DBuf<int32_t> d_sf_node, d_sf_mem, d_sf_off;
+  int n_sfm = 0;
+  std::vector<int32_t> sf_nodes;   // host copy of d_sf_node
+  void sf_start(bool pdl);
+  void sf_extall(bool pdl);
   DBuf<double> d_fed, d_qtran;    // Feddes table, QTRANIE
   DBuf<int32_t> d_mem, d_loc, d_node_off;
   DBuf<double> d_nodal[ND_NUM];
@@ -4531,6 +4642,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   std::vector<double> h_x(N), h_y(N), h_z(N), h_arenod(N, 0.0);
   std::vector<uint8_t> h_sdir(N, 0);
   std::vector<double> h_presc(N, 0.0), h_qneu(N, 0.0), h_pinit(N, 0.0);
+  std::vector<uint8_t> h_sneu(N, 0), h_sfx(N, 0);  // CONTQ nodes; seepage-face state
+  std::vector<int32_t> h_sfnode, h_sfmem, h_sfoff(1, 0);
   std::vector<double> h_fed;     // Feddes rows of the members with SCF > 0
   std::vector<int32_t> h_vegi;   // per node: row of h_fed (surface nodes)
   std::vector<double> tabs[8];
@@ -4633,7 +4746,29 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       const int nd0 = B.contq[k] - 1;
       if (nd0 < 0 || nd0 >= g.n) throw std::string("CONTQ out of range");
       h_qneu[no + nd0] += B.q[k];
+      h_sneu[no + nd0] = 1;
       if (B.q[k] > 0.0) h.nnin += B.q[k]; else h.nnout += B.q[k];
+    }
+    // seepage faces (sfvone.f: descending elevations along each face)
+    if (B.nsf > 0) {
+      if (!B.sfnum || !B.sfnod) throw std::string("seepage faces without node lists");
+      int e = 0;
+      for (int f = 0; f < B.nsf; ++f)
+        for (int j = 0; j < B.sfnum[f]; ++j, ++e) {
+          const int nd0 = B.sfnod[e] - 1;
+          if (nd0 < 0 || nd0 >= g.n) throw std::string("seepage-face node out of range");
+          if (h_sfx[no + nd0] || h_sdir[no + nd0] || h_sneu[no + nd0])
+            throw std::string("seepage-face node repeated or also a Dirichlet/Neumann node");
+          if (j > 0 && g.z[B.sfnod[e - 1] - 1] < g.z[nd0])
+            throw std::string("seepage-face nodes not in descending elevation");
+          h_sfx[no + nd0] = 1;
+          h_sfnode.push_back(no + nd0);
+        }
+      h_sfmem.push_back(m);
+      h_sfoff.push_back((int32_t)h_sfnode.size());
+      h.sf_first = h_sfoff[h_sfoff.size() - 2];
+      h.sf_count = h_sfoff.back() - h.sf_first;
+      h.sfchek = (h.parm.isfcvg == 1);
     }
     // initial conditions (inital.f:97-103)
     for (int i = 0; i < g.nnod; ++i)
@@ -4645,6 +4780,13 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         else if (B.indp == 2) v = g.z[i] - g.z[kk];
         else v = g.z[i] - g.z[kk] - B.wtposition;
         h_pinit[no + kk] = v;
+      }
+    // SFINIT (sfinit.f:22-50): face nodes at an initial head >= 1e-8 start
+    // as exit points (SFEX = SFEXP = 1) at zero head
+    if (B.nsf > 0)
+      for (int c = h_sfoff[h_sfoff.size() - 2]; c < h_sfoff.back(); ++c) {
+        const int gi = h_sfnode[c];
+        if (h_pinit[gi] >= 1.0e-8) { h_sfx[gi] |= 6; h_pinit[gi] = 0.0; }
       }
     h.pmin = S.pmin;
     h.scf = S.scf;
@@ -4717,7 +4859,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
     for (int i = 0; i < nnod; ++i) {
       const int g0 = no + i;
       if (h_sdir[g0]) { h_ifatm[g0] = -1; h_ifatmp[g0] = -1; continue; }
-      if (h_qneu[g0] != 0.0) { h_ifatm[g0] = -1; h_ifatmp[g0] = -1; continue; }
+      // CONTQ and seepage-face nodes are not atmospheric (atmone.f:104-119)
+      if (h_sneu[g0] || h_sfx[g0]) { h_ifatm[g0] = -1; h_ifatmp[g0] = -1; continue; }
       if (h_pnew[g0] >= h.pondh_min) { h_ifatm[g0] = 2; h_ifatmp[g0] = 2; continue; }
       if (h_pnew[g0] >= 0.0 && h_atmpot[g0] > 0.0) h_ifatm[g0] = 1;
       if (h_ptimep[g0] >= 0.0 && h_atmold[g0] > 0.0) h_ifatmp[g0] = 1;
@@ -4842,6 +4985,17 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   nd.pmb = P(ND_PMB); nd.bet = P(ND_BET); nd.set = P(ND_SET);
   nd.mba = P(ND_MBA); nd.mbb = P(ND_MBB); nd.mbc = P(ND_MBC); nd.mbd = P(ND_MBD);
   nd.sdir = d_sdir.p; nd.dmask = d_dmask.p; nd.ifatm = d_ifatm.p; nd.ifatmp = d_ifatmp.p;
+  if (!h_sfnode.empty()) {
+    d_sfx.alloc(N + 4); d_sfx.zero(st); d_sfx.upload(h_sfx.data(), N, st);
+    d_sfq.alloc(N); d_sfq.zero(st);
+    d_sfqp.alloc(N); d_sfqp.zero(st);
+    d_sf_node.alloc(h_sfnode.size()); d_sf_node.upload(h_sfnode.data(), h_sfnode.size(), st);
+    d_sf_mem.alloc(h_sfmem.size()); d_sf_mem.upload(h_sfmem.data(), h_sfmem.size(), st);
+    d_sf_off.alloc(h_sfoff.size()); d_sf_off.upload(h_sfoff.data(), h_sfoff.size(), st);
+    n_sfm = (int)h_sfmem.size();
+    sf_nodes = h_sfnode;
+    nd.sfx = d_sfx.p; nd.sfq = d_sfq.p; nd.sfqp = d_sfqp.p;
+  }
   if (!h_fed.empty()) {
     d_vegi.alloc(N); d_vegi.upload(h_vegi.data(), N, st);
     d_fed.alloc(h_fed.size()); d_fed.upload(h_fed.data(), h_fed.size(), st);
@@ -5141,6 +5295,10 @@ void Engine::save_initial() {
   cp(s_pnew, nd.pnew); cp(s_ptimep, nd.ptimep); cp(s_atmpot, nd.atmpot);
   cp(s_atmact, nd.atmact); cp(s_atmold, nd.atmold); cp(s_qpnew, nd.qpnew);
   s_ifatm.alloc(N); s_ifatmp.alloc(N);
+  if (nd.sfx) {
+    s_sfx.alloc(N);
+    CG_TRY(cudaMemcpyAsync(s_sfx.p, nd.sfx, N, cudaMemcpyDeviceToDevice, st));
+  }
   CG_TRY(cudaMemcpyAsync(s_ifatm.p, nd.ifatm, N, cudaMemcpyDeviceToDevice, st));
   CG_TRY(cudaMemcpyAsync(s_ifatmp.p, nd.ifatmp, N, cudaMemcpyDeviceToDevice, st));
   CG_TRY(cudaStreamSynchronize(st));
@@ -5157,6 +5315,11 @@ void Engine::reset() {
   cp(nd.qpold, s_qpnew);
   CG_TRY(cudaMemcpyAsync(nd.ifatm, s_ifatm.p, N, cudaMemcpyDeviceToDevice, st));
   CG_TRY(cudaMemcpyAsync(nd.ifatmp, s_ifatmp.p, N, cudaMemcpyDeviceToDevice, st));
+  if (nd.sfx) {
+    CG_TRY(cudaMemcpyAsync(nd.sfx, s_sfx.p, N, cudaMemcpyDeviceToDevice, st));
+    d_sfq.zero(st);
+    d_sfqp.zero(st);
+  }
   if (precision == 1 && iopt == 1) {
     k_init_carry<<<cdiv(N, kThreads), kThreads, 0, st>>>(0, N, nd);
     check_launch();
@@ -5671,6 +5834,7 @@ void Engine::iteration_pre(int solve_phase) {
     // correction to opts.inner_tol.
     // step actions + soil characteristics + Krylov member flags in one pass
     phase(0);
+    sf_start(true);
     if (cbms.nblk && nd.qtran) {
       launch(k_etran, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
              (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf.qneu);
@@ -5726,6 +5890,7 @@ void Engine::iteration_post(bool fused) {
              (const uint8_t*)d_act.p, (const uint8_t*)d_switch.p, (const MemberScal*)d_ms.p, nd);
       count();
     }
+    sf_extall(true);
     phase(-1);
     check_launch();
     return;
@@ -5747,8 +5912,30 @@ void Engine::iteration_post(bool fused) {
   if (cbms.nblk)
     k_switch<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_switch.p, d_ms.p, nd);
   count(5);
+  sf_extall(false);
   phase(-1);
   check_launch();
+}
+
+// Seepage-face step actions and EXTALL (k_sf_start, k_extall): launched only
+// when a member has seepage faces; pdl: through launch() (graph capture).
+void Engine::sf_start(bool pdl) {
+  if (!n_sfm) return;
+  if (pdl)
+    launch(k_sf_start, n_sfm, kThreads, (const int32_t*)d_sf_mem.p, (const int32_t*)d_sf_off.p,
+           (const int32_t*)d_sf_node.p, (const uint8_t*)d_act.p, nd);
+  else
+    k_sf_start<<<n_sfm, kThreads, 0, st>>>(d_sf_mem.p, d_sf_off.p, d_sf_node.p, d_act.p, nd);
+  count();
+}
+void Engine::sf_extall(bool pdl) {
+  if (!n_sfm) return;
+  if (pdl)
+    launch(k_extall, n_sfm, kThreads, (const int32_t*)d_sf_mem.p, (const int32_t*)d_sf_off.p,
+           (const int32_t*)d_sf_node.p, (const uint8_t*)d_act.p, nd, d_red.p);
+  else
+    k_extall<<<n_sfm, kThreads, 0, st>>>(d_sf_mem.p, d_sf_off.p, d_sf_node.p, d_act.p, nd, d_red.p);
+  count();
 }
 
 void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
@@ -5760,9 +5947,9 @@ void Engine::picard_or_newton_iteration(const std::vector<int>& itm) {
 // The step actions at the start of a macro-iteration (COMMIT, BACKSTEP,
 // START/NEXT for every member with work).
 void Engine::start_kernels() {
+  sf_start(false);
   if (cbm1.nblk)
     k_start_nodes<<<cbm1.nblk, kThreads, 0, st>>>(cbm1.mem.p, cbm1.r0.p, cbm1.r1.p, d_act.p, d_ms.p, nd, 0, need_sw_flag());
-  if (cbms.nblk)
   if (cbms.nblk && nd.qtran) {
     k_etran<<<cbms.nblk, kThreads, 0, st>>>(cbms.mem.p, cbms.r0.p, cbms.r1.p, d_act.p, d_ms.p, nd, nf.qneu);
     count();
@@ -6096,6 +6283,7 @@ int Engine::macro_iteration() {
       iteration_pre(0);
       iteration_post(true);
     } else if (cbm1.nblk) {
+      sf_start(true);
       if (cbms.nblk && nd.qtran) {
         launch(k_etran, cbms.nblk, kThreads, cbms.mem.p, cbms.r0.p, cbms.r1.p,
                (const uint8_t*)d_act.p, (const MemberScal*)d_ms.p, nd, nf.qneu);
@@ -6188,13 +6376,16 @@ int Engine::macro_iteration() {
     const bool itagen = h.iter < P.ituns;
     const bool errgmx = (pl2 >= P.ernlmx || pinf >= P.ernlmx || fl2 >= P.ernlmx || finf >= P.ernlmx);
     const bool normcv = (P.l2norm == 0) ? (pinf <= P.toluns) : (pl2 <= P.toluns);
-    if (!lsfail && !errgmx && !normcv && itagen) {
+    const bool ksfzer = !(R[RD_KSF] > 0.0);  // no exit point moved (conver.f:100-104)
+    if ((!lsfail && !errgmx && !normcv && itagen) ||
+        (!lsfail && !errgmx && itagen && h.sfchek && !ksfzer)) {
       h.pend |= ACT_NEXT;
       h.iter++;
       continue;
     }
     h.iterating = false;
-    if (!lsfail && !errgmx && normcv) {
+    if ((!h.sfchek && !lsfail && !errgmx && normcv) ||
+        (h.sfchek && !lsfail && !errgmx && normcv && ksfzer)) {
       conv_mask[m] = 1;
       any_conv = true;
     } else if (h.dtgmin) {
@@ -6241,8 +6432,11 @@ int Engine::macro_iteration() {
       sr = cathy_step_rec_t{};
       sr.nstep = h.nstep; sr.iter = h.iter; sr.nitert = h.nitert; sr.nback = h.kbackt;
       sr.deltat = h.deltat; sr.time = h.time;
+      const double vsfflw = (R[RD_SFFLW] + h.sfflwp) * deltam;
       sr.vin = vadin + vndin + vanin + vnnin;
-      sr.vout = vadout + vndout + vanout + vnnout;
+      sr.vout = vadout + vndout + vanout + vnnout + vsfflw;
+      sr.sfflw = R[RD_SFFLW];
+      h.sfflwp = R[RD_SFFLW];
       h.rec_pending = true;
       if (!mixed) finish_step_record(h, R[RD_DSTORE], st1[(size_t)m * RD_NUM + RD_STORE1]);
       h.adinp = R[RD_ADIN]; h.adoutp = R[RD_ADOUT]; h.ndinp = R[RD_NDIN]; h.ndoutp = R[RD_NDOUT];
@@ -6420,11 +6614,50 @@ int engine_get_saturation(Engine* e, int m, double* sw) {
   return 0;
 }
 
-int engine_set_state(Engine* e, int m, const double* ptimep, double time,
+int engine_get_seepage(Engine* e, int m, int32_t* sfex, double* sfq) {
+  if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
+  const MemberHost& h = *e->M[m];
+  if (!h.sf_count) return CATHY_GB300_EINVAL;
+  const int off = e->node_off[m], n = h.meshp->n;
+  std::vector<uint8_t> x(n);
+  std::vector<double> q(n);
+  CG_TRY(cudaMemcpyAsync(x.data(), e->nd.sfx + off, n, cudaMemcpyDeviceToHost, e->st));
+  CG_TRY(cudaMemcpyAsync(q.data(), e->nd.sfq + off, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+  CG_TRY(cudaStreamSynchronize(e->st));
+  for (int c = 0; c < h.sf_count; ++c) {
+    const int loc = e->sf_nodes[h.sf_first + c] - off;
+    sfex[c] = (x[loc] >> 1) & 1;
+    sfq[c] = q[loc];
+  }
+  return 0;
+}
+
+int engine_set_state(Engine* e, int m, const double* ptimep_in, double time,
                      double deltat) {
   if (m < 0 || m >= e->nmem) return CATHY_GB300_EINVAL;
   MemberHost& h = *e->M[m];
   const size_t n = h.meshp->n;
+  const double* ptimep = ptimep_in;
+  std::vector<double> pt;
+  if (h.sf_count) {
+    // a new initial condition: SFINIT (sfinit.f:22-50) on the member's faces
+    const int off = e->node_off[m];
+    pt.assign(ptimep_in, ptimep_in + n);
+    std::vector<uint8_t> x(n);
+    CG_TRY(cudaMemcpyAsync(x.data(), e->nd.sfx + off, n, cudaMemcpyDeviceToHost, e->st));
+    CG_TRY(cudaStreamSynchronize(e->st));
+    for (int c = 0; c < h.sf_count; ++c) {
+      const int loc = e->sf_nodes[h.sf_first + c] - off;
+      const bool ex = pt[loc] >= 1.0e-8;
+      if (ex) pt[loc] = 0.0;
+      x[loc] = (uint8_t)(1 | (ex ? 6 : 0));
+    }
+    CG_TRY(cudaMemcpyAsync(e->nd.sfx + off, x.data(), n, cudaMemcpyHostToDevice, e->st));
+    CG_TRY(cudaMemsetAsync(e->nd.sfq + off, 0, sizeof(double) * n, e->st));
+    CG_TRY(cudaMemsetAsync(e->nd.sfqp + off, 0, sizeof(double) * n, e->st));
+    h.sfflwp = 0.0;
+    ptimep = pt.data();
+  }
   CG_TRY(cudaMemcpyAsync(e->nd.pnew + e->node_off[m], ptimep, sizeof(double) * n,
                          cudaMemcpyHostToDevice, e->st));
   CG_TRY(cudaMemcpyAsync(e->nd.ptimep + e->node_off[m], ptimep, sizeof(double) * n,
@@ -6491,6 +6724,7 @@ int engine_picard_system(Engine* e, int m, double* vals, double* rhs, double* xt
   e->push_scalars();
   e->d_act.upload(act.data(), e->nmem, e->st);
   e->compact_maps(std::vector<uint8_t>(e->nmem, 1));
+  e->sf_start(false);
   k_start_nodes<<<e->bm1.nblk, kThreads, 0, e->st>>>(e->bm1.mem.p, e->bm1.r0.p, e->bm1.r1.p, e->d_act.p, e->d_ms.p, e->nd, 0, e->need_sw_flag());
   if (e->nd.qtran)
     k_etran<<<e->bms.nblk, kThreads, 0, e->st>>>(e->bms.mem.p, e->bms.r0.p, e->bms.r1.p, e->d_act.p, e->d_ms.p, e->nd, e->nf.qneu);

@@ -87,6 +87,7 @@ int engine_get_state(Engine* e, int m, double* pnew, double* time,
 int engine_set_state(Engine* e, int m, const double* ptimep, double time,
                      double deltat);
 int engine_get_saturation(Engine* e, int m, double* sw);
+int engine_get_seepage(Engine* e, int m, int32_t* sfex, double* sfq);
 int engine_num_records(Engine* e, int m, int32_t* ni, int32_t* ns);
 int engine_get_records(Engine* e, int m, cathy_iter_rec_t* ir,
                        cathy_step_rec_t* sr);

@@ -50,7 +50,9 @@ struct MemberScal {
 // is committed, see k_start_vg_f32).
 enum {
   RD_DSTORE = 0, RD_NDIN, RD_NDOUT, RD_ADIN, RD_ADOUT, RD_ANIN, RD_ANOUT,
-  RD_PL2, RD_FL2, RD_STORE1, RD_DSTORE_C, RD_STORE1_C, RD_NUM
+  RD_PL2, RD_FL2, RD_STORE1, RD_DSTORE_C, RD_STORE1_C,
+  RD_SFFLW, RD_KSF,  // seepage faces: SFFLW and KSF of the iteration (k_extall)
+  RD_NUM
 };
 
 template <class MT>
