@@ -322,11 +322,17 @@ def run_large(args):
     BiCGSTAB inside the FP64 loop; its first `--steps` time steps, the
     build and the device memory are the figures of interest)."""
     from pycathy_wrapper_gb300.api import Simulation
-    from pycathy_wrapper_gb300.inputs import config1, config4_member
+    from pycathy_wrapper_gb300.inputs import config1, config4_member, with_vegetation
     import torch
     if args.workload == "config1":
         cases = [config1(tmax=172800.0)]
         cases[0].parm.precond = 2
+        steps = 0
+    elif args.workload == "vegetated":
+        # the bench's ensemble with the Feddes root-water uptake switched on
+        # (SCF = 1, two vegetation types, rain then evaporation): the cost of
+        # ETRAN at ensemble scale, on the bench's FP32 graph path
+        cases = [with_vegetation(c) for c in _cases(args.members, 0, args.tmax, precond=2)]
         steps = 0
     else:
         nm = min(args.members, 32)  # 32 members by default; fewer for a profiling run
@@ -334,7 +340,7 @@ def run_large(args):
         steps = max(args.steps, 1)
     free0 = torch.cuda.mem_get_info()[0]
     t0 = time.perf_counter()
-    with Simulation(cases, precision=1, graphs=args.workload == "config1") as s:
+    with Simulation(cases, precision=1, graphs=args.workload != "config4") as s:
         build_s = time.perf_counter() - t0
         dev_gb = (free0 - torch.cuda.mem_get_info()[0]) / 1e9
         a = s.stats()
@@ -376,10 +382,12 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--only", default="",
                     help="comma-separated member indices: run only these (profiling)")
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "config1", "config4"],
+    ap.add_argument("--workload", default="ensemble",
+                    choices=["ensemble", "config1", "config4", "vegetated"],
                     help="config1 / config4: the single large mesh (200x200x30, 2 simulated days) "
                          "or the 32-member Newton batch (300x300x25 each, first steps) at their "
-                         "stated sizes; a line of its own, not the bench line")
+                         "stated sizes; vegetated: the ensemble day with the Feddes sink; a "
+                         "line of its own, not the bench line")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -325,6 +325,26 @@ def config2_members(nmembers=256, tmax=86400.0, base_seed=1000,
     return cases
 
 
+# Feddes rows (PCANA PCREF PCWLT ZROOT PZ OMGC) of the two vegetation types
+# of with_vegetation: shallow grass roots, deeper shrub roots
+FEDDES_GRASS_SHRUB = np.array([[0.0, -4.0, -150.0, 0.6, 1.0, 1.0],
+                               [-0.5, -3.0, -100.0, 1.2, 2.0, 0.5]])
+
+
+def with_vegetation(case: Case) -> Case:
+    """The same member with the Feddes root-water uptake switched on: SCF =
+    1, shrubs on the upper half of the DEM's elevation range and grass on
+    the rest, under a day of rain (6 h at 2e-7 m/s) then evaporation (up to
+    2e-7 m/s), so that ETRAN takes the evaporation through the roots."""
+    d, s = case.dem, case.soil
+    soil = dataclasses.replace(s, scf=1.0, feddes=FEDDES_GRASS_SHRUB.copy(),
+                               root_map=np.where(d.dem > np.median(d.dem), 2.0, 1.0))
+    t = np.array([0.0, 21600.0, 43200.0, 64800.0, 86400.0, 1e9])
+    rate = np.array([2e-7, 2e-7, -1e-7, -2e-7, -1e-7, -1e-7])
+    bc = dataclasses.replace(case.bc, atmtim=t, atminp=rate)
+    return case.replace(soil=soil, bc=bc, name=case.name + "_veg")
+
+
 def config4_member(ncell=300, nstr=25, seed=0, tmax=43200.0) -> Case:
     """Dry clay loam under a 0.05 m ponded head on the top face (Newton +
     BiCGSTAB): fractal DEM, 25 layers to 10 m, IC -10 m."""

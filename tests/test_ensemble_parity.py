@@ -13,7 +13,9 @@ FP32 inner tolerance (1e-8).  A config-1-style
 member (40x40 fractal DEM, 15 layers, per-cell lognormal Ks) is checked for
 the 6-hour rain pulse the same way.  The FP64 path (``precision=0``, IC(0))
 is checked iterate for iterate on two of the members, and the CPU-runnable
-hillslope configuration for its full simulated day on both paths.
+hillslope configuration for its full simulated day on both paths.  Three of
+the draws run again with the Feddes root-water uptake switched on
+(``inputs.with_vegetation``).
 
 Tolerances, written where they are asserted:
   * heads: max |psi_gpu - psi_oracle| <= 1e-6 m at the end of the run;
@@ -43,6 +45,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 MEMBERS = [7, 46, 53, 123, 115, 36]       # seeds 1000 + m
 FAILING = {115, 36}
+VEG_MEMBERS = [7, 46, 123]                # the same draws with the Feddes sink
 FP64_MEMBERS = [46, 36]
 DAY = 86400.0
 
@@ -56,6 +59,9 @@ def _oracle_job(args):
     if kind == "c2":
         c = I.config2_members(256, tmax=tmax)[idx]
         c.parm.precond = 0
+    elif kind == "veg":
+        c = I.with_vegetation(I.config2_members(256, tmax=tmax)[idx])
+        c.parm.precond = 0
     else:
         c = I.config1(ncell=40, nstr=15, tmax=tmax)
     o = O.Oracle(c)
@@ -68,12 +74,11 @@ def _oracle_job(args):
 @pytest.fixture(scope="module")
 def oracle_runs():
     ctx = mp.get_context("spawn")  # the test process may already hold a GPU context
-    jobs = [("c2", m, DAY) for m in MEMBERS] + [("c1", 0, 21600.0)]
+    jobs = ([("c2", m, DAY) for m in MEMBERS] + [("c1", 0, 21600.0)] +
+            [("veg", m, DAY) for m in VEG_MEMBERS])
     with ctx.Pool(processes=len(jobs)) as pool:
         res = pool.map(_oracle_job, jobs)
-    out = {("c2", m): r for m, r in zip(MEMBERS, res)}
-    out[("c1", 0)] = res[-1]
-    return out
+    return {(k, m): r for (k, m, _), r in zip(jobs, res)}
 
 
 def _gpu(cases, **kw):
@@ -129,6 +134,21 @@ def test_bench_path_heterogeneous_ks_member_matches_oracle(oracle_runs):
     g = _gpu([c], precision=1, graphs=True)[0]
     o = oracle_runs[("c1", 0)]
     _check_finished(g, o, head_tol=1e-6, mbe_tol=1e-7, iter_frac=0.99)
+
+
+def test_bench_path_vegetated_members_match_oracle(oracle_runs):
+    """Three of the draws with the Feddes root-water uptake switched on (SCF
+    = 1, grass and shrubs, rain then evaporation) on the bench path for the
+    full day; the transpired volume is part of CERRAS on both sides."""
+    from pycathy_wrapper_gb300.inputs import config2_members, with_vegetation
+    allc = config2_members(256, tmax=DAY)
+    cases = [with_vegetation(allc[m]) for m in VEG_MEMBERS]
+    for c in cases:
+        c.parm.precond = 2
+    got = _gpu(cases, precision=1, graphs=True)
+    for m, g in zip(VEG_MEMBERS, got):
+        _check_finished(g, oracle_runs[("veg", m)], head_tol=1e-6, mbe_tol=1e-7,
+                        iter_frac=0.99)
 
 
 def test_fp64_path_matches_oracle_iterate_for_iterate(oracle_runs):

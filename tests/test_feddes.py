@@ -131,6 +131,22 @@ def test_oracle_refuses_bad_feddes_inputs():
     O.Oracle(feddes_case(feddes=deep, scf=0.0))  # ETRAN not used: accepted
 
 
+def test_vegetated_ensemble_member_transpires():
+    """inputs.with_vegetation on a small ensemble draw: both vegetation
+    types present, no sink while it rains, a sink once it evaporates."""
+    import oracle as O
+    from pycathy_wrapper_gb300.inputs import config2_members, with_vegetation
+    c = with_vegetation(config2_members(1, tmax=50000.0, min_cells=8, max_cells=10)[0])
+    o = O.Oracle(c)
+    assert o.step() == 0
+    q, vt = o.qtranie()
+    assert set(np.unique(vt)) == {1, 2} and not q.any()
+    while o.state()[1] < 45000.0:
+        assert o.step() == 0
+    q, _ = o.qtranie()
+    assert q.min() == 0.0 and q.max() > 0.0
+
+
 def test_project_reader_parses_feddes_and_root_map():
     case = load_golden_case("weill")
     assert case.soil.scf == 1.0
