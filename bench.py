@@ -340,7 +340,8 @@ def run_large(args):
         steps = max(args.steps, 1)
     free0 = torch.cuda.mem_get_info()[0]
     t0 = time.perf_counter()
-    with Simulation(cases, precision=1, graphs=args.workload != "config4") as s:
+    with Simulation(cases, precision=1,
+                    graphs=args.workload != "config4" and not args.no_graphs) as s:
         build_s = time.perf_counter() - t0
         dev_gb = (free0 - torch.cuda.mem_get_info()[0]) / 1e9
         a = s.stats()

@@ -240,7 +240,9 @@ struct Nodal {  // per node
   // it): row of the Feddes table per surface node, the table (PCANA PCREF
   // PCWLT ZROOT PZ OMGC per row), node elevations and QTRANIE of the step
   const int32_t* vegi;
-  const double *fed, *zc;
+  const double* fed;         // 8 per row: the 6 inputs, 1/(PCREF-PCWLT), 1/(S2-S1)
+  const double *etr_bdz, *etr_btran;  // BETA*DZ per root-zone node, BTRAN per column
+  const uint8_t* etr_jr;     // root-zone nodes per column
   double* qtran;
   // seepage faces (null when no member has one): per node bit 0 = node of a
   // seepage face, bit 1 = exit point SFEX, bit 2 = SFEXP of the previous
@@ -365,43 +367,38 @@ __global__ void k_geom(int nt, const int4* tet, const double* x, const double* y
 // COMMIT bookkeeping + ATM update + switching
 // ETRAN (etran.f:21-79) for the column below surface node i: root water
 // uptake QTRANIE of the new time step from PNEW before SWITCH_OLD and the
-// new ATMPOT.  Column node j (0 = surface) is i + j * NNOD.  QTRANIE holds
-// BTRANI during the root-zone pass.  The host checked that every root zone
-// ends above the bottom node.  qn32: the FP32 Picard path's Neumann term,
+// new ATMPOT.  Column node j (0 = surface) is i + j * NNOD.  The weights
+// that depend on the mesh only -- BETA*DZ of the JR root-zone nodes and
+// their sum BTRAN (etran.f:32-63) -- are formed once on the host, as the
+// reference forms them; a step computes the stress factor GX of each
+// root-zone node with the vegetation type's reciprocals 1/(PCREF-PCWLT) and
+// 1/(S2-S1) (table columns 6, 7) and one quotient ETP/BTRAN/max(OMG, OMGC)
+// per column, within a few ulp of etran.f's quotients.  QTRANIE stays 0
+// below the root zone.  qn32: the FP32 Picard path's Neumann term,
 // Q - QTRANIE (bcpic.f:73-86), or null.
-__device__ __noinline__ void etran_column(int i, double pot, const MemberScal& S, Nodal& nd,
-                                          float* qn32) {
+__device__ __forceinline__ void etran_column(int i, double pot, const MemberScal& S,
+                                             Nodal& nd, float* qn32) {
   const int nnod = S.nnod;
-  const double* fp = nd.fed + 6 * nd.vegi[i];
-  const double pcana = fp[0], pcref = fp[1], pcwlt = fp[2], zroot = fp[3], pz = fp[4];
-  const double omgc = fp[5];
-  const double zsurf = nd.zc[i];
+  const double* fp = nd.fed + 8 * nd.vegi[i];
+  const double pcana = fp[0], pcwlt = fp[2], omgc = fp[5], r1 = fp[6], r2 = fp[7];
   const double etp = (pot < 0.0) ? -1.0 * S.scf * pot : 0.0;
-  const double s1 = pcana, s2 = pcana + 1.0e-3;
-  double btran = 0.0, omg = 0.0, depth = 0.0;
-  int j = 0;
-  while (depth <= zroot) {
+  const int jr = nd.etr_jr[i];
+  double omg = 0.0;
+  for (int j = 0; j < jr; ++j) {
     const int k = i + j * nnod;
-    const double dz = (j == 0) ? (zsurf - nd.zc[k + nnod]) / 2.0
-                               : (nd.zc[k - nnod] - nd.zc[k + nnod]) / 2.0;
-    const double sh2o = nd.pnew[k];
-    const double gx1 = fmin(1.0, fmax(0.0, (sh2o - pcwlt) / (pcref - pcwlt)));
-    const double gx2 = fmin(1.0, fmax(0.0, 1.0 - (sh2o - s1) / (s2 - s1)));
+    const double sh2o = nd.pnew[k], bdz = nd.etr_bdz[k];
+    const double gx1 = fmin(1.0, fmax(0.0, (sh2o - pcwlt) * r1));
+    const double gx2 = fmin(1.0, fmax(0.0, 1.0 - (sh2o - pcana) * r2));
     const double gx = fmin(gx1, gx2);
-    const double beta = (1 - depth / zroot) * exp(-1.0 * pz * depth / zroot);
-    nd.qtran[k] = fmax(0.0, beta * dz * gx);
-    btran = btran + beta * dz;
-    omg = omg + gx * beta * dz;
-    ++j;
-    depth = zsurf - nd.zc[i + j * nnod];
+    nd.qtran[k] = fmax(0.0, bdz * gx);  // BTRANI
+    omg = omg + gx * bdz;
   }
-  const int jr = j;
-  btran = fmax(0.0, btran);
+  const double btran = nd.etr_btran[i];
   omg = omg / btran;
-  const double den = fmax(omg, omgc);
-  for (j = 0; j <= S.nstr; ++j) {
+  const double f = etp / btran / fmax(omg, omgc);
+  for (int j = 0; j < jr; ++j) {
     const int k = i + j * nnod;
-    const double q = (j < jr) ? etp * nd.qtran[k] / btran / den : 0.0;
+    const double q = nd.qtran[k] * f;
     nd.qtran[k] = q;
     if (qn32) qn32[k] = (float)(nd.qneu[k] - q);
   }
@@ -4101,6 +4098,8 @@ struct Engine {
   std::vector<int32_t> node_off, tet_off, nnz_off;
   // device buffers
   DBuf<int32_t> d_vegi;          // Feddes row per node (surface nodes)
+  DBuf<double> d_etr_bdz, d_etr_btran;
+  DBuf<uint8_t> d_etr_jr;
   // seepage faces: per-node state, and the face nodes grouped by member
   // (block b of k_extall / k_sf_start: member sf_mem[b], nodes
   // sf_node[sf_off[b] .. sf_off[b+1]))
@@ -4646,6 +4645,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   std::vector<int32_t> h_sfnode, h_sfmem, h_sfoff(1, 0);
   std::vector<double> h_fed;     // Feddes rows of the members with SCF > 0
   std::vector<int32_t> h_vegi;   // per node: row of h_fed (surface nodes)
+  std::vector<double> h_bdz, h_btran;  // ETRAN's mesh weights (etran_column)
+  std::vector<uint8_t> h_jr;
   std::vector<double> tabs[8];
   std::vector<int32_t> soil_off(nmem + 1, 0);
   h_inc.reserve(4 * NT);
@@ -4799,16 +4800,45 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       std::vector<int32_t> vt;
       if (!node_map_types(mem[m].dem, S.root_map, g, vt))
         throw std::string("root_map is 0 on an active DEM cell");
-      const int row0 = (int)(h_fed.size() / 6);
-      h_fed.insert(h_fed.end(), S.feddes, S.feddes + 6 * (size_t)S.nveg);
-      if (h_vegi.empty()) h_vegi.assign(N, 0);
-      for (int i = 0; i < g.nnod; ++i) {
+      const int row0 = (int)(h_fed.size() / 8);
+      for (int v = 0; v < S.nveg; ++v) {
+        const double* f6 = S.feddes + 6 * (size_t)v;
+        const double s1 = f6[0], s2 = f6[0] + 1.0e-3;
+        h_fed.insert(h_fed.end(), f6, f6 + 6);
+        h_fed.push_back(1.0 / (f6[1] - f6[2]));
+        h_fed.push_back(1.0 / (s2 - s1));
+      }
+      if (h_vegi.empty()) {
+        h_vegi.assign(N, 0);
+        h_bdz.assign(N, 0.0); h_btran.assign(N, 0.0); h_jr.assign(N, 0);
+      }
+      const int nnod = g.nnod;
+      for (int i = 0; i < nnod; ++i) {
         if (vt[i] < 1 || vt[i] > S.nveg) throw std::string("vegetation type outside 1..NVEG");
-        const double zroot = S.feddes[6 * (vt[i] - 1) + 3];
+        const double* f6 = S.feddes + 6 * (vt[i] - 1);
+        const double zroot = f6[3], pz = f6[4];
         // the reference stops here (etran.f:60-65: DECREASE ZROOT)
-        if (!(g.z[i] - g.z[(size_t)g.nstr * g.nnod + i] > zroot))
+        if (!(g.z[i] - g.z[(size_t)g.nstr * nnod + i] > zroot))
           throw std::string("ZROOT reaches the bottom node of a column");
         h_vegi[no + i] = row0 + vt[i] - 1;
+        // the root zone's BETA*DZ and their sum BTRAN (etran.f:32-63, the
+        // mesh-only part of the loop)
+        const double zsurf = g.z[i];
+        double depth = 0.0, btran = 0.0;
+        int j = 0;
+        while (depth <= zroot) {
+          const size_t k = (size_t)j * nnod + i;
+          const double dz = (j == 0) ? (zsurf - g.z[k + nnod]) / 2.0
+                                     : (g.z[k - nnod] - g.z[k + nnod]) / 2.0;
+          const double beta = (1 - depth / zroot) * std::exp(-1.0 * pz * depth / zroot);
+          h_bdz[no + k] = beta * dz;
+          btran = btran + beta * dz;
+          ++j;
+          depth = zsurf - g.z[(size_t)j * nnod + i];
+        }
+        if (j > 255) throw std::string("root zone deeper than 255 layers");
+        h_btran[no + i] = std::max(0.0, btran);
+        h_jr[no + i] = (uint8_t)j;
       }
     }
     h.pondh_min = (h.parm.isimgr <= 1) ? 1.0e10 : h.parm.pondh_min;
@@ -4999,8 +5029,12 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
   if (!h_fed.empty()) {
     d_vegi.alloc(N); d_vegi.upload(h_vegi.data(), N, st);
     d_fed.alloc(h_fed.size()); d_fed.upload(h_fed.data(), h_fed.size(), st);
+    d_etr_bdz.alloc(N); d_etr_bdz.upload(h_bdz.data(), N, st);
+    d_etr_btran.alloc(N); d_etr_btran.upload(h_btran.data(), N, st);
+    d_etr_jr.alloc(N); d_etr_jr.upload(h_jr.data(), N, st);
     d_qtran.alloc(N); d_qtran.zero(st);
-    nd.vegi = d_vegi.p; nd.fed = d_fed.p; nd.zc = P(ND_Z); nd.qtran = d_qtran.p;
+    nd.vegi = d_vegi.p; nd.fed = d_fed.p; nd.qtran = d_qtran.p;
+    nd.etr_bdz = d_etr_bdz.p; nd.etr_btran = d_etr_btran.p; nd.etr_jr = d_etr_jr.p;
   }
   // TPNODI/CHPARM then geometry
   k_tpnodi<<<cdiv(N, kThreads), kThreads, 0, st>>>(N, d_inc_ptr.p, d_inc.p, d_tetsoil.p,
