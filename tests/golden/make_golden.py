@@ -1,5 +1,8 @@
 """Generate the golden fixtures from the reference's stored CATHY runs.
 
+The ETRAN record of the first time step (the first line of the run's
+fort.666: TIME and QTRAN, the sum of QTRANIE) is kept as well.
+
 Run where the reference checkout is available, giving its path:
 
     python tests/golden/make_golden.py <path to the reference checkout>
@@ -26,6 +29,9 @@ from pycathy_wrapper_gb300.project import read_project  # noqa: E402
 EXAMPLES = {
     "weill": "examples/SSHydro/weill_exemple",
     "soil3d": "examples/SSHydro/soil3d_from_weill",
+    # spatially variable evaporation with SCF = 1 over a DEM with no-data
+    # cells: the only forcing of its first iteration is the Feddes sink
+    "etp": "examples/SSHydro/atmbc_spatially_from_weill_withnodata",
 }
 
 
@@ -77,6 +83,12 @@ def main(ref):
         case_to_npz(case, os.path.join(HERE, f"{key}_case.npz"))
         rec, nterm, lin = first_iter(prj)
         out[key] = dict(source=rel, first_iter=rec, nterm=nterm, linear=lin)
+        # ETRAN's record of the first time step (cathy_main.f:2929-2940
+        # writes TIME, QTRAN = sum of QTRANIE, RWU to unit 666)
+        f666 = os.path.join(prj, "fort.666")
+        if os.path.exists(f666):
+            t0, q0 = (float(v) for v in open(f666).readline().split()[:2])
+            out[key]["etran_first"] = dict(time=t0, qtran=q0)
         if key == "weill":
             g = open(os.path.join(prj, "output", "grid3d")).read().split("\n")
             nnod, n, nt = (int(v) for v in g[0].split())

@@ -19,7 +19,7 @@ def _sim(case, **kw):
     return Simulation(case, **kw)
 
 
-@pytest.mark.parametrize("key", ["weill", "soil3d"])
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp"])
 def test_first_iteration_matches_reference_golden(key):
     g = golden_json()[key]
     case = load_golden_case(key)
@@ -32,7 +32,12 @@ def test_first_iteration_matches_reference_golden(key):
     assert r["ikmax"] == fi["ikmax"]
     for k in ("pl2", "pinf", "fl2", "finf"):
         assert abs(r[k] - fi[k]) / abs(fi[k]) < 6e-4, (k, r[k], fi[k])
-    assert abs(r["lin_err"] - lin["err"]) / lin["err"] < 1e-4
+    # the PCG's last residual: to 1e-4 where the system is well scaled; the
+    # evaporation run's only forcing is the Feddes sink (|RHS| ~ 1e-7), and
+    # its 28th residual (4.8e-11) moves by about 1 % with the order of the
+    # parallel FP64 dot products (the serial oracle matches it to 2e-6)
+    lin_tol = 5e-2 if key == "etp" else 1e-4
+    assert abs(r["lin_err"] - lin["err"]) / lin["err"] < lin_tol
 
 
 @pytest.mark.parametrize("key", ["weill", "soil3d"])

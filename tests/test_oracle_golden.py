@@ -1,9 +1,13 @@
 """Pin the CPU oracle on the reference's stored CATHY outputs.
 
 Known answers (tests/golden, generated by tests/golden/make_golden.py from
-examples/SSHydro/{weill_exemple,soil3d_from_weill}/output):
-GEN3D mesh (grid3d), NTERM (risul) and the first nonlinear iteration of the
-first time step (iter + the SYMMETRIC SOLVER line of risul).
+examples/SSHydro/{weill_exemple,soil3d_from_weill,
+atmbc_spatially_from_weill_withnodata}):
+GEN3D mesh (grid3d), NTERM (risul), the first nonlinear iteration of the
+first time step (iter + the SYMMETRIC SOLVER line of risul), and ETRAN's
+QTRAN of the first time step (the first line of fort.666).  The third run
+evaporates with SCF = 1 over a DEM with no-data cells: the Feddes sink is
+the only forcing of its first iteration.
 """
 import os
 
@@ -17,7 +21,7 @@ def _rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
-@pytest.mark.parametrize("key", ["weill", "soil3d"])
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp"])
 def test_first_iteration_matches_reference(key):
     import oracle as O
     g = golden_json()[key]
@@ -35,6 +39,22 @@ def test_first_iteration_matches_reference(key):
     # PNEW/POLD at IKMAX are printed with 3 significant digits (E10.2)
     assert _rel(r["pnew_ik"], fi["pnew_ik"]) < 5.1e-3
     assert _rel(r["pold_ik"], fi["pold_ik"]) < 5.1e-3
+
+
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp"])
+def test_etran_first_step_matches_reference(key):
+    """QTRAN = sum of QTRANIE at the first time step, as the reference
+    binary wrote it to fort.666 (17 significant digits)."""
+    import oracle as O
+    g = golden_json()[key]["etran_first"]
+    o = O.Oracle(load_golden_case(key))
+    o.first_iteration()
+    q, _ = o.qtranie()
+    if g["qtran"] == 0.0:
+        assert not q.any()
+    else:
+        assert _rel(q.sum(), g["qtran"]) < 1e-13
+        assert np.count_nonzero(q) > 0
 
 
 def test_gen3d_mesh_matches_grid3d():
