@@ -32,7 +32,13 @@ EXAMPLES = {
     # spatially variable evaporation with SCF = 1 over a DEM with no-data
     # cells: the only forcing of its first iteration is the Feddes sink
     "etp": "examples/SSHydro/atmbc_spatially_from_weill_withnodata",
+    # a 1,271-node catchment forced by an Earth-observation ET/rain series
+    # (30 spatial records; the fixture keeps the two around the first step)
+    "eo": "examples/EOdata/mapping_atmbc_from_EO_dataset",
 }
+# keys whose fixture keeps only the atmospheric records the first time step
+# interpolates between
+FIRST_STEP_ONLY = {"eo"}
 
 
 def first_iter(prj):
@@ -80,6 +86,11 @@ def main(ref):
     for key, rel in EXAMPLES.items():
         prj = os.path.join(ref, rel)
         case = read_project(prj)
+        if key in FIRST_STEP_ONLY:
+            t = np.asarray(case.bc.atmtim)
+            keep = int(np.searchsorted(t, case.parm.deltat, side="left")) + 1
+            case.bc.atmtim = t[:max(keep, 2)]
+            case.bc.atminp = np.asarray(case.bc.atminp)[:max(keep, 2)]
         case_to_npz(case, os.path.join(HERE, f"{key}_case.npz"))
         rec, nterm, lin = first_iter(prj)
         out[key] = dict(source=rel, first_iter=rec, nterm=nterm, linear=lin)

@@ -19,7 +19,7 @@ def _sim(case, **kw):
     return Simulation(case, **kw)
 
 
-@pytest.mark.parametrize("key", ["weill", "soil3d", "etp"])
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp", "eo"])
 def test_first_iteration_matches_reference_golden(key):
     g = golden_json()[key]
     case = load_golden_case(key)

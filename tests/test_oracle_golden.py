@@ -2,7 +2,8 @@
 
 Known answers (tests/golden, generated by tests/golden/make_golden.py from
 examples/SSHydro/{weill_exemple,soil3d_from_weill,
-atmbc_spatially_from_weill_withnodata}):
+atmbc_spatially_from_weill_withnodata} and
+examples/EOdata/mapping_atmbc_from_EO_dataset):
 GEN3D mesh (grid3d), NTERM (risul), the first nonlinear iteration of the
 first time step (iter + the SYMMETRIC SOLVER line of risul), and ETRAN's
 QTRAN of the first time step (the first line of fort.666).  The third run
@@ -21,7 +22,7 @@ def _rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
-@pytest.mark.parametrize("key", ["weill", "soil3d", "etp"])
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp", "eo"])
 def test_first_iteration_matches_reference(key):
     import oracle as O
     g = golden_json()[key]
@@ -41,7 +42,7 @@ def test_first_iteration_matches_reference(key):
     assert _rel(r["pold_ik"], fi["pold_ik"]) < 5.1e-3
 
 
-@pytest.mark.parametrize("key", ["weill", "soil3d", "etp"])
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp", "eo"])
 def test_etran_first_step_matches_reference(key):
     """QTRAN = sum of QTRANIE at the first time step, as the reference
     binary wrote it to fort.666 (17 significant digits)."""
