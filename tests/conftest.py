@@ -33,7 +33,8 @@ def load_golden_case(key):
                 root_map=z["soil_root_map"] if "soil_root_map" in z else None)
     parm = Parm(**meta["parm"])
     bc = BC(atmtim=z["atmtim"], atminp=z["atminp"], hspatm=meta["hspatm"],
-            ieto=meta["ieto"], indp=meta["indp"], wtposition=meta["wtposition"])
+            ieto=meta["ieto"], indp=meta["indp"], wtposition=meta["wtposition"],
+            pinit=z["pinit"] if "pinit" in z else None)
     return Case(dem, soil, parm, bc, name=key)
 
 

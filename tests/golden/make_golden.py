@@ -35,6 +35,10 @@ EXAMPLES = {
     # a 1,271-node catchment forced by an Earth-observation ET/rain series
     # (30 spatial records; the fixture keeps the two around the first step)
     "eo": "examples/EOdata/mapping_atmbc_from_EO_dataset",
+    # a DA ensemble member started from nodal heads (INDP = 1); its risul
+    # keeps no solver lines.  (Member 1's stored iter is the same file
+    # while its ic was rewritten by the analysis step: not a pin.)
+    "da2": "examples/DA/DA_with_swc/DA_SMC/DA_Ensemble/cathy_2",
 }
 # keys whose fixture keeps only the atmospheric records the first time step
 # interpolates between
@@ -62,6 +66,7 @@ def first_iter(prj):
 
 
 def case_to_npz(case, path):
+    """The parsed inputs of a project as arrays (+ a JSON of the scalars)."""
     d, s, p, b = case.dem, case.soil, case.parm, case.bc
     arrs = dict(dem=d.dem, zratio=d.zratio,
                 zone=d.zone if d.zone is not None else np.ones_like(d.dem, np.int32))
@@ -73,6 +78,8 @@ def case_to_npz(case, path):
         arrs["soil_root_map"] = np.asarray(s.root_map, float)
     arrs["atmtim"] = b.atmtim
     arrs["atminp"] = b.atminp
+    if b.pinit is not None:
+        arrs["pinit"] = np.asarray(b.pinit, float)
     meta = dict(delta_x=d.delta_x, delta_y=d.delta_y, base=d.base, ivert=d.ivert,
                 west=d.west, south=d.south, factor=d.factor,
                 pmin=s.pmin, scf=s.scf, kslope=s.kslope, tolksl=s.tolksl,

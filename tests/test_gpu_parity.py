@@ -19,7 +19,7 @@ def _sim(case, **kw):
     return Simulation(case, **kw)
 
 
-@pytest.mark.parametrize("key", ["weill", "soil3d", "etp", "eo"])
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp", "eo", "da2"])
 def test_first_iteration_matches_reference_golden(key):
     g = golden_json()[key]
     case = load_golden_case(key)
@@ -37,7 +37,8 @@ def test_first_iteration_matches_reference_golden(key):
     # its 28th residual (4.8e-11) moves by about 1 % with the order of the
     # parallel FP64 dot products (the serial oracle matches it to 2e-6)
     lin_tol = 5e-2 if key == "etp" else 1e-4
-    assert abs(r["lin_err"] - lin["err"]) / lin["err"] < lin_tol
+    if lin is not None:
+        assert abs(r["lin_err"] - lin["err"]) / lin["err"] < lin_tol
 
 
 @pytest.mark.parametrize("key", ["weill", "soil3d"])

@@ -22,21 +22,24 @@ def _rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
-@pytest.mark.parametrize("key", ["weill", "soil3d", "etp", "eo"])
+@pytest.mark.parametrize("key", ["weill", "soil3d", "etp", "eo", "da2"])
 def test_first_iteration_matches_reference(key):
     import oracle as O
     g = golden_json()[key]
     o = O.Oracle(load_golden_case(key))
-    assert o.nterm == g["nterm"]
+    if g["nterm"] is not None:
+        assert o.nterm == g["nterm"]
     r = o.first_iteration()
     fi, lin = g["first_iter"], g["linear"]
-    assert r["niter"] == fi["niter"] == lin["niter"]
+    assert r["niter"] == fi["niter"]
     assert r["ikmax"] == fi["ikmax"]
     # iter prints 4 significant digits (E10.3), risul 7 (E15.6)
     for k in ("pl2", "pinf", "fl2", "finf"):
         assert _rel(r[k], fi[k]) < 6e-4, (k, r[k], fi[k])
-    assert _rel(r["lin_err"], lin["err"]) < 2e-6
-    assert _rel(r["lin_res"], lin["res"]) < 2e-6
+    if lin is not None:
+        assert r["niter"] == lin["niter"]
+        assert _rel(r["lin_err"], lin["err"]) < 2e-6
+        assert _rel(r["lin_res"], lin["res"]) < 2e-6
     # PNEW/POLD at IKMAX are printed with 3 significant digits (E10.2)
     assert _rel(r["pnew_ik"], fi["pnew_ik"]) < 5.1e-3
     assert _rel(r["pold_ik"], fi["pold_ik"]) < 5.1e-3
