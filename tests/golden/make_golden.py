@@ -33,16 +33,46 @@ EXAMPLES = {
     # cells: the only forcing of its first iteration is the Feddes sink
     "etp": "examples/SSHydro/atmbc_spatially_from_weill_withnodata",
     # a 1,271-node catchment forced by an Earth-observation ET/rain series
-    # (30 spatial records; the fixture keeps the two around the first step)
+    # (30 spatial records): it never ponds, so its whole 29-day run is a
+    # subsurface run -- every iter record and mbeconv row is kept
     "eo": "examples/EOdata/mapping_atmbc_from_EO_dataset",
     # a DA ensemble member started from nodal heads (INDP = 1); its risul
     # keeps no solver lines.  (Member 1's stored iter is the same file
     # while its ic was rewritten by the analysis step: not a pin.)
     "da2": "examples/DA/DA_with_swc/DA_SMC/DA_Ensemble/cathy_2",
 }
-# keys whose fixture keeps only the atmospheric records the first time step
-# interpolates between
-FIRST_STEP_ONLY = {"eo"}
+# keys whose whole run is kept: every record of output/iter and
+# output/mbeconv (as printed)
+WHOLE_RUN = {"eo"}
+
+
+def run_records(prj):
+    """Every nonlinear-iteration record of output/iter (the step header's
+    NSTEP and DELTAT, then ITER, NITER, PL2, PINF, IKMAX) and every row of
+    output/mbeconv (19 columns, as printed)."""
+    import re
+    it = []
+    head = None
+    for ln in open(os.path.join(prj, "output", "iter")):
+        m = re.search(r"NSTEP:\s+(\d+)\s+DELTAT:\s+([^\s)]+)", ln)
+        if m:
+            head = (int(m.group(1)), float(m.group(2)))
+            continue
+        t = ln.split()
+        if head and len(t) == 9 and t[0].isdigit():
+            it.append((head[0], int(t[0]), int(t[1]), int(t[4]), head[1], float(t[2]),
+                       float(t[3])))
+    mb = []
+    for ln in open(os.path.join(prj, "output", "mbeconv")):
+        if ln.startswith("#") or not ln.strip():
+            continue
+        try:
+            mb.append([float(x) for x in ln.split()])
+        except ValueError:
+            pass
+    it = np.array(it)
+    return dict(it_int=it[:, :4].astype(np.int32), it_dt=it[:, 4], it_norm=it[:, 5:7],
+                mbeconv=np.array(mb))
 
 
 def first_iter(prj):
@@ -93,12 +123,9 @@ def main(ref):
     for key, rel in EXAMPLES.items():
         prj = os.path.join(ref, rel)
         case = read_project(prj)
-        if key in FIRST_STEP_ONLY:
-            t = np.asarray(case.bc.atmtim)
-            keep = int(np.searchsorted(t, case.parm.deltat, side="left")) + 1
-            case.bc.atmtim = t[:max(keep, 2)]
-            case.bc.atminp = np.asarray(case.bc.atminp)[:max(keep, 2)]
         case_to_npz(case, os.path.join(HERE, f"{key}_case.npz"))
+        if key in WHOLE_RUN:
+            np.savez_compressed(os.path.join(HERE, f"{key}_run.npz"), **run_records(prj))
         rec, nterm, lin = first_iter(prj)
         out[key] = dict(source=rel, first_iter=rec, nterm=nterm, linear=lin)
         # ETRAN's record of the first time step (cathy_main.f:2929-2940

@@ -368,3 +368,17 @@ def test_every_autotuner_schedule_gives_the_same_heads():
                                           t["spmv_staged"])
         s.run()
         assert all(s.state(m)[3] == 1 for m in range(len(cases)))
+
+
+def test_eo_run_matches_reference_records():
+    """The EO-dataset project's whole stored run (1,078 steps, every iter
+    record and mbeconv row, see test_oracle_golden.py) on the FP64 path
+    through the C ABI, at the records' printed precision."""
+    from test_oracle_golden import _eo_records, check_eo_run
+    case = load_golden_case("eo")
+    _, _, _, mb = _eo_records()
+    with _sim(case) as s:
+        for _ in range(len(mb)):
+            s.step()
+        its, sts = s.records(0)
+    check_eo_run(its, sts, strict=False)
