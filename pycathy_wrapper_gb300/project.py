@@ -206,8 +206,8 @@ def read_sfbc(path, tmax=np.inf):
                 k += 1
             faces.append(np.array(ids[:cnt], dtype=np.int32))
         blocks.append((t, faces))
-    if not blocks:
-        return []
+    if not blocks or not any(faces for _, faces in blocks):
+        return []  # no seepage face at any time
     if blocks[0][0] > 0.0:
         raise ValueError("input/sfbc: the first block must start at TIME = 0")
     ref = blocks[0][1]

@@ -36,6 +36,8 @@ EXAMPLES = {
     # (30 spatial records): it never ponds, so its whole 29-day run is a
     # subsurface run -- every iter record and mbeconv row is kept
     "eo": "examples/EOdata/mapping_atmbc_from_EO_dataset",
+    # the same catchment with the coarse EO series: 6,069 stored steps
+    "eoc": "examples/EOdata/mapping_atmbc_from_coarse_EO_dataset",
     # a DA ensemble member started from nodal heads (INDP = 1); its risul
     # keeps no solver lines.  (Member 1's stored iter is the same file
     # while its ic was rewritten by the analysis step: not a pin.)
@@ -43,7 +45,7 @@ EXAMPLES = {
 }
 # keys whose whole run is kept: every record of output/iter and
 # output/mbeconv (as printed)
-WHOLE_RUN = {"eo"}
+WHOLE_RUN = {"eo", "eoc"}
 
 
 def run_records(prj):
@@ -86,7 +88,8 @@ def first_iter(prj):
             break
     nterm = None
     lin = None
-    for ln in open(os.path.join(prj, "output", "risul")):
+    risul = os.path.join(prj, "output", "risul")
+    for ln in (open(risul) if os.path.exists(risul) else []):
         if "NTERM" in ln and nterm is None:
             nterm = int(ln.split("=")[1])
         if "<<SYMMETRIC SOLVER>>" in ln and lin is None:

@@ -370,15 +370,16 @@ def test_every_autotuner_schedule_gives_the_same_heads():
         assert all(s.state(m)[3] == 1 for m in range(len(cases)))
 
 
-def test_eo_run_matches_reference_records():
-    """The EO-dataset project's whole stored run (1,078 steps, every iter
-    record and mbeconv row, see test_oracle_golden.py) on the FP64 path
+@pytest.mark.parametrize("key,nsteps", [("eo", None), ("eoc", 1500)])
+def test_stored_run_matches_reference_records(key, nsteps):
+    """The EO-dataset projects' stored runs (every iter record and mbeconv
+    row of the steps run, see test_oracle_golden.py) on the FP64 path
     through the C ABI, at the records' printed precision."""
-    from test_oracle_golden import _eo_records, check_eo_run
-    case = load_golden_case("eo")
-    _, _, _, mb = _eo_records()
+    from test_oracle_golden import _run_records, check_stored_run
+    case = load_golden_case(key)
+    _, _, _, mb = _run_records(key)
     with _sim(case) as s:
-        for _ in range(len(mb)):
+        for _ in range(len(mb) if nsteps is None else nsteps):
             s.step()
         its, sts = s.records(0)
-    check_eo_run(its, sts, strict=False)
+    check_stored_run(key, its, sts, nsteps, strict=False)

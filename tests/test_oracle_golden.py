@@ -87,23 +87,28 @@ def test_strpic_pattern_properties():
         assert np.all(np.diff(row) > 0)
 
 
-def _eo_records():
-    z = np.load(os.path.join(GOLDEN, "eo_run.npz"))
+def _run_records(key):
+    z = np.load(os.path.join(GOLDEN, f"{key}_run.npz"))
     return z["it_int"], z["it_dt"], z["it_norm"], z["mbeconv"]
 
 
-def check_eo_run(iters, steps, strict=True):
-    """Compare a run of the EO-dataset project with the reference binary's
-    stored records, at their printed precision: every output/iter record
-    (NSTEP, ITER, NITER, IKMAX exact; DELTAT 5 digits; PL2, PINF 4) and every
+def check_stored_run(key, iters, steps, nsteps=None, strict=True):
+    """Compare a run of a stored project with the reference binary's
+    records at their printed precision (half a unit of the last printed
+    digit): every output/iter record of the first nsteps steps (NSTEP, ITER,
+    NITER, IKMAX exact; DELTAT 5 digits; PL2, PINF 4) and every
     output/mbeconv row (DELTAT, TIME 7 digits, NLIN exact, STORE1 7, DSTORE
     6, VIN, VOUT, M.BAL.ERR, CUM.MBE 4).  strict=False (GPU) allows PCG
     counts one apart and an IKMAX tie resolved elsewhere at 1 % of the
-    records: the parallel dot products round differently."""
-    ii, idt, inorm, mb = _eo_records()
+    records, and the boundary-flux volumes to 2 %: the parallel dot
+    products round differently."""
+    ii, idt, inorm, mb = _run_records(key)
+    if nsteps is not None:
+        ii, idt, inorm = ii[ii[:, 0] <= nsteps], idt[ii[:, 0] <= nsteps], inorm[ii[:, 0] <= nsteps]
+        mb = mb[:nsteps]
     assert len(iters) >= len(ii) and len(steps) >= len(mb)
-    key = np.array([[r["nstep"], r["iter"]] for r in iters[: len(ii)]])
-    np.testing.assert_array_equal(key, ii[:, :2])
+    key_ = np.array([[r["nstep"], r["iter"]] for r in iters[: len(ii)]])
+    np.testing.assert_array_equal(key_, ii[:, :2])
     niter = np.array([r["niter"] for r in iters[: len(ii)]])
     ikmax = np.array([r["ikmax"] for r in iters[: len(ii)]])
     if strict:
@@ -122,23 +127,33 @@ def check_eo_run(iters, steps, strict=True):
     np.testing.assert_allclose(col("deltat"), mb[:, 1], rtol=1e-6)
     np.testing.assert_allclose(col("time"), mb[:, 2], rtol=1e-6)
     np.testing.assert_array_equal(col("iter"), mb[:, 3])
-    np.testing.assert_allclose(col("store1"), mb[:, 5], rtol=2e-7)
-    np.testing.assert_allclose(col("dstore"), mb[:, 7], rtol=8e-6)
+    np.testing.assert_allclose(col("store1"), mb[:, 5], rtol=6e-7)
+    np.testing.assert_allclose(col("dstore"), mb[:, 7], rtol=6e-6)
     for k, c in (("vin", 9), ("vout", 11), ("erras", 15), ("cerras", 17)):
         a, b = col(k), mb[:, c]
-        assert np.all(np.abs(a - b) <= 6e-4 * np.abs(b) + (b == 0) * 1e-12), k
+        if strict:
+            assert np.all(np.abs(a - b) <= 6e-4 * np.abs(b) + (b == 0) * 1e-12), k
+        else:
+            # the fluxes back-calculated at air-dry Dirichlet surface nodes
+            # are differences of terms orders of magnitude larger, so they
+            # carry the PCG solutions' round-off amplified: about 1 % on the
+            # GPU where the serial oracle agrees to the printed digits
+            tol = 2e-2 * np.abs(b) + 1e-3 * np.abs(b).max()
+            assert np.all(np.abs(a - b) <= tol), k
 
 
 @pytest.mark.slow
-def test_eo_run_matches_reference_records():
-    """The EO-dataset project never ponds, so its stored ISIMGR = 2 run is a
-    subsurface run: 1,078 time steps (back-steps to dt = 0.039 s, then up
-    to 1.7 s), 3,780 iteration records, every mass-balance row -- the
-    oracle's FLOW3D loop, TIMUPD/BKSTEP, MASBAL and ETRAN against the
-    reference binary's own files."""
+@pytest.mark.parametrize("key,nsteps", [("eo", None), ("eoc", 600)])
+def test_stored_run_matches_reference_records(key, nsteps):
+    """The EO-dataset projects never pond, so their stored ISIMGR = 2 runs
+    are subsurface runs: "eo" in full (1,078 steps: back-steps to dt =
+    0.039 s, then up to 1.7 s; 3,780 iteration records), "eoc" (the coarse
+    series, 6,069 stored steps, all reproduced; 600 here to keep the suite
+    short) -- the oracle's FLOW3D loop, TIMUPD/BKSTEP, MASBAL and ETRAN
+    against the reference binary's own files."""
     import oracle as O
-    o = O.Oracle(load_golden_case("eo"))
-    _, _, _, mb = _eo_records()
-    for _ in range(len(mb)):
+    o = O.Oracle(load_golden_case(key))
+    _, _, _, mb = _run_records(key)
+    for _ in range(len(mb) if nsteps is None else nsteps):
         assert o.step() == 0
-    check_eo_run(o.iter_records(), o.step_records(), strict=True)
+    check_stored_run(key, o.iter_records(), o.step_records(), nsteps, strict=True)
