@@ -174,6 +174,25 @@ def write_mbeconv(path: str, step_records, initial_volume: float) -> None:
             f.write(" ".join(vals) + "\n")
 
 
+def write_hgsfdet(path: str, step_records) -> None:
+    """The seepage-face hydrograph (hgsfdet: header mbinit.f:30, rows
+    cathy_main.f:3666, format I7,4(4X,1PE17.9)): per accepted step NSTEP,
+    DELTAT, TIME, the seepage-face volume VSFFLW = (SFFLW + SFFLWP) DELTAT/2
+    (masbal.f) and VSFFLW/DELTAT.  The reference writes it whether or not
+    the project has seepage faces."""
+    with open(path, "w") as f:
+        f.write("# NSTEP            DELTAT              TIME"
+                "  NET SEEPFACE VOL  NET SEEPFACE FLX\n")
+        prev = 0.0
+        for r in step_records:
+            dt = r["deltat"]
+            sf = r.get("sfflw", 0.0)
+            vol = (sf + prev) * (0.5 * dt if dt < 1.0e15 else 1.0)
+            prev = sf
+            f.write(f"{int(r['nstep']):7d}" + "".join(
+                f"    {v:17.9E}" for v in (dt, r["time"], vol, vol / dt)) + "\n")
+
+
 _PHASE_LINES = (
     " TOT CPU FOR UNSAT CHARACTERISTICS    = ", " TOT CPU FOR INIT. OF SYSTEM MATRICES = ",
     " TOT CPU FOR LOCAL SYSTEM ASSEMBLY    = ", " TOT CPU FOR RHS CALCULATION W/O BC'S = ",
@@ -283,6 +302,7 @@ def _write_member(prj: str, parm, mesh, snaps, wt, its, recs, phase_s=None,
     v0 = (recs[0]["store2"] - recs[0]["cdstor"]) if recs else 0.0
     write_mbeconv(os.path.join(out, "mbeconv"), recs, v0)
     write_iter(os.path.join(out, "iter"), parm, its)
+    write_hgsfdet(os.path.join(out, "hgsfdet"), recs)
     if parm.nodvp:
         write_wtdepth(os.path.join(out, "wtdepth"), wt)
     write_grid3d(os.path.join(out, "grid3d"), mesh)

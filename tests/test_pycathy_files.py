@@ -418,3 +418,29 @@ def test_run_ensemble_on_project_folders_matches_api(tmp_path):
         assert wt.shape[0] == nsteps[m] and wt[-1, 0] == pytest.approx(1800.0)
         assert sorted(os.listdir(os.path.join(dirs[m], "output"))) == [
             "grid3d", "iter", "mbeconv", "psi", "risul", "sw", "wtdepth", "xyz"]
+
+
+def test_hgsfdet_from_oracle_seepage_records(tmp_path):
+    """The seepage-face hydrograph written from a seepage run's step records
+    reads back with the reference's layout (one header line, I7 and four
+    E17.9 columns) and its volumes are the trapezoids of SFFLW."""
+    import oracle as O
+    from test_seepage import seepage_case
+    from pycathy_wrapper_gb300.pycathy import write_hgsfdet
+    o = O.Oracle(seepage_case())
+    for _ in range(20):
+        assert o.step() == 0
+    recs = o.step_records()
+    path = str(tmp_path / "hgsfdet")
+    write_hgsfdet(path, recs)
+    lines = open(path).read().splitlines()
+    assert lines[0].startswith("# NSTEP") and lines[0].endswith("NET SEEPFACE FLX")
+    assert len(lines) == len(recs) + 1
+    assert len(lines[1]) == 7 + 4 * 21
+    tab = np.loadtxt(path, skiprows=1)
+    prev = np.concatenate([[0.0], [r["sfflw"] for r in recs[:-1]]])
+    vol = np.array([(r["sfflw"] + q) * 0.5 * r["deltat"] for r, q in zip(recs, prev)])
+    np.testing.assert_array_equal(tab[:, 0], [r["nstep"] for r in recs])
+    np.testing.assert_allclose(tab[:, 3], vol, rtol=1e-9, atol=1e-300)
+    np.testing.assert_allclose(tab[:, 4], vol / tab[:, 1], rtol=1e-8, atol=1e-300)
+    assert (tab[:, 3] < 0).all()
