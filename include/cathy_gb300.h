@@ -91,6 +91,10 @@ typedef struct cathy_bc {
   const double* atminp;        /* natm * (hspatm ? 1 : nnod) rates         */
   int32_t np; const int32_t* contp; const double* presc;
   int32_t nq; const int32_t* contq; const double* q;
+  /* initial heads (inital.f:97-103): INDP 0 uniform pinit[0], 1 nodal
+     pinit[n], 2 water table at the surface (icvhe.f), 3 water table
+     WTPOSITION above each column's bottom node (icvhwt.f), 4 water table
+     WTPOSITION below the surface (icvdwt.f)                                */
   int32_t indp; double wtposition; const double* pinit;
   /* seepage faces (input/sfbc as sfvone.f reads it, time-invariant): nsf
      faces of sfnum[f] nodes, sfnod = the 1-based node lists one after the

@@ -1841,7 +1841,9 @@ void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,
   o->atm_t.assign(bc->atmtim, bc->atmtim + bc->natm);
   size_t nv = (size_t)bc->natm * (bc->hspatm ? 1 : nnod);
   o->atm_v.assign(bc->atminp, bc->atminp + nv);
-  // initial conditions (inital.f:97-103; icvhe.f, icvdwt.f; INDP 0/1 direct)
+  // initial conditions (inital.f:97-103; icvhe.f, icvhwt.f, icvdwt.f;
+  // INDP 0/1 direct)
+  if (bc->indp < 0 || bc->indp > 4) { delete o; return nullptr; }
   if (bc->indp == 0) {
     for (int k = 1; k <= n; ++k) o->ptimep[k] = bc->pinit[0];
   } else if (bc->indp == 1) {
@@ -1852,7 +1854,14 @@ void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,
         int kk = k * nnod + i;
         o->ptimep[kk] = o->z[i] - o->z[kk];
       }
-  } else {  // INDP = 4
+  } else if (bc->indp == 3) {
+    // ICVHWT (icvhwt.f:31-37): water table WTPOSITION above the bottom node
+    for (int i = 1; i <= nnod; ++i)
+      for (int k = 0; k <= nstr; ++k) {
+        int kk = k * nnod + i;
+        o->ptimep[kk] = bc->wtposition - o->z[kk] + o->z[nstr * nnod + i];
+      }
+  } else {  // INDP = 4, ICVDWT: water table WTPOSITION below the surface
     for (int i = 1; i <= nnod; ++i)
       for (int k = 0; k <= nstr; ++k) {
         int kk = k * nnod + i;

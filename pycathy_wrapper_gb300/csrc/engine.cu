@@ -4771,7 +4771,11 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       h.sf_count = h_sfoff.back() - h.sf_first;
       h.sfchek = (h.parm.isfcvg == 1);
     }
-    // initial conditions (inital.f:97-103)
+    // initial conditions (inital.f:97-103): uniform, nodal, hydrostatic
+    // with the water table at the surface (icvhe.f), WTPOSITION above the
+    // bottom node (icvhwt.f) or WTPOSITION below the surface (icvdwt.f)
+    if (B.indp < 0 || B.indp > 4) throw std::string("INDP outside 0..4");
+    if ((B.indp == 0 || B.indp == 1) && !B.pinit) throw std::string("INDP 0/1 without PINIT");
     for (int i = 0; i < g.nnod; ++i)
       for (int k = 0; k <= nstr; ++k) {
         const int kk = k * g.nnod + i;
@@ -4779,6 +4783,7 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
         if (B.indp == 0) v = B.pinit[0];
         else if (B.indp == 1) v = B.pinit[kk];
         else if (B.indp == 2) v = g.z[i] - g.z[kk];
+        else if (B.indp == 3) v = B.wtposition - g.z[kk] + g.z[(size_t)nstr * g.nnod + i];
         else v = g.z[i] - g.z[kk] - B.wtposition;
         h_pinit[no + kk] = v;
       }

@@ -167,7 +167,8 @@ class BC:
     time (atmnxt.f:47).  ``contp``/``presc`` and ``contq``/``q`` are the
     non-atmospheric Dirichlet and Neumann node lists (1-based) with constant
     values.  ``indp`` selects the initial condition (0 uniform ``pinit[0]``,
-    1 nodal ``pinit``, 2 water table at the surface, 4 water table at depth
+    1 nodal ``pinit``, 2 water table at the surface, 3 water table at height
+    ``wtposition`` above the bottom of each column, 4 water table at depth
     ``wtposition``).  ``sfnod`` lists the seepage faces (``input/sfbc``),
     one array of 1-based node numbers per face, ordered by descending
     elevation (sfvone.f).

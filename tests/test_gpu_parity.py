@@ -98,6 +98,18 @@ def test_hillslope_steps_match_oracle(precond):
     assert max(dn) <= 1
 
 
+def test_hillslope_indp3_initial_condition_matches_oracle():
+    """INDP = 3 (water table 1.5 m above each column's bottom node,
+    icvhwt.f) through the engine, against the oracle over 10 steps."""
+    from pycathy_wrapper_gb300.inputs import config0
+    case = config0(tmax=3600.0, precond=0)
+    case.bc.indp, case.bc.wtposition = 3, 1.5
+    o, (p, t, sts, its), (po, osr, oir) = _run_both(case, 10)
+    assert len(sts) == len(osr)
+    np.testing.assert_allclose([r["time"] for r in sts], [r["time"] for r in osr], rtol=0, atol=1e-9)
+    assert np.max(np.abs(p - po)) <= 1e-6
+
+
 def test_hillslope_column_line_preconditioner_matches_oracle_heads():
     from pycathy_wrapper_gb300.inputs import config0
     import oracle as O

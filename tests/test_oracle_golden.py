@@ -63,6 +63,25 @@ def test_etran_first_step_matches_reference(key):
         assert np.count_nonzero(q) > 0
 
 
+def test_initial_conditions_indp_3_and_4():
+    """ICVHWT (INDP = 3: water table WTPOSITION above the column's bottom
+    node, icvhwt.f:31-37) and ICVDWT (INDP = 4: WTPOSITION below the
+    surface); INDP outside 0..4 is refused."""
+    import oracle as O
+    from pycathy_wrapper_gb300.inputs import config0
+    for indp in (3, 4):
+        c = config0(tmax=600.0)
+        c.bc.indp, c.bc.wtposition = indp, 1.5
+        o = O.Oracle(c)
+        z = o.mesh()["z"].reshape(c.dem.nstr + 1, o.nnod)
+        ref = (1.5 - z + z[-1]) if indp == 3 else (z[0] - z - 1.5)
+        np.testing.assert_array_equal(o.state()[0], ref.reshape(-1))
+    c = config0(tmax=600.0)
+    c.bc.indp = 5
+    with pytest.raises(RuntimeError):
+        O.Oracle(c)
+
+
 def test_gen3d_mesh_matches_grid3d():
     import oracle as O
     z = np.load(os.path.join(GOLDEN, "weill_grid3d.npz"))
