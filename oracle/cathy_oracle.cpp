@@ -805,6 +805,8 @@ static void str_build(int n, int nt, const ivec& tetra, int n1, bool sym,
 }
 
 bool Oracle::build_mesh(const orc_dem_t* d) {
+  // IVERT 3 needs the per-node DEPTH map of gen3d.f:67-68: not an input here
+  if (d->ivert != 0 && d->ivert != 1 && d->ivert != 2 && d->ivert != 4) return false;
   nrow = d->nrow; ncol = d->ncol; nstr = d->nstr;
   // TRIANGOLI with DOSTEP=1
   vector<int> nodi((nrow + 2) * (ncol + 2), 0);

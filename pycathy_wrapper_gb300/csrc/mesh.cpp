@@ -113,6 +113,9 @@ bool node_map_types(const cathy_dem_t& d, const double* map, const HostMesh& m,
 }
 
 bool build_mesh(const cathy_dem_t& d, int iopt, HostMesh& m) {
+  // GEN3D's IVERT 3 takes a per-node depth map (gen3d.f:67-68), which the
+  // DEM inputs here do not carry: refused, as are values GEN3D does not know
+  if (d.ivert != 0 && d.ivert != 1 && d.ivert != 2 && d.ivert != 4) return false;
   m.nrow = d.nrow; m.ncol = d.ncol; m.nstr = d.nstr; m.iopt = iopt;
   std::vector<double> zs;
   if (!surface_mesh(d, m, zs)) return false;
@@ -155,7 +158,7 @@ bool build_mesh(const cathy_dem_t& d, int iopt, HostMesh& m) {
         case 1: zz = zs[i] - zr * zthick; break;
         case 2: zz = zmin - zr * d.base; break;
         case 4: zz = (j == nstr) ? zmin - d.base : zs[i] - zr * d.base; break;
-        default: zz = zs[i] - zr * d.base; break;
+        default: zz = zs[i] - zr * d.base; break;  // IVERT 0
       }
       m.z[kk] = zz;
     }

@@ -4,7 +4,7 @@ Restates the input semantics of the reference's ``datin.f`` for the
 subsurface solver (parm :81-117, DEM/zone rasters via RAST_INPUT_DEM /
 RAST_INPUT_LZ :189-257, dem_parameters :195-266, ic :380-405, soil
 :421-517) plus the atmospheric (``atmone.f``) and non-atmospheric BC files
-(``bcone.f``; the first time block is used, held constant).  The result is a
+(``bcone.f``; constant in time: later blocks must repeat the first).  The result is a
 :class:`~pycathy_wrapper_gb300.inputs.Case`, so a pyCATHY project can be run
 on the GPU without changing how the project is written.
 """
@@ -97,6 +97,9 @@ def read_project(prj: str) -> Case:
     delta_x, delta_y, factor = dp[0][0], dp[1][0], dp[2][0]
     nzone, nstr = int(dp[4][0]), int(dp[4][1])
     ivert, base = int(dp[5][0]), dp[5][2]
+    if ivert not in (0, 1, 2, 4):
+        # IVERT 3 reads a per-node depth map (gen3d.f:67-68)
+        raise ValueError(f"IVERT = {ivert} is not supported (0, 1, 2 and 4 are)")
     zr = np.array(dp[6][:nstr])
     dem_map, hdr = read_raster(pre("dem"))
     zone_map = None
@@ -160,10 +163,10 @@ def read_project(prj: str) -> Case:
         i += per
     bc.atmtim = np.array(times)
     bc.atminp = np.array(vals) if per != 1 else np.array([v[0] for v in vals])
-    parm_dir = _read_bc_list(inp("nansfdirbc"))
+    parm_dir = _read_bc_list(inp("nansfdirbc"), parm.tmax)
     if parm_dir is not None:
         bc.contp, bc.presc = parm_dir
-    neu = _read_bc_list(inp("nansfneubc"))
+    neu = _read_bc_list(inp("nansfneubc"), parm.tmax)
     if neu is not None:
         bc.contq, bc.q = neu
     if os.path.exists(inp("sfbc")):
@@ -231,22 +234,33 @@ def _count_nodes(dem_map):
     return int(act.sum())
 
 
-def _read_bc_list(path):
-    """First time block of a nansfdirbc / nansfneubc file:
-    ``time`` / ``NDIR NDIRC`` (or ``ZERO NQ``) / node ids / values."""
+def _read_bc_list(path, tmax=np.inf):
+    """A nansfdirbc / nansfneubc file as BCONE/BCNXT read it (bcone.f):
+    blocks of ``time`` / ``NDIR NDIRC`` (or ``ZERO NQ``) / node ids /
+    values.  The solver holds these conditions constant, so every block
+    that takes effect before TMAX must repeat the first one (BCNXT would
+    interpolate between differing blocks)."""
     if not os.path.exists(path):
         return None
     toks = []
     for ln in _lines(path):
         toks.extend(_nums(ln))
-    if len(toks) < 3:
+    blocks, i = [], 0
+    while i + 2 < len(toks):
+        t, n1, n2 = toks[i], int(toks[i + 1]), int(toks[i + 2])
+        cnt = n1 + n2
+        ids = np.array(toks[i + 3:i + 3 + cnt], dtype=np.int32)
+        vals = np.array(toks[i + 3 + cnt:i + 3 + 2 * cnt], dtype=float)
+        if len(vals) < cnt:
+            vals = np.zeros(cnt)
+        blocks.append((t, ids, vals))
+        i += 3 + 2 * cnt
+    if not blocks or len(blocks[0][1]) == 0:
+        if any(len(b[1]) for b in blocks if b[0] < tmax):
+            raise ValueError(f"{path}: time-varying boundary conditions are not supported")
         return None
-    n1, n2 = int(toks[1]), int(toks[2])
-    cnt = n1 + n2
-    if cnt == 0:
-        return None
-    ids = np.array(toks[3:3 + cnt], dtype=np.int32)
-    vals = np.array(toks[3 + cnt:3 + 2 * cnt], dtype=float)
-    if len(vals) < cnt:
-        vals = np.zeros(cnt)
-    return ids, vals
+    _, ids0, vals0 = blocks[0]
+    for t, ids, vals in blocks[1:]:
+        if t < tmax and not (np.array_equal(ids, ids0) and np.array_equal(vals, vals0)):
+            raise ValueError(f"{path}: time-varying boundary conditions are not supported")
+    return ids0, vals0

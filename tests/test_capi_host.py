@@ -95,3 +95,42 @@ def test_mesh_with_inactive_cells_and_zones():
     om = o.mesh()
     np.testing.assert_array_equal(m["tetra"], om["tetra"])
     np.testing.assert_array_equal(m["z"], om["z"])
+
+
+def test_gen3d_vertical_modes_and_refusals():
+    """IVERT 0, 1, 2 and 4 build the same mesh in the host library and the
+    oracle; IVERT 3 (a per-node depth map, gen3d.f:67-68) is refused by
+    both instead of being built as another mode."""
+    import oracle as O
+    from pycathy_wrapper_gb300.api import build_mesh
+    from pycathy_wrapper_gb300.inputs import config0
+    for ivert in (0, 1, 2, 4):
+        case = config0()
+        case.dem.ivert = ivert
+        m = build_mesh(case, iopt=1)
+        np.testing.assert_array_equal(m["z"], O.Oracle(case).mesh()["z"])
+    case = config0()
+    case.dem.ivert = 3
+    with pytest.raises(Exception):
+        build_mesh(case, iopt=1)
+    with pytest.raises(RuntimeError):
+        O.Oracle(case)
+
+
+def test_bc_lists_held_constant_or_refused(tmp_path):
+    """nansfdirbc / nansfneubc: blocks that repeat the first one (or start
+    at or after TMAX) are accepted; values that change before TMAX, which
+    BCNXT would interpolate, are refused."""
+    from pycathy_wrapper_gb300.project import _read_bc_list
+    p = tmp_path / "nansfneubc"
+    same = "0 time\n0 2 ZERO NQ\n5\n6\n1.0e-6\n2.0e-6\n"
+    p.write_text(same + same.replace("0 time", "600 time"))
+    ids, vals = _read_bc_list(str(p), tmax=3600.0)
+    assert list(ids) == [5, 6] and list(vals) == [1e-6, 2e-6]
+    p.write_text(same + same.replace("0 time", "600 time").replace("2.0e-6", "3.0e-6"))
+    with pytest.raises(ValueError):
+        _read_bc_list(str(p), tmax=3600.0)
+    ids, vals = _read_bc_list(str(p), tmax=600.0)  # the change comes at TMAX
+    assert list(vals) == [1e-6, 2e-6]
+    p.write_text("0 time\n0 0 ZERO NQ\n1800 time\n0 0 ZERO NQ\n")
+    assert _read_bc_list(str(p)) is None
