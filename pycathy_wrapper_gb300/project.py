@@ -133,7 +133,13 @@ def read_project(prj: str) -> Case:
                 feddes=feddes, root_map=root_map)
     # initial conditions
     il = [ln for ln in _lines(inp("ic")) if ln.strip()]
-    indp = int(_nums(il[0])[0])
+    head = _nums(il[0])
+    indp = int(head[0])
+    ipond = int(head[1]) if len(head) > 1 else 0
+    if ipond != 0 and parm.isimgr == 2:
+        # datin.f:380-410: ponded initial heads, read only with surface
+        # routing (ISIMGR = 2), which this solver does not model
+        raise ValueError("IPOND != 0 (ponded initial conditions) needs surface routing")
     bc = BC(indp=indp)
     if indp in (3, 4):
         bc.wtposition = _nums(il[1])[0]

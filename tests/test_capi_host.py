@@ -134,3 +134,26 @@ def test_bc_lists_held_constant_or_refused(tmp_path):
     assert list(vals) == [1e-6, 2e-6]
     p.write_text("0 time\n0 0 ZERO NQ\n1800 time\n0 0 ZERO NQ\n")
     assert _read_bc_list(str(p)) is None
+
+
+def test_reader_refuses_ponded_initial_conditions(tmp_path):
+    """IPOND != 0 with ISIMGR = 2 (ponded initial heads, datin.f:380-410)
+    needs surface routing: refused; with ISIMGR <= 1 the reference itself
+    ignores IPOND (datin.f:381)."""
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.project import read_project
+    from pycathy_wrapper_gb300.pycathy import write_project
+    case = config0(tmax=600.0)
+    for isimgr, ok in ((1, True), (2, False)):
+        case.parm.isimgr = isimgr
+        prj = tmp_path / f"p{isimgr}"
+        write_project(case, str(prj))
+        ic = prj / "input" / "ic"
+        lines = ic.read_text().splitlines()
+        lines[0] = f"{case.bc.indp} 1\tINDP IPOND"
+        ic.write_text("\n".join(lines + ["0.05\tPONDNOD"]) + "\n")
+        if ok:
+            assert read_project(str(prj)).bc.indp == case.bc.indp
+        else:
+            with pytest.raises(ValueError):
+                read_project(str(prj))
