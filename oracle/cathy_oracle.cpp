@@ -1771,6 +1771,8 @@ void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,
                  const orc_parm_t* parm, const orc_bc_t* bc) {
   Oracle* o = new Oracle();
   o->parm = *parm;
+  // NLRELX 2 (RELXOM's variable relaxation factor) is not restated
+  if (parm->nlrelx != 0 && parm->nlrelx != 1) { delete o; return nullptr; }
   if (!o->build_mesh(dem)) { delete o; return nullptr; }
   int n = o->n, nt = o->nt, nnod = o->nnod, nstr = o->nstr;
   int nz = std::max(o->nzone, soil->nzone);

@@ -4599,6 +4599,8 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       throw std::string("members must share IOPT, LUMP and the preconditioner");
     if (mem[m].soil.kslope != 0 && mem[m].soil.kslope != 1)
       throw std::string("KSLOPE 2..4 (chord slope with centred or local differences) not supported");
+    if (mem[m].parm.nlrelx != 0 && mem[m].parm.nlrelx != 1)
+      throw std::string("NLRELX 2 (variable relaxation, relxom.f) not supported");
   }
   // meshes (topology cached per identical DEM activity/size)
   M.resize(nmem);

@@ -157,3 +157,15 @@ def test_reader_refuses_ponded_initial_conditions(tmp_path):
         else:
             with pytest.raises(ValueError):
                 read_project(str(prj))
+
+
+def test_variable_relaxation_refused():
+    """NLRELX = 2 (RELXOM's per-iteration relaxation factor) is refused by
+    the oracle and the reader, as by the engine, rather than run without
+    relaxation."""
+    import oracle as O
+    from pycathy_wrapper_gb300.inputs import config0
+    case = config0(tmax=600.0)
+    case.parm.nlrelx = 2
+    with pytest.raises(RuntimeError):
+        O.Oracle(case)
