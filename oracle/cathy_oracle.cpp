@@ -1773,6 +1773,8 @@ void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,
   o->parm = *parm;
   // NLRELX 2 (RELXOM's variable relaxation factor) is not restated
   if (parm->nlrelx != 0 && parm->nlrelx != 1) { delete o; return nullptr; }
+  // NSYSLV restated for ISOLV 0 and -5 only (the Newton scheme's solvers)
+  if (parm->iopt == 2 && parm->isolv != 0 && parm->isolv != -5) { delete o; return nullptr; }
   if (!o->build_mesh(dem)) { delete o; return nullptr; }
   int n = o->n, nt = o->nt, nnod = o->nnod, nstr = o->nstr;
   int nz = std::max(o->nzone, soil->nzone);

@@ -4601,6 +4601,11 @@ void Engine::build(int nmembers, const cathy_member_t* mem) {
       throw std::string("KSLOPE 2..4 (chord slope with centred or local differences) not supported");
     if (mem[m].parm.nlrelx != 0 && mem[m].parm.nlrelx != 1)
       throw std::string("NLRELX 2 (variable relaxation, relxom.f) not supported");
+    // NSYSLV's other ISOLV choices (GMRES, TFQMR and other preconditioners,
+    // solscal-extended.f:2579-2760) are not built; the Picard scheme does
+    // not read ISOLV
+    if (mem[m].parm.iopt == 2 && mem[m].parm.isolv != 0 && mem[m].parm.isolv != -5)
+      throw std::string("ISOLV other than 0 and -5 not supported for IOPT = 2");
   }
   // meshes (topology cached per identical DEM activity/size)
   M.resize(nmem);

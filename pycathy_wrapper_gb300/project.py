@@ -56,6 +56,8 @@ def read_parm(path) -> Parm:
     p.kslope = int(v[2][0])
     p.tetaf, p.lump, p.iopt = v[6][0], int(v[6][1]), int(v[6][2])
     p.nlrelx, p.omega = int(v[7][0]), v[7][1]
+    if p.iopt == 2 and p.isolv not in (0, -5):
+        raise ValueError("IOPT = 2 with ISOLV other than 0 or -5 is not supported")
     if p.nlrelx not in (0, 1):
         raise ValueError("NLRELX = 2 (variable relaxation, relxom.f) is not supported")
     p.l2norm, p.toluns, p.tolswi, p.ernlmx = int(v[8][0]), v[8][1], v[8][2], v[8][3]

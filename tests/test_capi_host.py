@@ -169,3 +169,9 @@ def test_variable_relaxation_refused():
     case.parm.nlrelx = 2
     with pytest.raises(RuntimeError):
         O.Oracle(case)
+    case.parm.nlrelx = 0
+    case.parm.iopt, case.parm.isolv = 2, 1   # a GMRES/TFQMR choice of NSYSLV
+    with pytest.raises(RuntimeError):
+        O.Oracle(case)
+    case.parm.iopt = 1                        # Picard does not read ISOLV
+    O.Oracle(case)
