@@ -122,7 +122,15 @@ def read_project(prj: str) -> Case:
         nveg = max(1, int(np.max(root_map)))
     sl = [ln for ln in _lines(inp("soil")) if _nums(ln)]
     pmin = _nums(sl[0])[0]
-    scf = _nums(sl[1])[1]
+    ipeat, scf = int(_nums(sl[1])[0]), _nums(sl[1])[1]
+    if ipeat != 0:
+        raise ValueError("IPEAT = 1 (peat soil deformation) is not supported")
+    # nudging (input/nudging: NUDFLAG NUDN WFLAG) adds terms this solver
+    # does not model
+    if os.path.exists(inp("nudging")):
+        nud = [_nums(ln) for ln in _lines(inp("nudging")) if _nums(ln)]
+        if nud and len(nud[0]) > 1 and int(nud[0][1]) > 0:
+            raise ValueError("nudging observations (NUDN > 0) are not supported")
     feddes = np.array([_nums(sl[3 + v])[:6] for v in range(nveg)], dtype=float)
     ivghu = int(_nums(sl[3 + nveg])[0])
     if ivghu != 0:

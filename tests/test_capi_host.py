@@ -175,3 +175,26 @@ def test_variable_relaxation_refused():
         O.Oracle(case)
     case.parm.iopt = 1                        # Picard does not read ISOLV
     O.Oracle(case)
+
+
+def test_reader_refuses_peat_and_nudging(tmp_path):
+    """IPEAT = 1 (peat deformation) and NUDN > 0 (nudging observations) are
+    refused by the project reader; the zero settings every stored example
+    uses read as before."""
+    from pycathy_wrapper_gb300.inputs import config0
+    from pycathy_wrapper_gb300.project import read_project
+    from pycathy_wrapper_gb300.pycathy import write_project
+    case = config0(tmax=600.0)
+    write_project(case, str(tmp_path))
+    read_project(str(tmp_path))
+    soil = tmp_path / "input" / "soil"
+    txt = soil.read_text()
+    soil.write_text(txt.replace("0 0.0\tIPEAT SCF", "1 0.0\tIPEAT SCF"))
+    with pytest.raises(ValueError):
+        read_project(str(tmp_path))
+    soil.write_text(txt)
+    (tmp_path / "input" / "nudging").write_text("0 2 0\tNUDFLAG NUDN WFLAG\n")
+    with pytest.raises(ValueError):
+        read_project(str(tmp_path))
+    (tmp_path / "input" / "nudging").write_text("0 0 0\tNUDFLAG NUDN WFLAG\n")
+    read_project(str(tmp_path))
