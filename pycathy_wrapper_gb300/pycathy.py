@@ -158,7 +158,7 @@ def write_mbeconv(path: str, step_records, initial_volume: float) -> None:
     """One row per accepted time step with the 19 columns of the reference's
     mbeconv file."""
     with open(path, "w") as f:
-        f.write(f"#INITIAL VOLUME OF WATER IN THE SUBSURFACE = {initial_volume:12.5E}\n")
+        f.write(f"#INITIAL VOLUME OF WATER IN THE SUBSURFACE = {initial_volume:13.5E}\n")
         f.write(_MBE_HDR)
         for r in step_records:
             it = max(int(r["iter"]), 1)

@@ -129,6 +129,13 @@ def main(ref):
         case_to_npz(case, os.path.join(HERE, f"{key}_case.npz"))
         if key in WHOLE_RUN:
             np.savez_compressed(os.path.join(HERE, f"{key}_run.npz"), **run_records(prj))
+        if key == "eo":
+            # the binary's own text of its first 200 steps: mbeconv's three
+            # header lines and 200 rows, and the first 700 lines of iter
+            mb = open(os.path.join(prj, "output", "mbeconv")).read().splitlines()[:203]
+            it = open(os.path.join(prj, "output", "iter")).read().splitlines()[:700]
+            np.savez_compressed(os.path.join(HERE, "eo_text.npz"),
+                                mbeconv_head=np.array(mb), iter_head=np.array(it))
         rec, nterm, lin = first_iter(prj)
         out[key] = dict(source=rel, first_iter=rec, nterm=nterm, linear=lin)
         # ETRAN's record of the first time step (cathy_main.f:2929-2940

@@ -176,3 +176,24 @@ def test_stored_run_matches_reference_records(key, nsteps):
     for _ in range(len(mb) if nsteps is None else nsteps):
         assert o.step() == 0
     check_stored_run(key, o.iter_records(), o.step_records(), nsteps, strict=True)
+
+
+def test_output_files_byte_identical_to_reference(tmp_path):
+    """mbeconv and iter written by the package's writers from the oracle's
+    records of the EO-dataset run's first 200 steps are the reference
+    binary's own files, byte for byte (every header, step line and
+    record)."""
+    import oracle as O
+    from pycathy_wrapper_gb300.pycathy import write_iter, write_mbeconv
+    case = load_golden_case("eo")
+    o = O.Oracle(case)
+    for _ in range(200):
+        assert o.step() == 0
+    recs, its = o.step_records(), o.iter_records()
+    write_mbeconv(str(tmp_path / "mbeconv"), recs, recs[0]["store2"] - recs[0]["cdstor"])
+    write_iter(str(tmp_path / "iter"), case.parm, its)
+    z = np.load(os.path.join(GOLDEN, "eo_text.npz"))
+    mine = open(tmp_path / "mbeconv").read().splitlines()
+    assert mine == [str(s) for s in z["mbeconv_head"]]
+    mine = open(tmp_path / "iter").read().splitlines()
+    assert mine[: len(z["iter_head"])] == [str(s) for s in z["iter_head"]]
