@@ -131,11 +131,18 @@ def main(ref):
             np.savez_compressed(os.path.join(HERE, f"{key}_run.npz"), **run_records(prj))
         if key == "eo":
             # the binary's own text of its first 200 steps: mbeconv's three
-            # header lines and 200 rows, and the first 700 lines of iter
-            mb = open(os.path.join(prj, "output", "mbeconv")).read().splitlines()[:203]
-            it = open(os.path.join(prj, "output", "iter")).read().splitlines()[:700]
+            # header lines and 200 rows, the first 700 lines of iter, the
+            # header line and 200 rows of wtdepth and hgsfdet, and psi's
+            # second block (the heads after step 1)
+            rd = lambda f: open(os.path.join(prj, "output", f)).read().splitlines()
+            psi = rd("psi")
+            blk = [i for i, ln in enumerate(psi) if ln.endswith("NSTEP   TIME")]
             np.savez_compressed(os.path.join(HERE, "eo_text.npz"),
-                                mbeconv_head=np.array(mb), iter_head=np.array(it))
+                                mbeconv_head=np.array(rd("mbeconv")[:203]),
+                                iter_head=np.array(rd("iter")[:700]),
+                                wtdepth_head=np.array(rd("wtdepth")[:201]),
+                                hgsfdet_head=np.array(rd("hgsfdet")[:201]),
+                                psi_step1=np.array(psi[blk[1]:(blk + [len(psi)])[2]]))
         rec, nterm, lin = first_iter(prj)
         out[key] = dict(source=rel, first_iter=rec, nterm=nterm, linear=lin)
         # ETRAN's record of the first time step (cathy_main.f:2929-2940

@@ -179,20 +179,36 @@ def test_stored_run_matches_reference_records(key, nsteps):
 
 
 def test_output_files_byte_identical_to_reference(tmp_path):
-    """mbeconv and iter written by the package's writers from the oracle's
-    records of the EO-dataset run's first 200 steps are the reference
-    binary's own files, byte for byte (every header, step line and
-    record)."""
+    """mbeconv, iter, wtdepth, hgsfdet and psi written by the package's
+    writers from the oracle's run of the EO-dataset project's first 200
+    steps are the reference binary's own files, byte for byte (every
+    header, step line, record and head)."""
     import oracle as O
-    from pycathy_wrapper_gb300.pycathy import write_iter, write_mbeconv
+    from pycathy_wrapper_gb300.pycathy import (water_table, write_hgsfdet, write_iter,
+                                               write_mbeconv, write_psi, write_wtdepth)
     case = load_golden_case("eo")
     o = O.Oracle(case)
-    for _ in range(200):
+    mesh = o.mesh()
+    rows, psi1 = [], None
+    for k in range(200):
         assert o.step() == 0
+        p, t = o.state()[0], o.step_records()[-1]["time"]
+        rows.append((t, water_table(p, mesh["z"], o.nnod, case.dem.nstr, case.parm.nodvp)))
+        if k == 0:
+            psi1 = (1, t, p.copy())
     recs, its = o.step_records(), o.iter_records()
+    z = np.load(os.path.join(GOLDEN, "eo_text.npz"))
+    write_wtdepth(str(tmp_path / "wtdepth"), rows)
+    write_hgsfdet(str(tmp_path / "hgsfdet"), recs)
+    write_psi(str(tmp_path / "psi"), [psi1])
+    for name, key in (("wtdepth", "wtdepth_head"), ("hgsfdet", "hgsfdet_head"),
+                      ("psi", "psi_step1")):
+        ref = [str(s) for s in z[key]]
+        mine = open(tmp_path / name).read().splitlines()
+        # the stored run was stopped: its psi ends inside the step-1 block
+        assert mine[: len(ref)] == ref and len(ref) > 0.99 * len(mine), name
     write_mbeconv(str(tmp_path / "mbeconv"), recs, recs[0]["store2"] - recs[0]["cdstor"])
     write_iter(str(tmp_path / "iter"), case.parm, its)
-    z = np.load(os.path.join(GOLDEN, "eo_text.npz"))
     mine = open(tmp_path / "mbeconv").read().splitlines()
     assert mine == [str(s) for s in z["mbeconv_head"]]
     mine = open(tmp_path / "iter").read().splitlines()
