@@ -179,16 +179,18 @@ def test_stored_run_matches_reference_records(key, nsteps):
 
 
 def test_output_files_byte_identical_to_reference(tmp_path):
-    """mbeconv, iter, wtdepth, hgsfdet and psi written by the package's
+    """mbeconv, iter, wtdepth, hgsfdet, psi and sw written by the package's
     writers from the oracle's run of the EO-dataset project's first 200
     steps are the reference binary's own files, byte for byte (every
     header, step line, record and head)."""
     import oracle as O
     from pycathy_wrapper_gb300.pycathy import (water_table, write_hgsfdet, write_iter,
-                                               write_mbeconv, write_psi, write_wtdepth)
+                                               write_mbeconv, write_psi, write_sw,
+                                               write_wtdepth)
     case = load_golden_case("eo")
     o = O.Oracle(case)
     mesh = o.mesh()
+    sw = [(0, 0.0, o.vg_nodal(o.state()[0])["sw"])]
     rows, psi1 = [], None
     for k in range(200):
         assert o.step() == 0
@@ -196,16 +198,18 @@ def test_output_files_byte_identical_to_reference(tmp_path):
         rows.append((t, water_table(p, mesh["z"], o.nnod, case.dem.nstr, case.parm.nodvp)))
         if k == 0:
             psi1 = (1, t, p.copy())
+            sw.append((1, t, o.vg_nodal(p)["sw"]))
     recs, its = o.step_records(), o.iter_records()
     z = np.load(os.path.join(GOLDEN, "eo_text.npz"))
     write_wtdepth(str(tmp_path / "wtdepth"), rows)
     write_hgsfdet(str(tmp_path / "hgsfdet"), recs)
     write_psi(str(tmp_path / "psi"), [psi1])
+    write_sw(str(tmp_path / "sw"), sw)
     for name, key in (("wtdepth", "wtdepth_head"), ("hgsfdet", "hgsfdet_head"),
-                      ("psi", "psi_step1")):
+                      ("psi", "psi_step1"), ("sw", "sw_all")):
         ref = [str(s) for s in z[key]]
         mine = open(tmp_path / name).read().splitlines()
-        # the stored run was stopped: its psi ends inside the step-1 block
+        # the stored run was stopped: psi and sw end inside the step-1 block
         assert mine[: len(ref)] == ref and len(ref) > 0.99 * len(mine), name
     write_mbeconv(str(tmp_path / "mbeconv"), recs, recs[0]["store2"] - recs[0]["cdstor"])
     write_iter(str(tmp_path / "iter"), case.parm, its)
