@@ -138,6 +138,9 @@ typedef struct cathy_step_rec {
   double deltat, time, store1, store2, dstore, cdstor, vin, cvin, vout, cvout,
          erras, errel, cerras, caeras;
   double sfflw;                /* seepage-face flux SFFLW (fluxmb.f:46-60)  */
+  double vnd, vnn;             /* volumes through the non-atmospheric
+                                  Dirichlet and Neumann nodes over the step,
+                                  VNDIN+VNDOUT and VNNIN+VNNOUT (masbal.f) */
 } cathy_step_rec_t;
 
 /* ---- library ----------------------------------------------------------- */

@@ -506,6 +506,7 @@ struct Oracle {
   ivec sfnode, sfex, sfexp;
   dvec sfq, sfqp;
   double sfflw = 0.0, sfflwp = 0.0;
+  double vnd = 0.0, vnn = 0.0;  // VNDIN+VNDOUT, VNNIN+VNNOUT of the last MASBAL
   int ksf = 0;
   bool sfchek = false, ksfzer = true;
   // nodal soil parameters (SOILCHAR.H) and element porosity
@@ -1520,6 +1521,8 @@ void Oracle::masbal() {
   double vanin = (anin + aninp) * deltam, vanout = (anout + anoutp) * deltam;
   double vnnin = (nnin + nninp) * deltam, vnnout = (nnout + nnoutp) * deltam;
   const double vsfflw = (sfflw + sfflwp) * deltam;
+  vnd = vndin + vndout;
+  vnn = vnnin + vnnout;
   vin = vadin + vndin + vanin + vnnin;
   vout = vadout + vndout + vanout + vnnout + vsfflw;
   erras = vin + vout - dstore;
@@ -1740,6 +1743,8 @@ int Oracle::step() {
   rec.vout = vout; rec.cvout = cvout; rec.erras = erras; rec.errel = errel;
   rec.cerras = cerras; rec.caeras = caeras;
   rec.sfflw = sfflw;
+  rec.vnd = vnd;
+  rec.vnn = vnn;
   step_recs.push_back(rec);
   adinp = adin; adoutp = adout; ndinp = ndin; ndoutp = ndout;
   aninp = anin; anoutp = anout; nninp = nnin; nnoutp = nnout;

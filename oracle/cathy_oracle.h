@@ -86,6 +86,7 @@ typedef struct orc_step_rec {
   double deltat, time, store1, store2, dstore, cdstor, vin, cvin, vout, cvout,
          erras, errel, cerras, caeras;
   double sfflw;    /* seepage-face flux SFFLW of the step (fluxmb.f:46-60) */
+  double vnd, vnn; /* non-atmospheric Dirichlet / Neumann volumes of the step */
 } orc_step_rec_t;
 
 void* orc_create(const orc_dem_t* dem, const orc_soil_t* soil,

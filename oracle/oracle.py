@@ -68,7 +68,8 @@ class StepRec(C.Structure):
     _fields_ = [(k, C.c_int32) for k in ("nstep", "iter", "nitert", "nback")] + [
         (k, C.c_double) for k in ("deltat", "time", "store1", "store2", "dstore",
                                    "cdstor", "vin", "cvin", "vout", "cvout",
-                                   "erras", "errel", "cerras", "caeras", "sfflw")]
+                                   "erras", "errel", "cerras", "caeras", "sfflw",
+                                   "vnd", "vnn")]
 
 
 def build(force: bool = False) -> str:

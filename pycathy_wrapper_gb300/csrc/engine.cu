@@ -6482,6 +6482,8 @@ int Engine::macro_iteration() {
       sr.vin = vadin + vndin + vanin + vnnin;
       sr.vout = vadout + vndout + vanout + vnnout + vsfflw;
       sr.sfflw = R[RD_SFFLW];
+      sr.vnd = vndin + vndout;
+      sr.vnn = vnnin + vnnout;
       h.sfflwp = R[RD_SFFLW];
       h.rec_pending = true;
       if (!mixed) finish_step_record(h, R[RD_DSTORE], st1[(size_t)m * RD_NUM + RD_STORE1]);

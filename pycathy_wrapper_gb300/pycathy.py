@@ -193,6 +193,32 @@ def write_hgsfdet(path: str, step_records) -> None:
                 f"    {v:17.9E}" for v in (dt, r["time"], vol, vol / dt)) + "\n")
 
 
+def write_cumflowvol(path: str, step_records) -> None:
+    """Cumulative flow volumes (cumflowvol: header mbinit.f:95-97, rows
+    cathy_main.f:3677 in format I7,6(1PE10.2),1PE12.4): per accepted step
+    NSTEP, DELTAT, TIME and the running sums VSFTOT (seepage faces, the
+    trapezoids of SFFLW), VNDTOT and VNNTOT (non-atmospheric Dirichlet and
+    Neumann nodes), VNUDTOT (nudging, 0 here) and VTOT (VIN + VOUT)
+    (cathy_main.f:3259-3263)."""
+    with open(path, "w") as f:
+        f.write(" " * 21 + "#***** Cumulative flow volumes ***** \n")
+        f.write("# Nstep    Deltat      Time  SeepageF  nansfDir  nansfNeu   Nudging"
+                "  net (VTOT)\n")
+        vsf = vnd = vnn = vtot = 0.0
+        prev = 0.0
+        for r in step_records:
+            dt = r["deltat"]
+            sf = r.get("sfflw", 0.0)
+            vsf += (sf + prev) * (0.5 * dt if dt < 1.0e15 else 1.0)
+            prev = sf
+            vnd += r.get("vnd", 0.0)
+            vnn += r.get("vnn", 0.0)
+            vtot += r["vin"] + r["vout"]
+            f.write(f"{int(r['nstep']):7d}" + "".join(
+                _fmt_e(v, 10, 2) for v in (dt, r["time"], vsf, vnd, vnn, 0.0)) +
+                _fmt_e(vtot, 12, 4) + "\n")
+
+
 _PHASE_LINES = (
     " TOT CPU FOR UNSAT CHARACTERISTICS    = ", " TOT CPU FOR INIT. OF SYSTEM MATRICES = ",
     " TOT CPU FOR LOCAL SYSTEM ASSEMBLY    = ", " TOT CPU FOR RHS CALCULATION W/O BC'S = ",
@@ -303,6 +329,7 @@ def _write_member(prj: str, parm, mesh, snaps, wt, its, recs, phase_s=None,
     write_mbeconv(os.path.join(out, "mbeconv"), recs, v0)
     write_iter(os.path.join(out, "iter"), parm, its)
     write_hgsfdet(os.path.join(out, "hgsfdet"), recs)
+    write_cumflowvol(os.path.join(out, "cumflowvol"), recs)
     if parm.nodvp:
         write_wtdepth(os.path.join(out, "wtdepth"), wt)
     write_grid3d(os.path.join(out, "grid3d"), mesh)

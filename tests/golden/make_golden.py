@@ -143,7 +143,8 @@ def main(ref):
                                 wtdepth_head=np.array(rd("wtdepth")[:201]),
                                 hgsfdet_head=np.array(rd("hgsfdet")[:201]),
                                 psi_step1=np.array(psi[blk[1]:(blk + [len(psi)])[2]]),
-                                sw_all=np.array(rd("sw")))
+                                sw_all=np.array(rd("sw")),
+                                cumflowvol_head=np.array(rd("cumflowvol")[:202]))
         rec, nterm, lin = first_iter(prj)
         out[key] = dict(source=rel, first_iter=rec, nterm=nterm, linear=lin)
         # ETRAN's record of the first time step (cathy_main.f:2929-2940

@@ -179,14 +179,14 @@ def test_stored_run_matches_reference_records(key, nsteps):
 
 
 def test_output_files_byte_identical_to_reference(tmp_path):
-    """mbeconv, iter, wtdepth, hgsfdet, psi and sw written by the package's
-    writers from the oracle's run of the EO-dataset project's first 200
-    steps are the reference binary's own files, byte for byte (every
-    header, step line, record and head)."""
+    """mbeconv, iter, wtdepth, hgsfdet, cumflowvol, psi and sw written by
+    the package's writers from the oracle's run of the EO-dataset project's
+    first 200 steps are the reference binary's own files, byte for byte
+    (every header, step line, record and head)."""
     import oracle as O
-    from pycathy_wrapper_gb300.pycathy import (water_table, write_hgsfdet, write_iter,
-                                               write_mbeconv, write_psi, write_sw,
-                                               write_wtdepth)
+    from pycathy_wrapper_gb300.pycathy import (water_table, write_cumflowvol,
+                                               write_hgsfdet, write_iter, write_mbeconv,
+                                               write_psi, write_sw, write_wtdepth)
     case = load_golden_case("eo")
     o = O.Oracle(case)
     mesh = o.mesh()
@@ -205,8 +205,10 @@ def test_output_files_byte_identical_to_reference(tmp_path):
     write_hgsfdet(str(tmp_path / "hgsfdet"), recs)
     write_psi(str(tmp_path / "psi"), [psi1])
     write_sw(str(tmp_path / "sw"), sw)
+    write_cumflowvol(str(tmp_path / "cumflowvol"), recs)
     for name, key in (("wtdepth", "wtdepth_head"), ("hgsfdet", "hgsfdet_head"),
-                      ("psi", "psi_step1"), ("sw", "sw_all")):
+                      ("psi", "psi_step1"), ("sw", "sw_all"),
+                      ("cumflowvol", "cumflowvol_head")):
         ref = [str(s) for s in z[key]]
         mine = open(tmp_path / name).read().splitlines()
         # the stored run was stopped: psi and sw end inside the step-1 block
