@@ -129,6 +129,10 @@ def main(ref):
         case_to_npz(case, os.path.join(HERE, f"{key}_case.npz"))
         if key in WHOLE_RUN:
             np.savez_compressed(os.path.join(HERE, f"{key}_run.npz"), **run_records(prj))
+        if key == "etp":
+            # the mesh of a DEM with no-data cells, as GEN3D wrote it
+            np.savez_compressed(os.path.join(HERE, "etp_xyz.npz"), xyz=np.array(
+                open(os.path.join(prj, "output", "xyz")).read().splitlines()))
         if key == "eo":
             # the binary's own text of its first 200 steps: mbeconv's three
             # header lines and 200 rows, the first 700 lines of iter, the

@@ -219,3 +219,12 @@ def test_output_files_byte_identical_to_reference(tmp_path):
     assert mine == [str(s) for s in z["mbeconv_head"]]
     mine = open(tmp_path / "iter").read().splitlines()
     assert mine[: len(z["iter_head"])] == [str(s) for s in z["iter_head"]]
+
+
+def test_xyz_of_a_dem_with_no_data_cells_byte_identical(tmp_path):
+    """The node coordinates of the no-data DEM run as the package writes
+    them from the host mesh builder are the reference's xyz file."""
+    from pycathy_wrapper_gb300.pycathy import mesh_gen3d, write_xyz
+    write_xyz(str(tmp_path / "xyz"), mesh_gen3d(load_golden_case("etp")))
+    ref = [str(s) for s in np.load(os.path.join(GOLDEN, "etp_xyz.npz"))["xyz"]]
+    assert open(tmp_path / "xyz").read().splitlines() == ref
